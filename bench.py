@@ -1,0 +1,321 @@
+"""Benchmark: time to an FP64-true relative residual of 1e-10 for CG on the staggered normal
+equations M^dagger M x = b, 1024x1024 periodic lattice, m = 0.01, U(1) links
+exp(i theta) with theta uniform in (-pi, pi) and a complex Gaussian source (std::mt19937 seed
+1337, the reference tests' generators), x0 = 0.
+
+One step = one complete solve with the inputs resident in HBM.  The headline arm is the
+mixed-precision CG (FP16-storage / FP32-arithmetic inner iterations, FP64 reliable updates);
+the FP32-inner, BF16-storage and plain FP64 GPU CG are timed on the same system and reported
+beside it.  Between steps the L2 is flushed by writing a 512 MiB buffer (outside the events).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs under torchrun as independent replicas (one system per GPU, no collective on the
+data path); rank 0 prints one JSON line.  --impl reference times the reference algorithm on
+the host cores (the CPU oracle, a restatement of the reference's CG), rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LX = LY = 1024
+MASS = 0.01
+EPS = 1e-10
+SEED = 1337
+MAX_ITER = 100000
+# FP64 CG iterations of the reference on this exact system (same generators, same seed),
+# measured with the reference's own minv_vector_cg; the GPU FP64 CG reproduces the count.
+REF_ITERS = 2093
+METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB300; HBM GB/s"
+HEADLINE = ("fp16", 2)
+VARIANTS = [("fp16", 2), ("fp32", 1), ("bf16", 3)]
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(iters_needed, n_iter=30):
+    """The reference's CG (CPU oracle restatement, single thread) on the same system, a
+    bounded sample of n_iter iterations, extrapolated to the full iteration count."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    gl = importlib.import_module("generic-linalg_gb300")
+    g = gl.Generator(SEED)
+    U = g.rand_gauge_u1(LX, LY)
+    b = g.gaussian(LX * LY)
+    O = pyoracle.Oracle()
+    op = pyoracle.Operator("staggered_normal", LX, LY, MASS, U)
+    t0 = time.perf_counter()
+    _, info, _ = O.solve("cg", op, b, max_iter=n_iter, eps=EPS)
+    dt = time.perf_counter() - t0
+    # the sample ran n_iter iterations plus 3 setup / check operator applications
+    per_iter = dt / (info["iter"] + 3 * 0.67)
+    return {
+        "value": per_iter * iters_needed * 1e3, "unit": "ms", "cores": 1, "kind": "port",
+        "sample": f"{info['iter']} CG iterations of the 1024^2 m=0.01 system ({dt:.1f} s, "
+                  f"{per_iter * 1e3:.1f} ms/iteration) extrapolated to {iters_needed} iterations",
+    }
+
+
+def run_reference(args):
+    """--impl reference: the reference algorithm on the host cores (rank 0 only)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    samples = []
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(REF_ITERS, n_iter=args.ref_iters)
+        if i >= args.warmup:
+            samples.append(cb["value"])
+    v = statistics.mean(samples)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "staggered normal-equation CG, 1024x1024, m=0.01, tol 1e-10, FP64 (reference CPU CG)",
+                   "lattice": [LX, LY], "mass": MASS, "tol": EPS, "seed": SEED},
+        "cpu_baseline": {**cb, "value": v},
+        "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--ref-iters", type=int, default=30)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    gl = importlib.import_module("generic-linalg_gb300")
+    L = gl.lib()
+    stream = torch.cuda.current_stream()
+    gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
+
+    # inputs: every replica solves the same seeded system (the work per GPU is fixed)
+    g = gl.Generator(SEED)
+    U = g.rand_gauge_u1(LX, LY)
+    b = g.gaussian(LX * LY)
+    Ud = torch.from_numpy(U).to(dev)
+    bd = torch.from_numpy(b).to(dev)
+    op = gl.Operator(2, LX, LY, MASS, Ud)
+    x = torch.zeros_like(bd)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def solve(prec):
+        x.zero_()
+        flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        info = gl.minv_vector_cg(x, bd, bd.numel(), MAX_ITER, EPS, gl.square_staggered_normal_u1, op,
+                                 precision=prec)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if not info.success:
+            raise RuntimeError(f"solve did not converge: {info}")
+        return e0.elapsed_time(e1), info
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    results = {}
+    clocks = ClockSampler(local)
+    head_name, head_prec = HEADLINE
+    for name, prec in [HEADLINE] + [v for v in VARIANTS if v != HEADLINE]:
+        for _ in range(args.warmup):
+            solve(prec)
+        barrier()
+        if name == head_name:
+            clocks.start()
+        times, infos = [], []
+        for _ in range(args.steps):
+            t, info = solve(prec)
+            times.append(t)
+            infos.append(info)
+        barrier()
+        if name == head_name:
+            clk = clocks.stop()
+        results[name] = (times, infos)
+    # the plain FP64 GPU CG (reference recurrence) on the same system
+    solve(0)
+    t64 = [solve(0) for _ in range(max(1, args.fp64_steps))]
+    results["fp64"] = ([t for t, _ in t64], [i for _, i in t64])
+
+    head_times, head_infos = results[head_name]
+    ms = statistics.mean(head_times)
+    ms_max = ms
+    if dist:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_max = tt.item()
+
+    # true residual of the last headline solve, rechecked with the FP64 operator
+    Ax = torch.zeros_like(bd)
+    op.apply(Ax, x)
+
+    # dominant kernel: kernel B of the headline precision, timed alone with CUDA events
+    kms = (C_double * 2)()
+    kbytes = (C_double * 2)()
+    gl._capi.check(L.glinalg_profile_mixed_kernels(op.handle, head_prec, 200, kms, kbytes), "profile")
+    peak, peak_src = peaks()
+    achieved = kbytes[1] / (kms[1] * 1e-3) / 1e9
+    achieved_a = kbytes[0] / (kms[0] * 1e-3) / 1e9
+
+    # e2e through the public API with host buffers (pinned), copies inside the timed region
+    Uh = torch.from_numpy(U).pin_memory().numpy()
+    bh = torch.from_numpy(b).pin_memory().numpy()
+    xh = torch.zeros(LX * LY, dtype=torch.complex128).pin_memory().numpy()
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        xh[:] = 0
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        info = gl.minv_vector_cg(xh, bh, bh.size, MAX_ITER, EPS, gl.square_staggered_normal_u1,
+                                 gl.StaggeredU1Op(Uh, MASS, LX, LY), precision=head_prec)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_times.append((time.perf_counter() - t0) * 1e3)
+        assert info.success
+    e2e_ms = statistics.mean(e2e_times)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    cb = None if args.no_cpu_baseline else cpu_baseline(results["fp64"][1][0].iter)
+    hi = head_infos[-1]
+    t64m = statistics.mean(results["fp64"][0])
+    relres = (torch.linalg.vector_norm(bd - Ax) / torch.linalg.vector_norm(bd)).item()
+    variants = {}
+    for name in ("fp16", "fp32", "bf16", "fp64"):
+        ts, ins = results[name]
+        variants[name] = {"ms": round(statistics.mean(ts), 3), "iters": ins[-1].iter,
+                          "reliable_updates": ins[-1].reliable_updates,
+                          "true_relres": float(np.sqrt(ins[-1].resSq) / np.linalg.norm(b)),
+                          "gbytes": round(ins[-1].gbytes, 3)}
+    launches = 3 * (hi.iter + 1) + 8 * hi.reliable_updates + 7
+    line = {
+        "metric": METRIC, "value": round(ms_max, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f16-storage/f32-accumulate (fp64 reliable updates)",
+        "data": "synthetic (seeded U(1) links and Gaussian source, std::mt19937 1337)",
+        "config": {"workload": "staggered normal-equation CG to FP64-true relres 1e-10, 1024x1024, m=0.01, x0=0",
+                   "lattice": [LX, LY], "mass": MASS, "tol": EPS, "variant": f"{head_name} inner + fp64 reliable updates",
+                   "parallelism": f"replicas x{world}", "l2": "flushed (512 MiB write) before every step",
+                   "inner_iters": hi.iter, "reliable_updates": hi.reliable_updates,
+                   "true_relres_fp64": relres, "fp64_gpu_ms": round(t64m, 3),
+                   "speedup_vs_fp64_gpu": round(t64m / ms, 2), "variants": variants},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 3), "traffic": None,
+                     "kernel": f"k_mx_B_stag<{head_name}> (D^dagger t + x/r update + |r|^2)",
+                     "bytes_per_launch": kbytes[1], "ms_per_launch": round(kms[1], 5),
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                     "kernel_A": {"achieved": round(achieved_a, 1), "bytes_per_launch": kbytes[0],
+                                  "ms_per_launch": round(kms[0], 5)}},
+        "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": int(Uh.nbytes + bh.nbytes + xh.nbytes),
+                "d2h_bytes_per_step": int(xh.nbytes)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if cb:
+        line["cpu_baseline"] = cb
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+from ctypes import c_double as C_double, c_void_p as C_void  # noqa: E402
+
+if __name__ == "__main__":
+    main()

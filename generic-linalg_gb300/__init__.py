@@ -1,0 +1,496 @@
+"""GB300 (sm_103a) implementation of generic-linalg's hot path, Python side.
+
+The compute lives in ``libglinalg_gb300.so`` (CUDA kernels behind the C-ABI declared in
+``include/glinalg.h``).  This module loads it with ctypes and mirrors the reference's
+interface for the path:
+
+* operator descriptors ``StaggeredU1Op`` (operators.h:7-15) and ``Stencil2D``
+  (coarse_stencil.h:33-67);
+* operator callbacks ``square_staggered_u1``, ``square_staggered_dagger_u1``,
+  ``square_staggered_normal_u1``, ``square_laplace_u1``, ``apply_stencil_2d``,
+  ``apply_stencil_2d_eo``, ``apply_stencil_2d_oe`` with the reference's
+  ``matrix_vector(lhs, rhs, extra)`` convention;
+* solvers ``minv_vector_cg``, ``minv_vector_cg_restart``, ``minv_vector_cg_m``,
+  ``minv_vector_bicgstab``, ``minv_vector_bicgstab_restart``, ``minv_vector_gcr``,
+  ``minv_vector_gcr_restart`` with the reference's argument order, returning
+  ``InversionInfo`` (inverter_struct.h:14-43);
+* ``InversionVerboseStruct`` and the ``VERB_*`` levels (verbosity.h:9-24).
+
+Fields are numpy complex128 arrays (host) or CUDA torch tensors of dtype complex128
+(device; the call then passes device pointers).  As in the reference, the solver recognises
+the operator by the callback it is given and the descriptor in ``extra_info``; any other
+callback raises ``UnsupportedOperator`` -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _capi
+from ._capi import (GLINALG_PTR_DEVICE, GLINALG_PTR_HOST, PREC_BFLOAT, PREC_DOUBLE, PREC_HALF,
+                    PREC_SINGLE, GlinalgError, InfoStruct, OpDesc, SolverParams, VerbStruct, lib,
+                    load_library)
+
+__all__ = [
+    "lib", "load_library", "GlinalgError", "UnsupportedOperator",
+    "StaggeredU1Op", "Stencil2D", "Operator", "InversionInfo", "InversionVerboseStruct",
+    "VERB_PASS_THROUGH", "VERB_NONE", "VERB_SUMMARY", "VERB_RESTART_DETAIL", "VERB_DETAIL",
+    "square_staggered_u1", "square_staggered_dagger_u1", "square_staggered_normal_u1",
+    "square_laplace_u1", "apply_stencil_2d", "apply_stencil_2d_eo", "apply_stencil_2d_oe",
+    "get_square_staggered_u1_stencil", "get_square_staggered_dagger_u1_stencil",
+    "minv_vector_cg", "minv_vector_cg_restart", "minv_vector_cg_m", "minv_vector_bicgstab",
+    "minv_vector_bicgstab_restart", "minv_vector_gcr", "minv_vector_gcr_restart",
+    "Generator", "dot", "norm2sq", "staggered_force", "staggered_action_grad",
+    "cg_batch", "cg_m_multi",
+    "PREC_DOUBLE", "PREC_SINGLE", "PREC_HALF", "PREC_BFLOAT",
+]
+
+VERB_PASS_THROUGH, VERB_NONE, VERB_SUMMARY, VERB_RESTART_DETAIL, VERB_DETAIL = -1, 0, 1, 2, 3
+
+KIND_STAGGERED, KIND_STAGGERED_DAGGER, KIND_STAGGERED_NORMAL, KIND_LAPLACE = 0, 1, 2, 3
+KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE = 4, 5, 6
+
+
+class UnsupportedOperator(GlinalgError):
+    pass
+
+
+# ---------------------------------------------------------------- field plumbing
+
+def _is_torch(a):
+    return type(a).__module__.startswith("torch")
+
+
+def _field_ptr(a, writable=False):
+    """(pointer, n_complex, device) for a complex128 numpy array or torch tensor."""
+    if _is_torch(a):
+        import torch
+        if a.dtype != torch.complex128 or not a.is_contiguous():
+            raise TypeError("torch fields must be contiguous complex128 tensors")
+        return C.c_void_p(a.data_ptr()), a.numel(), a.is_cuda
+    if not isinstance(a, np.ndarray) or a.dtype != np.complex128 or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError("numpy fields must be C-contiguous complex128 arrays")
+    if writable and not a.flags["WRITEABLE"]:
+        raise TypeError("output array is read-only")
+    return C.c_void_p(a.ctypes.data), a.size, False
+
+
+def _dptr(p):
+    return C.cast(p, C.POINTER(C.c_double))
+
+
+# ---------------------------------------------------------------- operator descriptors
+
+class StaggeredU1Op:
+    """Mirror of staggered_u1_op (operators.h:7-15)."""
+
+    def __init__(self, lattice, mass, x_fine, y_fine, Nc=1, wilson_coeff=0.0):
+        self.lattice = np.ascontiguousarray(lattice, dtype=np.complex128) if not _is_torch(lattice) else lattice
+        self.mass = float(mass)
+        self.x_fine, self.y_fine = int(x_fine), int(y_fine)
+        self.Nc = int(Nc)
+        self.wilson_coeff = float(wilson_coeff)
+
+
+class Stencil2D:
+    """Mirror of stencil_2d (coarse_stencil.h:33-67) on an lx x ly lattice with nc colours.
+    stencil_size 2 allocates the two-link term."""
+
+    def __init__(self, lx, ly, nc, stencil_size=1, shift=0j, eo_shift=0j, dof_shift=0j):
+        self.lx, self.ly, self.nc = int(lx), int(ly), int(nc)
+        v = self.lx * self.ly * self.nc * self.nc
+        self.clover = np.zeros(v, np.complex128)
+        self.hopping = np.zeros(4 * v, np.complex128)
+        self.has_two = stencil_size == 2
+        self.two_link = np.zeros(8 * v, np.complex128) if self.has_two else None
+        self.shift, self.eo_shift, self.dof_shift = complex(shift), complex(eo_shift), complex(dof_shift)
+        self.generated = False
+
+
+class Operator:
+    """A device-resident operator (glinalg_operator): links or stencil coefficients are copied
+    to the GPU once; apply / solve calls then reuse them."""
+
+    def __init__(self, kind, lx, ly, mass=0.0, links=None, nc=1, clover=None, hopping=None,
+                 two_link=None, shift=0j, eo_shift=0j, dof_shift=0j):
+        d = OpDesc()
+        d.kind, d.lx, d.ly, d.nc, d.mass = int(kind), int(lx), int(ly), int(nc), float(mass)
+        keep = []
+        dev_flags = []
+
+        def put(name, a):
+            if a is None:
+                return
+            p, _, dev = _field_ptr(a if _is_torch(a) else np.ascontiguousarray(a, dtype=np.complex128))
+            keep.append(a)
+            dev_flags.append(dev)
+            setattr(d, name, _dptr(p))
+
+        put("links", links)
+        put("clover", clover)
+        put("hopping", hopping)
+        put("two_link", two_link)
+        for nm, z in (("shift", shift), ("eo_shift", eo_shift), ("dof_shift", dof_shift)):
+            z = complex(z)
+            getattr(d, nm)[0], getattr(d, nm)[1] = z.real, z.imag
+        if dev_flags and all(dev_flags):
+            d.flags = GLINALG_PTR_DEVICE
+        elif any(dev_flags):
+            raise TypeError("operator arrays must all be on the host or all on the device")
+        h = C.c_void_p()
+        _capi.check(lib().glinalg_operator_create(C.byref(d), C.byref(h)), "glinalg_operator_create")
+        self.handle = h
+        self.kind, self.lx, self.ly, self.nc = int(kind), int(lx), int(ly), int(nc)
+
+    @property
+    def size(self):
+        return int(lib().glinalg_operator_size(self.handle))
+
+    def set_mass(self, mass):
+        _capi.check(lib().glinalg_operator_set_mass(self.handle, float(mass)), "set_mass")
+
+    def apply(self, lhs, rhs):
+        lp, ln, ldev = _field_ptr(lhs, writable=True)
+        rp, rn, rdev = _field_ptr(rhs)
+        if ln != self.size or rn != self.size or ldev != rdev:
+            raise ValueError("field sizes/devices do not match the operator")
+        _capi.check(lib().glinalg_operator_apply(self.handle, _dptr(lp), _dptr(rp),
+                                                 GLINALG_PTR_DEVICE if ldev else 0), "apply")
+        return lhs
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().glinalg_operator_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------- reference-named callbacks
+
+def _op_for(kind, extra):
+    if isinstance(extra, Operator):
+        return extra, False
+    if kind in (KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE):
+        if not isinstance(extra, Stencil2D):
+            raise UnsupportedOperator("stencil callbacks need a Stencil2D extra_info")
+        return Operator(kind, extra.lx, extra.ly, nc=extra.nc, clover=extra.clover,
+                        hopping=extra.hopping, two_link=extra.two_link, shift=extra.shift,
+                        eo_shift=extra.eo_shift, dof_shift=extra.dof_shift), True
+    if not isinstance(extra, StaggeredU1Op):
+        raise UnsupportedOperator("U(1) callbacks need a StaggeredU1Op extra_info")
+    return Operator(kind, extra.x_fine, extra.y_fine, mass=extra.mass, links=extra.lattice), True
+
+
+def _callback(kind, name, ref):
+    def cb(lhs, rhs, extra_data):
+        op, temp = _op_for(kind, extra_data)
+        try:
+            op.apply(lhs, rhs)
+        finally:
+            if temp:
+                op.close()
+    cb.__name__ = name
+    cb.__doc__ = f"lhs = A rhs on the GPU; replaces {name} ({ref})."
+    cb._glinalg_kind = kind
+    return cb
+
+
+square_staggered_u1 = _callback(KIND_STAGGERED, "square_staggered_u1", "operators.cpp:184")
+square_staggered_dagger_u1 = _callback(KIND_STAGGERED_DAGGER, "square_staggered_dagger_u1", "operators.cpp:372")
+square_staggered_normal_u1 = _callback(KIND_STAGGERED_NORMAL, "square_staggered_normal_u1", "operators.cpp:444")
+square_laplace_u1 = _callback(KIND_LAPLACE, "square_laplace_u1", "operators.cpp:73")
+apply_stencil_2d = _callback(KIND_STENCIL, "apply_stencil_2d", "coarse_stencil.cpp:12")
+apply_stencil_2d_eo = _callback(KIND_STENCIL_EO, "apply_stencil_2d_eo", "coarse_stencil.cpp:395")
+apply_stencil_2d_oe = _callback(KIND_STENCIL_OE, "apply_stencil_2d_oe", "coarse_stencil.cpp:560")
+
+
+def _stencil_builder(dagger):
+    def build(stenc: Stencil2D, stagif: StaggeredU1Op):
+        """Fills stenc's hopping terms from staggered links (operators_stencil.cpp:14-63 /
+        :120-169); no-op if already generated or nc != 1, like the reference."""
+        if stenc.generated or stenc.nc != 1:
+            return
+        sh = np.zeros(2)
+        _capi.check(lib().glinalg_staggered_stencil(
+            _dptr(_field_ptr(stagif.lattice)[0]), stenc.lx, stenc.ly, stagif.mass, int(dagger),
+            _dptr(C.c_void_p(stenc.hopping.ctypes.data)), sh.ctypes.data_as(C.POINTER(C.c_double)), 0),
+            "glinalg_staggered_stencil")
+        stenc.shift, stenc.eo_shift, stenc.dof_shift = complex(sh[0], sh[1]), 0j, 0j
+        stenc.generated = True
+    return build
+
+
+get_square_staggered_u1_stencil = _stencil_builder(False)
+get_square_staggered_dagger_u1_stencil = _stencil_builder(True)
+
+
+# ---------------------------------------------------------------- solvers
+
+class InversionVerboseStruct:
+    """Mirror of inversion_verbose_struct (verbosity.h:18-24)."""
+
+    def __init__(self, verbosity=VERB_NONE, verb_prefix="", precond_verbosity=VERB_NONE,
+                 precond_verb_prefix=""):
+        self.verbosity, self.verb_prefix = verbosity, verb_prefix
+        self.precond_verbosity, self.precond_verb_prefix = precond_verbosity, precond_verb_prefix
+
+    def struct(self):
+        v = VerbStruct()
+        self._b = (self.verb_prefix.encode(), self.precond_verb_prefix.encode())
+        v.verbosity, v.verb_prefix = self.verbosity, self._b[0]
+        v.precond_verbosity, v.precond_verb_prefix = self.precond_verbosity, self._b[1]
+        return v
+
+
+class InversionInfo:
+    """Mirror of inversion_info (inverter_struct.h:14-43) plus device diagnostics."""
+
+    def __init__(self, s: InfoStruct, resSqmrhs=None):
+        self.resSq = s.resSq
+        self.iter = s.iter
+        self.success = bool(s.success)
+        self.name = s.name.decode()
+        self.ops_count = s.ops_count
+        self.resSqmrhs = resSqmrhs
+        self.n_rhs = s.n_rhs if resSqmrhs is not None else -1
+        self.status = s.status
+        self.reliable_updates = s.reliable_updates
+        self.device_ms = s.device_ms
+        self.gbytes = s.gbytes
+
+    def __repr__(self):
+        return (f"InversionInfo(name={self.name!r}, iter={self.iter}, success={self.success}, "
+                f"ops_count={self.ops_count}, resSq={self.resSq:.6g}, status={self.status})")
+
+
+def _resolve(matrix_vector, extra_info):
+    kind = getattr(matrix_vector, "_glinalg_kind", None)
+    if kind is None:
+        raise UnsupportedOperator(
+            f"{getattr(matrix_vector, '__name__', matrix_vector)!r} is not one of the GPU operator "
+            "callbacks; there is no CPU fallback")
+    return _op_for(kind, extra_info)
+
+
+def _params(precision=PREC_DOUBLE, delta=0.0, device=False):
+    p = SolverParams()
+    p.precision, p.delta, p.flags = int(precision), float(delta), GLINALG_PTR_DEVICE if device else 0
+    return p
+
+
+def _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity, restart=None,
+           precision=PREC_DOUBLE, delta=0.0):
+    op, temp = _resolve(matrix_vector, extra_info)
+    try:
+        pp, pn, pdev = _field_ptr(phi, writable=True)
+        bp, bn, bdev = _field_ptr(phi0)
+        if pdev != bdev:
+            raise ValueError("phi and phi0 must both be on the host or both on the device")
+        if pn < size or bn < size:
+            raise ValueError("fields are shorter than size")
+        info = InfoStruct()
+        verb = verbosity.struct() if verbosity is not None else None
+        args = [op.handle, _dptr(pp), _dptr(bp), int(size), int(max_iter), float(eps)]
+        if restart is not None:
+            args.append(int(restart))
+        args += [C.byref(verb) if verb is not None else None,
+                 C.byref(_params(precision, delta, pdev)), C.byref(info)]
+        _capi.check(fn(*args), fn.__name__)
+        return InversionInfo(info)
+    finally:
+        if temp:
+            op.close()
+
+
+def minv_vector_cg(phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity=None,
+                   precision=PREC_DOUBLE, delta=0.0):
+    """minv_vector_cg (generic_cg.cpp:278).  precision != PREC_DOUBLE selects the mixed-precision
+    CG with FP64 reliable updates (Hermitian operators only)."""
+    return _solve(lib().glinalg_cg, phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                  verbosity, precision=precision, delta=delta)
+
+
+def minv_vector_cg_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector, extra_info,
+                           verbosity=None):
+    """minv_vector_cg_restart (generic_cg.cpp:387)."""
+    return _solve(lib().glinalg_cg_restart, phi, phi0, size, max_iter, eps, matrix_vector,
+                  extra_info, verbosity, restart=restart_freq)
+
+
+def minv_vector_bicgstab(phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity=None):
+    """minv_vector_bicgstab (generic_bicgstab.cpp:205)."""
+    return _solve(lib().glinalg_bicgstab, phi, phi0, size, max_iter, eps, matrix_vector,
+                  extra_info, verbosity)
+
+
+def minv_vector_bicgstab_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector,
+                                 extra_info, verbosity=None):
+    """minv_vector_bicgstab_restart (generic_bicgstab.cpp:345)."""
+    return _solve(lib().glinalg_bicgstab_restart, phi, phi0, size, max_iter, eps, matrix_vector,
+                  extra_info, verbosity, restart=restart_freq)
+
+
+def minv_vector_gcr(phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity=None):
+    """minv_vector_gcr (generic_gcr.cpp:202)."""
+    return _solve(lib().glinalg_gcr, phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                  verbosity)
+
+
+def minv_vector_gcr_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector,
+                            extra_info, verbosity=None):
+    """minv_vector_gcr_restart (generic_gcr.cpp:337)."""
+    return _solve(lib().glinalg_gcr_restart, phi, phi0, size, max_iter, eps, matrix_vector,
+                  extra_info, verbosity, restart=restart_freq)
+
+
+def minv_vector_cg_m(phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, shifts,
+                     matrix_vector, extra_info, worst_first=False, verbosity=None):
+    """minv_vector_cg_m (generic_cg_m.cpp:312).  phi: a list of n_shift output fields."""
+    op, temp = _resolve(matrix_vector, extra_info)
+    try:
+        ptrs = [_field_ptr(p, writable=True) for p in phi[:n_shift]]
+        bp, _, bdev = _field_ptr(phi0)
+        if any(d != bdev for _, _, d in ptrs):
+            raise ValueError("phi and phi0 must all be on the host or all on the device")
+        arr = (C.POINTER(C.c_double) * n_shift)(*[_dptr(p) for p, _, _ in ptrs])
+        sh = np.ascontiguousarray(shifts[:n_shift], dtype=np.float64)
+        res = np.zeros(n_shift)
+        info = InfoStruct()
+        info.resSqmrhs = res.ctypes.data_as(C.POINTER(C.c_double))
+        info.n_rhs = n_shift
+        verb = verbosity.struct() if verbosity is not None else None
+        _capi.check(lib().glinalg_cg_m(op.handle, arr, _dptr(bp), int(n_shift), int(size),
+                                       int(resid_freq_check), int(max_iter), float(eps),
+                                       sh.ctypes.data_as(C.POINTER(C.c_double)), int(bool(worst_first)),
+                                       C.byref(verb) if verb is not None else None,
+                                       C.byref(_params(device=bdev)), C.byref(info)), "glinalg_cg_m")
+        return InversionInfo(info, res)
+    finally:
+        if temp:
+            op.close()
+
+
+# ---------------------------------------------------------------- batched, force, BLAS, RNG
+
+def cg_m_multi(op: Operator, phi, phi0, shifts, resid_freq_check=1, max_iter=10000, eps=1e-10):
+    """Multishift CG for several sources at once.  phi: (n_rhs, n_shift, size), phi0:
+    (n_rhs, size); both complex128, host or device."""
+    n_rhs, n_shift = phi.shape[0], phi.shape[1]
+    pp, _, dev = _field_ptr(phi, writable=True)
+    bp, _, _ = _field_ptr(phi0)
+    sh = np.ascontiguousarray(shifts, dtype=np.float64)
+    infos = (InfoStruct * n_rhs)()
+    res = [np.zeros(n_shift) for _ in range(n_rhs)]
+    for q in range(n_rhs):
+        infos[q].resSqmrhs = res[q].ctypes.data_as(C.POINTER(C.c_double))
+        infos[q].n_rhs = n_shift
+    _capi.check(lib().glinalg_cg_m_multi(op.handle, _dptr(pp), _dptr(bp), n_rhs, n_shift, op.size,
+                                         int(resid_freq_check), int(max_iter), float(eps),
+                                         sh.ctypes.data_as(C.POINTER(C.c_double)),
+                                         C.byref(_params(device=dev)), infos), "glinalg_cg_m_multi")
+    return [InversionInfo(infos[q], res[q]) for q in range(n_rhs)]
+
+
+def cg_batch(ops, phis, phi0s, max_iter=10000, eps=1e-10, precision=PREC_DOUBLE, delta=0.0):
+    """CG on independent Hermitian systems (one Operator each)."""
+    n = len(ops)
+    hs = (C.c_void_p * n)(*[o.handle.value for o in ops])
+    pps = [_field_ptr(p, writable=True) for p in phis]
+    bps = [_field_ptr(b) for b in phi0s]
+    dev = pps[0][2]
+    parr = (C.POINTER(C.c_double) * n)(*[_dptr(p) for p, _, _ in pps])
+    barr = (C.POINTER(C.c_double) * n)(*[_dptr(p) for p, _, _ in bps])
+    infos = (InfoStruct * n)()
+    _capi.check(lib().glinalg_cg_batch(hs, n, parr, barr, int(max_iter), float(eps),
+                                       C.byref(_params(precision, delta, dev)), infos), "glinalg_cg_batch")
+    return [InversionInfo(infos[q]) for q in range(n)]
+
+
+def staggered_force(op: Operator, X, Y, grad):
+    xp, _, dev = _field_ptr(X)
+    yp, _, _ = _field_ptr(Y)
+    if _is_torch(grad):
+        gp = C.c_void_p(grad.data_ptr())
+    else:
+        gp = C.c_void_p(grad.ctypes.data)
+    _capi.check(lib().glinalg_staggered_force(op.handle, _dptr(xp), _dptr(yp), _dptr(gp),
+                                              GLINALG_PTR_DEVICE if dev else 0), "glinalg_staggered_force")
+    return grad
+
+
+def staggered_action_grad(op: Operator, phi, sigma=0.0, eps=1e-12, max_iter=100000,
+                          precision=PREC_DOUBLE, delta=0.0, X_out=None):
+    """Returns (S, dS/dtheta, InversionInfo) for S = phi^dagger (D^dagger D + sigma)^-1 phi."""
+    pp, n, dev = _field_ptr(phi)
+    if dev:
+        import torch
+        grad = torch.zeros(2 * n, dtype=torch.float64, device=phi.device)
+        gp = C.c_void_p(grad.data_ptr())
+    else:
+        grad = np.zeros(2 * n)
+        gp = C.c_void_p(grad.ctypes.data)
+    xo = _dptr(_field_ptr(X_out, writable=True)[0]) if X_out is not None else None
+    act = C.c_double()
+    info = InfoStruct()
+    _capi.check(lib().glinalg_staggered_action_grad(op.handle, _dptr(pp), float(sigma), float(eps),
+                                                    int(max_iter), C.byref(act), _dptr(gp), xo,
+                                                    C.byref(_params(precision, delta, dev)), C.byref(info)),
+                "glinalg_staggered_action_grad")
+    return act.value, grad, InversionInfo(info)
+
+
+def dot(a, b):
+    """<a, b> = sum conj(a_i) b_i (generic_vector.h:102)."""
+    ap, n, dev = _field_ptr(a)
+    bp, _, _ = _field_ptr(b)
+    out = (C.c_double * 2)()
+    _capi.check(lib().glinalg_dot(_dptr(ap), _dptr(bp), n, out, GLINALG_PTR_DEVICE if dev else 0), "dot")
+    return complex(out[0], out[1])
+
+
+def norm2sq(a):
+    """sum |a_i|^2 (generic_vector.h:132)."""
+    ap, n, dev = _field_ptr(a)
+    out = C.c_double()
+    _capi.check(lib().glinalg_norm2sq(_dptr(ap), n, C.byref(out), GLINALG_PTR_DEVICE if dev else 0), "norm2sq")
+    return out.value
+
+
+class Generator:
+    """One std::mt19937 stream as the reference's tests use it (``std::mt19937 generator(seed)``)."""
+
+    def __init__(self, seed):
+        self.h = C.c_void_p()
+        _capi.check(lib().glinalg_rng_create(C.c_uint32(seed), C.byref(self.h)), "rng_create")
+
+    def rand_gauge_u1(self, lx, ly):
+        """rand_gauge_u1 (u1_utils.cpp:79-87)."""
+        U = np.zeros(2 * lx * ly, np.complex128)
+        _capi.check(lib().glinalg_rng_gauge_u1(self.h, _dptr(C.c_void_p(U.ctypes.data)), lx, ly), "gauge")
+        return U
+
+    def gauss_gauge_u1(self, lx, ly, beta):
+        """gauss_gauge_u1 (u1_utils.cpp:92-112)."""
+        U = np.zeros(2 * lx * ly, np.complex128)
+        _capi.check(lib().glinalg_rng_gauss_gauge_u1(self.h, _dptr(C.c_void_p(U.ctypes.data)), lx, ly,
+                                                     float(beta)), "gauss_gauge")
+        return U
+
+    def gaussian(self, n):
+        """gaussian<complex> (generic_vector.h:48-60)."""
+        v = np.zeros(n, np.complex128)
+        _capi.check(lib().glinalg_rng_gaussian(self.h, _dptr(C.c_void_p(v.ctypes.data)), C.c_long(n)), "gaussian")
+        return v
+
+    def __del__(self):
+        try:
+            lib().glinalg_rng_destroy(self.h)
+        except Exception:
+            pass

@@ -1,0 +1,126 @@
+"""ctypes declarations of the C-ABI in include/glinalg.h and the library loader.
+
+The library is the in-tree ``libglinalg_gb300.so`` built by ``build.py``.  Loading fails
+loudly when it is missing: there is no CPU implementation to fall back to.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libglinalg_gb300.so")
+
+GLINALG_PTR_HOST, GLINALG_PTR_DEVICE = 0, 1
+PREC_DOUBLE, PREC_SINGLE, PREC_HALF, PREC_BFLOAT = 0, 1, 2, 3
+
+_dp = C.POINTER(C.c_double)
+
+
+class GlinalgError(RuntimeError):
+    pass
+
+
+class OpDesc(C.Structure):
+    _fields_ = [("kind", C.c_int), ("lx", C.c_int), ("ly", C.c_int), ("nc", C.c_int),
+                ("mass", C.c_double), ("links", _dp), ("clover", _dp), ("hopping", _dp),
+                ("two_link", _dp), ("shift", C.c_double * 2), ("eo_shift", C.c_double * 2),
+                ("dof_shift", C.c_double * 2), ("flags", C.c_int)]
+
+
+class VerbStruct(C.Structure):
+    _fields_ = [("verbosity", C.c_int), ("verb_prefix", C.c_char_p),
+                ("precond_verbosity", C.c_int), ("precond_verb_prefix", C.c_char_p)]
+
+
+class InfoStruct(C.Structure):
+    _fields_ = [("resSq", C.c_double), ("iter", C.c_int), ("success", C.c_int),
+                ("ops_count", C.c_int), ("name", C.c_char * 32), ("resSqmrhs", _dp),
+                ("n_rhs", C.c_int), ("status", C.c_int), ("reliable_updates", C.c_int),
+                ("device_ms", C.c_double), ("gbytes", C.c_double)]
+
+
+class SolverParams(C.Structure):
+    _fields_ = [("precision", C.c_int), ("delta", C.c_double), ("flags", C.c_int),
+                ("reserved", C.c_int)]
+
+
+# Every function the header declares, with its ctypes prototype.
+def _prototypes():
+    P, vp, i, d, l, u32 = C.POINTER, C.c_void_p, C.c_int, C.c_double, C.c_long, C.c_uint32
+    st = C.c_int
+    solver = [vp, _dp, _dp, i, i, d, P(VerbStruct), P(SolverParams), P(InfoStruct)]
+    restart = [vp, _dp, _dp, i, i, d, i, P(VerbStruct), P(SolverParams), P(InfoStruct)]
+    return {
+        "glinalg_abi_version": (i, []),
+        "glinalg_status_string": (C.c_char_p, [st]),
+        "glinalg_last_error": (C.c_char_p, []),
+        "glinalg_device_count": (i, []),
+        "glinalg_set_stream": (st, [vp, i]),
+        "glinalg_profile_mixed_kernels": (st, [vp, i, i, _dp, _dp]),
+        "glinalg_operator_create": (st, [P(OpDesc), P(vp)]),
+        "glinalg_operator_destroy": (st, [vp]),
+        "glinalg_operator_set_mass": (st, [vp, d]),
+        "glinalg_operator_size": (l, [vp]),
+        "glinalg_operator_apply": (st, [vp, _dp, _dp, i]),
+        "glinalg_staggered_stencil": (st, [_dp, i, i, d, i, _dp, _dp, i]),
+        "glinalg_dot": (st, [_dp, _dp, l, _dp, i]),
+        "glinalg_norm2sq": (st, [_dp, l, _dp, i]),
+        "glinalg_cg": (st, solver),
+        "glinalg_cg_restart": (st, restart),
+        "glinalg_bicgstab": (st, solver),
+        "glinalg_bicgstab_restart": (st, restart),
+        "glinalg_gcr": (st, solver),
+        "glinalg_gcr_restart": (st, restart),
+        "glinalg_cg_m": (st, [vp, P(_dp), _dp, i, i, i, i, d, _dp, i, P(VerbStruct),
+                              P(SolverParams), P(InfoStruct)]),
+        "glinalg_cg_m_multi": (st, [vp, _dp, _dp, i, i, i, i, i, d, _dp, P(SolverParams),
+                                    P(InfoStruct)]),
+        "glinalg_cg_batch": (st, [P(vp), i, P(_dp), P(_dp), i, d, P(SolverParams), P(InfoStruct)]),
+        "glinalg_staggered_force": (st, [vp, _dp, _dp, _dp, i]),
+        "glinalg_staggered_action_grad": (st, [vp, _dp, d, d, i, _dp, _dp, _dp, P(SolverParams),
+                                               P(InfoStruct)]),
+        "glinalg_rng_create": (st, [u32, P(vp)]),
+        "glinalg_rng_destroy": (st, [vp]),
+        "glinalg_rng_gauge_u1": (st, [vp, _dp, i, i]),
+        "glinalg_rng_gauss_gauge_u1": (st, [vp, _dp, i, i, d]),
+        "glinalg_rng_gaussian": (st, [vp, _dp, l]),
+    }
+
+
+PROTOTYPES = _prototypes()
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load the CUDA library (building nothing); raises GlinalgError if it is absent."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(path):
+            raise GlinalgError(
+                f"{path} is missing: build it with `python generic-linalg_gb300/build.py` "
+                "(there is no CPU fallback)")
+        L = C.CDLL(path)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def lib():
+    return _lib if _lib is not None else load_library()
+
+
+def check(status, what):
+    if status != 0:
+        L = lib()
+        msg = L.glinalg_status_string(status).decode()
+        detail = L.glinalg_last_error().decode()
+        raise GlinalgError(f"{what}: {msg} ({detail})")

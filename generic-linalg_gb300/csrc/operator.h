@@ -1,0 +1,65 @@
+// operator.h -- the device-resident operator object behind glinalg_operator and the
+// launchers of its kernels.
+#pragma once
+
+#include "common.cuh"
+
+struct glinalg_operator_s {
+    int kind = 0;
+    int lx = 0, ly = 0, nc = 1;
+    double mass = 0.0;
+    long vol = 0;   // lx*ly sites
+    long size = 0;  // complex entries of a field (vol * nc)
+    int device = 0;
+
+    // FP64 device copies of the reference's data.
+    double2 *U = nullptr;         // links, U[2*i+mu]
+    double2 *clover = nullptr;    // stencil kinds
+    double2 *hopping = nullptr;
+    double2 *two_link = nullptr;
+    double2 shift{0, 0}, eo_shift{0, 0}, dof_shift{0, 0};
+
+    // Reduced-precision link copies for the inner iterations of mixed-precision solves,
+    // built on first use: the staggered hopping coefficients with the 1/2 and eta folded
+    // in (exact in every format: powers of two and signs).  Layout per site i:
+    // {h_x(i) = -1/2 U_x(i), h_y(i) = -1/2 eta(i) U_y(i)}.
+    float2 *H32 = nullptr;
+    __half2 *H16 = nullptr;
+    __nv_bfloat162 *Hbf = nullptr;
+
+    ~glinalg_operator_s();
+};
+
+namespace glinalg {
+
+bool is_staggered(int kind);
+bool is_stencil(int kind);
+bool is_hermitian(int kind);  // kinds CG may drive: D^dagger D and the gauge Laplacian
+
+// lhs = A rhs on `stream` (device pointers).  tmp: a scratch field of op->size entries for
+// the normal operator (may be null for other kinds).  done: optional device flag; when it
+// points at a non-zero value the kernels return without writing (used inside solver loops).
+glinalg_status launch_apply(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs,
+                            double2 *tmp, const int *done, cudaStream_t stream);
+
+// lhs = (A + sigma) rhs, optionally skipped when *done is set.
+glinalg_status launch_apply_sigma(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs,
+                                  double2 *tmp, double sigma, const int *done, cudaStream_t stream);
+// lhs = (A + sigma) rhs.
+glinalg_status launch_apply_shifted(const glinalg_operator_s *op, double2 *lhs,
+                                    const double2 *rhs, double2 *tmp, double sigma,
+                                    cudaStream_t stream);
+
+// Staggered-only pieces (used by the force and by the fused solver kernels).
+glinalg_status launch_staggered(const glinalg_operator_s *op, double2 *out, const double2 *in,
+                                double sign, const int *done, cudaStream_t stream);
+
+// The library's stream on the current device and its device-side scratch allocator.
+cudaStream_t lib_stream();
+void set_user_stream(cudaStream_t s, bool use);
+glinalg_status ensure_device();
+
+// Bytes an application of the operator moves (algorithmic), for info->gbytes.
+double apply_bytes(const glinalg_operator_s *op);
+
+}  // namespace glinalg

@@ -1,0 +1,139 @@
+// solver_util.h -- host-side plumbing shared by the solvers: scratch allocation on the
+// library stream, host/device staging of phi/phi0, the CUDA-graph while-loop that drives an
+// iteration body without host round trips, timing, and the reference's verbosity output.
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "operator.h"
+
+namespace glinalg {
+
+// Stream-ordered scratch allocations released when the object goes out of scope.
+class Scratch {
+  public:
+    explicit Scratch(cudaStream_t st) : st_(st) {}
+    ~Scratch()
+    {
+        for (void *p : ptrs_) cudaFreeAsync(p, st_);
+    }
+    template <class T>
+    glinalg_status alloc(T **out, size_t count)
+    {
+        void *p = nullptr;
+        cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (count ? count : 1), st_);
+        if (e != cudaSuccess) {
+            set_last_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+            return e == cudaErrorMemoryAllocation ? GLINALG_ERROR_OUT_OF_MEMORY : GLINALG_ERROR_CUDA;
+        }
+        ptrs_.push_back(p);
+        *out = (T *)p;
+        return GLINALG_SUCCESS;
+    }
+    template <class T>
+    glinalg_status zeros(T **out, size_t count)
+    {
+        GL_TRY(alloc(out, count));
+        GL_CUDA(cudaMemsetAsync(*out, 0, sizeof(T) * (count ? count : 1), st_));
+        return GLINALG_SUCCESS;
+    }
+
+  private:
+    cudaStream_t st_;
+    std::vector<void *> ptrs_;
+};
+
+// A CUDA graph holding one conditional WHILE node whose body is captured from `body`.
+// The body must end with a kernel that clears the condition once the solve is done.
+class LoopGraph {
+  public:
+    ~LoopGraph();
+    template <class F>
+    glinalg_status build(cudaStream_t st, F body)
+    {
+        GL_CUDA(cudaGraphCreate(&g_, 0));
+        GL_CUDA(cudaGraphConditionalHandleCreate(&h_, g_, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h_;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        GL_CUDA(cudaGraphAddNode(&node, g_, nullptr, nullptr, 0, &np));
+        cudaGraph_t bg = np.conditional.phGraph_out[0];
+        GL_CUDA(cudaStreamBeginCaptureToGraph(st, bg, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+        glinalg_status s = body(st, h_);
+        cudaGraph_t captured = nullptr;
+        cudaError_t e = cudaStreamEndCapture(st, &captured);
+        if (s != GLINALG_SUCCESS) return s;
+        GL_CUDA(e);
+        GL_CUDA(cudaGraphInstantiate(&ex_, g_, 0));
+        return GLINALG_SUCCESS;
+    }
+    glinalg_status launch(cudaStream_t st)
+    {
+        GL_CUDA(cudaGraphLaunch(ex_, st));
+        return GLINALG_SUCCESS;
+    }
+
+  private:
+    cudaGraph_t g_ = nullptr;
+    cudaGraphExec_t ex_ = nullptr;
+    cudaGraphConditionalHandle h_ = 0;
+};
+
+// Ends the enclosing while loop once *done is set (one thread).
+__global__ void k_loop_guard(const int *done, cudaGraphConditionalHandle h);
+
+// Device copies of phi (in/out) and phi0 (in) for a solve; copies back on finish().
+struct Staged {
+    double2 *x = nullptr;
+    const double2 *b = nullptr;
+    glinalg_status stage(Scratch &sc, double *phi, const double *phi0, long n, bool dev,
+                         cudaStream_t st);
+    glinalg_status finish(double *phi, long n, bool dev, cudaStream_t st);
+};
+
+struct EventTimer {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventTimer();
+    ~EventTimer();
+    void start(cudaStream_t st) { cudaEventRecord(a, st); }
+    void stop(cudaStream_t st) { cudaEventRecord(b, st); }
+    double ms();
+};
+
+// generic BLAS launchers (device pointers, results into device slots)
+glinalg_status launch_norm2(const double2 *a, long n, double *partials, unsigned *counter,
+                            double *out, cudaStream_t st);
+glinalg_status launch_dot(const double2 *a, const double2 *b, long n, double *partials,
+                          unsigned *counter, double2 *out, cudaStream_t st);
+glinalg_status launch_diffnorm2(const double2 *a, const double2 *b, long n, double *partials,
+                                unsigned *counter, double *out, cudaStream_t st);
+glinalg_status launch_sub(double2 *out, const double2 *a, const double2 *b, long n,
+                          cudaStream_t st);  // out = a - b
+
+// The reference's verbosity output (verbosity.h:73-131), byte-compatible lines on stdout.
+struct Verb {
+    int level = 0;
+    std::string prefix;
+    int precond_level = 0;
+    std::string precond_prefix;
+    bool present = false;
+    static Verb from(const glinalg_verbosity *v);
+    Verb restart_inner() const;  // shuffle_verbosity_restart (verbosity.h:27-43)
+    void resid(const std::string &alg, int iter, int ops, double relres) const;
+    void summary(const std::string &alg, bool success, int iter, int ops, double relres) const;
+    void summary_multi(bool success, int iter, int ops, const double *relres, int n) const;
+    void restart(const std::string &alg, int iter, int ops, double relres) const;
+};
+
+void fill_name(glinalg_info *info, const std::string &name);
+
+// Validates the common solver arguments and returns whether pointers are device pointers.
+glinalg_status check_solver_args(glinalg_operator op, const void *phi, const void *phi0,
+                                 int size, bool *dev, const glinalg_solver_params *params);
+
+}  // namespace glinalg

@@ -1,0 +1,31 @@
+// solvers.h -- internal solver entry points on device pointers (x in/out, b in).
+#pragma once
+
+#include "solver_util.h"
+
+namespace glinalg {
+
+// sigma: diagonal shift added to the operator (the reference's CG has none; used by the force)
+glinalg_status cg_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                       double eps, const Verb &verb, glinalg_info *info, cudaStream_t st,
+                       double sigma = 0.0);
+glinalg_status bicgstab_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b,
+                             int max_iter, double eps, const Verb &verb, glinalg_info *info,
+                             cudaStream_t st);
+glinalg_status gcr_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                        double eps, const Verb &verb, glinalg_info *info, cudaStream_t st);
+glinalg_status cg_m_fp64(const glinalg_operator_s *op, double2 *const *X, const double2 *b,
+                         int n_shift, int rfc, int max_iter, double eps, const double *shifts,
+                         bool worst_first, const Verb &verb, glinalg_info *info, cudaStream_t st);
+// which: 0 CG, 1 BiCGstab, 2 GCR
+glinalg_status restart_driver(int which, const glinalg_operator_s *op, double2 *x,
+                              const double2 *b, int max_iter, double eps, int restart_freq,
+                              const Verb &verb, glinalg_info *info, cudaStream_t st);
+
+// Mixed-precision CG with FP64 reliable updates (cg_mixed.cu).  sigma: diagonal shift added to
+// the operator (0 for the plain system).
+glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                        double eps, int precision, double delta, double sigma, const Verb &verb,
+                        glinalg_info *info, cudaStream_t st);
+
+}  // namespace glinalg

@@ -1,0 +1,264 @@
+/*
+ * glinalg.h -- C-ABI of the GB300 (sm_103a) implementation of generic-linalg's hot path:
+ * the 2D U(1) lattice operators (staggered D, D^dagger, D^dagger D, gauge Laplacian, the
+ * generic stencil_2d operator) and the Krylov solvers that call them (CG, multishift CG,
+ * BiCGstab, GCR and their restarted forms).
+ *
+ * Conventions shared with the reference (generic-linalg):
+ *   - A complex field is an array of complex<double> stored as interleaved (re, im) doubles;
+ *     site i = y*lx + x (x fastest), times nc colours for stencil operators
+ *     (lattice/lattice.h:52-83).
+ *   - Links: U[2*i + mu], mu = 0 for +x, mu = 1 for +y (operators.cpp:215-224).
+ *   - stencil_2d coefficient arrays keep the reference's layout
+ *     (stencil_2d/coarse_stencil.h:33-67): clover[c + nc*i], hopping[c + nc*i + d*nc*V*nc]
+ *     for d in {+x,+y,-x,-y}, two_link[...] for {+2x,+x+y,+2y,-x+y,-2x,-x-y,-2y,+x-y}.
+ *   - Solver arguments follow the reference's minv_vector_* signatures (phi = initial guess
+ *     in / solution out, phi0 = source, size, max_iter, eps = relative tolerance), and the
+ *     returned glinalg_info carries the fields of the reference's inversion_info.
+ *
+ * Every call is blocking: it returns after the device work it issued has finished.
+ * Pointers are host pointers unless GLINALG_PTR_DEVICE is set in the relevant flags, in
+ * which case they must be device pointers on the current CUDA device.  There is no CPU
+ * fallback: without a usable CUDA device every compute entry point returns
+ * GLINALG_ERROR_NO_DEVICE.
+ */
+#ifndef GLINALG_H
+#define GLINALG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLINALG_ABI_VERSION 1
+
+typedef enum glinalg_status {
+    GLINALG_SUCCESS = 0,
+    GLINALG_ERROR_INVALID_VALUE = 1,   /* bad argument (null pointer, size mismatch, ...) */
+    GLINALG_ERROR_UNSUPPORTED_OP = 2,  /* operator kind the entry point cannot drive */
+    GLINALG_ERROR_CUDA = 3,            /* a CUDA runtime call failed */
+    GLINALG_ERROR_NO_DEVICE = 4,       /* no usable CUDA device */
+    GLINALG_ERROR_OUT_OF_MEMORY = 5,
+    GLINALG_ERROR_INTERNAL = 6
+} glinalg_status;
+
+/* Outcome of a solve, in glinalg_info.status (the call itself returns GLINALG_SUCCESS). */
+typedef enum glinalg_solve_status {
+    GLINALG_SOLVE_CONVERGED = 0,
+    GLINALG_SOLVE_MAX_ITER = 1,   /* the reference's success == false */
+    GLINALG_SOLVE_BREAKDOWN = 2,  /* a recurrence denominator was exactly zero */
+    GLINALG_SOLVE_NONFINITE = 3   /* NaN or Inf appeared in a residual norm */
+} glinalg_solve_status;
+
+/* Operator kinds.  Each names the reference callback it replaces. */
+typedef enum glinalg_op_kind {
+    GLINALG_OP_STAGGERED = 0,         /* square_staggered_u1          operators.cpp:184 */
+    GLINALG_OP_STAGGERED_DAGGER = 1,  /* square_staggered_dagger_u1   operators.cpp:372 */
+    GLINALG_OP_STAGGERED_NORMAL = 2,  /* square_staggered_normal_u1   operators.cpp:444 */
+    GLINALG_OP_LAPLACE = 3,           /* square_laplace_u1            operators.cpp:73  */
+    GLINALG_OP_STENCIL = 4,           /* apply_stencil_2d             coarse_stencil.cpp:12  */
+    GLINALG_OP_STENCIL_EO = 5,        /* apply_stencil_2d_eo          coarse_stencil.cpp:395 */
+    GLINALG_OP_STENCIL_OE = 6         /* apply_stencil_2d_oe          coarse_stencil.cpp:560 */
+} glinalg_op_kind;
+
+/* Pointer-location flags. */
+#define GLINALG_PTR_HOST 0
+#define GLINALG_PTR_DEVICE 1
+
+/* Operator description; replaces staggered_u1_op (operators.h:7-15) and stencil_2d
+ * (coarse_stencil.h:33-67).  Arrays are read at glinalg_operator_create time and copied
+ * to the device; the caller may free them afterwards. */
+typedef struct glinalg_op_desc {
+    int kind;               /* glinalg_op_kind */
+    int lx, ly;             /* lattice extents (x_fine, y_fine) */
+    int nc;                 /* colours per site for stencil kinds (1 otherwise) */
+    double mass;            /* staggered_u1_op::mass (staggered and Laplace kinds) */
+    const double *links;    /* 2*lx*ly complex; staggered and Laplace kinds */
+    const double *clover;   /* lx*ly*nc*nc complex; stencil kinds */
+    const double *hopping;  /* 4*lx*ly*nc*nc complex; stencil kinds */
+    const double *two_link; /* 8*lx*ly*nc*nc complex or NULL (stencil_size 1) */
+    double shift[2];        /* stencil_2d::shift     (re, im) */
+    double eo_shift[2];     /* stencil_2d::eo_shift  (re, im) */
+    double dof_shift[2];    /* stencil_2d::dof_shift (re, im) */
+    int flags;              /* GLINALG_PTR_DEVICE if the arrays above are device pointers */
+} glinalg_op_desc;
+
+typedef struct glinalg_operator_s *glinalg_operator;
+
+/* inversion_verbose_struct (verbosity.h:18-24); levels as inversion_verbose_level
+ * (verbosity.h:9-16): -1 pass-through, 0 none, 1 summary, 2 restart detail, 3 detail.
+ * Lines are printed to stdout in the reference's format after the solve completes. */
+typedef struct glinalg_verbosity {
+    int verbosity;
+    const char *verb_prefix;
+    int precond_verbosity;
+    const char *precond_verb_prefix;
+} glinalg_verbosity;
+
+/* inversion_info (inverter_struct.h:14-43) plus device-side diagnostics. */
+typedef struct glinalg_info {
+    double resSq;        /* squared absolute true residual |b - A x|^2 (0 for CG-M, as in the reference) */
+    int iter;            /* iterations */
+    int success;         /* 1 if converged */
+    int ops_count;       /* operator applications, counted as the reference counts them */
+    char name[32];       /* "CG", "CG(n)", "CG-M", "BiCGStab", "GCR", ... */
+    double *resSqmrhs;   /* caller-provided, n_rhs entries: per-shift |(A+s)x - b|^2 (CG-M) */
+    int n_rhs;
+    int status;          /* glinalg_solve_status */
+    int reliable_updates;/* mixed precision: number of FP64 residual recomputations */
+    double device_ms;    /* device time of the solve, CUDA events */
+    double gbytes;       /* algorithmic bytes moved by the solve's kernels, in GB */
+} glinalg_info;
+
+/* Arithmetic of a solve. */
+typedef enum glinalg_precision {
+    GLINALG_PREC_DOUBLE = 0,  /* FP64 throughout, the reference's recurrence */
+    GLINALG_PREC_SINGLE = 1,  /* FP32 inner iterations, FP64 reliable updates */
+    GLINALG_PREC_HALF = 2,    /* FP16 storage / FP32 arithmetic inner, FP64 reliable updates */
+    GLINALG_PREC_BFLOAT = 3   /* BF16 storage / FP32 arithmetic inner, FP64 reliable updates */
+} glinalg_precision;
+
+typedef struct glinalg_solver_params {
+    int precision;     /* glinalg_precision; only CG on Hermitian kinds accepts != DOUBLE */
+    double delta;      /* reliable-update trigger: recompute when |r| < delta * max|r| (0 -> 0.1) */
+    int flags;         /* GLINALG_PTR_DEVICE: phi / phi0 are device pointers */
+    int reserved;
+} glinalg_solver_params;
+
+/* ---- library ---- */
+int glinalg_abi_version(void);
+const char *glinalg_status_string(glinalg_status s);
+/* Text of the last error raised on the calling host thread ("" if none). */
+const char *glinalg_last_error(void);
+/* Number of CUDA devices the library can use (0 if none). */
+int glinalg_device_count(void);
+/* Issue the library's work on `stream` (a cudaStream_t of the current device) instead of
+ * its own non-blocking stream; use = 0 goes back to the library's stream.  Calls still
+ * return only after their work has finished. */
+glinalg_status glinalg_set_stream(void *stream, int use);
+
+/* ---- operators ---- */
+glinalg_status glinalg_operator_create(const glinalg_op_desc *desc, glinalg_operator *out);
+glinalg_status glinalg_operator_destroy(glinalg_operator op);
+/* The reference's tests shift the operator by editing staggered_u1_op::mass between solves
+ * (tests/multishift/multishift.cpp:446); this is the same edit. */
+glinalg_status glinalg_operator_set_mass(glinalg_operator op, double mass);
+/* Number of complex entries of a field (lx*ly, times nc for stencil kinds). */
+long glinalg_operator_size(glinalg_operator op);
+/* lhs = A rhs, the operator callback of the reference (lhs overwritten, rhs untouched). */
+glinalg_status glinalg_operator_apply(glinalg_operator op, double *lhs, const double *rhs,
+                                      int flags);
+
+/* get_square_staggered_u1_stencil / get_square_staggered_dagger_u1_stencil
+ * (operators_stencil.cpp:14-63, :120-169): fills hopping_out (4*lx*ly complex) with the
+ * staggered hopping coefficients and shift_out (1 complex) with the mass. */
+glinalg_status glinalg_staggered_stencil(const double *links, int lx, int ly, double mass,
+                                         int dagger, double *hopping_out, double *shift_out,
+                                         int flags);
+
+/* ---- BLAS-1 on fields (generic_vector.h) ---- */
+glinalg_status glinalg_dot(const double *a, const double *b, long n, double out[2], int flags);
+glinalg_status glinalg_norm2sq(const double *a, long n, double *out, int flags);
+
+/* ---- solvers (the reference's minv_vector_* calling convention) ---- */
+/* minv_vector_cg                generic_cg.cpp:278 */
+glinalg_status glinalg_cg(glinalg_operator op, double *phi, const double *phi0, int size,
+                          int max_iter, double eps, const glinalg_verbosity *verb,
+                          const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_cg_restart        generic_cg.cpp:387 */
+glinalg_status glinalg_cg_restart(glinalg_operator op, double *phi, const double *phi0, int size,
+                                  int max_iter, double eps, int restart_freq,
+                                  const glinalg_verbosity *verb,
+                                  const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_bicgstab          generic_bicgstab.cpp:205 */
+glinalg_status glinalg_bicgstab(glinalg_operator op, double *phi, const double *phi0, int size,
+                                int max_iter, double eps, const glinalg_verbosity *verb,
+                                const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_bicgstab_restart  generic_bicgstab.cpp:345 */
+glinalg_status glinalg_bicgstab_restart(glinalg_operator op, double *phi, const double *phi0,
+                                        int size, int max_iter, double eps, int restart_freq,
+                                        const glinalg_verbosity *verb,
+                                        const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_gcr               generic_gcr.cpp:202 */
+glinalg_status glinalg_gcr(glinalg_operator op, double *phi, const double *phi0, int size,
+                           int max_iter, double eps, const glinalg_verbosity *verb,
+                           const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_gcr_restart       generic_gcr.cpp:337 */
+glinalg_status glinalg_gcr_restart(glinalg_operator op, double *phi, const double *phi0, int size,
+                                   int max_iter, double eps, int restart_freq,
+                                   const glinalg_verbosity *verb,
+                                   const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_cg_m              generic_cg_m.cpp:312.  phi: n_shift pointers to solution
+ * vectors (zeroed, then written); shifts must be sorted ascending as in the reference and
+ * are left unchanged on return; info->resSqmrhs (n_shift entries) receives the explicit
+ * squared residual of every shifted system. */
+glinalg_status glinalg_cg_m(glinalg_operator op, double *const *phi, const double *phi0,
+                            int n_shift, int size, int resid_freq_check, int max_iter,
+                            double eps, const double *shifts, int worst_first,
+                            const glinalg_verbosity *verb, const glinalg_solver_params *params,
+                            glinalg_info *info);
+
+/* ---- batched solves (no reference counterpart: the reference solves systems one at a
+ * time in a loop; these run many independent systems in one device launch sequence) ---- */
+
+/* Multishift CG for n_rhs independent sources of one operator, all shifts and sources
+ * iterated together.  phi: n_rhs*n_shift*size complex (rhs-major, then shift), phi0:
+ * n_rhs*size complex.  infos: n_rhs entries (each with resSqmrhs of n_shift entries or NULL).
+ * Same recurrence per source as glinalg_cg_m. */
+glinalg_status glinalg_cg_m_multi(glinalg_operator op, double *phi, const double *phi0,
+                                  int n_rhs, int n_shift, int size, int resid_freq_check,
+                                  int max_iter, double eps, const double *shifts,
+                                  const glinalg_solver_params *params, glinalg_info *infos);
+
+/* CG on n_sys independent Hermitian systems (staggered-normal or Laplace kinds, any sizes)
+ * advanced together with per-system convergence masks.  phi[s] / phi0[s] have
+ * glinalg_operator_size(ops[s]) complex entries. */
+glinalg_status glinalg_cg_batch(const glinalg_operator *ops, int n_sys, double *const *phi,
+                                const double *const *phi0, int max_iter, double eps,
+                                const glinalg_solver_params *params, glinalg_info *infos);
+
+/* ---- adjoint force (no reference counterpart) ----
+ * For S(theta) = phi^dagger (D^dagger D + sigma)^-1 phi with U_mu(x) = exp(i theta_mu(x)):
+ * given X = (D^dagger D + sigma)^-1 phi and Y = D X, writes
+ * dS/dtheta_mu(x) = -2 Re(Y^dagger dD/dtheta_mu(x) X) to grad[2*i + mu] (2*lx*ly reals).
+ * op must be a staggered kind (its links and mass define D). */
+glinalg_status glinalg_staggered_force(glinalg_operator op, const double *X, const double *Y,
+                                       double *grad, int flags);
+/* Forward solve plus force: X = (D^dagger D + sigma)^-1 phi by CG to relative residual eps
+ * (params->precision selects the arithmetic), Y = D X, grad as above, *action = Re(phi^dagger X).
+ * X_out may be NULL. */
+glinalg_status glinalg_staggered_action_grad(glinalg_operator op, const double *phi, double sigma,
+                                             double eps, int max_iter, double *action,
+                                             double *grad, double *X_out,
+                                             const glinalg_solver_params *params,
+                                             glinalg_info *info);
+
+/* ---- measurement ----
+ * Times the two inner-iteration kernels of the mixed-precision CG (A: direction update +
+ * D p + norm; B: D^dagger t + solution/residual update + norm) on op's lattice, each launched
+ * n_launch times on its own between CUDA events, on resident buffers.  ms[0], ms[1]: mean
+ * duration of one launch of A and B; bytes[0], bytes[1]: algorithmic bytes one launch moves.
+ * op must be GLINALG_OP_STAGGERED_NORMAL; precision SINGLE, HALF or BFLOAT. */
+glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision, int n_launch,
+                                             double ms[2], double bytes[2]);
+
+/* ---- inputs the way the reference's tests make them (host side) ----
+ * A generator is one std::mt19937 stream (as `std::mt19937 generator(seed)` in the tests);
+ * successive calls continue the stream. */
+typedef struct glinalg_rng_s *glinalg_rng;
+glinalg_status glinalg_rng_create(uint32_t seed, glinalg_rng *out);
+glinalg_status glinalg_rng_destroy(glinalg_rng rng);
+/* rand_gauge_u1 (u1_utils.cpp:79-87): U = exp(i theta), theta uniform in (-pi, pi). */
+glinalg_status glinalg_rng_gauge_u1(glinalg_rng rng, double *links, int lx, int ly);
+/* gauss_gauge_u1 (u1_utils.cpp:92-112): theta normal with variance 1/beta. */
+glinalg_status glinalg_rng_gauss_gauge_u1(glinalg_rng rng, double *links, int lx, int ly,
+                                          double beta);
+/* gaussian<complex> (generic_vector.h:48-60): re and im independent N(0,1). */
+glinalg_status glinalg_rng_gaussian(glinalg_rng rng, double *v, long n_complex);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GLINALG_H */

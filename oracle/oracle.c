@@ -1,0 +1,605 @@
+/*
+ * oracle.c -- CPU oracle (TEST INFRASTRUCTURE ONLY; see oracle.h).
+ *
+ * Plain C99 with double _Complex.  GCC lowers complex * and / to the same C99 Annex G
+ * sequences (__muldc3 / __divdc3 on the NaN path and for division) that libstdc++'s
+ * std::complex<double> uses, so with -O2 -ffp-contract=off this file reproduces the
+ * reference's floating-point operation order.  The ordering of every accumulation below is
+ * deliberate: it follows the cited reference loop term by term.
+ */
+#include "oracle.h"
+
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include <stdio.h>
+#include <string.h>
+
+typedef double _Complex cplx;
+
+#define CX(p) ((cplx *)(p))
+#define CCX(p) ((const cplx *)(p))
+
+static inline cplx mk(double re, double im) { cplx z; __real__ z = re; __imag__ z = im; return z; }
+
+/* ---------------------------------------------------------------- operators */
+
+/* operator_utils/operators.cpp:184-239 (square_staggered_u1): hopping with eta_x = 1,
+ * eta_y = (-1)^x, then 0.5 * sum, then + mass*psi.  sign = +1 for D, -1 for D^dagger
+ * (operators.cpp:372-441 flips every hopping sign and keeps the mass). */
+static void staggered_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass, int lx,
+                            int ly, double sign)
+{
+    for (long i = 0; i < (long)lx * ly; i++) {
+        int x = (int)(i % lx), y = (int)(i / lx);
+        double eta1 = (double)(1 - 2 * (x % 2));
+        int xp = (x + 1) % lx, xm = (x + lx - 1) % lx;
+        int yp = (y + 1) % ly, ym = (y + ly - 1) % ly;
+        cplx acc = 0.0;
+        cplx t;
+        t = U[(long)y * lx * 2 + x * 2] * rhs[(long)y * lx + xp];
+        acc = (sign > 0) ? acc - t : acc + t;
+        t = conj(U[(long)y * lx * 2 + xm * 2]) * rhs[(long)y * lx + xm];
+        acc = (sign > 0) ? acc + t : acc - t;
+        t = (eta1 * U[(long)y * lx * 2 + x * 2 + 1]) * rhs[(long)yp * lx + x];
+        acc = (sign > 0) ? acc - t : acc + t;
+        t = (eta1 * conj(U[(long)ym * lx * 2 + x * 2 + 1])) * rhs[(long)ym * lx + x];
+        acc = (sign > 0) ? acc + t : acc - t;
+        acc = 0.5 * acc;
+        acc = acc + mass * rhs[i];
+        lhs[i] = acc;
+    }
+}
+
+/* operator_utils/operators.cpp:73-120 (square_laplace_u1): lhs = (4+mass) psi
+ * - sum_mu [U_mu(x) psi(x+mu) + U_mu(x-mu)^* psi(x-mu)], accumulated in the order
+ * +x, -x, +y, -y, then the diagonal. */
+static void laplace_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass, int lx, int ly)
+{
+    for (long i = 0; i < (long)lx * ly; i++) {
+        int x = (int)(i % lx), y = (int)(i / lx);
+        int xp = (x + 1) % lx, xm = (x + lx - 1) % lx;
+        int yp = (y + 1) % ly, ym = (y + ly - 1) % ly;
+        cplx acc = 0.0;
+        acc = acc - U[(long)y * lx * 2 + x * 2] * rhs[(long)y * lx + xp];
+        acc = acc - conj(U[(long)y * lx * 2 + xm * 2]) * rhs[(long)y * lx + xm];
+        acc = acc - U[(long)y * lx * 2 + x * 2 + 1] * rhs[(long)yp * lx + x];
+        acc = acc - conj(U[(long)ym * lx * 2 + x * 2 + 1]) * rhs[(long)ym * lx + x];
+        acc = acc + (4 + mass) * rhs[i];
+        lhs[i] = acc;
+    }
+}
+
+/* stencil_2d/coarse_stencil.cpp:12-172 (apply_stencil_2d, DIR_ALL), :395-460 (_eo) and
+ * :560-625 (_oe).  parity: 0 = full stencil, 1 = even output sites only (hopping only),
+ * 2 = odd output sites only (hopping only).  Site parity is even when x+y is even
+ * (lattice/lattice.h:128-139). */
+static void stencil_apply(const orc_op *op, cplx *lhs, const cplx *rhs, int parity)
+{
+    const int lx = op->lx, ly = op->ly, nc = op->nc;
+    const long vol = (long)lx * ly;
+    const long lsize = vol * nc;
+    const cplx *clov = CCX(op->clover), *hop = CCX(op->hopping), *two = CCX(op->two_link);
+    const cplx shift = mk(op->shift[0], op->shift[1]);
+    const cplx eo_shift = mk(op->eo_shift[0], op->eo_shift[1]);
+    const cplx dof_shift = mk(op->dof_shift[0], op->dof_shift[1]);
+    /* neighbour offsets in the reference's order: hopping {+x,+y,-x,-y}, two-link
+     * {+2x,+x+y,+2y,-x+y,-2x,-x-y,-2y,+x-y} (coarse_stencil.h:44-54). */
+    static const int hx[4] = {1, 0, -1, 0}, hy[4] = {0, 1, 0, -1};
+    static const int tx[8] = {2, 1, 0, -1, -2, -1, 0, 1}, ty[8] = {0, 1, 2, 1, 0, -1, -2, -1};
+
+    for (long i = 0; i < lsize; i++) {
+        int color = (int)(i % nc);
+        long site = i / nc;
+        int x = (int)(site % lx), y = (int)(site / lx);
+        int even = ((x + y) % 2) == 0;
+        cplx acc = 0.0;
+        if (parity == 1 && !even) { lhs[i] = 0.0; continue; }
+        if (parity == 2 && even) { lhs[i] = 0.0; continue; }
+        if (parity == 0)
+            for (int c = 0; c < nc; c++) acc += clov[c + (long)nc * i] * rhs[site * nc + c];
+        for (int d = 0; d < 4; d++) {
+            int xx = (x + hx[d] + lx) % lx, yy = (y + hy[d] + ly) % ly;
+            long nb = ((long)yy * lx + xx) * nc;
+            for (int c = 0; c < nc; c++)
+                acc += hop[c + (long)nc * i + (long)d * nc * lsize] * rhs[nb + c];
+        }
+        if (parity == 0 && two != NULL) {
+            for (int d = 0; d < 8; d++) {
+                int xx = (x + tx[d] + 2 * lx) % lx, yy = (y + ty[d] + 2 * ly) % ly;
+                long nb = ((long)yy * lx + xx) * nc;
+                for (int c = 0; c < nc; c++)
+                    acc += two[c + (long)nc * i + (long)d * nc * lsize] * rhs[nb + c];
+            }
+        }
+        if (parity == 0) {
+            if (cabs(shift) != 0.0) acc += shift * rhs[i];
+            if (cabs(eo_shift) != 0.0) acc += ((even ? 1.0 : -1.0) * eo_shift) * rhs[i];
+            if (cabs(dof_shift) != 0.0) acc += ((color < nc / 2 ? 1.0 : -1.0) * dof_shift) * rhs[i];
+        }
+        lhs[i] = acc;
+    }
+}
+
+long orc_op_size(const orc_op *op)
+{
+    long v = (long)op->lx * op->ly;
+    if (op->kind >= ORC_STENCIL) v *= op->nc;
+    return v;
+}
+
+void orc_apply(const orc_op *op, double *lhs, const double *rhs)
+{
+    const cplx *U = CCX(op->links);
+    switch (op->kind) {
+    case ORC_STAGGERED:
+        staggered_apply(CX(lhs), CCX(rhs), U, op->mass, op->lx, op->ly, +1.0);
+        break;
+    case ORC_STAGGERED_DAGGER:
+        staggered_apply(CX(lhs), CCX(rhs), U, op->mass, op->lx, op->ly, -1.0);
+        break;
+    case ORC_STAGGERED_NORMAL: {
+        /* operators.cpp:444-453: tmp = D rhs; lhs = D^dagger tmp. */
+        long v = (long)op->lx * op->ly;
+        cplx *tmp = (cplx *)malloc(sizeof(cplx) * v);
+        staggered_apply(tmp, CCX(rhs), U, op->mass, op->lx, op->ly, +1.0);
+        staggered_apply(CX(lhs), tmp, U, op->mass, op->lx, op->ly, -1.0);
+        free(tmp);
+        break;
+    }
+    case ORC_LAPLACE:
+        laplace_apply(CX(lhs), CCX(rhs), U, op->mass, op->lx, op->ly);
+        break;
+    case ORC_STENCIL: stencil_apply(op, CX(lhs), CCX(rhs), 0); break;
+    case ORC_STENCIL_EO: stencil_apply(op, CX(lhs), CCX(rhs), 1); break;
+    case ORC_STENCIL_OE: stencil_apply(op, CX(lhs), CCX(rhs), 2); break;
+    default: break;
+    }
+}
+
+/* operator_utils/operators_stencil.cpp:14-63 (get_square_staggered_u1_stencil) and
+ * :120-169 (get_square_staggered_dagger_u1_stencil): hopping = {-1/2 U_x(x),
+ * -1/2 eta U_y(x), +1/2 U_x(x-x)^*, +1/2 eta U_y(x-y)^*}, negated for the dagger. */
+void orc_staggered_stencil(double *hopping, const double *links, int lx, int ly, int dagger)
+{
+    cplx *H = CX(hopping);
+    const cplx *U = CCX(links);
+    const long vol = (long)lx * ly;
+    const double s = dagger ? -1.0 : 1.0;
+    for (long i = 0; i < vol; i++) {
+        int x = (int)(i % lx), y = (int)(i / lx);
+        int eta1 = 1 - 2 * (x % 2);
+        long im_x = (long)y * lx + (x - 1 + lx) % lx;
+        long im_y = (long)((y - 1 + ly) % ly) * lx + x;
+        H[i] = (-0.5 * s) * U[2 * i];
+        H[i + vol] = ((-0.5 * s) * eta1) * U[2 * i + 1];
+        H[i + 2 * vol] = (0.5 * s) * conj(U[2 * im_x]);
+        H[i + 3 * vol] = ((0.5 * s) * eta1) * conj(U[2 * im_y + 1]);
+    }
+}
+
+/* ---------------------------------------------------------------- BLAS-1 */
+
+/* generic_vector.h:102-114: res = sum conj(a_i) b_i, serial left to right. */
+static cplx cdot(const cplx *a, const cplx *b, long n)
+{
+    cplx r = 0.0;
+    for (long i = 0; i < n; i++) r = r + conj(a[i]) * b[i];
+    return r;
+}
+
+/* generic_vector.h:132-145 */
+static double cnorm2(const cplx *a, long n)
+{
+    double r = 0.0;
+    for (long i = 0; i < n; i++) r = r + creal(conj(a[i]) * a[i]);
+    return r;
+}
+
+/* generic_vector.h:160-169 */
+static double cdiffnorm2(const cplx *a, const cplx *b, long n)
+{
+    double r = 0.0;
+    for (long i = 0; i < n; i++) r = r + creal(conj(a[i] - b[i]) * (a[i] - b[i]));
+    return r;
+}
+
+void orc_dot(const double *a, const double *b, long n, double out[2])
+{
+    cplx r = cdot(CCX(a), CCX(b), n);
+    out[0] = creal(r);
+    out[1] = cimag(r);
+}
+double orc_norm2sq(const double *a, long n) { return cnorm2(CCX(a), n); }
+double orc_diffnorm2sq(const double *a, const double *b, long n) { return cdiffnorm2(CCX(a), CCX(b), n); }
+
+/* libstdc++'s real / complex constructs complex(x, 0) and divides (operator/(T, complex)). */
+static inline cplx rdivc(double x, cplx y) { return mk(x, 0.0) / y; }
+/* libstdc++'s complex / real divides each component (complex::operator/=(T)). */
+static inline cplx cdivr(cplx x, double y) { return mk(creal(x) / y, cimag(x) / y); }
+
+static void record(double *hist, int cap, int k, double v)
+{
+    if (hist != NULL && k >= 0 && k < cap) hist[k] = v;
+}
+
+static void set_name(orc_info *info, const char *name)
+{
+    strncpy(info->name, name, sizeof(info->name) - 1);
+    info->name[sizeof(info->name) - 1] = 0;
+}
+
+/* ---------------------------------------------------------------- CG */
+
+/* generic_cg.cpp:278-382 (complex minv_vector_cg). */
+void orc_cg(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+            double eps, orc_info *info, double *hist, int hist_cap)
+{
+    cplx *phi = CX(phi_);
+    const cplx *phi0 = CCX(phi0_);
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta;
+    double rsq, rsqNew = 0.0, bsqrt, truersq;
+    int k, ops = 0;
+    long i;
+
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)p, (const double *)phi); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
+    memcpy(p, r, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    rsq = cnorm2(r, size);
+
+    for (k = 0; k < max_iter; k++) {
+        alpha = rdivc(rsq, cdot(p, Ap, size));
+        for (i = 0; i < size; i++) {
+            phi[i] = phi[i] + alpha * p[i];
+            r[i] = r[i] - alpha * Ap[i];
+        }
+        rsqNew = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsqNew) / bsqrt);
+        if (sqrt(rsqNew) < eps * bsqrt || k == max_iter - 1) break;
+        beta = mk(rsqNew / rsq, 0.0);
+        rsq = rsqNew;
+        for (i = 0; i < size; i++) p[i] = r[i] + beta * p[i];
+        orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    k++;
+    orc_apply(op, (double *)Ap, (const double *)phi); ops++;
+    truersq = cdiffnorm2(Ap, phi0, size);
+    free(r); free(p); free(Ap);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "CG");
+}
+
+/* Restart driver shared by CG / BiCGstab / GCR: generic_cg.cpp:387-427,
+ * generic_bicgstab.cpp:345-385, generic_gcr.cpp:337-378. */
+typedef void (*orc_solver_fn)(const orc_op *, double *, const double *, long, int, double,
+                              orc_info *, double *, int);
+
+static void restart_driver(orc_solver_fn fn, const char *base, const orc_op *op, double *phi,
+                           const double *phi0, long size, int max_iter, double res,
+                           int restart_freq, orc_info *info)
+{
+    double bsqrt = sqrt(cnorm2(CCX(phi0), size));
+    int iter = 0, ops = 0;
+    orc_info inner;
+    memset(&inner, 0, sizeof(inner));
+    do {
+        fn(op, phi, phi0, size, restart_freq, res, &inner, NULL, 0);
+        iter += inner.iter;
+        ops += inner.ops_count;
+    } while (iter < max_iter && inner.success == 0 && sqrt(inner.resSq) / bsqrt > res);
+    *info = inner;
+    info->iter = iter;
+    info->ops_count = ops;
+    info->success = (sqrt(inner.resSq) / bsqrt > res) ? 0 : 1;
+    char nm[32];
+    snprintf(nm, sizeof(nm), "%s(%d)", base, restart_freq);
+    set_name(info, nm);
+}
+
+void orc_cg_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                    double eps, int restart_freq, orc_info *info)
+{
+    restart_driver(orc_cg, "CG", op, phi, phi0, size, max_iter, eps, restart_freq, info);
+}
+
+/* ---------------------------------------------------------------- BiCGstab */
+
+/* generic_bicgstab.cpp:205-341 (complex minv_vector_bicgstab). */
+void orc_bicgstab(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+                  double eps, orc_info *info, double *hist, int hist_cap)
+{
+    cplx *phi = CX(phi_);
+    const cplx *phi0 = CCX(phi0_);
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *r0 = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx *s = (cplx *)calloc(size, sizeof(cplx));
+    cplx *As = (cplx *)calloc(size, sizeof(cplx));
+    cplx rho, rhoNew, alpha, beta, omega;
+    double rsq, bsqrt, truersq;
+    int k, ops = 0;
+    long i;
+
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)Ap, (const double *)phi); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - Ap[i];
+    memcpy(r0, r, sizeof(cplx) * size);
+    memcpy(p, r, sizeof(cplx) * size);
+    rho = cdot(r0, r, size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+
+    for (k = 0; k < max_iter; k++) {
+        alpha = rho / cdot(r0, Ap, size);
+        for (i = 0; i < size; i++) s[i] = r[i] - alpha * Ap[i];
+        orc_apply(op, (double *)As, (const double *)s); ops++;
+        omega = cdot(As, s, size) / cdot(As, As, size);
+        for (i = 0; i < size; i++) phi[i] = phi[i] + alpha * p[i] + omega * s[i];
+        for (i = 0; i < size; i++) r[i] = s[i] - omega * As[i];
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+        if (sqrt(rsq) < eps * bsqrt || k == max_iter - 1) break;
+        rhoNew = cdot(r0, r, size);
+        beta = rhoNew / rho * (alpha / omega);
+        rho = rhoNew;
+        for (i = 0; i < size; i++) p[i] = r[i] + beta * (p[i] - omega * Ap[i]);
+        orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    k++;
+    orc_apply(op, (double *)Ap, (const double *)phi); ops++;
+    truersq = cdiffnorm2(Ap, phi0, size);
+    free(r); free(r0); free(p); free(Ap); free(s); free(As);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "BiCGStab");
+}
+
+void orc_bicgstab_restart(const orc_op *op, double *phi, const double *phi0, long size,
+                          int max_iter, double eps, int restart_freq, orc_info *info)
+{
+    restart_driver(orc_bicgstab, "BiCGStab", op, phi, phi0, size, max_iter, eps, restart_freq, info);
+}
+
+/* ---------------------------------------------------------------- GCR */
+
+/* generic_gcr.cpp:202-333 (complex minv_vector_gcr): every search direction p_i and A p_i
+ * is kept and the new direction is A-orthogonalised against all of them. */
+void orc_gcr(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+             double eps, orc_info *info, double *hist, int hist_cap)
+{
+    cplx *phi = CX(phi_);
+    const cplx *phi0 = CCX(phi0_);
+    cplx *x = (cplx *)calloc(size, sizeof(cplx));
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ar = (cplx *)calloc(size, sizeof(cplx));
+    int cap = (max_iter > 0 ? max_iter : 1) + 1;
+    cplx **ps = (cplx **)calloc(cap, sizeof(cplx *));
+    cplx **Aps = (cplx **)calloc(cap, sizeof(cplx *));
+    int nstore = 0;
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta_ij;
+    double rsq, bsqrt, truersq = 0.0;
+    int k, ops = 0, ii;
+    long i;
+
+    memcpy(x, phi, sizeof(cplx) * size);
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)p, (const double *)x); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
+    memcpy(p, r, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+
+    for (k = 0; k < max_iter; k++) {
+        ps[nstore] = p;
+        Aps[nstore] = Ap;
+        nstore++;
+        alpha = cdivr(cdot(Ap, r, size), cnorm2(Ap, size));
+        for (i = 0; i < size; i++) {
+            x[i] = x[i] + alpha * p[i];
+            r[i] = r[i] - alpha * Ap[i];
+        }
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+        if (sqrt(rsq) < eps * bsqrt || k == max_iter - 1) break;
+        orc_apply(op, (double *)Ar, (const double *)r); ops++;
+        p = (cplx *)malloc(sizeof(cplx) * size);
+        memcpy(p, r, sizeof(cplx) * size);
+        Ap = (cplx *)malloc(sizeof(cplx) * size);
+        memcpy(Ap, Ar, sizeof(cplx) * size);
+        for (ii = 0; ii <= k; ii++) {
+            beta_ij = cdivr(-cdot(Aps[ii], Ar, size), cnorm2(Aps[ii], size));
+            for (i = 0; i < size; i++) {
+                p[i] += beta_ij * ps[ii][i];
+                Ap[i] += beta_ij * Aps[ii][i];
+            }
+        }
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    k++;
+    /* the true-residual check reuses a scratch vector (generic_gcr.cpp:303-305) */
+    cplx *chk = (cplx *)calloc(size, sizeof(cplx));
+    orc_apply(op, (double *)chk, (const double *)x); ops++;
+    for (i = 0; i < size; i++) truersq += creal(conj(chk[i] - phi0[i]) * (chk[i] - phi0[i]));
+    memcpy(phi, x, sizeof(cplx) * size);
+    free(chk);
+    /* when the loop ran zero times the initial p / Ap were never stored */
+    if (nstore == 0) { free(p); free(Ap); }
+    for (ii = 0; ii < nstore; ii++) { free(ps[ii]); free(Aps[ii]); }
+    free(ps); free(Aps); free(x); free(r); free(Ar);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "GCR");
+}
+
+void orc_gcr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                     double eps, int restart_freq, orc_info *info)
+{
+    restart_driver(orc_gcr, "GCR", op, phi, phi0, size, max_iter, eps, restart_freq, info);
+}
+
+/* ---------------------------------------------------------------- CG-M */
+
+/* generic_cg_m.cpp:312-600 (complex minv_vector_cg_m, Jegerlehner hep-lat/9612014).
+ * Converged shifts are swapped to the tail (:434-486) and the order is restored at the
+ * end (:533-558); here the permutation acts on local index tables, which is observably the
+ * same as the reference's in-place permutation of the caller's phi[] and shifts[]. */
+void orc_cg_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shift, long size,
+              int resid_freq_check, int max_iter, double eps, const double *shifts_in,
+              int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap)
+{
+    const cplx *phi0 = CCX(phi0_);
+    cplx **phi = (cplx **)malloc(sizeof(cplx *) * n_shift);
+    cplx **p_s = (cplx **)malloc(sizeof(cplx *) * n_shift);
+    cplx *alpha_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *beta_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *zeta_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *zeta_s_prev = (cplx *)malloc(sizeof(cplx) * n_shift);
+    double *shifts = (double *)malloc(sizeof(double) * n_shift);
+    int *mapping = (int *)malloc(sizeof(int) * n_shift);
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta, beta_prev, tmp;
+    double rsq, rsqNew = 0.0, bsqrt;
+    int k, n, n_shift_rem = n_shift, ops = 0;
+    long i;
+
+    for (n = 0; n < n_shift; n++) {
+        phi[n] = CX(phi_all) + (long)n * size;
+        p_s[n] = (cplx *)malloc(sizeof(cplx) * size);
+        mapping[n] = n;
+        shifts[n] = shifts_in[n];
+        beta_s[n] = zeta_s[n] = zeta_s_prev[n] = 1.0;
+        alpha_s[n] = 0.0;
+    }
+    beta = 1.0;
+    alpha = 0.0;
+    bsqrt = sqrt(cnorm2(phi0, size));
+    for (n = 0; n < n_shift; n++) {
+        memcpy(p_s[n], phi0, sizeof(cplx) * size);
+        memset(phi[n], 0, sizeof(cplx) * size);
+    }
+    memcpy(p, phi0, sizeof(cplx) * size);
+    memcpy(r, phi0, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    rsq = cnorm2(r, size);
+
+    for (k = 0; k < max_iter; k++) {
+        beta_prev = beta;
+        beta = rdivc(-rsq, cdot(p, Ap, size));
+        for (n = 0; n < n_shift_rem; n++) {
+            tmp = zeta_s[n];
+            zeta_s[n] = (zeta_s[n] * zeta_s_prev[n] * beta_prev) /
+                        (beta * alpha * (zeta_s_prev[n] - zeta_s[n]) +
+                         zeta_s_prev[n] * beta_prev * (mk(1.0, 0.0) - shifts[n] * beta));
+            zeta_s_prev[n] = tmp;
+            beta_s[n] = beta * zeta_s[n] / zeta_s_prev[n];
+            for (i = 0; i < size; i++) phi[n][i] = phi[n][i] - beta_s[n] * p_s[n][i];
+        }
+        for (i = 0; i < size; i++) r[i] = r[i] + beta * Ap[i];
+        rsqNew = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsqNew) / bsqrt);
+
+        if (k % resid_freq_check == 0) {
+            for (n = 0; n < n_shift_rem; n++) {
+                if (cabs(zeta_s[n]) * sqrt(rsqNew) < eps * bsqrt) {
+                    n_shift_rem--;
+                    if (n_shift_rem != n) {
+                        int ti = mapping[n_shift_rem]; mapping[n_shift_rem] = mapping[n]; mapping[n] = ti;
+                        cplx *tp = phi[n_shift_rem]; phi[n_shift_rem] = phi[n]; phi[n] = tp;
+                        tp = p_s[n_shift_rem]; p_s[n_shift_rem] = p_s[n]; p_s[n] = tp;
+                        cplx tc;
+                        tc = alpha_s[n_shift_rem]; alpha_s[n_shift_rem] = alpha_s[n]; alpha_s[n] = tc;
+                        tc = beta_s[n_shift_rem]; beta_s[n_shift_rem] = beta_s[n]; beta_s[n] = tc;
+                        tc = zeta_s[n_shift_rem]; zeta_s[n_shift_rem] = zeta_s[n]; zeta_s[n] = tc;
+                        tc = zeta_s_prev[n_shift_rem]; zeta_s_prev[n_shift_rem] = zeta_s_prev[n]; zeta_s_prev[n] = tc;
+                        double td = shifts[n_shift_rem]; shifts[n_shift_rem] = shifts[n]; shifts[n] = td;
+                        n--;
+                    }
+                }
+            }
+        }
+        if ((worst_first && cabs(zeta_s[0]) * sqrt(rsqNew) < eps * bsqrt) || n_shift_rem == 0 ||
+            k == max_iter - 1)
+            break;
+
+        alpha = mk(rsqNew / rsq, 0.0);
+        rsq = rsqNew;
+        for (n = 0; n < n_shift_rem; n++) {
+            alpha_s[n] = alpha * zeta_s[n] * beta_s[n] / (zeta_s_prev[n] * beta);
+            for (i = 0; i < size; i++) p_s[n][i] = zeta_s[n] * r[i] + alpha_s[n] * p_s[n][i];
+        }
+        for (i = 0; i < size; i++) p[i] = r[i] + alpha * p[i];
+        orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    k++;
+
+    /* undo the permutation (generic_cg_m.cpp:533-558) */
+    for (n = 0; n < n_shift; n++) {
+        if (mapping[n] != n) {
+            for (int m = n + 1; m < n_shift; m++) {
+                if (mapping[m] == n) {
+                    cplx *tp = phi[m]; phi[m] = phi[n]; phi[n] = tp;
+                    double td = shifts[m]; shifts[m] = shifts[n]; shifts[n] = td;
+                    mapping[m] = mapping[n];
+                    mapping[n] = n;
+                    n--;
+                    break;
+                }
+            }
+        }
+    }
+    /* explicit residuals of every shifted system (generic_cg_m.cpp:561-572) */
+    for (n = 0; n < n_shift; n++) {
+        memset(Ap, 0, sizeof(cplx) * size);
+        orc_apply(op, (double *)Ap, (const double *)phi[n]); ops++;
+        for (i = 0; i < size; i++) Ap[i] = Ap[i] + (shifts[n] * phi[n][i]);
+        if (resSqmrhs) resSqmrhs[n] = cdiffnorm2(Ap, phi0, size);
+    }
+    for (n = 0; n < n_shift; n++) free(p_s[n]);
+    free(p_s); free(phi); free(alpha_s); free(beta_s); free(zeta_s); free(zeta_s_prev);
+    free(shifts); free(mapping); free(r); free(p); free(Ap);
+    info->resSq = 0.0; /* the reference leaves resSq at its initial 0 (generic_cg_m.cpp:596) */
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "CG-M");
+}
+
+/* ---------------------------------------------------------------- force */
+
+/* dS/dtheta_mu(s) for S = phi^dagger (D^dagger D + sigma)^-1 phi.  With X the solution and
+ * Y = D X, dS/dtheta = -2 Re(Y^dagger dD X).  The link U_x(s) enters D at row s as
+ * -1/2 U psi(s+x) and at row s+x as +1/2 U^* psi(s) (operators.cpp:215-218); for U_y the
+ * same with eta(s) = (-1)^x (operators.cpp:221-224).  dU/dtheta = iU, so
+ * dS/dtheta_x(s) = -Im( Y(s)^* U X(s+x) + Y(s+x)^* U^* X(s) ), and eta(s) times the same
+ * for y. */
+void orc_staggered_force(const double *links, double mass, int lx, int ly, const double *X_,
+                         const double *Y_, double *out)
+{
+    (void)mass;
+    const cplx *U = CCX(links), *X = CCX(X_), *Y = CCX(Y_);
+    for (long i = 0; i < (long)lx * ly; i++) {
+        int x = (int)(i % lx), y = (int)(i / lx);
+        long ixp = (long)y * lx + (x + 1) % lx;
+        long iyp = (long)((y + 1) % ly) * lx + x;
+        double eta1 = (double)(1 - 2 * (x % 2));
+        cplx ux = U[2 * i], uy = U[2 * i + 1];
+        cplx fx = conj(Y[i]) * ux * X[ixp] + conj(Y[ixp]) * conj(ux) * X[i];
+        cplx fy = conj(Y[i]) * uy * X[iyp] + conj(Y[iyp]) * conj(uy) * X[i];
+        out[2 * i] = -cimag(fx);
+        out[2 * i + 1] = -eta1 * cimag(fy);
+    }
+}

@@ -1,0 +1,98 @@
+/*
+ * oracle.h -- CPU oracle for the 2D U(1) lattice hot path (TEST INFRASTRUCTURE ONLY).
+ *
+ * This is a plain-C99 restatement of generic-linalg's CPU algorithms for the operators
+ * (staggered D, D^dagger, D^dagger D, gauge Laplacian, stencil_2d apply/eo/oe and the
+ * staggered stencil builders) and the Krylov solvers that call them (CG, restarted CG,
+ * multishift CG, BiCGstab, restarted BiCGstab, GCR, restarted GCR).  Every function cites
+ * the reference file:line it follows.  It exists so that tests, the smoke check and the
+ * CPU-baseline leg of the benchmark have something to compare the CUDA path against.
+ * The product (the CUDA library and its C-ABI) never links, loads or calls it.
+ *
+ * Parity pin: tests/golden/ holds outputs of the reference itself (compiled from its own
+ * sources by oracle/Makefile into oracle/_ref/), and tests/test_oracle_golden.py checks
+ * this oracle against them.
+ *
+ * Data layout (identical to the reference): a field is V = lx*ly complex<double> values,
+ * site i = y*lx + x, stored as interleaved (re, im) doubles.  Links are U[2*i + mu],
+ * mu = 0 for +x and mu = 1 for +y.  stencil_2d arrays use the reference's layout:
+ * clover[c + nc*i], hopping[c + nc*i + dir*nc*V*nc], two_link[c + nc*i + dir*nc*V*nc]
+ * with i = site*nc + row.
+ */
+#ifndef GLINALG_ORACLE_H
+#define GLINALG_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum orc_kind {
+    ORC_STAGGERED = 0,        /* square_staggered_u1 */
+    ORC_STAGGERED_DAGGER = 1, /* square_staggered_dagger_u1 */
+    ORC_STAGGERED_NORMAL = 2, /* square_staggered_normal_u1 */
+    ORC_LAPLACE = 3,          /* square_laplace_u1 */
+    ORC_STENCIL = 4,          /* apply_stencil_2d (DIR_ALL) */
+    ORC_STENCIL_EO = 5,       /* apply_stencil_2d_eo */
+    ORC_STENCIL_OE = 6        /* apply_stencil_2d_oe */
+};
+
+typedef struct {
+    int kind;
+    int lx, ly, nc;
+    double mass;
+    const double *links;      /* 2*lx*ly complex */
+    const double *clover;     /* lx*ly*nc*nc complex */
+    const double *hopping;    /* 4*lx*ly*nc*nc complex */
+    const double *two_link;   /* 8*lx*ly*nc*nc complex or NULL */
+    double shift[2], eo_shift[2], dof_shift[2];
+} orc_op;
+
+typedef struct {
+    double resSq;
+    int iter;
+    int success;
+    int ops_count;
+    char name[32];
+} orc_info;
+
+/* Operators: lhs is overwritten, rhs is read. */
+void orc_apply(const orc_op *op, double *lhs, const double *rhs);
+long orc_op_size(const orc_op *op); /* number of complex entries of a field */
+
+/* Stencil builders (fill hopping[4*V], clover untouched, shift = mass). */
+void orc_staggered_stencil(double *hopping, const double *links, int lx, int ly, int dagger);
+
+/* BLAS-1 helpers (generic_vector.h). */
+void orc_dot(const double *a, const double *b, long n, double out[2]);
+double orc_norm2sq(const double *a, long n);
+double orc_diffnorm2sq(const double *a, const double *b, long n);
+
+/* Solvers.  hist (optional, may be NULL) receives the relative residual printed at each
+ * iteration by the reference's DETAIL verbosity, hist_cap entries at most. */
+void orc_cg(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+            double eps, orc_info *info, double *hist, int hist_cap);
+void orc_cg_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                    double eps, int restart_freq, orc_info *info);
+void orc_bicgstab(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                  double eps, orc_info *info, double *hist, int hist_cap);
+void orc_bicgstab_restart(const orc_op *op, double *phi, const double *phi0, long size,
+                          int max_iter, double eps, int restart_freq, orc_info *info);
+void orc_gcr(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+             double eps, orc_info *info, double *hist, int hist_cap);
+void orc_gcr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                     double eps, int restart_freq, orc_info *info);
+/* phi: n_shift solution vectors laid out back to back (n_shift*size complex). */
+void orc_cg_m(const orc_op *op, double *phi, const double *phi0, int n_shift, long size,
+              int resid_freq_check, int max_iter, double eps, const double *shifts,
+              int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap);
+
+/* Adjoint force for S = phi^dagger (D^dagger D + sigma)^-1 phi with respect to the link
+ * angles theta_mu(x) (U = exp(i theta)), given X = (D^dagger D + sigma)^-1 phi and Y = D X:
+ * dS/dtheta_mu(x) = -2 Re( Y^dagger (dD/dtheta_mu(x)) X ).  out has 2*lx*ly reals. */
+void orc_staggered_force(const double *links, double mass, int lx, int ly, const double *X,
+                         const double *Y, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,262 @@
+"""ctypes bindings for the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+``Oracle`` wraps oracle/_build/liboracle.so, the C99 restatement of the reference's
+operators and solvers (oracle.c).  ``RefOracle`` wraps oracle/_ref/libref_oracle.so, the
+reference's own sources compiled by ``make -C oracle ref``; it exists only where the
+reference checkout is present and is used to pin the restatement and to write the golden
+fixtures.  Only tests, the smoke check and the CPU-baseline leg of bench.py import this
+module; the product never does.
+
+Fields are numpy complex128 arrays (site i = y*lx + x); links are complex128 of length
+2*lx*ly with U[2*i + mu].
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_oracle.so")
+
+KIND = {
+    "staggered": 0,
+    "staggered_dagger": 1,
+    "staggered_normal": 2,
+    "laplace": 3,
+    "stencil": 4,
+    "stencil_eo": 5,
+    "stencil_oe": 6,
+}
+
+_dp = C.POINTER(C.c_double)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_dp)
+
+
+class OrcOp(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("lx", C.c_int), ("ly", C.c_int), ("nc", C.c_int),
+        ("mass", C.c_double),
+        ("links", _dp), ("clover", _dp), ("hopping", _dp), ("two_link", _dp),
+        ("shift", C.c_double * 2), ("eo_shift", C.c_double * 2), ("dof_shift", C.c_double * 2),
+    ]
+
+
+class OrcInfo(C.Structure):
+    _fields_ = [("resSq", C.c_double), ("iter", C.c_int), ("success", C.c_int),
+                ("ops_count", C.c_int), ("name", C.c_char * 32)]
+
+    def as_dict(self):
+        return {"resSq": self.resSq, "iter": self.iter, "success": bool(self.success),
+                "ops_count": self.ops_count, "name": self.name.decode()}
+
+
+def build(quiet=True):
+    """Compile liboracle.so (and libref_oracle.so when the reference checkout exists)."""
+    out = subprocess.DEVNULL if quiet else None
+    subprocess.check_call(["make", "-s", "-C", HERE], stdout=out)
+    ref = os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
+    if os.path.isdir(ref):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], stdout=out)
+
+
+class Operator:
+    """Keeps the numpy arrays of one operator alive for the OrcOp that points at them."""
+
+    def __init__(self, kind, lx, ly, mass=0.0, links=None, nc=1, clover=None, hopping=None,
+                 two_link=None, shift=0j, eo_shift=0j, dof_shift=0j):
+        self.kind = KIND[kind] if isinstance(kind, str) else int(kind)
+        self.lx, self.ly, self.nc, self.mass = int(lx), int(ly), int(nc), float(mass)
+        c = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.complex128)
+        self.links, self.clover, self.hopping, self.two_link = c(links), c(clover), c(hopping), c(two_link)
+        self.shift, self.eo_shift, self.dof_shift = complex(shift), complex(eo_shift), complex(dof_shift)
+        s = OrcOp()
+        s.kind, s.lx, s.ly, s.nc, s.mass = self.kind, self.lx, self.ly, self.nc, self.mass
+        s.links, s.clover = _ptr(self.links), _ptr(self.clover)
+        s.hopping, s.two_link = _ptr(self.hopping), _ptr(self.two_link)
+        for name in ("shift", "eo_shift", "dof_shift"):
+            z = getattr(self, name)
+            getattr(s, name)[0], getattr(s, name)[1] = z.real, z.imag
+        self.struct = s
+
+    @property
+    def size(self):
+        v = self.lx * self.ly
+        return v * self.nc if self.kind >= KIND["stencil"] else v
+
+    def shifts6(self):
+        return np.array([self.shift.real, self.shift.imag, self.eo_shift.real,
+                         self.eo_shift.imag, self.dof_shift.real, self.dof_shift.imag])
+
+
+class Oracle:
+    def __init__(self, path=LIB_PATH):
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        self.lib = L
+        P = C.POINTER
+        L.orc_apply.argtypes = [P(OrcOp), _dp, _dp]
+        L.orc_staggered_stencil.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_int]
+        L.orc_dot.argtypes = [_dp, _dp, C.c_long, _dp]
+        L.orc_norm2sq.argtypes = [_dp, C.c_long]
+        L.orc_norm2sq.restype = C.c_double
+        L.orc_diffnorm2sq.argtypes = [_dp, _dp, C.c_long]
+        L.orc_diffnorm2sq.restype = C.c_double
+        solver_args = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, P(OrcInfo), _dp, C.c_int]
+        for n in ("orc_cg", "orc_bicgstab", "orc_gcr"):
+            getattr(L, n).argtypes = solver_args
+        for n in ("orc_cg_restart", "orc_bicgstab_restart", "orc_gcr_restart"):
+            getattr(L, n).argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int, P(OrcInfo)]
+        L.orc_cg_m.argtypes = [P(OrcOp), _dp, _dp, C.c_int, C.c_long, C.c_int, C.c_int, C.c_double,
+                               _dp, C.c_int, P(OrcInfo), _dp, _dp, C.c_int]
+        L.orc_staggered_force.argtypes = [_dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp]
+
+    def apply(self, op: Operator, rhs):
+        rhs = np.ascontiguousarray(rhs, dtype=np.complex128)
+        lhs = np.empty_like(rhs)
+        self.lib.orc_apply(C.byref(op.struct), _ptr(lhs), _ptr(rhs))
+        return lhs
+
+    def staggered_stencil(self, links, lx, ly, dagger=False):
+        links = np.ascontiguousarray(links, dtype=np.complex128)
+        hop = np.zeros(4 * lx * ly, dtype=np.complex128)
+        self.lib.orc_staggered_stencil(_ptr(hop), _ptr(links), lx, ly, int(dagger))
+        return hop
+
+    def dot(self, a, b):
+        out = np.zeros(2)
+        self.lib.orc_dot(_ptr(a), _ptr(b), a.size, _ptr(out))
+        return complex(out[0], out[1])
+
+    def norm2sq(self, a):
+        return self.lib.orc_norm2sq(_ptr(a), a.size)
+
+    def solve(self, solver, op: Operator, phi0, phi=None, max_iter=10000, eps=1e-10,
+              restart_freq=0, hist_cap=0):
+        """solver in {"cg", "bicgstab", "gcr"}; returns (phi, info dict, hist)."""
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        phi = np.zeros_like(phi0) if phi is None else np.array(phi, dtype=np.complex128)
+        info = OrcInfo()
+        hist = np.zeros(max(hist_cap, 1))
+        if restart_freq > 0:
+            getattr(self.lib, f"orc_{solver}_restart")(C.byref(op.struct), _ptr(phi), _ptr(phi0),
+                                                       phi0.size, max_iter, eps, restart_freq,
+                                                       C.byref(info))
+        else:
+            getattr(self.lib, f"orc_{solver}")(C.byref(op.struct), _ptr(phi), _ptr(phi0), phi0.size,
+                                               max_iter, eps, C.byref(info),
+                                               _ptr(hist) if hist_cap else None, hist_cap)
+        d = info.as_dict()
+        return phi, d, hist[: min(hist_cap, d["iter"])] if hist_cap else None
+
+    def cg_m(self, op: Operator, phi0, shifts, resid_freq_check=1, max_iter=10000, eps=1e-10,
+             worst_first=False, hist_cap=0):
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        shifts = np.ascontiguousarray(shifts, dtype=np.float64)
+        ns = shifts.size
+        phi = np.zeros((ns, phi0.size), dtype=np.complex128)
+        res = np.zeros(ns)
+        hist = np.zeros(max(hist_cap, 1))
+        info = OrcInfo()
+        self.lib.orc_cg_m(C.byref(op.struct), _ptr(phi), _ptr(phi0), ns, phi0.size,
+                          resid_freq_check, max_iter, eps, _ptr(shifts), int(worst_first),
+                          C.byref(info), _ptr(res), _ptr(hist) if hist_cap else None, hist_cap)
+        return phi, info.as_dict(), res
+
+    def staggered_force(self, links, mass, lx, ly, X, Y):
+        out = np.zeros(2 * lx * ly)
+        self.lib.orc_staggered_force(_ptr(np.ascontiguousarray(links)), mass, lx, ly,
+                                     _ptr(np.ascontiguousarray(X)), _ptr(np.ascontiguousarray(Y)),
+                                     _ptr(out))
+        return out
+
+
+class RefOracle:
+    """The reference's own code (compiled from its sources); available only where the
+    reference checkout exists."""
+
+    def __init__(self, path=REF_LIB_PATH):
+        L = C.CDLL(path)
+        self.lib = L
+        cp = C.c_char_p
+        L.ref_make_inputs.argtypes = [C.c_uint, C.c_int, C.c_int, _dp, _dp, C.c_int, C.c_long]
+        L.ref_gauss_gauge.argtypes = [C.c_uint, C.c_int, C.c_int, C.c_double, _dp]
+        L.ref_read_gauge.argtypes = [cp, C.c_int, C.c_int, _dp]
+        opargs = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _dp, _dp, _dp, _dp, _dp]
+        L.ref_apply.argtypes = opargs + [_dp, _dp]
+        L.ref_staggered_stencil.argtypes = [C.c_int, C.c_int, C.c_double, _dp, C.c_int, _dp, _dp]
+        L.ref_solve.argtypes = [C.c_int, C.c_int] + opargs + [_dp, _dp, C.c_int, C.c_double, C.c_int,
+                                                              cp, _dp, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
+        L.ref_cg_m.argtypes = opargs + [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int,
+                                        C.c_int, cp, _dp, _dp, C.c_char_p, C.c_int]
+
+    def make_inputs(self, seed, lx, ly, n_src=1, src_len=None):
+        links = np.zeros(2 * lx * ly, dtype=np.complex128)
+        src_len = lx * ly if src_len is None else src_len
+        src = np.zeros((n_src, src_len), dtype=np.complex128)
+        self.lib.ref_make_inputs(seed, lx, ly, _ptr(links), _ptr(src), n_src, src_len)
+        return links, src
+
+    def read_gauge(self, path, lx, ly):
+        links = np.zeros(2 * lx * ly, dtype=np.complex128)
+        self.lib.ref_read_gauge(path.encode(), lx, ly, _ptr(links))
+        return links
+
+    def _opargs(self, op: Operator):
+        return (op.kind, op.lx, op.ly, op.nc, op.mass, _ptr(op.links), _ptr(op.clover),
+                _ptr(op.hopping), _ptr(op.two_link), _ptr(op._s6))
+
+    def apply(self, op: Operator, rhs):
+        op._s6 = op.shifts6()
+        rhs = np.ascontiguousarray(rhs, dtype=np.complex128)
+        lhs = np.zeros_like(rhs)
+        self.lib.ref_apply(*self._opargs(op), _ptr(lhs), _ptr(rhs))
+        return lhs
+
+    def staggered_stencil(self, links, lx, ly, mass, dagger=False):
+        hop = np.zeros(4 * lx * ly, dtype=np.complex128)
+        sh = np.zeros(2)
+        self.lib.ref_staggered_stencil(lx, ly, mass, _ptr(np.ascontiguousarray(links)), int(dagger),
+                                       _ptr(hop), _ptr(sh))
+        return hop, complex(sh[0], sh[1])
+
+    def solve(self, solver, op: Operator, phi0, phi=None, max_iter=10000, eps=1e-10,
+              restart_freq=0, verbosity=0, prefix=""):
+        op._s6 = op.shifts6()
+        sid = {"cg": 0, "bicgstab": 1, "gcr": 2}[solver]
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        phi = np.zeros_like(phi0) if phi is None else np.array(phi, dtype=np.complex128)
+        info = np.zeros(4)
+        name = C.create_string_buffer(64)
+        log = C.create_string_buffer(1 << 20)
+        self.lib.ref_solve(sid, restart_freq, *self._opargs(op), _ptr(phi), _ptr(phi0), max_iter, eps,
+                           verbosity, prefix.encode(), _ptr(info), name, 64, log, 1 << 20)
+        d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]),
+             "ops_count": int(info[3]), "name": name.value.decode()}
+        return phi, d, log.value.decode()
+
+    def cg_m(self, op: Operator, phi0, shifts, resid_freq_check=1, max_iter=10000, eps=1e-10,
+             worst_first=False, verbosity=0, prefix=""):
+        op._s6 = op.shifts6()
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        shifts = np.array(shifts, dtype=np.float64)
+        ns = shifts.size
+        phi = np.zeros((ns, phi0.size), dtype=np.complex128)
+        info = np.zeros(4)
+        res = np.zeros(ns)
+        log = C.create_string_buffer(1 << 20)
+        self.lib.ref_cg_m(*self._opargs(op), _ptr(phi), _ptr(phi0), ns, resid_freq_check, max_iter,
+                          eps, _ptr(shifts), int(worst_first), verbosity, prefix.encode(), _ptr(info),
+                          _ptr(res), log, 1 << 20)
+        d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]),
+             "ops_count": int(info[3]), "name": "CG-M"}
+        return phi, d, res, log.value.decode()

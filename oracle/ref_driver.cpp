@@ -1,0 +1,244 @@
+// ref_driver.cpp -- extern "C" wrappers around the reference's own C++ code
+// (TEST INFRASTRUCTURE ONLY).
+//
+// oracle/Makefile compiles this file together with the reference's unmodified sources,
+// read in place from the reference checkout, into oracle/_ref/libref_oracle.so.  The
+// library is used in this container to pin the C oracle (oracle.c) and to write the golden
+// fixtures under tests/golden/.  Nothing in the product links it.
+//
+// Complex fields cross the boundary as interleaved (re, im) doubles, which is the memory
+// layout of std::complex<double> arrays.
+
+#include <complex>
+#include <cstring>
+#include <random>
+#include <sstream>
+#include <iostream>
+#include <string>
+
+#include "generic_vector.h"
+#include "inverter_struct.h"
+#include "verbosity.h"
+#include "generic_cg.h"
+#include "generic_cg_m.h"
+#include "generic_bicgstab.h"
+#include "generic_gcr.h"
+#include "lattice.h"
+#include "operators.h"
+#include "coarse_stencil.h"
+#include "operators_stencil.h"
+#include "u1_utils.h"
+
+using cd = std::complex<double>;
+typedef void (*mv_fn)(cd *, cd *, void *);
+
+namespace {
+
+// One operator as the reference sees it: a callback and its extra_info.
+struct RefOp {
+    int kind;
+    staggered_u1_op stag;
+    Lattice *lat = nullptr;
+    stencil_2d *st = nullptr;
+    mv_fn fn = nullptr;
+    void *extra = nullptr;
+    long size = 0;
+    ~RefOp()
+    {
+        delete st;
+        delete lat;
+    }
+};
+
+// kind: 0 D, 1 D^dagger, 2 D^dagger D, 3 gauge Laplacian, 4 stencil, 5 stencil_eo,
+// 6 stencil_oe (same numbering as oracle.h).
+RefOp *make_op(int kind, int lx, int ly, int nc, double mass, const double *links,
+               const double *clover, const double *hopping, const double *two_link,
+               const double *shifts6)
+{
+    RefOp *o = new RefOp();
+    o->kind = kind;
+    o->stag.lattice = (cd *)links;
+    o->stag.mass = mass;
+    o->stag.x_fine = lx;
+    o->stag.y_fine = ly;
+    o->stag.Nc = 1;
+    o->stag.wilson_coeff = 0.0;
+    o->size = (long)lx * ly;
+    switch (kind) {
+    case 0: o->fn = square_staggered_u1; break;
+    case 1: o->fn = square_staggered_dagger_u1; break;
+    case 2: o->fn = square_staggered_normal_u1; break;
+    case 3: o->fn = square_laplace_u1; break;
+    default: {
+        int dims[2] = {lx, ly};
+        o->lat = new Lattice(2, dims, nc);
+        o->st = new stencil_2d(o->lat, two_link ? 2 : 1);
+        long v = (long)lx * ly * nc * nc;
+        std::memcpy(o->st->clover, clover, sizeof(cd) * v);
+        std::memcpy(o->st->hopping, hopping, sizeof(cd) * v * 4);
+        if (two_link) std::memcpy(o->st->two_link, two_link, sizeof(cd) * v * 8);
+        if (shifts6) {
+            o->st->shift = cd(shifts6[0], shifts6[1]);
+            o->st->eo_shift = cd(shifts6[2], shifts6[3]);
+            o->st->dof_shift = cd(shifts6[4], shifts6[5]);
+        }
+        o->st->generated = true;
+        o->fn = kind == 4 ? apply_stencil_2d : (kind == 5 ? apply_stencil_2d_eo : apply_stencil_2d_oe);
+        o->size = (long)lx * ly * nc;
+        break;
+    }
+    }
+    o->extra = o->st ? (void *)o->st : (void *)&o->stag;
+    return o;
+}
+
+void fill_info(const inversion_info &inv, double *out4, char *name, int name_cap)
+{
+    out4[0] = inv.resSq;
+    out4[1] = inv.iter;
+    out4[2] = inv.success ? 1.0 : 0.0;
+    out4[3] = inv.ops_count;
+    if (name && name_cap > 0) {
+        std::strncpy(name, inv.name.c_str(), name_cap - 1);
+        name[name_cap - 1] = 0;
+    }
+}
+
+// Runs fn with std::cout redirected into log (if given), so the verbosity lines the
+// reference prints can be stored as fixtures.
+template <typename F>
+void with_log(char *log, int log_cap, F fn)
+{
+    std::ostringstream ss;
+    std::streambuf *old = nullptr;
+    if (log) old = std::cout.rdbuf(ss.rdbuf());
+    fn();
+    if (log) {
+        std::cout.rdbuf(old);
+        std::string s = ss.str();
+        std::strncpy(log, s.c_str(), log_cap - 1);
+        log[log_cap - 1] = 0;
+    }
+}
+
+inversion_verbose_struct make_verb(int level, const char *prefix)
+{
+    inversion_verbose_struct v;
+    v.verbosity = (inversion_verbose_level)level;
+    v.verb_prefix = prefix ? prefix : "";
+    v.precond_verbosity = VERB_NONE;
+    v.precond_verb_prefix = "";
+    return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Inputs the way the reference's tests make them: one std::mt19937(seed), then
+// rand_gauge_u1 (u1_utils.cpp:79-87), then n_src gaussian vectors (generic_vector.h:48-60).
+void ref_make_inputs(unsigned seed, int lx, int ly, double *links, double *src, int n_src,
+                     long src_len)
+{
+    std::mt19937 gen(seed);
+    if (links) rand_gauge_u1((cd *)links, lx, ly, gen);
+    for (int n = 0; n < n_src; n++) gaussian<double>((cd *)src + (long)n * src_len, (int)src_len, gen);
+}
+
+void ref_gauss_gauge(unsigned seed, int lx, int ly, double beta, double *links)
+{
+    std::mt19937 gen(seed);
+    gauss_gauge_u1((cd *)links, lx, ly, gen, beta);
+}
+
+void ref_read_gauge(const char *path, int lx, int ly, double *links)
+{
+    read_gauge_u1((cd *)links, lx, ly, std::string(path));
+}
+
+void ref_apply(int kind, int lx, int ly, int nc, double mass, const double *links,
+               const double *clover, const double *hopping, const double *two_link,
+               const double *shifts6, double *lhs, const double *rhs)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> in((const cd *)rhs, (const cd *)rhs + o->size);
+    o->fn((cd *)lhs, in.data(), o->extra);
+    delete o;
+}
+
+void ref_staggered_stencil(int lx, int ly, double mass, const double *links, int dagger,
+                           double *hopping_out, double *shift_out)
+{
+    int dims[2] = {lx, ly};
+    Lattice lat(2, dims, 1);
+    stencil_2d st(&lat, 1);
+    staggered_u1_op s;
+    s.lattice = (cd *)links;
+    s.mass = mass;
+    s.x_fine = lx;
+    s.y_fine = ly;
+    s.Nc = 1;
+    s.wilson_coeff = 0.0;
+    if (dagger) get_square_staggered_dagger_u1_stencil(&st, &s);
+    else get_square_staggered_u1_stencil(&st, &s);
+    std::memcpy(hopping_out, st.hopping, sizeof(cd) * (long)lx * ly * 4);
+    shift_out[0] = st.shift.real();
+    shift_out[1] = st.shift.imag();
+}
+
+// solver: 0 CG, 1 BiCGstab, 2 GCR; restart_freq > 0 selects the restarted variant.
+void ref_solve(int solver, int restart_freq, int kind, int lx, int ly, int nc, double mass,
+               const double *links, const double *clover, const double *hopping,
+               const double *two_link, const double *shifts6, double *phi, const double *phi0,
+               int max_iter, double eps, int verbosity, const char *prefix, double *info4,
+               char *name, int name_cap, char *log, int log_cap)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> b((const cd *)phi0, (const cd *)phi0 + o->size);
+    inversion_verbose_struct verb = make_verb(verbosity, prefix);
+    inversion_info inv;
+    with_log(log, log_cap, [&]() {
+        cd *x = (cd *)phi;
+        int sz = (int)o->size;
+        if (solver == 0)
+            inv = restart_freq > 0
+                      ? minv_vector_cg_restart(x, b.data(), sz, max_iter, eps, restart_freq, o->fn, o->extra, &verb)
+                      : minv_vector_cg(x, b.data(), sz, max_iter, eps, o->fn, o->extra, &verb);
+        else if (solver == 1)
+            inv = restart_freq > 0
+                      ? minv_vector_bicgstab_restart(x, b.data(), sz, max_iter, eps, restart_freq, o->fn, o->extra, &verb)
+                      : minv_vector_bicgstab(x, b.data(), sz, max_iter, eps, o->fn, o->extra, &verb);
+        else
+            inv = restart_freq > 0
+                      ? minv_vector_gcr_restart(x, b.data(), sz, max_iter, eps, restart_freq, o->fn, o->extra, &verb)
+                      : minv_vector_gcr(x, b.data(), sz, max_iter, eps, o->fn, o->extra, &verb);
+    });
+    fill_info(inv, info4, name, name_cap);
+    delete o;
+}
+
+// Multishift CG (generic_cg_m.cpp:312).  phi holds n_shift vectors back to back.
+void ref_cg_m(int kind, int lx, int ly, int nc, double mass, const double *links,
+              const double *clover, const double *hopping, const double *two_link,
+              const double *shifts6, double *phi, const double *phi0, int n_shift,
+              int resid_freq_check, int max_iter, double eps, double *shifts, int worst_first,
+              int verbosity, const char *prefix, double *info4, double *resSqmrhs, char *log,
+              int log_cap)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> b((const cd *)phi0, (const cd *)phi0 + o->size);
+    std::vector<cd *> ptrs(n_shift);
+    for (int n = 0; n < n_shift; n++) ptrs[n] = (cd *)phi + (long)n * o->size;
+    inversion_verbose_struct verb = make_verb(verbosity, prefix);
+    inversion_info inv;
+    with_log(log, log_cap, [&]() {
+        inv = minv_vector_cg_m(ptrs.data(), b.data(), n_shift, (int)o->size, resid_freq_check,
+                               max_iter, eps, shifts, o->fn, o->extra, worst_first != 0, &verb);
+    });
+    fill_info(inv, info4, nullptr, 0);
+    for (int n = 0; n < n_shift; n++) resSqmrhs[n] = inv.resSqmrhs[n];
+    delete o;
+}
+
+}  // extern "C"

@@ -1,0 +1,125 @@
+"""Writes the golden fixtures in this directory from the reference's own code.
+
+The reference's operators, stencil builders, solvers and input generators are compiled from
+the reference checkout (``make -C oracle ref``, sources read in place) into
+oracle/_ref/libref_oracle.so; this script calls them through ctypes on seeded inputs and
+stores inputs, outputs, solver infos and verbosity logs:
+
+  reference_vectors.npz   complex128 fields (inputs and outputs)
+  reference_info.json     solver infos, verbosity logs, parameters
+
+Run from the repository root:  python tests/golden/make_golden.py
+(requires the reference checkout; GLINALG_REFERENCE_DIR overrides its location).
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import pyoracle  # noqa: E402
+
+
+def main():
+    pyoracle.build()
+    R = pyoracle.RefOracle()
+    Op = pyoracle.Operator
+    vec = {}
+    info = {"cases": {}}
+
+    # ---- inputs: std::mt19937(seed) -> rand_gauge_u1 -> gaussian source(s)
+    lat = {"l32": (32, 32, 1337), "l8": (8, 8, 7), "l12x6": (12, 6, 3)}
+    for key, (lx, ly, seed) in lat.items():
+        links, src = R.make_inputs(seed, lx, ly, 2)
+        vec[f"{key}_links"], vec[f"{key}_src"], vec[f"{key}_src2"] = links, src[0], src[1]
+        info["cases"][key] = {"lx": lx, "ly": ly, "seed": seed}
+    # gauss_gauge_u1 with beta = 6 (a smooth field), seed 11, 16x16
+    vec["g16_links"] = np.zeros(2 * 256, np.complex128)
+    R.lib.ref_gauss_gauge(11, 16, 16, 6.0, vec["g16_links"].ctypes.data_as(pyoracle._dp))
+    info["cases"]["g16"] = {"lx": 16, "ly": 16, "seed": 11, "beta": 6.0}
+
+    # ---- operators (operators.cpp)
+    for key in ("l32", "l8", "l12x6"):
+        lx, ly, _ = lat[key]
+        U, b = vec[f"{key}_links"], vec[f"{key}_src"]
+        for kind in ("staggered", "staggered_dagger", "staggered_normal"):
+            vec[f"{key}_{kind}"] = R.apply(Op(kind, lx, ly, 0.1, U), b)
+        vec[f"{key}_laplace"] = R.apply(Op("laplace", lx, ly, 0.01, U), b)
+        # stencil builders (operators_stencil.cpp) and the stencil applied to the source
+        for dag in (0, 1):
+            hop, sh = R.staggered_stencil(U, lx, ly, 0.1, bool(dag))
+            vec[f"{key}_stencil_hop{dag}"] = hop
+            vec[f"{key}_stencil_apply{dag}"] = R.apply(
+                Op("stencil", lx, ly, nc=1, clover=np.zeros(lx * ly, np.complex128), hopping=hop, shift=sh), b)
+
+    # ---- generic stencil, Nc = 3, with and without two-link terms, all three parities
+    rng = np.random.default_rng(2024)
+    lx, ly, nc = 6, 4, 3
+    v = lx * ly * nc * nc
+    cl = rng.normal(size=v) + 1j * rng.normal(size=v)
+    hp = rng.normal(size=4 * v) + 1j * rng.normal(size=4 * v)
+    tl = rng.normal(size=8 * v) + 1j * rng.normal(size=8 * v)
+    x = rng.normal(size=lx * ly * nc) + 1j * rng.normal(size=lx * ly * nc)
+    vec.update({"st3_clover": cl, "st3_hopping": hp, "st3_two": tl, "st3_x": x})
+    shifts = {"shift": 0.3 + 0.1j, "eo_shift": 0.2 - 0.05j, "dof_shift": -0.4j}
+    info["cases"]["st3"] = {"lx": lx, "ly": ly, "nc": nc, **{k: [z.real, z.imag] for k, z in shifts.items()}}
+    for kind in ("stencil", "stencil_eo", "stencil_oe"):
+        for two in (0, 1):
+            o = Op(kind, lx, ly, nc=nc, clover=cl, hopping=hp, two_link=tl if two else None, **shifts)
+            vec[f"st3_{kind}_two{two}"] = R.apply(o, x)
+
+    # ---- solvers on the 32x32 system (BASELINE configuration 1: m = 0.1, tol 1e-10)
+    lx, ly = 32, 32
+    U, b = vec["l32_links"], vec["l32_src"]
+    normal = Op("staggered_normal", lx, ly, 0.1, U)
+    stag = Op("staggered", lx, ly, 0.1, U)
+    solves = [
+        ("cg", normal, 0), ("cg", normal, 17), ("bicgstab", stag, 0), ("bicgstab", stag, 17),
+        ("gcr", stag, 0), ("gcr", stag, 17),
+    ]
+    for solver, op, rf in solves:
+        x0 = np.zeros_like(b)
+        xs, d, log = R.solve(solver, op, b, phi=x0, max_iter=10000, eps=1e-10, restart_freq=rf,
+                             verbosity=1 if rf == 0 else 2, prefix="[GOLD] ")
+        key = f"l32_{solver}" + (f"_r{rf}" if rf else "")
+        vec[key] = xs
+        info["cases"][key] = {**{k: (bool(v_) if isinstance(v_, (bool, np.bool_)) else v_) for k, v_ in d.items()},
+                              "log": log, "restart_freq": rf, "max_iter": 10000, "eps": 1e-10,
+                              "op": "staggered_normal" if op is normal else "staggered"}
+    # detail-level log and a max_iter cut for CG (success == false path)
+    _, d, log = R.solve("cg", normal, b, max_iter=7, eps=1e-10, verbosity=3, prefix="[CG] ")
+    info["cases"]["l32_cg_maxiter7"] = {**d, "log": log}
+    _, d, log = R.solve("bicgstab", stag, b, max_iter=5, eps=1e-10, verbosity=3, prefix="")
+    info["cases"]["l32_bicgstab_maxiter5"] = {**d, "log": log}
+    _, d, log = R.solve("gcr", stag, b, max_iter=5, eps=1e-10, verbosity=3, prefix="")
+    info["cases"]["l32_gcr_maxiter5"] = {**d, "log": log}
+    # initial guess honoured: CG started from src2
+    xs, d, _ = R.solve("cg", normal, b, phi=vec["l32_src2"], max_iter=10000, eps=1e-10)
+    vec["l32_cg_guess"] = xs
+    info["cases"]["l32_cg_guess"] = d
+
+    # ---- multishift CG on the gauge Laplacian (tests/multishift/multishift.cpp:424-494 style)
+    lap = Op("laplace", lx, ly, 0.001, U)
+    msh = [0.0, 0.004, 0.009, 0.049, 0.099, 0.499, 0.999]
+    for rfc, wf in ((1, False), (3, False), (1, True)):
+        xs, d, res, log = R.cg_m(lap, b, msh, resid_freq_check=rfc, max_iter=10000, eps=1e-10,
+                                 worst_first=wf, verbosity=1, prefix="[CGM] ")
+        key = f"l32_cgm_rfc{rfc}_wf{int(wf)}"
+        vec[key] = xs.reshape(-1)
+        info["cases"][key] = {**d, "resSqmrhs": res.tolist(), "log": log, "shifts": msh,
+                              "rfc": rfc, "worst_first": wf, "mass": 0.001}
+
+    np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
+    with open(os.path.join(HERE, "reference_info.json"), "w") as f:
+        json.dump(info, f, indent=1, default=lambda o: o.item() if hasattr(o, "item") else str(o))
+    print("wrote", len(vec), "vectors")
+
+
+if __name__ == "__main__":
+    main()

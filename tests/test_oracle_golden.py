@@ -1,0 +1,103 @@
+"""The CPU oracle (oracle/oracle.c) against the reference's own outputs (tests/golden/,
+written by make_golden.py from the reference compiled from its sources).  Bit-exact: the
+oracle keeps the reference's operation order and complex arithmetic."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from pyoracle import Operator
+
+LATS = {"l32": (32, 32), "l8": (8, 8), "l12x6": (12, 6)}
+
+
+@pytest.mark.parametrize("key", list(LATS))
+@pytest.mark.parametrize("kind", ["staggered", "staggered_dagger", "staggered_normal", "laplace"])
+def test_operators_bit_exact(oracle, golden, key, kind):
+    vec, _ = golden
+    lx, ly = LATS[key]
+    mass = 0.01 if kind == "laplace" else 0.1
+    out = oracle.apply(Operator(kind, lx, ly, mass, vec[f"{key}_links"]), vec[f"{key}_src"])
+    assert np.array_equal(out, vec[f"{key}_{kind}"])
+
+
+@pytest.mark.parametrize("key", list(LATS))
+@pytest.mark.parametrize("dagger", [0, 1])
+def test_stencil_builder_bit_exact(oracle, golden, key, dagger):
+    vec, _ = golden
+    lx, ly = LATS[key]
+    hop = oracle.staggered_stencil(vec[f"{key}_links"], lx, ly, dagger=bool(dagger))
+    assert np.array_equal(hop, vec[f"{key}_stencil_hop{dagger}"])
+    op = Operator("stencil", lx, ly, nc=1, clover=np.zeros(lx * ly, np.complex128), hopping=hop, shift=0.1)
+    assert np.array_equal(oracle.apply(op, vec[f"{key}_src"]), vec[f"{key}_stencil_apply{dagger}"])
+
+
+def test_stencil_equals_function(golden):
+    """tests/staggered_stencil/staggered_stencil.cpp:212-251: stencil form == function form."""
+    vec, _ = golden
+    for key in LATS:
+        assert np.abs(vec[f"{key}_stencil_apply0"] - vec[f"{key}_staggered"]).max() < 1e-15
+        assert np.abs(vec[f"{key}_stencil_apply1"] - vec[f"{key}_staggered_dagger"]).max() < 1e-15
+
+
+@pytest.mark.parametrize("kind", ["stencil", "stencil_eo", "stencil_oe"])
+@pytest.mark.parametrize("two", [0, 1])
+def test_generic_stencil_bit_exact(oracle, golden, kind, two):
+    vec, cases = golden
+    c = cases["st3"]
+    op = Operator(kind, c["lx"], c["ly"], nc=c["nc"], clover=vec["st3_clover"], hopping=vec["st3_hopping"],
+                  two_link=vec["st3_two"] if two else None, shift=complex(*c["shift"]),
+                  eo_shift=complex(*c["eo_shift"]), dof_shift=complex(*c["dof_shift"]))
+    assert np.array_equal(oracle.apply(op, vec["st3_x"]), vec[f"st3_{kind}_two{two}"])
+
+
+SOLVES = [("cg", 0), ("cg", 17), ("bicgstab", 0), ("bicgstab", 17), ("gcr", 0), ("gcr", 17)]
+
+
+@pytest.mark.parametrize("solver,rf", SOLVES)
+def test_solvers_bit_exact(oracle, golden, solver, rf):
+    vec, cases = golden
+    key = f"l32_{solver}" + (f"_r{rf}" if rf else "")
+    c = cases[key]
+    op = Operator(c["op"], 32, 32, 0.1, vec["l32_links"])
+    x, info, _ = oracle.solve(solver, op, vec["l32_src"], max_iter=c["max_iter"], eps=c["eps"], restart_freq=rf)
+    for f in ("iter", "ops_count", "success", "name"):
+        assert info[f] == c[f], f
+    assert info["resSq"] == c["resSq"]
+    assert np.array_equal(x, vec[key])
+
+
+def test_cg_initial_guess(oracle, golden):
+    vec, cases = golden
+    op = Operator("staggered_normal", 32, 32, 0.1, vec["l32_links"])
+    x, info, _ = oracle.solve("cg", op, vec["l32_src"], phi=vec["l32_src2"])
+    assert info["iter"] == cases["l32_cg_guess"]["iter"]
+    assert np.array_equal(x, vec["l32_cg_guess"])
+
+
+@pytest.mark.parametrize("key,max_iter", [("l32_cg_maxiter7", 7), ("l32_bicgstab_maxiter5", 5), ("l32_gcr_maxiter5", 5)])
+def test_max_iter_failure_path(oracle, golden, key, max_iter):
+    """success == false when the loop reaches max_iter - 1 (generic_cg.cpp:356-363)."""
+    vec, cases = golden
+    solver = key.split("_")[1]
+    kind = "staggered_normal" if solver == "cg" else "staggered"
+    op = Operator(kind, 32, 32, 0.1, vec["l32_links"])
+    _, info, hist = oracle.solve(solver, op, vec["l32_src"], max_iter=max_iter, hist_cap=max_iter)
+    c = cases[key]
+    assert (info["iter"], info["ops_count"], info["success"]) == (c["iter"], c["ops_count"], c["success"])
+    assert info["resSq"] == c["resSq"]
+    # the DETAIL log prints the same relative residuals, %g-formatted
+    logged = [float(l.split("RelRes ")[1]) for l in c["log"].splitlines() if " Iter " in l and "Success" not in l]
+    assert np.allclose(hist[: len(logged)], logged, rtol=1e-5)
+
+
+@pytest.mark.parametrize("rfc,wf", [(1, 0), (3, 0), (1, 1)])
+def test_cg_m_bit_exact(oracle, golden, rfc, wf):
+    vec, cases = golden
+    key = f"l32_cgm_rfc{rfc}_wf{wf}"
+    c = cases[key]
+    op = Operator("laplace", 32, 32, c["mass"], vec["l32_links"])
+    x, info, res = oracle.cg_m(op, vec["l32_src"], c["shifts"], resid_freq_check=rfc, worst_first=bool(wf))
+    assert (info["iter"], info["ops_count"], info["success"]) == (c["iter"], c["ops_count"], c["success"])
+    assert np.array_equal(res, np.array(c["resSqmrhs"]))
+    assert np.array_equal(x.reshape(-1), vec[key])
