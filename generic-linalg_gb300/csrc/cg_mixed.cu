@@ -4,7 +4,10 @@
 //
 // Algorithm: conjugate gradients with reliable updates (Sleijpen & van der Vorst 1996; the
 // mixed-precision form of Clark et al., arXiv:0911.3191).  The inner loop runs the CG
-// recurrence in FP32 arithmetic on fields stored as FP32, FP16 or BF16.  Whenever the
+// recurrence in FP32 arithmetic.  Storage per variant (direction vectors p, t / links /
+// accumulators r, x_lo): SINGLE FP32 / FP32 / FP32; HALF FP16 / FP16 / FP32; BFLOAT
+// BF16 / FP32 / FP32 (BF16 links, 8-bit mantissa, make the inner operator too inexact for
+// kappa ~ 1e4 systems: defect correction needs |A_sloppy - A| kappa < 1).  Whenever the
 // iterated residual has dropped by `delta` since the last update (or claims convergence),
 // the FP64 solution is advanced by the low-precision correction and the residual is
 // recomputed in FP64 from the FP64 operator, r = b - A x; the search direction is
@@ -132,9 +135,9 @@ __device__ __forceinline__ bool mx_reduce(double (&v)[K], double *partials, unsi
 
 // Kernel A, staggered normal operator: p' = r + beta p_old at this site and its four
 // neighbours, t = D p' ; write p' and t ; |t|^2 + sigma |p'|^2 -> alpha.
-template <class S, class L>
+template <class S, class R, class L>
 __global__ void __launch_bounds__(kNT)
-k_mx_A_stag(const S *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
+k_mx_A_stag(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
             S *__restrict__ t, const L *__restrict__ H, float mass, int lx, int ly, MxDev *s,
             double *partials)
 {
@@ -146,7 +149,7 @@ k_mx_A_stag(const S *__restrict__ r, const S *__restrict__ p_old, S *__restrict_
         const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
         const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
         const long i = (long)y * lx + x;
-        auto P = [&](long j) { return fadd(Fmt<S>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
+        auto P = [&](long j) { return fadd(Fmt<R>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
         const float2 pc = P(i);
         const float2 hx = Fmt<L>::ld(H, 2 * i), hy = Fmt<L>::ld(H, 2 * i + 1);
         const float2 hxm = Fmt<L>::ld(H, 2 * ((long)y * lx + xm));
@@ -174,9 +177,9 @@ k_mx_A_stag(const S *__restrict__ r, const S *__restrict__ p_old, S *__restrict_
 }
 
 // Kernel A, gauge Laplacian: p' = r + beta p_old, Ap = (4 + m + sigma) p' + lap_sum(p').
-template <class S, class L>
+template <class S, class R, class L>
 __global__ void __launch_bounds__(kNT)
-k_mx_A_lap(const S *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
+k_mx_A_lap(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
            S *__restrict__ Ap, const L *__restrict__ G, float diag, int lx, int ly, MxDev *s,
            double *partials)
 {
@@ -188,7 +191,7 @@ k_mx_A_lap(const S *__restrict__ r, const S *__restrict__ p_old, S *__restrict__
         const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
         const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
         const long i = (long)y * lx + x;
-        auto P = [&](long j) { return fadd(Fmt<S>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
+        auto P = [&](long j) { return fadd(Fmt<R>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
         const float2 pc = P(i);
         float2 hs = fmul(Fmt<L>::ld(G, 2 * i), P((long)y * lx + xp));
         hs = fadd(hs, fmulc(Fmt<L>::ld(G, 2 * ((long)y * lx + xm)), P((long)y * lx + xm)));
@@ -235,9 +238,9 @@ __device__ __forceinline__ void mx_after_inner(MxDev *s, double rn, int dir_pari
 }
 
 // Kernel B, staggered normal: Ap = D^dagger t + sigma p', x_lo += alpha p', r -= alpha Ap.
-template <class S, class L>
+template <class S, class R, class L>
 __global__ void __launch_bounds__(kNT)
-k_mx_B_stag(const S *__restrict__ t, const S *__restrict__ p, S *__restrict__ r,
+k_mx_B_stag(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
             float2 *__restrict__ xlo, const L *__restrict__ H, float mass, float sigma, int lx,
             int ly, int dir_parity, MxDev *s, double *partials)
 {
@@ -252,18 +255,18 @@ k_mx_B_stag(const S *__restrict__ t, const S *__restrict__ p, S *__restrict__ r,
         const float2 av = fadd(fsub(fscale(mass, Fmt<S>::ld(t, i)), hs), fscale(sigma, pc));
         const float2 xo = xlo[i];
         xlo[i] = fadd(xo, fscale(alpha, pc));
-        const float2 rn = fsub(Fmt<S>::ld(r, i), fscale(alpha, av));
-        Fmt<S>::st(r, i, rn);
-        v[0] = (double)fn2(Fmt<S>::ld(r, i));
+        const float2 rn = fsub(Fmt<R>::ld(r, i), fscale(alpha, av));
+        Fmt<R>::st(r, i, rn);
+        v[0] = (double)fn2(Fmt<R>::ld(r, i));
     }
     if (mx_reduce<1>(v, partials, &s->cnt[1]) && threadIdx.x == 0 && threadIdx.y == 0)
         mx_after_inner(s, v[0], dir_parity);
 }
 
 // Kernel B, Laplacian: x_lo += alpha p', r -= alpha Ap.
-template <class S>
+template <class S, class R>
 __global__ void __launch_bounds__(kNT)
-k_mx_B_lap(const S *__restrict__ Ap, const S *__restrict__ p, S *__restrict__ r,
+k_mx_B_lap(const S *__restrict__ Ap, const S *__restrict__ p, R *__restrict__ r,
            float2 *__restrict__ xlo, int lx, int ly, int dir_parity, MxDev *s, double *partials)
 {
     if (s->done || s->reliable) return;
@@ -274,9 +277,9 @@ k_mx_B_lap(const S *__restrict__ Ap, const S *__restrict__ p, S *__restrict__ r,
         const long i = (long)y * lx + x;
         const float2 pc = Fmt<S>::ld(p, i);
         xlo[i] = fadd(xlo[i], fscale(alpha, pc));
-        const float2 rn = fsub(Fmt<S>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i)));
-        Fmt<S>::st(r, i, rn);
-        v[0] = (double)fn2(Fmt<S>::ld(r, i));
+        const float2 rn = fsub(Fmt<R>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i)));
+        Fmt<R>::st(r, i, rn);
+        v[0] = (double)fn2(Fmt<R>::ld(r, i));
     }
     if (mx_reduce<1>(v, partials, &s->cnt[1]) && threadIdx.x == 0 && threadIdx.y == 0)
         mx_after_inner(s, v[0], dir_parity);
@@ -348,9 +351,9 @@ k_mx_R2(double2 *__restrict__ rhi, const double2 *__restrict__ b, const double2 
 
 // R3: r_lo = r_hi / scale ; p_lo *= f ; reduce <r_lo, p_lo> (real part) and |r_lo|^2.
 // p_lo is the buffer holding the current direction (p0 or p1 by s->parity).
-template <class S>
+template <class S, class R>
 __global__ void __launch_bounds__(kRedThreads)
-k_mx_R3(S *__restrict__ rlo, S *p0, S *p1, const double2 *__restrict__ rhi, long n,
+k_mx_R3(R *__restrict__ rlo, S *p0, S *p1, const double2 *__restrict__ rhi, long n,
         MxDev *s, double *partials)
 {
     if (s->done) return;
@@ -360,10 +363,10 @@ k_mx_R3(S *__restrict__ rlo, S *p0, S *p1, const double2 *__restrict__ rhi, long
     double v[2] = {0.0, 0.0};
     for (long i = blockIdx.x * (long)kRedThreads + threadIdx.x; i < n; i += (long)gridDim.x * kRedThreads) {
         const double2 rh = rhi[i];
-        Fmt<S>::st(rlo, i, make_float2((float)(rh.x * inv), (float)(rh.y * inv)));
+        Fmt<R>::st(rlo, i, make_float2((float)(rh.x * inv), (float)(rh.y * inv)));
         const float2 pq = fscale(f, Fmt<S>::ld(plo, i));
         Fmt<S>::st(plo, i, pq);
-        const float2 rq = Fmt<S>::ld(rlo, i), pr = Fmt<S>::ld(plo, i);
+        const float2 rq = Fmt<R>::ld(rlo, i), pr = Fmt<S>::ld(plo, i);
         v[0] += (double)(rq.x * pr.x + rq.y * pr.y);
         v[1] += (double)fn2(rq);
     }
@@ -379,14 +382,14 @@ k_mx_R3(S *__restrict__ rlo, S *p0, S *p1, const double2 *__restrict__ rhi, long
 
 // R4: p0 = p_lo - rp * r_lo (restore r orthogonal to p); the direction is in p0 afterwards
 // (the tail kernel resets s->parity).
-template <class S>
-__global__ void k_mx_R4(S *p0, const S *p1, const S *__restrict__ rlo, long n, const MxDev *s)
+template <class S, class R>
+__global__ void k_mx_R4(S *p0, const S *p1, const R *__restrict__ rlo, long n, const MxDev *s)
 {
     if (s->done) return;
     const S *plo = s->parity ? p1 : p0;
     const float rp = (float)s->rp;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        Fmt<S>::st(p0, i, fsub(Fmt<S>::ld(plo, i), fscale(rp, Fmt<S>::ld(rlo, i))));
+        Fmt<S>::st(p0, i, fsub(Fmt<S>::ld(plo, i), fscale(rp, Fmt<R>::ld(rlo, i))));
 }
 
 __global__ void k_mx_outer_tail(MxDev *s, cudaGraphConditionalHandle outer)
@@ -438,7 +441,7 @@ static int vgrid(long n)
 
 // ---------------------------------------------------------------- driver
 
-template <class S>
+template <class S, class R, class LK>
 static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b,
                                 int max_iter, double eps, double delta, double sigma,
                                 glinalg_info *info, cudaStream_t st, const char *name)
@@ -447,7 +450,9 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     const int lx = op->lx, ly = op->ly;
     const bool stag = op->kind == GLINALG_OP_STAGGERED_NORMAL;
     Scratch sc(st);
-    S *r, *p0, *p1, *t, *L;
+    R *r;
+    S *p0, *p1, *t;
+    LK *L;
     float2 *xlo;
     double2 *rhi, *tmp64, *Ax;
     double *partials;
@@ -466,8 +471,8 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     GL_TRY(sc.alloc(&Ax, n));
     GL_TRY(sc.alloc(&partials, 2 * (size_t)std::max<long>(nb, nblk2d)));
     GL_TRY(sc.alloc(&s, 1));
-    if (stag) k_make_hop<S><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
-    else k_copy_links<S><<<vgrid(2 * n), 256, 0, st>>>(L, op->U, 2 * n);
+    if (stag) k_make_hop<LK><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
+    else k_copy_links<LK><<<vgrid(2 * n), 256, 0, st>>>(L, op->U, 2 * n);
     GL_CUDA(cudaGetLastError());
 
     MxDev h = {};
@@ -495,8 +500,8 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         }
         k_mx_R2<<<nb, kRedThreads, 0, cs>>>(rhi, b, Ax, x, n, s, partials);
         // the current direction lives in p0 or p1 according to s->parity
-        k_mx_R3<S><<<nb, kRedThreads, 0, cs>>>(r, p0, p1, rhi, n, s, partials);
-        k_mx_R4<S><<<vgrid(n), 256, 0, cs>>>(p0, p1, r, n, s);
+        k_mx_R3<S, R><<<nb, kRedThreads, 0, cs>>>(r, p0, p1, rhi, n, s, partials);
+        k_mx_R4<S, R><<<vgrid(n), 256, 0, cs>>>(p0, p1, r, n, s);
         GL_CUDA(cudaGetLastError());
         return GLINALG_SUCCESS;
     };
@@ -505,12 +510,12 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     // inner iteration pair, for a given direction buffer parity
     auto inner_pair = [&](cudaStream_t cs, S *pold, S *pnew, int dir_parity) -> glinalg_status {
         if (stag) {
-            k_mx_A_stag<S, S><<<grd, blk, 0, cs>>>(r, pold, pnew, t, L, (float)op->mass, lx, ly, s, partials);
-            k_mx_B_stag<S, S><<<grd, blk, 0, cs>>>(t, pnew, r, xlo, L, (float)op->mass, (float)sigma, lx, ly, dir_parity, s, partials);
+            k_mx_A_stag<S, R, LK><<<grd, blk, 0, cs>>>(r, pold, pnew, t, L, (float)op->mass, lx, ly, s, partials);
+            k_mx_B_stag<S, R, LK><<<grd, blk, 0, cs>>>(t, pnew, r, xlo, L, (float)op->mass, (float)sigma, lx, ly, dir_parity, s, partials);
         } else {
             const float diag = (float)(4.0 + op->mass + sigma);
-            k_mx_A_lap<S, S><<<grd, blk, 0, cs>>>(r, pold, pnew, t, L, diag, lx, ly, s, partials);
-            k_mx_B_lap<S><<<grd, blk, 0, cs>>>(t, pnew, r, xlo, lx, ly, dir_parity, s, partials);
+            k_mx_A_lap<S, R, LK><<<grd, blk, 0, cs>>>(r, pold, pnew, t, L, diag, lx, ly, s, partials);
+            k_mx_B_lap<S, R><<<grd, blk, 0, cs>>>(t, pnew, r, xlo, lx, ly, dir_parity, s, partials);
         }
         GL_CUDA(cudaGetLastError());
         return GLINALG_SUCCESS;
@@ -523,6 +528,9 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ex = nullptr;
     glinalg_status status = GLINALG_SUCCESS;
+    // graphs are captured on a private stream (capturing the caller's stream would fail for
+    // the legacy default stream and would serialise with the caller's work)
+    cudaStream_t cap_st = capture_stream();
     auto cleanup = [&]() {
         if (ex) cudaGraphExecDestroy(ex);
         if (g) cudaGraphDestroy(g);
@@ -542,10 +550,10 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         if (cudaGraphConditionalHandleCreate(&h_in, body_out, 0, 0) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
 
         // outer body part 1: arm the inner loop
-        if (cudaStreamBeginCaptureToGraph(st, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        k_mx_arm_inner<<<1, 32, 0, st>>>(s, h_in);
+        if (cudaStreamBeginCaptureToGraph(cap_st, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        k_mx_arm_inner<<<1, 32, 0, cap_st>>>(s, h_in);
         cudaGraph_t cap = nullptr;
-        if (cudaStreamEndCapture(st, &cap) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
         // the arm node is the only node so far: find it to hang the inner node after it
         size_t nn = 0;
         cudaGraphGetNodes(body_out, nullptr, &nn);
@@ -561,20 +569,20 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         cudaGraph_t body_in = ip.conditional.phGraph_out[0];
         // inner body: one iteration; parity flips in the guard; the direction buffers are
         // read through the parity in two predicated kernel pairs
-        if (cudaStreamBeginCaptureToGraph(st, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        glinalg_status bs = inner_pair(st, p0, p1, 1);
-        if (bs == GLINALG_SUCCESS) k_mx_inner_guard<<<1, 32, 0, st>>>(s, h_in);
+        if (cudaStreamBeginCaptureToGraph(cap_st, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        glinalg_status bs = inner_pair(cap_st, p0, p1, 1);
+        if (bs == GLINALG_SUCCESS) k_mx_inner_guard<<<1, 32, 0, cap_st>>>(s, h_in);
         if (bs == GLINALG_SUCCESS) {
             // second iteration of the pair with the buffers swapped
-            bs = inner_pair(st, p1, p0, 0);
-            if (bs == GLINALG_SUCCESS) k_mx_inner_guard<<<1, 32, 0, st>>>(s, h_in);
+            bs = inner_pair(cap_st, p1, p0, 0);
+            if (bs == GLINALG_SUCCESS) k_mx_inner_guard<<<1, 32, 0, cap_st>>>(s, h_in);
         }
-        if (cudaStreamEndCapture(st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { status = bs ? bs : GLINALG_ERROR_CUDA; break; }
+        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { status = bs ? bs : GLINALG_ERROR_CUDA; break; }
         // outer body part 2 (after the inner node): reliable update and tail
-        if (cudaStreamBeginCaptureToGraph(st, body_out, &n_in, nullptr, 1, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        bs = reliable_seq(st);
-        if (bs == GLINALG_SUCCESS) k_mx_outer_tail<<<1, 32, 0, st>>>(s, h_out);
-        if (cudaStreamEndCapture(st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { status = bs ? bs : GLINALG_ERROR_CUDA; break; }
+        if (cudaStreamBeginCaptureToGraph(cap_st, body_out, &n_in, nullptr, 1, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        bs = reliable_seq(cap_st);
+        if (bs == GLINALG_SUCCESS) k_mx_outer_tail<<<1, 32, 0, cap_st>>>(s, h_out);
+        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { status = bs ? bs : GLINALG_ERROR_CUDA; break; }
         if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
         if (cudaGraphLaunch(ex, st) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
     } while (0);
@@ -597,8 +605,9 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     info->status = h.status;
     info->reliable_updates = h.n_reliable;
     info->device_ms = tm.ms();
-    const double w = Fmt<S>::bytes;
-    const double per_iter = stag ? (14.0 * w + 8.0 * 2) : (12.0 * w + 8.0 * 2);
+    const double w = Fmt<S>::bytes, wr = Fmt<R>::bytes, wl = Fmt<LK>::bytes;
+    // A: r(wr) p_old(w) links(2wl) -> p'(w) t(w); B: t(w) links(2wl) p'(w) r(2 wr) x_lo(16)
+    const double per_iter = stag ? (6.0 * w + 4.0 * wl + 3.0 * wr + 16.0) : (6.0 * w + 2.0 * wl + 3.0 * wr + 16.0);
     info->gbytes = ((double)h.k * per_iter * n + (double)h.n_reliable * (8.0 + 4.0 * 2) * 16.0 * n) * 1e-9;
     fill_name(info, name);
     return GLINALG_SUCCESS;
@@ -615,9 +624,9 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
     if (!(delta > 0.0 && delta < 1.0)) delta = 0.1;
     glinalg_status s;
     switch (precision) {
-    case GLINALG_PREC_SINGLE: s = run_mixed<float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32"); break;
-    case GLINALG_PREC_HALF: s = run_mixed<__half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16"); break;
-    case GLINALG_PREC_BFLOAT: s = run_mixed<__nv_bfloat162>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16"); break;
+    case GLINALG_PREC_SINGLE: s = run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32"); break;
+    case GLINALG_PREC_HALF: s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16"); break;
+    case GLINALG_PREC_BFLOAT: s = run_mixed<__nv_bfloat162, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16"); break;
     default: set_last_error("unknown precision"); return GLINALG_ERROR_INVALID_VALUE;
     }
     if (s != GLINALG_SUCCESS) return s;
@@ -646,14 +655,16 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
 
 namespace glinalg {
 
-template <class S>
+template <class S, class R, class LK>
 static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, double ms[2], double bytes[2])
 {
     const long n = op->size;
     const int lx = op->lx, ly = op->ly;
     cudaStream_t st = lib_stream();
     Scratch sc(st);
-    S *r, *p0, *p1, *t, *L;
+    R *r;
+    S *p0, *p1, *t;
+    LK *L;
     float2 *xlo;
     double2 *ones;
     double *partials;
@@ -668,11 +679,11 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, 
     GL_TRY(sc.alloc(&ones, n));
     GL_TRY(sc.alloc(&partials, (size_t)grd.x * grd.y));
     GL_TRY(sc.alloc(&s, 1));
-    k_make_hop<S><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
+    k_make_hop<LK><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
     // r = 1 everywhere (any non-zero field gives a positive <p, A p>)
     std::vector<double2> h1(n, cmk(1.0, 0.0));
     GL_CUDA(cudaMemcpyAsync(ones, h1.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st));
-    k_copy_links<S><<<vgrid(n), 256, 0, st>>>(r, ones, n);
+    k_copy_links<R><<<vgrid(n), 256, 0, st>>>(r, ones, n);
     GL_CUDA(cudaGetLastError());
     // a state under which neither kernel early-exits or triggers an update: rsq = 0 makes
     // alpha = 0 (the updates add zero but run in full), delta = eps = 0 never trigger.
@@ -689,10 +700,10 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, 
         GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
         S *po = (it & 1) ? p1 : p0, *pn = (it & 1) ? p0 : p1;
         ta.start(st);
-        k_mx_A_stag<S, S><<<grd, blk, 0, st>>>(r, po, pn, t, L, mass, lx, ly, s, partials);
+        k_mx_A_stag<S, R, LK><<<grd, blk, 0, st>>>(r, po, pn, t, L, mass, lx, ly, s, partials);
         ta.stop(st);
         tb.start(st);
-        k_mx_B_stag<S, S><<<grd, blk, 0, st>>>(t, pn, r, xlo, L, mass, 0.f, lx, ly, 0, s, partials);
+        k_mx_B_stag<S, R, LK><<<grd, blk, 0, st>>>(t, pn, r, xlo, L, mass, 0.f, lx, ly, 0, s, partials);
         tb.stop(st);
         GL_CUDA(cudaGetLastError());
         const double a = ta.ms(), b = tb.ms();
@@ -703,11 +714,11 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, 
     }
     ms[0] = sa / n_launch;
     ms[1] = sb / n_launch;
-    const double w = Fmt<S>::bytes;
-    // A: r, p_old in; p', t out; hopping coefficients (2 per site).  B: t, p, r in; r out;
-    // x_lo (FP32) in and out; hopping coefficients.
-    bytes[0] = (double)n * (2 * w + 2 * w + 2 * w);
-    bytes[1] = (double)n * (3 * w + w + 16.0 + 2 * w);
+    const double w = Fmt<S>::bytes, wr = Fmt<R>::bytes, wl = Fmt<LK>::bytes;
+    // A: r, p_old in; p', t out; hopping coefficients (2 per site).  B: t, p in; r in and
+    // out; x_lo (FP32) in and out; hopping coefficients.
+    bytes[0] = (double)n * (wr + w + 2 * wl + 2 * w);
+    bytes[1] = (double)n * (w + w + 2 * wr + 16.0 + 2 * wl);
     return GLINALG_SUCCESS;
 }
 
@@ -721,9 +732,9 @@ extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int
     if (op->kind != GLINALG_OP_STAGGERED_NORMAL) return GLINALG_ERROR_UNSUPPORTED_OP;
     GL_TRY(ensure_device());
     switch (precision) {
-    case GLINALG_PREC_SINGLE: return profile_inner<float2>(op, n_launch, ms, bytes);
-    case GLINALG_PREC_HALF: return profile_inner<__half2>(op, n_launch, ms, bytes);
-    case GLINALG_PREC_BFLOAT: return profile_inner<__nv_bfloat162>(op, n_launch, ms, bytes);
+    case GLINALG_PREC_SINGLE: return profile_inner<float2, float2, float2>(op, n_launch, ms, bytes);
+    case GLINALG_PREC_HALF: return profile_inner<__half2, float2, __half2>(op, n_launch, ms, bytes);
+    case GLINALG_PREC_BFLOAT: return profile_inner<__nv_bfloat162, float2, float2>(op, n_launch, ms, bytes);
     default: return GLINALG_ERROR_INVALID_VALUE;
     }
 }

@@ -57,6 +57,8 @@ glinalg_status launch_staggered(const glinalg_operator_s *op, double2 *out, cons
 // The library's stream on the current device and its device-side scratch allocator.
 cudaStream_t lib_stream();
 void set_user_stream(cudaStream_t s, bool use);
+// A private stream of the current device used only to capture CUDA graphs.
+cudaStream_t capture_stream();
 glinalg_status ensure_device();
 
 // Bytes an application of the operator moves (algorithmic), for info->gbytes.

@@ -55,6 +55,16 @@ cudaStream_t lib_stream()
     return g_stream[d];
 }
 
+static cudaStream_t g_capture[64] = {};
+
+cudaStream_t capture_stream()
+{
+    int d = cur_dev();
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_capture[d]) cudaStreamCreateWithFlags(&g_capture[d], cudaStreamNonBlocking);
+    return g_capture[d];
+}
+
 void set_user_stream(cudaStream_t s, bool use)
 {
     int d = cur_dev();

@@ -168,13 +168,13 @@ Verb Verb::restart_inner() const
 void Verb::resid(const std::string &alg, int iter, int ops, double relres) const
 {
     if (present && level == 3)
-        std::cout << prefix << alg << " Iter " << iter << " Ops " << ops << " RelRes " << relres << "\n";
+        std::cout << prefix << alg << " Iter " << iter << " Ops " << ops << " RelRes " << relres << "\n" << std::flush;
 }
 void Verb::summary(const std::string &alg, bool success, int iter, int ops, double relres) const
 {
     if (present && (level == 1 || level == 2 || level == 3))
         std::cout << prefix << alg << " Success " << (success ? "Y" : "N") << " Iter " << iter
-                  << " Ops " << ops << " RelRes " << relres << "\n";
+                  << " Ops " << ops << " RelRes " << relres << "\n" << std::flush;
 }
 void Verb::summary_multi(bool success, int iter, int ops, const double *relres, int n) const
 {
@@ -182,13 +182,13 @@ void Verb::summary_multi(bool success, int iter, int ops, const double *relres, 
         std::cout << prefix << "CG-M " << " Success " << (success ? "Y" : "N") << " Iter " << iter
                   << " Ops " << ops << " RelRes ";
         for (int i = 0; i < n; i++) std::cout << relres[i] << " ";
-        std::cout << "\n";
+        std::cout << "\n" << std::flush;
     }
 }
 void Verb::restart(const std::string &alg, int iter, int ops, double relres) const
 {
     if (present && (level == 2 || level == 3))
-        std::cout << prefix << alg << " Iter " << iter << " Ops " << ops << " RelRes " << relres << "\n";
+        std::cout << prefix << alg << " Iter " << iter << " Ops " << ops << " RelRes " << relres << "\n" << std::flush;
 }
 
 void fill_name(glinalg_info *info, const std::string &name)

@@ -62,11 +62,14 @@ class LoopGraph {
         cudaGraphNode_t node;
         GL_CUDA(cudaGraphAddNode(&node, g_, nullptr, nullptr, 0, &np));
         cudaGraph_t bg = np.conditional.phGraph_out[0];
-        GL_CUDA(cudaStreamBeginCaptureToGraph(st, bg, nullptr, nullptr, 0,
+        // capture on a private stream; the graph is launched on `st`
+        cudaStream_t cs = capture_stream();
+        (void)st;
+        GL_CUDA(cudaStreamBeginCaptureToGraph(cs, bg, nullptr, nullptr, 0,
                                               cudaStreamCaptureModeThreadLocal));
-        glinalg_status s = body(st, h_);
+        glinalg_status s = body(cs, h_);
         cudaGraph_t captured = nullptr;
-        cudaError_t e = cudaStreamEndCapture(st, &captured);
+        cudaError_t e = cudaStreamEndCapture(cs, &captured);
         if (s != GLINALG_SUCCESS) return s;
         GL_CUDA(e);
         GL_CUDA(cudaGraphInstantiate(&ex_, g_, 0));
