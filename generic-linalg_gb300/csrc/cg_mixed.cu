@@ -7,68 +7,39 @@
 // recurrence in FP32 arithmetic.  Storage per variant (direction vectors p, t / links /
 // accumulators r, x_lo): SINGLE FP32 / FP32 / FP32; HALF FP16 / FP16 / FP32; BFLOAT
 // BF16 / FP32 / FP32 (BF16 links, 8-bit mantissa, make the inner operator too inexact for
-// kappa ~ 1e4 systems: defect correction needs |A_sloppy - A| kappa < 1).  Whenever the
-// iterated residual has dropped by `delta` since the last update (or claims convergence),
-// the FP64 solution is advanced by the low-precision correction and the residual is
-// recomputed in FP64 from the FP64 operator, r = b - A x; the search direction is
+// kappa ~ 1e4 systems: defect correction needs |A_sloppy - A| kappa < 1).
+// Whenever the iterated residual has dropped by `delta` since the last update (or claims
+// convergence), the FP64 solution is advanced by the low-precision correction and the
+// residual is recomputed in FP64 from the FP64 operator, r = b - A x; the search direction is
 // re-orthogonalised against the new residual and the recurrence continues.  The solve stops
 // only on an FP64-true relative residual below eps.
 //
 // Reduced-precision vectors are stored scaled: r_true ~= scale * r_lo with scale chosen at
 // every reliable update so that entries of r_lo are O(1), which keeps FP16 in range.
 //
-// Per inner iteration (staggered normal operator), two kernels:
+// Per inner iteration (staggered normal operator), two kernels (stag_tiles.cuh tiling):
 //   A: p' = r + beta p (read p from one buffer, write p' to the other), t = D p',
 //      |t|^2 (+ sigma |p'|^2) -> alpha = rsq / <p', A p'>
 //   B: Ap = D^dagger t (+ sigma p'), x_lo += alpha p', r -= alpha Ap, |r|^2 -> beta or update
-// For the Laplacian, A stores Ap and B reads it.
+// For the Laplacian, A stores Ap and B reads it.  The tile shape of the staggered kernels is
+// picked per lattice by timing the candidates on first use (autotune below).
 //
 // The whole solve is one CUDA graph: an outer WHILE node (until FP64 convergence) whose body
 // holds an inner WHILE node (inner iterations until a reliable update is due) followed by the
-// reliable-update kernels.
+// reliable-update kernels.  The last block of each inner kernel's reduction ends the inner
+// loop itself when an update is due or the solve has stopped.
 
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "solvers.h"
+#include "stag_tiles.cuh"
 
 namespace glinalg {
-
-// ---------------------------------------------------------------- storage formats
-
-template <class S>
-struct Fmt;
-template <>
-struct Fmt<float2> {
-    static __device__ __forceinline__ float2 ld(const float2 *p, long i) { return p[i]; }
-    static __device__ __forceinline__ void st(float2 *p, long i, float2 v) { p[i] = v; }
-    static __host__ __device__ __forceinline__ float2 from(double2 v) { return make_float2((float)v.x, (float)v.y); }
-    static constexpr int bytes = 8;
-};
-template <>
-struct Fmt<__half2> {
-    static __device__ __forceinline__ float2 ld(const __half2 *p, long i) { return __half22float2(p[i]); }
-    static __device__ __forceinline__ void st(__half2 *p, long i, float2 v) { p[i] = __float22half2_rn(v); }
-    static __device__ __forceinline__ __half2 from(double2 v) { return __floats2half2_rn((float)v.x, (float)v.y); }
-    static constexpr int bytes = 4;
-};
-template <>
-struct Fmt<__nv_bfloat162> {
-    static __device__ __forceinline__ float2 ld(const __nv_bfloat162 *p, long i) { return __bfloat1622float2(p[i]); }
-    static __device__ __forceinline__ void st(__nv_bfloat162 *p, long i, float2 v) { p[i] = __float22bfloat162_rn(v); }
-    static __device__ __forceinline__ __nv_bfloat162 from(double2 v) { return __floats2bfloat162_rn((float)v.x, (float)v.y); }
-    static constexpr int bytes = 4;
-};
-
-__device__ __forceinline__ float2 fadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 fsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 fscale(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
-// a * b
-__device__ __forceinline__ float2 fmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-// conj(a) * b
-__device__ __forceinline__ float2 fmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }
-__device__ __forceinline__ float fn2(float2 a) { return a.x * a.x + a.y * a.y; }
 
 // ---------------------------------------------------------------- device state
 
@@ -88,134 +59,28 @@ struct MxDev {
     unsigned cnt[6];
 };
 
-// ---------------------------------------------------------------- inner kernels
-
-// Staggered hopping at site (x,y) of field f with hopping coefficients H (h_x, h_y per
-// site, 1/2 and eta folded in):  sum = h_x(i) f(i+x) - h_x(i-x)^* f(i-x)
-//                                       + h_y(i) f(i+y) - h_y(i-y)^* f(i-y).
-// D = m + sum, D^dagger = m - sum.
-template <class S, class L>
-__device__ __forceinline__ float2 hop_sum(const S *f, const L *H, int x, int y, int lx, int ly)
+__device__ __forceinline__ void mx_stop_inner(cudaGraphConditionalHandle cond, int use_cond)
 {
-    const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
-    const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
-    const long i = (long)y * lx + x;
-    const float2 hx = Fmt<L>::ld(H, 2 * i), hy = Fmt<L>::ld(H, 2 * i + 1);
-    const float2 hxm = Fmt<L>::ld(H, 2 * ((long)y * lx + xm));
-    const float2 hym = Fmt<L>::ld(H, 2 * ((long)ym * lx + x) + 1);
-    float2 s = fmul(hx, Fmt<S>::ld(f, (long)y * lx + xp));
-    s = fsub(s, fmulc(hxm, Fmt<S>::ld(f, (long)y * lx + xm)));
-    s = fadd(s, fmul(hy, Fmt<S>::ld(f, (long)yp * lx + x)));
-    s = fsub(s, fmulc(hym, Fmt<S>::ld(f, (long)ym * lx + x)));
-    return s;
+    if (use_cond) cudaGraphSetConditional(cond, 0);
 }
 
-// Gauge Laplacian hopping: -sum_mu [U_mu(i) f(i+mu) + U_mu(i-mu)^* f(i-mu)] with G = U.
-template <class S, class L>
-__device__ __forceinline__ float2 lap_sum(const S *f, const L *G, int x, int y, int lx, int ly)
+// After the reduction of A: alpha = rsq / <p, A p>, or stop on breakdown.
+__device__ __forceinline__ void mx_after_A(MxDev *s, double pAp, cudaGraphConditionalHandle cond,
+                                           int use_cond)
 {
-    const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
-    const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
-    const long i = (long)y * lx + x;
-    float2 s = fmul(Fmt<L>::ld(G, 2 * i), Fmt<S>::ld(f, (long)y * lx + xp));
-    s = fadd(s, fmulc(Fmt<L>::ld(G, 2 * ((long)y * lx + xm)), Fmt<S>::ld(f, (long)y * lx + xm)));
-    s = fadd(s, fmul(Fmt<L>::ld(G, 2 * i + 1), Fmt<S>::ld(f, (long)yp * lx + x)));
-    s = fadd(s, fmulc(Fmt<L>::ld(G, 2 * ((long)ym * lx + x) + 1), Fmt<S>::ld(f, (long)ym * lx + x)));
-    return make_float2(-s.x, -s.y);
-}
-
-constexpr int kBX = 32, kBY = 8, kNT = kBX * kBY;
-
-template <int K>
-__device__ __forceinline__ bool mx_reduce(double (&v)[K], double *partials, unsigned *cnt)
-{
-    // blocks are 2D; grid_sum works on the flattened thread id
-    return grid_sum<K, kNT>(v, partials, cnt);
-}
-
-// Kernel A, staggered normal operator: p' = r + beta p_old at this site and its four
-// neighbours, t = D p' ; write p' and t ; |t|^2 + sigma |p'|^2 -> alpha.
-template <class S, class R, class L>
-__global__ void __launch_bounds__(kNT)
-k_mx_A_stag(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
-            S *__restrict__ t, const L *__restrict__ H, float mass, int lx, int ly, MxDev *s,
-            double *partials)
-{
-    if (s->done || s->reliable) return;
-    const float beta = (float)s->beta;
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y;
-    double v[1] = {0.0};
-    if (x < lx && y < ly) {
-        const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
-        const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
-        const long i = (long)y * lx + x;
-        auto P = [&](long j) { return fadd(Fmt<R>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
-        const float2 pc = P(i);
-        const float2 hx = Fmt<L>::ld(H, 2 * i), hy = Fmt<L>::ld(H, 2 * i + 1);
-        const float2 hxm = Fmt<L>::ld(H, 2 * ((long)y * lx + xm));
-        const float2 hym = Fmt<L>::ld(H, 2 * ((long)ym * lx + x) + 1);
-        float2 hs = fmul(hx, P((long)y * lx + xp));
-        hs = fsub(hs, fmulc(hxm, P((long)y * lx + xm)));
-        hs = fadd(hs, fmul(hy, P((long)yp * lx + x)));
-        hs = fsub(hs, fmulc(hym, P((long)ym * lx + x)));
-        const float2 tv = fadd(fscale(mass, pc), hs);
-        Fmt<S>::st(p_new, i, pc);
-        Fmt<S>::st(t, i, tv);
-        // accumulate what was stored, so that alpha matches the rounded vectors
-        const float2 pq = Fmt<S>::ld(p_new, i), tq = Fmt<S>::ld(t, i);
-        v[0] = (double)fn2(tq) + s->sigma * (double)fn2(pq);
+    if (!(pAp > 0.0) || !isfinite(pAp)) {
+        s->status = pAp == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
+        s->done = 1;
+        mx_stop_inner(cond, use_cond);
+        return;
     }
-    if (mx_reduce<1>(v, partials, &s->cnt[0]) && threadIdx.x == 0 && threadIdx.y == 0) {
-        const double pAp = v[0];
-        if (!(pAp > 0.0) || !isfinite(pAp)) {
-            s->status = pAp == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
-            s->done = 1;
-            return;
-        }
-        s->alpha = s->rsq / pAp;
-    }
+    s->alpha = s->rsq / pAp;
 }
 
-// Kernel A, gauge Laplacian: p' = r + beta p_old, Ap = (4 + m + sigma) p' + lap_sum(p').
-template <class S, class R, class L>
-__global__ void __launch_bounds__(kNT)
-k_mx_A_lap(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
-           S *__restrict__ Ap, const L *__restrict__ G, float diag, int lx, int ly, MxDev *s,
-           double *partials)
-{
-    if (s->done || s->reliable) return;
-    const float beta = (float)s->beta;
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y;
-    double v[1] = {0.0};
-    if (x < lx && y < ly) {
-        const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
-        const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
-        const long i = (long)y * lx + x;
-        auto P = [&](long j) { return fadd(Fmt<R>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
-        const float2 pc = P(i);
-        float2 hs = fmul(Fmt<L>::ld(G, 2 * i), P((long)y * lx + xp));
-        hs = fadd(hs, fmulc(Fmt<L>::ld(G, 2 * ((long)y * lx + xm)), P((long)y * lx + xm)));
-        hs = fadd(hs, fmul(Fmt<L>::ld(G, 2 * i + 1), P((long)yp * lx + x)));
-        hs = fadd(hs, fmulc(Fmt<L>::ld(G, 2 * ((long)ym * lx + x) + 1), P((long)ym * lx + x)));
-        const float2 av = fsub(fscale(diag, pc), hs);
-        Fmt<S>::st(p_new, i, pc);
-        Fmt<S>::st(Ap, i, av);
-        const float2 pq = Fmt<S>::ld(p_new, i), aq = Fmt<S>::ld(Ap, i);
-        v[0] = (double)(pq.x * aq.x + pq.y * aq.y);  // Re <p, Ap>
-    }
-    if (mx_reduce<1>(v, partials, &s->cnt[0]) && threadIdx.x == 0 && threadIdx.y == 0) {
-        const double pAp = v[0];
-        if (!(pAp > 0.0) || !isfinite(pAp)) {
-            s->status = pAp == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
-            s->done = 1;
-            return;
-        }
-        s->alpha = s->rsq / pAp;
-    }
-}
-
-// Decide what follows an inner iteration (last block, one thread).
-__device__ __forceinline__ void mx_after_inner(MxDev *s, double rn, int dir_parity)
+// After the reduction of B: beta for the next iteration, or flag a reliable update (which
+// also covers convergence of the iterated residual and the iteration cap).
+__device__ __forceinline__ void mx_after_B(MxDev *s, double rn, int dir_parity,
+                                           cudaGraphConditionalHandle cond, int use_cond)
 {
     const int k = s->k;
     s->parity = dir_parity;
@@ -224,6 +89,7 @@ __device__ __forceinline__ void mx_after_inner(MxDev *s, double rn, int dir_pari
     if (!isfinite(rn)) {
         s->status = GLINALG_SOLVE_NONFINITE;
         s->done = 1;
+        mx_stop_inner(cond, use_cond);
         return;
     }
     const double rho = sqrt(rn) * s->scale;  // true-scale iterated residual
@@ -231,64 +97,159 @@ __device__ __forceinline__ void mx_after_inner(MxDev *s, double rn, int dir_pari
     const double bsqrt = sqrt(s->bsq);
     if (rho < s->delta * s->rmax || rho < s->eps * bsqrt || k + 1 >= s->max_iter) {
         s->reliable = 1;
+        mx_stop_inner(cond, use_cond);
         return;
     }
     s->beta = rn / s->rsq;
     s->rsq = rn;
 }
 
-// Kernel B, staggered normal: Ap = D^dagger t + sigma p', x_lo += alpha p', r -= alpha Ap.
-template <class S, class R, class L>
-__global__ void __launch_bounds__(kNT)
-k_mx_B_stag(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
-            float2 *__restrict__ xlo, const L *__restrict__ H, float mass, float sigma, int lx,
-            int ly, int dir_parity, MxDev *s, double *partials)
+// ---------------------------------------------------------------- staggered inner kernels
+
+// A: p' = r + beta p_old ; t = D p' ; |t|^2 + sigma |p'|^2
+template <class S, class R, class LK, int BY, int NY, bool XS>
+__global__ void __launch_bounds__(32 * BY)
+k_stA(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
+      S *__restrict__ t, const LK *__restrict__ H, float mass, float sigma, int lx, int ly,
+      MxDev *s, double *partials, cudaGraphConditionalHandle cond, int use_cond)
 {
     if (s->done || s->reliable) return;
-    const float alpha = (float)s->alpha;
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y;
-    double v[1] = {0.0};
-    if (x < lx && y < ly) {
-        const long i = (long)y * lx + x;
-        const float2 hs = hop_sum<S, L>(t, H, x, y, lx, ly);
-        const float2 pc = Fmt<S>::ld(p, i);
-        const float2 av = fadd(fsub(fscale(mass, Fmt<S>::ld(t, i)), hs), fscale(sigma, pc));
-        const float2 xo = xlo[i];
-        xlo[i] = fadd(xo, fscale(alpha, pc));
-        const float2 rn = fsub(Fmt<R>::ld(r, i), fscale(alpha, av));
-        Fmt<R>::st(r, i, rn);
-        v[0] = (double)fn2(Fmt<R>::ld(r, i));
+    const float beta = (float)s->beta;
+    const int lane = threadIdx.x;
+    const int x = blockIdx.x * 32 + lane;
+    const int ybase = blockIdx.y * (BY * NY) + threadIdx.y * NY;
+    const bool xval = x < lx;
+    const int xc = xval ? x : lx - 1;
+    const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
+    float2 c[NY + 2];
+    load_col<NY>(c, r, p_old, beta, xc, ybase, lx, ly);
+    float2 fxm[NY], fxp[NY];
+    auto edge = [&](int col, int j) -> float2 {
+        const long i = (long)wrapi(ybase + j, ly) * lx + col;
+        return fadd(Fmt<R>::ld(r, i), fscale(beta, Fmt<S>::ld(p_old, i)));
+    };
+    x_neighbours<NY, XS>(fxm, fxp, c, lane, xm, xp, edge);
+    float2 hs[NY];
+    hop_col<NY>(hs, c, fxm, fxp, H, xc, xm, ybase, lx, ly);
+    float acc[1] = {0.f};
+#pragma unroll
+    for (int j = 0; j < NY; j++) {
+        const int y = ybase + j;
+        if (xval && y < ly) {
+            const long i = (long)y * lx + x;
+            const float2 pc = c[j + 1];
+            const float2 tv = fadd(fscale(mass, pc), hs[j]);
+            Fmt<S>::st(p_new, i, pc);
+            Fmt<S>::st(t, i, tv);
+            // reduce what was stored, so that alpha matches the rounded vectors
+            const float2 pq = Fmt<S>::ld(p_new, i), tq = Fmt<S>::ld(t, i);
+            acc[0] += fn2(tq) + sigma * fn2(pq);
+        }
     }
-    if (mx_reduce<1>(v, partials, &s->cnt[1]) && threadIdx.x == 0 && threadIdx.y == 0)
-        mx_after_inner(s, v[0], dir_parity);
+    double out[1];
+    if (grid_sum_f<1, 32 * BY>(acc, partials, &s->cnt[0], out) && threadIdx.x == 0 && threadIdx.y == 0)
+        mx_after_A(s, out[0], cond, use_cond);
 }
 
-// Kernel B, Laplacian: x_lo += alpha p', r -= alpha Ap.
-template <class S, class R>
-__global__ void __launch_bounds__(kNT)
-k_mx_B_lap(const S *__restrict__ Ap, const S *__restrict__ p, R *__restrict__ r,
-           float2 *__restrict__ xlo, int lx, int ly, int dir_parity, MxDev *s, double *partials)
+// B: Ap = D^dagger t + sigma p' ; x_lo += alpha p' ; r -= alpha Ap ; |r|^2
+template <class S, class R, class LK, int BY, int NY, bool XS>
+__global__ void __launch_bounds__(32 * BY)
+k_stB(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
+      float2 *__restrict__ xlo, const LK *__restrict__ H, float mass, float sigma, int lx, int ly,
+      int dir_parity, MxDev *s, double *partials, cudaGraphConditionalHandle cond, int use_cond)
 {
     if (s->done || s->reliable) return;
     const float alpha = (float)s->alpha;
-    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y;
-    double v[1] = {0.0};
+    const int lane = threadIdx.x;
+    const int x = blockIdx.x * 32 + lane;
+    const int ybase = blockIdx.y * (BY * NY) + threadIdx.y * NY;
+    const bool xval = x < lx;
+    const int xc = xval ? x : lx - 1;
+    const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
+    float2 c[NY + 2];
+    load_col<NY, S, S>(c, t, (const S *)nullptr, 0.f, xc, ybase, lx, ly);
+    float2 fxm[NY], fxp[NY];
+    auto edge = [&](int col, int j) -> float2 {
+        return Fmt<S>::ld(t, (long)wrapi(ybase + j, ly) * lx + col);
+    };
+    x_neighbours<NY, XS>(fxm, fxp, c, lane, xm, xp, edge);
+    float2 hs[NY];
+    hop_col<NY>(hs, c, fxm, fxp, H, xc, xm, ybase, lx, ly);
+    float acc[1] = {0.f};
+#pragma unroll
+    for (int j = 0; j < NY; j++) {
+        const int y = ybase + j;
+        if (xval && y < ly) {
+            const long i = (long)y * lx + x;
+            const float2 pc = Fmt<S>::ld(p, i);
+            const float2 av = fadd(fsub(fscale(mass, c[j + 1]), hs[j]), fscale(sigma, pc));
+            xlo[i] = fadd(xlo[i], fscale(alpha, pc));
+            Fmt<R>::st(r, i, fsub(Fmt<R>::ld(r, i), fscale(alpha, av)));
+            acc[0] += fn2(Fmt<R>::ld(r, i));
+        }
+    }
+    double out[1];
+    if (grid_sum_f<1, 32 * BY>(acc, partials, &s->cnt[1], out) && threadIdx.x == 0 && threadIdx.y == 0)
+        mx_after_B(s, out[0], dir_parity, cond, use_cond);
+}
+
+// ---------------------------------------------------------------- Laplacian inner kernels
+
+constexpr int kLBX = 32, kLBY = 8, kLNT = kLBX * kLBY;
+
+// A: p' = r + beta p_old, Ap = (4 + m + sigma) p' - sum_mu [U p'(+mu) + U^* p'(-mu)]
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kLNT)
+k_lapA(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_new,
+       S *__restrict__ Ap, const LK *__restrict__ G, float diag, int lx, int ly, MxDev *s,
+       double *partials, cudaGraphConditionalHandle cond, int use_cond)
+{
+    if (s->done || s->reliable) return;
+    const float beta = (float)s->beta;
+    const int x = blockIdx.x * kLBX + threadIdx.x, y = blockIdx.y * kLBY + threadIdx.y;
+    float acc[1] = {0.f};
+    if (x < lx && y < ly) {
+        const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
+        const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
+        const long i = (long)y * lx + x;
+        auto P = [&](long j) { return fadd(Fmt<R>::ld(r, j), fscale(beta, Fmt<S>::ld(p_old, j))); };
+        const float2 pc = P(i);
+        float2 hs = fmul(Fmt<LK>::ld(G, 2 * i), P((long)y * lx + xp));
+        hs = fadd(hs, fmulc(Fmt<LK>::ld(G, 2 * ((long)y * lx + xm)), P((long)y * lx + xm)));
+        hs = fadd(hs, fmul(Fmt<LK>::ld(G, 2 * i + 1), P((long)yp * lx + x)));
+        hs = fadd(hs, fmulc(Fmt<LK>::ld(G, 2 * ((long)ym * lx + x) + 1), P((long)ym * lx + x)));
+        const float2 av = fsub(fscale(diag, pc), hs);
+        Fmt<S>::st(p_new, i, pc);
+        Fmt<S>::st(Ap, i, av);
+        const float2 pq = Fmt<S>::ld(p_new, i), aq = Fmt<S>::ld(Ap, i);
+        acc[0] = pq.x * aq.x + pq.y * aq.y;  // Re <p, Ap>
+    }
+    double out[1];
+    if (grid_sum_f<1, kLNT>(acc, partials, &s->cnt[0], out) && threadIdx.x == 0 && threadIdx.y == 0)
+        mx_after_A(s, out[0], cond, use_cond);
+}
+
+// B: x_lo += alpha p', r -= alpha Ap
+template <class S, class R>
+__global__ void __launch_bounds__(kLNT)
+k_lapB(const S *__restrict__ Ap, const S *__restrict__ p, R *__restrict__ r,
+       float2 *__restrict__ xlo, int lx, int ly, int dir_parity, MxDev *s, double *partials,
+       cudaGraphConditionalHandle cond, int use_cond)
+{
+    if (s->done || s->reliable) return;
+    const float alpha = (float)s->alpha;
+    const int x = blockIdx.x * kLBX + threadIdx.x, y = blockIdx.y * kLBY + threadIdx.y;
+    float acc[1] = {0.f};
     if (x < lx && y < ly) {
         const long i = (long)y * lx + x;
         const float2 pc = Fmt<S>::ld(p, i);
         xlo[i] = fadd(xlo[i], fscale(alpha, pc));
-        const float2 rn = fsub(Fmt<R>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i)));
-        Fmt<R>::st(r, i, rn);
-        v[0] = (double)fn2(Fmt<R>::ld(r, i));
+        Fmt<R>::st(r, i, fsub(Fmt<R>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i))));
+        acc[0] = fn2(Fmt<R>::ld(r, i));
     }
-    if (mx_reduce<1>(v, partials, &s->cnt[1]) && threadIdx.x == 0 && threadIdx.y == 0)
-        mx_after_inner(s, v[0], dir_parity);
-}
-
-__global__ void k_mx_inner_guard(MxDev *s, cudaGraphConditionalHandle h)
-{
-    if (threadIdx.x != 0) return;
-    if (s->done || s->reliable || s->k >= s->max_iter) cudaGraphSetConditional(h, 0);
+    double out[1];
+    if (grid_sum_f<1, kLNT>(acc, partials, &s->cnt[1], out) && threadIdx.x == 0 && threadIdx.y == 0)
+        mx_after_B(s, out[0], dir_parity, cond, use_cond);
 }
 
 // ---------------------------------------------------------------- reliable update kernels
@@ -353,8 +314,8 @@ k_mx_R2(double2 *__restrict__ rhi, const double2 *__restrict__ b, const double2 
 // p_lo is the buffer holding the current direction (p0 or p1 by s->parity).
 template <class S, class R>
 __global__ void __launch_bounds__(kRedThreads)
-k_mx_R3(R *__restrict__ rlo, S *p0, S *p1, const double2 *__restrict__ rhi, long n,
-        MxDev *s, double *partials)
+k_mx_R3(R *__restrict__ rlo, S *p0, S *p1, const double2 *__restrict__ rhi, long n, MxDev *s,
+        double *partials)
 {
     if (s->done) return;
     S *plo = s->parity ? p1 : p0;
@@ -439,12 +400,125 @@ static int vgrid(long n)
     return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
+// ---------------------------------------------------------------- tile shapes and autotuning
+
+template <class S, class R, class LK>
+struct StagKernels {
+    using FA = void (*)(const R *, const S *, S *, S *, const LK *, float, float, int, int, MxDev *,
+                        double *, cudaGraphConditionalHandle, int);
+    using FB = void (*)(const S *, const S *, R *, float2 *, const LK *, float, float, int, int, int,
+                        MxDev *, double *, cudaGraphConditionalHandle, int);
+    FA A;
+    FB B;
+    int by, ny;
+    dim3 block() const { return dim3(32, by); }
+    dim3 grid(int lx, int ly) const { return dim3((lx + 31) / 32, (ly + by * ny - 1) / (by * ny)); }
+};
+
+// Tile-shape candidates (BY thread rows, NY sites per thread along y).
+constexpr int kNumTiles = 4;
+static const int kTileBY[kNumTiles] = {8, 8, 4, 16};
+static const int kTileNY[kNumTiles] = {2, 4, 8, 2};
+
+template <class S, class R, class LK, int BY, int NY>
+static StagKernels<S, R, LK> make_kernels(bool xs)
+{
+    StagKernels<S, R, LK> k;
+    k.A = xs ? k_stA<S, R, LK, BY, NY, true> : k_stA<S, R, LK, BY, NY, false>;
+    k.B = xs ? k_stB<S, R, LK, BY, NY, true> : k_stB<S, R, LK, BY, NY, false>;
+    k.by = BY;
+    k.ny = NY;
+    return k;
+}
+
+template <class S, class R, class LK>
+static StagKernels<S, R, LK> kernels_for(int cand, bool xs)
+{
+    switch (cand) {
+    case 0: return make_kernels<S, R, LK, 8, 2>(xs);
+    case 1: return make_kernels<S, R, LK, 8, 4>(xs);
+    case 2: return make_kernels<S, R, LK, 4, 8>(xs);
+    default: return make_kernels<S, R, LK, 16, 2>(xs);
+    }
+}
+
+static long max_tile_blocks(int lx, int ly)
+{
+    long m = 0;
+    for (int c = 0; c < kNumTiles; c++) {
+        long b = (long)((lx + 31) / 32) * ((ly + kTileBY[c] * kTileNY[c] - 1) / (kTileBY[c] * kTileNY[c]));
+        m = std::max(m, b);
+    }
+    return m;
+}
+
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, int> g_tuned;  // (device, lx, ly, variant) -> candidate
+
+// Times every tile candidate on the solve's own buffers (A then B, 8 launches each after one
+// warm-up) and returns the fastest; cached per device, lattice and variant.
+template <class S, class R, class LK>
+static int autotune(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p1, S *t, float2 *xlo,
+                    const LK *L, MxDev *s, double *partials, cudaStream_t st)
+{
+    const int lx = op->lx, ly = op->ly;
+    const auto key = std::make_tuple(op->device, lx, ly, variant);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) return it->second;
+    }
+    const bool xs = lx % 32 == 0;
+    // a state under which the kernels neither stop nor trigger an update: rsq = 0 gives
+    // alpha = 0 (updates add zero but run in full); delta = eps = 0 never trigger
+    MxDev h = {};
+    h.beta = 0.5;
+    h.scale = 1.0;
+    h.rmax = 1e300;
+    h.max_iter = 0x7fffffff;
+    std::vector<double2> ones(op->size, cmk(1.0, 0.0));
+    double2 *d1 = nullptr;
+    if (cudaMallocAsync((void **)&d1, sizeof(double2) * op->size, st) != cudaSuccess) return 1;
+    cudaMemcpyAsync(d1, ones.data(), sizeof(double2) * op->size, cudaMemcpyHostToDevice, st);
+    k_copy_links<R><<<vgrid(op->size), 256, 0, st>>>(r, d1, op->size);
+    cudaFreeAsync(d1, st);
+    int best = 1;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int c = 0; c < kNumTiles; c++) {
+        auto k = kernels_for<S, R, LK>(c, xs);
+        float tot = 0.f;
+        for (int it = 0; it < 9; it++) {
+            cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st);
+            cudaEventRecord(e0, st);
+            k.A<<<k.grid(lx, ly), k.block(), 0, st>>>(r, p0, p1, t, L, (float)op->mass, 0.f, lx, ly, s, partials, 0, 0);
+            k.B<<<k.grid(lx, ly), k.block(), 0, st>>>(t, p1, r, xlo, L, (float)op->mass, 0.f, lx, ly, 1, s, partials, 0, 0);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (it > 0) tot += ms;
+        }
+        if (cudaGetLastError() == cudaSuccess && tot < best_ms) {
+            best_ms = tot;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best;
+    return best;
+}
+
 // ---------------------------------------------------------------- driver
 
 template <class S, class R, class LK>
 static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b,
                                 int max_iter, double eps, double delta, double sigma,
-                                glinalg_info *info, cudaStream_t st, const char *name)
+                                glinalg_info *info, cudaStream_t st, const char *name, int variant)
 {
     const long n = op->size;
     const int lx = op->lx, ly = op->ly;
@@ -458,8 +532,8 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     double *partials;
     MxDev *s;
     const int nb = reduction_blocks(n);
-    const dim3 blk(kBX, kBY), grd((lx + kBX - 1) / kBX, (ly + kBY - 1) / kBY);
-    const long nblk2d = (long)grd.x * grd.y;
+    const dim3 lblk(kLBX, kLBY), lgrd((lx + kLBX - 1) / kLBX, (ly + kLBY - 1) / kLBY);
+    const long max_blocks = std::max<long>(std::max<long>(nb, (long)lgrd.x * lgrd.y), max_tile_blocks(lx, ly));
     GL_TRY(sc.alloc(&r, n));
     GL_TRY(sc.zeros(&p0, n));
     GL_TRY(sc.zeros(&p1, n));
@@ -469,11 +543,21 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     GL_TRY(sc.alloc(&rhi, n));
     GL_TRY(sc.alloc(&tmp64, n));
     GL_TRY(sc.alloc(&Ax, n));
-    GL_TRY(sc.alloc(&partials, 2 * (size_t)std::max<long>(nb, nblk2d)));
-    GL_TRY(sc.alloc(&s, 1));
+    GL_TRY(sc.alloc(&partials, 2 * (size_t)max_blocks));
+    GL_TRY(sc.zeros(&s, 1));
     if (stag) k_make_hop<LK><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
     else k_copy_links<LK><<<vgrid(2 * n), 256, 0, st>>>(L, op->U, 2 * n);
     GL_CUDA(cudaGetLastError());
+
+    StagKernels<S, R, LK> sk{};
+    if (stag) {
+        const int cand = autotune<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, partials, st);
+        sk = kernels_for<S, R, LK>(cand, lx % 32 == 0);
+        // the tuning runs wrote the work vectors: start from zero again
+        GL_CUDA(cudaMemsetAsync(p0, 0, sizeof(S) * n, st));
+        GL_CUDA(cudaMemsetAsync(p1, 0, sizeof(S) * n, st));
+        GL_CUDA(cudaMemsetAsync(xlo, 0, sizeof(float2) * n, st));
+    }
 
     MxDev h = {};
     h.eps = eps;
@@ -507,54 +591,53 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     };
     GL_TRY(reliable_seq(st));
 
-    // inner iteration pair, for a given direction buffer parity
-    auto inner_pair = [&](cudaStream_t cs, S *pold, S *pnew, int dir_parity) -> glinalg_status {
+    // one inner iteration reading the direction from pold and writing it to pnew
+    auto inner = [&](cudaStream_t cs, S *pold, S *pnew, int dir_parity,
+                     cudaGraphConditionalHandle hin) -> glinalg_status {
         if (stag) {
-            k_mx_A_stag<S, R, LK><<<grd, blk, 0, cs>>>(r, pold, pnew, t, L, (float)op->mass, lx, ly, s, partials);
-            k_mx_B_stag<S, R, LK><<<grd, blk, 0, cs>>>(t, pnew, r, xlo, L, (float)op->mass, (float)sigma, lx, ly, dir_parity, s, partials);
+            sk.A<<<sk.grid(lx, ly), sk.block(), 0, cs>>>(r, pold, pnew, t, L, (float)op->mass, (float)sigma,
+                                                        lx, ly, s, partials, hin, 1);
+            sk.B<<<sk.grid(lx, ly), sk.block(), 0, cs>>>(t, pnew, r, xlo, L, (float)op->mass, (float)sigma,
+                                                        lx, ly, dir_parity, s, partials, hin, 1);
         } else {
             const float diag = (float)(4.0 + op->mass + sigma);
-            k_mx_A_lap<S, R, LK><<<grd, blk, 0, cs>>>(r, pold, pnew, t, L, diag, lx, ly, s, partials);
-            k_mx_B_lap<S, R><<<grd, blk, 0, cs>>>(t, pnew, r, xlo, lx, ly, dir_parity, s, partials);
+            k_lapA<S, R, LK><<<lgrd, lblk, 0, cs>>>(r, pold, pnew, t, L, diag, lx, ly, s, partials, hin, 1);
+            k_lapB<S, R><<<lgrd, lblk, 0, cs>>>(t, pnew, r, xlo, lx, ly, dir_parity, s, partials, hin, 1);
         }
         GL_CUDA(cudaGetLastError());
         return GLINALG_SUCCESS;
     };
 
-    // Graph: while (!done) { arm inner; while (inner) { A(p0->p1) B guard ; A(p1->p0) B guard } ;
+    // Graph: while (!done) { arm inner; while (inner) { A(p0->p1) B ; A(p1->p0) B } ;
     // reliable update ; tail }.  The inner body holds two iterations so that the direction
     // buffers alternate without a copy; B records which buffer holds the current direction
-    // and the reliable update moves it back to p0.
+    // and the reliable update moves it back to p0.  Graphs are captured on a private stream
+    // (capturing the caller's stream would fail for the legacy default stream).
+    cudaStream_t cap_st = capture_stream();
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ex = nullptr;
     glinalg_status status = GLINALG_SUCCESS;
-    // graphs are captured on a private stream (capturing the caller's stream would fail for
-    // the legacy default stream and would serialise with the caller's work)
-    cudaStream_t cap_st = capture_stream();
-    auto cleanup = [&]() {
-        if (ex) cudaGraphExecDestroy(ex);
-        if (g) cudaGraphDestroy(g);
+    auto fail = [&](glinalg_status e) {
+        if (status == GLINALG_SUCCESS) status = e;
     };
     do {
         cudaGraphConditionalHandle h_out, h_in;
-        if (cudaGraphCreate(&g, 0) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        if (cudaGraphConditionalHandleCreate(&h_out, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaGraphCreate(&g, 0) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
+        if (cudaGraphConditionalHandleCreate(&h_out, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         cudaGraphNodeParams op_ = {};
         op_.type = cudaGraphNodeTypeConditional;
         op_.conditional.handle = h_out;
         op_.conditional.type = cudaGraphCondTypeWhile;
         op_.conditional.size = 1;
         cudaGraphNode_t n_out;
-        if (cudaGraphAddNode(&n_out, g, nullptr, nullptr, 0, &op_) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaGraphAddNode(&n_out, g, nullptr, nullptr, 0, &op_) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         cudaGraph_t body_out = op_.conditional.phGraph_out[0];
-        if (cudaGraphConditionalHandleCreate(&h_in, body_out, 0, 0) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-
+        if (cudaGraphConditionalHandleCreate(&h_in, body_out, 0, 0) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         // outer body part 1: arm the inner loop
-        if (cudaStreamBeginCaptureToGraph(cap_st, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaStreamBeginCaptureToGraph(cap_st, body_out, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         k_mx_arm_inner<<<1, 32, 0, cap_st>>>(s, h_in);
         cudaGraph_t cap = nullptr;
-        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        // the arm node is the only node so far: find it to hang the inner node after it
+        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         size_t nn = 0;
         cudaGraphGetNodes(body_out, nullptr, &nn);
         std::vector<cudaGraphNode_t> nodes(nn);
@@ -565,38 +648,34 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         ip.conditional.type = cudaGraphCondTypeWhile;
         ip.conditional.size = 1;
         cudaGraphNode_t n_in;
-        if (cudaGraphAddNode(&n_in, body_out, nodes.data(), nullptr, nn, &ip) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaGraphAddNode(&n_in, body_out, nodes.data(), nullptr, nn, &ip) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         cudaGraph_t body_in = ip.conditional.phGraph_out[0];
-        // inner body: one iteration; parity flips in the guard; the direction buffers are
-        // read through the parity in two predicated kernel pairs
-        if (cudaStreamBeginCaptureToGraph(cap_st, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        glinalg_status bs = inner_pair(cap_st, p0, p1, 1);
-        if (bs == GLINALG_SUCCESS) k_mx_inner_guard<<<1, 32, 0, cap_st>>>(s, h_in);
-        if (bs == GLINALG_SUCCESS) {
-            // second iteration of the pair with the buffers swapped
-            bs = inner_pair(cap_st, p1, p0, 0);
-            if (bs == GLINALG_SUCCESS) k_mx_inner_guard<<<1, 32, 0, cap_st>>>(s, h_in);
-        }
-        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { status = bs ? bs : GLINALG_ERROR_CUDA; break; }
+        // inner body: two iterations with the direction buffers swapped
+        if (cudaStreamBeginCaptureToGraph(cap_st, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
+        glinalg_status bs = inner(cap_st, p0, p1, 1, h_in);
+        if (bs == GLINALG_SUCCESS) bs = inner(cap_st, p1, p0, 0, h_in);
+        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { fail(bs ? bs : GLINALG_ERROR_CUDA); break; }
         // outer body part 2 (after the inner node): reliable update and tail
-        if (cudaStreamBeginCaptureToGraph(cap_st, body_out, &n_in, nullptr, 1, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaStreamBeginCaptureToGraph(cap_st, body_out, &n_in, nullptr, 1, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         bs = reliable_seq(cap_st);
         if (bs == GLINALG_SUCCESS) k_mx_outer_tail<<<1, 32, 0, cap_st>>>(s, h_out);
-        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { status = bs ? bs : GLINALG_ERROR_CUDA; break; }
-        if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
-        if (cudaGraphLaunch(ex, st) != cudaSuccess) { status = GLINALG_ERROR_CUDA; break; }
+        if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { fail(bs ? bs : GLINALG_ERROR_CUDA); break; }
+        if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
+        if (cudaGraphLaunch(ex, st) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
     } while (0);
     if (status != GLINALG_SUCCESS) {
         cudaError_t e = cudaGetLastError();
         set_last_error(std::string("mixed CG graph: ") + cudaGetErrorString(e));
         cudaStreamSynchronize(st);
-        cleanup();
+        if (ex) cudaGraphExecDestroy(ex);
+        if (g) cudaGraphDestroy(g);
         return status;
     }
     tm.stop(st);
     GL_CUDA(cudaMemcpyAsync(&h, s, sizeof(h), cudaMemcpyDeviceToHost, st));
     GL_CUDA(cudaStreamSynchronize(st));
-    cleanup();
+    cudaGraphExecDestroy(ex);
+    cudaGraphDestroy(g);
     info->resSq = h.rsq_true;
     info->iter = h.k;
     info->success = h.status == GLINALG_SOLVE_CONVERGED ? 1 : 0;
@@ -608,7 +687,9 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     const double w = Fmt<S>::bytes, wr = Fmt<R>::bytes, wl = Fmt<LK>::bytes;
     // A: r(wr) p_old(w) links(2wl) -> p'(w) t(w); B: t(w) links(2wl) p'(w) r(2 wr) x_lo(16)
     const double per_iter = stag ? (6.0 * w + 4.0 * wl + 3.0 * wr + 16.0) : (6.0 * w + 2.0 * wl + 3.0 * wr + 16.0);
-    info->gbytes = ((double)h.k * per_iter * n + (double)h.n_reliable * (8.0 + 4.0 * 2) * 16.0 * n) * 1e-9;
+    // reliable update: x_hi r/w + x_lo r/w, FP64 operator (two passes), r_hi, r_lo, p
+    const double per_rel = 16.0 * 2 + 16.0 + 8.0 * 64.0 / 8.0 + 16.0 * 3 + 2 * wr + 4 * w;
+    info->gbytes = ((double)h.k * per_iter * n + (double)h.n_reliable * per_rel * n) * 1e-9;
     fill_name(info, name);
     return GLINALG_SUCCESS;
 }
@@ -624,9 +705,15 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
     if (!(delta > 0.0 && delta < 1.0)) delta = 0.1;
     glinalg_status s;
     switch (precision) {
-    case GLINALG_PREC_SINGLE: s = run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32"); break;
-    case GLINALG_PREC_HALF: s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16"); break;
-    case GLINALG_PREC_BFLOAT: s = run_mixed<__nv_bfloat162, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16"); break;
+    case GLINALG_PREC_SINGLE:
+        s = run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32", 1);
+        break;
+    case GLINALG_PREC_HALF:
+        s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16", 2);
+        break;
+    case GLINALG_PREC_BFLOAT:
+        s = run_mixed<__nv_bfloat162, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16", 3);
+        break;
     default: set_last_error("unknown precision"); return GLINALG_ERROR_INVALID_VALUE;
     }
     if (s != GLINALG_SUCCESS) return s;
@@ -649,14 +736,11 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
     return GLINALG_SUCCESS;
 }
 
-}  // namespace glinalg
-
 // ---------------------------------------------------------------- kernel timing hook
 
-namespace glinalg {
-
 template <class S, class R, class LK>
-static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, double ms[2], double bytes[2])
+static glinalg_status profile_inner(const glinalg_operator_s *op, int variant, int n_launch, double ms[2],
+                                    double bytes[2])
 {
     const long n = op->size;
     const int lx = op->lx, ly = op->ly;
@@ -666,33 +750,25 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, 
     S *p0, *p1, *t;
     LK *L;
     float2 *xlo;
-    double2 *ones;
     double *partials;
     MxDev *s;
-    const dim3 blk(kBX, kBY), grd((lx + kBX - 1) / kBX, (ly + kBY - 1) / kBY);
     GL_TRY(sc.alloc(&r, n));
     GL_TRY(sc.zeros(&p0, n));
     GL_TRY(sc.zeros(&p1, n));
     GL_TRY(sc.zeros(&t, n));
     GL_TRY(sc.alloc(&L, 2 * n));
     GL_TRY(sc.zeros(&xlo, n));
-    GL_TRY(sc.alloc(&ones, n));
-    GL_TRY(sc.alloc(&partials, (size_t)grd.x * grd.y));
-    GL_TRY(sc.alloc(&s, 1));
+    GL_TRY(sc.alloc(&partials, (size_t)max_tile_blocks(lx, ly)));
+    GL_TRY(sc.zeros(&s, 1));
     k_make_hop<LK><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
-    // r = 1 everywhere (any non-zero field gives a positive <p, A p>)
-    std::vector<double2> h1(n, cmk(1.0, 0.0));
-    GL_CUDA(cudaMemcpyAsync(ones, h1.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st));
-    k_copy_links<R><<<vgrid(n), 256, 0, st>>>(r, ones, n);
     GL_CUDA(cudaGetLastError());
-    // a state under which neither kernel early-exits or triggers an update: rsq = 0 makes
-    // alpha = 0 (the updates add zero but run in full), delta = eps = 0 never trigger.
+    const int cand = autotune<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, partials, st);
+    auto k = kernels_for<S, R, LK>(cand, lx % 32 == 0);
     MxDev h = {};
     h.beta = 0.5;
     h.scale = 1.0;
     h.rmax = 1e300;
     h.max_iter = 0x7fffffff;
-    GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
     EventTimer ta, tb;
     double sa = 0.0, sb = 0.0;
     const float mass = (float)op->mass;
@@ -700,10 +776,10 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, 
         GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
         S *po = (it & 1) ? p1 : p0, *pn = (it & 1) ? p0 : p1;
         ta.start(st);
-        k_mx_A_stag<S, R, LK><<<grd, blk, 0, st>>>(r, po, pn, t, L, mass, lx, ly, s, partials);
+        k.A<<<k.grid(lx, ly), k.block(), 0, st>>>(r, po, pn, t, L, mass, 0.f, lx, ly, s, partials, 0, 0);
         ta.stop(st);
         tb.start(st);
-        k_mx_B_stag<S, R, LK><<<grd, blk, 0, st>>>(t, pn, r, xlo, L, mass, 0.f, lx, ly, 0, s, partials);
+        k.B<<<k.grid(lx, ly), k.block(), 0, st>>>(t, pn, r, xlo, L, mass, 0.f, lx, ly, 0, s, partials, 0, 0);
         tb.stop(st);
         GL_CUDA(cudaGetLastError());
         const double a = ta.ms(), b = tb.ms();
@@ -722,6 +798,13 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int n_launch, 
     return GLINALG_SUCCESS;
 }
 
+int tuned_tile(const glinalg_operator_s *op, int variant)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(std::make_tuple(op->device, op->lx, op->ly, variant));
+    return it == g_tuned.end() ? -1 : it->second;
+}
+
 }  // namespace glinalg
 
 extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision, int n_launch,
@@ -732,9 +815,14 @@ extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int
     if (op->kind != GLINALG_OP_STAGGERED_NORMAL) return GLINALG_ERROR_UNSUPPORTED_OP;
     GL_TRY(ensure_device());
     switch (precision) {
-    case GLINALG_PREC_SINGLE: return profile_inner<float2, float2, float2>(op, n_launch, ms, bytes);
-    case GLINALG_PREC_HALF: return profile_inner<__half2, float2, __half2>(op, n_launch, ms, bytes);
-    case GLINALG_PREC_BFLOAT: return profile_inner<__nv_bfloat162, float2, float2>(op, n_launch, ms, bytes);
+    case GLINALG_PREC_SINGLE: return profile_inner<float2, float2, float2>(op, 1, n_launch, ms, bytes);
+    case GLINALG_PREC_HALF: return profile_inner<__half2, float2, __half2>(op, 2, n_launch, ms, bytes);
+    case GLINALG_PREC_BFLOAT: return profile_inner<__nv_bfloat162, float2, float2>(op, 3, n_launch, ms, bytes);
     default: return GLINALG_ERROR_INVALID_VALUE;
     }
+}
+
+extern "C" int glinalg_tuned_tile(glinalg_operator op, int precision)
+{
+    return op ? glinalg::tuned_tile(op, precision) : -1;
 }

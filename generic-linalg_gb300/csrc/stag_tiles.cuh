@@ -1,0 +1,179 @@
+// stag_tiles.cuh -- register-tiled stencil kernels for the inner iterations of the
+// mixed-precision CG on the staggered normal operator D^dagger D (+ sigma).
+//
+// Thread block: 32 x BY threads; thread (tx, ty) owns column x = X0 + tx and the NY
+// consecutive rows y = Y0 + ty*NY + j, j = 0..NY-1, so a block covers a 32 x (BY*NY) tile.
+// The thread loads its column for rows -1..NY (NY+2 values), which gives every y-neighbour
+// from registers; x-neighbours come from the adjacent lanes by warp shuffle (only lanes 0
+// and 31 load across the warp edge), or by direct loads when lx is not a multiple of 32.
+// Row indices are wrapped modulo ly, so partial tiles and lattices smaller than a tile are
+// handled; rows past ly are loaded (wrapped) but neither stored nor reduced.
+//
+// Reductions: each thread sums its rows in FP32, the warp in FP32, the block in FP64, and the
+// grid in FP64 (one partial per block, summed by the last block in block order).
+#pragma once
+
+#include "common.cuh"
+
+namespace glinalg {
+
+template <class S>
+struct Fmt;
+template <>
+struct Fmt<float2> {
+    static __device__ __forceinline__ float2 ld(const float2 *p, long i) { return p[i]; }
+    static __device__ __forceinline__ void st(float2 *p, long i, float2 v) { p[i] = v; }
+    static __host__ __device__ __forceinline__ float2 from(double2 v) { return make_float2((float)v.x, (float)v.y); }
+    static constexpr int bytes = 8;
+};
+template <>
+struct Fmt<__half2> {
+    static __device__ __forceinline__ float2 ld(const __half2 *p, long i) { return __half22float2(p[i]); }
+    static __device__ __forceinline__ void st(__half2 *p, long i, float2 v) { p[i] = __float22half2_rn(v); }
+    static __device__ __forceinline__ __half2 from(double2 v) { return __floats2half2_rn((float)v.x, (float)v.y); }
+    static constexpr int bytes = 4;
+};
+template <>
+struct Fmt<__nv_bfloat162> {
+    static __device__ __forceinline__ float2 ld(const __nv_bfloat162 *p, long i) { return __bfloat1622float2(p[i]); }
+    static __device__ __forceinline__ void st(__nv_bfloat162 *p, long i, float2 v) { p[i] = __float22bfloat162_rn(v); }
+    static __device__ __forceinline__ __nv_bfloat162 from(double2 v) { return __floats2bfloat162_rn((float)v.x, (float)v.y); }
+    static constexpr int bytes = 4;
+};
+
+__device__ __forceinline__ float2 fadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 fsub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 fscale(float s, float2 a) { return make_float2(s * a.x, s * a.y); }
+// a * b
+__device__ __forceinline__ float2 fmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// conj(a) * b
+__device__ __forceinline__ float2 fmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x); }
+__device__ __forceinline__ float fn2(float2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ float2 shfl_down2(float2 v, int d)
+{
+    return make_float2(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d));
+}
+__device__ __forceinline__ float2 shfl_up2(float2 v, int d)
+{
+    return make_float2(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d));
+}
+
+// Grid sum of K floats per thread: FP32 within a warp, FP64 across warps and blocks.
+// Returns true in all threads of the last block to arrive; the totals are then in out[]
+// of its first thread.  partials: K * (number of blocks) doubles; *counter is 0 on entry
+// and left 0.
+template <int K, int NT>
+__device__ __forceinline__ bool grid_sum_f(float (&vf)[K], double *partials, unsigned *counter,
+                                           double (&out)[K])
+{
+    __shared__ double sm[K][NT / 32];
+    __shared__ unsigned ticket;
+    const unsigned tid = flat_tid(), bid = flat_bid(), nbk = flat_nblocks();
+    const int lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) vf[j] += __shfl_down_sync(0xffffffffu, vf[j], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < K; j++) sm[j][warp] = (double)vf[j];
+    }
+    __syncthreads();
+    if (tid == 0) {
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            double s = 0.0;
+            for (int w = 0; w < NT / 32; w++) s += sm[j][w];
+            partials[(size_t)j * nbk + bid] = s;
+        }
+        __threadfence();
+        ticket = atomicAdd(counter, 1u);
+    }
+    __syncthreads();
+    if (ticket != nbk - 1) return false;
+    __threadfence();
+    double s[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) s[j] = 0.0;
+    for (unsigned b = tid; b < nbk; b += NT) {
+#pragma unroll
+        for (int j = 0; j < K; j++) s[j] += __ldcg(partials + (size_t)j * nbk + b);
+    }
+    block_sum<K, NT>(s);
+#pragma unroll
+    for (int j = 0; j < K; j++) out[j] = s[j];
+    if (tid == 0) *counter = 0u;
+    return true;
+}
+
+__device__ __forceinline__ int wrapi(int v, int n)
+{
+    v %= n;
+    return v < 0 ? v + n : v;
+}
+
+// Loads the tile column of field f (rows -1..NY, wrapped) for a thread, optionally combined
+// as a + beta * b (the CG direction update p' = r + beta p) when B is non-null.
+template <int NY, class SA, class SB>
+__device__ __forceinline__ void load_col(float2 (&c)[NY + 2], const SA *a, const SB *b, float beta,
+                                         int x, int ybase, int lx, int ly)
+{
+#pragma unroll
+    for (int j = 0; j < NY + 2; j++) {
+        const long i = (long)wrapi(ybase + j - 1, ly) * lx + x;
+        float2 v = Fmt<SA>::ld(a, i);
+        if (b) v = fadd(v, fscale(beta, Fmt<SB>::ld(b, i)));
+        c[j] = v;
+    }
+}
+
+// Staggered hopping sum at the NY rows of a thread's column:
+//   hs_j = h_x(x,y) f(x+1,y) - h_x(x-1,y)^* f(x-1,y) + h_y(x,y) f(x,y+1) - h_y(x,y-1)^* f(x,y-1)
+// c: the column of f (rows -1..NY); xm / xp: f at columns x-1 / x+1 for rows 0..NY-1.
+template <int NY, class LK>
+__device__ __forceinline__ void hop_col(float2 (&hs)[NY], const float2 (&c)[NY + 2],
+                                        const float2 (&fxm)[NY], const float2 (&fxp)[NY],
+                                        const LK *H, int x, int xm, int ybase, int lx, int ly)
+{
+    float2 hy_prev = Fmt<LK>::ld(H, 2 * ((long)wrapi(ybase - 1, ly) * lx + x) + 1);
+#pragma unroll
+    for (int j = 0; j < NY; j++) {
+        const long row = (long)wrapi(ybase + j, ly) * lx;
+        const float2 hx = Fmt<LK>::ld(H, 2 * (row + x));
+        const float2 hy = Fmt<LK>::ld(H, 2 * (row + x) + 1);
+        const float2 hxm = Fmt<LK>::ld(H, 2 * (row + xm));
+        float2 s = fmul(hx, fxp[j]);
+        s = fsub(s, fmulc(hxm, fxm[j]));
+        s = fadd(s, fmul(hy, c[j + 2]));
+        s = fsub(s, fmulc(hy_prev, c[j]));
+        hs[j] = s;
+        hy_prev = hy;
+    }
+}
+
+// x-neighbour columns of the tile column c: by shuffle within the warp when XS (lx a
+// multiple of 32), with the two warp-edge lanes computing their outside neighbour through
+// `edge(col, j)`; otherwise every lane uses `edge`.
+template <int NY, bool XS, class F>
+__device__ __forceinline__ void x_neighbours(float2 (&fxm)[NY], float2 (&fxp)[NY],
+                                             const float2 (&c)[NY + 2], int lane, int xm, int xp,
+                                             F edge)
+{
+#pragma unroll
+    for (int j = 0; j < NY; j++) {
+        if (XS) {
+            float2 up = shfl_down2(c[j + 1], 1);   // value of lane+1 -> column x+1
+            float2 dn = shfl_up2(c[j + 1], 1);     // value of lane-1 -> column x-1
+            if (lane == 31) up = edge(xp, j);
+            if (lane == 0) dn = edge(xm, j);
+            fxp[j] = up;
+            fxm[j] = dn;
+        } else {
+            fxp[j] = edge(xp, j);
+            fxm[j] = edge(xm, j);
+        }
+    }
+}
+
+}  // namespace glinalg

@@ -243,6 +243,10 @@ glinalg_status glinalg_staggered_action_grad(glinalg_operator op, const double *
  * op must be GLINALG_OP_STAGGERED_NORMAL; precision SINGLE, HALF or BFLOAT. */
 glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision, int n_launch,
                                              double ms[2], double bytes[2]);
+/* Tile shape the autotuner picked for op's lattice and precision (an index into the
+ * library's candidate list: 0 = 32x16, 1 = 32x32, 2 = 32x32 (4 rows of 8), 3 = 32x32
+ * (16 rows of 2) sites per block), or -1 if no mixed solve has run on this lattice yet. */
+int glinalg_tuned_tile(glinalg_operator op, int precision);
 
 /* ---- inputs the way the reference's tests make them (host side) ----
  * A generator is one std::mt19937 stream (as `std::mt19937 generator(seed)` in the tests);
