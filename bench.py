@@ -4,9 +4,8 @@ exp(i theta) with theta uniform in (-pi, pi) and a complex Gaussian source (std:
 1337, the reference tests' generators), x0 = 0.
 
 One step = one complete solve with the inputs resident in HBM.  The headline arm is the
-mixed-precision CG (FP16-storage / FP32-arithmetic inner iterations, FP64 reliable updates);
-the FP32-inner, BF16-storage and plain FP64 GPU CG are timed on the same system and reported
-beside it.  Between steps the L2 is flushed by writing a 512 MiB buffer (outside the events).
+mixed-precision CG (FP32 inner iterations, FP64 reliable updates); the FP16- and BF16-storage
+variants and the plain FP64 GPU CG are timed on the same system and reported beside it.  Between steps the L2 is flushed by writing a 512 MiB buffer (outside the events).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -38,8 +37,8 @@ MAX_ITER = 100000
 # measured with the reference's own minv_vector_cg; the GPU FP64 CG reproduces the count.
 REF_ITERS = 2093
 METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB300; HBM GB/s"
-HEADLINE = ("fp16", 2)
-VARIANTS = [("fp16", 2), ("fp32", 1), ("bf16", 3)]
+HEADLINE = ("fp32", 1)
+VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 
 
 def peaks():
@@ -177,6 +176,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--ref-iters", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variants", default="fp32,fp16,bf16,fp64",
+                    help="comma list of the variants to time besides the headline (fp32)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only time the two inner-iteration kernels of the headline variant "
                          "(a small case for ncu captures)")
@@ -237,7 +238,8 @@ def main():
     results = {}
     clocks = ClockSampler(local)
     head_name, head_prec = HEADLINE
-    for name, prec in [HEADLINE] + [v for v in VARIANTS if v != HEADLINE]:
+    wanted = set(args.variants.split(","))
+    for name, prec in [HEADLINE] + [v for v in VARIANTS if v != HEADLINE and v[0] in wanted]:
         for _ in range(args.warmup):
             solve(prec)
         barrier()
@@ -253,9 +255,10 @@ def main():
             clk = clocks.stop()
         results[name] = (times, infos)
     # the plain FP64 GPU CG (reference recurrence) on the same system
-    solve(0)
-    t64 = [solve(0) for _ in range(max(1, args.fp64_steps))]
-    results["fp64"] = ([t for t, _ in t64], [i for _, i in t64])
+    if "fp64" in wanted:
+        solve(0)
+        t64 = [solve(0) for _ in range(max(1, args.fp64_steps))]
+        results["fp64"] = ([t for t, _ in t64], [i for _, i in t64])
 
     head_times, head_infos = results[head_name]
     ms = statistics.mean(head_times)
@@ -299,12 +302,12 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    cb = None if args.no_cpu_baseline else cpu_baseline(results["fp64"][1][0].iter)
+    cb = None if args.no_cpu_baseline else cpu_baseline(results["fp64"][1][0].iter if "fp64" in results else REF_ITERS)
     hi = head_infos[-1]
-    t64m = statistics.mean(results["fp64"][0])
+    t64m = statistics.mean(results["fp64"][0]) if "fp64" in results else float("nan")
     relres = (torch.linalg.vector_norm(bd - Ax) / torch.linalg.vector_norm(bd)).item()
     variants = {}
-    for name in ("fp16", "fp32", "bf16", "fp64"):
+    for name in [n for n in ("fp32", "fp16", "bf16", "fp64") if n in results]:
         ts, ins = results[name]
         variants[name] = {"ms": round(statistics.mean(ts), 3), "iters": ins[-1].iter,
                           "converged": bool(ins[-1].success),
@@ -315,7 +318,7 @@ def main():
     line = {
         "metric": METRIC, "value": round(ms_max, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f16-storage/f32-accumulate (fp64 reliable updates)",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (inner iterations; fp64 reliable updates and solution)",
         "data": "synthetic (seeded U(1) links and Gaussian source, std::mt19937 1337)",
         "config": {"workload": "staggered normal-equation CG to FP64-true relres 1e-10, 1024x1024, m=0.01, x0=0",
                    "lattice": [LX, LY], "mass": MASS, "tol": EPS, "variant": f"{head_name} inner + fp64 reliable updates",
@@ -325,10 +328,11 @@ def main():
                    "speedup_vs_fp64_gpu": round(t64m / ms, 2), "variants": variants},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "traffic": None,
-                     "kernel": f"k_mx_B_stag<{head_name}> (D^dagger t + x/r update + |r|^2)",
+                     "kernel": f"k_stB<{head_name}> (D^dagger t + x/r update + |r|^2, register-tiled)",
                      "bytes_per_launch": kbytes[1], "ms_per_launch": round(kms[1], 5),
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel_A": {"achieved": round(achieved_a, 1), "bytes_per_launch": kbytes[0],
+                     "kernel_A": {"name": f"k_stA<{head_name}> (p = r + beta p, D p, |Dp|^2)",
+                                  "achieved": round(achieved_a, 1), "bytes_per_launch": kbytes[0],
                                   "ms_per_launch": round(kms[0], 5)}},
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": int(Uh.nbytes + bh.nbytes + xh.nbytes),
                 "d2h_bytes_per_step": int(xh.nbytes)},

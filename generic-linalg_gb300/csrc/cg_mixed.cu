@@ -30,6 +30,7 @@
 // loop itself when an update is due or the solve has stopped.
 
 #include <cmath>
+#include <cstddef>
 #include <map>
 #include <mutex>
 #include <string>
@@ -142,7 +143,7 @@ k_stA(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_ne
             Fmt<S>::st(p_new, i, pc);
             Fmt<S>::st(t, i, tv);
             // reduce what was stored, so that alpha matches the rounded vectors
-            const float2 pq = Fmt<S>::ld(p_new, i), tq = Fmt<S>::ld(t, i);
+            const float2 pq = Fmt<S>::round(pc), tq = Fmt<S>::round(tv);
             acc[0] += fn2(tq) + sigma * fn2(pq);
         }
     }
@@ -184,8 +185,9 @@ k_stB(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
             const float2 pc = Fmt<S>::ld(p, i);
             const float2 av = fadd(fsub(fscale(mass, c[j + 1]), hs[j]), fscale(sigma, pc));
             xlo[i] = fadd(xlo[i], fscale(alpha, pc));
-            Fmt<R>::st(r, i, fsub(Fmt<R>::ld(r, i), fscale(alpha, av)));
-            acc[0] += fn2(Fmt<R>::ld(r, i));
+            const float2 rn = Fmt<R>::round(fsub(Fmt<R>::ld(r, i), fscale(alpha, av)));
+            Fmt<R>::st(r, i, rn);
+            acc[0] += fn2(rn);
         }
     }
     double out[1];
@@ -221,7 +223,7 @@ k_lapA(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_n
         const float2 av = fsub(fscale(diag, pc), hs);
         Fmt<S>::st(p_new, i, pc);
         Fmt<S>::st(Ap, i, av);
-        const float2 pq = Fmt<S>::ld(p_new, i), aq = Fmt<S>::ld(Ap, i);
+        const float2 pq = Fmt<S>::round(pc), aq = Fmt<S>::round(av);
         acc[0] = pq.x * aq.x + pq.y * aq.y;  // Re <p, Ap>
     }
     double out[1];
@@ -244,8 +246,9 @@ k_lapB(const S *__restrict__ Ap, const S *__restrict__ p, R *__restrict__ r,
         const long i = (long)y * lx + x;
         const float2 pc = Fmt<S>::ld(p, i);
         xlo[i] = fadd(xlo[i], fscale(alpha, pc));
-        Fmt<R>::st(r, i, fsub(Fmt<R>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i))));
-        acc[0] = fn2(Fmt<R>::ld(r, i));
+        const float2 rn = Fmt<R>::round(fsub(Fmt<R>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i))));
+        Fmt<R>::st(r, i, rn);
+        acc[0] = fn2(rn);
     }
     double out[1];
     if (grid_sum_f<1, kLNT>(acc, partials, &s->cnt[1], out) && threadIdx.x == 0 && threadIdx.y == 0)
@@ -353,7 +356,7 @@ __global__ void k_mx_R4(S *p0, const S *p1, const R *__restrict__ rlo, long n, c
         Fmt<S>::st(p0, i, fsub(Fmt<S>::ld(plo, i), fscale(rp, Fmt<R>::ld(rlo, i))));
 }
 
-__global__ void k_mx_outer_tail(MxDev *s, cudaGraphConditionalHandle outer)
+__global__ void k_mx_outer_tail(MxDev *s, cudaGraphConditionalHandle outer, int use_cond)
 {
     if (threadIdx.x != 0) return;
     s->outer++;
@@ -362,7 +365,7 @@ __global__ void k_mx_outer_tail(MxDev *s, cudaGraphConditionalHandle outer)
         s->done = 1;
     }
     if (s->done) {
-        cudaGraphSetConditional(outer, 0);
+        if (use_cond) cudaGraphSetConditional(outer, 0);
         return;
     }
     s->reliable = 0;
@@ -593,16 +596,16 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
 
     // one inner iteration reading the direction from pold and writing it to pnew
     auto inner = [&](cudaStream_t cs, S *pold, S *pnew, int dir_parity,
-                     cudaGraphConditionalHandle hin) -> glinalg_status {
+                     cudaGraphConditionalHandle hin, int uc) -> glinalg_status {
         if (stag) {
             sk.A<<<sk.grid(lx, ly), sk.block(), 0, cs>>>(r, pold, pnew, t, L, (float)op->mass, (float)sigma,
-                                                        lx, ly, s, partials, hin, 1);
+                                                        lx, ly, s, partials, hin, uc);
             sk.B<<<sk.grid(lx, ly), sk.block(), 0, cs>>>(t, pnew, r, xlo, L, (float)op->mass, (float)sigma,
-                                                        lx, ly, dir_parity, s, partials, hin, 1);
+                                                        lx, ly, dir_parity, s, partials, hin, uc);
         } else {
             const float diag = (float)(4.0 + op->mass + sigma);
-            k_lapA<S, R, LK><<<lgrd, lblk, 0, cs>>>(r, pold, pnew, t, L, diag, lx, ly, s, partials, hin, 1);
-            k_lapB<S, R><<<lgrd, lblk, 0, cs>>>(t, pnew, r, xlo, lx, ly, dir_parity, s, partials, hin, 1);
+            k_lapA<S, R, LK><<<lgrd, lblk, 0, cs>>>(r, pold, pnew, t, L, diag, lx, ly, s, partials, hin, uc);
+            k_lapB<S, R><<<lgrd, lblk, 0, cs>>>(t, pnew, r, xlo, lx, ly, dir_parity, s, partials, hin, uc);
         }
         GL_CUDA(cudaGetLastError());
         return GLINALG_SUCCESS;
@@ -620,7 +623,30 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     auto fail = [&](glinalg_status e) {
         if (status == GLINALG_SUCCESS) status = e;
     };
+    if (!use_graphs()) {
+        // host-driven: the same kernels in the same order, flags read after every launch pair
+        // f[0] = done, f[2] = reliable (MxDev keeps done, status, reliable adjacent)
+        static_assert(offsetof(MxDev, reliable) == offsetof(MxDev, done) + 2 * sizeof(int),
+                      "flag layout");
+        for (long outer = 0;; outer++) {
+            int hflags[3];
+            GL_CUDA(cudaMemcpyAsync(hflags, &s->done, sizeof(hflags), cudaMemcpyDeviceToHost, st));
+            GL_CUDA(cudaStreamSynchronize(st));
+            if (hflags[0]) break;
+            for (long it = 0;; it++) {
+                GL_TRY(inner(st, (it & 1) ? p1 : p0, (it & 1) ? p0 : p1, (it & 1) ? 0 : 1, 0, 0));
+                int f[3];
+                GL_CUDA(cudaMemcpyAsync(f, &s->done, sizeof(f), cudaMemcpyDeviceToHost, st));
+                GL_CUDA(cudaStreamSynchronize(st));
+                if (f[0] || f[2]) break;  // done or reliable
+            }
+            GL_TRY(reliable_seq(st));
+            k_mx_outer_tail<<<1, 32, 0, st>>>(s, 0, 0);
+            GL_CUDA(cudaGetLastError());
+        }
+    }
     do {
+        if (!use_graphs()) break;
         cudaGraphConditionalHandle h_out, h_in;
         if (cudaGraphCreate(&g, 0) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         if (cudaGraphConditionalHandleCreate(&h_out, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
@@ -652,13 +678,13 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         cudaGraph_t body_in = ip.conditional.phGraph_out[0];
         // inner body: two iterations with the direction buffers swapped
         if (cudaStreamBeginCaptureToGraph(cap_st, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
-        glinalg_status bs = inner(cap_st, p0, p1, 1, h_in);
-        if (bs == GLINALG_SUCCESS) bs = inner(cap_st, p1, p0, 0, h_in);
+        glinalg_status bs = inner(cap_st, p0, p1, 1, h_in, 1);
+        if (bs == GLINALG_SUCCESS) bs = inner(cap_st, p1, p0, 0, h_in, 1);
         if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { fail(bs ? bs : GLINALG_ERROR_CUDA); break; }
         // outer body part 2 (after the inner node): reliable update and tail
         if (cudaStreamBeginCaptureToGraph(cap_st, body_out, &n_in, nullptr, 1, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         bs = reliable_seq(cap_st);
-        if (bs == GLINALG_SUCCESS) k_mx_outer_tail<<<1, 32, 0, cap_st>>>(s, h_out);
+        if (bs == GLINALG_SUCCESS) k_mx_outer_tail<<<1, 32, 0, cap_st>>>(s, h_out, 1);
         if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { fail(bs ? bs : GLINALG_ERROR_CUDA); break; }
         if (cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         if (cudaGraphLaunch(ex, st) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }

@@ -3,6 +3,7 @@
 
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <iostream>
 #include <mutex>
@@ -14,10 +15,13 @@ namespace glinalg {
 static thread_local std::string t_last_error;
 void set_last_error(const std::string &msg) { t_last_error = msg; }
 
-LoopGraph::~LoopGraph()
+bool use_graphs()
 {
-    if (ex_) cudaGraphExecDestroy(ex_);
-    if (g_) cudaGraphDestroy(g_);
+    static const bool on = [] {
+        const char *e = std::getenv("GLINALG_SOLVER_GRAPHS");
+        return !(e && e[0] == '0');
+    }();
+    return on;
 }
 
 __global__ void k_loop_guard(const int *done, cudaGraphConditionalHandle h)

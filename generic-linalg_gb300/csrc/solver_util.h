@@ -44,51 +44,68 @@ class Scratch {
     std::vector<void *> ptrs_;
 };
 
-// A CUDA graph holding one conditional WHILE node whose body is captured from `body`.
-// The body must end with a kernel that clears the condition once the solve is done.
-class LoopGraph {
-  public:
-    ~LoopGraph();
-    template <class F>
-    glinalg_status build(cudaStream_t st, F body)
-    {
-        GL_CUDA(cudaGraphCreate(&g_, 0));
-        GL_CUDA(cudaGraphConditionalHandleCreate(&h_, g_, 1, cudaGraphCondAssignDefault));
-        cudaGraphNodeParams np = {};
-        np.type = cudaGraphNodeTypeConditional;
-        np.conditional.handle = h_;
-        np.conditional.type = cudaGraphCondTypeWhile;
-        np.conditional.size = 1;
-        cudaGraphNode_t node;
-        GL_CUDA(cudaGraphAddNode(&node, g_, nullptr, nullptr, 0, &np));
-        cudaGraph_t bg = np.conditional.phGraph_out[0];
-        // capture on a private stream; the graph is launched on `st`
-        cudaStream_t cs = capture_stream();
-        (void)st;
-        GL_CUDA(cudaStreamBeginCaptureToGraph(cs, bg, nullptr, nullptr, 0,
-                                              cudaStreamCaptureModeThreadLocal));
-        glinalg_status s = body(cs, h_);
-        cudaGraph_t captured = nullptr;
-        cudaError_t e = cudaStreamEndCapture(cs, &captured);
-        if (s != GLINALG_SUCCESS) return s;
-        GL_CUDA(e);
-        GL_CUDA(cudaGraphInstantiate(&ex_, g_, 0));
-        return GLINALG_SUCCESS;
-    }
-    glinalg_status launch(cudaStream_t st)
-    {
-        GL_CUDA(cudaGraphLaunch(ex_, st));
-        return GLINALG_SUCCESS;
-    }
-
-  private:
-    cudaGraph_t g_ = nullptr;
-    cudaGraphExec_t ex_ = nullptr;
-    cudaGraphConditionalHandle h_ = 0;
-};
+// Whether solver loops run as CUDA graphs with conditional WHILE nodes (the default) or from
+// a host loop that launches the same kernels and reads the stop flag after every pass
+// (environment GLINALG_SOLVER_GRAPHS=0; used for per-kernel profiling, since profilers do not
+// resolve kernel nodes inside conditional graphs, and as a fallback).
+bool use_graphs();
 
 // Ends the enclosing while loop once *done is set (one thread).
 __global__ void k_loop_guard(const int *done, cudaGraphConditionalHandle h);
+
+// Runs `body(stream)` (the kernels of one iteration, each returning early once *done is set)
+// until *done: as one CUDA graph with a conditional WHILE node whose body is captured from
+// `body` followed by k_loop_guard, or from a host loop.  Returns once the work is enqueued
+// (graph) or finished (host loop).
+template <class F>
+glinalg_status run_loop(cudaStream_t st, const int *done, F body)
+{
+    if (!use_graphs()) {
+        for (long pass = 0;; pass++) {
+            GL_TRY(body(st));
+            int h = 0;
+            GL_CUDA(cudaMemcpyAsync(&h, done, sizeof(int), cudaMemcpyDeviceToHost, st));
+            GL_CUDA(cudaStreamSynchronize(st));
+            if (h) return GLINALG_SUCCESS;
+        }
+    }
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    glinalg_status s = GLINALG_SUCCESS;
+    auto fail = [&](cudaError_t e, const char *what) {
+        set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+        s = GLINALG_ERROR_CUDA;
+    };
+    cudaError_t e;
+    do {
+        if ((e = cudaGraphCreate(&g, 0)) != cudaSuccess) { fail(e, "cudaGraphCreate"); break; }
+        if ((e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) { fail(e, "cudaGraphConditionalHandleCreate"); break; }
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if ((e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np)) != cudaSuccess) { fail(e, "cudaGraphAddNode"); break; }
+        cudaGraph_t bg = np.conditional.phGraph_out[0];
+        // capture on a private stream; the graph is launched on `st`
+        cudaStream_t cs = capture_stream();
+        if ((e = cudaStreamBeginCaptureToGraph(cs, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) { fail(e, "capture"); break; }
+        glinalg_status bs = body(cs);
+        if (bs == GLINALG_SUCCESS) k_loop_guard<<<1, 32, 0, cs>>>(done, h);
+        cudaGraph_t captured = nullptr;
+        e = cudaStreamEndCapture(cs, &captured);
+        if (bs != GLINALG_SUCCESS) { s = bs; break; }
+        if (e != cudaSuccess) { fail(e, "end capture"); break; }
+        if ((e = cudaGraphInstantiate(&ex, g, 0)) != cudaSuccess) { fail(e, "cudaGraphInstantiate"); break; }
+        if ((e = cudaGraphLaunch(ex, st)) != cudaSuccess) { fail(e, "cudaGraphLaunch"); break; }
+    } while (0);
+    // the executable graph may be destroyed while its launch is in flight
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    return s;
+}
 
 // Device copies of phi (in/out) and phi0 (in) for a solve; copies back on finish().
 struct Staged {

@@ -147,18 +147,15 @@ glinalg_status cg_fp64(const glinalg_operator_s *op, double2 *x, const double2 *
     GL_TRY(launch_norm2(r, n, partials, &s->cnt[2], &s->rsq, st));
 
     if (max_iter > 0) {
-        LoopGraph lg;
         const int vg = vec_grid(n);
-        GL_TRY(lg.build(st, [&](cudaStream_t cs, cudaGraphConditionalHandle hnd) -> glinalg_status {
+        GL_TRY(run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
             k_cg_alpha<<<nb, kRedThreads, 0, cs>>>(p, Ap, n, s, partials);
             k_cg_update<<<nb, kRedThreads, 0, cs>>>(x, r, p, Ap, n, s, partials);
             k_cg_xpay<<<vg, 256, 0, cs>>>(p, r, n, s);
             GL_TRY(launch_apply_sigma(op, Ap, p, tmp, sigma, &s->done, cs));
-            k_loop_guard<<<1, 32, 0, cs>>>(&s->done, hnd);
             GL_CUDA(cudaGetLastError());
             return GLINALG_SUCCESS;
         }));
-        GL_TRY(lg.launch(st));
     }
     // true residual (generic_cg.cpp:366-367)
     double *truersq;
@@ -362,9 +359,8 @@ glinalg_status bicgstab_fp64(const glinalg_operator_s *op, double2 *x, const dou
     GL_TRY(launch_apply(op, Ap, p, tmp, nullptr, st));
 
     if (max_iter > 0) {
-        LoopGraph lg;
         const int vg = vec_grid(n);
-        GL_TRY(lg.build(st, [&](cudaStream_t cs, cudaGraphConditionalHandle hnd) -> glinalg_status {
+        GL_TRY(run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
             k_bi_alpha<<<nb, kRedThreads, 0, cs>>>(r0, Ap, n, s, partials);
             k_bi_s<<<vg, 256, 0, cs>>>(sv, r, Ap, n, s);
             GL_TRY(launch_apply(op, As, sv, tmp, &s->done, cs));
@@ -372,11 +368,9 @@ glinalg_status bicgstab_fp64(const glinalg_operator_s *op, double2 *x, const dou
             k_bi_update<<<nb, kRedThreads, 0, cs>>>(x, r, p, sv, As, r0, n, s, partials);
             k_bi_p<<<vg, 256, 0, cs>>>(p, r, Ap, n, s);
             GL_TRY(launch_apply(op, Ap, p, tmp, &s->done, cs));
-            k_loop_guard<<<1, 32, 0, cs>>>(&s->done, hnd);
             GL_CUDA(cudaGetLastError());
             return GLINALG_SUCCESS;
         }));
-        GL_TRY(lg.launch(st));
     }
     double *truersq;
     GL_TRY(sc.alloc(&truersq, 1));
@@ -855,17 +849,14 @@ glinalg_status cg_m_fp64(const glinalg_operator_s *op, double2 *const *X_host, c
     GL_TRY(launch_apply(op, Ap, p, tmp, nullptr, st));
     GL_TRY(launch_norm2(r, n, partials, &s->cnt[2], &s->rsq, st));
     if (max_iter > 0) {
-        LoopGraph lg;
-        GL_TRY(lg.build(st, [&](cudaStream_t cs, cudaGraphConditionalHandle hnd) -> glinalg_status {
+        GL_TRY(run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
             k_cgm_beta<<<nb, kRedThreads, 0, cs>>>(p, Ap, n, s, partials);
             k_cgm_r<<<nb, kRedThreads, 0, cs>>>(r, Ap, n, s, partials);
             k_cgm_vec<<<vg, 256, 0, cs>>>(dX, dP, p, r, n, s);
             GL_TRY(launch_apply(op, Ap, p, tmp, &s->done, cs));
-            k_loop_guard<<<1, 32, 0, cs>>>(&s->done, hnd);
             GL_CUDA(cudaGetLastError());
             return GLINALG_SUCCESS;
         }));
-        GL_TRY(lg.launch(st));
     }
     GL_CUDA(cudaMemcpyAsync(&h, s, sizeof(h), cudaMemcpyDeviceToHost, st));
     // explicit residuals of the shifted systems in the caller's order (:561-572)

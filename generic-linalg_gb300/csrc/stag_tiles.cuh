@@ -24,6 +24,7 @@ struct Fmt<float2> {
     static __device__ __forceinline__ float2 ld(const float2 *p, long i) { return p[i]; }
     static __device__ __forceinline__ void st(float2 *p, long i, float2 v) { p[i] = v; }
     static __host__ __device__ __forceinline__ float2 from(double2 v) { return make_float2((float)v.x, (float)v.y); }
+    static __device__ __forceinline__ float2 round(float2 v) { return v; }
     static constexpr int bytes = 8;
 };
 template <>
@@ -31,6 +32,8 @@ struct Fmt<__half2> {
     static __device__ __forceinline__ float2 ld(const __half2 *p, long i) { return __half22float2(p[i]); }
     static __device__ __forceinline__ void st(__half2 *p, long i, float2 v) { p[i] = __float22half2_rn(v); }
     static __device__ __forceinline__ __half2 from(double2 v) { return __floats2half2_rn((float)v.x, (float)v.y); }
+    // the value a store followed by a load would give, without the memory round trip
+    static __device__ __forceinline__ float2 round(float2 v) { return __half22float2(__float22half2_rn(v)); }
     static constexpr int bytes = 4;
 };
 template <>
@@ -38,6 +41,7 @@ struct Fmt<__nv_bfloat162> {
     static __device__ __forceinline__ float2 ld(const __nv_bfloat162 *p, long i) { return __bfloat1622float2(p[i]); }
     static __device__ __forceinline__ void st(__nv_bfloat162 *p, long i, float2 v) { p[i] = __float22bfloat162_rn(v); }
     static __device__ __forceinline__ __nv_bfloat162 from(double2 v) { return __floats2bfloat162_rn((float)v.x, (float)v.y); }
+    static __device__ __forceinline__ float2 round(float2 v) { return __bfloat1622float2(__float22bfloat162_rn(v)); }
     static constexpr int bytes = 4;
 };
 
