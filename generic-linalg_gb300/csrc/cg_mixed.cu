@@ -129,7 +129,7 @@ k_stA(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_ne
         const long i = (long)wrapi(ybase + j, ly) * lx + col;
         return fadd(Fmt<R>::ld(r, i), fscale(beta, Fmt<S>::ld(p_old, i)));
     };
-    x_neighbours<NY, XS>(fxm, fxp, c, lane, xm, xp, edge);
+    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
     float2 hs[NY];
     hop_col<NY>(hs, c, fxm, fxp, H, xc, xm, ybase, lx, ly);
     float acc[1] = {0.f};
@@ -173,7 +173,7 @@ k_stB(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
     auto edge = [&](int col, int j) -> float2 {
         return Fmt<S>::ld(t, (long)wrapi(ybase + j, ly) * lx + col);
     };
-    x_neighbours<NY, XS>(fxm, fxp, c, lane, xm, xp, edge);
+    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
     float2 hs[NY];
     hop_col<NY>(hs, c, fxm, fxp, H, xc, xm, ybase, lx, ly);
     float acc[1] = {0.f};
@@ -700,8 +700,8 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     tm.stop(st);
     GL_CUDA(cudaMemcpyAsync(&h, s, sizeof(h), cudaMemcpyDeviceToHost, st));
     GL_CUDA(cudaStreamSynchronize(st));
-    cudaGraphExecDestroy(ex);
-    cudaGraphDestroy(g);
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
     info->resSq = h.rsq_true;
     info->iter = h.k;
     info->success = h.status == GLINALG_SOLVE_CONVERGED ? 1 : 0;

@@ -161,18 +161,25 @@ __device__ __forceinline__ void hop_col(float2 (&hs)[NY], const float2 (&c)[NY +
 // `edge(col, j)`; otherwise every lane uses `edge`.
 template <int NY, bool XS, class F>
 __device__ __forceinline__ void x_neighbours(float2 (&fxm)[NY], float2 (&fxp)[NY],
-                                             const float2 (&c)[NY + 2], int lane, int xm, int xp,
-                                             F edge)
+                                             const float2 (&c)[NY + 2], int lane, int xc, int xm,
+                                             int xp, F edge)
 {
+    // The edge values are loaded by every lane without a branch (lanes 1..30 load their own
+    // column, a cache hit, and discard it), so these loads issue together with the others
+    // instead of serialising behind divergent single-lane branches.
+    const int ecol = lane == 0 ? xm : (lane == 31 ? xp : xc);
+    float2 ev[NY];
+    if (XS) {
+#pragma unroll
+        for (int j = 0; j < NY; j++) ev[j] = edge(ecol, j);
+    }
 #pragma unroll
     for (int j = 0; j < NY; j++) {
         if (XS) {
             float2 up = shfl_down2(c[j + 1], 1);   // value of lane+1 -> column x+1
             float2 dn = shfl_up2(c[j + 1], 1);     // value of lane-1 -> column x-1
-            if (lane == 31) up = edge(xp, j);
-            if (lane == 0) dn = edge(xm, j);
-            fxp[j] = up;
-            fxm[j] = dn;
+            fxp[j] = lane == 31 ? ev[j] : up;
+            fxm[j] = lane == 0 ? ev[j] : dn;
         } else {
             fxp[j] = edge(xp, j);
             fxm[j] = edge(xm, j);
