@@ -199,6 +199,24 @@ k_stB(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
 
 constexpr int kLBX = 32, kLBY = 8, kLNT = kLBX * kLBY;
 
+// Inner iterations per pass of the inner WHILE body (even).  Every body pass is one device-side
+// graph launch; more iterations per pass amortise its latency, and the kernels of the
+// iterations after the stopping one return at once.
+constexpr int kInnerUnroll = 8;
+
+// Keeps the GPU busy for about `ns` nanoseconds (bounded: reads %globaltimer), so that work
+// queued behind it starts without host launch latency in between; used by the timing hook.
+__global__ void k_busy_wait(long long ns)
+{
+    long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    for (int i = 0; i < (1 << 22); i++) {
+        long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 >= ns) break;
+    }
+}
+
 // A: p' = r + beta p_old, Ap = (4 + m + sigma) p' - sum_mu [U p'(+mu) + U^* p'(-mu)]
 template <class S, class R, class LK>
 __global__ void __launch_bounds__(kLNT)
@@ -495,6 +513,7 @@ static int autotune(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p
         float tot = 0.f;
         for (int it = 0; it < 9; it++) {
             cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st);
+            k_busy_wait<<<1, 1, 0, st>>>(30000);  // keep launch latency out of the events
             cudaEventRecord(e0, st);
             k.A<<<k.grid(lx, ly), k.block(), 0, st>>>(r, p0, p1, t, L, (float)op->mass, 0.f, lx, ly, s, partials, 0, 0);
             k.B<<<k.grid(lx, ly), k.block(), 0, st>>>(t, p1, r, xlo, L, (float)op->mass, 0.f, lx, ly, 1, s, partials, 0, 0);
@@ -676,10 +695,12 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         cudaGraphNode_t n_in;
         if (cudaGraphAddNode(&n_in, body_out, nodes.data(), nullptr, nn, &ip) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         cudaGraph_t body_in = ip.conditional.phGraph_out[0];
-        // inner body: two iterations with the direction buffers swapped
+        // inner body: kInnerUnroll iterations, the direction buffers swapped between them
+        // (an even count, so every body pass starts from p0)
         if (cudaStreamBeginCaptureToGraph(cap_st, body_in, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
-        glinalg_status bs = inner(cap_st, p0, p1, 1, h_in, 1);
-        if (bs == GLINALG_SUCCESS) bs = inner(cap_st, p1, p0, 0, h_in, 1);
+        glinalg_status bs = GLINALG_SUCCESS;
+        for (int u = 0; u < kInnerUnroll && bs == GLINALG_SUCCESS; u++)
+            bs = (u & 1) ? inner(cap_st, p1, p0, 0, h_in, 1) : inner(cap_st, p0, p1, 1, h_in, 1);
         if (cudaStreamEndCapture(cap_st, &cap) != cudaSuccess || bs != GLINALG_SUCCESS) { fail(bs ? bs : GLINALG_ERROR_CUDA); break; }
         // outer body part 2 (after the inner node): reliable update and tail
         if (cudaStreamBeginCaptureToGraph(cap_st, body_out, &n_in, nullptr, 1, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
@@ -801,6 +822,9 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int variant, i
     for (int it = 0; it < n_launch + 2; it++) {
         GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
         S *po = (it & 1) ? p1 : p0, *pn = (it & 1) ? p0 : p1;
+        // queue both kernels behind a 50 us busy wait, so the events time the kernels and not
+        // the host's launch latency
+        k_busy_wait<<<1, 1, 0, st>>>(50000);
         ta.start(st);
         k.A<<<k.grid(lx, ly), k.block(), 0, st>>>(r, po, pn, t, L, mass, 0.f, lx, ly, s, partials, 0, 0);
         ta.stop(st);
