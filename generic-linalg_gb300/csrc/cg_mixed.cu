@@ -31,6 +31,7 @@
 
 #include <cmath>
 #include <cstddef>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -421,6 +422,300 @@ static int vgrid(long n)
     return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
+// ---------------------------------------------------------------- persistent inner loop
+//
+// One cooperative launch runs inner iterations until a reliable update is due: one block of
+// 32 x 32 threads per SM, each warp walking a static list of 32 x NY tiles (the tile code of
+// k_stA / k_stB), two grid-wide barriers per iteration (after the |t|^2 and after the |r|^2
+// partial sums), and every block summing the per-block partials in the same order, so all
+// blocks hold bitwise-identical scalars without a broadcast.  Fields written by other blocks
+// during the launch are read with ld.global.cg (L2), never through the non-coherent L1.
+
+struct GridSync {
+    unsigned arrive;
+    unsigned gen;
+    int error;
+    int pad;
+};
+
+__device__ __forceinline__ long long gtimer()
+{
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bound on one barrier wait; a wait that runs out raises g->error (the solve then reports
+// GLINALG_SOLVE_TIMEOUT) instead of spinning on.
+constexpr long long kBarrierTimeoutNs = 2000000000LL;
+
+// Grid-wide barrier for a co-resident grid (sense by generation counter).  Returns false in
+// every thread of the block once any block has given up waiting.
+__device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        volatile unsigned *vgen = &g->gen;
+        volatile int *verr = &g->error;
+        const unsigned my = *vgen;
+        int good = 1;
+        __threadfence();
+        const unsigned a = atomicAdd(&g->arrive, 1u);
+        if (a == nblocks - 1) {
+            atomicExch(&g->arrive, 0u);
+            __threadfence();
+            atomicAdd(&g->gen, 1u);
+        } else {
+            const long long t0 = gtimer();
+            while (*vgen == my) {
+                if (*verr) { good = 0; break; }
+                if (gtimer() - t0 > kBarrierTimeoutNs) {
+                    atomicExch(&g->error, 1);
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        if (*verr) good = 0;
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+template <class S>
+__device__ __forceinline__ float2 ldcg2(const S *p, long i);
+template <>
+__device__ __forceinline__ float2 ldcg2<float2>(const float2 *p, long i) { return __ldcg(p + i); }
+template <>
+__device__ __forceinline__ float2 ldcg2<__half2>(const __half2 *p, long i) { return __half22float2(__ldcg(p + i)); }
+template <>
+__device__ __forceinline__ float2 ldcg2<__nv_bfloat162>(const __nv_bfloat162 *p, long i)
+{
+    return __bfloat1622float2(__ldcg(p + i));
+}
+
+// Sum of the per-block partials in block order, identical in every block; all threads get it.
+__device__ __forceinline__ double grid_total(const double *part, unsigned nb, double *sm)
+{
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double v = 0.0;
+        for (unsigned b = threadIdx.x; b < nb; b += 32) v += __ldcg(part + b);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) sm[32] = v;
+    }
+    __syncthreads();
+    return sm[32];
+}
+
+// Block sum of one float per thread (FP32 within warps, FP64 across the 32 warps) written to
+// part[blockIdx.x] by the block's first thread.
+__device__ __forceinline__ void block_partial(float acc, double *part, double *sm)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) sm[threadIdx.y] = (double)acc;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double v = threadIdx.x < blockDim.y ? sm[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
+}
+
+template <class S, class R, class LK, int BY, int NY>
+__global__ void __launch_bounds__(32 * BY, 1)
+k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float mass, float sigma,
+          int lx, int ly, MxDev *s, GridSync *gs, double *partA, double *partB)
+{
+    __shared__ double sm[33];
+    if (s->done || s->reliable) return;
+    const unsigned nb = gridDim.x;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int ntx = lx / 32, ntiles = ntx * ((ly + NY - 1) / NY);
+    const int gw = blockIdx.x * BY + warp, nw = nb * BY;
+    double rsq = s->rsq, beta = s->beta, rmax = s->rmax, rn = 0.0;
+    const double scale = s->scale, delta = s->delta, eps = s->eps, bsqrt = sqrt(s->bsq);
+    int k = s->k;
+    const int max_iter = s->max_iter;
+    int j = 0, status = -1;
+    bool reliable = false;
+    for (;;) {
+        const S *pold = (j & 1) ? p1 : p0;
+        S *pnew = (j & 1) ? p0 : p1;
+        const float fb = (float)beta;
+        // ---- A: p' = r + beta p_old ; t = D p' ; |t|^2 + sigma |p'|^2
+        float acc = 0.f;
+        for (int tile = gw; tile < ntiles; tile += nw) {
+            const int x = (tile % ntx) * 32 + lane, ybase = (tile / ntx) * NY;
+            const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
+            float2 c[NY + 2];
+#pragma unroll
+            for (int q = 0; q < NY + 2; q++) {
+                const long i = (long)wrapi(ybase + q - 1, ly) * lx + x;
+                c[q] = fadd(ldcg2<R>(r, i), fscale(fb, ldcg2<S>(pold, i)));
+            }
+            float2 fxm[NY], fxp[NY];
+            auto edge = [&](int col, int q) -> float2 {
+                const long i = (long)wrapi(ybase + q, ly) * lx + col;
+                return fadd(ldcg2<R>(r, i), fscale(fb, ldcg2<S>(pold, i)));
+            };
+            x_neighbours<NY, true>(fxm, fxp, c, lane, x, xm, xp, edge);
+            float2 hs[NY];
+            hop_col<NY>(hs, c, fxm, fxp, H, x, xm, ybase, lx, ly);
+#pragma unroll
+            for (int q = 0; q < NY; q++) {
+                const int y = ybase + q;
+                if (y < ly) {
+                    const long i = (long)y * lx + x;
+                    const float2 pc = c[q + 1];
+                    const float2 tv = fadd(fscale(mass, pc), hs[q]);
+                    Fmt<S>::st(pnew, i, pc);
+                    Fmt<S>::st(t, i, tv);
+                    const float2 pq = Fmt<S>::round(pc), tq = Fmt<S>::round(tv);
+                    acc += fn2(tq) + sigma * fn2(pq);
+                }
+            }
+        }
+        block_partial(acc, partA, sm);
+        if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
+        const double pAp = grid_total(partA, nb, sm);
+        if (!(pAp > 0.0) || !isfinite(pAp)) {
+            status = pAp == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
+            break;
+        }
+        const float alpha = (float)(rsq / pAp);
+        // ---- B: Ap = D^dagger t + sigma p' ; x_lo += alpha p' ; r -= alpha Ap ; |r|^2
+        acc = 0.f;
+        for (int tile = gw; tile < ntiles; tile += nw) {
+            const int x = (tile % ntx) * 32 + lane, ybase = (tile / ntx) * NY;
+            const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
+            float2 c[NY + 2];
+#pragma unroll
+            for (int q = 0; q < NY + 2; q++) c[q] = ldcg2<S>(t, (long)wrapi(ybase + q - 1, ly) * lx + x);
+            float2 fxm[NY], fxp[NY];
+            auto edge = [&](int col, int q) -> float2 {
+                return ldcg2<S>(t, (long)wrapi(ybase + q, ly) * lx + col);
+            };
+            x_neighbours<NY, true>(fxm, fxp, c, lane, x, xm, xp, edge);
+            float2 hs[NY];
+            hop_col<NY>(hs, c, fxm, fxp, H, x, xm, ybase, lx, ly);
+#pragma unroll
+            for (int q = 0; q < NY; q++) {
+                const int y = ybase + q;
+                if (y < ly) {
+                    const long i = (long)y * lx + x;
+                    const float2 pc = ldcg2<S>(pnew, i);
+                    const float2 av = fadd(fsub(fscale(mass, c[q + 1]), hs[q]), fscale(sigma, pc));
+                    xlo[i] = fadd(__ldcg(xlo + i), fscale(alpha, pc));
+                    const float2 rv = Fmt<R>::round(fsub(ldcg2<R>(r, i), fscale(alpha, av)));
+                    Fmt<R>::st(r, i, rv);
+                    acc += fn2(rv);
+                }
+            }
+        }
+        block_partial(acc, partB, sm);
+        if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
+        rn = grid_total(partB, nb, sm);
+        j++;
+        k++;
+        if (!isfinite(rn)) { status = GLINALG_SOLVE_NONFINITE; break; }
+        const double rho = sqrt(rn) * scale;
+        if (rho > rmax) rmax = rho;
+        if (rho < delta * rmax || rho < eps * bsqrt || k >= max_iter) {
+            reliable = true;
+            break;
+        }
+        beta = rn / rsq;
+        rsq = rn;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+        s->k = k;
+        s->rmax = rmax;
+        s->rsq = rsq;
+        s->beta = beta;
+        s->rsq_new = rn;
+        s->parity = j & 1;
+        if (status >= 0) {
+            s->status = status;
+            s->done = 1;
+        }
+        if (reliable) s->reliable = 1;
+    }
+}
+
+template <class S, class R, class LK>
+struct PersistKernel {
+    using F = void (*)(const LK *, R *, S *, S *, S *, float2 *, float, float, int, int, MxDev *, GridSync *,
+                       double *, double *);
+    F f = nullptr;
+    int by = 0, ny = 0;
+    int grid = 0;
+};
+
+// Persistent-kernel shapes (warps per block, rows per thread); one block per SM.
+constexpr int kNumPersist = 3;
+static const int kPersistBY[kNumPersist] = {32, 16, 16};
+static const int kPersistNY[kNumPersist] = {4, 8, 4};
+
+template <class S, class R, class LK>
+static PersistKernel<S, R, LK> persist_cand(int c)
+{
+    PersistKernel<S, R, LK> pk;
+    pk.by = kPersistBY[c];
+    pk.ny = kPersistNY[c];
+    pk.f = c == 0 ? k_persist<S, R, LK, 32, 4> : (c == 1 ? k_persist<S, R, LK, 16, 8> : k_persist<S, R, LK, 16, 4>);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pk.f, 32 * pk.by, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        pk.f = nullptr;
+        return pk;
+    }
+    pk.grid = sm_count();
+    return pk;
+}
+
+// The persistent path serves lattices with lx a multiple of 32 and enough tiles to give
+// every warp of the grid work.
+static bool persist_applies(int lx, int ly)
+{
+    return lx % 32 == 0 && (long)(lx / 32) * ((ly + 7) / 8) >= (long)sm_count() * 16;
+}
+
+// GLINALG_PERSIST=0 disables the persistent inner loop (the per-kernel graph path runs).
+static bool persist_enabled()
+{
+    static const bool on = [] {
+        const char *e = std::getenv("GLINALG_PERSIST");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+// Cooperative launch of the persistent kernel (capturable into a graph).
+template <class S, class R, class LK>
+static cudaError_t launch_persist(const PersistKernel<S, R, LK> &pk, cudaStream_t st, const LK *H, R *r, S *p0,
+                                  S *p1, S *t, float2 *xlo, float mass, float sigma, int lx, int ly, MxDev *s,
+                                  GridSync *gs, double *partA, double *partB)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(pk.grid);
+    cfg.blockDim = dim3(32, pk.by);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, pk.f, H, r, p0, p1, t, xlo, mass, sigma, lx, ly, s, gs, partA, partB);
+}
+
 // ---------------------------------------------------------------- tile shapes and autotuning
 
 template <class S, class R, class LK>
@@ -535,6 +830,83 @@ static int autotune(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p
     return best;
 }
 
+static std::map<std::tuple<int, int, int, int>, int> g_ptuned;  // persistent shape per lattice
+
+static int persist_tuned(int lx, int ly, int variant)
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_ptuned.find(std::make_tuple(dev, lx, ly, variant));
+    return it == g_ptuned.end() ? 0 : it->second;
+}
+
+// Times every persistent shape on 16 CG iterations of A x = 1 (from r = 1, p = 0) and keeps
+// the fastest for this device, lattice and variant.
+template <class S, class R, class LK>
+static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p1, S *t, float2 *xlo,
+                             const LK *L, MxDev *s, GridSync *gs, double *partA, double *partB, cudaStream_t st)
+{
+    const int lx = op->lx, ly = op->ly;
+    const auto key = std::make_tuple(op->device, lx, ly, variant);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        if (g_ptuned.count(key)) return;
+    }
+    const long n = op->size;
+    std::vector<double2> ones(n, cmk(1.0, 0.0));
+    double2 *d1 = nullptr;
+    if (cudaMallocAsync((void **)&d1, sizeof(double2) * n, st) != cudaSuccess) return;
+    cudaMemcpyAsync(d1, ones.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st);
+    MxDev h = {};
+    h.rsq = (double)n;  // |r|^2 of r = 1
+    h.beta = 0.0;
+    h.scale = 1.0;
+    h.bsq = 1.0;
+    h.rmax = 1e300;
+    h.max_iter = 16;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int best = -1;
+    float best_ms = 1e30f;
+    for (int c = 0; c < kNumPersist; c++) {
+        const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(c);
+        if (!pk.f) continue;
+        float m = 1e30f;
+        for (int rep = 0; rep < 3; rep++) {
+            k_copy_links<R><<<vgrid(n), 256, 0, st>>>(r, d1, n);
+            cudaMemsetAsync(p0, 0, sizeof(S) * n, st);
+            cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st);
+            k_busy_wait<<<1, 1, 0, st>>>(30000);
+            cudaEventRecord(e0, st);
+            cudaError_t e = launch_persist(pk, st, L, r, p0, p1, t, xlo, (float)op->mass, 0.f, lx, ly, s, gs,
+                                           partA, partB);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            MxDev back;
+            cudaMemcpy(&back, s, sizeof(back), cudaMemcpyDeviceToHost);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess || back.done || back.k != 16) {
+                cudaGetLastError();
+                m = 1e30f;
+                break;
+            }
+            m = std::min(m, ms);
+        }
+        if (m < best_ms) {
+            best_ms = m;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFreeAsync(d1, st);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_ptuned[key] = best < 0 ? 0 : best;
+}
+
 // ---------------------------------------------------------------- driver
 
 template <class S, class R, class LK>
@@ -572,9 +944,18 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     GL_CUDA(cudaGetLastError());
 
     StagKernels<S, R, LK> sk{};
+    const bool use_persist = stag && persist_enabled() && persist_applies(lx, ly);
+    GridSync *gs = nullptr;
+    double *partA = nullptr, *partB = nullptr;
+    if (use_persist) {
+        GL_TRY(sc.zeros(&gs, 1));
+        GL_TRY(sc.alloc(&partA, sm_count()));
+        GL_TRY(sc.alloc(&partB, sm_count()));
+    }
     if (stag) {
         const int cand = autotune<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, partials, st);
         sk = kernels_for<S, R, LK>(cand, lx % 32 == 0);
+        if (use_persist) autotune_persist<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, gs, partA, partB, st);
         // the tuning runs wrote the work vectors: start from zero again
         GL_CUDA(cudaMemsetAsync(p0, 0, sizeof(S) * n, st));
         GL_CUDA(cudaMemsetAsync(p1, 0, sizeof(S) * n, st));
@@ -642,7 +1023,27 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     auto fail = [&](glinalg_status e) {
         if (status == GLINALG_SUCCESS) status = e;
     };
-    if (!use_graphs()) {
+    // Persistent path (staggered operator, large lattices): while (!done) { persistent inner
+    // loop ; reliable update ; tail } -- one cooperative kernel per reliable-update cycle.
+    bool persisted = false;
+    if (use_persist) {
+        const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(persist_tuned(lx, ly, variant));
+        if (pk.f) {
+            glinalg_status ps = run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
+                GL_CUDA(launch_persist(pk, cs, L, r, p0, p1, t, xlo, (float)op->mass, (float)sigma, lx, ly, s,
+                                       gs, partA, partB));
+                GL_TRY(reliable_seq(cs));
+                k_mx_outer_tail<<<1, 32, 0, cs>>>(s, 0, 0);
+                GL_CUDA(cudaGetLastError());
+                return GLINALG_SUCCESS;
+            });
+            if (ps == GLINALG_SUCCESS) persisted = true;
+            else cudaGetLastError();  // fall through to the per-kernel path below
+        }
+    }
+    if (persisted) {
+        // nothing more to enqueue
+    } else if (!use_graphs()) {
         // host-driven: the same kernels in the same order, flags read after every launch pair
         // f[0] = done, f[2] = reliable (MxDev keeps done, status, reliable adjacent)
         static_assert(offsetof(MxDev, reliable) == offsetof(MxDev, done) + 2 * sizeof(int),
@@ -665,7 +1066,7 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         }
     }
     do {
-        if (!use_graphs()) break;
+        if (!use_graphs() || persisted) break;
         cudaGraphConditionalHandle h_out, h_in;
         if (cudaGraphCreate(&g, 0) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
         if (cudaGraphConditionalHandleCreate(&h_out, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) { fail(GLINALG_ERROR_CUDA); break; }
@@ -723,6 +1124,10 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     GL_CUDA(cudaStreamSynchronize(st));
     if (ex) cudaGraphExecDestroy(ex);
     if (g) cudaGraphDestroy(g);
+    if (h.status == GLINALG_SOLVE_TIMEOUT) {
+        set_last_error("a grid-wide barrier of the persistent CG kernel timed out");
+        return GLINALG_ERROR_INTERNAL;
+    }
     info->resSq = h.rsq_true;
     info->iter = h.k;
     info->success = h.status == GLINALG_SOLVE_CONVERGED ? 1 : 0;

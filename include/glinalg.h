@@ -49,7 +49,9 @@ typedef enum glinalg_solve_status {
     GLINALG_SOLVE_CONVERGED = 0,
     GLINALG_SOLVE_MAX_ITER = 1,   /* the reference's success == false */
     GLINALG_SOLVE_BREAKDOWN = 2,  /* a recurrence denominator was exactly zero */
-    GLINALG_SOLVE_NONFINITE = 3   /* NaN or Inf appeared in a residual norm */
+    GLINALG_SOLVE_NONFINITE = 3,  /* NaN or Inf appeared in a residual norm */
+    GLINALG_SOLVE_TIMEOUT = 4     /* a bounded device-side wait gave up (the call reports
+                                     GLINALG_ERROR_INTERNAL) */
 } glinalg_solve_status;
 
 /* Operator kinds.  Each names the reference callback it replaces. */
