@@ -116,38 +116,10 @@ k_stA(const R *__restrict__ r, const S *__restrict__ p_old, S *__restrict__ p_ne
       MxDev *s, double *partials, cudaGraphConditionalHandle cond, int use_cond)
 {
     if (s->done || s->reliable) return;
-    const float beta = (float)s->beta;
-    const int lane = threadIdx.x;
-    const int x = blockIdx.x * 32 + lane;
+    const int x = blockIdx.x * 32 + threadIdx.x;
     const int ybase = blockIdx.y * (BY * NY) + threadIdx.y * NY;
-    const bool xval = x < lx;
-    const int xc = xval ? x : lx - 1;
-    const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
-    float2 c[NY + 2];
-    load_col<NY>(c, r, p_old, beta, xc, ybase, lx, ly);
-    float2 fxm[NY], fxp[NY];
-    auto edge = [&](int col, int j) -> float2 {
-        const long i = (long)wrapi(ybase + j, ly) * lx + col;
-        return fadd(Fmt<R>::ld(r, i), fscale(beta, Fmt<S>::ld(p_old, i)));
-    };
-    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
-    float2 hs[NY];
-    hop_col<NY>(hs, c, fxm, fxp, H, xc, xm, ybase, lx, ly);
-    float acc[1] = {0.f};
-#pragma unroll
-    for (int j = 0; j < NY; j++) {
-        const int y = ybase + j;
-        if (xval && y < ly) {
-            const long i = (long)y * lx + x;
-            const float2 pc = c[j + 1];
-            const float2 tv = fadd(fscale(mass, pc), hs[j]);
-            Fmt<S>::st(p_new, i, pc);
-            Fmt<S>::st(t, i, tv);
-            // reduce what was stored, so that alpha matches the rounded vectors
-            const float2 pq = Fmt<S>::round(pc), tq = Fmt<S>::round(tv);
-            acc[0] += fn2(tq) + sigma * fn2(pq);
-        }
-    }
+    float acc[1] = {tile_A<S, R, LK, NY, XS, false>(r, p_old, p_new, t, H, (float)s->beta, mass, sigma, lx, ly,
+                                                     threadIdx.x, x, x < lx, ybase)};
     double out[1];
     if (grid_sum_f<1, 32 * BY>(acc, partials, &s->cnt[0], out) && threadIdx.x == 0 && threadIdx.y == 0)
         mx_after_A(s, out[0], cond, use_cond);
@@ -161,36 +133,10 @@ k_stB(const S *__restrict__ t, const S *__restrict__ p, R *__restrict__ r,
       int dir_parity, MxDev *s, double *partials, cudaGraphConditionalHandle cond, int use_cond)
 {
     if (s->done || s->reliable) return;
-    const float alpha = (float)s->alpha;
-    const int lane = threadIdx.x;
-    const int x = blockIdx.x * 32 + lane;
+    const int x = blockIdx.x * 32 + threadIdx.x;
     const int ybase = blockIdx.y * (BY * NY) + threadIdx.y * NY;
-    const bool xval = x < lx;
-    const int xc = xval ? x : lx - 1;
-    const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
-    float2 c[NY + 2];
-    load_col<NY, S, S>(c, t, (const S *)nullptr, 0.f, xc, ybase, lx, ly);
-    float2 fxm[NY], fxp[NY];
-    auto edge = [&](int col, int j) -> float2 {
-        return Fmt<S>::ld(t, (long)wrapi(ybase + j, ly) * lx + col);
-    };
-    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
-    float2 hs[NY];
-    hop_col<NY>(hs, c, fxm, fxp, H, xc, xm, ybase, lx, ly);
-    float acc[1] = {0.f};
-#pragma unroll
-    for (int j = 0; j < NY; j++) {
-        const int y = ybase + j;
-        if (xval && y < ly) {
-            const long i = (long)y * lx + x;
-            const float2 pc = Fmt<S>::ld(p, i);
-            const float2 av = fadd(fsub(fscale(mass, c[j + 1]), hs[j]), fscale(sigma, pc));
-            xlo[i] = fadd(xlo[i], fscale(alpha, pc));
-            const float2 rn = Fmt<R>::round(fsub(Fmt<R>::ld(r, i), fscale(alpha, av)));
-            Fmt<R>::st(r, i, rn);
-            acc[0] += fn2(rn);
-        }
-    }
+    float acc[1] = {tile_B<S, R, LK, NY, XS, false>(t, p, r, xlo, H, (float)s->alpha, mass, sigma, lx, ly,
+                                                     threadIdx.x, x, x < lx, ybase)};
     double out[1];
     if (grid_sum_f<1, 32 * BY>(acc, partials, &s->cnt[1], out) && threadIdx.x == 0 && threadIdx.y == 0)
         mx_after_B(s, out[0], dir_parity, cond, use_cond);
@@ -485,18 +431,6 @@ __device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
     return ok != 0;
 }
 
-template <class S>
-__device__ __forceinline__ float2 ldcg2(const S *p, long i);
-template <>
-__device__ __forceinline__ float2 ldcg2<float2>(const float2 *p, long i) { return __ldcg(p + i); }
-template <>
-__device__ __forceinline__ float2 ldcg2<__half2>(const __half2 *p, long i) { return __half22float2(__ldcg(p + i)); }
-template <>
-__device__ __forceinline__ float2 ldcg2<__nv_bfloat162>(const __nv_bfloat162 *p, long i)
-{
-    return __bfloat1622float2(__ldcg(p + i));
-}
-
 // Sum of the per-block partials in block order, identical in every block; all threads get it.
 __device__ __forceinline__ double grid_total(const double *part, unsigned nb, double *sm)
 {
@@ -551,37 +485,9 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
         const float fb = (float)beta;
         // ---- A: p' = r + beta p_old ; t = D p' ; |t|^2 + sigma |p'|^2
         float acc = 0.f;
-        for (int tile = gw; tile < ntiles; tile += nw) {
-            const int x = (tile % ntx) * 32 + lane, ybase = (tile / ntx) * NY;
-            const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
-            float2 c[NY + 2];
-#pragma unroll
-            for (int q = 0; q < NY + 2; q++) {
-                const long i = (long)wrapi(ybase + q - 1, ly) * lx + x;
-                c[q] = fadd(ldcg2<R>(r, i), fscale(fb, ldcg2<S>(pold, i)));
-            }
-            float2 fxm[NY], fxp[NY];
-            auto edge = [&](int col, int q) -> float2 {
-                const long i = (long)wrapi(ybase + q, ly) * lx + col;
-                return fadd(ldcg2<R>(r, i), fscale(fb, ldcg2<S>(pold, i)));
-            };
-            x_neighbours<NY, true>(fxm, fxp, c, lane, x, xm, xp, edge);
-            float2 hs[NY];
-            hop_col<NY>(hs, c, fxm, fxp, H, x, xm, ybase, lx, ly);
-#pragma unroll
-            for (int q = 0; q < NY; q++) {
-                const int y = ybase + q;
-                if (y < ly) {
-                    const long i = (long)y * lx + x;
-                    const float2 pc = c[q + 1];
-                    const float2 tv = fadd(fscale(mass, pc), hs[q]);
-                    Fmt<S>::st(pnew, i, pc);
-                    Fmt<S>::st(t, i, tv);
-                    const float2 pq = Fmt<S>::round(pc), tq = Fmt<S>::round(tv);
-                    acc += fn2(tq) + sigma * fn2(pq);
-                }
-            }
-        }
+        for (int tile = gw; tile < ntiles; tile += nw)
+            acc += tile_A<S, R, LK, NY, true, true>(r, pold, pnew, t, H, fb, mass, sigma, lx, ly, lane,
+                                                    (tile % ntx) * 32 + lane, true, (tile / ntx) * NY);
         block_partial(acc, partA, sm);
         if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
         const double pAp = grid_total(partA, nb, sm);
@@ -592,33 +498,9 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
         const float alpha = (float)(rsq / pAp);
         // ---- B: Ap = D^dagger t + sigma p' ; x_lo += alpha p' ; r -= alpha Ap ; |r|^2
         acc = 0.f;
-        for (int tile = gw; tile < ntiles; tile += nw) {
-            const int x = (tile % ntx) * 32 + lane, ybase = (tile / ntx) * NY;
-            const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
-            float2 c[NY + 2];
-#pragma unroll
-            for (int q = 0; q < NY + 2; q++) c[q] = ldcg2<S>(t, (long)wrapi(ybase + q - 1, ly) * lx + x);
-            float2 fxm[NY], fxp[NY];
-            auto edge = [&](int col, int q) -> float2 {
-                return ldcg2<S>(t, (long)wrapi(ybase + q, ly) * lx + col);
-            };
-            x_neighbours<NY, true>(fxm, fxp, c, lane, x, xm, xp, edge);
-            float2 hs[NY];
-            hop_col<NY>(hs, c, fxm, fxp, H, x, xm, ybase, lx, ly);
-#pragma unroll
-            for (int q = 0; q < NY; q++) {
-                const int y = ybase + q;
-                if (y < ly) {
-                    const long i = (long)y * lx + x;
-                    const float2 pc = ldcg2<S>(pnew, i);
-                    const float2 av = fadd(fsub(fscale(mass, c[q + 1]), hs[q]), fscale(sigma, pc));
-                    xlo[i] = fadd(__ldcg(xlo + i), fscale(alpha, pc));
-                    const float2 rv = Fmt<R>::round(fsub(ldcg2<R>(r, i), fscale(alpha, av)));
-                    Fmt<R>::st(r, i, rv);
-                    acc += fn2(rv);
-                }
-            }
-        }
+        for (int tile = gw; tile < ntiles; tile += nw)
+            acc += tile_B<S, R, LK, NY, true, true>(t, pnew, r, xlo, H, alpha, mass, sigma, lx, ly, lane,
+                                                    (tile % ntx) * 32 + lane, true, (tile / ntx) * NY);
         block_partial(acc, partB, sm);
         if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
         rn = grid_total(partB, nb, sm);

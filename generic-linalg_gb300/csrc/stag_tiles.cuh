@@ -188,3 +188,179 @@ __device__ __forceinline__ void x_neighbours(float2 (&fxm)[NY], float2 (&fxp)[NY
 }
 
 }  // namespace glinalg
+
+namespace glinalg {
+
+// ---------------------------------------------------------------- tile bodies
+//
+// One thread's share of a 32 x NY tile: column x, rows ybase .. ybase+NY-1.  CG selects
+// ld.global.cg for the fields (needed when other blocks of the same launch write them).
+
+template <class T>
+__device__ __forceinline__ float2 ldcg2(const T *p, int i);
+template <>
+__device__ __forceinline__ float2 ldcg2<float2>(const float2 *p, int i) { return __ldcg(p + i); }
+template <>
+__device__ __forceinline__ float2 ldcg2<__half2>(const __half2 *p, int i) { return __half22float2(__ldcg(p + i)); }
+template <>
+__device__ __forceinline__ float2 ldcg2<__nv_bfloat162>(const __nv_bfloat162 *p, int i)
+{
+    return __bfloat1622float2(__ldcg(p + i));
+}
+
+template <bool CG, class T>
+__device__ __forceinline__ float2 ldf(const T *p, int i)
+{
+    if (CG) return ldcg2<T>(p, i);
+    return Fmt<T>::ld(p, i);
+}
+
+// Both hopping coefficients of a site (h_x, h_y stored adjacently) in one vector load.
+template <class LK>
+struct LinkPair;
+template <>
+struct LinkPair<float2> {
+    static __device__ __forceinline__ void ld(const float2 *H, int site, float2 &hx, float2 &hy)
+    {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(H) + site);
+        hx = make_float2(v.x, v.y);
+        hy = make_float2(v.z, v.w);
+    }
+    static __device__ __forceinline__ float2 ldx(const float2 *H, int site) { return __ldg(H + 2 * site); }
+};
+template <>
+struct LinkPair<__half2> {
+    static __device__ __forceinline__ void ld(const __half2 *H, int site, float2 &hx, float2 &hy)
+    {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(H) + site);
+        hx = __half22float2(*reinterpret_cast<const __half2 *>(&v.x));
+        hy = __half22float2(*reinterpret_cast<const __half2 *>(&v.y));
+    }
+    static __device__ __forceinline__ float2 ldx(const __half2 *H, int site) { return __half22float2(__ldg(H + 2 * site)); }
+};
+template <>
+struct LinkPair<__nv_bfloat162> {
+    static __device__ __forceinline__ void ld(const __nv_bfloat162 *H, int site, float2 &hx, float2 &hy)
+    {
+        const uint2 v = __ldg(reinterpret_cast<const uint2 *>(H) + site);
+        hx = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&v.x));
+        hy = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&v.y));
+    }
+    static __device__ __forceinline__ float2 ldx(const __nv_bfloat162 *H, int site)
+    {
+        return __bfloat1622float2(__ldg(H + 2 * site));
+    }
+};
+
+// Row offsets y*lx of rows ybase-1 .. ybase+NY, wrapped periodically (a compare and an add
+// in the usual case; a modulo only for lattices shorter than a tile).
+template <int NY>
+__device__ __forceinline__ void row_offsets(int (&off)[NY + 2], int ybase, int lx, int ly)
+{
+#pragma unroll
+    for (int q = 0; q < NY + 2; q++) {
+        int y = ybase + q - 1;
+        if (y < 0) y += ly;
+        if (y >= ly) {
+            y -= ly;
+            if (y >= ly) y %= ly;
+        }
+        off[q] = y * lx;
+    }
+}
+
+// Kernel-A share: p' = r + beta p_old ; t = D p' = m p' + hop(p') ; stores p', t and returns
+// sum |t|^2 + sigma |p'|^2 over the thread's rows (computed from the rounded stored values).
+template <class S, class R, class LK, int NY, bool XS, bool CG>
+__device__ __forceinline__ float tile_A(const R *r, const S *pold, S *pnew, S *t, const LK *H, float beta,
+                                        float mass, float sigma, int lx, int ly, int lane, int x, bool xval,
+                                        int ybase)
+{
+    const int xc = xval ? x : lx - 1;
+    const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
+    int off[NY + 2];
+    row_offsets<NY>(off, ybase, lx, ly);
+    float2 c[NY + 2];
+#pragma unroll
+    for (int q = 0; q < NY + 2; q++) {
+        const int i = off[q] + xc;
+        c[q] = fadd(ldf<CG>(r, i), fscale(beta, ldf<CG>(pold, i)));
+    }
+    float2 fxm[NY], fxp[NY];
+    auto edge = [&](int col, int q) -> float2 {
+        const int i = off[q + 1] + col;
+        return fadd(ldf<CG>(r, i), fscale(beta, ldf<CG>(pold, i)));
+    };
+    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
+    float2 hx, hyp;
+    LinkPair<LK>::ld(H, off[0] + xc, hx, hyp);  // h_y of the row below the tile
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        float2 hy;
+        LinkPair<LK>::ld(H, off[q + 1] + xc, hx, hy);
+        const float2 hxm = LinkPair<LK>::ldx(H, off[q + 1] + xm);
+        float2 hs = fmul(hx, fxp[q]);
+        hs = fsub(hs, fmulc(hxm, fxm[q]));
+        hs = fadd(hs, fmul(hy, c[q + 2]));
+        hs = fsub(hs, fmulc(hyp, c[q]));
+        hyp = hy;
+        if (xval && ybase + q < ly) {
+            const int i = off[q + 1] + x;
+            const float2 pc = c[q + 1];
+            const float2 tv = fadd(fscale(mass, pc), hs);
+            Fmt<S>::st(pnew, i, pc);
+            Fmt<S>::st(t, i, tv);
+            // reduce what was stored, so that alpha matches the rounded vectors
+            const float2 pq = Fmt<S>::round(pc), tq = Fmt<S>::round(tv);
+            acc += fn2(tq) + sigma * fn2(pq);
+        }
+    }
+    return acc;
+}
+
+// Kernel-B share: Ap = D^dagger t + sigma p' = m t - hop(t) + sigma p' ; x_lo += alpha p' ;
+// r -= alpha Ap ; returns sum |r|^2 over the thread's rows.
+template <class S, class R, class LK, int NY, bool XS, bool CG>
+__device__ __forceinline__ float tile_B(const S *t, const S *p, R *r, float2 *xlo, const LK *H, float alpha,
+                                        float mass, float sigma, int lx, int ly, int lane, int x, bool xval,
+                                        int ybase)
+{
+    const int xc = xval ? x : lx - 1;
+    const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
+    int off[NY + 2];
+    row_offsets<NY>(off, ybase, lx, ly);
+    float2 c[NY + 2];
+#pragma unroll
+    for (int q = 0; q < NY + 2; q++) c[q] = ldf<CG>(t, off[q] + xc);
+    float2 fxm[NY], fxp[NY];
+    auto edge = [&](int col, int q) -> float2 { return ldf<CG>(t, off[q + 1] + col); };
+    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
+    float2 hx, hyp;
+    LinkPair<LK>::ld(H, off[0] + xc, hx, hyp);
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        float2 hy;
+        LinkPair<LK>::ld(H, off[q + 1] + xc, hx, hy);
+        const float2 hxm = LinkPair<LK>::ldx(H, off[q + 1] + xm);
+        float2 hs = fmul(hx, fxp[q]);
+        hs = fsub(hs, fmulc(hxm, fxm[q]));
+        hs = fadd(hs, fmul(hy, c[q + 2]));
+        hs = fsub(hs, fmulc(hyp, c[q]));
+        hyp = hy;
+        if (xval && ybase + q < ly) {
+            const int i = off[q + 1] + x;
+            const float2 pc = ldf<CG>(p, i);
+            const float2 av = fadd(fsub(fscale(mass, c[q + 1]), hs), fscale(sigma, pc));
+            const float2 xo = CG ? __ldcg(xlo + i) : xlo[i];
+            xlo[i] = fadd(xo, fscale(alpha, pc));
+            const float2 rv = Fmt<R>::round(fsub(ldf<CG>(r, i), fscale(alpha, av)));
+            Fmt<R>::st(r, i, rv);
+            acc += fn2(rv);
+        }
+    }
+    return acc;
+}
+
+}  // namespace glinalg
