@@ -272,13 +272,15 @@ def main():
     Ax = torch.zeros_like(bd)
     op.apply(Ax, x)
 
-    # dominant kernel: kernel B of the headline precision, timed alone with CUDA events
-    kms = (C_double * 2)()
-    kbytes = (C_double * 2)()
-    gl._capi.check(L.glinalg_profile_mixed_kernels(op.handle, head_prec, 200, kms, kbytes), "profile")
+    # dominant kernel: the persistent inner-loop kernel of the headline solve (both stencil
+    # phases, the vector updates and the grid barriers); its device time is read by the kernel
+    # itself (%globaltimer at entry and exit, summed over its launches) during the timed solves
     peak, peak_src = peaks()
-    achieved = kbytes[1] / (kms[1] * 1e-3) / 1e9
-    achieved_a = kbytes[0] / (kms[0] * 1e-3) / 1e9
+    hi_ = head_infos[-1]
+    k_launch = max(1, hi_.kernel_launches)
+    k_ms = hi_.kernel_ms / k_launch
+    k_bytes = hi_.kernel_gbytes * 1e9 / k_launch
+    achieved = (k_bytes / (k_ms * 1e-3) / 1e9) if k_ms > 0 else 0.0
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
     Uh = torch.from_numpy(U).pin_memory().numpy()
@@ -328,12 +330,12 @@ def main():
                    "speedup_vs_fp64_gpu": round(t64m / ms, 2), "variants": variants},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "traffic": None,
-                     "kernel": f"k_stB<{head_name}> (D^dagger t + x/r update + |r|^2, register-tiled)",
-                     "bytes_per_launch": kbytes[1], "ms_per_launch": round(kms[1], 5),
-                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                     "kernel_A": {"name": f"k_stA<{head_name}> (p = r + beta p, D p, |Dp|^2)",
-                                  "achieved": round(achieved_a, 1), "bytes_per_launch": kbytes[0],
-                                  "ms_per_launch": round(kms[0], 5)}},
+                     "kernel": f"k_persist<{head_name}> (inner CG iterations: D p, D^dagger t, updates, 2 grid barriers)",
+                     "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 4),
+                     "launches_per_solve": hi_.kernel_launches,
+                     "share_of_solve": round(hi_.kernel_ms / hi_.device_ms, 3) if hi_.device_ms else None,
+                     "timing": "device clock read by the kernel at entry and exit, inside the timed solves",
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": int(Uh.nbytes + bh.nbytes + xh.nbytes),
                 "d2h_bytes_per_step": int(xh.nbytes)},
         "gpu_launches": launches,

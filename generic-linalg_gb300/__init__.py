@@ -264,6 +264,9 @@ class InversionInfo:
         self.reliable_updates = s.reliable_updates
         self.device_ms = s.device_ms
         self.gbytes = s.gbytes
+        self.kernel_ms = s.kernel_ms
+        self.kernel_gbytes = s.kernel_gbytes
+        self.kernel_launches = s.kernel_launches
 
     def __repr__(self):
         return (f"InversionInfo(name={self.name!r}, iter={self.iter}, success={self.success}, "

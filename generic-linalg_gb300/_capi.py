@@ -38,7 +38,8 @@ class InfoStruct(C.Structure):
     _fields_ = [("resSq", C.c_double), ("iter", C.c_int), ("success", C.c_int),
                 ("ops_count", C.c_int), ("name", C.c_char * 32), ("resSqmrhs", _dp),
                 ("n_rhs", C.c_int), ("status", C.c_int), ("reliable_updates", C.c_int),
-                ("device_ms", C.c_double), ("gbytes", C.c_double)]
+                ("device_ms", C.c_double), ("gbytes", C.c_double), ("kernel_ms", C.c_double),
+                ("kernel_gbytes", C.c_double), ("kernel_launches", C.c_int)]
 
 
 class SolverParams(C.Structure):

@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstddef>
 #include <cstdlib>
+#include <cuda/atomic>
 #include <map>
 #include <mutex>
 #include <string>
@@ -59,6 +60,9 @@ struct MxDev {
     int k, max_iter, done, status, reliable, n_reliable, outer;
     int parity;        // which p buffer (0 or 1) holds the current direction
     unsigned cnt[6];
+    long long inner_ns;  // device time spent in the persistent inner-loop kernel
+    int inner_iters;     // iterations it ran
+    int inner_launches;
 };
 
 __device__ __forceinline__ void mx_stop_inner(cudaGraphConditionalHandle cond, int use_cond)
@@ -395,36 +399,34 @@ __device__ __forceinline__ long long gtimer()
 // GLINALG_SOLVE_TIMEOUT) instead of spinning on.
 constexpr long long kBarrierTimeoutNs = 2000000000LL;
 
-// Grid-wide barrier for a co-resident grid (sense by generation counter).  Returns false in
-// every thread of the block once any block has given up waiting.
+// Grid-wide barrier for a co-resident grid (generation counter; acquire/release atomics at
+// device scope).  Returns false in every thread of the block once any block has given up
+// waiting.
 __device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
 {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-        volatile unsigned *vgen = &g->gen;
-        volatile int *verr = &g->error;
-        const unsigned my = *vgen;
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(g->gen), arr(g->arrive);
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(g->error);
+        const unsigned my = gen.load(cuda::memory_order_acquire);
         int good = 1;
-        __threadfence();
-        const unsigned a = atomicAdd(&g->arrive, 1u);
+        const unsigned a = arr.fetch_add(1u, cuda::memory_order_acq_rel);
         if (a == nblocks - 1) {
-            atomicExch(&g->arrive, 0u);
-            __threadfence();
-            atomicAdd(&g->gen, 1u);
+            arr.store(0u, cuda::memory_order_relaxed);
+            gen.fetch_add(1u, cuda::memory_order_release);
         } else {
             const long long t0 = gtimer();
-            while (*vgen == my) {
-                if (*verr) { good = 0; break; }
+            while (gen.load(cuda::memory_order_acquire) == my) {
+                if (err.load(cuda::memory_order_relaxed)) { good = 0; break; }
                 if (gtimer() - t0 > kBarrierTimeoutNs) {
-                    atomicExch(&g->error, 1);
+                    err.store(1, cuda::memory_order_relaxed);
                     good = 0;
                     break;
                 }
             }
         }
-        if (*verr) good = 0;
-        __threadfence();
+        if (err.load(cuda::memory_order_relaxed)) good = 0;
         ok = good;
     }
     __syncthreads();
@@ -469,6 +471,7 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
 {
     __shared__ double sm[33];
     if (s->done || s->reliable) return;
+    const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int ntx = lx / 32, ntiles = ntx * ((ly + NY - 1) / NY);
@@ -528,6 +531,9 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
             s->done = 1;
         }
         if (reliable) s->reliable = 1;
+        s->inner_ns += gtimer() - t_start;
+        s->inner_iters += j;
+        s->inner_launches += 1;
     }
 }
 
@@ -541,9 +547,9 @@ struct PersistKernel {
 };
 
 // Persistent-kernel shapes (warps per block, rows per thread); one block per SM.
-constexpr int kNumPersist = 3;
-static const int kPersistBY[kNumPersist] = {32, 16, 16};
-static const int kPersistNY[kNumPersist] = {4, 8, 4};
+constexpr int kNumPersist = 4;
+static const int kPersistBY[kNumPersist] = {16, 16, 32, 16};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2};
 
 template <class S, class R, class LK>
 static PersistKernel<S, R, LK> persist_cand(int c)
@@ -551,7 +557,12 @@ static PersistKernel<S, R, LK> persist_cand(int c)
     PersistKernel<S, R, LK> pk;
     pk.by = kPersistBY[c];
     pk.ny = kPersistNY[c];
-    pk.f = c == 0 ? k_persist<S, R, LK, 32, 4> : (c == 1 ? k_persist<S, R, LK, 16, 8> : k_persist<S, R, LK, 16, 4>);
+    switch (c) {
+    case 0: pk.f = k_persist<S, R, LK, 16, 4>; break;
+    case 1: pk.f = k_persist<S, R, LK, 16, 8>; break;
+    case 2: pk.f = k_persist<S, R, LK, 32, 2>; break;
+    default: pk.f = k_persist<S, R, LK, 16, 2>; break;
+    }
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pk.f, 32 * pk.by, 0) != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
@@ -1024,6 +1035,9 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     // reliable update: x_hi r/w + x_lo r/w, FP64 operator (two passes), r_hi, r_lo, p
     const double per_rel = 16.0 * 2 + 16.0 + 8.0 * 64.0 / 8.0 + 16.0 * 3 + 2 * wr + 4 * w;
     info->gbytes = ((double)h.k * per_iter * n + (double)h.n_reliable * per_rel * n) * 1e-9;
+    info->kernel_ms = (double)h.inner_ns * 1e-6;
+    info->kernel_gbytes = (double)h.inner_iters * per_iter * n * 1e-9;
+    info->kernel_launches = h.inner_launches;
     fill_name(info, name);
     return GLINALG_SUCCESS;
 }

@@ -269,6 +269,11 @@ __device__ __forceinline__ void row_offsets(int (&off)[NY + 2], int ybase, int l
     }
 }
 
+// The tile bodies issue every load of the tile first (the column with its halo rows, the
+// warp-edge values, both links of every row, and for B the per-site operands), then compute,
+// then store: no load waits behind a store that might alias it, so all of a thread's loads
+// are in flight together (the kernels are bound by L2 latency, not by instruction issue).
+
 // Kernel-A share: p' = r + beta p_old ; t = D p' = m p' + hop(p') ; stores p', t and returns
 // sum |t|^2 + sigma |p'|^2 over the thread's rows (computed from the rounded stored values).
 template <class S, class R, class LK, int NY, bool XS, bool CG>
@@ -280,40 +285,73 @@ __device__ __forceinline__ float tile_A(const R *r, const S *pold, S *pnew, S *t
     const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
     int off[NY + 2];
     row_offsets<NY>(off, ybase, lx, ly);
-    float2 c[NY + 2];
+    // ---- loads
+    float2 rr[NY + 2], pp[NY + 2];
 #pragma unroll
     for (int q = 0; q < NY + 2; q++) {
-        const int i = off[q] + xc;
-        c[q] = fadd(ldf<CG>(r, i), fscale(beta, ldf<CG>(pold, i)));
+        rr[q] = ldf<CG>(r, off[q] + xc);
+        pp[q] = ldf<CG>(pold, off[q] + xc);
     }
-    float2 fxm[NY], fxp[NY];
-    auto edge = [&](int col, int q) -> float2 {
-        const int i = off[q + 1] + col;
-        return fadd(ldf<CG>(r, i), fscale(beta, ldf<CG>(pold, i)));
-    };
-    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
-    float2 hx, hyp;
-    LinkPair<LK>::ld(H, off[0] + xc, hx, hyp);  // h_y of the row below the tile
-    float acc = 0.f;
+    float2 erm[NY], epm[NY], erp[NY], epp[NY];
+    const int ecol = lane == 0 ? xm : (lane == 31 ? xp : xc);
 #pragma unroll
     for (int q = 0; q < NY; q++) {
-        float2 hy;
-        LinkPair<LK>::ld(H, off[q + 1] + xc, hx, hy);
-        const float2 hxm = LinkPair<LK>::ldx(H, off[q + 1] + xm);
-        float2 hs = fmul(hx, fxp[q]);
-        hs = fsub(hs, fmulc(hxm, fxm[q]));
-        hs = fadd(hs, fmul(hy, c[q + 2]));
-        hs = fsub(hs, fmulc(hyp, c[q]));
-        hyp = hy;
+        if (XS) {
+            // only the two warp-edge lanes need a value from outside the warp
+            erm[q] = epm[q] = make_float2(0.f, 0.f);
+            if (lane == 0 || lane == 31) {
+                erm[q] = ldf<CG>(r, off[q + 1] + ecol);
+                epm[q] = ldf<CG>(pold, off[q + 1] + ecol);
+            }
+        } else {
+            erm[q] = ldf<CG>(r, off[q + 1] + xm);
+            epm[q] = ldf<CG>(pold, off[q + 1] + xm);
+            erp[q] = ldf<CG>(r, off[q + 1] + xp);
+            epp[q] = ldf<CG>(pold, off[q + 1] + xp);
+        }
+    }
+    float2 hx[NY], hy[NY + 1], hxm[NY], dummy;
+    LinkPair<LK>::ld(H, off[0] + xc, dummy, hy[0]);
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        LinkPair<LK>::ld(H, off[q + 1] + xc, hx[q], hy[q + 1]);
+        hxm[q] = LinkPair<LK>::ldx(H, off[q + 1] + xm);
+    }
+    // ---- compute
+    float2 c[NY + 2];
+#pragma unroll
+    for (int q = 0; q < NY + 2; q++) c[q] = fadd(rr[q], fscale(beta, pp[q]));
+    float acc = 0.f;
+    float2 pv[NY], tv[NY];
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        float2 fxp, fxm;
+        if (XS) {
+            const float2 ev = fadd(erm[q], fscale(beta, epm[q]));
+            const float2 up = shfl_down2(c[q + 1], 1), dn = shfl_up2(c[q + 1], 1);
+            fxp = lane == 31 ? ev : up;
+            fxm = lane == 0 ? ev : dn;
+        } else {
+            fxm = fadd(erm[q], fscale(beta, epm[q]));
+            fxp = fadd(erp[q], fscale(beta, epp[q]));
+        }
+        float2 hs = fmul(hx[q], fxp);
+        hs = fsub(hs, fmulc(hxm[q], fxm));
+        hs = fadd(hs, fmul(hy[q + 1], c[q + 2]));
+        hs = fsub(hs, fmulc(hy[q], c[q]));
+        pv[q] = c[q + 1];
+        tv[q] = fadd(fscale(mass, pv[q]), hs);
+        // reduce what is stored, so that alpha matches the rounded vectors
+        const float2 pq = Fmt<S>::round(pv[q]), tq = Fmt<S>::round(tv[q]);
+        if (xval && ybase + q < ly) acc += fn2(tq) + sigma * fn2(pq);
+    }
+    // ---- stores
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
         if (xval && ybase + q < ly) {
             const int i = off[q + 1] + x;
-            const float2 pc = c[q + 1];
-            const float2 tv = fadd(fscale(mass, pc), hs);
-            Fmt<S>::st(pnew, i, pc);
-            Fmt<S>::st(t, i, tv);
-            // reduce what was stored, so that alpha matches the rounded vectors
-            const float2 pq = Fmt<S>::round(pc), tq = Fmt<S>::round(tv);
-            acc += fn2(tq) + sigma * fn2(pq);
+            Fmt<S>::st(pnew, i, pv[q]);
+            Fmt<S>::st(t, i, tv[q]);
         }
     }
     return acc;
@@ -330,34 +368,66 @@ __device__ __forceinline__ float tile_B(const S *t, const S *p, R *r, float2 *xl
     const int xp = xc + 1 == lx ? 0 : xc + 1, xm = xc == 0 ? lx - 1 : xc - 1;
     int off[NY + 2];
     row_offsets<NY>(off, ybase, lx, ly);
+    // ---- loads
     float2 c[NY + 2];
 #pragma unroll
     for (int q = 0; q < NY + 2; q++) c[q] = ldf<CG>(t, off[q] + xc);
-    float2 fxm[NY], fxp[NY];
-    auto edge = [&](int col, int q) -> float2 { return ldf<CG>(t, off[q + 1] + col); };
-    x_neighbours<NY, XS>(fxm, fxp, c, lane, xc, xm, xp, edge);
-    float2 hx, hyp;
-    LinkPair<LK>::ld(H, off[0] + xc, hx, hyp);
+    float2 em[NY], ep[NY];
+    const int ecol = lane == 0 ? xm : (lane == 31 ? xp : xc);
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (XS) {
+            em[q] = make_float2(0.f, 0.f);
+            if (lane == 0 || lane == 31) em[q] = ldf<CG>(t, off[q + 1] + ecol);
+        } else {
+            em[q] = ldf<CG>(t, off[q + 1] + xm);
+            ep[q] = ldf<CG>(t, off[q + 1] + xp);
+        }
+    }
+    float2 hx[NY], hy[NY + 1], hxm[NY], dummy;
+    LinkPair<LK>::ld(H, off[0] + xc, dummy, hy[0]);
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        LinkPair<LK>::ld(H, off[q + 1] + xc, hx[q], hy[q + 1]);
+        hxm[q] = LinkPair<LK>::ldx(H, off[q + 1] + xm);
+    }
+    float2 pv[NY], rv[NY], xv[NY];
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        const int i = off[q + 1] + xc;
+        pv[q] = ldf<CG>(p, i);
+        rv[q] = ldf<CG>(r, i);
+        xv[q] = CG ? __ldcg(xlo + i) : xlo[i];
+    }
+    // ---- compute
     float acc = 0.f;
 #pragma unroll
     for (int q = 0; q < NY; q++) {
-        float2 hy;
-        LinkPair<LK>::ld(H, off[q + 1] + xc, hx, hy);
-        const float2 hxm = LinkPair<LK>::ldx(H, off[q + 1] + xm);
-        float2 hs = fmul(hx, fxp[q]);
-        hs = fsub(hs, fmulc(hxm, fxm[q]));
-        hs = fadd(hs, fmul(hy, c[q + 2]));
-        hs = fsub(hs, fmulc(hyp, c[q]));
-        hyp = hy;
+        float2 fxp, fxm;
+        if (XS) {
+            const float2 up = shfl_down2(c[q + 1], 1), dn = shfl_up2(c[q + 1], 1);
+            fxp = lane == 31 ? em[q] : up;
+            fxm = lane == 0 ? em[q] : dn;
+        } else {
+            fxm = em[q];
+            fxp = ep[q];
+        }
+        float2 hs = fmul(hx[q], fxp);
+        hs = fsub(hs, fmulc(hxm[q], fxm));
+        hs = fadd(hs, fmul(hy[q + 1], c[q + 2]));
+        hs = fsub(hs, fmulc(hy[q], c[q]));
+        const float2 av = fadd(fsub(fscale(mass, c[q + 1]), hs), fscale(sigma, pv[q]));
+        xv[q] = fadd(xv[q], fscale(alpha, pv[q]));
+        rv[q] = Fmt<R>::round(fsub(rv[q], fscale(alpha, av)));
+        if (xval && ybase + q < ly) acc += fn2(rv[q]);
+    }
+    // ---- stores
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
         if (xval && ybase + q < ly) {
             const int i = off[q + 1] + x;
-            const float2 pc = ldf<CG>(p, i);
-            const float2 av = fadd(fsub(fscale(mass, c[q + 1]), hs), fscale(sigma, pc));
-            const float2 xo = CG ? __ldcg(xlo + i) : xlo[i];
-            xlo[i] = fadd(xo, fscale(alpha, pc));
-            const float2 rv = Fmt<R>::round(fsub(ldf<CG>(r, i), fscale(alpha, av)));
-            Fmt<R>::st(r, i, rv);
-            acc += fn2(rv);
+            xlo[i] = xv[q];
+            Fmt<R>::st(r, i, rv[q]);
         }
     }
     return acc;

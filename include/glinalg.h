@@ -112,6 +112,10 @@ typedef struct glinalg_info {
     int reliable_updates;/* mixed precision: number of FP64 residual recomputations */
     double device_ms;    /* device time of the solve, CUDA events */
     double gbytes;       /* algorithmic bytes moved by the solve's kernels, in GB */
+    double kernel_ms;    /* mixed CG: device time inside the persistent inner-loop kernel
+                            (device clock, summed over its launches; 0 if it did not run) */
+    double kernel_gbytes;/* algorithmic bytes that kernel moved, in GB */
+    int kernel_launches; /* its launches */
 } glinalg_info;
 
 /* Arithmetic of a solve. */
