@@ -677,6 +677,16 @@ static int autotune(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p
         auto it = g_tuned.find(key);
         if (it != g_tuned.end()) return it->second;
     }
+    // GLINALG_TILE=<candidate> fixes the shape: timing picks can differ between processes, and
+    // a different tile changes the order of the reductions (results differ at rounding level)
+    if (const char *e = std::getenv("GLINALG_TILE")) {
+        const int c = std::atoi(e);
+        if (c >= 0 && c < kNumTiles) {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_tuned[key] = c;
+            return c;
+        }
+    }
     const bool xs = lx % 32 == 0;
     // a state under which the kernels neither stop nor trigger an update: rsq = 0 gives
     // alpha = 0 (updates add zero but run in full); delta = eps = 0 never trigger
@@ -745,6 +755,14 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         if (g_ptuned.count(key)) return;
+    }
+    if (const char *e = std::getenv("GLINALG_PERSIST_SHAPE")) {  // as GLINALG_TILE
+        const int c = std::atoi(e);
+        if (c >= 0 && c < kNumPersist) {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            g_ptuned[key] = c;
+            return;
+        }
     }
     const long n = op->size;
     std::vector<double2> ones(n, cmk(1.0, 0.0));

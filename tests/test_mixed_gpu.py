@@ -117,6 +117,9 @@ np.savez(sys.argv[1], **out)
     np.savez(tmp_path / "in.npz", U=vec["l32_links"], b=vec["l32_src"])
     import os
     env = dict(os.environ)
+    # the same tile shape in both processes (the autotuner's timing-based pick may differ)
+    env["GLINALG_TILE"] = "1"
+    env["GLINALG_PERSIST_SHAPE"] = "0"
     res = {}
     for mode in ("1", "0"):
         env["GLINALG_SOLVER_GRAPHS"] = mode
