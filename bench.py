@@ -170,7 +170,7 @@ def kernels_only(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
@@ -316,7 +316,10 @@ def main():
                           "reliable_updates": ins[-1].reliable_updates,
                           "true_relres": float(np.sqrt(ins[-1].resSq) / np.linalg.norm(b)),
                           "gbytes": round(ins[-1].gbytes, 3)}
-    launches = 3 * (hi.iter + 1) + 8 * hi.reliable_updates + 7
+    # kernels of one headline solve: link packing, |b|^2 and the setup reliable update (6),
+    # then per cycle of the outer loop the persistent inner-loop kernel, the reliable update
+    # (6), the outer-loop tail and the graph's loop guard
+    launches = 8 + 9 * hi.kernel_launches
     line = {
         "metric": METRIC, "value": round(ms_max, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False,

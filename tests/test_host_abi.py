@@ -82,3 +82,19 @@ def test_gauss_gauge_matches_reference(gl, golden):
     c = cases["g16"]
     U = gl.Generator(c["seed"]).gauss_gauge_u1(c["lx"], c["ly"], c["beta"])
     assert np.array_equal(U, vec["g16_links"])
+
+
+def test_product_never_touches_the_oracle():
+    """The package and its CUDA sources name no oracle module, library or path: the oracle is
+    test infrastructure only."""
+    pkg = os.path.join(ROOT, "generic-linalg_gb300")
+    offenders = []
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath:
+            continue
+        for fn in files:
+            if fn.endswith((".py", ".cu", ".cuh", ".h", ".cpp")):
+                txt = open(os.path.join(dirpath, fn)).read()
+                if re.search(r"pyoracle|liboracle|oracle/|import\s+oracle|orc_", txt):
+                    offenders.append(fn)
+    assert not offenders, offenders
