@@ -241,6 +241,24 @@ glinalg_status glinalg_staggered_action_grad(glinalg_operator op, const double *
                                              const glinalg_solver_params *params,
                                              glinalg_info *info);
 
+/* ---- allocation-free operator ----
+ * No counterpart in the reference.  For callers that must not allocate device memory while
+ * they run (an application that has reserved HBM for its own pools, a code path under another
+ * framework's allocator or memory budget, a latency-critical loop that cannot afford
+ * cudaMalloc / cudaFree): lhs = D^dagger D rhs, the staggered normal operator of
+ * square_staggered_normal_u1, on caller-provided DEVICE buffers (links: 2*lx*ly complex,
+ * lhs / rhs: lx*ly complex), issued on `stream` (a cudaStream_t, NULL for the legacy default
+ * stream) and finished before return.  The intermediate D rhs lives in a fixed array inside
+ * the library (GLINALG_NOALLOC_MAX_SITES complex values, 4 MiB, held on every GPU that loads
+ * the library until exit); lattices with more sites are rejected with
+ * GLINALG_ERROR_INVALID_VALUE.  The first call on a device looks up that array's address;
+ * make it before any stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised by the caller. */
+#define GLINALG_NOALLOC_MAX_SITES (1L << 18)
+glinalg_status glinalg_staggered_normal_apply_noalloc(const double *links, double mass, int lx,
+                                                      int ly, double *lhs, const double *rhs,
+                                                      void *stream);
+
 /* ---- measurement ----
  * Times the two inner-iteration kernels of the mixed-precision CG (A: direction update +
  * D p + norm; B: D^dagger t + solution/residual update + norm) on op's lattice, each launched
