@@ -38,6 +38,9 @@ MAX_ITER = 100000
 REF_ITERS = 2093
 METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB300; HBM GB/s"
 HEADLINE = ("fp32", 1)
+# DRAM bytes (read + write) of one launch of the FP32 persistent inner-loop kernel on this
+# workload, from an ncu --set full capture (profiles/k_persist_fp32_1024.md)
+K_PERSIST_DRAM_BYTES = 41.987328e6 + 3.212544e6
 VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 
 
@@ -167,6 +170,144 @@ def kernels_only(args):
                           "GB/s": kbytes[j] / (kms[j] * 1e-3) / 1e9}))
 
 
+def _flush_and_time(fn, flush, stream):
+    """fn() between CUDA events on `stream`, after writing the L2-flush buffer."""
+    import torch
+    flush.fill_(1.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def workload_multishift(args):
+    """Multishift CG on the staggered normal equations, 512x512, m = 0.05, 12 shifts log-spaced
+    over [1e-4, 1], tolerance 1e-10 per shift: one source, and 64 sources in one batched solve
+    (glinalg_cg_m_multi) against 64 single-source solves one after another.  Inputs from
+    std::mt19937(1337): links, then the sources in order."""
+    import numpy as np
+    import torch
+    gl = importlib.import_module("generic-linalg_gb300")
+    L = gl.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
+    lx = ly = 512
+    n_rhs, shifts = 64, np.logspace(-4, 0, 12)
+    g = gl.Generator(SEED)
+    U = g.rand_gauge_u1(lx, ly)
+    B = np.stack([g.gaussian(lx * ly) for _ in range(n_rhs)])
+    op = gl.Operator(2, lx, ly, 0.05, torch.from_numpy(U).to(dev))
+    Bd = torch.from_numpy(B).to(dev)
+    X = torch.zeros((n_rhs, len(shifts), lx * ly), dtype=torch.complex128, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    res = {}
+    for nr in (1, n_rhs):
+        for i in range(args.warmup + args.steps):
+            X.zero_()
+            t, infos = _flush_and_time(lambda: gl.cg_m_multi(op, X[:nr], Bd[:nr], shifts, 1, 100000, 1e-10),
+                                       flush, stream)
+            if i >= args.warmup:
+                res.setdefault(nr, []).append(t)
+        assert all(inf.success for inf in infos)
+        res[f"info{nr}"] = infos
+    # the same 64 sources, one single-source solve after another
+    xs = [torch.zeros(lx * ly, dtype=torch.complex128, device=dev) for _ in shifts]
+
+    def one_by_one():
+        for q in range(n_rhs):
+            gl.minv_vector_cg_m(xs, Bd[q], len(shifts), lx * ly, 1, 100000, 1e-10, shifts.copy(),
+                                gl.square_staggered_normal_u1, op)
+    t_seq, _ = _flush_and_time(one_by_one, flush, stream)
+    i1, i64 = res["info1"], res[f"info{n_rhs}"]
+    ms1, ms64 = statistics.mean(res[1]), statistics.mean(res[n_rhs])
+    gb64 = sum(inf.gbytes for inf in i64)
+    line = {"workload": "multishift CG, staggered normal equations 512x512, m=0.05, 12 shifts logspace[1e-4,1], tol 1e-10",
+            "steps": args.steps, "warmup": args.warmup, "l2": "flushed (512 MiB write) before every solve",
+            "one_source_ms": round(ms1, 3), "one_source_iters": i1[0].iter,
+            "sources": n_rhs, "batched_ms": round(ms64, 3),
+            "batched_iters_min_max": [min(i.iter for i in i64), max(i.iter for i in i64)],
+            "batched_ms_per_source": round(ms64 / n_rhs, 3),
+            "one_by_one_ms": round(t_seq, 3), "batch_speedup": round(t_seq / ms64, 2),
+            "batched_algorithmic_GBps": round(gb64 / (ms64 * 1e-3), 1),
+            "max_shift_relres": float(max(np.sqrt(np.max(inf.resSqmrhs)) / np.linalg.norm(B[q])
+                                          for q, inf in enumerate(i64)))}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        O = pyoracle.Oracle()
+        oop = pyoracle.Operator("staggered_normal", lx, ly, 0.05, U)
+        t0 = time.perf_counter()
+        O.cg_m(oop, B[0], shifts, max_iter=20, eps=1e-10)
+        dt = time.perf_counter() - t0
+        per = dt / 20
+        line["cpu_baseline"] = {"value": per * i1[0].iter * 1e3 * n_rhs, "unit": "ms (64 sources)", "cores": 1,
+                                "kind": "port",
+                                "sample": f"20 CG-M iterations of one source ({dt:.2f} s), extrapolated to "
+                                          f"{i1[0].iter} iterations x {n_rhs} sources"}
+    print(json.dumps(line))
+
+
+def workload_batch(args):
+    """256 independent systems in one batch: sides from {32, 64, 128, 256}, links U(1) random,
+    masses log-uniform in [0.01, 0.5]; even systems staggered D^dagger D (mass m), odd systems
+    the gauge Laplacian (mass m^2); FP32 inner iterations with FP64 reliable updates, tolerance
+    1e-10.  One batched call (glinalg_cg_batch) against one mixed solve per system."""
+    import numpy as np
+    import torch
+    gl = importlib.import_module("generic-linalg_gb300")
+    L = gl.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
+    g = gl.Generator(2024)
+    rng = np.random.default_rng(2024)
+    ops, bs, xs, meta = [], [], [], []
+    for q in range(256):
+        side = int(rng.choice([32, 64, 128, 256]))
+        m = float(np.exp(rng.uniform(np.log(0.01), np.log(0.5))))
+        kind = 2 if q % 2 == 0 else 3
+        U = g.rand_gauge_u1(side, side)
+        b = g.gaussian(side * side)
+        mass = m if kind == 2 else m * m
+        ops.append(gl.Operator(kind, side, side, mass, torch.from_numpy(U).to(dev)))
+        bs.append(torch.from_numpy(b).to(dev))
+        xs.append(torch.zeros(side * side, dtype=torch.complex128, device=dev))
+        meta.append((kind, side, mass))
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    times = []
+    for i in range(args.warmup + args.steps):
+        for x in xs:
+            x.zero_()
+        t, infos = _flush_and_time(lambda: gl.cg_batch(ops, xs, bs, 100000, 1e-10, precision=1), flush, stream)
+        if i >= args.warmup:
+            times.append(t)
+    assert all(inf.success for inf in infos)
+
+    def one_by_one():
+        for q in range(len(ops)):
+            cb = gl.square_staggered_normal_u1 if meta[q][0] == 2 else gl.square_laplace_u1
+            gl.minv_vector_cg(xs[q], bs[q], xs[q].numel(), 100000, 1e-10, cb, ops[q], precision=1)
+    for x in xs:
+        x.zero_()
+    one_by_one()
+    for x in xs:
+        x.zero_()
+    t_seq, _ = _flush_and_time(one_by_one, flush, stream)
+    ms = statistics.mean(times)
+    sites = sum(s * s for _, s, _ in meta)
+    line = {"workload": "256 uneven systems (sides 32..256, half staggered normal, half Laplacian), FP32 inner + FP64 reliable, tol 1e-10",
+            "steps": args.steps, "warmup": args.warmup, "sites": sites, "l2": "flushed (512 MiB write) before every solve",
+            "batched_ms": round(ms, 3), "iters_min_max": [min(i.iter for i in infos), max(i.iter for i in infos)],
+            "one_by_one_ms": round(t_seq, 3), "batch_speedup": round(t_seq / ms, 2),
+            "algorithmic_GBps": round(sum(i.gbytes for i in infos) / (ms * 1e-3), 1)}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,7 +322,13 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only time the two inner-iteration kernels of the headline variant "
                          "(a small case for ncu captures)")
+    ap.add_argument("--workload", default="headline", choices=["headline", "multishift", "batch"],
+                    help="multishift / batch: time the batched workloads instead (one JSON line each)")
     args = ap.parse_args()
+    if args.workload == "multishift" and args.impl == "ours":
+        return workload_multishift(args)
+    if args.workload == "batch" and args.impl == "ours":
+        return workload_batch(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.kernels_only:
@@ -332,7 +479,11 @@ def main():
                    "true_relres_fp64": relres, "fp64_gpu_ms": round(t64m, 3),
                    "speedup_vs_fp64_gpu": round(t64m / ms, 2), "variants": variants},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "traffic": None,
+                     "frac": round(achieved / peak, 3), "traffic": K_PERSIST_DRAM_BYTES,
+                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one k_persist launch "
+                                     "(the first of a solve, 254 inner iterations; profiles/k_persist_fp32_1024.md): "
+                                     "the FP32 working set stays in L2, so DRAM traffic is the compulsory first read "
+                                     "and does not grow with the iterations of a launch",
                      "kernel": f"k_persist<{head_name}> (inner CG iterations: D p, D^dagger t, updates, 2 grid barriers)",
                      "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 4),
                      "launches_per_solve": hi_.kernel_launches,
