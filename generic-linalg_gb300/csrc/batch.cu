@@ -1,14 +1,20 @@
 // batch.cu -- entry points for many independent systems (no reference counterpart: the
 // reference solves one system per call, e.g. tests/multishift/multishift.cpp:446-489).
 //
-// glinalg_cg_m_multi: multishift CG for n_rhs sources of one operator.
-// glinalg_cg_batch:   CG on n_sys independent Hermitian systems of any sizes.
+// glinalg_cg_m_multi: multishift CG for n_rhs sources of one operator (all sources in one
+//                     CUDA graph, cgm_batch.cu, for the staggered-normal and Laplace kinds).
+// glinalg_cg_batch:   CG on n_sys independent Hermitian systems of any sizes (mixed precision:
+//                     all systems advanced by the same kernels, cg_batch.cu).
 
 #include <vector>
 
 #include "solvers.h"
 
 using namespace glinalg;
+
+static glinalg_status cg_m_each_impl(const glinalg_operator_s *op, double2 *X, const double2 *B, int n_rhs,
+                                     int n_shift, int resid_freq_check, int max_iter, double eps,
+                                     const double *shifts, glinalg_info *infos, cudaStream_t st);
 
 extern "C" glinalg_status glinalg_cg_m_multi(glinalg_operator op, double *phi, const double *phi0,
                                              int n_rhs, int n_shift, int size, int resid_freq_check,
@@ -34,6 +40,23 @@ extern "C" glinalg_status glinalg_cg_m_multi(glinalg_operator op, double *phi, c
         X = tx;
         B = tb;
     }
+    if (cg_m_batch_supported(op, n_shift)) {
+        GL_TRY(cg_m_batch(op, X, B, n_rhs, n_shift, resid_freq_check, max_iter, eps, shifts, infos, st));
+    } else {
+        // other operator kinds: one source after another
+        GL_TRY(cg_m_each_impl(op, X, B, n_rhs, n_shift, resid_freq_check, max_iter, eps, shifts, infos, st));
+    }
+    if (!dev)
+        GL_CUDA(cudaMemcpyAsync(phi, X, sizeof(double2) * n * n_rhs * n_shift, cudaMemcpyDeviceToHost, st));
+    GL_CUDA(cudaStreamSynchronize(st));
+    return GLINALG_SUCCESS;
+}
+
+static glinalg_status cg_m_each_impl(const glinalg_operator_s *op, double2 *X, const double2 *B, int n_rhs,
+                                     int n_shift, int resid_freq_check, int max_iter, double eps,
+                                     const double *shifts, glinalg_info *infos, cudaStream_t st)
+{
+    const long n = op->size;
     const Verb quiet;
     for (int q = 0; q < n_rhs; q++) {
         std::vector<double2 *> xs(n_shift);
@@ -44,9 +67,6 @@ extern "C" glinalg_status glinalg_cg_m_multi(glinalg_operator op, double *phi, c
         GL_TRY(cg_m_fp64(op, xs.data(), B + (size_t)q * n, n_shift, resid_freq_check, max_iter, eps,
                          shifts, false, quiet, &infos[q], st));
     }
-    if (!dev)
-        GL_CUDA(cudaMemcpyAsync(phi, X, sizeof(double2) * n * n_rhs * n_shift, cudaMemcpyDeviceToHost, st));
-    GL_CUDA(cudaStreamSynchronize(st));
     return GLINALG_SUCCESS;
 }
 
@@ -63,27 +83,39 @@ extern "C" glinalg_status glinalg_cg_batch(const glinalg_operator *ops, int n_sy
     const double delta = params && params->delta > 0 ? params->delta : 0.1;
     cudaStream_t st = lib_stream();
     Scratch sc(st);
-    const Verb quiet;
+    std::vector<double2 *> xs(n_sys);
+    std::vector<const double2 *> bs(n_sys);
     for (int q = 0; q < n_sys; q++) {
         const long n = ops[q]->size;
-        double2 *x = (double2 *)phi[q];
-        const double2 *b = (const double2 *)phi0[q];
+        xs[q] = (double2 *)phi[q];
+        bs[q] = (const double2 *)phi0[q];
         if (!dev) {
             double2 *tx, *tb;
             GL_TRY(sc.alloc(&tx, n));
             GL_TRY(sc.alloc(&tb, n));
             GL_CUDA(cudaMemcpyAsync(tx, phi[q], sizeof(double2) * n, cudaMemcpyHostToDevice, st));
             GL_CUDA(cudaMemcpyAsync(tb, phi0[q], sizeof(double2) * n, cudaMemcpyHostToDevice, st));
-            x = tx;
-            b = tb;
+            xs[q] = tx;
+            bs[q] = tb;
         }
-        double *keep = infos[q].resSqmrhs;
-        infos[q] = glinalg_info{};
-        infos[q].resSqmrhs = keep;
-        if (prec == GLINALG_PREC_DOUBLE) GL_TRY(cg_fp64(ops[q], x, b, max_iter, eps, quiet, &infos[q], st));
-        else GL_TRY(cg_mixed(ops[q], x, b, max_iter, eps, prec, delta, 0.0, quiet, &infos[q], st));
-        if (!dev) GL_CUDA(cudaMemcpyAsync(phi[q], x, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
     }
+    if (prec != GLINALG_PREC_DOUBLE) {
+        // every system advanced by the same kernels (cg_batch.cu)
+        std::vector<const glinalg_operator_s *> po(ops, ops + n_sys);
+        GL_TRY(cg_batch_mixed(po.data(), n_sys, xs.data(), bs.data(), max_iter, eps, prec, delta, infos, st));
+    } else {
+        // FP64: the reference recurrence, one system after another
+        const Verb quiet;
+        for (int q = 0; q < n_sys; q++) {
+            double *keep = infos[q].resSqmrhs;
+            infos[q] = glinalg_info{};
+            infos[q].resSqmrhs = keep;
+            GL_TRY(cg_fp64(ops[q], xs[q], bs[q], max_iter, eps, quiet, &infos[q], st));
+        }
+    }
+    if (!dev)
+        for (int q = 0; q < n_sys; q++)
+            GL_CUDA(cudaMemcpyAsync(phi[q], xs[q], sizeof(double2) * ops[q]->size, cudaMemcpyDeviceToHost, st));
     GL_CUDA(cudaStreamSynchronize(st));
     return GLINALG_SUCCESS;
 }

@@ -1,0 +1,663 @@
+// cg_batch.cu -- CG with reduced-precision inner iterations and FP64 reliable updates on many
+// independent Hermitian systems of different sizes and kinds (staggered D^dagger D and the
+// gauge Laplacian), all advanced by the same kernels (glinalg_cg_batch).  The reference solves
+// one system per minv_vector_cg call (generic_cg.cpp:278-382).
+//
+// Per system the algorithm is the single-system mixed solver's (cg_mixed.cu: the same MxDev
+// state, the same scalar updates mx_after_A / mx_after_B, the same reliable-update steps and
+// the same tile bodies), so each system converges to the same FP64-true tolerance.
+//
+// Layout: the work vectors of all systems are packed one after another (system s starts at
+// site sys[s].off).  Inner kernels run one block per tile of one system (tile blocks are
+// numbered system by system; tblk maps a block to its system); the vector and FP64 kernels run
+// blocks of up to 1024 sites of one system (vblk).  Every reduction is over the blocks of one
+// system (grid_sum_*_ids with the block's index inside its system), so a system's sums do not
+// depend on the other systems.
+//
+// Control: every kernel starts by reading its system's flags, and a block whose system has
+// nothing to do returns at once.  The graph body is kBatchUnroll inner iterations (A, B) for the
+// systems that are iterating, then the reliable-update steps (R1, FP64 operator, R2, R3, R4)
+// for the systems that flagged one, then a tail that re-arms those systems and ends the loop
+// when every system has stopped.  A system that flags an update during the unrolled iterations
+// waits for the end of the pass; its own arithmetic does not depend on the pass structure.
+// The tile shape of the inner kernels is picked for the batch by timing the candidates.
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "mixed_state.cuh"
+#include "sites.cuh"
+
+namespace glinalg {
+
+// bounded spin on the device clock (cg_mixed.cu)
+__global__ void k_busy_wait(long long ns);
+
+namespace {
+
+constexpr int kBatchUnroll = 4;
+constexpr int kVecSites = 1024;  // sites per block of the vector kernels (256 threads x 4)
+
+struct BSys {
+    long off;          // first site in the packed work vectors
+    const double2 *U;  // FP64 links (the operator's device copy)
+    double2 *x;        // FP64 solution (device)
+    const double2 *b;  // source (device)
+    double mass;       // staggered: mass; Laplace: the reference's additive mass
+    int lx, ly, stag, xs;  // stag: D^dagger D (else Laplace); xs: lx % 32 == 0
+    int tb0, ntb, tiles_x;
+    int vb0, nvb;
+};
+
+template <class S, class R, class LK>
+struct BArgs {
+    const BSys *sys;
+    MxDev *st;
+    const int *tblk, *vblk;
+    R *r;
+    S *p0, *p1, *t;
+    float2 *xlo;
+    LK *L;
+    double2 *rhi, *tmp64, *Ax;
+    double *tpart, *vpart;
+    int *all_done;
+    int nsys;
+};
+
+// ---------------------------------------------------------------- Laplace tile bodies
+// The arithmetic of k_lapA / k_lapB (cg_mixed.cu), NY rows of column x per thread.
+
+template <class S, class R, class LK, int NY>
+__device__ __forceinline__ float lap_tile_A(const R *r, const S *pold, S *pnew, S *Ap, const LK *G,
+                                            float beta, float diag, int lx, int ly, int x, int ybase)
+{
+    float acc = 0.f;
+    if (x >= lx) return acc;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        const int y = ybase + q;
+        if (y >= ly) break;
+        const int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
+        const int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
+        const long i = (long)y * lx + x;
+        auto P = [&](long j) { return fadd(Fmt<R>::ld(r, j), fscale(beta, Fmt<S>::ld(pold, j))); };
+        const float2 pc = P(i);
+        float2 hs = fmul(Fmt<LK>::ld(G, 2 * i), P((long)y * lx + xp));
+        hs = fadd(hs, fmulc(Fmt<LK>::ld(G, 2 * ((long)y * lx + xm)), P((long)y * lx + xm)));
+        hs = fadd(hs, fmul(Fmt<LK>::ld(G, 2 * i + 1), P((long)yp * lx + x)));
+        hs = fadd(hs, fmulc(Fmt<LK>::ld(G, 2 * ((long)ym * lx + x) + 1), P((long)ym * lx + x)));
+        const float2 av = fsub(fscale(diag, pc), hs);
+        Fmt<S>::st(pnew, i, pc);
+        Fmt<S>::st(Ap, i, av);
+        const float2 pq = Fmt<S>::round(pc), aq = Fmt<S>::round(av);
+        acc += pq.x * aq.x + pq.y * aq.y;
+    }
+    return acc;
+}
+
+template <class S, class R, int NY>
+__device__ __forceinline__ float lap_tile_B(const S *Ap, const S *p, R *r, float2 *xlo, float alpha, int lx,
+                                            int ly, int x, int ybase)
+{
+    float acc = 0.f;
+    if (x >= lx) return acc;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        const int y = ybase + q;
+        if (y >= ly) break;
+        const long i = (long)y * lx + x;
+        const float2 pc = Fmt<S>::ld(p, i);
+        xlo[i] = fadd(xlo[i], fscale(alpha, pc));
+        const float2 rn = Fmt<R>::round(fsub(Fmt<R>::ld(r, i), fscale(alpha, Fmt<S>::ld(Ap, i))));
+        Fmt<R>::st(r, i, rn);
+        acc += fn2(rn);
+    }
+    return acc;
+}
+
+// ---------------------------------------------------------------- inner kernels
+
+// A: p' = r + beta p ; t = D p' and |t|^2 (staggered) or Ap = L p' and <p', Ap> (Laplace)
+template <class S, class R, class LK, int BY, int NY>
+__global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a)
+{
+    const int sid = a.tblk[blockIdx.x];
+    const BSys sy = a.sys[sid];
+    MxDev *s = a.st + sid;
+    if (s->done || s->reliable) return;
+    const int lb = blockIdx.x - sy.tb0;
+    const int x = (lb % sy.tiles_x) * 32 + threadIdx.x;
+    const int ybase = (lb / sy.tiles_x) * (BY * NY) + threadIdx.y * NY;
+    const int par = s->parity;
+    const long o = sy.off;
+    const S *pold = (par ? a.p1 : a.p0) + o;
+    S *pnew = (par ? a.p0 : a.p1) + o;
+    const float beta = (float)s->beta;
+    float acc[1];
+    if (!sy.stag)
+        acc[0] = lap_tile_A<S, R, LK, NY>(a.r + o, pold, pnew, a.t + o, a.L + 2 * o, beta, (float)(4.0 + sy.mass),
+                                          sy.lx, sy.ly, x, ybase);
+    else if (sy.xs)
+        acc[0] = tile_A<S, R, LK, NY, true, false>(a.r + o, pold, pnew, a.t + o, a.L + 2 * o, beta, (float)sy.mass,
+                                                   0.f, sy.lx, sy.ly, threadIdx.x, x, true, ybase);
+    else
+        acc[0] = tile_A<S, R, LK, NY, false, false>(a.r + o, pold, pnew, a.t + o, a.L + 2 * o, beta,
+                                                    (float)sy.mass, 0.f, sy.lx, sy.ly, threadIdx.x, x, x < sy.lx,
+                                                    ybase);
+    double out[1];
+    if (grid_sum_f_ids<1, 32 * BY>(acc, a.tpart + sy.tb0, &s->cnt[0], out, lb, sy.ntb) && threadIdx.x == 0 &&
+        threadIdx.y == 0)
+        mx_after_A(s, out[0], 0, 0);
+}
+
+// B: Ap = D^dagger t (staggered; Laplace reads Ap from t) ; x_lo += alpha p' ; r -= alpha Ap
+template <class S, class R, class LK, int BY, int NY>
+__global__ void __launch_bounds__(32 * BY) k_bB(BArgs<S, R, LK> a)
+{
+    const int sid = a.tblk[blockIdx.x];
+    const BSys sy = a.sys[sid];
+    MxDev *s = a.st + sid;
+    if (s->done || s->reliable) return;
+    const int lb = blockIdx.x - sy.tb0;
+    const int x = (lb % sy.tiles_x) * 32 + threadIdx.x;
+    const int ybase = (lb / sy.tiles_x) * (BY * NY) + threadIdx.y * NY;
+    const int par = s->parity;  // A wrote the new direction into the other buffer
+    const long o = sy.off;
+    const S *p = (par ? a.p0 : a.p1) + o;
+    const float alpha = (float)s->alpha;
+    float acc[1];
+    if (!sy.stag)
+        acc[0] = lap_tile_B<S, R, NY>(a.t + o, p, a.r + o, a.xlo + o, alpha, sy.lx, sy.ly, x, ybase);
+    else if (sy.xs)
+        acc[0] = tile_B<S, R, LK, NY, true, false>(a.t + o, p, a.r + o, a.xlo + o, a.L + 2 * o, alpha,
+                                                   (float)sy.mass, 0.f, sy.lx, sy.ly, threadIdx.x, x, true, ybase);
+    else
+        acc[0] = tile_B<S, R, LK, NY, false, false>(a.t + o, p, a.r + o, a.xlo + o, a.L + 2 * o, alpha,
+                                                    (float)sy.mass, 0.f, sy.lx, sy.ly, threadIdx.x, x, x < sy.lx,
+                                                    ybase);
+    double out[1];
+    if (grid_sum_f_ids<1, 32 * BY>(acc, a.tpart + sy.tb0, &s->cnt[1], out, lb, sy.ntb) && threadIdx.x == 0 &&
+        threadIdx.y == 0)
+        mx_after_B(s, out[0], 1 - par, 0, 0);
+}
+
+// ---------------------------------------------------------------- reliable-update kernels
+// One block covers up to kVecSites sites of one system; `upd` is true for systems that run a
+// reliable update in this pass.
+
+#define BATCH_VEC_PROLOGUE                                                                  \
+    const int sid = a.vblk[blockIdx.x];                                                     \
+    const BSys sy = a.sys[sid];                                                             \
+    MxDev *s = a.st + sid;                                                                  \
+    if (s->done || !s->reliable) return;                                                    \
+    const unsigned lb = blockIdx.x - sy.vb0;                                                \
+    const long n = (long)sy.lx * sy.ly, o = sy.off;                                         \
+    const long i0 = (long)lb * kRedThreads + threadIdx.x, di = (long)sy.nvb * kRedThreads;
+
+// R1: x_hi += scale x_lo ; x_lo = 0
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bR1(BArgs<S, R, LK> a)
+{
+    BATCH_VEC_PROLOGUE
+    const double sc = s->scale;
+    for (long i = i0; i < n; i += di) {
+        const float2 d = a.xlo[o + i];
+        const double2 xv = sy.x[i];
+        sy.x[i] = cmk(xv.x + sc * (double)d.x, xv.y + sc * (double)d.y);
+        a.xlo[o + i] = make_float2(0.f, 0.f);
+    }
+}
+
+// FP64 operator on x: staggered pass 1 (tmp = D x) or the Laplacian (Ax = L x)
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bOp1(BArgs<S, R, LK> a)
+{
+    BATCH_VEC_PROLOGUE
+    const double2 *x = sy.x;
+    auto ld = [x](long j) { return x[j]; };
+    for (long i = i0; i < n; i += di) {
+        if (sy.stag) a.tmp64[o + i] = stag_site(ld, sy.U, sy.mass, sy.lx, sy.ly, +1.0, i);
+        else a.Ax[o + i] = lap_site(ld, sy.U, sy.mass, sy.lx, sy.ly, i);
+    }
+}
+
+// staggered pass 2: Ax = D^dagger tmp
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bOp2(BArgs<S, R, LK> a)
+{
+    BATCH_VEC_PROLOGUE
+    if (!sy.stag) return;
+    const double2 *tm = a.tmp64 + o;
+    auto ld = [tm](long j) { return tm[j]; };
+    for (long i = i0; i < n; i += di) a.Ax[o + i] = stag_site(ld, sy.U, sy.mass, sy.lx, sy.ly, -1.0, i);
+}
+
+// R2: r_hi = b - A x ; |r_hi|^2 -> convergence and the new scale (as k_mx_R2, sigma = 0)
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bR2(BArgs<S, R, LK> a)
+{
+    BATCH_VEC_PROLOGUE
+    double v[1] = {0.0};
+    for (long i = i0; i < n; i += di) {
+        const double2 ri = csub(sy.b[i], a.Ax[o + i]);
+        a.rhi[o + i] = ri;
+        v[0] += cabs2(ri);
+    }
+    if (!(grid_sum_ids<1, kRedThreads>(v, a.vpart + 2 * sy.vb0, &s->cnt[2], lb, sy.nvb) && threadIdx.x == 0))
+        return;
+    const double rt = v[0];
+    s->rsq_old_true = s->rsq * s->scale * s->scale;
+    s->rsq_true = rt;
+    s->n_reliable++;
+    const double bsqrt = sqrt(s->bsq);
+    if (!isfinite(rt)) {
+        s->status = GLINALG_SOLVE_NONFINITE;
+        s->done = 1;
+        return;
+    }
+    if (sqrt(rt) < s->eps * bsqrt) {
+        s->status = GLINALG_SOLVE_CONVERGED;
+        s->done = 1;
+        return;
+    }
+    if (s->k >= s->max_iter) {
+        s->status = GLINALG_SOLVE_MAX_ITER;
+        s->done = 1;
+        return;
+    }
+    const double new_scale = sqrt(rt / (double)n);
+    s->pscale = s->scale / new_scale;
+    s->scale = new_scale;
+    s->rmax = sqrt(rt);
+}
+
+// R3: r_lo = r_hi / scale ; p *= pscale ; <r_lo, p>, |r_lo|^2 (as k_mx_R3)
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bR3(BArgs<S, R, LK> a)
+{
+    BATCH_VEC_PROLOGUE
+    S *plo = (s->parity ? a.p1 : a.p0) + o;
+    R *rlo = a.r + o;
+    const double inv = 1.0 / s->scale;
+    const float f = (float)s->pscale;
+    double v[2] = {0.0, 0.0};
+    for (long i = i0; i < n; i += di) {
+        const double2 rh = a.rhi[o + i];
+        Fmt<R>::st(rlo, i, make_float2((float)(rh.x * inv), (float)(rh.y * inv)));
+        const float2 pq = fscale(f, Fmt<S>::ld(plo, i));
+        Fmt<S>::st(plo, i, pq);
+        const float2 rq = Fmt<R>::ld(rlo, i), pr = Fmt<S>::ld(plo, i);
+        v[0] += (double)(rq.x * pr.x + rq.y * pr.y);
+        v[1] += (double)fn2(rq);
+    }
+    if (grid_sum_ids<2, kRedThreads>(v, a.vpart + 2 * sy.vb0, &s->cnt[3], lb, sy.nvb) && threadIdx.x == 0) {
+        const double rr = v[1];
+        s->rp = rr > 0.0 ? v[0] / rr : 0.0;
+        const double sc2 = s->scale * s->scale;
+        s->beta = s->rsq_old_true > 0.0 ? (rr * sc2) / s->rsq_old_true : 0.0;
+        s->rsq = rr;
+    }
+}
+
+// R4: p0 = p - rp r_lo (the direction is in p0 afterwards)
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bR4(BArgs<S, R, LK> a)
+{
+    BATCH_VEC_PROLOGUE
+    const S *plo = (s->parity ? a.p1 : a.p0) + o;
+    S *p0 = a.p0 + o;
+    const R *rlo = a.r + o;
+    const float rp = (float)s->rp;
+    for (long i = i0; i < n; i += di) Fmt<S>::st(p0, i, fsub(Fmt<S>::ld(plo, i), fscale(rp, Fmt<R>::ld(rlo, i))));
+}
+
+// |b|^2 of every system
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bNorm(BArgs<S, R, LK> a)
+{
+    const int sid = a.vblk[blockIdx.x];
+    const BSys sy = a.sys[sid];
+    MxDev *s = a.st + sid;
+    const unsigned lb = blockIdx.x - sy.vb0;
+    const long n = (long)sy.lx * sy.ly;
+    double v[1] = {0.0};
+    for (long i = (long)lb * kRedThreads + threadIdx.x; i < n; i += (long)sy.nvb * kRedThreads)
+        v[0] += cabs2(sy.b[i]);
+    if (grid_sum_ids<1, kRedThreads>(v, a.vpart + 2 * sy.vb0, &s->cnt[4], lb, sy.nvb) && threadIdx.x == 0)
+        s->bsq = v[0];
+}
+
+// r = 1 at every site (the autotuner's input)
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bFillR(BArgs<S, R, LK> a)
+{
+    const int sid = a.vblk[blockIdx.x];
+    const BSys sy = a.sys[sid];
+    const unsigned lb = blockIdx.x - sy.vb0;
+    const long n = (long)sy.lx * sy.ly;
+    for (long i = (long)lb * kRedThreads + threadIdx.x; i < n; i += (long)sy.nvb * kRedThreads)
+        Fmt<R>::st(a.r + sy.off, i, make_float2(1.f, 0.f));
+}
+
+// Links in the inner format: the staggered hopping table (1/2 and eta folded in, as k_make_hop)
+// or the Laplacian's links as they are.
+template <class S, class R, class LK>
+__global__ void __launch_bounds__(kRedThreads) k_bLinks(BArgs<S, R, LK> a)
+{
+    const int sid = a.vblk[blockIdx.x];
+    const BSys sy = a.sys[sid];
+    const unsigned lb = blockIdx.x - sy.vb0;
+    const long n = (long)sy.lx * sy.ly, o = sy.off;
+    for (long i = (long)lb * kRedThreads + threadIdx.x; i < n; i += (long)sy.nvb * kRedThreads) {
+        if (sy.stag) {
+            const int x = (int)(i % sy.lx);
+            const double eta = (x & 1) ? -1.0 : 1.0;
+            a.L[2 * (o + i)] = Fmt<LK>::from(cscale(-0.5, sy.U[2 * i]));
+            a.L[2 * (o + i) + 1] = Fmt<LK>::from(cscale(-0.5 * eta, sy.U[2 * i + 1]));
+        } else {
+            a.L[2 * (o + i)] = Fmt<LK>::from(sy.U[2 * i]);
+            a.L[2 * (o + i) + 1] = Fmt<LK>::from(sy.U[2 * i + 1]);
+        }
+    }
+}
+
+// After the reliable-update steps: systems that ran one go back to iterating (as
+// k_mx_outer_tail); when every system has stopped, the loop ends.  setup = 1 after the initial
+// residual computation (no outer-iteration count).
+__global__ void k_bTail(MxDev *st, int nsys, int *all_done, int setup)
+{
+    __shared__ int fin;
+    if (threadIdx.x == 0) fin = 0;
+    __syncthreads();
+    int mine = 0;
+    for (int q = threadIdx.x; q < nsys; q += blockDim.x) {
+        MxDev *s = st + q;
+        if (s->reliable && !s->done) {
+            if (!setup) {
+                s->outer++;
+                if (s->outer > s->max_iter + 2) {
+                    s->status = GLINALG_SOLVE_MAX_ITER;
+                    s->done = 1;
+                }
+            }
+            if (!s->done) {
+                s->reliable = 0;
+                s->parity = 0;
+            }
+        }
+        mine += s->done != 0;
+    }
+    atomicAdd(&fin, mine);
+    __syncthreads();
+    if (threadIdx.x == 0 && fin == nsys) *all_done = 1;
+}
+
+// ---------------------------------------------------------------- tile candidates
+
+constexpr int kNumBatchTiles = 4;
+constexpr int kBatchTileRows[kNumBatchTiles] = {16, 32, 32, 32};  // BY * NY
+
+template <class S, class R, class LK>
+struct BKern {
+    void (*A)(BArgs<S, R, LK>);
+    void (*B)(BArgs<S, R, LK>);
+    dim3 block;
+};
+
+template <class S, class R, class LK>
+BKern<S, R, LK> batch_kernels(int c)
+{
+    switch (c) {
+    case 0: return {k_bA<S, R, LK, 8, 2>, k_bB<S, R, LK, 8, 2>, dim3(32, 8)};
+    case 1: return {k_bA<S, R, LK, 8, 4>, k_bB<S, R, LK, 8, 4>, dim3(32, 8)};
+    case 2: return {k_bA<S, R, LK, 4, 8>, k_bB<S, R, LK, 4, 8>, dim3(32, 4)};
+    default: return {k_bA<S, R, LK, 16, 2>, k_bB<S, R, LK, 16, 2>, dim3(32, 16)};
+    }
+}
+
+std::mutex g_btune_mu;
+std::map<std::tuple<int, int, std::vector<int>>, int> g_btuned;
+
+// Tile-block layout of the batch for candidate c; returns the number of tile blocks.
+int layout_tiles(std::vector<BSys> &sys, std::vector<int> &tblk, int c)
+{
+    const int rows = kBatchTileRows[c];
+    tblk.clear();
+    for (int q = 0; q < (int)sys.size(); q++) {
+        BSys &y = sys[q];
+        y.tiles_x = (y.lx + 31) / 32;
+        y.tb0 = (int)tblk.size();
+        y.ntb = y.tiles_x * ((y.ly + rows - 1) / rows);
+        tblk.insert(tblk.end(), y.ntb, q);
+    }
+    return (int)tblk.size();
+}
+
+template <class S, class R, class LK>
+glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2 *const *X,
+                         const double2 *const *B, int max_iter, double eps, double delta, int variant,
+                         glinalg_info *infos, cudaStream_t st, const char *name)
+{
+    const int dev = ops[0]->device;
+    Scratch sc(st);
+    std::vector<BSys> sys(nsys);
+    std::vector<int> vblk, tblk;
+    long N = 0;
+    std::vector<int> sig;
+    for (int q = 0; q < nsys; q++) {
+        const glinalg_operator_s *op = ops[q];
+        BSys &y = sys[q];
+        y = BSys{};
+        y.off = N;
+        y.U = op->U;
+        y.x = X[q];
+        y.b = B[q];
+        y.mass = op->mass;
+        y.lx = op->lx;
+        y.ly = op->ly;
+        y.stag = op->kind == GLINALG_OP_STAGGERED_NORMAL;
+        y.xs = op->lx % 32 == 0;
+        const long n = op->size;
+        y.vb0 = (int)vblk.size();
+        y.nvb = (int)((n + kVecSites - 1) / kVecSites);
+        vblk.insert(vblk.end(), y.nvb, q);
+        N += n;
+        sig.push_back(y.lx);
+        sig.push_back(y.ly);
+        sig.push_back(y.stag);
+    }
+    const int nvb = (int)vblk.size();
+    BArgs<S, R, LK> a = {};
+    GL_TRY(sc.alloc(&a.r, N));
+    GL_TRY(sc.zeros(&a.p0, N));
+    GL_TRY(sc.zeros(&a.p1, N));
+    GL_TRY(sc.alloc(&a.t, N));
+    GL_TRY(sc.zeros(&a.xlo, N));
+    GL_TRY(sc.alloc(&a.L, 2 * N));
+    GL_TRY(sc.alloc(&a.rhi, N));
+    GL_TRY(sc.alloc(&a.tmp64, N));
+    GL_TRY(sc.alloc(&a.Ax, N));
+    GL_TRY(sc.alloc(&a.vpart, 2 * (size_t)nvb));
+    GL_TRY(sc.zeros(&a.st, nsys));
+    GL_TRY(sc.zeros(&a.all_done, 1));
+    BSys *dsys;
+    int *dvblk, *dtblk;
+    GL_TRY(sc.alloc(&dsys, nsys));
+    GL_TRY(sc.alloc(&dvblk, nvb));
+    // the largest tile-block count over the candidates
+    int max_tb = 0;
+    for (int c = 0; c < kNumBatchTiles; c++) max_tb = std::max(max_tb, layout_tiles(sys, tblk, c));
+    GL_TRY(sc.alloc(&dtblk, max_tb));
+    GL_TRY(sc.alloc(&a.tpart, max_tb));
+    a.sys = dsys;
+    a.vblk = dvblk;
+    a.tblk = dtblk;
+    a.nsys = nsys;
+    GL_CUDA(cudaMemcpyAsync(dvblk, vblk.data(), sizeof(int) * nvb, cudaMemcpyHostToDevice, st));
+    auto upload = [&](int c) -> glinalg_status {
+        const int ntb = layout_tiles(sys, tblk, c);
+        GL_CUDA(cudaMemcpyAsync(dsys, sys.data(), sizeof(BSys) * nsys, cudaMemcpyHostToDevice, st));
+        GL_CUDA(cudaMemcpyAsync(dtblk, tblk.data(), sizeof(int) * ntb, cudaMemcpyHostToDevice, st));
+        return GLINALG_SUCCESS;
+    };
+    GL_TRY(upload(0));
+    k_bLinks<S, R, LK><<<nvb, kRedThreads, 0, st>>>(a);
+    GL_CUDA(cudaGetLastError());
+
+    // ---- tile shape for this batch: time two inner iterations of every candidate once
+    int cand = -1;
+    const auto key = std::make_tuple(dev, variant, sig);
+    {
+        std::lock_guard<std::mutex> lk(g_btune_mu);
+        auto it = g_btuned.find(key);
+        if (it != g_btuned.end()) cand = it->second;
+    }
+    if (const char *e = std::getenv("GLINALG_TILE")) {
+        const int c = std::atoi(e);
+        if (c >= 0 && c < kNumBatchTiles) cand = c;
+    }
+    if (cand < 0) {
+        std::vector<MxDev> hs(nsys);
+        for (int q = 0; q < nsys; q++) {
+            hs[q] = MxDev{};
+            hs[q].rsq = (double)ops[q]->size;  // |r|^2 of r = 1
+            hs[q].scale = 1.0;
+            hs[q].bsq = 1.0;
+            hs[q].rmax = 1e300;  // delta = eps = 0: no reliable update during the timing
+            hs[q].max_iter = 1 << 30;
+        }
+        cudaEvent_t e0, e1;
+        GL_CUDA(cudaEventCreate(&e0));
+        GL_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        for (int c = 0; c < kNumBatchTiles; c++) {
+            GL_TRY(upload(c));
+            const BKern<S, R, LK> k = batch_kernels<S, R, LK>(c);
+            const int ntb = sys.back().tb0 + sys.back().ntb;
+            float m = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
+                // r = 1 everywhere, p = 0, fresh state
+                k_bFillR<S, R, LK><<<nvb, kRedThreads, 0, st>>>(a);
+                GL_CUDA(cudaMemsetAsync(a.p0, 0, sizeof(S) * N, st));
+                GL_CUDA(cudaMemcpyAsync(a.st, hs.data(), sizeof(MxDev) * nsys, cudaMemcpyHostToDevice, st));
+                k_busy_wait<<<1, 1, 0, st>>>(30000);  // keep launch latency out of the events
+                GL_CUDA(cudaEventRecord(e0, st));
+                for (int it = 0; it < 2; it++) {
+                    k.A<<<ntb, k.block, 0, st>>>(a);
+                    k.B<<<ntb, k.block, 0, st>>>(a);
+                }
+                GL_CUDA(cudaEventRecord(e1, st));
+                GL_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                GL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                m = std::min(m, ms);
+            }
+            if (m < best) {
+                best = m;
+                cand = c;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        std::lock_guard<std::mutex> lk(g_btune_mu);
+        g_btuned[key] = cand;
+        GL_CUDA(cudaMemsetAsync(a.p0, 0, sizeof(S) * N, st));
+        GL_CUDA(cudaMemsetAsync(a.p1, 0, sizeof(S) * N, st));
+        GL_CUDA(cudaMemsetAsync(a.xlo, 0, sizeof(float2) * N, st));
+    }
+    GL_TRY(upload(cand));
+    const BKern<S, R, LK> k = batch_kernels<S, R, LK>(cand);
+    const int ntb = sys.back().tb0 + sys.back().ntb;
+
+    // ---- initial state: every system starts with a reliable update (r = b - A x0)
+    {
+        std::vector<MxDev> hs(nsys);
+        for (int q = 0; q < nsys; q++) {
+            hs[q] = MxDev{};
+            hs[q].eps = eps;
+            hs[q].delta = delta;
+            hs[q].max_iter = max_iter;
+            hs[q].scale = 1.0;
+            hs[q].reliable = 1;
+        }
+        GL_CUDA(cudaMemcpyAsync(a.st, hs.data(), sizeof(MxDev) * nsys, cudaMemcpyHostToDevice, st));
+    }
+    EventTimer tm;
+    tm.start(st);
+    auto reliable_seq = [&](cudaStream_t cs) -> glinalg_status {
+        k_bR1<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        k_bOp1<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        k_bOp2<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        k_bR2<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        k_bR3<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        k_bR4<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        GL_CUDA(cudaGetLastError());
+        return GLINALG_SUCCESS;
+    };
+    k_bNorm<S, R, LK><<<nvb, kRedThreads, 0, st>>>(a);
+    GL_TRY(reliable_seq(st));
+    k_bTail<<<1, 256, 0, st>>>(a.st, nsys, a.all_done, 1);
+    GL_CUDA(cudaGetLastError());
+    GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
+        for (int u = 0; u < kBatchUnroll; u++) {
+            k.A<<<ntb, k.block, 0, cs>>>(a);
+            k.B<<<ntb, k.block, 0, cs>>>(a);
+        }
+        GL_TRY(reliable_seq(cs));
+        k_bTail<<<1, 256, 0, cs>>>(a.st, nsys, a.all_done, 0);
+        GL_CUDA(cudaGetLastError());
+        return GLINALG_SUCCESS;
+    }));
+    tm.stop(st);
+    std::vector<MxDev> hs(nsys);
+    GL_CUDA(cudaMemcpyAsync(hs.data(), a.st, sizeof(MxDev) * nsys, cudaMemcpyDeviceToHost, st));
+    GL_CUDA(cudaStreamSynchronize(st));
+    const double w = Fmt<S>::bytes, wr = Fmt<R>::bytes, wl = Fmt<LK>::bytes;
+    for (int q = 0; q < nsys; q++) {
+        const MxDev &h = hs[q];
+        const long n = ops[q]->size;
+        glinalg_info *info = &infos[q];
+        double *keep = info->resSqmrhs;
+        *info = glinalg_info{};
+        info->resSqmrhs = keep;
+        info->resSq = h.rsq_true;
+        info->iter = h.k;
+        info->success = h.status == GLINALG_SOLVE_CONVERGED ? 1 : 0;
+        info->ops_count = h.k + h.n_reliable;
+        info->status = h.status;
+        info->reliable_updates = h.n_reliable;
+        info->device_ms = tm.ms();
+        const bool stg = sys[q].stag;
+        const double per_iter = stg ? (6.0 * w + 4.0 * wl + 3.0 * wr + 16.0) : (6.0 * w + 2.0 * wl + 3.0 * wr + 16.0);
+        const double per_rel = 16.0 * 2 + 16.0 + 8.0 * 64.0 / 8.0 + 16.0 * 3 + 2 * wr + 4 * w;
+        info->gbytes = ((double)h.k * per_iter * n + (double)h.n_reliable * per_rel * n) * 1e-9;
+        fill_name(info, name);
+    }
+    return GLINALG_SUCCESS;
+}
+
+}  // namespace
+
+glinalg_status cg_batch_mixed(const glinalg_operator_s *const *ops, int nsys, double2 *const *X,
+                              const double2 *const *B, int max_iter, double eps, int precision, double delta,
+                              glinalg_info *infos, cudaStream_t st)
+{
+    if (!(delta > 0.0 && delta < 1.0)) delta = 0.1;
+    switch (precision) {
+    case GLINALG_PREC_SINGLE:
+        return run_batch<float2, float2, float2>(ops, nsys, X, B, max_iter, eps, delta, 1, infos, st, "CG-FP32");
+    case GLINALG_PREC_HALF:
+        return run_batch<__half2, float2, __half2>(ops, nsys, X, B, max_iter, eps, delta, 2, infos, st, "CG-FP16");
+    case GLINALG_PREC_BFLOAT:
+        return run_batch<__nv_bfloat162, float2, float2>(ops, nsys, X, B, max_iter, eps, delta, 3, infos, st,
+                                                         "CG-BF16");
+    default:
+        set_last_error("batched mixed-precision CG: precision must be SINGLE, HALF or BFLOAT");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+}
+
+}  // namespace glinalg

@@ -150,6 +150,50 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double *partials, unsig
     return true;
 }
 
+template <int K, int NT>
+__device__ __forceinline__ bool grid_sum_ids(double (&v)[K], double *partials, unsigned *counter,
+                                             unsigned bid, unsigned nbk);
+// grid_sum for grids whose rows (blockIdx.y) are independent problems: sums over the blocks
+// of this block's row only (1D blocks of NT threads).  partials and counter belong to the row.
+template <int K, int NT>
+__device__ __forceinline__ bool grid_sum_row(double (&v)[K], double *partials, unsigned *counter)
+{
+    return grid_sum_ids<K, NT>(v, partials, counter, blockIdx.x, gridDim.x);
+}
+
+// grid_sum over a group of nbk blocks that reduce one problem together (1D blocks of NT
+// threads); bid is this block's index within the group.  partials and counter belong to the
+// group.
+template <int K, int NT>
+__device__ __forceinline__ bool grid_sum_ids(double (&v)[K], double *partials, unsigned *counter,
+                                             unsigned bid, unsigned nbk)
+{
+    __shared__ unsigned ticket;
+    const unsigned tid = threadIdx.x;
+    block_sum<K, NT>(v);
+    if (tid == 0) {
+#pragma unroll
+        for (int j = 0; j < K; j++) partials[(size_t)j * nbk + bid] = v[j];
+        __threadfence();
+        ticket = atomicAdd(counter, 1u);
+    }
+    __syncthreads();
+    if (ticket != nbk - 1) return false;
+    __threadfence();
+    double s[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) s[j] = 0.0;
+    for (unsigned b = tid; b < nbk; b += NT) {
+#pragma unroll
+        for (int j = 0; j < K; j++) s[j] += __ldcg(partials + (size_t)j * nbk + b);
+    }
+    block_sum<K, NT>(s);
+#pragma unroll
+    for (int j = 0; j < K; j++) v[j] = s[j];
+    if (tid == 0) *counter = 0u;
+    return true;
+}
+
 // Grid used by every reduction kernel over n elements (fixed for a given n, so reductions
 // are reproducible run to run).
 int reduction_blocks(long n);

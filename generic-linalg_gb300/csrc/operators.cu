@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "operator.h"
+#include "sites.cuh"
 
 namespace glinalg {
 
@@ -118,9 +119,6 @@ double apply_bytes(const glinalg_operator_s *op)
 
 // ---------------------------------------------------------------- kernels
 
-__device__ __forceinline__ int wrap_p(int v, int n) { return v + 1 == n ? 0 : v + 1; }
-__device__ __forceinline__ int wrap_m(int v, int n) { return v == 0 ? n - 1 : v - 1; }
-
 // square_staggered_u1 (sign = +1) and square_staggered_dagger_u1 (sign = -1), FP64,
 // one site per thread.
 __global__ void k_staggered(double2 *__restrict__ out, const double2 *__restrict__ in,
@@ -129,45 +127,23 @@ __global__ void k_staggered(double2 *__restrict__ out, const double2 *__restrict
 {
     if (done && *done) return;
     const long vol = (long)lx * ly;
+    auto ld = [in](long j) { return in[j]; };
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < vol;
-         i += (long)gridDim.x * blockDim.x) {
-        const int y = (int)(i / lx), x = (int)(i - (long)y * lx);
-        const int xp = wrap_p(x, lx), xm = wrap_m(x, lx), yp = wrap_p(y, ly), ym = wrap_m(y, ly);
-        const double eta = (x & 1) ? -1.0 : 1.0;
-        const long row = (long)y * lx;
-        double2 acc = cmk(0.0, 0.0), t;
-        t = cmul(U[2 * i], in[row + xp]);
-        acc = sign > 0 ? csub(acc, t) : cadd(acc, t);
-        t = cmul(cconj(U[2 * (row + xm)]), in[row + xm]);
-        acc = sign > 0 ? cadd(acc, t) : csub(acc, t);
-        t = cmul(cscale(eta, U[2 * i + 1]), in[(long)yp * lx + x]);
-        acc = sign > 0 ? csub(acc, t) : cadd(acc, t);
-        t = cmul(cscale(eta, cconj(U[2 * ((long)ym * lx + x) + 1])), in[(long)ym * lx + x]);
-        acc = sign > 0 ? cadd(acc, t) : csub(acc, t);
-        acc = cscale(0.5, acc);
-        out[i] = cadd(acc, cscale(mass, in[i]));
-    }
+         i += (long)gridDim.x * blockDim.x)
+        out[i] = stag_site(ld, U, mass, lx, ly, sign, i);
 }
 
-// square_laplace_u1, FP64.  sigma is an extra diagonal shift (0 for the plain operator).
+// square_laplace_u1, FP64.
 __global__ void k_laplace(double2 *__restrict__ out, const double2 *__restrict__ in,
                           const double2 *__restrict__ U, double mass, int lx, int ly,
                           const int *__restrict__ done)
 {
     if (done && *done) return;
     const long vol = (long)lx * ly;
+    auto ld = [in](long j) { return in[j]; };
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < vol;
-         i += (long)gridDim.x * blockDim.x) {
-        const int y = (int)(i / lx), x = (int)(i - (long)y * lx);
-        const int xp = wrap_p(x, lx), xm = wrap_m(x, lx), yp = wrap_p(y, ly), ym = wrap_m(y, ly);
-        const long row = (long)y * lx;
-        double2 acc = cmk(0.0, 0.0);
-        acc = csub(acc, cmul(U[2 * i], in[row + xp]));
-        acc = csub(acc, cmul(cconj(U[2 * (row + xm)]), in[row + xm]));
-        acc = csub(acc, cmul(U[2 * i + 1], in[(long)yp * lx + x]));
-        acc = csub(acc, cmul(cconj(U[2 * ((long)ym * lx + x) + 1]), in[(long)ym * lx + x]));
-        out[i] = cadd(acc, cscale(4.0 + mass, in[i]));
-    }
+         i += (long)gridDim.x * blockDim.x)
+        out[i] = lap_site(ld, U, mass, lx, ly, i);
 }
 
 // apply_stencil_2d (parity 0), _eo (parity 1: even output sites, hopping only) and _oe

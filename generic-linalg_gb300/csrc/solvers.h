@@ -17,6 +17,17 @@ glinalg_status gcr_fp64(const glinalg_operator_s *op, double2 *x, const double2 
 glinalg_status cg_m_fp64(const glinalg_operator_s *op, double2 *const *X, const double2 *b,
                          int n_shift, int rfc, int max_iter, double eps, const double *shifts,
                          bool worst_first, const Verb &verb, glinalg_info *info, cudaStream_t st);
+// Multishift CG of n_rhs sources advanced together (cgm_batch.cu); X: n_rhs * n_shift fields
+// (source-major), B: n_rhs fields.  Staggered-normal and Laplace kinds, n_shift <= 32.
+bool cg_m_batch_supported(const glinalg_operator_s *op, int n_shift);
+glinalg_status cg_m_batch(const glinalg_operator_s *op, double2 *X, const double2 *B, int n_rhs,
+                          int n_shift, int rfc, int max_iter, double eps, const double *shifts,
+                          glinalg_info *infos, cudaStream_t st);
+// Mixed-precision CG (FP64 reliable updates) on nsys independent systems of any sizes,
+// staggered-normal or Laplace kinds, advanced together (cg_batch.cu).  X[q], B[q]: device fields.
+glinalg_status cg_batch_mixed(const glinalg_operator_s *const *ops, int nsys, double2 *const *X,
+                              const double2 *const *B, int max_iter, double eps, int precision, double delta,
+                              glinalg_info *infos, cudaStream_t st);
 // which: 0 CG, 1 BiCGstab, 2 GCR
 glinalg_status restart_driver(int which, const glinalg_operator_s *op, double2 *x,
                               const double2 *b, int max_iter, double eps, int restart_freq,

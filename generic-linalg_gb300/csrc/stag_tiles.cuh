@@ -67,12 +67,24 @@ __device__ __forceinline__ float2 shfl_up2(float2 v, int d)
 // of its first thread.  partials: K * (number of blocks) doubles; *counter is 0 on entry
 // and left 0.
 template <int K, int NT>
+__device__ __forceinline__ bool grid_sum_f_ids(float (&vf)[K], double *partials, unsigned *counter,
+                                               double (&out)[K], unsigned bid, unsigned nbk);
+template <int K, int NT>
 __device__ __forceinline__ bool grid_sum_f(float (&vf)[K], double *partials, unsigned *counter,
                                            double (&out)[K])
 {
+    return grid_sum_f_ids<K, NT>(vf, partials, counter, out, flat_bid(), flat_nblocks());
+}
+
+// grid_sum_f over a group of nbk blocks that reduce one problem together; bid is this block's
+// index within the group.
+template <int K, int NT>
+__device__ __forceinline__ bool grid_sum_f_ids(float (&vf)[K], double *partials, unsigned *counter,
+                                               double (&out)[K], unsigned bid, unsigned nbk)
+{
     __shared__ double sm[K][NT / 32];
     __shared__ unsigned ticket;
-    const unsigned tid = flat_tid(), bid = flat_bid(), nbk = flat_nblocks();
+    const unsigned tid = flat_tid();
     const int lane = tid & 31, warp = tid >> 5;
 #pragma unroll
     for (int j = 0; j < K; j++) {
