@@ -39,7 +39,7 @@ REF_ITERS = 2093
 METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB300; HBM GB/s"
 HEADLINE = ("fp32", 1)
 # DRAM bytes (read + write) of one launch of the FP32 persistent inner-loop kernel on this
-# workload, from an ncu --set full capture (profiles/k_persist_fp32_1024.md)
+# workload (the first launch of a solve, 254 inner iterations), from an ncu --set full capture
 K_PERSIST_DRAM_BYTES = 41.987328e6 + 3.212544e6
 VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 
@@ -168,6 +168,23 @@ def kernels_only(args):
     for nm, j in (("A", 0), ("B", 1)):
         print(json.dumps({"kernel": nm, "variant": HEADLINE[0], "ms": kms[j], "bytes": kbytes[j],
                           "GB/s": kbytes[j] / (kms[j] * 1e-3) / 1e9}))
+
+
+def probe_solve(args):
+    """One headline-variant solve of the 1024x1024 system stopped after --probe-iters inner
+    iterations: one launch of the persistent inner-loop kernel, a small case for ncu captures."""
+    import torch
+    gl = importlib.import_module("generic-linalg_gb300")
+    g = gl.Generator(SEED)
+    U = g.rand_gauge_u1(LX, LY)
+    b = g.gaussian(LX * LY)
+    op = gl.Operator(2, LX, LY, MASS, torch.from_numpy(U).cuda())
+    bd = torch.from_numpy(b).cuda()
+    x = torch.zeros_like(bd)
+    info = gl.minv_vector_cg(x, bd, bd.numel(), args.probe_iters, EPS, gl.square_staggered_normal_u1, op,
+                             precision=HEADLINE[1])
+    print(json.dumps({"probe": "headline variant, 1024x1024", "iters": info.iter,
+                      "kernel_launches": info.kernel_launches, "kernel_ms": info.kernel_ms}))
 
 
 def _flush_and_time(fn, flush, stream):
@@ -324,7 +341,12 @@ def main():
                          "(a small case for ncu captures)")
     ap.add_argument("--workload", default="headline", choices=["headline", "multishift", "batch"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")
+    ap.add_argument("--probe-iters", type=int, default=0,
+                    help="run one headline-variant solve stopped after this many inner iterations "
+                         "(one persistent-kernel launch; a small case for ncu captures) and exit")
     args = ap.parse_args()
+    if args.probe_iters > 0 and args.impl == "ours":
+        return probe_solve(args)
     if args.workload == "multishift" and args.impl == "ours":
         return workload_multishift(args)
     if args.workload == "batch" and args.impl == "ours":
@@ -481,7 +503,7 @@ def main():
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "traffic": K_PERSIST_DRAM_BYTES,
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one k_persist launch "
-                                     "(the first of a solve, 254 inner iterations; profiles/k_persist_fp32_1024.md): "
+                                     "(the first of a solve, 254 inner iterations; ncu --set full capture): "
                                      "the FP32 working set stays in L2, so DRAM traffic is the compulsory first read "
                                      "and does not grow with the iterations of a launch",
                      "kernel": f"k_persist<{head_name}> (inner CG iterations: D p, D^dagger t, updates, 2 grid barriers)",

@@ -40,6 +40,7 @@
 #include <vector>
 
 #include "mixed_state.cuh"
+#include "stag_bulk.cuh"
 
 namespace glinalg {
 
@@ -314,89 +315,6 @@ static int vgrid(long n)
 // blocks hold bitwise-identical scalars without a broadcast.  Fields written by other blocks
 // during the launch are read with ld.global.cg (L2), never through the non-coherent L1.
 
-struct GridSync {
-    unsigned arrive;
-    unsigned gen;
-    int error;
-    int pad;
-};
-
-__device__ __forceinline__ long long gtimer()
-{
-    long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bound on one barrier wait; a wait that runs out raises g->error (the solve then reports
-// GLINALG_SOLVE_TIMEOUT) instead of spinning on.
-constexpr long long kBarrierTimeoutNs = 2000000000LL;
-
-// Grid-wide barrier for a co-resident grid (generation counter; acquire/release atomics at
-// device scope).  Returns false in every thread of the block once any block has given up
-// waiting.
-__device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
-{
-    __shared__ int ok;
-    __syncthreads();
-    if (threadIdx.x == 0 && threadIdx.y == 0) {
-        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(g->gen), arr(g->arrive);
-        cuda::atomic_ref<int, cuda::thread_scope_device> err(g->error);
-        const unsigned my = gen.load(cuda::memory_order_acquire);
-        int good = 1;
-        const unsigned a = arr.fetch_add(1u, cuda::memory_order_acq_rel);
-        if (a == nblocks - 1) {
-            arr.store(0u, cuda::memory_order_relaxed);
-            gen.fetch_add(1u, cuda::memory_order_release);
-        } else {
-            const long long t0 = gtimer();
-            while (gen.load(cuda::memory_order_acquire) == my) {
-                if (err.load(cuda::memory_order_relaxed)) { good = 0; break; }
-                if (gtimer() - t0 > kBarrierTimeoutNs) {
-                    err.store(1, cuda::memory_order_relaxed);
-                    good = 0;
-                    break;
-                }
-            }
-        }
-        if (err.load(cuda::memory_order_relaxed)) good = 0;
-        ok = good;
-    }
-    __syncthreads();
-    return ok != 0;
-}
-
-// Sum of the per-block partials in block order, identical in every block; all threads get it.
-__device__ __forceinline__ double grid_total(const double *part, unsigned nb, double *sm)
-{
-    __syncthreads();
-    if (threadIdx.y == 0) {
-        double v = 0.0;
-        for (unsigned b = threadIdx.x; b < nb; b += 32) v += __ldcg(part + b);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) sm[32] = v;
-    }
-    __syncthreads();
-    return sm[32];
-}
-
-// Block sum of one float per thread (FP32 within warps, FP64 across the 32 warps) written to
-// part[blockIdx.x] by the block's first thread.
-__device__ __forceinline__ void block_partial(float acc, double *part, double *sm)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (threadIdx.x == 0) sm[threadIdx.y] = (double)acc;
-    __syncthreads();
-    if (threadIdx.y == 0) {
-        double v = threadIdx.x < blockDim.y ? sm[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (threadIdx.x == 0) part[blockIdx.x] = v;
-    }
-}
-
 template <class S, class R, class LK, int BY, int NY>
 __global__ void __launch_bounds__(32 * BY, 1)
 k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float mass, float sigma,
@@ -477,12 +395,22 @@ struct PersistKernel {
     F f = nullptr;
     int by = 0, ny = 0;
     int grid = 0;
+    int smem = 0;  // dynamic shared memory per block
 };
 
-// Persistent-kernel shapes (warps per block, rows per thread); one block per SM.
-constexpr int kNumPersist = 4;
-static const int kPersistBY[kNumPersist] = {16, 16, 32, 16};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2};
+// Persistent-kernel shapes (warps per block, rows per thread); one block per SM.  Candidate 4
+// is the bulk-copy kernel (stag_bulk.cuh: 16 warps, tiles staged through shared memory).
+constexpr int kNumPersist = 6;
+static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0};
+
+// Whether persistent candidate c serves an lx x ly lattice.
+static bool persist_cand_applies(int c, int lx, int ly)
+{
+    if (c == 4) return bulk_applies<bulk::Geom256x4>(lx, ly, sm_count());
+    if (c == 5) return bulk_applies<bulk::Geom512x2>(lx, ly, sm_count());
+    return true;
+}
 
 template <class S, class R, class LK>
 static PersistKernel<S, R, LK> persist_cand(int c)
@@ -494,10 +422,21 @@ static PersistKernel<S, R, LK> persist_cand(int c)
     case 0: pk.f = k_persist<S, R, LK, 16, 4>; break;
     case 1: pk.f = k_persist<S, R, LK, 16, 8>; break;
     case 2: pk.f = k_persist<S, R, LK, 32, 2>; break;
+    case 4: pk.f = k_persist_bulk<S, R, LK, bulk::Geom256x4>; break;
+    case 5: pk.f = k_persist_bulk<S, R, LK, bulk::Geom512x2>; break;
     default: pk.f = k_persist<S, R, LK, 16, 2>; break;
     }
+    if (c >= 4) {
+        pk.smem = c == 4 ? bulk::Layout<S, R, LK, bulk::Geom256x4>::SMEM : bulk::Layout<S, R, LK, bulk::Geom512x2>::SMEM;
+        if (cudaFuncSetAttribute(pk.f, cudaFuncAttributeMaxDynamicSharedMemorySize, pk.smem) != cudaSuccess) {
+            cudaGetLastError();
+            pk.f = nullptr;
+            return pk;
+        }
+    }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pk.f, 32 * pk.by, 0) != cudaSuccess || per_sm < 1) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pk.f, 32 * pk.by, pk.smem) != cudaSuccess ||
+        per_sm < 1) {
         cudaGetLastError();
         pk.f = nullptr;
         return pk;
@@ -532,7 +471,7 @@ static cudaError_t launch_persist(const PersistKernel<S, R, LK> &pk, cudaStream_
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(pk.grid);
     cfg.blockDim = dim3(32, pk.by);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = pk.smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -691,7 +630,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     }
     if (const char *e = std::getenv("GLINALG_PERSIST_SHAPE")) {  // as GLINALG_TILE
         const int c = std::atoi(e);
-        if (c >= 0 && c < kNumPersist) {
+        if (c >= 0 && c < kNumPersist && persist_cand_applies(c, lx, ly)) {
             std::lock_guard<std::mutex> lk(g_tune_mu);
             g_ptuned[key] = c;
             return;
@@ -715,6 +654,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     int best = -1;
     float best_ms = 1e30f;
     for (int c = 0; c < kNumPersist; c++) {
+        if (!persist_cand_applies(c, lx, ly)) continue;
         const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(c);
         if (!pk.f) continue;
         float m = 1e30f;

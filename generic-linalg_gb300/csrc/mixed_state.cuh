@@ -2,6 +2,8 @@
 // and the scalar updates that follow each inner kernel's reduction (cg_mixed.cu, cg_batch.cu).
 #pragma once
 
+#include <cuda/atomic>
+
 #include "solvers.h"
 #include "stag_tiles.cuh"
 
@@ -69,6 +71,91 @@ __device__ __forceinline__ void mx_after_B(MxDev *s, double rn, int dir_parity,
     }
     s->beta = rn / s->rsq;
     s->rsq = rn;
+}
+
+// ---------------------------------------------------------------- persistent-kernel helpers
+
+struct GridSync {
+    unsigned arrive;
+    unsigned gen;
+    int error;
+    int pad;
+};
+
+__device__ __forceinline__ long long gtimer()
+{
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bound on one barrier wait; a wait that runs out raises g->error (the solve then reports
+// GLINALG_SOLVE_TIMEOUT) instead of spinning on.
+constexpr long long kBarrierTimeoutNs = 2000000000LL;
+
+// Grid-wide barrier for a co-resident grid (generation counter; acquire/release atomics at
+// device scope).  Returns false in every thread of the block once any block has given up
+// waiting.
+__device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        cuda::atomic_ref<unsigned, cuda::thread_scope_device> gen(g->gen), arr(g->arrive);
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(g->error);
+        const unsigned my = gen.load(cuda::memory_order_acquire);
+        int good = 1;
+        const unsigned a = arr.fetch_add(1u, cuda::memory_order_acq_rel);
+        if (a == nblocks - 1) {
+            arr.store(0u, cuda::memory_order_relaxed);
+            gen.fetch_add(1u, cuda::memory_order_release);
+        } else {
+            const long long t0 = gtimer();
+            while (gen.load(cuda::memory_order_acquire) == my) {
+                if (err.load(cuda::memory_order_relaxed)) { good = 0; break; }
+                if (gtimer() - t0 > kBarrierTimeoutNs) {
+                    err.store(1, cuda::memory_order_relaxed);
+                    good = 0;
+                    break;
+                }
+            }
+        }
+        if (err.load(cuda::memory_order_relaxed)) good = 0;
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Sum of the per-block partials in block order, identical in every block; all threads get it.
+__device__ __forceinline__ double grid_total(const double *part, unsigned nb, double *sm)
+{
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double v = 0.0;
+        for (unsigned b = threadIdx.x; b < nb; b += 32) v += __ldcg(part + b);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) sm[32] = v;
+    }
+    __syncthreads();
+    return sm[32];
+}
+
+// Block sum of one float per thread (FP32 within warps, FP64 across the 32 warps) written to
+// part[blockIdx.x] by the block's first thread.
+__device__ __forceinline__ void block_partial(float acc, double *part, double *sm)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) sm[threadIdx.y] = (double)acc;
+    __syncthreads();
+    if (threadIdx.y == 0) {
+        double v = threadIdx.x < blockDim.y ? sm[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) part[blockIdx.x] = v;
+    }
 }
 
 }  // namespace glinalg

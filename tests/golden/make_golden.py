@@ -74,7 +74,7 @@ def main():
             o = Op(kind, lx, ly, nc=nc, clover=cl, hopping=hp, two_link=tl if two else None, **shifts)
             vec[f"st3_{kind}_two{two}"] = R.apply(o, x)
 
-    # ---- solvers on the 32x32 system (BASELINE configuration 1: m = 0.1, tol 1e-10)
+    # ---- solvers on the 32x32 system (m = 0.1, tol 1e-10)
     lx, ly = 32, 32
     U, b = vec["l32_links"], vec["l32_src"]
     normal = Op("staggered_normal", lx, ly, 0.1, U)

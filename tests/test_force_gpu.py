@@ -68,7 +68,7 @@ def test_gradient_vs_finite_differences_small(gl, gpu):
 
 
 def test_gradient_vs_finite_differences_256(gl, gpu):
-    """BASELINE configuration 5: 256x256, m = 0.05, sigma = 0, forward mixed-precision CG to
+    """The adjoint-gradient workload: 256x256, m = 0.05, sigma = 0, forward mixed-precision CG to
     1e-12; 64 seeded random links; central differences with h = 1e-5 in FP64.
 
     At this volume S is ~1e6 times a single link derivative, so S(theta+h) - S(theta-h)

@@ -67,7 +67,7 @@ def test_mixed_cg_initial_guess_and_device(gl, gpu, golden):
 
 @pytest.mark.parametrize("prec", ["single", "half", "bfloat"])
 def test_mixed_cg_1024_true_residual(gl, gpu, prec):
-    """The BASELINE configuration 2 system (1024x1024, m = 0.01): the mixed solve must reach
+    """The large single-lattice system (1024x1024, m = 0.01): the mixed solve must reach
     an FP64-true relative residual of 1e-10, re-checked with the FP64 GPU operator, and agree
     with the FP64 GPU CG solution to kappa * 1e-10 (kappa ~ 2e4)."""
     import torch

@@ -1,5 +1,5 @@
 """GPU solvers (FP64, the reference's recurrences) against the reference's own runs
-(golden fixtures, 32x32 U(1) system of BASELINE configuration 1: m = 0.1, tol 1e-10).
+(golden fixtures: the 32x32 U(1) system with m = 0.1, tol 1e-10).
 
 Bars: CG solution within 1e-11 relative of the reference's CG solution with the same
 iteration and operator counts; GCR within 1e-9 and +-1 iteration; CG-M per-shift solutions
