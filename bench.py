@@ -42,6 +42,12 @@ HEADLINE = ("fp32", 1)
 # workload (the first launch of a solve, 254 inner iterations), from an ncu --set full capture
 K_PERSIST_DRAM_BYTES = 41.987328e6 + 3.212544e6
 VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
+# persistent inner-loop kernels by the library's candidate index (glinalg_tuned_persist)
+PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 rows>",
+                   2: "k_persist<32 warps, 2 rows>", 3: "k_persist<16 warps, 2 rows>",
+                   4: "k_persist_bulk<256x4 tiles>", 5: "k_persist_bulk<512x2 tiles>",
+                   6: "k_resident<16 warps> (rectangle state on chip)",
+                   7: "k_resident<32 warps> (rectangle state on chip)"}
 
 
 def peaks():
@@ -447,6 +453,7 @@ def main():
     peak, peak_src = peaks()
     hi_ = head_infos[-1]
     k_launch = max(1, hi_.kernel_launches)
+    persist_kernel = PERSIST_KERNELS.get(L.glinalg_tuned_persist(op.handle, head_prec), "none")
     k_ms = hi_.kernel_ms / k_launch
     k_bytes = hi_.kernel_gbytes * 1e9 / k_launch
     achieved = (k_bytes / (k_ms * 1e-3) / 1e9) if k_ms > 0 else 0.0
@@ -506,7 +513,7 @@ def main():
                                      "(the first of a solve, 254 inner iterations; ncu --set full capture): "
                                      "the FP32 working set stays in L2, so DRAM traffic is the compulsory first read "
                                      "and does not grow with the iterations of a launch",
-                     "kernel": f"k_persist<{head_name}> (inner CG iterations: D p, D^dagger t, updates, 2 grid barriers)",
+                     "kernel": f"{persist_kernel} ({head_name}; inner CG iterations: D p, D^dagger t, updates, 2 grid barriers)",
                      "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 4),
                      "launches_per_solve": hi_.kernel_launches,
                      "share_of_solve": round(hi_.kernel_ms / hi_.device_ms, 3) if hi_.device_ms else None,

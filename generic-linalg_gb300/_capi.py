@@ -61,6 +61,7 @@ def _prototypes():
         "glinalg_set_stream": (st, [vp, i]),
         "glinalg_profile_mixed_kernels": (st, [vp, i, i, _dp, _dp]),
         "glinalg_tuned_tile": (i, [vp, i]),
+        "glinalg_tuned_persist": (i, [vp, i]),
         "glinalg_staggered_normal_apply_noalloc": (st, [_dp, d, i, i, _dp, _dp, vp]),
         "glinalg_operator_create": (st, [P(OpDesc), P(vp)]),
         "glinalg_operator_destroy": (st, [vp]),

@@ -37,10 +37,12 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 #include <vector>
 
 #include "mixed_state.cuh"
 #include "stag_bulk.cuh"
+#include "stag_resident.cuh"
 
 namespace glinalg {
 
@@ -392,32 +394,109 @@ template <class S, class R, class LK>
 struct PersistKernel {
     using F = void (*)(const LK *, R *, S *, S *, S *, float2 *, float, float, int, int, MxDev *, GridSync *,
                        double *, double *);
+    // the rectangle-resident kernel synchronises through phase words and takes its rectangle
+    // grid as two more arguments
+    using FR = void (*)(const LK *, R *, S *, S *, S *, float2 *, float, float, int, int, MxDev *,
+                        res::PhaseFlags *, int, int);
     F f = nullptr;
+    FR fr = nullptr;
+    res::Plan plan;
     int by = 0, ny = 0;
     int grid = 0;
     int smem = 0;  // dynamic shared memory per block
+    bool ok() const { return f || fr; }
 };
 
-// Persistent-kernel shapes (warps per block, rows per thread); one block per SM.  Candidate 4
-// is the bulk-copy kernel (stag_bulk.cuh: 16 warps, tiles staged through shared memory).
-constexpr int kNumPersist = 6;
-static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0};
+// Persistent-kernel shapes (warps per block, rows per thread); one block per SM.  Candidates
+// 4 and 5 are the bulk-copy kernel (stag_bulk.cuh: 16 warps, tiles staged through shared
+// memory); candidates 6 and 7 are the rectangle-resident kernel (stag_resident.cuh, FP32
+// only) with 16 and 32 warps.
+constexpr int kNumPersist = 8;
+static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0};
+constexpr int kResidentCand = 6;  // and 7
+static bool is_resident(int c) { return c == kResidentCand || c == kResidentCand + 1; }
+static int resident_wy(int c) { return c == kResidentCand ? 4 : 8; }
 
-// Whether persistent candidate c serves an lx x ly lattice.
-static bool persist_cand_applies(int c, int lx, int ly)
+// The rectangle grid of the resident kernel on this device (its static shared memory, the
+// reduction scratch, comes out of the same per-block budget: 512 bytes are kept for it).
+static res::Plan resident_plan(int lx, int ly, int wy)
 {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return res::Plan{};
+    }
+    return res::plan(lx, ly, sm_count(), (size_t)std::max(0, optin - 512), wy);
+}
+
+static bool persist_applies(int lx, int ly);
+
+// Whether persistent candidate c serves an lx x ly lattice in variant `variant` (the resident
+// kernel exists for the FP32 variant only).
+static bool persist_cand_applies(int c, int lx, int ly, int variant)
+{
+    if (is_resident(c)) return variant == 1 && resident_plan(lx, ly, resident_wy(c)).ok;
+    if (!persist_applies(lx, ly)) return false;
     if (c == 4) return bulk_applies<bulk::Geom256x4>(lx, ly, sm_count());
     if (c == 5) return bulk_applies<bulk::Geom512x2>(lx, ly, sm_count());
-    return true;
+    return c >= 0 && c < kNumPersist;
+}
+
+// Whether any persistent candidate serves the lattice.
+static bool any_persist_applies(int lx, int ly, int variant)
+{
+    for (int c = 0; c < kNumPersist; c++)
+        if (persist_cand_applies(c, lx, ly, variant)) return true;
+    return false;
 }
 
 template <class S, class R, class LK>
-static PersistKernel<S, R, LK> persist_cand(int c)
+static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy)
+{
+    if constexpr (std::is_same<S, float2>::value && std::is_same<R, float2>::value &&
+                  std::is_same<LK, float2>::value) {
+        pk.plan = resident_plan(lx, ly, wy);
+        if (!pk.plan.ok || pk.plan.gx * pk.plan.gy > res::kMaxBlocks) return;
+        if (wy == 4) {
+            switch (pk.plan.ny) {
+            case 4: pk.fr = k_resident<4, 4>; break;
+            case 8: pk.fr = k_resident<8, 4>; break;
+            default: pk.fr = k_resident<14, 4>; break;
+            }
+        } else {
+            switch (pk.plan.ny) {
+            case 2: pk.fr = k_resident<2, 8>; break;
+            case 4: pk.fr = k_resident<4, 8>; break;
+            default: pk.fr = k_resident<7, 8>; break;
+            }
+        }
+        pk.smem = (int)pk.plan.smem;
+        pk.grid = pk.plan.gx * pk.plan.gy;
+    }
+}
+
+template <class S, class R, class LK>
+static PersistKernel<S, R, LK> persist_cand(int c, int lx, int ly)
 {
     PersistKernel<S, R, LK> pk;
+    if (c < 0 || c >= kNumPersist) return pk;
     pk.by = kPersistBY[c];
     pk.ny = kPersistNY[c];
+    if (is_resident(c)) {
+        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c));
+        if (!pk.fr) return pk;
+        const void *fp = reinterpret_cast<const void *>(pk.fr);
+        int per_sm = 0;
+        if (cudaFuncSetAttribute(fp, cudaFuncAttributeMaxDynamicSharedMemorySize, pk.smem) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fp, 32 * pk.by, pk.smem) != cudaSuccess ||
+            per_sm < 1 || pk.grid > sm_count() * per_sm) {
+            cudaGetLastError();
+            pk.fr = nullptr;
+        }
+        return pk;
+    }
     switch (c) {
     case 0: pk.f = k_persist<S, R, LK, 16, 4>; break;
     case 1: pk.f = k_persist<S, R, LK, 16, 8>; break;
@@ -466,7 +545,7 @@ static bool persist_enabled()
 template <class S, class R, class LK>
 static cudaError_t launch_persist(const PersistKernel<S, R, LK> &pk, cudaStream_t st, const LK *H, R *r, S *p0,
                                   S *p1, S *t, float2 *xlo, float mass, float sigma, int lx, int ly, MxDev *s,
-                                  GridSync *gs, double *partA, double *partB)
+                                  GridSync *gs, double *partA, double *partB, res::PhaseFlags *pf)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(pk.grid);
@@ -478,6 +557,9 @@ static cudaError_t launch_persist(const PersistKernel<S, R, LK> &pk, cudaStream_
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    if (pk.fr)
+        return cudaLaunchKernelEx(&cfg, pk.fr, H, r, p0, p1, t, xlo, mass, sigma, lx, ly, s, pf, pk.plan.ty,
+                                  pk.plan.gx);
     return cudaLaunchKernelEx(&cfg, pk.f, H, r, p0, p1, t, xlo, mass, sigma, lx, ly, s, gs, partA, partB);
 }
 
@@ -607,20 +689,22 @@ static int autotune(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p
 
 static std::map<std::tuple<int, int, int, int>, int> g_ptuned;  // persistent shape per lattice
 
+// The tuned persistent candidate, or -1 when none serves the lattice.
 static int persist_tuned(int lx, int ly, int variant)
 {
     int dev = 0;
     cudaGetDevice(&dev);
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_ptuned.find(std::make_tuple(dev, lx, ly, variant));
-    return it == g_ptuned.end() ? 0 : it->second;
+    return it == g_ptuned.end() ? -1 : it->second;
 }
 
 // Times every persistent shape on 16 CG iterations of A x = 1 (from r = 1, p = 0) and keeps
 // the fastest for this device, lattice and variant.
 template <class S, class R, class LK>
 static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p1, S *t, float2 *xlo,
-                             const LK *L, MxDev *s, GridSync *gs, double *partA, double *partB, cudaStream_t st)
+                             const LK *L, MxDev *s, GridSync *gs, double *partA, double *partB,
+                             res::PhaseFlags *pf, cudaStream_t st)
 {
     const int lx = op->lx, ly = op->ly;
     const auto key = std::make_tuple(op->device, lx, ly, variant);
@@ -630,7 +714,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     }
     if (const char *e = std::getenv("GLINALG_PERSIST_SHAPE")) {  // as GLINALG_TILE
         const int c = std::atoi(e);
-        if (c >= 0 && c < kNumPersist && persist_cand_applies(c, lx, ly)) {
+        if (c >= 0 && c < kNumPersist && persist_cand_applies(c, lx, ly, variant)) {
             std::lock_guard<std::mutex> lk(g_tune_mu);
             g_ptuned[key] = c;
             return;
@@ -654,9 +738,9 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     int best = -1;
     float best_ms = 1e30f;
     for (int c = 0; c < kNumPersist; c++) {
-        if (!persist_cand_applies(c, lx, ly)) continue;
-        const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(c);
-        if (!pk.f) continue;
+        if (!persist_cand_applies(c, lx, ly, variant)) continue;
+        const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(c, lx, ly);
+        if (!pk.ok()) continue;
         float m = 1e30f;
         for (int rep = 0; rep < 3; rep++) {
             k_copy_links<R><<<vgrid(n), 256, 0, st>>>(r, d1, n);
@@ -665,7 +749,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
             k_busy_wait<<<1, 1, 0, st>>>(30000);
             cudaEventRecord(e0, st);
             cudaError_t e = launch_persist(pk, st, L, r, p0, p1, t, xlo, (float)op->mass, 0.f, lx, ly, s, gs,
-                                           partA, partB);
+                                           partA, partB, pf);
             cudaEventRecord(e1, st);
             cudaEventSynchronize(e1);
             MxDev back;
@@ -688,7 +772,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     cudaEventDestroy(e1);
     cudaFreeAsync(d1, st);
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_ptuned[key] = best < 0 ? 0 : best;
+    g_ptuned[key] = best;
 }
 
 // ---------------------------------------------------------------- driver
@@ -728,18 +812,20 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     GL_CUDA(cudaGetLastError());
 
     StagKernels<S, R, LK> sk{};
-    const bool use_persist = stag && persist_enabled() && persist_applies(lx, ly);
+    const bool use_persist = stag && persist_enabled() && any_persist_applies(lx, ly, variant);
     GridSync *gs = nullptr;
+    res::PhaseFlags *pf = nullptr;
     double *partA = nullptr, *partB = nullptr;
     if (use_persist) {
         GL_TRY(sc.zeros(&gs, 1));
+        GL_TRY(sc.zeros(&pf, 1));
         GL_TRY(sc.alloc(&partA, sm_count()));
         GL_TRY(sc.alloc(&partB, sm_count()));
     }
     if (stag) {
         const int cand = autotune<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, partials, st);
         sk = kernels_for<S, R, LK>(cand, lx % 32 == 0);
-        if (use_persist) autotune_persist<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, gs, partA, partB, st);
+        if (use_persist) autotune_persist<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, gs, partA, partB, pf, st);
         // the tuning runs wrote the work vectors: start from zero again
         GL_CUDA(cudaMemsetAsync(p0, 0, sizeof(S) * n, st));
         GL_CUDA(cudaMemsetAsync(p1, 0, sizeof(S) * n, st));
@@ -811,11 +897,11 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     // loop ; reliable update ; tail } -- one cooperative kernel per reliable-update cycle.
     bool persisted = false;
     if (use_persist) {
-        const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(persist_tuned(lx, ly, variant));
-        if (pk.f) {
+        const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(persist_tuned(lx, ly, variant), lx, ly);
+        if (pk.ok()) {
             glinalg_status ps = run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
                 GL_CUDA(launch_persist(pk, cs, L, r, p0, p1, t, xlo, (float)op->mass, (float)sigma, lx, ly, s,
-                                       gs, partA, partB));
+                                       gs, partA, partB, pf));
                 GL_TRY(reliable_seq(cs));
                 k_mx_outer_tail<<<1, 32, 0, cs>>>(s, 0, 0);
                 GL_CUDA(cudaGetLastError());
@@ -1047,6 +1133,13 @@ int tuned_tile(const glinalg_operator_s *op, int variant)
     return it == g_tuned.end() ? -1 : it->second;
 }
 
+int tuned_persist(const glinalg_operator_s *op, int variant)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_ptuned.find(std::make_tuple(op->device, op->lx, op->ly, variant));
+    return it == g_ptuned.end() ? -1 : it->second;
+}
+
 }  // namespace glinalg
 
 extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision, int n_launch,
@@ -1067,4 +1160,9 @@ extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int
 extern "C" int glinalg_tuned_tile(glinalg_operator op, int precision)
 {
     return op ? glinalg::tuned_tile(op, precision) : -1;
+}
+
+extern "C" int glinalg_tuned_persist(glinalg_operator op, int precision)
+{
+    return op ? glinalg::tuned_persist(op, precision) : -1;
 }

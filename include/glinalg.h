@@ -271,6 +271,11 @@ glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision,
  * library's candidate list: 0 = 32x16, 1 = 32x32, 2 = 32x32 (4 rows of 8), 3 = 32x32
  * (16 rows of 2) sites per block), or -1 if no mixed solve has run on this lattice yet. */
 int glinalg_tuned_tile(glinalg_operator op, int precision);
+/* Persistent inner-loop kernel the autotuner picked for op's lattice and precision: 0-3 the
+ * register-tiled kernel (16 warps x 4 rows, 16 x 8, 32 x 2, 16 x 2), 4-5 the bulk-copy kernel
+ * (256 x 4 and 512 x 2 tiles), 6-7 the rectangle-resident kernel (FP32 only; 16 and 32
+ * warps); -1 if none serves the lattice or no mixed solve has run on it yet. */
+int glinalg_tuned_persist(glinalg_operator op, int precision);
 
 /* ---- inputs the way the reference's tests make them (host side) ----
  * A generator is one std::mt19937 stream (as `std::mt19937 generator(seed)` in the tests);

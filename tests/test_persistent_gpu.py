@@ -1,0 +1,88 @@
+"""The persistent inner-loop kernels of the FP32 mixed-precision CG (one cooperative launch per
+reliable-update cycle): the register-tiled kernels, the bulk-copy kernels and the
+rectangle-resident kernel (shared-memory / register state per SM, borders exchanged through
+L2).  Each candidate is forced with GLINALG_PERSIST_SHAPE in a process of its own (the
+autotuner's pick is cached per process).
+
+Bar: the FP64-true relative residual below 1e-10 (re-checked with the FP64 GPU operator), the
+iteration count within 5% of the FP64 CG's, and the solution within kappa * 1e-10 of the
+FP64 GPU CG solution."""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+SCRIPT = r'''
+import importlib, json, sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+gl = importlib.import_module("generic-linalg_gb300")
+lx, ly, mass, seed = int(sys.argv[2]), int(sys.argv[3]), float(sys.argv[4]), int(sys.argv[5])
+g = gl.Generator(seed)
+U = g.rand_gauge_u1(lx, ly)
+b = g.gaussian(lx * ly)
+dev = torch.device("cuda:0")
+op = gl.Operator(2, lx, ly, mass, torch.from_numpy(U).to(dev))
+bt = torch.from_numpy(b).to(dev)
+out = {}
+for prec in (1, 0):
+    x = torch.zeros_like(bt)
+    info = gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=prec)
+    Ax = torch.zeros_like(bt)
+    op.apply(Ax, x)
+    out[prec] = {"x": x, "iter": info.iter, "success": bool(info.success),
+                 "launches": info.kernel_launches,
+                 "relres": (torch.linalg.vector_norm(bt - Ax) / torch.linalg.vector_norm(bt)).item()}
+err = (torch.linalg.vector_norm(out[1]["x"] - out[0]["x"]) / torch.linalg.vector_norm(out[0]["x"])).item()
+print(json.dumps({"iter": out[1]["iter"], "iter64": out[0]["iter"], "success": out[1]["success"],
+                  "relres": out[1]["relres"], "err": err, "launches": out[1]["launches"],
+                  "tuned": gl.lib().glinalg_tuned_persist(op.handle, 1)}))
+'''
+
+
+def run_case(tmp_path, lx, ly, mass, seed, shape=None):
+    script = tmp_path / "persist_case.py"
+    script.write_text(SCRIPT)
+    env = dict(os.environ)
+    env.pop("GLINALG_PERSIST_SHAPE", None)
+    if shape is not None:
+        env["GLINALG_PERSIST_SHAPE"] = str(shape)
+    p = subprocess.run([sys.executable, str(script), ROOT, str(lx), str(ly), str(mass), str(seed)], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-3000:]
+    return json.loads(p.stdout.strip().splitlines()[-1])
+
+
+def check(res, kappa):
+    assert res["success"], res
+    assert res["relres"] < 1e-10, res
+    assert abs(res["iter"] - res["iter64"]) <= 0.05 * res["iter64"] + 2, res
+    assert res["err"] < kappa * 1e-10, res
+    assert res["launches"] >= 1, res  # the persistent inner loop ran
+
+
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7])
+def test_persistent_candidate_1024(gl, gpu, tmp_path, shape):
+    """The 1024x1024, m = 0.01 system (kappa ~ 2e4) with each persistent kernel forced."""
+    res = run_case(tmp_path, 1024, 1024, 0.01, 1337, shape)
+    assert res["tuned"] == shape
+    check(res, 2e4)
+
+
+@pytest.mark.parametrize("lx,ly", [(256, 256), (512, 300), (384, 200), (128, 90)])
+def test_resident_kernel_small_lattices(gl, gpu, tmp_path, lx, ly):
+    """Lattices that only the rectangle-resident kernel serves: one or several 128-column
+    rectangles across, full and short last rectangles, one-row rectangles (128 x 90)."""
+    for shape in (6, 7):
+        res = run_case(tmp_path, lx, ly, 0.05, 99, shape)
+        assert res["tuned"] == shape
+        check(res, 1e3)
