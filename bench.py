@@ -46,8 +46,9 @@ VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 rows>",
                    2: "k_persist<32 warps, 2 rows>", 3: "k_persist<16 warps, 2 rows>",
                    4: "k_persist_bulk<256x4 tiles>", 5: "k_persist_bulk<512x2 tiles>",
-                   6: "k_resident<16 warps> (rectangle state on chip)",
-                   7: "k_resident<32 warps> (rectangle state on chip)"}
+                   6: "k_resident<16 warps, x_lo in registers> (rectangle state on chip)",
+                   7: "k_resident<32 warps> (rectangle state on chip)",
+                   8: "k_resident<16 warps> (rectangle state on chip)"}
 
 
 def peaks():

@@ -396,8 +396,8 @@ struct PersistKernel {
                        double *, double *);
     // the rectangle-resident kernel synchronises through phase words and takes its rectangle
     // grid as two more arguments
-    using FR = void (*)(const LK *, R *, S *, S *, S *, float2 *, float, float, int, int, MxDev *,
-                        res::PhaseFlags *, int, int);
+    using FR = void (*)(const LK *, R *, S *, float2 *, float, float, int, int, MxDev *, res::PhaseFlags *,
+                        unsigned long long *, int, int);
     F f = nullptr;
     FR fr = nullptr;
     res::Plan plan;
@@ -409,14 +409,16 @@ struct PersistKernel {
 
 // Persistent-kernel shapes (warps per block, rows per thread); one block per SM.  Candidates
 // 4 and 5 are the bulk-copy kernel (stag_bulk.cuh: 16 warps, tiles staged through shared
-// memory); candidates 6 and 7 are the rectangle-resident kernel (stag_resident.cuh, FP32
-// only) with 16 and 32 warps.
-constexpr int kNumPersist = 8;
-static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0};
-constexpr int kResidentCand = 6;  // and 7
-static bool is_resident(int c) { return c == kResidentCand || c == kResidentCand + 1; }
-static int resident_wy(int c) { return c == kResidentCand ? 4 : 8; }
+// memory); candidates 6-8 are the rectangle-resident kernel (stag_resident.cuh, FP32 only):
+// 16 warps with x_lo in registers, 32 warps, 16 warps with x_lo in global memory.
+constexpr int kNumPersist = 9;
+static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8,
+                                            res::kWX * 4};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0};
+constexpr int kResidentCand = 6;  // 6, 7 and 8
+static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 2; }
+static int resident_wy(int c) { return c == kResidentCand + 1 ? 8 : 4; }
+static bool resident_xreg(int c) { return c == kResidentCand; }
 
 // The rectangle grid of the resident kernel on this device (its static shared memory, the
 // reduction scratch, comes out of the same per-block budget: 512 bytes are kept for it).
@@ -453,23 +455,29 @@ static bool any_persist_applies(int lx, int ly, int variant)
 }
 
 template <class S, class R, class LK>
-static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy)
+static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy, bool xreg)
 {
     if constexpr (std::is_same<S, float2>::value && std::is_same<R, float2>::value &&
                   std::is_same<LK, float2>::value) {
         pk.plan = resident_plan(lx, ly, wy);
         if (!pk.plan.ok || pk.plan.gx * pk.plan.gy > res::kMaxBlocks) return;
-        if (wy == 4) {
+        if (wy == 4 && xreg) {
             switch (pk.plan.ny) {
-            case 4: pk.fr = k_resident<4, 4>; break;
-            case 8: pk.fr = k_resident<8, 4>; break;
-            default: pk.fr = k_resident<14, 4>; break;
+            case 4: pk.fr = k_resident<4, 4, true>; break;
+            case 8: pk.fr = k_resident<8, 4, true>; break;
+            default: pk.fr = k_resident<14, 4, true>; break;
+            }
+        } else if (wy == 4) {
+            switch (pk.plan.ny) {
+            case 4: pk.fr = k_resident<4, 4, false>; break;
+            case 8: pk.fr = k_resident<8, 4, false>; break;
+            default: pk.fr = k_resident<14, 4, false>; break;
             }
         } else {
             switch (pk.plan.ny) {
-            case 2: pk.fr = k_resident<2, 8>; break;
-            case 4: pk.fr = k_resident<4, 8>; break;
-            default: pk.fr = k_resident<7, 8>; break;
+            case 2: pk.fr = k_resident<2, 8, false>; break;
+            case 4: pk.fr = k_resident<4, 8, false>; break;
+            default: pk.fr = k_resident<7, 8, false>; break;
             }
         }
         pk.smem = (int)pk.plan.smem;
@@ -485,7 +493,7 @@ static PersistKernel<S, R, LK> persist_cand(int c, int lx, int ly)
     pk.by = kPersistBY[c];
     pk.ny = kPersistNY[c];
     if (is_resident(c)) {
-        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c));
+        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xreg(c));
         if (!pk.fr) return pk;
         const void *fp = reinterpret_cast<const void *>(pk.fr);
         int per_sm = 0;
@@ -545,7 +553,8 @@ static bool persist_enabled()
 template <class S, class R, class LK>
 static cudaError_t launch_persist(const PersistKernel<S, R, LK> &pk, cudaStream_t st, const LK *H, R *r, S *p0,
                                   S *p1, S *t, float2 *xlo, float mass, float sigma, int lx, int ly, MxDev *s,
-                                  GridSync *gs, double *partA, double *partB, res::PhaseFlags *pf)
+                                  GridSync *gs, double *partA, double *partB, res::PhaseFlags *pf,
+                                  unsigned long long *mbox)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(pk.grid);
@@ -558,7 +567,7 @@ static cudaError_t launch_persist(const PersistKernel<S, R, LK> &pk, cudaStream_
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     if (pk.fr)
-        return cudaLaunchKernelEx(&cfg, pk.fr, H, r, p0, p1, t, xlo, mass, sigma, lx, ly, s, pf, pk.plan.ty,
+        return cudaLaunchKernelEx(&cfg, pk.fr, H, r, p0, xlo, mass, sigma, lx, ly, s, pf, mbox, pk.plan.ty,
                                   pk.plan.gx);
     return cudaLaunchKernelEx(&cfg, pk.f, H, r, p0, p1, t, xlo, mass, sigma, lx, ly, s, gs, partA, partB);
 }
@@ -704,7 +713,7 @@ static int persist_tuned(int lx, int ly, int variant)
 template <class S, class R, class LK>
 static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p1, S *t, float2 *xlo,
                              const LK *L, MxDev *s, GridSync *gs, double *partA, double *partB,
-                             res::PhaseFlags *pf, cudaStream_t st)
+                             res::PhaseFlags *pf, unsigned long long *mbox, cudaStream_t st)
 {
     const int lx = op->lx, ly = op->ly;
     const auto key = std::make_tuple(op->device, lx, ly, variant);
@@ -749,7 +758,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
             k_busy_wait<<<1, 1, 0, st>>>(30000);
             cudaEventRecord(e0, st);
             cudaError_t e = launch_persist(pk, st, L, r, p0, p1, t, xlo, (float)op->mass, 0.f, lx, ly, s, gs,
-                                           partA, partB, pf);
+                                           partA, partB, pf, mbox);
             cudaEventRecord(e1, st);
             cudaEventSynchronize(e1);
             MxDev back;
@@ -815,17 +824,22 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     const bool use_persist = stag && persist_enabled() && any_persist_applies(lx, ly, variant);
     GridSync *gs = nullptr;
     res::PhaseFlags *pf = nullptr;
+    unsigned long long *mbox = nullptr;
     double *partA = nullptr, *partB = nullptr;
     if (use_persist) {
         GL_TRY(sc.zeros(&gs, 1));
         GL_TRY(sc.zeros(&pf, 1));
+        // border mailboxes of the rectangle-resident kernel (the same rectangles for 16 and 32 warps)
+        const res::Plan rp = resident_plan(lx, ly, 4);
+        if (variant == 1 && rp.ok) GL_TRY(sc.zeros(&mbox, res::mbox_words(sm_count(), rp.ty)));
         GL_TRY(sc.alloc(&partA, sm_count()));
         GL_TRY(sc.alloc(&partB, sm_count()));
     }
     if (stag) {
         const int cand = autotune<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, partials, st);
         sk = kernels_for<S, R, LK>(cand, lx % 32 == 0);
-        if (use_persist) autotune_persist<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, gs, partA, partB, pf, st);
+        if (use_persist)
+            autotune_persist<S, R, LK>(op, variant, r, p0, p1, t, xlo, L, s, gs, partA, partB, pf, mbox, st);
         // the tuning runs wrote the work vectors: start from zero again
         GL_CUDA(cudaMemsetAsync(p0, 0, sizeof(S) * n, st));
         GL_CUDA(cudaMemsetAsync(p1, 0, sizeof(S) * n, st));
@@ -901,7 +915,7 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         if (pk.ok()) {
             glinalg_status ps = run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
                 GL_CUDA(launch_persist(pk, cs, L, r, p0, p1, t, xlo, (float)op->mass, (float)sigma, lx, ly, s,
-                                       gs, partA, partB, pf));
+                                       gs, partA, partB, pf, mbox));
                 GL_TRY(reliable_seq(cs));
                 k_mx_outer_tail<<<1, 32, 0, cs>>>(s, 0, 0);
                 GL_CUDA(cudaGetLastError());

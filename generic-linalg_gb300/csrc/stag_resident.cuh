@@ -2,28 +2,24 @@
 // operator D^dagger D (+ sigma) with each block's share of the lattice held on chip.
 //
 // One cooperative launch, one block of 16 or 32 warps per SM (4 across, WY down), and every
-// block owns one fixed rectangle of the lattice (128 columns by `ty` rows) for the whole launch:
-//   shared memory: the hopping coefficients of the rectangle (h_x and h_y arrays) plus the h_x
-//                  column left of it and the h_y row below it; the direction p' and t = D p',
-//                  each with a one-site ring around the rectangle;
-//   registers:     the residual r and the low-precision solution x_lo of the thread's sites
-//                  (one column, NY rows).
-// Per inner iteration nothing but the rectangle borders leaves the SM:
-//   A: p' = r + beta p (own sites from shared memory and registers, the ring from the
-//      neighbours' exported r and p'), t = D p', |t|^2 + sigma |p'|^2; export the border of t.
-//   -- grid barrier (alpha) --
-//   B: import the ring of t, Ap = D^dagger t + sigma p', x_lo += alpha p', r -= alpha Ap,
-//      |r|^2; export the border of r and p'.
-//   -- grid barrier (beta, or a reliable update is due) --
-// The exchange goes through the solve's global r, t and p1 arrays (only border sites are
-// written; loads use ld.global.cg).  Both barriers already separate every export from the
-// imports that read it and from the next export to the same sites, so no extra
-// synchronisation is needed.  The lattice wraps periodically through the same exchange, which
-// also covers a rectangle that spans the whole lattice in one direction.
+// block owns one fixed rectangle of the lattice (128 columns by `ty` rows) for the whole launch.
+// Per inner iteration nothing but the rectangle borders leaves the SM.  The iteration is CG on
+// A = D^dagger D + sigma written so that each stencil needs only the neighbours' borders and the
+// grid-wide sum it waits for is due only after the stencil (the sum's latency, a few
+// microseconds on GB300, hides behind it):
+//   A: u = D r; then beta (the total of the previous B); t = u + beta t_old (= D p'),
+//      p' = r + beta p, |t|^2 + sigma |p'|^2; export the border of t.
+//   B: Ap = D^dagger t + sigma p'; then alpha = |r|^2 / <p', A p'> (the total of A);
+//      x_lo += alpha p', r -= alpha Ap, |r|^2; export the border of r.
+// Shared memory holds r and t, each with a one-site ring, and the hopping coefficients; the
+// direction p' and (16-warp blocks) x_lo stay in registers.  Border sites travel through
+// epoch-tagged mailboxes in global memory (L2), with no memory fence in the loop (see the
+// exchange section below).
 //
-// On entry the kernel loads r, x_lo and the direction (p0) of its rectangle; on exit it writes
-// them back (the direction to p0, parity 0) for the FP64 reliable update.  The per-site
-// arithmetic and its order are those of tile_A / tile_B (stag_tiles.cuh).
+// On entry the kernel loads r and the direction (p0) of its rectangle and computes t_old = D p;
+// on exit it writes r, x_lo and the direction (to p0, parity 0) back for the FP64 reliable
+// update.  The per-site arithmetic is that of tile_A / tile_B (stag_tiles.cuh) except that
+// D p' is formed as D r + beta D p.
 #pragma once
 
 #include "mixed_state.cuh"
@@ -33,13 +29,13 @@ namespace res {
 
 constexpr int kWX = 4;         // warps along x
 constexpr int kTX = 32 * kWX;  // rectangle width (sites)
-constexpr int kPW = kTX + 2;   // row pitch of the p' / t buffers (one ring site each side)
+constexpr int kPW = kTX + 2;   // row pitch of the r / t buffers (one ring site each side)
 
 // Dynamic shared memory of a rectangle of ty rows.
 inline size_t smem_bytes(int ty)
 {
     return 2 * (size_t)ty * kTX * sizeof(float2)          // h_x and h_y of the rectangle
-           + 2 * (size_t)(ty + 2) * kPW * sizeof(float2)  // p' and t with their ring
+           + 2 * (size_t)(ty + 2) * kPW * sizeof(float2)  // r and t with their ring
            + (size_t)ty * sizeof(float2)                  // h_x of the column left of the rectangle
            + (size_t)kTX * sizeof(float2);                // h_y of the row below it
 }
@@ -82,7 +78,7 @@ inline Plan plan(int lx, int ly, int nsm, size_t max_smem, int wy)
     return p;
 }
 
-// Ring site k of a rectangle (x0, y0, 128 x tyb): its slot in a p' / t buffer and its lattice
+// Ring site k of a rectangle (x0, y0, 128 x tyb): its slot in an r / t buffer and its lattice
 // index.  k < 128: the row below; < 256: the row above; then the column left, the column right.
 __device__ __forceinline__ void ring_site(int k, int tyb, int x0, int y0, int lx, int ly, int &slot, int &gi)
 {
@@ -110,7 +106,7 @@ __device__ __forceinline__ void ring_site(int k, int tyb, int x0, int y0, int lx
 // The shared-memory view of a rectangle.
 struct Rect {
     float2 *HX, *HY;  // h_x, h_y at [yl * kTX + xl]
-    float2 *P, *T;    // p', t at [(yl + 1) * kPW + xl + 1], ring included
+    float2 *F, *T;    // r, t at [(yl + 1) * kPW + xl + 1], ring included
     float2 *HxL;      // h_x at column x0 - 1, [yl]
     float2 *HyB;      // h_y at row y0 - 1, [xl]
 };
@@ -146,28 +142,36 @@ __device__ __forceinline__ void hop_rows(const float2 *__restrict__ F, const flo
     }
 }
 
-// ---------------------------------------------------------------- phase exchange
+// ---------------------------------------------------------------- exchange between blocks
 //
-// Each reduction of the inner loop is also the grid-wide barrier: every block publishes its
-// partial sum as one 64-bit word (the phase's epoch in the high half, the FP32 partial in the
-// low half) and one warp per block polls all blocks' words with relaxed loads until each
-// carries the current epoch, then fences (acquire).  The publishing store follows a
-// __syncthreads and a fence (release), so the border sites a block exported before the phase
-// are visible to every block that has seen its word.  Words alternate between two arrays by
-// phase parity: a block overwrites its word of phase e only in phase e + 2, which it reaches
-// after every block has published phase e + 1, i.e. after every block has finished reading
-// phase e.  The partials are summed in block order in FP64, so every block holds the same
-// total.  Waits are bounded (kBarrierTimeoutNs); a wait that runs out raises the error word,
-// which ends the other blocks' waits too.
+// Nothing in the inner loop waits for a memory fence.  Every value one block hands to another
+// carries the epoch of the phase that produced it, in 64-bit words that are single-copy
+// atomic: a border site of r or t goes out as two words (epoch << 32 | float bits of the real
+// and of the imaginary part) into the producing block's mailbox, and a block's partial sum as
+// one word (epoch << 32 | float bits).  A consumer polls the words it needs with relaxed loads
+// until they carry the current epoch, so a value is used only once it has arrived.
+//
+// Epochs grow by one per phase (two per iteration) across the launches of a solve.  A mailbox
+// slot is rewritten two phases later (the same field, the next iteration), and a block reaches
+// that write only after the grid-wide sum in between, which every block contributes to only
+// after it has read the slot's previous contents; partial-sum words alternate between two
+// arrays by phase parity for the same reason.  Every wait is bounded (kSpinCycles); a wait
+// that runs out raises the error word, which ends the waits of every other block too.
 
 constexpr int kMaxBlocks = 256;  // one rectangle per SM: above any GB300 SM count
 constexpr int kPerLane = kMaxBlocks / 32;
+constexpr long long kSpinCycles = 4000000000LL;  // about 2 s at GB300 clocks
 
 struct PhaseFlags {
-    unsigned long long w[2][kMaxBlocks];
-    unsigned epoch;  // phases completed by all launches so far
+    unsigned long long w[2][kMaxBlocks];  // partial-sum words by phase parity
+    unsigned epoch;                       // phases completed by all launches so far
     int error;
 };
+
+// Mailbox slots of a block with ty-row rectangles: bottom row, top row, left column, right column.
+__host__ __device__ inline int mbox_slots(int ty) { return 2 * kTX + 2 * ty; }
+// 64-bit words of the mailboxes of both fields (r and t) for nb blocks.
+inline size_t mbox_words(int nb, int ty) { return 2 * (size_t)nb * mbox_slots(ty) * 2; }
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p)
 {
@@ -179,34 +183,118 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned l
 {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+__device__ __forceinline__ void ld_relaxed_2u64(const unsigned long long *p, unsigned long long &a,
+                                                unsigned long long &b)
+{
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_2u64(unsigned long long *p, unsigned long long a, unsigned long long b)
+{
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
 __device__ __forceinline__ int ld_relaxed_s32(const int *p)
 {
     int v;
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned long long tag(unsigned e, float v)
+{
+    return ((unsigned long long)e << 32) | __float_as_uint(v);
+}
 
-// Phase exchange, called by every thread of the block with its partial `acc`.  On return the
-// grid total is in lane 0 of warp 0 (`total`); the function returns false there when a wait ran
-// out.  The caller broadcasts what lane 0 derives from the total and synchronises the block.
+// Writes border site (xl, yl) of the block's rectangle (tyb rows) with value v and epoch e into
+// every mailbox slot it belongs to.  M: the field's mailboxes; my: this block's first word.
+__device__ __forceinline__ void post_border(unsigned long long *M, int my, int ty, int tyb, int xl, int yl,
+                                            float2 v, unsigned e)
+{
+    const unsigned long long a = tag(e, v.x), b = tag(e, v.y);
+    if (yl == 0) st_relaxed_2u64(M + my + 2 * xl, a, b);
+    if (yl == tyb - 1) st_relaxed_2u64(M + my + 2 * (kTX + xl), a, b);
+    if (xl == 0) st_relaxed_2u64(M + my + 2 * (2 * kTX + yl), a, b);
+    if (xl == kTX - 1) st_relaxed_2u64(M + my + 2 * (2 * kTX + ty + yl), a, b);
+}
+
+// The mailbox word (within a field) that feeds ring site k: the row below comes from the top
+// row of the block below, the row above from the bottom row of the block above, the column left
+// from the right column of the block to the left, the column right from the left column of the
+// block to the right.
+__device__ __forceinline__ int ring_source(int k, int ty, int tyb, int nslot, int nb_l, int nb_r, int nb_d,
+                                           int nb_u)
+{
+    int b, slot;
+    if (k < kTX) {
+        b = nb_d;
+        slot = kTX + k;
+    } else if (k < 2 * kTX) {
+        b = nb_u;
+        slot = k - kTX;
+    } else if (k < 2 * kTX + tyb) {
+        b = nb_l;
+        slot = 2 * kTX + ty + (k - 2 * kTX);
+    } else {
+        b = nb_r;
+        slot = 2 * kTX + (k - 2 * kTX - tyb);
+    }
+    return 2 * (b * nslot + slot);
+}
+
+// Polls a mailbox slot until both words carry epoch e; returns the value, or sets *err (and the
+// error word) when the wait runs out or another block has raised the error word.
+__device__ __forceinline__ float2 poll_slot(const unsigned long long *p, unsigned e, PhaseFlags *pf, int *err)
+{
+    unsigned long long a, b;
+    const long long t0 = clock64();
+    for (unsigned n = 1;; n++) {
+        ld_relaxed_2u64(p, a, b);
+        if ((unsigned)(a >> 32) == e && (unsigned)(b >> 32) == e) break;
+        if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
+            atomicExch(&pf->error, 1);
+            *err = 1;
+            break;
+        }
+    }
+    return make_float2(__uint_as_float((unsigned)a), __uint_as_float((unsigned)b));
+}
+
+// *p += v, performed in L2 (no value comes back).
+__device__ __forceinline__ void red_add2(float2 *p, float2 v)
+{
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(v.x), "f"(v.y) : "memory");
+}
+
+// s + c = a + b exactly (Knuth's TwoSum), for the compensated sums below.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &c)
+{
+    s = a + b;
+    const float bb = s - a;
+    c = (a - (s - bb)) + (b - bb);
+}
+
+// Publishes the block's partial sum of phase e (every thread passes its `acc`): FP32 within
+// warps and across the block's warps, one tagged word written by thread 0.
 template <int NW>
-__device__ __forceinline__ bool phase_exchange(float acc, PhaseFlags *pf, unsigned e, unsigned nb, float *sm_w,
-                                               double &total)
+__device__ __forceinline__ void publish(float acc, PhaseFlags *pf, unsigned e, float *sm_w)
 {
     const int lane = threadIdx.x, warp = threadIdx.y;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) sm_w[warp] = acc;
-    __syncthreads();  // the block's partials and exported border sites are complete
-    if (warp != 0) return true;
-    float v = lane < NW ? sm_w[lane] : 0.f;
+    __syncthreads();
+    if (warp == 0) {
+        float v = lane < NW ? sm_w[lane] : 0.f;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    unsigned long long *W = pf->w[e & 1];
-    if (lane == 0) {
-        __threadfence();  // release: this block's stores before its word
-        st_relaxed_u64(W + blockIdx.x, ((unsigned long long)e << 32) | __float_as_uint(v));
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) st_relaxed_u64(pf->w[e & 1] + blockIdx.x, tag(e, v));
     }
+}
+
+// Called by warp 0: waits until every block's word carries epoch e and sums the partials in
+// block order (compensated FP32), identically in every block.  The total is in lane 0.
+__device__ __forceinline__ bool wait_total(PhaseFlags *pf, unsigned e, unsigned nb, float &total)
+{
+    const int lane = threadIdx.x;
+    const unsigned long long *W = pf->w[e & 1];
     float vals[kPerLane];
     unsigned pending = 0;
 #pragma unroll
@@ -214,9 +302,9 @@ __device__ __forceinline__ bool phase_exchange(float acc, PhaseFlags *pf, unsign
         vals[i] = 0.f;
         if (lane + 32 * i < (int)nb) pending |= 1u << i;
     }
-    const long long t0 = gtimer();
+    const long long t0 = clock64();
     bool ok = true;
-    for (;;) {
+    for (unsigned n = 1;; n++) {
 #pragma unroll
         for (int i = 0; i < kPerLane; i++) {
             if (pending & (1u << i)) {
@@ -228,68 +316,123 @@ __device__ __forceinline__ bool phase_exchange(float acc, PhaseFlags *pf, unsign
             }
         }
         if (__all_sync(0xffffffffu, pending == 0)) break;
-        const bool give_up = gtimer() - t0 > kBarrierTimeoutNs || ld_relaxed_s32(&pf->error) != 0;
+        const bool give_up =
+            (n & 15) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0);
         if (__any_sync(0xffffffffu, give_up)) {
             if (lane == 0) atomicExch(&pf->error, 1);
             ok = false;
             break;
         }
     }
-    __threadfence();  // acquire: every block's stores before its word are visible from here
-    double part = 0.0;
+    float hi = 0.f, lo = 0.f;
 #pragma unroll
-    for (int i = 0; i < kPerLane; i++) part += (double)vals[i];
+    for (int i = 0; i < kPerLane; i++) {
+        float c;
+        two_sum(hi, vals[i], hi, c);
+        lo += c;
+    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_down_sync(0xffffffffu, part, o);
-    total = part;
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
+        float c;
+        two_sum(hi, h2, hi, c);
+        lo += l2 + c;
+    }
+    total = hi + lo;
     return ok;
 }
 
 }  // namespace res
 
-// Control word broadcast by lane 0 of warp 0 after each phase exchange.
+// Control word broadcast by lane 0 of warp 0 after each grid-wide total.
 enum : int { kResGo = 0, kResReliable = 1, kResStop = 2 };
 
-template <int NY, int WY>
+// The scalar recurrence of a block, kept in shared memory and used by thread 0 only (so that
+// it occupies no registers in the other threads), in FP32: the inner iteration's scalars are
+// FP32, and the FP64 state is written back at exit.
+struct ResScalars {
+    float rsq, rmax, rn, beta, scale, delta, stop;
+    int k, max_iter, status, reliable, iters;
+};
+
+// XREG: x_lo of the thread's sites in registers for the whole launch; else every update goes to
+// global memory as a vector reduction (fire-and-forget, no register and no round trip; each site
+// has one writer, so the additions happen in program order).
+template <int NY, int WY, bool XREG>
 __global__ void __launch_bounds__(32 * res::kWX * WY, 1)
-k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *p1, float2 *t, float2 *xlo, float mass,
-           float sigma, int lx, int ly, MxDev *s, res::PhaseFlags *pf, int ty, int gx)
+k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, float mass, float sigma, int lx, int ly,
+           MxDev *s, res::PhaseFlags *pf, unsigned long long *mbox, int ty, int gx)
 {
     using namespace res;
     constexpr int NW = kWX * WY, NT = 32 * NW;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ float sm_w[32];
-    __shared__ float sm_alpha, sm_beta;
-    __shared__ int sm_ctl;
+    __shared__ float sm_scalar;
+    __shared__ int sm_ctl, sm_err;
+    __shared__ ResScalars sc;
     if (s->done || s->reliable) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int tid = warp * 32 + lane;
     const int xl = (warp % kWX) * 32 + lane, yb = (warp / kWX) * NY;
-    const int x0 = (blockIdx.x % gx) * kTX, y0 = (blockIdx.x / gx) * ty;
+    const int bx = blockIdx.x % gx, by = blockIdx.x / gx, gy = (int)nb / gx;
+    const int x0 = bx * kTX, y0 = by * ty;
     const int tyb = min(ty, ly - y0);  // rows of this rectangle
     const int nrow = min(NY, tyb - yb);  // rows of this thread (<= 0: none)
     const int nring = 2 * kTX + 2 * tyb;
+    const int nslot = mbox_slots(ty);
+    // the blocks owning the ring: left, right, below, above (periodic)
+    const int nb_l = by * gx + (bx + gx - 1) % gx, nb_r = by * gx + (bx + 1) % gx;
+    const int nb_d = ((by + gy - 1) % gy) * gx + bx, nb_u = ((by + 1) % gy) * gx + bx;
+    unsigned long long *const Mr = mbox, *const Mt = mbox + 2 * (size_t)nb * nslot;
+    const int my = 2 * (int)blockIdx.x * nslot;
     Rect R;
     R.HX = reinterpret_cast<float2 *>(smraw);
     R.HY = R.HX + (size_t)ty * kTX;
-    R.P = R.HY + (size_t)ty * kTX;
-    R.T = R.P + (ty + 2) * kPW;
+    R.F = R.HY + (size_t)ty * kTX;
+    R.T = R.F + (ty + 2) * kPW;
     R.HxL = R.T + (ty + 2) * kPW;
     R.HyB = R.HxL + ty;
+    float2 *const Rr = R.F;
+    const bool has_ring = tid < nring;
+    int rslot = 0, rgi = 0, rsrc = 0;
+    if (has_ring) {
+        ring_site(tid, tyb, x0, y0, lx, ly, rslot, rgi);
+        rsrc = ring_source(tid, ty, tyb, nslot, nb_l, nb_r, nb_d, nb_u);
+    }
+    const bool border = xl == 0 || xl == kTX - 1;  // or the first / last row, tested per row
+    const int grow = (y0 + yb) * lx + x0 + xl;      // lattice index of the thread's first row
+    if (tid == 0) {
+        sm_err = 0;
+        sc.rsq = (float)s->rsq;
+        sc.rmax = (float)fmin(s->rmax, 1e38);
+        sc.rn = 0.f;
+        sc.beta = (float)s->beta;
+        sc.scale = (float)s->scale;
+        sc.delta = (float)s->delta;
+        sc.stop = (float)(s->eps * sqrt(s->bsq));
+        sc.k = s->k;
+        sc.max_iter = s->max_iter;
+        sc.status = -1;
+        sc.reliable = 0;
+        sc.iters = 0;
+    }
 
-    // ---- entry: the rectangle's state into registers and shared memory
-    float2 rv[NY], xv[NY];
+    // ---- entry: r, links and the direction p of the rectangle on chip (p in registers and,
+    // for one stencil, in T with its ring); t_old = D p into T
+    float2 pv[NY], tmp[NY], xv[XREG ? NY : 1];
 #pragma unroll
     for (int q = 0; q < NY; q++) {
         const int yl = yb + q;
-        rv[q] = xv[q] = make_float2(0.f, 0.f);
+        pv[q] = make_float2(0.f, 0.f);
+        if (XREG) xv[q] = make_float2(0.f, 0.f);
         if (q < nrow) {
-            const int gi = (y0 + yl) * lx + x0 + xl;
-            rv[q] = __ldcg(r + gi);
-            xv[q] = __ldcg(xlo + gi);
-            R.P[(yl + 1) * kPW + xl + 1] = __ldcg(p0 + gi);
+            const int gi = grow + q * lx;
+            Rr[(yl + 1) * kPW + xl + 1] = __ldcg(r + gi);
+            pv[q] = __ldcg(p0 + gi);
+            if (XREG) xv[q] = __ldcg(xlo + gi);
+            R.T[(yl + 1) * kPW + xl + 1] = pv[q];
             const float4 h = __ldg(reinterpret_cast<const float4 *>(H) + gi);
             R.HX[yl * kTX + xl] = make_float2(h.x, h.y);
             R.HY[yl * kTX + xl] = make_float2(h.z, h.w);
@@ -304,149 +447,155 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *p1, floa
             R.HyB[k - tyb] = __ldg(H + 2 * (ym * lx + x0 + (k - tyb)) + 1);
         }
     }
-
-    // FP64 recurrence state: used by lane 0 of warp 0 only
-    double rsq = s->rsq, rmax = s->rmax, rn = 0.0;
-    double beta64 = s->beta;
-    const double scale = s->scale;
-    const float delta = (float)s->delta, stop = (float)(s->eps * sqrt(s->bsq));
-    int k = s->k;
-    const int max_iter = s->max_iter;
-    const unsigned ebase = pf->epoch;
-    int j = 0, status = -1, phases = 0;
-    bool reliable = false;
-    float fb = (float)s->beta;
-    const bool has_ring = tid < nring;
-    int rslot = 0, rgi = 0;
-    if (has_ring) ring_site(tid, tyb, x0, y0, lx, ly, rslot, rgi);
-    const bool border_x = xl == 0 || xl == kTX - 1;
-    const int grow = (y0 + yb) * lx + x0 + xl;  // lattice index of the thread's first row
+    if (has_ring) {
+        Rr[rslot] = __ldcg(r + rgi);
+        R.T[rslot] = __ldcg(p0 + rgi);
+    }
     __syncthreads();
+    {
+        auto body = [&](int q, int, float2 cur, float2 hs) { tmp[q] = fadd(fscale(mass, cur), hs); };
+        if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+        else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NY; q++)
+        if (q < nrow) R.T[(yb + q + 1) * kPW + xl + 1] = tmp[q];
+
+    unsigned ep = pf->epoch;  // epoch of the last phase published (every launch continues it)
+    float fb = (float)s->beta;
+    bool first = true;
     for (;;) {
-        // the neighbours' direction: the launch's input (p0) before their first export to p1
-        const float2 *pex = j == 0 ? p0 : p1;
-        // ---- A: p' = r + beta p on the rectangle and its ring (the ring loads first, so that
-        // their latency overlaps the update of the own sites)
-        float2 ra = make_float2(0.f, 0.f), rb = ra;
-        if (has_ring) {
-            ra = __ldcg(r + rgi);
-            rb = __ldcg(pex + rgi);
+        // ---- A: u = D r (needs only the ring of r), then beta from the previous phase's total;
+        // t = u + beta t_old (= D p'), p' = r + beta p
+        {
+            auto body = [&](int q, int, float2 cur, float2 hs) { tmp[q] = fadd(fscale(mass, cur), hs); };
+            if (nrow == NY) hop_rows<NY, true>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            else if (nrow > 0) hop_rows<NY, false>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
+        if (!first) {
+            if (warp == 0) {
+                float tot = 0.f;
+                const bool ok = wait_total(pf, ep, nb, tot);
+                if (lane == 0) {
+                    int ctl = kResGo;
+                    sc.rn = tot;
+                    sc.k++;
+                    sc.iters++;
+                    if (!ok || sm_err) {
+                        sc.status = GLINALG_SOLVE_TIMEOUT;
+                        ctl = kResStop;
+                    } else if (!isfinite(tot)) {
+                        sc.status = GLINALG_SOLVE_NONFINITE;
+                        ctl = kResStop;
+                    } else {
+                        const float rho = sqrtf(tot) * sc.scale;  // true-scale iterated residual
+                        if (rho > sc.rmax) sc.rmax = rho;
+                        if (rho < sc.delta * sc.rmax || rho < sc.stop || sc.k >= sc.max_iter) {
+                            sc.reliable = 1;
+                            ctl = kResReliable;
+                        } else {
+                            sc.beta = tot / sc.rsq;
+                            sc.rsq = tot;
+                            sm_scalar = sc.beta;
+                        }
+                    }
+                    sm_ctl = ctl;
+                }
+            }
+            __syncthreads();
+            if (sm_ctl != kResGo) break;
+            fb = sm_scalar;
+        }
+        first = false;
+        const unsigned eA = ++ep;
+        float acc = 0.f;
 #pragma unroll
         for (int q = 0; q < NY; q++) {
             if (q < nrow) {
-                float2 &pp = R.P[(yb + q + 1) * kPW + xl + 1];
-                pp = fadd(rv[q], fscale(fb, pp));
+                const int yl = yb + q, c = (yl + 1) * kPW + xl + 1;
+                const float2 tv = fadd(tmp[q], fscale(fb, R.T[c]));
+                const float2 pn = fadd(Rr[c], fscale(fb, pv[q]));
+                pv[q] = pn;
+                R.T[c] = tv;
+                acc += fn2(tv) + sigma * fn2(pn);
+                if (yl == 0 || yl == tyb - 1 || border) post_border(Mt, my, ty, tyb, xl, yl, tv, eA);
             }
         }
-        if (has_ring) R.P[rslot] = fadd(ra, fscale(fb, rb));
+        publish<NW>(acc, pf, eA, sm_w);
+        if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err);
         __syncthreads();
-        // t = D p' ; |t|^2 + sigma |p'|^2 ; export the border of t
-        float acc = 0.f;
+        // ---- B: Ap = D^dagger t + sigma p' (needs only the ring of t), then alpha from the
+        // total of A; x_lo += alpha p', r -= alpha Ap
         {
-            float2 *__restrict__ Tw = R.T;
-            auto body = [&](int q, int yl, float2 cur, float2 hs) {
-                const float2 tv = fadd(fscale(mass, cur), hs);
-                Tw[(yl + 1) * kPW + xl + 1] = tv;
-                acc += fn2(tv) + sigma * fn2(cur);
-                if (yl == 0 || yl == tyb - 1 || border_x) t[grow + q * lx] = tv;
-            };
-            if (nrow == NY) hop_rows<NY, true>(R.P, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
-            else if (nrow > 0) hop_rows<NY, false>(R.P, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
-        }
-        double tot = 0.0;
-        const bool okA = phase_exchange<NW>(acc, pf, ebase + ++phases, nb, sm_w, tot);
-        if (tid == 0) {
-            int ctl = kResGo;
-            if (!okA) {
-                status = GLINALG_SOLVE_TIMEOUT;
-                ctl = kResStop;
-            } else if (!(tot > 0.0) || !isfinite(tot)) {
-                status = tot == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
-                ctl = kResStop;
-            }
-            sm_alpha = (float)rsq / (float)tot;
-            sm_ctl = ctl;
-        }
-        __syncthreads();
-        if (sm_ctl != kResGo) break;
-        const float alpha = sm_alpha;
-        // ---- B: the ring of t, then Ap = D^dagger t + sigma p', x_lo += alpha p', r -= alpha Ap
-        if (has_ring) R.T[rslot] = __ldcg(t + rgi);
-        __syncthreads();
-        acc = 0.f;
-        {
-            const float2 *__restrict__ Pr = R.P;
-            auto body = [&](int q, int yl, float2 cur, float2 hs) {
-                const float2 pv = Pr[(yl + 1) * kPW + xl + 1];
-                const float2 av = fadd(fsub(fscale(mass, cur), hs), fscale(sigma, pv));
-                xv[q] = fadd(xv[q], fscale(alpha, pv));
-                rv[q] = fsub(rv[q], fscale(alpha, av));
-                acc += fn2(rv[q]);
-                if (yl == 0 || yl == tyb - 1 || border_x) {
-                    r[grow + q * lx] = rv[q];
-                    p1[grow + q * lx] = pv;
-                }
+            auto body = [&](int q, int, float2 cur, float2 hs) {
+                tmp[q] = fadd(fsub(fscale(mass, cur), hs), fscale(sigma, pv[q]));
             };
             if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
             else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
-        const bool okB = phase_exchange<NW>(acc, pf, ebase + ++phases, nb, sm_w, tot);
-        j++;
-        if (tid == 0) {
-            int ctl = kResGo;
-            rn = tot;
-            k++;
-            if (!okB) {
-                status = GLINALG_SOLVE_TIMEOUT;
-                ctl = kResStop;
-            } else if (!isfinite(rn)) {
-                status = GLINALG_SOLVE_NONFINITE;
-                ctl = kResStop;
-            } else {
-                const float rho = sqrtf((float)rn) * (float)scale;  // true-scale iterated residual
-                if (rho > rmax) rmax = rho;
-                if (rho < delta * (float)rmax || rho < stop || k >= max_iter) {
-                    reliable = true;
-                    ctl = kResReliable;
-                } else {
-                    const float b = (float)rn / (float)rsq;
-                    beta64 = b;
-                    rsq = rn;
-                    sm_beta = b;
+        if (warp == 0) {
+            float tot = 0.f;
+            const bool ok = wait_total(pf, eA, nb, tot);
+            if (lane == 0) {
+                int ctl = kResGo;
+                if (!ok || sm_err) {
+                    sc.status = GLINALG_SOLVE_TIMEOUT;
+                    ctl = kResStop;
+                } else if (!(tot > 0.f) || !isfinite(tot)) {
+                    sc.status = tot == 0.f ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
+                    ctl = kResStop;
                 }
+                sm_scalar = sc.rsq / tot;
+                sm_ctl = ctl;
             }
-            sm_ctl = ctl;
         }
         __syncthreads();
         if (sm_ctl != kResGo) break;
-        fb = sm_beta;
+        const float alpha = sm_scalar;
+        const unsigned eB = ++ep;
+        acc = 0.f;
+#pragma unroll
+        for (int q = 0; q < NY; q++) {
+            if (q < nrow) {
+                const int yl = yb + q, c = (yl + 1) * kPW + xl + 1;
+                if (XREG) xv[q] = fadd(xv[q], fscale(alpha, pv[q]));
+                else red_add2(xlo + grow + q * lx, fscale(alpha, pv[q]));
+                const float2 rnv = fsub(Rr[c], fscale(alpha, tmp[q]));
+                Rr[c] = rnv;
+                acc += fn2(rnv);
+                if (yl == 0 || yl == tyb - 1 || border) post_border(Mr, my, ty, tyb, xl, yl, rnv, eB);
+            }
+        }
+        publish<NW>(acc, pf, eB, sm_w);
+        if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err);
+        __syncthreads();
     }
     // ---- exit: the rectangle's r, x_lo and direction back to global memory (direction in p0)
 #pragma unroll
     for (int q = 0; q < NY; q++) {
         if (q < nrow) {
             const int gi = grow + q * lx;
-            r[gi] = rv[q];
-            xlo[gi] = xv[q];
-            p0[gi] = R.P[(yb + q + 1) * kPW + xl + 1];
+            r[gi] = Rr[(yb + q + 1) * kPW + xl + 1];
+            p0[gi] = pv[q];
+            if (XREG) xlo[gi] = xv[q];
         }
     }
     if (blockIdx.x == 0 && tid == 0) {
-        pf->epoch = ebase + phases;  // every block ran the same phases
-        s->k = k;
-        s->rmax = rmax;
-        s->rsq = rsq;
-        s->beta = beta64;
-        s->rsq_new = rn;
+        pf->epoch = ep;  // every block ran the same phases
+        s->k = sc.k;
+        s->rmax = sc.rmax;
+        s->rsq = sc.rsq;
+        s->beta = sc.beta;
+        s->rsq_new = sc.rn;
         s->parity = 0;
-        if (status >= 0) {
-            s->status = status;
+        if (sc.status >= 0) {
+            s->status = sc.status;
             s->done = 1;
         }
-        if (reliable) s->reliable = 1;
+        if (sc.reliable) s->reliable = 1;
         s->inner_ns += gtimer() - t_start;
-        s->inner_iters += j;
+        s->inner_iters += sc.iters;
         s->inner_launches += 1;
     }
 }

@@ -273,8 +273,9 @@ glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision,
 int glinalg_tuned_tile(glinalg_operator op, int precision);
 /* Persistent inner-loop kernel the autotuner picked for op's lattice and precision: 0-3 the
  * register-tiled kernel (16 warps x 4 rows, 16 x 8, 32 x 2, 16 x 2), 4-5 the bulk-copy kernel
- * (256 x 4 and 512 x 2 tiles), 6-7 the rectangle-resident kernel (FP32 only; 16 and 32
- * warps); -1 if none serves the lattice or no mixed solve has run on it yet. */
+ * (256 x 4 and 512 x 2 tiles), 6-8 the rectangle-resident kernel (FP32 only: 16 warps with
+ * x_lo in registers, 32 warps, 16 warps with x_lo in memory); -1 if none serves the lattice or
+ * no mixed solve has run on it yet. */
 int glinalg_tuned_persist(glinalg_operator op, int precision);
 
 /* ---- inputs the way the reference's tests make them (host side) ----

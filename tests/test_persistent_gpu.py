@@ -70,7 +70,7 @@ def check(res, kappa):
     assert res["launches"] >= 1, res  # the persistent inner loop ran
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7, 8])
 def test_persistent_candidate_1024(gl, gpu, tmp_path, shape):
     """The 1024x1024, m = 0.01 system (kappa ~ 2e4) with each persistent kernel forced."""
     res = run_case(tmp_path, 1024, 1024, 0.01, 1337, shape)
@@ -82,7 +82,7 @@ def test_persistent_candidate_1024(gl, gpu, tmp_path, shape):
 def test_resident_kernel_small_lattices(gl, gpu, tmp_path, lx, ly):
     """Lattices that only the rectangle-resident kernel serves: one or several 128-column
     rectangles across, full and short last rectangles, one-row rectangles (128 x 90)."""
-    for shape in (6, 7):
+    for shape in (6, 7, 8):
         res = run_case(tmp_path, lx, ly, 0.05, 99, shape)
         assert res["tuned"] == shape
         check(res, 1e3)
