@@ -203,16 +203,30 @@ __device__ __forceinline__ unsigned long long tag(unsigned e, float v)
     return ((unsigned long long)e << 32) | __float_as_uint(v);
 }
 
-// Writes border site (xl, yl) of the block's rectangle (tyb rows) with value v and epoch e into
-// every mailbox slot it belongs to.  M: the field's mailboxes; my: this block's first word.
-__device__ __forceinline__ void post_border(unsigned long long *M, int my, int ty, int tyb, int xl, int yl,
-                                            float2 v, unsigned e)
+// Border slot k of a rectangle (tyb rows): the shared-memory position of the site it carries and
+// its slot in the block's mailbox.  Slots: bottom row, top row (kTX each), then the left and
+// the right column (ty each, tyb used); a corner site is carried by two slots.
+__device__ __forceinline__ void border_slot(int k, int ty, int tyb, int &pos, int &slot)
 {
-    const unsigned long long a = tag(e, v.x), b = tag(e, v.y);
-    if (yl == 0) st_relaxed_2u64(M + my + 2 * xl, a, b);
-    if (yl == tyb - 1) st_relaxed_2u64(M + my + 2 * (kTX + xl), a, b);
-    if (xl == 0) st_relaxed_2u64(M + my + 2 * (2 * kTX + yl), a, b);
-    if (xl == kTX - 1) st_relaxed_2u64(M + my + 2 * (2 * kTX + ty + yl), a, b);
+    int xl, yl;
+    if (k < kTX) {
+        xl = k;
+        yl = 0;
+        slot = k;
+    } else if (k < 2 * kTX) {
+        xl = k - kTX;
+        yl = tyb - 1;
+        slot = k;
+    } else if (k < 2 * kTX + tyb) {
+        xl = 0;
+        yl = k - 2 * kTX;
+        slot = 2 * kTX + yl;
+    } else {
+        xl = kTX - 1;
+        yl = k - 2 * kTX - tyb;
+        slot = 2 * kTX + ty + yl;
+    }
+    pos = (yl + 1) * kPW + xl + 1;
 }
 
 // The mailbox word (within a field) that feeds ring site k: the row below comes from the top
@@ -271,12 +285,14 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &c)
     c = (a - (s - bb)) + (b - bb);
 }
 
-// Publishes the block's partial sum of phase e (every thread passes its `acc`): FP32 within
-// warps and across the block's warps, one tagged word written by thread 0.
+// Publishes phase e (every thread passes its `acc`): the block's partial sum (FP32 within warps
+// and across the block's warps, one tagged word written by thread 0) and the border of the field
+// F just written to shared memory (thread k < nborder posts border slot k to the mailbox M).
 template <int NW>
-__device__ __forceinline__ void publish(float acc, PhaseFlags *pf, unsigned e, float *sm_w)
+__device__ __forceinline__ void publish(float acc, PhaseFlags *pf, unsigned e, float *sm_w, const float2 *F,
+                                        unsigned long long *M, int nborder, int bpos, int bslot)
 {
-    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (lane == 0) sm_w[warp] = acc;
@@ -287,48 +303,43 @@ __device__ __forceinline__ void publish(float acc, PhaseFlags *pf, unsigned e, f
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) st_relaxed_u64(pf->w[e & 1] + blockIdx.x, tag(e, v));
     }
+    if (tid < nborder) {
+        const float2 v = F[bpos];
+        st_relaxed_2u64(M + 2 * bslot, tag(e, v.x), tag(e, v.y));
+    }
 }
 
-// Called by warp 0: waits until every block's word carries epoch e and sums the partials in
-// block order (compensated FP32), identically in every block.  The total is in lane 0.
-__device__ __forceinline__ bool wait_total(PhaseFlags *pf, unsigned e, unsigned nb, float &total)
+// Called by threads 0 .. nb-1: thread b waits until block b's word carries epoch e and stages
+// its partial in sm_part[b]; a wait that runs out sets *err.  One word per thread keeps the
+// poll's registers few (they count for every thread of the block).
+__device__ __forceinline__ void poll_partial(PhaseFlags *pf, unsigned e, int b, float *sm_part, int *err)
+{
+    const unsigned long long *w = pf->w[e & 1] + b;
+    const long long t0 = clock64();
+    for (unsigned n = 1;; n++) {
+        const unsigned long long v = ld_relaxed_u64(w);
+        if ((unsigned)(v >> 32) == e) {
+            sm_part[b] = __uint_as_float((unsigned)v);
+            return;
+        }
+        if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
+            atomicExch(&pf->error, 1);
+            *err = 1;
+            sm_part[b] = 0.f;
+            return;
+        }
+    }
+}
+
+// Called by warp 0 after the partials are staged: their sum in block order (compensated FP32),
+// identical in every block; the total is in lane 0.
+__device__ __forceinline__ float sum_partials(const float *sm_part, unsigned nb)
 {
     const int lane = threadIdx.x;
-    const unsigned long long *W = pf->w[e & 1];
-    float vals[kPerLane];
-    unsigned pending = 0;
-#pragma unroll
-    for (int i = 0; i < kPerLane; i++) {
-        vals[i] = 0.f;
-        if (lane + 32 * i < (int)nb) pending |= 1u << i;
-    }
-    const long long t0 = clock64();
-    bool ok = true;
-    for (unsigned n = 1;; n++) {
-#pragma unroll
-        for (int i = 0; i < kPerLane; i++) {
-            if (pending & (1u << i)) {
-                const unsigned long long w = ld_relaxed_u64(W + lane + 32 * i);
-                if ((unsigned)(w >> 32) == e) {
-                    vals[i] = __uint_as_float((unsigned)w);
-                    pending &= ~(1u << i);
-                }
-            }
-        }
-        if (__all_sync(0xffffffffu, pending == 0)) break;
-        const bool give_up =
-            (n & 15) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0);
-        if (__any_sync(0xffffffffu, give_up)) {
-            if (lane == 0) atomicExch(&pf->error, 1);
-            ok = false;
-            break;
-        }
-    }
     float hi = 0.f, lo = 0.f;
-#pragma unroll
-    for (int i = 0; i < kPerLane; i++) {
+    for (int b = lane; b < (int)nb; b += 32) {
         float c;
-        two_sum(hi, vals[i], hi, c);
+        two_sum(hi, sm_part[b], hi, c);
         lo += c;
     }
 #pragma unroll
@@ -338,8 +349,7 @@ __device__ __forceinline__ bool wait_total(PhaseFlags *pf, unsigned e, unsigned 
         two_sum(hi, h2, hi, c);
         lo += l2 + c;
     }
-    total = hi + lo;
-    return ok;
+    return hi + lo;
 }
 
 }  // namespace res
@@ -370,6 +380,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     __shared__ float sm_scalar;
     __shared__ int sm_ctl, sm_err;
     __shared__ ResScalars sc;
+    __shared__ float sm_part[kMaxBlocks];
     if (s->done || s->reliable) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
@@ -386,7 +397,6 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     const int nb_l = by * gx + (bx + gx - 1) % gx, nb_r = by * gx + (bx + 1) % gx;
     const int nb_d = ((by + gy - 1) % gy) * gx + bx, nb_u = ((by + 1) % gy) * gx + bx;
     unsigned long long *const Mr = mbox, *const Mt = mbox + 2 * (size_t)nb * nslot;
-    const int my = 2 * (int)blockIdx.x * nslot;
     Rect R;
     R.HX = reinterpret_cast<float2 *>(smraw);
     R.HY = R.HX + (size_t)ty * kTX;
@@ -401,7 +411,14 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         ring_site(tid, tyb, x0, y0, lx, ly, rslot, rgi);
         rsrc = ring_source(tid, ty, tyb, nslot, nb_l, nb_r, nb_d, nb_u);
     }
-    const bool border = xl == 0 || xl == kTX - 1;  // or the first / last row, tested per row
+    // border slot tid (posted from shared memory after each pointwise pass); the slot index
+    // includes this block's mailbox offset
+    const int nborder = nring;
+    int bpos = 0, bslot = 0;
+    if (tid < nborder) {
+        border_slot(tid, ty, tyb, bpos, bslot);
+        bslot += (int)blockIdx.x * nslot;
+    }
     const int grow = (y0 + yb) * lx + x0 + xl;      // lattice index of the thread's first row
     if (tid == 0) {
         sm_err = 0;
@@ -474,15 +491,16 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             else if (nrow > 0) hop_rows<NY, false>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
         if (!first) {
+            if (tid < (int)nb) poll_partial(pf, ep, tid, sm_part, &sm_err);
+            __syncthreads();
             if (warp == 0) {
-                float tot = 0.f;
-                const bool ok = wait_total(pf, ep, nb, tot);
+                const float tot = sum_partials(sm_part, nb);
                 if (lane == 0) {
                     int ctl = kResGo;
                     sc.rn = tot;
                     sc.k++;
                     sc.iters++;
-                    if (!ok || sm_err) {
+                    if (sm_err) {
                         sc.status = GLINALG_SOLVE_TIMEOUT;
                         ctl = kResStop;
                     } else if (!isfinite(tot)) {
@@ -519,10 +537,9 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
                 pv[q] = pn;
                 R.T[c] = tv;
                 acc += fn2(tv) + sigma * fn2(pn);
-                if (yl == 0 || yl == tyb - 1 || border) post_border(Mt, my, ty, tyb, xl, yl, tv, eA);
             }
         }
-        publish<NW>(acc, pf, eA, sm_w);
+        publish<NW>(acc, pf, eA, sm_w, R.T, Mt, nborder, bpos, bslot);
         if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err);
         __syncthreads();
         // ---- B: Ap = D^dagger t + sigma p' (needs only the ring of t), then alpha from the
@@ -534,12 +551,13 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
             else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
+        if (tid < (int)nb) poll_partial(pf, eA, tid, sm_part, &sm_err);
+        __syncthreads();
         if (warp == 0) {
-            float tot = 0.f;
-            const bool ok = wait_total(pf, eA, nb, tot);
+            const float tot = sum_partials(sm_part, nb);
             if (lane == 0) {
                 int ctl = kResGo;
-                if (!ok || sm_err) {
+                if (sm_err) {
                     sc.status = GLINALG_SOLVE_TIMEOUT;
                     ctl = kResStop;
                 } else if (!(tot > 0.f) || !isfinite(tot)) {
@@ -564,10 +582,9 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
                 const float2 rnv = fsub(Rr[c], fscale(alpha, tmp[q]));
                 Rr[c] = rnv;
                 acc += fn2(rnv);
-                if (yl == 0 || yl == tyb - 1 || border) post_border(Mr, my, ty, tyb, xl, yl, rnv, eB);
             }
         }
-        publish<NW>(acc, pf, eB, sm_w);
+        publish<NW>(acc, pf, eB, sm_w, Rr, Mr, nborder, bpos, bslot);
         if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err);
         __syncthreads();
     }
