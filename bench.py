@@ -38,9 +38,15 @@ MAX_ITER = 100000
 REF_ITERS = 2093
 METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB300; HBM GB/s"
 HEADLINE = ("fp32", 1)
-# DRAM bytes (read + write) of one launch of the FP32 persistent inner-loop kernel on this
-# workload (the first launch of a solve, 254 inner iterations), from an ncu --set full capture
+# DRAM bytes (read + write) of one launch of the persistent inner-loop kernels on this workload,
+# from ncu --set full captures: k_persist (fields in L2; the first launch of a solve, 254 inner
+# iterations) and k_resident (rectangle state on chip; a 20-iteration launch).  In both the
+# traffic is the compulsory load of the launch's state and does not grow with its iterations.
 K_PERSIST_DRAM_BYTES = 41.987328e6 + 3.212544e6
+K_RESIDENT_DRAM_BYTES = 42.633728e6 + 0.0128e6
+# Shared-memory wavefronts (128 B) per SM and inner iteration of k_resident at 1024^2, from the
+# same capture (24.65 M over 152 SMs and 20 iterations); GB300 serves one per clock per SM.
+K_RESIDENT_SMEM_WAVEFRONTS = 8.1e3
 VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 # persistent inner-loop kernels by the library's candidate index (glinalg_tuned_persist)
 PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 rows>",
@@ -335,7 +341,7 @@ def workload_batch(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=2)
@@ -449,15 +455,27 @@ def main():
     op.apply(Ax, x)
 
     # dominant kernel: the persistent inner-loop kernel of the headline solve (both stencil
-    # phases, the vector updates and the grid barriers); its device time is read by the kernel
-    # itself (%globaltimer at entry and exit, summed over its launches) during the timed solves
+    # phases, the vector updates and the grid-wide sums), timed with CUDA events around launches
+    # of its own on the library stream, each running the timed solve's mean inner iterations per
+    # launch; cross-checked with the kernel's device clock inside the timed solves
     peak, peak_src = peaks()
     hi_ = head_infos[-1]
     k_launch = max(1, hi_.kernel_launches)
-    persist_kernel = PERSIST_KERNELS.get(L.glinalg_tuned_persist(op.handle, head_prec), "none")
-    k_ms = hi_.kernel_ms / k_launch
-    k_bytes = hi_.kernel_gbytes * 1e9 / k_launch
-    achieved = (k_bytes / (k_ms * 1e-3) / 1e9) if k_ms > 0 else 0.0
+    persist_cand = L.glinalg_tuned_persist(op.handle, head_prec)
+    persist_kernel = PERSIST_KERNELS.get(persist_cand, "none")
+    resident = persist_cand in (6, 7, 8)
+    # algorithmic bytes: the canonical CG iteration on D^dagger D, 17 complex words per site
+    # (D p -> t: p, 2 links, t; D^dagger t -> Ap: t, 2 links, Ap; x, p, r, Ap in, x, r out;
+    # p = r + beta p: 3), 136 B per site in FP32
+    cg_bytes = 17 * 8.0 * LX * LY
+    k_ms_solve = hi_.kernel_ms / k_launch
+    achieved_solve = (cg_bytes * hi_.iter / k_launch / (k_ms_solve * 1e-3) / 1e9) if k_ms_solve > 0 else 0.0
+    it_per_launch = max(1, round(hi_.iter / k_launch))
+    ev_ms, ev_bytes, ev_cand = C_double(), C_double(), C_int()
+    gl._capi.check(L.glinalg_profile_persist_kernel(op.handle, head_prec, 5, it_per_launch, ev_ms, ev_bytes,
+                                                    ev_cand), "profile_persist_kernel")
+    k_ms, k_bytes = ev_ms.value, cg_bytes * it_per_launch
+    achieved = k_bytes / (k_ms * 1e-3) / 1e9
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
     Uh = torch.from_numpy(U).pin_memory().numpy()
@@ -497,6 +515,23 @@ def main():
     # then per cycle of the outer loop the persistent inner-loop kernel, the reliable update
     # (6), the outer-loop tail and the graph's loop guard
     launches = 8 + 9 * hi.kernel_launches
+    roof_note = ("dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel (ncu --set full "
+                 "capture): the compulsory load of the launch's state, which does not grow with its iterations")
+    onchip = None
+    if resident:
+        # the CG iteration's fields never leave the SM: the HBM-roofline fraction (algorithmic bytes
+        # over the HBM peak) above 1 says how much faster than any HBM-streaming iteration it runs;
+        # the binding on-chip resource is shared-memory bandwidth (measured wavefronts per iteration)
+        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+        iters_l = it_per_launch
+        smem_bytes = K_RESIDENT_SMEM_WAVEFRONTS * 128.0 * n_sm * iters_l
+        sm_clk = (clk.get("sm_mhz") or 2070.0) if isinstance(clk, dict) else 2070.0
+        smem_peak = 128.0 * sm_clk * 1e6 * n_sm / 1e9
+        smem_ach = smem_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else 0.0
+        onchip = {"resource": "shared memory", "achieved": round(smem_ach, 1), "peak": round(smem_peak, 1),
+                  "unit": "GB/s", "frac": round(smem_ach / smem_peak, 3),
+                  "note": "128 B x 8.1k wavefronts per SM and iteration (ncu) over the kernel's device time; peak "
+                          "128 B per clock per SM at the sampled SM clock"}
     line = {
         "metric": METRIC, "value": round(ms_max, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False,
@@ -509,16 +544,24 @@ def main():
                    "true_relres_fp64": relres, "fp64_gpu_ms": round(t64m, 3),
                    "speedup_vs_fp64_gpu": round(t64m / ms, 2), "variants": variants},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "traffic": K_PERSIST_DRAM_BYTES,
-                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one k_persist launch "
-                                     "(the first of a solve, 254 inner iterations; ncu --set full capture): "
-                                     "the FP32 working set stays in L2, so DRAM traffic is the compulsory first read "
-                                     "and does not grow with the iterations of a launch",
-                     "kernel": f"{persist_kernel} ({head_name}; inner CG iterations: D p, D^dagger t, updates, 2 grid barriers)",
+                     "frac": round(achieved / peak, 3),
+                     "traffic": K_RESIDENT_DRAM_BYTES if resident else K_PERSIST_DRAM_BYTES,
+                     "traffic_note": roof_note,
+                     "algorithmic_bytes": "136 B per site and inner iteration: the CG iteration on D^dagger D "
+                                          "as 17 complex FP32 words per site (D p -> t: 4; D^dagger t -> Ap: 4; "
+                                          "x, p, r, Ap in, x, r out: 6; p = r + beta p: 3), its traffic if its "
+                                          "fields streamed from memory",
+                     "onchip": onchip,
+                     "kernel": f"{persist_kernel} ({head_name}; inner CG iterations: D p, D^dagger t, updates, "
+                               "2 grid-wide sums)",
                      "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 4),
-                     "launches_per_solve": hi_.kernel_launches,
+                     "iters_per_launch": it_per_launch, "launches_per_solve": hi_.kernel_launches,
                      "share_of_solve": round(hi_.kernel_ms / hi_.device_ms, 3) if hi_.device_ms else None,
-                     "timing": "device clock read by the kernel at entry and exit, inside the timed solves",
+                     "timing": "CUDA events on the library stream around 5 launches of the kernel, each running "
+                               "the timed solve's mean inner iterations per launch",
+                     "achieved_in_solve": round(achieved_solve, 1),
+                     "timing_in_solve": "device clock read by the kernel at entry and exit, summed over its "
+                                        "launches inside the timed solves",
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": int(Uh.nbytes + bh.nbytes + xh.nbytes),
                 "d2h_bytes_per_step": int(xh.nbytes)},
@@ -532,7 +575,7 @@ def main():
         dist.destroy_process_group()
 
 
-from ctypes import c_double as C_double, c_void_p as C_void  # noqa: E402
+from ctypes import c_double as C_double, c_int as C_int, c_void_p as C_void  # noqa: E402
 
 if __name__ == "__main__":
     main()

@@ -1140,6 +1140,88 @@ static glinalg_status profile_inner(const glinalg_operator_s *op, int variant, i
     return GLINALG_SUCCESS;
 }
 
+// Times the tuned persistent inner-loop kernel of op's lattice with CUDA events: n_launch
+// launches (after one untimed) of exactly n_iter inner iterations each, on CG for A x = 1 from
+// r = 1, p = 0 (the per-iteration work does not depend on the values).  Each launch is queued
+// behind a short busy wait so that the events bracket the kernel, not the host's launch latency.
+template <class S, class R, class LK>
+static glinalg_status profile_persist(const glinalg_operator_s *op, int variant, int n_launch, int n_iter,
+                                      double *ms, double *bytes, int *cand_out)
+{
+    const long n = op->size;
+    const int lx = op->lx, ly = op->ly;
+    const int cand = persist_tuned(lx, ly, variant);
+    if (cand < 0) {
+        set_last_error("no persistent inner-loop kernel has been tuned for this lattice and precision "
+                       "(run a mixed-precision solve on it first)");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    const PersistKernel<S, R, LK> pk = persist_cand<S, R, LK>(cand, lx, ly);
+    if (!pk.ok()) {
+        set_last_error("the tuned persistent kernel is not available");
+        return GLINALG_ERROR_INTERNAL;
+    }
+    cudaStream_t st = lib_stream();
+    Scratch sc(st);
+    R *r;
+    S *p0, *p1, *t;
+    LK *L;
+    float2 *xlo;
+    MxDev *s;
+    GridSync *gs;
+    res::PhaseFlags *pf;
+    unsigned long long *mbox = nullptr;
+    double *partA, *partB, *ones;
+    GL_TRY(sc.alloc(&r, n));
+    GL_TRY(sc.zeros(&p0, n));
+    GL_TRY(sc.zeros(&p1, n));
+    GL_TRY(sc.zeros(&t, n));
+    GL_TRY(sc.alloc(&L, 2 * n));
+    GL_TRY(sc.zeros(&xlo, n));
+    GL_TRY(sc.zeros(&s, 1));
+    GL_TRY(sc.zeros(&gs, 1));
+    GL_TRY(sc.zeros(&pf, 1));
+    GL_TRY(sc.alloc(&partA, sm_count()));
+    GL_TRY(sc.alloc(&partB, sm_count()));
+    GL_TRY(sc.alloc(&ones, 2 * n));
+    if (pk.fr) GL_TRY(sc.zeros(&mbox, res::mbox_words(sm_count(), pk.plan.ty)));
+    std::vector<double2> h1(n, cmk(1.0, 0.0));
+    GL_CUDA(cudaMemcpyAsync(ones, h1.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+    k_make_hop<LK><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
+    GL_CUDA(cudaGetLastError());
+    MxDev h = {};
+    h.rsq = (double)n;  // |r|^2 of r = 1
+    h.scale = 1.0;
+    h.bsq = 1.0;
+    h.rmax = 1e300;
+    h.max_iter = n_iter;  // delta = eps = 0: the launch runs exactly n_iter iterations
+    EventTimer tm;
+    double sum = 0.0;
+    for (int it = 0; it <= n_launch; it++) {
+        k_copy_links<R><<<vgrid(n), 256, 0, st>>>(r, reinterpret_cast<const double2 *>(ones), n);
+        GL_CUDA(cudaMemsetAsync(p0, 0, sizeof(S) * n, st));
+        GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+        k_busy_wait<<<1, 1, 0, st>>>(50000);
+        tm.start(st);
+        GL_CUDA(launch_persist(pk, st, L, r, p0, p1, t, xlo, (float)op->mass, 0.f, lx, ly, s, gs, partA, partB, pf,
+                               mbox));
+        tm.stop(st);
+        MxDev back;
+        GL_CUDA(cudaMemcpyAsync(&back, s, sizeof(back), cudaMemcpyDeviceToHost, st));
+        GL_CUDA(cudaStreamSynchronize(st));
+        if (back.k != n_iter || back.done) {
+            set_last_error("the persistent kernel did not run the requested iterations");
+            return GLINALG_ERROR_INTERNAL;
+        }
+        if (it > 0) sum += tm.ms();
+    }
+    *ms = sum / n_launch;
+    const double w = Fmt<S>::bytes, wr = Fmt<R>::bytes, wl = Fmt<LK>::bytes;
+    *bytes = (double)n_iter * (6.0 * w + 4.0 * wl + 3.0 * wr + 16.0) * n;  // per launch, as in info->kernel_gbytes
+    *cand_out = cand;
+    return GLINALG_SUCCESS;
+}
+
 int tuned_tile(const glinalg_operator_s *op, int variant)
 {
     std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1167,6 +1249,22 @@ extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int
     case GLINALG_PREC_SINGLE: return profile_inner<float2, float2, float2>(op, 1, n_launch, ms, bytes);
     case GLINALG_PREC_HALF: return profile_inner<__half2, float2, __half2>(op, 2, n_launch, ms, bytes);
     case GLINALG_PREC_BFLOAT: return profile_inner<__nv_bfloat162, float2, float2>(op, 3, n_launch, ms, bytes);
+    default: return GLINALG_ERROR_INVALID_VALUE;
+    }
+}
+
+extern "C" glinalg_status glinalg_profile_persist_kernel(glinalg_operator op, int precision, int n_launch,
+                                                         int n_iter, double *ms, double *bytes, int *cand)
+{
+    using namespace glinalg;
+    if (!op || !ms || !bytes || !cand || n_launch <= 0 || n_iter <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (op->kind != GLINALG_OP_STAGGERED_NORMAL) return GLINALG_ERROR_UNSUPPORTED_OP;
+    GL_TRY(ensure_device());
+    switch (precision) {
+    case GLINALG_PREC_SINGLE: return profile_persist<float2, float2, float2>(op, 1, n_launch, n_iter, ms, bytes, cand);
+    case GLINALG_PREC_HALF: return profile_persist<__half2, float2, __half2>(op, 2, n_launch, n_iter, ms, bytes, cand);
+    case GLINALG_PREC_BFLOAT:
+        return profile_persist<__nv_bfloat162, float2, float2>(op, 3, n_launch, n_iter, ms, bytes, cand);
     default: return GLINALG_ERROR_INVALID_VALUE;
     }
 }

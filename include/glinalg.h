@@ -267,6 +267,13 @@ glinalg_status glinalg_staggered_normal_apply_noalloc(const double *links, doubl
  * op must be GLINALG_OP_STAGGERED_NORMAL; precision SINGLE, HALF or BFLOAT. */
 glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision, int n_launch,
                                              double ms[2], double bytes[2]);
+/* Times the persistent inner-loop kernel the autotuner picked for op's lattice and precision
+ * (a mixed-precision solve must have run on it): n_launch launches of exactly n_iter inner CG
+ * iterations each, bracketed by CUDA events on the library stream.  ms: mean milliseconds per
+ * launch; bytes: algorithmic bytes per launch; cand: the kernel (as glinalg_tuned_persist).
+ * Staggered normal operator only. */
+glinalg_status glinalg_profile_persist_kernel(glinalg_operator op, int precision, int n_launch, int n_iter,
+                                              double *ms, double *bytes, int *cand);
 /* Tile shape the autotuner picked for op's lattice and precision (an index into the
  * library's candidate list: 0 = 32x16, 1 = 32x32, 2 = 32x32 (4 rows of 8), 3 = 32x32
  * (16 rows of 2) sites per block), or -1 if no mixed solve has run on this lattice yet. */

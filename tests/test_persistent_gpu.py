@@ -43,9 +43,13 @@ for prec in (1, 0):
                  "launches": info.kernel_launches,
                  "relres": (torch.linalg.vector_norm(bt - Ax) / torch.linalg.vector_norm(bt)).item()}
 err = (torch.linalg.vector_norm(out[1]["x"] - out[0]["x"]) / torch.linalg.vector_norm(out[0]["x"])).item()
+import ctypes as C
+ms, nbytes, cand = C.c_double(), C.c_double(), C.c_int()
+st = gl.lib().glinalg_profile_persist_kernel(op.handle, 1, 2, 16, ms, nbytes, cand)
 print(json.dumps({"iter": out[1]["iter"], "iter64": out[0]["iter"], "success": out[1]["success"],
                   "relres": out[1]["relres"], "err": err, "launches": out[1]["launches"],
-                  "tuned": gl.lib().glinalg_tuned_persist(op.handle, 1)}))
+                  "tuned": gl.lib().glinalg_tuned_persist(op.handle, 1),
+                  "profile": [st, ms.value, nbytes.value, cand.value], "sites": lx * ly}))
 '''
 
 
@@ -68,6 +72,9 @@ def check(res, kappa):
     assert abs(res["iter"] - res["iter64"]) <= 0.05 * res["iter64"] + 2, res
     assert res["err"] < kappa * 1e-10, res
     assert res["launches"] >= 1, res  # the persistent inner loop ran
+    st, ms, nbytes, cand = res["profile"]  # the event-timed launches of the same kernel
+    assert st == 0 and ms > 0 and cand == res["tuned"], res
+    assert nbytes > 0, res
 
 
 @pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7, 8])
