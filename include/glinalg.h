@@ -128,7 +128,8 @@ typedef enum glinalg_precision {
 
 typedef struct glinalg_solver_params {
     int precision;     /* glinalg_precision; only CG on Hermitian kinds accepts != DOUBLE */
-    double delta;      /* reliable-update trigger: recompute when |r| < delta * max|r| (0 -> 0.1) */
+    double delta;      /* reliable-update trigger: recompute when |r| < delta * max|r| (0 -> 0.01
+                          for SINGLE, 0.1 for HALF and BFLOAT) */
     int flags;         /* GLINALG_PTR_DEVICE: phi / phi0 are device pointers */
     int reserved;
 } glinalg_solver_params;
