@@ -645,7 +645,8 @@ glinalg_status cg_batch_mixed(const glinalg_operator_s *const *ops, int nsys, do
                               const double2 *const *B, int max_iter, double eps, int precision, double delta,
                               glinalg_info *infos, cudaStream_t st)
 {
-    if (!(delta > 0.0 && delta < 1.0)) delta = 0.1;
+    // the single-system defaults: 0.01 for FP32 iterates, 0.1 for 16-bit storage
+    if (!(delta > 0.0 && delta < 1.0)) delta = precision == GLINALG_PREC_SINGLE ? 0.01 : 0.1;
     switch (precision) {
     case GLINALG_PREC_SINGLE:
         return run_batch<float2, float2, float2>(ops, nsys, X, B, max_iter, eps, delta, 1, infos, st, "CG-FP32");

@@ -121,10 +121,100 @@ static void stencil_apply(const orc_op *op, cplx *lhs, const cplx *rhs, int pari
     }
 }
 
+/* operator_utils/operators.cpp:455-497 (square_staggered_deo_u1) and :499-541
+ * (square_staggered_doe_u1): the hopping part of square_staggered_u1 (no mass) at the even
+ * (odd = 0) or odd (odd = 1) output sites, in the reference's order +x, -x, +y, -y, then the
+ * factor 1/2; sites of the other parity are zeroed. */
+static void staggered_hop_parity(cplx *lhs, const cplx *rhs, const cplx *U, int lx, int ly, int odd)
+{
+    for (long i = 0; i < (long)lx * ly; i++) {
+        int x = (int)(i % lx), y = (int)(i / lx);
+        double eta1 = (double)(1 - 2 * (x % 2));
+        lhs[i] = 0.0;
+        if ((x + y) % 2 != odd) continue;
+        int xp = (x + 1) % lx, xm = (x + lx - 1) % lx;
+        int yp = (y + 1) % ly, ym = (y + ly - 1) % ly;
+        cplx acc = 0.0;
+        acc = acc - U[(long)y * lx * 2 + x * 2] * rhs[(long)y * lx + xp];
+        acc = acc + conj(U[(long)y * lx * 2 + xm * 2]) * rhs[(long)y * lx + xm];
+        acc = acc - (eta1 * U[(long)y * lx * 2 + x * 2 + 1]) * rhs[(long)yp * lx + x];
+        acc = acc + (eta1 * conj(U[(long)ym * lx * 2 + x * 2 + 1])) * rhs[(long)ym * lx + x];
+        lhs[i] = 0.5 * acc;
+    }
+}
+
+static int site_even(long i, int lx) { return ((i % lx) + (i / lx)) % 2 == 0; }
+
+/* operators.cpp:566-589 (square_staggered_m2mdeodoe_u1): tmp = D_oe rhs; lhs = D_eo tmp;
+ * lhs = m*m rhs - lhs on even sites (odd sites stay zero).  The stencil form
+ * (operators_stencil.cpp:195-216, apply_square_staggered_m2mdeodoe_stencil) uses
+ * apply_stencil_2d_oe / _eo and shift*shift. */
+static void m2mdeodoe_apply(const orc_op *op, cplx *lhs, const cplx *rhs)
+{
+    const long v = (long)op->lx * op->ly;
+    cplx *tmp = (cplx *)malloc(sizeof(cplx) * v);
+    if (op->kind == ORC_STAGGERED_M2MDEODOE) {
+        staggered_hop_parity(tmp, rhs, CCX(op->links), op->lx, op->ly, 1);
+        staggered_hop_parity(lhs, tmp, CCX(op->links), op->lx, op->ly, 0);
+        for (long i = 0; i < v; i++)
+            if (site_even(i, op->lx)) lhs[i] = (op->mass * op->mass) * rhs[i] - lhs[i];
+    } else {
+        const cplx shift = mk(op->shift[0], op->shift[1]);
+        stencil_apply(op, tmp, rhs, 2);
+        stencil_apply(op, lhs, tmp, 1);
+        for (long i = 0; i < v; i++)
+            if (site_even(i, op->lx)) lhs[i] = (shift * shift) * rhs[i] - lhs[i];
+    }
+    free(tmp);
+}
+
+/* operators.cpp:543-563 (square_staggered_eoprec_prepare) and operators_stencil.cpp:179-193
+ * (apply_square_staggered_eoprec_prepare_stencil): rhs_e = D_eo rhs (odd sites zeroed), then
+ * rhs_e = m rhs - rhs_e on even sites (the stencil form: shift rhs - rhs_e). */
+void orc_eoprec_prepare(const orc_op *op, double *rhs_e_, const double *rhs_)
+{
+    cplx *rhs_e = CX(rhs_e_);
+    const cplx *rhs = CCX(rhs_);
+    const long v = (long)op->lx * op->ly;
+    if (op->kind == ORC_STAGGERED_M2MDEODOE) {
+        staggered_hop_parity(rhs_e, rhs, CCX(op->links), op->lx, op->ly, 0);
+        for (long i = 0; i < v; i++)
+            if (site_even(i, op->lx)) rhs_e[i] = op->mass * rhs[i] - rhs_e[i];
+    } else {
+        const cplx shift = mk(op->shift[0], op->shift[1]);
+        stencil_apply(op, rhs_e, rhs, 1);
+        for (long i = 0; i < v; i++)
+            if (site_even(i, op->lx)) rhs_e[i] = shift * rhs[i] - rhs_e[i];
+    }
+}
+
+/* operators.cpp:592-620 (square_staggered_eoprec_reconstruct) and operators_stencil.cpp:218-236
+ * (apply_square_staggered_eoprec_reconstruct_stencil): lhs_full = D_oe lhs_e; odd sites
+ * become inv_mass (rhs_o - lhs_full) with inv_mass = 1/m (the stencil form: 1/Re(shift)), even
+ * sites copy lhs_e. */
+void orc_eoprec_reconstruct(const orc_op *op, double *lhs_full_, const double *lhs_e_, const double *rhs_o_)
+{
+    cplx *lhs_full = CX(lhs_full_);
+    const cplx *lhs_e = CCX(lhs_e_), *rhs_o = CCX(rhs_o_);
+    const long v = (long)op->lx * op->ly;
+    double inv_mass;
+    if (op->kind == ORC_STAGGERED_M2MDEODOE) {
+        inv_mass = 1.0 / op->mass;
+        staggered_hop_parity(lhs_full, lhs_e, CCX(op->links), op->lx, op->ly, 1);
+    } else {
+        inv_mass = 1.0 / op->shift[0];
+        stencil_apply(op, lhs_full, lhs_e, 2);
+    }
+    for (long i = 0; i < v; i++) {
+        if (!site_even(i, op->lx)) lhs_full[i] = inv_mass * (rhs_o[i] - lhs_full[i]);
+        else lhs_full[i] = lhs_e[i];
+    }
+}
+
 long orc_op_size(const orc_op *op)
 {
     long v = (long)op->lx * op->ly;
-    if (op->kind >= ORC_STENCIL) v *= op->nc;
+    if (op->kind >= ORC_STENCIL && op->kind <= ORC_STENCIL_OE) v *= op->nc;
     return v;
 }
 
@@ -153,6 +243,10 @@ void orc_apply(const orc_op *op, double *lhs, const double *rhs)
     case ORC_STENCIL: stencil_apply(op, CX(lhs), CCX(rhs), 0); break;
     case ORC_STENCIL_EO: stencil_apply(op, CX(lhs), CCX(rhs), 1); break;
     case ORC_STENCIL_OE: stencil_apply(op, CX(lhs), CCX(rhs), 2); break;
+    case ORC_STAGGERED_DEO: staggered_hop_parity(CX(lhs), CCX(rhs), U, op->lx, op->ly, 0); break;
+    case ORC_STAGGERED_DOE: staggered_hop_parity(CX(lhs), CCX(rhs), U, op->lx, op->ly, 1); break;
+    case ORC_STAGGERED_M2MDEODOE:
+    case ORC_STENCIL_M2MDEODOE: m2mdeodoe_apply(op, CX(lhs), CCX(rhs)); break;
     default: break;
     }
 }

@@ -2,8 +2,9 @@
  * oracle.h -- CPU oracle for the 2D U(1) lattice hot path (TEST INFRASTRUCTURE ONLY).
  *
  * This is a plain-C99 restatement of generic-linalg's CPU algorithms for the operators
- * (staggered D, D^dagger, D^dagger D, gauge Laplacian, stencil_2d apply/eo/oe and the
- * staggered stencil builders) and the Krylov solvers that call them (CG, restarted CG,
+ * (staggered D, D^dagger, D^dagger D, gauge Laplacian, stencil_2d apply/eo/oe, the
+ * staggered stencil builders, and the even/odd pieces D_eo, D_oe, m^2 - D_eo D_oe with the
+ * prepare / reconstruct steps) and the Krylov solvers that call them (CG, restarted CG,
  * multishift CG, BiCGstab, restarted BiCGstab, GCR, restarted GCR).  Every function cites
  * the reference file:line it follows.  It exists so that tests, the smoke check and the
  * CPU-baseline leg of the benchmark have something to compare the CUDA path against.
@@ -33,7 +34,11 @@ enum orc_kind {
     ORC_LAPLACE = 3,          /* square_laplace_u1 */
     ORC_STENCIL = 4,          /* apply_stencil_2d (DIR_ALL) */
     ORC_STENCIL_EO = 5,       /* apply_stencil_2d_eo */
-    ORC_STENCIL_OE = 6        /* apply_stencil_2d_oe */
+    ORC_STENCIL_OE = 6,       /* apply_stencil_2d_oe */
+    ORC_STAGGERED_DEO = 7,    /* square_staggered_deo_u1 */
+    ORC_STAGGERED_DOE = 8,    /* square_staggered_doe_u1 */
+    ORC_STAGGERED_M2MDEODOE = 9, /* square_staggered_m2mdeodoe_u1 */
+    ORC_STENCIL_M2MDEODOE = 10   /* apply_square_staggered_m2mdeodoe_stencil */
 };
 
 typedef struct {
@@ -58,6 +63,13 @@ typedef struct {
 /* Operators: lhs is overwritten, rhs is read. */
 void orc_apply(const orc_op *op, double *lhs, const double *rhs);
 long orc_op_size(const orc_op *op); /* number of complex entries of a field */
+
+/* Even/odd preconditioning of the staggered operator, for op->kind ORC_STAGGERED_M2MDEODOE
+ * (the function form: mass and links) or ORC_STENCIL_M2MDEODOE (the stencil form: shift and
+ * hopping).  prepare: rhs_e = m rhs - D_eo rhs on even sites, 0 on odd sites.  reconstruct:
+ * lhs_full = lhs_e on even sites, (rhs_o - D_oe lhs_e) / m on odd sites. */
+void orc_eoprec_prepare(const orc_op *op, double *rhs_e, const double *rhs);
+void orc_eoprec_reconstruct(const orc_op *op, double *lhs_full, const double *lhs_e, const double *rhs_o);
 
 /* Stencil builders (fill hopping[4*V], clover untouched, shift = mass). */
 void orc_staggered_stencil(double *hopping, const double *links, int lx, int ly, int dagger);

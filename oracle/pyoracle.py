@@ -30,6 +30,10 @@ KIND = {
     "stencil": 4,
     "stencil_eo": 5,
     "stencil_oe": 6,
+    "staggered_deo": 7,
+    "staggered_doe": 8,
+    "staggered_m2mdeodoe": 9,
+    "stencil_m2mdeodoe": 10,
 }
 
 _dp = C.POINTER(C.c_double)
@@ -90,7 +94,7 @@ class Operator:
     @property
     def size(self):
         v = self.lx * self.ly
-        return v * self.nc if self.kind >= KIND["stencil"] else v
+        return v * self.nc if KIND["stencil"] <= self.kind <= KIND["stencil_oe"] else v
 
     def shifts6(self):
         return np.array([self.shift.real, self.shift.imag, self.eo_shift.real,
@@ -119,12 +123,27 @@ class Oracle:
         L.orc_cg_m.argtypes = [P(OrcOp), _dp, _dp, C.c_int, C.c_long, C.c_int, C.c_int, C.c_double,
                                _dp, C.c_int, P(OrcInfo), _dp, _dp, C.c_int]
         L.orc_staggered_force.argtypes = [_dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_eoprec_prepare.argtypes = [P(OrcOp), _dp, _dp]
+        L.orc_eoprec_reconstruct.argtypes = [P(OrcOp), _dp, _dp, _dp]
 
     def apply(self, op: Operator, rhs):
         rhs = np.ascontiguousarray(rhs, dtype=np.complex128)
         lhs = np.empty_like(rhs)
         self.lib.orc_apply(C.byref(op.struct), _ptr(lhs), _ptr(rhs))
         return lhs
+
+    def eoprec_prepare(self, op: Operator, rhs):
+        rhs = np.ascontiguousarray(rhs, dtype=np.complex128)
+        out = np.empty_like(rhs)
+        self.lib.orc_eoprec_prepare(C.byref(op.struct), _ptr(out), _ptr(rhs))
+        return out
+
+    def eoprec_reconstruct(self, op: Operator, lhs_e, rhs_o):
+        lhs_e = np.ascontiguousarray(lhs_e, dtype=np.complex128)
+        rhs_o = np.ascontiguousarray(rhs_o, dtype=np.complex128)
+        out = np.empty_like(lhs_e)
+        self.lib.orc_eoprec_reconstruct(C.byref(op.struct), _ptr(out), _ptr(lhs_e), _ptr(rhs_o))
+        return out
 
     def staggered_stencil(self, links, lx, ly, dagger=False):
         links = np.ascontiguousarray(links, dtype=np.complex128)
@@ -198,6 +217,8 @@ class RefOracle:
                                                               cp, _dp, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
         L.ref_cg_m.argtypes = opargs + [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int,
                                         C.c_int, cp, _dp, _dp, C.c_char_p, C.c_int]
+        L.ref_eoprec_prepare.argtypes = opargs + [_dp, _dp]
+        L.ref_eoprec_reconstruct.argtypes = opargs + [_dp, _dp, _dp]
 
     def make_inputs(self, seed, lx, ly, n_src=1, src_len=None):
         links = np.zeros(2 * lx * ly, dtype=np.complex128)
@@ -221,6 +242,21 @@ class RefOracle:
         lhs = np.zeros_like(rhs)
         self.lib.ref_apply(*self._opargs(op), _ptr(lhs), _ptr(rhs))
         return lhs
+
+    def eoprec_prepare(self, op: Operator, rhs):
+        op._s6 = op.shifts6()
+        rhs = np.ascontiguousarray(rhs, dtype=np.complex128)
+        out = np.zeros_like(rhs)
+        self.lib.ref_eoprec_prepare(*self._opargs(op), _ptr(out), _ptr(rhs))
+        return out
+
+    def eoprec_reconstruct(self, op: Operator, lhs_e, rhs_o):
+        op._s6 = op.shifts6()
+        lhs_e = np.ascontiguousarray(lhs_e, dtype=np.complex128)
+        rhs_o = np.ascontiguousarray(rhs_o, dtype=np.complex128)
+        out = np.zeros_like(lhs_e)
+        self.lib.ref_eoprec_reconstruct(*self._opargs(op), _ptr(out), _ptr(lhs_e), _ptr(rhs_o))
+        return out
 
     def staggered_stencil(self, links, lx, ly, mass, dagger=False):
         hop = np.zeros(4 * lx * ly, dtype=np.complex128)

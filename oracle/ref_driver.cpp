@@ -51,7 +51,8 @@ struct RefOp {
 };
 
 // kind: 0 D, 1 D^dagger, 2 D^dagger D, 3 gauge Laplacian, 4 stencil, 5 stencil_eo,
-// 6 stencil_oe (same numbering as oracle.h).
+// 6 stencil_oe, 7 D_eo, 8 D_oe, 9 m^2 - D_eo D_oe, 10 its stencil form (same numbering as
+// oracle.h).
 RefOp *make_op(int kind, int lx, int ly, int nc, double mass, const double *links,
                const double *clover, const double *hopping, const double *two_link,
                const double *shifts6)
@@ -70,6 +71,9 @@ RefOp *make_op(int kind, int lx, int ly, int nc, double mass, const double *link
     case 1: o->fn = square_staggered_dagger_u1; break;
     case 2: o->fn = square_staggered_normal_u1; break;
     case 3: o->fn = square_laplace_u1; break;
+    case 7: o->fn = square_staggered_deo_u1; break;
+    case 8: o->fn = square_staggered_doe_u1; break;
+    case 9: o->fn = square_staggered_m2mdeodoe_u1; break;
     default: {
         int dims[2] = {lx, ly};
         o->lat = new Lattice(2, dims, nc);
@@ -84,7 +88,9 @@ RefOp *make_op(int kind, int lx, int ly, int nc, double mass, const double *link
             o->st->dof_shift = cd(shifts6[4], shifts6[5]);
         }
         o->st->generated = true;
-        o->fn = kind == 4 ? apply_stencil_2d : (kind == 5 ? apply_stencil_2d_eo : apply_stencil_2d_oe);
+        o->fn = kind == 4 ? apply_stencil_2d
+                          : kind == 5 ? apply_stencil_2d_eo
+                          : kind == 6 ? apply_stencil_2d_oe : apply_square_staggered_m2mdeodoe_stencil;
         o->size = (long)lx * ly * nc;
         break;
     }
@@ -185,6 +191,33 @@ void ref_staggered_stencil(int lx, int ly, double mass, const double *links, int
     std::memcpy(hopping_out, st.hopping, sizeof(cd) * (long)lx * ly * 4);
     shift_out[0] = st.shift.real();
     shift_out[1] = st.shift.imag();
+}
+
+// Even/odd preconditioning steps for kind 9 (square_staggered_eoprec_prepare /
+// _reconstruct, operators.cpp:543 / :592) or kind 10 (the stencil forms,
+// operators_stencil.cpp:181 / :220).
+void ref_eoprec_prepare(int kind, int lx, int ly, int nc, double mass, const double *links,
+                        const double *clover, const double *hopping, const double *two_link,
+                        const double *shifts6, double *rhs_e, const double *rhs)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> in((const cd *)rhs, (const cd *)rhs + o->size);
+    if (kind == 9) square_staggered_eoprec_prepare((cd *)rhs_e, in.data(), o->extra);
+    else apply_square_staggered_eoprec_prepare_stencil((cd *)rhs_e, in.data(), o->st);
+    delete o;
+}
+
+void ref_eoprec_reconstruct(int kind, int lx, int ly, int nc, double mass, const double *links,
+                            const double *clover, const double *hopping, const double *two_link,
+                            const double *shifts6, double *lhs_full, const double *lhs_e,
+                            const double *rhs_o)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> e((const cd *)lhs_e, (const cd *)lhs_e + o->size);
+    std::vector<cd> b((const cd *)rhs_o, (const cd *)rhs_o + o->size);
+    if (kind == 9) square_staggered_eoprec_reconstruct((cd *)lhs_full, e.data(), b.data(), o->extra);
+    else apply_square_staggered_eoprec_reconstruct_stencil((cd *)lhs_full, e.data(), b.data(), o->st);
+    delete o;
 }
 
 // solver: 0 CG, 1 BiCGstab, 2 GCR; restart_freq > 0 selects the restarted variant.

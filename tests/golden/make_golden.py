@@ -115,6 +115,33 @@ def main():
         info["cases"][key] = {**d, "resSqmrhs": res.tolist(), "log": log, "shifts": msh,
                               "rfc": rfc, "worst_first": wf, "mass": 0.001}
 
+    # ---- even/odd preconditioning (operators.cpp:455-620, operators_stencil.cpp:179-236)
+    for key in ("l32", "l8", "l12x6"):
+        lx, ly, _ = lat[key]
+        U, b_, b2 = vec[f"{key}_links"], vec[f"{key}_src"], vec[f"{key}_src2"]
+        for kind in ("staggered_deo", "staggered_doe", "staggered_m2mdeodoe"):
+            vec[f"{key}_{kind}"] = R.apply(Op(kind, lx, ly, 0.1, U), b_)
+        eo = Op("staggered_m2mdeodoe", lx, ly, 0.1, U)
+        vec[f"{key}_eo_prepare"] = R.eoprec_prepare(eo, b_)
+        vec[f"{key}_eo_reconstruct"] = R.eoprec_reconstruct(eo, b2, b_)
+    # the stencil form on the 8x8 staggered stencil (shift = mass)
+    lx, ly = 8, 8
+    hop, sh = R.staggered_stencil(vec["l8_links"], lx, ly, 0.1, False)
+    seo = Op("stencil_m2mdeodoe", lx, ly, nc=1, clover=np.zeros(lx * ly, np.complex128), hopping=hop, shift=sh)
+    vec["l8_stencil_m2mdeodoe"] = R.apply(seo, vec["l8_src"])
+    vec["l8_stencil_eo_prepare"] = R.eoprec_prepare(seo, vec["l8_src"])
+    vec["l8_stencil_eo_reconstruct"] = R.eoprec_reconstruct(seo, vec["l8_src2"], vec["l8_src"])
+    # M x = b on the 32x32 system by even/odd preconditioning (tests/staggered_pieces/
+    # staggered_pieces.cpp:331-346): prepare, CG on m^2 - D_eo D_oe, reconstruct
+    lx, ly = 32, 32
+    U, b_ = vec["l32_links"], vec["l32_src"]
+    eo = Op("staggered_m2mdeodoe", lx, ly, 0.1, U)
+    rhs_e = R.eoprec_prepare(eo, b_)
+    xe, d, log = R.solve("cg", eo, rhs_e, max_iter=10000, eps=1e-10, verbosity=1, prefix="[EO] ")
+    vec["l32_eo_cg_even"] = xe
+    vec["l32_eo_solution"] = R.eoprec_reconstruct(eo, xe, b_)
+    info["cases"]["l32_eo_cg"] = {**d, "log": log, "max_iter": 10000, "eps": 1e-10, "mass": 0.1}
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     with open(os.path.join(HERE, "reference_info.json"), "w") as f:
         json.dump(info, f, indent=1, default=lambda o: o.item() if hasattr(o, "item") else str(o))

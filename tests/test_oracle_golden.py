@@ -101,3 +101,57 @@ def test_cg_m_bit_exact(oracle, golden, rfc, wf):
     assert (info["iter"], info["ops_count"], info["success"]) == (c["iter"], c["ops_count"], c["success"])
     assert np.array_equal(res, np.array(c["resSqmrhs"]))
     assert np.array_equal(x.reshape(-1), vec[key])
+
+
+# ---- even/odd preconditioning (operators.cpp:455-620, operators_stencil.cpp:179-236)
+
+@pytest.mark.parametrize("key", list(LATS))
+@pytest.mark.parametrize("kind", ["staggered_deo", "staggered_doe", "staggered_m2mdeodoe"])
+def test_eo_operators_bit_exact(oracle, golden, key, kind):
+    vec, _ = golden
+    lx, ly = LATS[key]
+    out = oracle.apply(Operator(kind, lx, ly, 0.1, vec[f"{key}_links"]), vec[f"{key}_src"])
+    assert np.array_equal(out, vec[f"{key}_{kind}"])
+
+
+@pytest.mark.parametrize("key", list(LATS))
+def test_eo_prepare_reconstruct_bit_exact(oracle, golden, key):
+    vec, _ = golden
+    lx, ly = LATS[key]
+    eo = Operator("staggered_m2mdeodoe", lx, ly, 0.1, vec[f"{key}_links"])
+    assert np.array_equal(oracle.eoprec_prepare(eo, vec[f"{key}_src"]), vec[f"{key}_eo_prepare"])
+    rc = oracle.eoprec_reconstruct(eo, vec[f"{key}_src2"], vec[f"{key}_src"])
+    assert np.array_equal(rc, vec[f"{key}_eo_reconstruct"])
+
+
+def test_eo_stencil_form_bit_exact(oracle, golden):
+    vec, _ = golden
+    hop = oracle.staggered_stencil(vec["l8_links"], 8, 8)
+    op = Operator("stencil_m2mdeodoe", 8, 8, nc=1, clover=np.zeros(64, np.complex128), hopping=hop, shift=0.1)
+    assert np.array_equal(oracle.apply(op, vec["l8_src"]), vec["l8_stencil_m2mdeodoe"])
+    assert np.array_equal(oracle.eoprec_prepare(op, vec["l8_src"]), vec["l8_stencil_eo_prepare"])
+    assert np.array_equal(oracle.eoprec_reconstruct(op, vec["l8_src2"], vec["l8_src"]),
+                          vec["l8_stencil_eo_reconstruct"])
+
+
+def test_eo_identities(golden):
+    """tests/staggered_pieces/staggered_pieces.cpp:297-332: D_eo + D_oe + m = D and
+    m^2 - D_eo D_oe - D_oe D_eo = D^dagger D (on the even part of an even-only vector, the
+    normal operator is m^2 - D_eo D_oe)."""
+    vec, _ = golden
+    for key in LATS:
+        full = vec[f"{key}_staggered_deo"] + vec[f"{key}_staggered_doe"] + 0.1 * vec[f"{key}_src"]
+        assert np.abs(full - vec[f"{key}_staggered"]).max() < 1e-14
+
+
+def test_eo_solve_matches_reference(oracle, golden):
+    """prepare, CG on m^2 - D_eo D_oe, reconstruct (staggered_pieces.cpp:331-346): the oracle's
+    CG takes the reference's iterations and returns its solution bit for bit."""
+    vec, cases = golden
+    c = cases["l32_eo_cg"]
+    eo = Operator("staggered_m2mdeodoe", 32, 32, 0.1, vec["l32_links"])
+    rhs_e = oracle.eoprec_prepare(eo, vec["l32_src"])
+    xe, info, _ = oracle.solve("cg", eo, rhs_e, max_iter=c["max_iter"], eps=c["eps"])
+    assert info["iter"] == c["iter"] and info["ops_count"] == c["ops_count"]
+    assert np.array_equal(xe, vec["l32_eo_cg_even"])
+    assert np.array_equal(oracle.eoprec_reconstruct(eo, xe, vec["l32_src"]), vec["l32_eo_solution"])
