@@ -8,8 +8,12 @@ interface for the path:
   (coarse_stencil.h:33-67);
 * operator callbacks ``square_staggered_u1``, ``square_staggered_dagger_u1``,
   ``square_staggered_normal_u1``, ``square_laplace_u1``, ``apply_stencil_2d``,
-  ``apply_stencil_2d_eo``, ``apply_stencil_2d_oe`` with the reference's
+  ``apply_stencil_2d_eo``, ``apply_stencil_2d_oe`` and the even/odd pieces
+  ``square_staggered_deo_u1``, ``square_staggered_doe_u1``, ``square_staggered_m2mdeodoe_u1``,
+  ``apply_square_staggered_m2mdeodoe_stencil`` with the reference's
   ``matrix_vector(lhs, rhs, extra)`` convention;
+* the even/odd steps ``square_staggered_eoprec_prepare`` / ``_reconstruct`` and their stencil
+  forms (operators.cpp:543-620, operators_stencil.cpp:179-236);
 * solvers ``minv_vector_cg``, ``minv_vector_cg_restart``, ``minv_vector_cg_m``,
   ``minv_vector_bicgstab``, ``minv_vector_bicgstab_restart``, ``minv_vector_gcr``,
   ``minv_vector_gcr_restart`` with the reference's argument order, returning
@@ -40,6 +44,10 @@ __all__ = [
     "square_staggered_u1", "square_staggered_dagger_u1", "square_staggered_normal_u1",
     "square_laplace_u1", "apply_stencil_2d", "apply_stencil_2d_eo", "apply_stencil_2d_oe",
     "get_square_staggered_u1_stencil", "get_square_staggered_dagger_u1_stencil",
+    "square_staggered_deo_u1", "square_staggered_doe_u1", "square_staggered_m2mdeodoe_u1",
+    "apply_square_staggered_m2mdeodoe_stencil", "square_staggered_eoprec_prepare",
+    "square_staggered_eoprec_reconstruct", "apply_square_staggered_eoprec_prepare_stencil",
+    "apply_square_staggered_eoprec_reconstruct_stencil",
     "minv_vector_cg", "minv_vector_cg_restart", "minv_vector_cg_m", "minv_vector_bicgstab",
     "minv_vector_bicgstab_restart", "minv_vector_gcr", "minv_vector_gcr_restart",
     "Generator", "dot", "norm2sq", "staggered_force", "staggered_action_grad",
@@ -51,6 +59,8 @@ VERB_PASS_THROUGH, VERB_NONE, VERB_SUMMARY, VERB_RESTART_DETAIL, VERB_DETAIL = -
 
 KIND_STAGGERED, KIND_STAGGERED_DAGGER, KIND_STAGGERED_NORMAL, KIND_LAPLACE = 0, 1, 2, 3
 KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE = 4, 5, 6
+KIND_STAGGERED_DEO, KIND_STAGGERED_DOE, KIND_STAGGERED_M2MDEODOE, KIND_STENCIL_M2MDEODOE = 7, 8, 9, 10
+_STENCIL_KINDS = (KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE, KIND_STENCIL_M2MDEODOE)
 
 
 class UnsupportedOperator(GlinalgError):
@@ -177,7 +187,7 @@ class Operator:
 def _op_for(kind, extra):
     if isinstance(extra, Operator):
         return extra, False
-    if kind in (KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE):
+    if kind in _STENCIL_KINDS:
         if not isinstance(extra, Stencil2D):
             raise UnsupportedOperator("stencil callbacks need a Stencil2D extra_info")
         return Operator(kind, extra.lx, extra.ly, nc=extra.nc, clover=extra.clover,
@@ -209,6 +219,57 @@ square_laplace_u1 = _callback(KIND_LAPLACE, "square_laplace_u1", "operators.cpp:
 apply_stencil_2d = _callback(KIND_STENCIL, "apply_stencil_2d", "coarse_stencil.cpp:12")
 apply_stencil_2d_eo = _callback(KIND_STENCIL_EO, "apply_stencil_2d_eo", "coarse_stencil.cpp:395")
 apply_stencil_2d_oe = _callback(KIND_STENCIL_OE, "apply_stencil_2d_oe", "coarse_stencil.cpp:560")
+square_staggered_deo_u1 = _callback(KIND_STAGGERED_DEO, "square_staggered_deo_u1", "operators.cpp:455")
+square_staggered_doe_u1 = _callback(KIND_STAGGERED_DOE, "square_staggered_doe_u1", "operators.cpp:499")
+square_staggered_m2mdeodoe_u1 = _callback(KIND_STAGGERED_M2MDEODOE, "square_staggered_m2mdeodoe_u1",
+                                          "operators.cpp:566")
+apply_square_staggered_m2mdeodoe_stencil = _callback(KIND_STENCIL_M2MDEODOE, "apply_square_staggered_m2mdeodoe_stencil",
+                                                     "operators_stencil.cpp:197")
+
+
+def _eo_step(kind, out, a, b, extra):
+    op, temp = _op_for(kind, extra)
+    try:
+        if op.kind not in (KIND_STAGGERED_M2MDEODOE, KIND_STENCIL_M2MDEODOE):
+            raise UnsupportedOperator("even/odd steps need an m^2 - D_eo D_oe operator")
+        op_, on, odev = _field_ptr(out, writable=True)
+        ap, an, adev = _field_ptr(a)
+        n = op.size
+        if on != n or an != n or adev != odev:
+            raise ValueError("field sizes/devices do not match the operator")
+        flags = GLINALG_PTR_DEVICE if odev else 0
+        if b is None:
+            _capi.check(lib().glinalg_eoprec_prepare(op.handle, _dptr(op_), _dptr(ap), flags), "eoprec_prepare")
+        else:
+            bp, bn, bdev = _field_ptr(b)
+            if bn != n or bdev != odev:
+                raise ValueError("field sizes/devices do not match the operator")
+            _capi.check(lib().glinalg_eoprec_reconstruct(op.handle, _dptr(op_), _dptr(ap), _dptr(bp), flags),
+                        "eoprec_reconstruct")
+    finally:
+        if temp:
+            op.close()
+    return out
+
+
+def square_staggered_eoprec_prepare(rhs_e, rhs_orig, extra_data):
+    """rhs_e = m rhs - D_eo rhs on even sites, 0 on odd sites (operators.cpp:543)."""
+    return _eo_step(KIND_STAGGERED_M2MDEODOE, rhs_e, rhs_orig, None, extra_data)
+
+
+def square_staggered_eoprec_reconstruct(lhs_full, lhs_e, rhs_o, extra_data):
+    """lhs_full = lhs_e on even sites, (rhs_o - D_oe lhs_e) / m on odd sites (operators.cpp:592)."""
+    return _eo_step(KIND_STAGGERED_M2MDEODOE, lhs_full, lhs_e, rhs_o, extra_data)
+
+
+def apply_square_staggered_eoprec_prepare_stencil(rhs_e, rhs_orig, stenc):
+    """The stencil form of square_staggered_eoprec_prepare (operators_stencil.cpp:181)."""
+    return _eo_step(KIND_STENCIL_M2MDEODOE, rhs_e, rhs_orig, None, stenc)
+
+
+def apply_square_staggered_eoprec_reconstruct_stencil(lhs_full, lhs_e, rhs_o, stenc):
+    """The stencil form of square_staggered_eoprec_reconstruct (operators_stencil.cpp:220)."""
+    return _eo_step(KIND_STENCIL_M2MDEODOE, lhs_full, lhs_e, rhs_o, stenc)
 
 
 def _stencil_builder(dagger):

@@ -62,6 +62,8 @@ def _prototypes():
         "glinalg_profile_mixed_kernels": (st, [vp, i, i, _dp, _dp]),
         "glinalg_tuned_tile": (i, [vp, i]),
         "glinalg_tuned_persist": (i, [vp, i]),
+        "glinalg_eoprec_prepare": (st, [vp, _dp, _dp, i]),
+        "glinalg_eoprec_reconstruct": (st, [vp, _dp, _dp, _dp, i]),
         "glinalg_profile_persist_kernel": (st, [vp, i, i, i, _dp, _dp, P(i)]),
         "glinalg_staggered_normal_apply_noalloc": (st, [_dp, d, i, i, _dp, _dp, vp]),
         "glinalg_operator_create": (st, [P(OpDesc), P(vp)]),

@@ -76,7 +76,9 @@ extern "C" glinalg_status glinalg_cg_batch(const glinalg_operator *ops, int n_sy
 {
     if (!ops || !phi || !phi0 || !infos || n_sys <= 0) return GLINALG_ERROR_INVALID_VALUE;
     for (int q = 0; q < n_sys; q++)
-        if (!ops[q] || !phi[q] || !phi0[q] || !is_hermitian(ops[q]->kind)) return GLINALG_ERROR_INVALID_VALUE;
+        if (!ops[q] || !phi[q] || !phi0[q] ||
+            !(ops[q]->kind == GLINALG_OP_STAGGERED_NORMAL || ops[q]->kind == GLINALG_OP_LAPLACE))
+            return GLINALG_ERROR_INVALID_VALUE;
     GL_TRY(ensure_device());
     const bool dev = params && (params->flags & GLINALG_PTR_DEVICE);
     const int prec = params ? params->precision : GLINALG_PREC_DOUBLE;

@@ -1033,12 +1033,46 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     return GLINALG_SUCCESS;
 }
 
+// Mixed-precision CG on m^2 - D_eo D_oe (square_staggered_m2mdeodoe_u1, operators.cpp:566).  On
+// even-only fields this operator equals D^dagger D, so the staggered normal solver runs on the
+// even parts of b and of the guess.  Only x's even sites are written: the odd sites keep their
+// input values, as in the reference's CG, whose operator zeroes them (b's odd sites must be
+// zero, as square_staggered_eoprec_prepare makes them; they are not read).
+static glinalg_status cg_mixed_even(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                                    double eps, int precision, double delta, double sigma, const Verb &verb,
+                                    glinalg_info *info, cudaStream_t st)
+{
+    Scratch sc(st);
+    double2 *be, *xe;
+    GL_TRY(sc.alloc(&be, op->size));
+    GL_TRY(sc.alloc(&xe, op->size));
+    GL_TRY(launch_even_part(op, be, b, st));
+    GL_TRY(launch_even_part(op, xe, x, st));
+    // D^dagger D on the same links and mass; the view owns no device memory
+    glinalg_operator_s view;
+    view.kind = GLINALG_OP_STAGGERED_NORMAL;
+    view.lx = op->lx;
+    view.ly = op->ly;
+    view.mass = op->mass;
+    view.vol = op->vol;
+    view.size = op->size;
+    view.device = op->device;
+    view.U = op->U;
+    const glinalg_status s = cg_mixed(&view, xe, be, max_iter, eps, precision, delta, sigma, verb, info, st);
+    view.U = nullptr;
+    GL_TRY(s);
+    return launch_even_into(op, x, xe, st);
+}
+
 glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
                         double eps, int precision, double delta, double sigma, const Verb &verb,
                         glinalg_info *info, cudaStream_t st)
 {
+    if (op->kind == GLINALG_OP_STAGGERED_M2MDEODOE)
+        return cg_mixed_even(op, x, b, max_iter, eps, precision, delta, sigma, verb, info, st);
     if (!(op->kind == GLINALG_OP_STAGGERED_NORMAL || op->kind == GLINALG_OP_LAPLACE)) {
-        set_last_error("mixed-precision CG needs the staggered normal operator or the gauge Laplacian");
+        set_last_error("mixed-precision CG needs the staggered normal operator, m^2 - D_eo D_oe or the gauge "
+                       "Laplacian");
         return GLINALG_ERROR_UNSUPPORTED_OP;
     }
     // default reliable-update trigger: FP32 iterates stay accurate over two orders of magnitude

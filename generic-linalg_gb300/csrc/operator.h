@@ -33,8 +33,9 @@ struct glinalg_operator_s {
 namespace glinalg {
 
 bool is_staggered(int kind);
-bool is_stencil(int kind);
-bool is_hermitian(int kind);  // kinds CG may drive: D^dagger D and the gauge Laplacian
+bool is_stencil(int kind);     // kinds described by a stencil_2d (clover, hopping, shifts)
+bool is_hermitian(int kind);   // D^dagger D, the gauge Laplacian, m^2 - D_eo D_oe
+bool needs_tmp(int kind);      // two-pass kinds: launch_apply needs a scratch field
 
 // lhs = A rhs on `stream` (device pointers).  tmp: a scratch field of op->size entries for
 // the normal operator (may be null for other kinds).  done: optional device flag; when it
@@ -49,6 +50,23 @@ glinalg_status launch_apply_sigma(const glinalg_operator_s *op, double2 *lhs, co
 glinalg_status launch_apply_shifted(const glinalg_operator_s *op, double2 *lhs,
                                     const double2 *rhs, double2 *tmp, double sigma,
                                     cudaStream_t stream);
+
+// apply_stencil_2d (parity 0), _eo (1) or _oe (2) of a stencil-described operator.
+glinalg_status launch_stencil_parity(const glinalg_operator_s *op, double2 *out, const double2 *in, int parity,
+                                     const int *done, cudaStream_t stream);
+
+// Even/odd preconditioning (eoprec.cu): D_eo, D_oe and m^2 - D_eo D_oe applied; the prepare and
+// reconstruct steps; the even part of a field; x = x_e on even sites.
+glinalg_status launch_eo_apply(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs, double2 *tmp,
+                               const int *done, cudaStream_t stream);
+glinalg_status launch_eo_prepare(const glinalg_operator_s *op, double2 *rhs_e, const double2 *rhs,
+                                 cudaStream_t stream);
+glinalg_status launch_eo_reconstruct(const glinalg_operator_s *op, double2 *full, const double2 *lhs_e,
+                                     const double2 *rhs_o, cudaStream_t stream);
+glinalg_status launch_even_part(const glinalg_operator_s *op, double2 *out, const double2 *in,
+                                cudaStream_t stream);
+glinalg_status launch_even_into(const glinalg_operator_s *op, double2 *x, const double2 *xe,
+                                cudaStream_t stream);
 
 // Staggered-only pieces (used by the force and by the fused solver kernels).
 glinalg_status launch_staggered(const glinalg_operator_s *op, double2 *out, const double2 *in,

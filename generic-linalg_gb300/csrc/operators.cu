@@ -100,15 +100,27 @@ bool is_staggered(int k)
     return k == GLINALG_OP_STAGGERED || k == GLINALG_OP_STAGGERED_DAGGER ||
            k == GLINALG_OP_STAGGERED_NORMAL;
 }
-bool is_stencil(int k) { return k >= GLINALG_OP_STENCIL && k <= GLINALG_OP_STENCIL_OE; }
-bool is_hermitian(int k) { return k == GLINALG_OP_STAGGERED_NORMAL || k == GLINALG_OP_LAPLACE; }
+bool is_stencil(int k)
+{
+    return (k >= GLINALG_OP_STENCIL && k <= GLINALG_OP_STENCIL_OE) || k == GLINALG_OP_STENCIL_M2MDEODOE;
+}
+bool is_hermitian(int k)
+{
+    return k == GLINALG_OP_STAGGERED_NORMAL || k == GLINALG_OP_LAPLACE || k == GLINALG_OP_STAGGERED_M2MDEODOE ||
+           k == GLINALG_OP_STENCIL_M2MDEODOE;
+}
+bool needs_tmp(int k)
+{
+    return k == GLINALG_OP_STAGGERED_NORMAL || k == GLINALG_OP_STAGGERED_M2MDEODOE ||
+           k == GLINALG_OP_STENCIL_M2MDEODOE;
+}
 
 double apply_bytes(const glinalg_operator_s *op)
 {
     // per output site: in + out + links (2 per site) as stored; the normal operator is two
     // passes.  Stencil: clover + 4 hops (+8 two-link) Nc x Nc per site plus in/out.
     const double w = 16.0;
-    if (op->kind == GLINALG_OP_STAGGERED_NORMAL) return 8.0 * w * op->vol;
+    if (needs_tmp(op->kind)) return 8.0 * w * op->vol;  // two passes (even/odd: zeros at one parity)
     if (is_stencil(op->kind)) {
         double nc = op->nc;
         double terms = 1 + 4 + (op->two_link ? 8 : 0);
@@ -276,34 +288,37 @@ glinalg_status launch_apply(const glinalg_operator_s *op, double2 *lhs, const do
         return GLINALG_SUCCESS;
     case GLINALG_OP_STENCIL:
     case GLINALG_OP_STENCIL_EO:
-    case GLINALG_OP_STENCIL_OE: {
-        const int parity = op->kind - GLINALG_OP_STENCIL;
-        const int g = grid_for(op->size, nt);
-        if (op->nc == 1)
-            k_stencil<1><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link,
-                                           op->shift, op->eo_shift, op->dof_shift, op->lx,
-                                           op->ly, 1, parity, done);
-        else if (op->nc == 2)
-            k_stencil<2><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link,
-                                           op->shift, op->eo_shift, op->dof_shift, op->lx,
-                                           op->ly, 2, parity, done);
-        else if (op->nc == 4)
-            k_stencil<4><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link,
-                                           op->shift, op->eo_shift, op->dof_shift, op->lx,
-                                           op->ly, 4, parity, done);
-        else if (op->nc == 8)
-            k_stencil<8><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link,
-                                           op->shift, op->eo_shift, op->dof_shift, op->lx,
-                                           op->ly, 8, parity, done);
-        else
-            k_stencil<0><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link,
-                                           op->shift, op->eo_shift, op->dof_shift, op->lx,
-                                           op->ly, op->nc, parity, done);
-        GL_CUDA(cudaGetLastError());
-        return GLINALG_SUCCESS;
-    }
+    case GLINALG_OP_STENCIL_OE: return launch_stencil_parity(op, lhs, rhs, op->kind - GLINALG_OP_STENCIL, done, st);
+    case GLINALG_OP_STAGGERED_DEO:
+    case GLINALG_OP_STAGGERED_DOE:
+    case GLINALG_OP_STAGGERED_M2MDEODOE:
+    case GLINALG_OP_STENCIL_M2MDEODOE: return launch_eo_apply(op, lhs, rhs, tmp, done, st);
     default: return GLINALG_ERROR_UNSUPPORTED_OP;
     }
+}
+
+glinalg_status launch_stencil_parity(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs, int parity,
+                                     const int *done, cudaStream_t st)
+{
+    const int nt = 256;
+    const int g = grid_for(op->size, nt);
+    if (op->nc == 1)
+        k_stencil<1><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
+                                       op->dof_shift, op->lx, op->ly, 1, parity, done);
+    else if (op->nc == 2)
+        k_stencil<2><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
+                                       op->dof_shift, op->lx, op->ly, 2, parity, done);
+    else if (op->nc == 4)
+        k_stencil<4><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
+                                       op->dof_shift, op->lx, op->ly, 4, parity, done);
+    else if (op->nc == 8)
+        k_stencil<8><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
+                                       op->dof_shift, op->lx, op->ly, 8, parity, done);
+    else
+        k_stencil<0><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
+                                       op->dof_shift, op->lx, op->ly, op->nc, parity, done);
+    GL_CUDA(cudaGetLastError());
+    return GLINALG_SUCCESS;
 }
 
 glinalg_status launch_apply_sigma(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs,
@@ -359,10 +374,14 @@ extern "C" glinalg_status glinalg_operator_create(const glinalg_op_desc *d, glin
     if (!d || !out) return GLINALG_ERROR_INVALID_VALUE;
     *out = nullptr;
     if (d->lx <= 0 || d->ly <= 0) return GLINALG_ERROR_INVALID_VALUE;
-    if (d->kind < GLINALG_OP_STAGGERED || d->kind > GLINALG_OP_STENCIL_OE)
+    if (d->kind < GLINALG_OP_STAGGERED || d->kind > GLINALG_OP_STENCIL_M2MDEODOE)
         return GLINALG_ERROR_UNSUPPORTED_OP;
     const bool sten = is_stencil(d->kind);
     if (sten && (d->nc <= 0 || !d->clover || !d->hopping)) return GLINALG_ERROR_INVALID_VALUE;
+    if (d->kind == GLINALG_OP_STENCIL_M2MDEODOE && d->nc != 1) {
+        set_last_error("the stencil form of m^2 - D_eo D_oe needs nc = 1 (a staggered stencil)");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
     if (!sten && !d->links) return GLINALG_ERROR_INVALID_VALUE;
     GL_TRY(ensure_device());
     auto *op = new glinalg_operator_s();
@@ -447,7 +466,7 @@ extern "C" glinalg_status glinalg_operator_apply(glinalg_operator op, double *lh
         d_in = (double2 *)rhs;
         d_out = (double2 *)lhs;
     }
-    if (e == cudaSuccess && op->kind == GLINALG_OP_STAGGERED_NORMAL)
+    if (e == cudaSuccess && needs_tmp(op->kind))
         e = cudaMallocAsync((void **)&d_tmp, bytes, st);
     if (e != cudaSuccess) fail(e);
     if (s == GLINALG_SUCCESS) s = launch_apply(op, d_out, d_in, d_tmp, nullptr, st);

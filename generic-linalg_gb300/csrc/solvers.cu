@@ -125,7 +125,7 @@ glinalg_status cg_fp64(const glinalg_operator_s *op, double2 *x, const double2 *
     GL_TRY(sc.alloc(&r, n));
     GL_TRY(sc.alloc(&p, n));
     GL_TRY(sc.alloc(&Ap, n));
-    if (op->kind == GLINALG_OP_STAGGERED_NORMAL) GL_TRY(sc.alloc(&tmp, n));
+    if (needs_tmp(op->kind)) GL_TRY(sc.alloc(&tmp, n));
     GL_TRY(sc.alloc(&partials, 2 * (size_t)nb));
     GL_TRY(sc.alloc(&hist, hist_cap ? hist_cap : 1));
     GL_TRY(sc.alloc(&s, 1));
@@ -334,7 +334,7 @@ glinalg_status bicgstab_fp64(const glinalg_operator_s *op, double2 *x, const dou
     GL_TRY(sc.alloc(&Ap, n));
     GL_TRY(sc.alloc(&sv, n));
     GL_TRY(sc.alloc(&As, n));
-    if (op->kind == GLINALG_OP_STAGGERED_NORMAL) GL_TRY(sc.alloc(&tmp, n));
+    if (needs_tmp(op->kind)) GL_TRY(sc.alloc(&tmp, n));
     GL_TRY(sc.alloc(&partials, 3 * (size_t)nb));
     GL_TRY(sc.alloc(&hist, hist_cap ? hist_cap : 1));
     GL_TRY(sc.alloc(&s, 1));
@@ -534,7 +534,7 @@ glinalg_status gcr_fp64(const glinalg_operator_s *op, double2 *phi, const double
     GL_TRY(sc.alloc(&x, n));
     GL_TRY(sc.alloc(&r, n));
     GL_TRY(sc.alloc(&Ar, n));
-    if (op->kind == GLINALG_OP_STAGGERED_NORMAL) GL_TRY(sc.alloc(&tmp, n));
+    if (needs_tmp(op->kind)) GL_TRY(sc.alloc(&tmp, n));
     GL_TRY(sc.alloc(&partials, 2 * kGcrDots * (size_t)nb));
     GL_TRY(sc.alloc(&hist, hist_cap ? hist_cap : 1));
     GL_TRY(sc.alloc(&apnorm, cap));
@@ -790,7 +790,7 @@ glinalg_status cg_m_fp64(const glinalg_operator_s *op, double2 *const *X_host, c
     GL_TRY(sc.alloc(&r, n));
     GL_TRY(sc.alloc(&p, n));
     GL_TRY(sc.alloc(&Ap, n));
-    if (op->kind == GLINALG_OP_STAGGERED_NORMAL) GL_TRY(sc.alloc(&tmp, n));
+    if (needs_tmp(op->kind)) GL_TRY(sc.alloc(&tmp, n));
     GL_TRY(sc.alloc(&partials, 2 * (size_t)nb));
     GL_TRY(sc.alloc(&hist, hist_cap ? hist_cap : 1));
     GL_TRY(sc.alloc(&s, 1));

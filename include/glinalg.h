@@ -62,7 +62,13 @@ typedef enum glinalg_op_kind {
     GLINALG_OP_LAPLACE = 3,           /* square_laplace_u1            operators.cpp:73  */
     GLINALG_OP_STENCIL = 4,           /* apply_stencil_2d             coarse_stencil.cpp:12  */
     GLINALG_OP_STENCIL_EO = 5,        /* apply_stencil_2d_eo          coarse_stencil.cpp:395 */
-    GLINALG_OP_STENCIL_OE = 6         /* apply_stencil_2d_oe          coarse_stencil.cpp:560 */
+    GLINALG_OP_STENCIL_OE = 6,        /* apply_stencil_2d_oe          coarse_stencil.cpp:560 */
+    /* even/odd pieces of the staggered operator (staggered-kind descriptor: links, mass) */
+    GLINALG_OP_STAGGERED_DEO = 7,     /* square_staggered_deo_u1      operators.cpp:455 */
+    GLINALG_OP_STAGGERED_DOE = 8,     /* square_staggered_doe_u1      operators.cpp:499 */
+    GLINALG_OP_STAGGERED_M2MDEODOE = 9, /* square_staggered_m2mdeodoe_u1 operators.cpp:566 */
+    /* the stencil form of m^2 - D_eo D_oe (stencil descriptor, nc = 1, shift = mass) */
+    GLINALG_OP_STENCIL_M2MDEODOE = 10 /* apply_square_staggered_m2mdeodoe_stencil operators_stencil.cpp:197 */
 } glinalg_op_kind;
 
 /* Pointer-location flags. */
@@ -157,6 +163,17 @@ long glinalg_operator_size(glinalg_operator op);
 /* lhs = A rhs, the operator callback of the reference (lhs overwritten, rhs untouched). */
 glinalg_status glinalg_operator_apply(glinalg_operator op, double *lhs, const double *rhs,
                                       int flags);
+
+/* Even/odd preconditioning of M x = b (M = m + D_stag).  op: GLINALG_OP_STAGGERED_M2MDEODOE
+ * (replacing square_staggered_eoprec_prepare / _reconstruct, operators.cpp:543 / :592) or
+ * GLINALG_OP_STENCIL_M2MDEODOE (apply_square_staggered_eoprec_prepare_stencil / _reconstruct_
+ * stencil, operators_stencil.cpp:181 / :220).  prepare: rhs_e = m rhs - D_eo rhs on even sites,
+ * 0 on odd sites.  reconstruct: lhs_full = lhs_e on even sites, (rhs_o - D_oe lhs_e) / m on
+ * odd sites (m: the mass, or Re(shift) for the stencil form).  Fields have op's size;
+ * GLINALG_PTR_DEVICE in flags marks device pointers. */
+glinalg_status glinalg_eoprec_prepare(glinalg_operator op, double *rhs_e, const double *rhs, int flags);
+glinalg_status glinalg_eoprec_reconstruct(glinalg_operator op, double *lhs_full, const double *lhs_e,
+                                          const double *rhs_o, int flags);
 
 /* get_square_staggered_u1_stencil / get_square_staggered_dagger_u1_stencil
  * (operators_stencil.cpp:14-63, :120-169): fills hopping_out (4*lx*ly complex) with the
