@@ -697,3 +697,730 @@ void orc_staggered_force(const double *links, double mass, int lx, int ly, const
         out[2 * i + 1] = -eta1 * cimag(fy);
     }
 }
+
+/* ================================================================ sibling Krylov solvers */
+
+/* ---------------------------------------------------------------- CR */
+
+/* generic_cr.cpp:198-323 (complex minv_vector_cr): conjugate residual, A Hermitian. */
+void orc_cr(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+            double eps, orc_info *info, double *hist, int hist_cap)
+{
+    const cplx *phi0 = CCX(phi0_);
+    cplx *x = (cplx *)calloc(size, sizeof(cplx));
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ar = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta;
+    double rsq, bsqrt, truersq, Apsq;
+    int k, ops = 0;
+    long i;
+
+    memcpy(x, phi_, sizeof(cplx) * size);
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)p, (const double *)x); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
+    memcpy(p, r, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    memcpy(Ar, Ap, sizeof(cplx) * size);
+    Apsq = cnorm2(Ap, size);
+
+    for (k = 0; k < max_iter; k++) {
+        alpha = cdivr(cdot(Ap, r, size), Apsq);
+        for (i = 0; i < size; i++) {
+            x[i] = x[i] + alpha * p[i];
+            r[i] = r[i] - alpha * Ap[i];
+        }
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+        if (sqrt(rsq) < eps * bsqrt || k == max_iter - 1) break;
+        orc_apply(op, (double *)Ar, (const double *)r); ops++;
+        beta = cdivr(-cdot(Ap, Ar, size), Apsq);
+        for (i = 0; i < size; i++) {
+            p[i] = r[i] + beta * p[i];
+            Ap[i] = Ar[i] + beta * Ap[i];
+        }
+        Apsq = cnorm2(Ap, size);
+    }
+    /* the reference tests k == max_iter here (generic_cr.cpp:287), not max_iter - 1 */
+    info->success = (k == max_iter) ? 0 : 1;
+    k++;
+    orc_apply(op, (double *)p, (const double *)x); ops++;
+    truersq = cdiffnorm2(p, phi0, size);
+    memcpy(phi_, x, sizeof(cplx) * size);
+    free(x); free(r); free(Ar); free(p); free(Ap);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "CR");
+}
+
+/* generic_cr.cpp:326-366 */
+void orc_cr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                    double eps, int restart_freq, orc_info *info)
+{
+    restart_driver(orc_cr, "CR", op, phi, phi0, size, max_iter, eps, restart_freq, info);
+}
+
+/* ---------------------------------------------------------------- MinRes */
+
+/* generic_minres.cpp (complex minv_vector_minres with omega, the "MR_<omega>" solver):
+ * x += omega alpha r, r -= omega alpha A r with alpha = <Ar, r> / |Ar|^2. */
+void orc_minres(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+                double eps, double omega, orc_info *info, double *hist, int hist_cap)
+{
+    const cplx *phi0 = CCX(phi0_);
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *x = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha;
+    double rsq, truersq, bsqrt;
+    int k, ops = 0;
+    long i;
+
+    memcpy(x, phi_, sizeof(cplx) * size);
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)p, phi_); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
+    for (k = 0; k < max_iter; k++) {
+        orc_apply(op, (double *)p, (const double *)r); ops++;
+        alpha = cdivr(cdot(p, r, size), cnorm2(p, size));
+        alpha = alpha * omega;
+        for (i = 0; i < size; i++) {
+            x[i] = x[i] + alpha * r[i];
+            r[i] = r[i] - alpha * p[i];
+        }
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+        if (sqrt(rsq) < eps * bsqrt) break;
+    }
+    info->success = (k == max_iter) ? 0 : 1;
+    orc_apply(op, (double *)p, (const double *)x); ops++;
+    truersq = cdiffnorm2(p, phi0, size);
+    memcpy(phi_, x, sizeof(cplx) * size);
+    free(p); free(r); free(x);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "Minimum Residual (MinRes)");
+}
+
+/* ---------------------------------------------------------------- CR-M */
+
+/* generic_cr_m.cpp:312-622 (complex minv_vector_cr_m): multishift conjugate residual.  The
+ * shift bookkeeping (retire, swap, restore) is the one of CG-M. */
+void orc_cr_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shift, long size,
+              int resid_freq_check, int max_iter, double eps, const double *shifts_in,
+              int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap)
+{
+    const cplx *phi0 = CCX(phi0_);
+    cplx **phi = (cplx **)malloc(sizeof(cplx *) * n_shift);
+    cplx **p_s = (cplx **)malloc(sizeof(cplx *) * n_shift);
+    cplx *alpha_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *beta_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *zeta_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *zeta_s_prev = (cplx *)malloc(sizeof(cplx) * n_shift);
+    double *shifts = (double *)malloc(sizeof(double) * n_shift);
+    int *mapping = (int *)malloc(sizeof(int) * n_shift);
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ar = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta, beta_prev, tmp;
+    double rsq, bsqrt, Apsq;
+    int k, n, n_shift_rem = n_shift, ops = 0;
+    long i;
+
+    for (n = 0; n < n_shift; n++) {
+        phi[n] = CX(phi_all) + (long)n * size;
+        p_s[n] = (cplx *)malloc(sizeof(cplx) * size);
+        mapping[n] = n;
+        shifts[n] = shifts_in[n];
+        beta_s[n] = zeta_s[n] = zeta_s_prev[n] = 1.0;
+        alpha_s[n] = 0.0;
+    }
+    beta = 1.0;
+    alpha = 0.0;
+    bsqrt = sqrt(cnorm2(phi0, size));
+    for (n = 0; n < n_shift; n++) {
+        memcpy(p_s[n], phi0, sizeof(cplx) * size);
+        memset(phi[n], 0, sizeof(cplx) * size);
+    }
+    memcpy(p, phi0, sizeof(cplx) * size);
+    memcpy(r, phi0, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    memcpy(Ar, Ap, sizeof(cplx) * size);
+    Apsq = cnorm2(Ap, size);
+    rsq = cnorm2(r, size);
+
+    for (k = 0; k < max_iter; k++) {
+        beta_prev = beta;
+        beta = cdivr(-cdot(Ap, r, size), Apsq);
+        for (n = 0; n < n_shift_rem; n++) {
+            tmp = zeta_s[n];
+            zeta_s[n] = (zeta_s[n] * zeta_s_prev[n] * beta_prev) /
+                        (beta * alpha * (zeta_s_prev[n] - zeta_s[n]) +
+                         zeta_s_prev[n] * beta_prev * (1.0 - shifts[n] * beta));
+            zeta_s_prev[n] = tmp;
+            beta_s[n] = beta * zeta_s[n] / zeta_s_prev[n];
+            for (i = 0; i < size; i++) phi[n][i] = phi[n][i] - beta_s[n] * p_s[n][i];
+        }
+        for (i = 0; i < size; i++) r[i] = r[i] + beta * Ap[i];
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+
+        if (k % resid_freq_check == 0) {
+            for (n = 0; n < n_shift_rem; n++) {
+                if (cabs(zeta_s[n]) * sqrt(rsq) < eps * bsqrt) {
+                    n_shift_rem--;
+                    if (n_shift_rem != n) {
+                        int ti = mapping[n_shift_rem]; mapping[n_shift_rem] = mapping[n]; mapping[n] = ti;
+                        cplx *tp = phi[n_shift_rem]; phi[n_shift_rem] = phi[n]; phi[n] = tp;
+                        tp = p_s[n_shift_rem]; p_s[n_shift_rem] = p_s[n]; p_s[n] = tp;
+                        cplx tc;
+                        tc = alpha_s[n_shift_rem]; alpha_s[n_shift_rem] = alpha_s[n]; alpha_s[n] = tc;
+                        tc = beta_s[n_shift_rem]; beta_s[n_shift_rem] = beta_s[n]; beta_s[n] = tc;
+                        tc = zeta_s[n_shift_rem]; zeta_s[n_shift_rem] = zeta_s[n]; zeta_s[n] = tc;
+                        tc = zeta_s_prev[n_shift_rem]; zeta_s_prev[n_shift_rem] = zeta_s_prev[n]; zeta_s_prev[n] = tc;
+                        double td = shifts[n_shift_rem]; shifts[n_shift_rem] = shifts[n]; shifts[n] = td;
+                        n--;
+                    }
+                }
+            }
+        }
+        if ((worst_first && cabs(zeta_s[0]) * sqrt(rsq) < eps * bsqrt) || n_shift_rem == 0 ||
+            k == max_iter - 1)
+            break;
+
+        orc_apply(op, (double *)Ar, (const double *)r); ops++;
+        alpha = cdivr(-cdot(Ap, Ar, size), Apsq);
+        for (n = 0; n < n_shift_rem; n++) {
+            alpha_s[n] = alpha * zeta_s[n] * beta_s[n] / (zeta_s_prev[n] * beta);
+            for (i = 0; i < size; i++) p_s[n][i] = zeta_s[n] * r[i] + alpha_s[n] * p_s[n][i];
+        }
+        for (i = 0; i < size; i++) {
+            p[i] = r[i] + alpha * p[i];
+            Ap[i] = Ar[i] + alpha * Ap[i];
+        }
+        Apsq = cnorm2(Ap, size);
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    k++;
+
+    for (n = 0; n < n_shift; n++) {
+        if (mapping[n] != n) {
+            for (int m = n + 1; m < n_shift; m++) {
+                if (mapping[m] == n) {
+                    cplx *tp = phi[m]; phi[m] = phi[n]; phi[n] = tp;
+                    double td = shifts[m]; shifts[m] = shifts[n]; shifts[n] = td;
+                    mapping[m] = mapping[n];
+                    mapping[n] = n;
+                    n--;
+                    break;
+                }
+            }
+        }
+    }
+    for (n = 0; n < n_shift; n++) {
+        memset(Ap, 0, sizeof(cplx) * size);
+        orc_apply(op, (double *)Ap, (const double *)phi[n]); ops++;
+        for (i = 0; i < size; i++) Ap[i] = Ap[i] + (shifts[n] * phi[n][i]);
+        if (resSqmrhs) resSqmrhs[n] = cdiffnorm2(Ap, phi0, size);
+    }
+    for (n = 0; n < n_shift; n++) free(p_s[n]);
+    free(p_s); free(phi); free(alpha_s); free(beta_s); free(zeta_s); free(zeta_s_prev);
+    free(shifts); free(mapping); free(r); free(Ar); free(p); free(Ap);
+    info->resSq = 0.0;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "CR-M");
+}
+
+/* ---------------------------------------------------------------- BiCGstab-l */
+
+/* generic_bicgstab_l.cpp:317-561 (complex minv_vector_bicgstab_l): l BiCG steps, then a
+ * minimal-residual polynomial of degree l by modified Gram-Schmidt (Sleijpen & Fokkema). */
+void orc_bicgstab_l(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+                    double eps, int l, orc_info *info, double *hist, int hist_cap)
+{
+    cplx *phi = CX(phi_);
+    const cplx *phi0 = CCX(phi0_);
+    cplx *r0 = (cplx *)calloc(size, sizeof(cplx));
+    cplx **r = (cplx **)malloc(sizeof(cplx *) * (l + 1));
+    cplx **u = (cplx **)malloc(sizeof(cplx *) * (l + 1));
+    double *sigma = (double *)calloc(l + 1, sizeof(double));
+    cplx *gamma = (cplx *)calloc(l + 1, sizeof(cplx));
+    cplx *gamma_p = (cplx *)calloc(l + 1, sizeof(cplx));
+    cplx *gamma_pp = (cplx *)calloc(l + 1, sizeof(cplx));
+    cplx *tau = (cplx *)calloc((size_t)(l + 1) * (l + 1), sizeof(cplx));
+#define TAU(a, b) tau[(a) * (l + 1) + (b)]
+    cplx rho0, rho1, alpha, omega, beta;
+    double bsqrt, truersq;
+    int k, i, j, ops = 0;
+    long h;
+    char nm[32];
+
+    for (i = 0; i <= l; i++) {
+        r[i] = (cplx *)calloc(size, sizeof(cplx));
+        u[i] = (cplx *)calloc(size, sizeof(cplx));
+    }
+    rho0 = 1.0;
+    alpha = 0.0;
+    omega = 1.0;
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)u[0], (const double *)phi); ops++;
+    for (h = 0; h < size; h++) r[0][h] = phi0[h] - u[0][h];
+    sigma[0] = cnorm2(r[0], size);
+    memcpy(r0, r[0], sizeof(cplx) * size);
+    memset(u[0], 0, sizeof(cplx) * size);
+
+    for (k = 0; k < max_iter; k += l) {
+        rho0 *= -omega;
+        for (j = 0; j < l; j++) {
+            rho1 = cdot(r0, r[j], size);
+            beta = alpha * rho1 / rho0;
+            rho0 = rho1;
+            for (i = 0; i <= j; i++)
+                for (h = 0; h < size; h++) u[i][h] = r[i][h] - beta * u[i][h];
+            orc_apply(op, (double *)u[j + 1], (const double *)u[j]); ops++;
+            alpha = rho0 / cdot(r0, u[j + 1], size);
+            for (i = 0; i <= j; i++)
+                for (h = 0; h < size; h++) r[i][h] = r[i][h] - alpha * u[i + 1][h];
+            orc_apply(op, (double *)r[j + 1], (const double *)r[j]); ops++;
+            for (h = 0; h < size; h++) phi[h] = phi[h] + alpha * u[0][h];
+        }
+        for (j = 1; j <= l; j++) {
+            for (i = 1; i < j; i++) {
+                TAU(i, j) = cdivr(cdot(r[i], r[j], size), sigma[i]);
+                for (h = 0; h < size; h++) r[j][h] = r[j][h] - TAU(i, j) * r[i][h];
+            }
+            sigma[j] = cnorm2(r[j], size);
+            gamma_p[j] = cdivr(cdot(r[j], r[0], size), sigma[j]);
+        }
+        gamma[l] = gamma_p[l];
+        omega = gamma[l];
+        for (j = l - 1; j > 0; j--) {
+            gamma[j] = gamma_p[j];
+            for (i = j + 1; i <= l; i++) gamma[j] = gamma[j] - TAU(j, i) * gamma[i];
+        }
+        for (j = 1; j < l; j++) {
+            gamma_pp[j] = gamma[j + 1];
+            for (i = j + 1; i < l; i++) gamma_pp[j] = gamma_pp[j] + TAU(j, i) * gamma[i + 1];
+        }
+        for (h = 0; h < size; h++) {
+            phi[h] = phi[h] + gamma[1] * r[0][h];
+            u[0][h] = u[0][h] - gamma[l] * u[l][h];
+            r[0][h] = r[0][h] - gamma_p[l] * r[l][h];
+        }
+        for (j = 1; j < l; j++) {
+            for (h = 0; h < size; h++) {
+                u[0][h] = u[0][h] - gamma[j] * u[j][h];
+                phi[h] = phi[h] + gamma_pp[j] * r[j][h];
+                r[0][h] = r[0][h] - gamma_p[j] * r[j][h];
+            }
+        }
+        sigma[0] = cnorm2(r[0], size);
+        record(hist, hist_cap, k / l, sqrt(sigma[0]) / bsqrt);
+        if (sqrt(sigma[0]) < eps * bsqrt) break;
+    }
+#undef TAU
+    info->success = (k >= max_iter - 1) ? 0 : 1;
+    k++;
+    orc_apply(op, (double *)u[0], (const double *)phi); ops++;
+    truersq = cdiffnorm2(u[0], phi0, size);
+    for (i = 0; i <= l; i++) { free(r[i]); free(u[i]); }
+    free(r); free(u); free(r0); free(sigma); free(gamma); free(gamma_p); free(gamma_pp); free(tau);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    snprintf(nm, sizeof(nm), "BiCGStab-%d", l);
+    set_name(info, nm);
+}
+
+/* generic_bicgstab_l.cpp:564-604 */
+void orc_bicgstab_l_restart(const orc_op *op, double *phi, const double *phi0, long size,
+                            int max_iter, double eps, int restart_freq, int l, orc_info *info)
+{
+    double bsqrt = sqrt(cnorm2(CCX(phi0), size));
+    int iter = 0, ops = 0;
+    orc_info inner;
+    memset(&inner, 0, sizeof(inner));
+    do {
+        orc_bicgstab_l(op, phi, phi0, size, restart_freq, eps, l, &inner, NULL, 0);
+        iter += inner.iter;
+        ops += inner.ops_count;
+    } while (iter < max_iter && inner.success == 0 && sqrt(inner.resSq) / bsqrt > eps);
+    *info = inner;
+    info->iter = iter;
+    info->ops_count = ops;
+    info->success = (sqrt(inner.resSq) / bsqrt > eps) ? 0 : 1;
+    char nm[64];
+    snprintf(nm, sizeof(nm), "BiCGStab-%d(%d)", l, restart_freq);
+    set_name(info, nm);
+}
+
+/* ---------------------------------------------------------------- BiCGstab-M */
+
+/* generic_bicgstab_m.cpp:398-774 (complex minv_vector_bicgstab_m): multishift BiCGstab
+ * (Jegerlehner, hep-lat/9612014).  The shadow vector is conj(b), so <wdag, v> = sum b_i v_i. */
+void orc_bicgstab_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shift, long size,
+                    int resid_freq_check, int max_iter, double eps, const double *shifts_in,
+                    int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap)
+{
+    const cplx *phi0 = CCX(phi0_);
+    cplx **phi = (cplx **)malloc(sizeof(cplx *) * n_shift);
+    cplx **s_s = (cplx **)malloc(sizeof(cplx *) * n_shift);
+    cplx *alpha_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *beta_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *zeta_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *zeta_s_prev = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *chi_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *rho_s = (cplx *)malloc(sizeof(cplx) * n_shift);
+    cplx *rho_s_prev = (cplx *)malloc(sizeof(cplx) * n_shift);
+    double *shifts = (double *)malloc(sizeof(double) * n_shift);
+    int *mapping = (int *)malloc(sizeof(int) * n_shift);
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *r_prev = (cplx *)calloc(size, sizeof(cplx));
+    cplx *s = (cplx *)calloc(size, sizeof(cplx));
+    cplx *As = (cplx *)calloc(size, sizeof(cplx));
+    cplx *w = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Aw = (cplx *)calloc(size, sizeof(cplx));
+    cplx *wdag = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta, beta_prev, psi, delta, delta_prev, chi, tmp;
+    double rsqNew, bsqrt;
+    int k, n, n_shift_rem = n_shift, ops = 0, breakdown = 0;
+    long i;
+
+    for (n = 0; n < n_shift; n++) {
+        phi[n] = CX(phi_all) + (long)n * size;
+        s_s[n] = (cplx *)malloc(sizeof(cplx) * size);
+        mapping[n] = n;
+        shifts[n] = shifts_in[n];
+        beta_s[n] = zeta_s[n] = zeta_s_prev[n] = rho_s[n] = rho_s_prev[n] = 1.0;
+        alpha_s[n] = chi_s[n] = 0.0;
+    }
+    beta = 1.0;
+    alpha = 0.0;
+    bsqrt = sqrt(cnorm2(phi0, size));
+    for (n = 0; n < n_shift; n++) {
+        memcpy(s_s[n], phi0, sizeof(cplx) * size);
+        memset(phi[n], 0, sizeof(cplx) * size);
+    }
+    memcpy(s, phi0, sizeof(cplx) * size);
+    memcpy(r, phi0, sizeof(cplx) * size);
+    memcpy(r_prev, r, sizeof(cplx) * size);
+    orc_apply(op, (double *)As, (const double *)s); ops++;
+    for (i = 0; i < size; i++) wdag[i] = conj(r[i]);
+    delta = delta_prev = cdot(wdag, r, size);
+    psi = cdot(wdag, As, size) / delta;
+
+    for (k = 0; k < max_iter; k++) {
+        beta_prev = beta;
+        beta = rdivc(-1.0, psi);
+        for (i = 0; i < size; i++) w[i] = r[i] + beta * As[i];
+        orc_apply(op, (double *)Aw, (const double *)w); ops++;
+        chi = cdivr(cdot(Aw, w, size), cnorm2(Aw, size));
+        memcpy(r_prev, r, sizeof(cplx) * size);
+        for (i = 0; i < size; i++) r[i] = w[i] - chi * Aw[i];
+        for (n = 0; n < n_shift_rem; n++) {
+            tmp = zeta_s[n];
+            zeta_s[n] = (zeta_s[n] * zeta_s_prev[n] * beta_prev) /
+                        (beta * alpha * (zeta_s_prev[n] - zeta_s[n]) +
+                         zeta_s_prev[n] * beta_prev * (1.0 - shifts[n] * beta));
+            zeta_s_prev[n] = tmp;
+            beta_s[n] = beta * zeta_s[n] / zeta_s_prev[n];
+            chi_s[n] = chi / (1.0 + chi * shifts[n]);
+            tmp = rho_s[n];
+            rho_s[n] = rho_s[n] / (1.0 + chi * shifts[n]);
+            rho_s_prev[n] = tmp;
+            for (i = 0; i < size; i++)
+                phi[n][i] = phi[n][i] - beta_s[n] * s_s[n][i] + chi_s[n] * rho_s_prev[n] * zeta_s[n] * w[i];
+        }
+        rsqNew = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsqNew) / bsqrt);
+        if (k % resid_freq_check == 0) {
+            for (n = 0; n < n_shift_rem; n++) {
+                if (cabs(zeta_s[n] * rho_s[n]) * sqrt(rsqNew) < eps * bsqrt) {
+                    n_shift_rem--;
+                    if (n_shift_rem != n) {
+                        int e = n_shift_rem;
+                        int ti = mapping[e]; mapping[e] = mapping[n]; mapping[n] = ti;
+                        cplx *tp = phi[e]; phi[e] = phi[n]; phi[n] = tp;
+                        tp = s_s[e]; s_s[e] = s_s[n]; s_s[n] = tp;
+                        cplx tc;
+                        tc = alpha_s[e]; alpha_s[e] = alpha_s[n]; alpha_s[n] = tc;
+                        tc = beta_s[e]; beta_s[e] = beta_s[n]; beta_s[n] = tc;
+                        tc = zeta_s[e]; zeta_s[e] = zeta_s[n]; zeta_s[n] = tc;
+                        tc = zeta_s_prev[e]; zeta_s_prev[e] = zeta_s_prev[n]; zeta_s_prev[n] = tc;
+                        tc = chi_s[e]; chi_s[e] = chi_s[n]; chi_s[n] = tc;
+                        tc = rho_s[e]; rho_s[e] = rho_s[n]; rho_s[n] = tc;
+                        tc = rho_s_prev[e]; rho_s_prev[e] = rho_s_prev[n]; rho_s_prev[n] = tc;
+                        double td = shifts[e]; shifts[e] = shifts[n]; shifts[n] = td;
+                        n--;
+                    }
+                }
+            }
+        }
+        if ((worst_first && (cabs(zeta_s[0] * rho_s[0]) * sqrt(rsqNew) < eps * bsqrt)) ||
+            rsqNew != rsqNew || n_shift_rem == 0 || k == max_iter - 1)
+            break;
+        delta_prev = delta;
+        delta = cdot(wdag, r, size);
+        alpha = -beta * delta / (delta_prev * chi);
+        for (n = 0; n < n_shift_rem; n++)
+            alpha_s[n] = alpha * zeta_s[n] * beta_s[n] / (zeta_s_prev[n] * beta);
+        for (i = 0; i < size; i++) s[i] = r[i] + alpha * (s[i] - chi * As[i]);
+        for (n = 0; n < n_shift_rem; n++) {
+            if (fabs(shifts[n]) != 0.0) {
+                for (i = 0; i < size; i++)
+                    s_s[n][i] = zeta_s[n] * rho_s[n] * r[i] +
+                                alpha_s[n] * (s_s[n][i] - chi_s[n] / beta_s[n] *
+                                                              (zeta_s[n] * rho_s_prev[n] * w[i] -
+                                                               zeta_s_prev[n] * rho_s_prev[n] * r_prev[i]));
+            } else {
+                memcpy(s_s[n], s, sizeof(cplx) * size);
+            }
+        }
+        orc_apply(op, (double *)As, (const double *)s); ops++;
+        psi = cdot(wdag, As, size) / delta;
+        if (cabs(psi) == 0) {
+            breakdown = 1;
+            break;
+        }
+    }
+    info->success = (k == max_iter - 1 || breakdown) ? 0 : 1;
+    k++;
+    for (n = 0; n < n_shift; n++) {
+        if (mapping[n] != n) {
+            for (int m = n + 1; m < n_shift; m++) {
+                if (mapping[m] == n) {
+                    cplx *tp = phi[m]; phi[m] = phi[n]; phi[n] = tp;
+                    double td = shifts[m]; shifts[m] = shifts[n]; shifts[n] = td;
+                    mapping[m] = mapping[n];
+                    mapping[n] = n;
+                    n--;
+                    break;
+                }
+            }
+        }
+    }
+    for (n = 0; n < n_shift; n++) {
+        memset(As, 0, sizeof(cplx) * size);
+        orc_apply(op, (double *)As, (const double *)phi[n]); ops++;
+        for (i = 0; i < size; i++) As[i] = As[i] + (shifts[n] * phi[n][i]);
+        if (resSqmrhs) resSqmrhs[n] = cdiffnorm2(As, phi0, size);
+    }
+    for (n = 0; n < n_shift; n++) free(s_s[n]);
+    free(s_s); free(phi); free(alpha_s); free(beta_s); free(zeta_s); free(zeta_s_prev);
+    free(chi_s); free(rho_s); free(rho_s_prev); free(shifts); free(mapping);
+    free(r); free(r_prev); free(s); free(As); free(w); free(Aw); free(wdag);
+    info->resSq = 0.0;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "BICGSTAB-M");
+}
+
+/* ---------------------------------------------------------------- preconditioned solvers */
+
+/* generic_precond.cpp: identity_preconditioner copies; minres_preconditioner runs n_step
+ * iterations of minv_vector_minres (omega 1) and gcr_preconditioner n_step iterations of
+ * minv_vector_gcr, both from the guess in lhs (the callers zero it). */
+static void precond_apply(const orc_precond *pc, cplx *lhs, const cplx *rhs, long size)
+{
+    orc_info tmp;
+    memset(&tmp, 0, sizeof(tmp));
+    switch (pc->kind) {
+    case ORC_PRECOND_MINRES:
+        orc_minres(pc->op, (double *)lhs, (const double *)rhs, size, pc->n_step, pc->rel_res, 1.0, &tmp, NULL, 0);
+        break;
+    case ORC_PRECOND_GCR:
+        orc_gcr(pc->op, (double *)lhs, (const double *)rhs, size, pc->n_step, pc->rel_res, &tmp, NULL, 0);
+        break;
+    default:
+        memcpy(lhs, rhs, sizeof(cplx) * size);
+        break;
+    }
+}
+
+/* generic_cg_flex_precond.cpp:208-365 (complex minv_vector_cg_flex_precond): flexible CG,
+ * each new direction A-orthogonalised against every stored one. */
+void orc_fpcg(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+              double eps, const orc_precond *pc, orc_info *info, double *hist, int hist_cap)
+{
+    cplx *phi = CX(phi_);
+    const cplx *phi0 = CCX(phi0_);
+    const int cap = (max_iter > 0 ? max_iter : 0) + 1;
+    cplx **p_store = (cplx **)calloc(cap, sizeof(cplx *));
+    cplx **Ap_store = (cplx **)calloc(cap, sizeof(cplx *));
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *z = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Az = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta_ij;
+    double rsq, bsqrt, truersq;
+    int k, ii, ops = 0, nstore = 0;
+    long i;
+
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)p, (const double *)phi); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
+    precond_apply(pc, z, r, size);
+    memcpy(p, z, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    for (k = 0; k < max_iter; k++) {
+        p_store[nstore] = p;
+        Ap_store[nstore] = Ap;
+        nstore++;
+        alpha = cdot(p, r, size) / cdot(p, Ap, size);
+        for (i = 0; i < size; i++) {
+            phi[i] = phi[i] + alpha * p[i];
+            r[i] = r[i] - alpha * Ap[i];
+        }
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+        if (sqrt(rsq) < eps * bsqrt || k == max_iter - 1) break;
+        memset(z, 0, sizeof(cplx) * size);
+        precond_apply(pc, z, r, size);
+        orc_apply(op, (double *)Az, (const double *)z); ops++;
+        p = (cplx *)malloc(sizeof(cplx) * size);
+        memcpy(p, z, sizeof(cplx) * size);
+        Ap = (cplx *)malloc(sizeof(cplx) * size);
+        memcpy(Ap, Az, sizeof(cplx) * size);
+        for (ii = 0; ii <= k; ii++) {
+            beta_ij = -cdot(Ap_store[ii], z, size) / cdot(p_store[ii], Ap_store[ii], size);
+            for (i = 0; i < size; i++) {
+                p[i] += beta_ij * p_store[ii][i];
+                Ap[i] += beta_ij * Ap_store[ii][i];
+            }
+        }
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    k++;
+    orc_apply(op, (double *)Az, (const double *)phi); ops++;
+    truersq = cdiffnorm2(Az, phi0, size);
+    for (ii = 0; ii < nstore; ii++) { free(p_store[ii]); free(Ap_store[ii]); }
+    if (nstore == 0) { free(p); free(Ap); }
+    free(p_store); free(Ap_store); free(r); free(z); free(Az);
+    info->resSq = truersq;
+    info->iter = k;
+    info->ops_count = ops;
+    set_name(info, "Flexibly Preconditioned CG");
+}
+
+/* generic_cg_flex_precond.cpp:368-415: the restarted driver adds one application for the
+ * final true residual to ops_count after printing the summary. */
+void orc_fpcg_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                      double eps, int restart_freq, const orc_precond *pc, orc_info *info)
+{
+    double bsqrt = sqrt(cnorm2(CCX(phi0), size));
+    int iter = 0, ops = 0;
+    orc_info inner;
+    memset(&inner, 0, sizeof(inner));
+    do {
+        orc_fpcg(op, phi, phi0, size, restart_freq, eps, pc, &inner, NULL, 0);
+        iter += inner.iter;
+        ops += inner.ops_count;
+    } while (iter < max_iter && inner.success == 0 && sqrt(inner.resSq) / bsqrt > eps);
+    cplx *Aphi = (cplx *)calloc(size, sizeof(cplx));
+    orc_apply(op, (double *)Aphi, phi); ops++;
+    inner.resSq = cdiffnorm2(Aphi, CCX(phi0), size);
+    free(Aphi);
+    *info = inner;
+    info->iter = iter;
+    info->ops_count = ops;
+    info->success = (sqrt(info->resSq) / bsqrt > eps) ? 0 : 1;
+    char nm[64];
+    snprintf(nm, sizeof(nm), "Flexibly Preconditioned Restarted CG(%d)", restart_freq);
+    set_name(info, nm);
+}
+
+/* generic_gcr_var_precond.cpp:221-364 (complex minv_vector_gcr_var_precond): GCR with a
+ * preconditioner that may change between iterations. */
+void orc_vpgcr(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
+               double eps, const orc_precond *pc, orc_info *info, double *hist, int hist_cap)
+{
+    const cplx *phi0 = CCX(phi0_);
+    const int cap = (max_iter > 0 ? max_iter : 0) + 1;
+    cplx **p_store = (cplx **)calloc(cap, sizeof(cplx *));
+    cplx **Ap_store = (cplx **)calloc(cap, sizeof(cplx *));
+    cplx *x = (cplx *)calloc(size, sizeof(cplx));
+    cplx *r = (cplx *)calloc(size, sizeof(cplx));
+    cplx *z = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Az = (cplx *)calloc(size, sizeof(cplx));
+    cplx *p = (cplx *)calloc(size, sizeof(cplx));
+    cplx *Ap = (cplx *)calloc(size, sizeof(cplx));
+    cplx alpha, beta_ij;
+    double rsq, bsqrt, truersq;
+    int k, ii, ops = 0, nstore = 0;
+    long i;
+
+    memcpy(x, phi_, sizeof(cplx) * size);
+    bsqrt = sqrt(cnorm2(phi0, size));
+    orc_apply(op, (double *)p, (const double *)x); ops++;
+    for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
+    precond_apply(pc, z, r, size);
+    memcpy(p, z, sizeof(cplx) * size);
+    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    for (k = 0; k < max_iter; k++) {
+        p_store[nstore] = p;
+        Ap_store[nstore] = Ap;
+        nstore++;
+        alpha = cdivr(cdot(Ap, r, size), cnorm2(Ap, size));
+        for (i = 0; i < size; i++) {
+            x[i] = x[i] + alpha * p[i];
+            r[i] = r[i] - alpha * Ap[i];
+        }
+        rsq = cnorm2(r, size);
+        record(hist, hist_cap, k, sqrt(rsq) / bsqrt);
+        if (sqrt(rsq) < eps * bsqrt || k == max_iter - 1) break;
+        memset(z, 0, sizeof(cplx) * size);
+        precond_apply(pc, z, r, size);
+        orc_apply(op, (double *)Az, (const double *)z); ops++;
+        p = (cplx *)malloc(sizeof(cplx) * size);
+        memcpy(p, z, sizeof(cplx) * size);
+        Ap = (cplx *)malloc(sizeof(cplx) * size);
+        memcpy(Ap, Az, sizeof(cplx) * size);
+        for (ii = 0; ii <= k; ii++) {
+            beta_ij = cdivr(-cdot(Ap_store[ii], Az, size), cnorm2(Ap_store[ii], size));
+            for (i = 0; i < size; i++) {
+                p[i] += beta_ij * p_store[ii][i];
+                Ap[i] += beta_ij * Ap_store[ii][i];
+            }
+        }
+    }
+    info->success = (k == max_iter - 1) ? 0 : 1;
+    orc_apply(op, (double *)Az, (const double *)x); ops++;
+    truersq = cdiffnorm2(Az, phi0, size);
+    memcpy(phi_, x, sizeof(cplx) * size);
+    for (ii = 0; ii < nstore; ii++) { free(p_store[ii]); free(Ap_store[ii]); }
+    if (nstore == 0) { free(p); free(Ap); }
+    free(p_store); free(Ap_store); free(x); free(r); free(z); free(Az);
+    info->resSq = truersq;
+    info->iter = nstore; /* the reference reports the number of stored directions (:350-362) */
+    info->ops_count = ops;
+    set_name(info, "Variably Preconditioned GCR");
+}
+
+/* generic_gcr_var_precond.cpp:367-411 */
+void orc_vpgcr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                       double eps, int restart_freq, const orc_precond *pc, orc_info *info)
+{
+    double bsqrt = sqrt(cnorm2(CCX(phi0), size));
+    int iter = 0, ops = 0;
+    orc_info inner;
+    memset(&inner, 0, sizeof(inner));
+    do {
+        orc_vpgcr(op, phi, phi0, size, restart_freq, eps, pc, &inner, NULL, 0);
+        iter += inner.iter;
+        ops += inner.ops_count;
+    } while (iter < max_iter && inner.success == 0 && sqrt(inner.resSq) / bsqrt > eps);
+    *info = inner;
+    info->iter = iter;
+    info->ops_count = ops;
+    info->success = (sqrt(inner.resSq) / bsqrt > eps) ? 0 : 1;
+    char nm[64];
+    snprintf(nm, sizeof(nm), "Variably Preconditioned Restarted GCR(%d)", restart_freq);
+    set_name(info, nm);
+}

@@ -5,7 +5,9 @@
  * (staggered D, D^dagger, D^dagger D, gauge Laplacian, stencil_2d apply/eo/oe, the
  * staggered stencil builders, and the even/odd pieces D_eo, D_oe, m^2 - D_eo D_oe with the
  * prepare / reconstruct steps) and the Krylov solvers that call them (CG, restarted CG,
- * multishift CG, BiCGstab, restarted BiCGstab, GCR, restarted GCR).  Every function cites
+ * multishift CG, BiCGstab, restarted BiCGstab, GCR, restarted GCR) and their siblings (CR,
+ * restarted CR, MinRes, multishift CR, BiCGstab-l, restarted BiCGstab-l, multishift BiCGstab,
+ * flexibly preconditioned CG and variably preconditioned GCR, with their restarted forms).  Every function cites
  * the reference file:line it follows.  It exists so that tests, the smoke check and the
  * CPU-baseline leg of the benchmark have something to compare the CUDA path against.
  * The product (the CUDA library and its C-ABI) never links, loads or calls it.
@@ -57,7 +59,7 @@ typedef struct {
     int iter;
     int success;
     int ops_count;
-    char name[32];
+    char name[64];
 } orc_info;
 
 /* Operators: lhs is overwritten, rhs is read. */
@@ -97,6 +99,42 @@ void orc_gcr_restart(const orc_op *op, double *phi, const double *phi0, long siz
 void orc_cg_m(const orc_op *op, double *phi, const double *phi0, int n_shift, long size,
               int resid_freq_check, int max_iter, double eps, const double *shifts,
               int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap);
+
+/* ---- sibling Krylov solvers ---- */
+void orc_cr(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+            double eps, orc_info *info, double *hist, int hist_cap);
+void orc_cr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                    double eps, int restart_freq, orc_info *info);
+void orc_minres(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                double eps, double omega, orc_info *info, double *hist, int hist_cap);
+void orc_cr_m(const orc_op *op, double *phi, const double *phi0, int n_shift, long size,
+              int resid_freq_check, int max_iter, double eps, const double *shifts,
+              int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap);
+/* hist receives one entry per l-step cycle */
+void orc_bicgstab_l(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                    double eps, int l, orc_info *info, double *hist, int hist_cap);
+void orc_bicgstab_l_restart(const orc_op *op, double *phi, const double *phi0, long size,
+                            int max_iter, double eps, int restart_freq, int l, orc_info *info);
+void orc_bicgstab_m(const orc_op *op, double *phi, const double *phi0, int n_shift, long size,
+                    int resid_freq_check, int max_iter, double eps, const double *shifts,
+                    int worst_first, orc_info *info, double *resSqmrhs, double *hist, int hist_cap);
+
+/* Preconditioners of the flexible solvers (generic_precond.h). */
+enum orc_precond_kind { ORC_PRECOND_IDENTITY = 0, ORC_PRECOND_MINRES = 1, ORC_PRECOND_GCR = 2 };
+typedef struct {
+    int kind;
+    int n_step;          /* iterations of the inner solve */
+    double rel_res;      /* its relative-residual target */
+    const orc_op *op;    /* its operator (matrix_vector of the precond struct) */
+} orc_precond;
+void orc_fpcg(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+              double eps, const orc_precond *pc, orc_info *info, double *hist, int hist_cap);
+void orc_fpcg_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                      double eps, int restart_freq, const orc_precond *pc, orc_info *info);
+void orc_vpgcr(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+               double eps, const orc_precond *pc, orc_info *info, double *hist, int hist_cap);
+void orc_vpgcr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
+                       double eps, int restart_freq, const orc_precond *pc, orc_info *info);
 
 /* Adjoint force for S = phi^dagger (D^dagger D + sigma)^-1 phi with respect to the link
  * angles theta_mu(x) (U = exp(i theta)), given X = (D^dagger D + sigma)^-1 phi and Y = D X:

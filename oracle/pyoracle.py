@@ -56,7 +56,7 @@ class OrcOp(C.Structure):
 
 class OrcInfo(C.Structure):
     _fields_ = [("resSq", C.c_double), ("iter", C.c_int), ("success", C.c_int),
-                ("ops_count", C.c_int), ("name", C.c_char * 32)]
+                ("ops_count", C.c_int), ("name", C.c_char * 64)]
 
     def as_dict(self):
         return {"resSq": self.resSq, "iter": self.iter, "success": bool(self.success),
@@ -70,6 +70,14 @@ def build(quiet=True):
     ref = os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
     if os.path.isdir(ref):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], stdout=out)
+
+
+PRECOND = {"identity": 0, "minres": 1, "gcr": 2}
+
+
+class OrcPrecond(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n_step", C.c_int), ("rel_res", C.c_double),
+                ("op", C.POINTER(OrcOp))]
 
 
 class Operator:
@@ -123,6 +131,22 @@ class Oracle:
         L.orc_cg_m.argtypes = [P(OrcOp), _dp, _dp, C.c_int, C.c_long, C.c_int, C.c_int, C.c_double,
                                _dp, C.c_int, P(OrcInfo), _dp, _dp, C.c_int]
         L.orc_staggered_force.argtypes = [_dp, C.c_double, C.c_int, C.c_int, _dp, _dp, _dp]
+        L.orc_cr.argtypes = solver_args
+        L.orc_cr_restart.argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int, P(OrcInfo)]
+        L.orc_minres.argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_double,
+                                 P(OrcInfo), _dp, C.c_int]
+        L.orc_bicgstab_l.argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                     P(OrcInfo), _dp, C.c_int]
+        L.orc_bicgstab_l_restart.argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                             C.c_int, P(OrcInfo)]
+        for n in ("orc_cr_m", "orc_bicgstab_m"):
+            getattr(L, n).argtypes = L.orc_cg_m.argtypes
+        for n in ("orc_fpcg", "orc_vpgcr"):
+            getattr(L, n).argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, P(OrcPrecond),
+                                      P(OrcInfo), _dp, C.c_int]
+        for n in ("orc_fpcg_restart", "orc_vpgcr_restart"):
+            getattr(L, n).argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
+                                      P(OrcPrecond), P(OrcInfo)]
         L.orc_eoprec_prepare.argtypes = [P(OrcOp), _dp, _dp]
         L.orc_eoprec_reconstruct.argtypes = [P(OrcOp), _dp, _dp, _dp]
 
@@ -191,6 +215,49 @@ class Oracle:
                           C.byref(info), _ptr(res), _ptr(hist) if hist_cap else None, hist_cap)
         return phi, info.as_dict(), res
 
+    def solve2(self, solver, op: Operator, phi0, phi=None, max_iter=10000, eps=1e-10,
+               restart_freq=0, l=2, omega=1.0, precond="identity", n_step=4, rel_res=1e-1,
+               hist_cap=0):
+        """The sibling solvers: solver in {"cr", "minres", "bicgstab_l", "fpcg", "vpgcr"};
+        the preconditioner of fpcg / vpgcr runs on op itself.  Returns (phi, info, hist)."""
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        phi = np.zeros_like(phi0) if phi is None else np.array(phi, dtype=np.complex128)
+        info = OrcInfo()
+        hist = np.zeros(max(hist_cap, 1))
+        hp = _ptr(hist) if hist_cap else None
+        a = (C.byref(op.struct), _ptr(phi), _ptr(phi0), phi0.size, max_iter, eps)
+        pc = OrcPrecond(PRECOND[precond], n_step, rel_res, C.pointer(op.struct))
+        L = self.lib
+        if solver == "cr":
+            if restart_freq > 0: L.orc_cr_restart(*a, restart_freq, C.byref(info))
+            else: L.orc_cr(*a, C.byref(info), hp, hist_cap)
+        elif solver == "minres":
+            L.orc_minres(*a, omega, C.byref(info), hp, hist_cap)
+        elif solver == "bicgstab_l":
+            if restart_freq > 0: L.orc_bicgstab_l_restart(*a, restart_freq, l, C.byref(info))
+            else: L.orc_bicgstab_l(*a, l, C.byref(info), hp, hist_cap)
+        else:
+            if restart_freq > 0: getattr(L, f"orc_{solver}_restart")(*a, restart_freq, C.byref(pc), C.byref(info))
+            else: getattr(L, f"orc_{solver}")(*a, C.byref(pc), C.byref(info), hp, hist_cap)
+        d = info.as_dict()
+        return phi, d, hist[: min(hist_cap, max(d["iter"], 0))] if hist_cap else None
+
+    def multishift(self, solver, op: Operator, phi0, shifts, resid_freq_check=1, max_iter=10000,
+                   eps=1e-10, worst_first=False, hist_cap=0):
+        """solver in {"cg_m", "cr_m", "bicgstab_m"}."""
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        shifts = np.ascontiguousarray(shifts, dtype=np.float64)
+        ns = shifts.size
+        phi = np.zeros((ns, phi0.size), dtype=np.complex128)
+        res = np.zeros(ns)
+        hist = np.zeros(max(hist_cap, 1))
+        info = OrcInfo()
+        getattr(self.lib, f"orc_{solver}")(C.byref(op.struct), _ptr(phi), _ptr(phi0), ns, phi0.size,
+                                           resid_freq_check, max_iter, eps, _ptr(shifts), int(worst_first),
+                                           C.byref(info), _ptr(res), _ptr(hist) if hist_cap else None,
+                                           hist_cap)
+        return phi, info.as_dict(), res
+
     def staggered_force(self, links, mass, lx, ly, X, Y):
         out = np.zeros(2 * lx * ly)
         self.lib.orc_staggered_force(_ptr(np.ascontiguousarray(links)), mass, lx, ly,
@@ -217,6 +284,11 @@ class RefOracle:
                                                               cp, _dp, C.c_char_p, C.c_int, C.c_char_p, C.c_int]
         L.ref_cg_m.argtypes = opargs + [_dp, _dp, C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int,
                                         C.c_int, cp, _dp, _dp, C.c_char_p, C.c_int]
+        L.ref_solve2.argtypes = [C.c_int, C.c_int] + opargs + [_dp, _dp, C.c_int, C.c_double, C.c_int,
+                                                               C.c_double, C.c_int, C.c_int, C.c_double,
+                                                               C.c_int, cp, C.c_int, cp, _dp, C.c_char_p,
+                                                               C.c_int, C.c_char_p, C.c_int]
+        L.ref_multishift2.argtypes = [C.c_int] + L.ref_cg_m.argtypes
         L.ref_eoprec_prepare.argtypes = opargs + [_dp, _dp]
         L.ref_eoprec_reconstruct.argtypes = opargs + [_dp, _dp, _dp]
 
@@ -295,4 +367,41 @@ class RefOracle:
                           _ptr(res), log, 1 << 20)
         d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]),
              "ops_count": int(info[3]), "name": "CG-M"}
+        return phi, d, res, log.value.decode()
+
+    def solve2(self, solver, op: Operator, phi0, phi=None, max_iter=10000, eps=1e-10,
+               restart_freq=0, l=2, omega=1.0, precond="identity", n_step=4, rel_res=1e-1,
+               verbosity=0, prefix="", precond_verbosity=0, precond_prefix=""):
+        """The reference's sibling solvers (see Oracle.solve2); returns (phi, info, log)."""
+        op._s6 = op.shifts6()
+        sid = {"cr": 3, "minres": 4, "bicgstab_l": 5, "fpcg": 6, "vpgcr": 7}[solver]
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        phi = np.zeros_like(phi0) if phi is None else np.array(phi, dtype=np.complex128)
+        info = np.zeros(4)
+        name = C.create_string_buffer(64)
+        log = C.create_string_buffer(1 << 21)
+        self.lib.ref_solve2(sid, restart_freq, *self._opargs(op), _ptr(phi), _ptr(phi0), max_iter, eps,
+                            l, omega, PRECOND[precond], n_step, rel_res, verbosity, prefix.encode(),
+                            precond_verbosity, precond_prefix.encode(), _ptr(info), name, 64, log, 1 << 21)
+        d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]),
+             "ops_count": int(info[3]), "name": name.value.decode()}
+        return phi, d, log.value.decode()
+
+    def multishift(self, solver, op: Operator, phi0, shifts, resid_freq_check=1, max_iter=10000,
+                   eps=1e-10, worst_first=False, verbosity=0, prefix=""):
+        """solver in {"cr_m", "bicgstab_m"}; returns (phi, info, resSqmrhs, log)."""
+        op._s6 = op.shifts6()
+        phi0 = np.ascontiguousarray(phi0, dtype=np.complex128)
+        shifts = np.array(shifts, dtype=np.float64)
+        ns = shifts.size
+        phi = np.zeros((ns, phi0.size), dtype=np.complex128)
+        info = np.zeros(4)
+        res = np.zeros(ns)
+        log = C.create_string_buffer(1 << 20)
+        self.lib.ref_multishift2({"cr_m": 0, "bicgstab_m": 1}[solver], *self._opargs(op), _ptr(phi),
+                                 _ptr(phi0), ns, resid_freq_check, max_iter, eps, _ptr(shifts),
+                                 int(worst_first), verbosity, prefix.encode(), _ptr(info), _ptr(res),
+                                 log, 1 << 20)
+        d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]),
+             "ops_count": int(info[3]), "name": {"cr_m": "CR-M", "bicgstab_m": "BICGSTAB-M"}[solver]}
         return phi, d, res, log.value.decode()

@@ -23,6 +23,14 @@
 #include "generic_cg_m.h"
 #include "generic_bicgstab.h"
 #include "generic_gcr.h"
+#include "generic_cr.h"
+#include "generic_cr_m.h"
+#include "generic_minres.h"
+#include "generic_bicgstab_l.h"
+#include "generic_bicgstab_m.h"
+#include "generic_cg_flex_precond.h"
+#include "generic_gcr_var_precond.h"
+#include "generic_precond.h"
 #include "lattice.h"
 #include "operators.h"
 #include "coarse_stencil.h"
@@ -268,6 +276,94 @@ void ref_cg_m(int kind, int lx, int ly, int nc, double mass, const double *links
     with_log(log, log_cap, [&]() {
         inv = minv_vector_cg_m(ptrs.data(), b.data(), n_shift, (int)o->size, resid_freq_check,
                                max_iter, eps, shifts, o->fn, o->extra, worst_first != 0, &verb);
+    });
+    fill_info(inv, info4, nullptr, 0);
+    for (int n = 0; n < n_shift; n++) resSqmrhs[n] = inv.resSqmrhs[n];
+    delete o;
+}
+
+// Sibling solvers.  solver: 3 CR, 4 MinRes (param = omega), 5 BiCGstab-l (l = iparam),
+// 6 flexibly preconditioned CG, 7 variably preconditioned GCR; restart_freq > 0 selects the
+// restarted variant (CR, BiCGstab-l, FPCG, VPGCR).  The preconditioner (6, 7) is
+// identity_preconditioner (pkind 0), minres_preconditioner (1) or gcr_preconditioner (2) with
+// n_step iterations to rel_res on the same operator (generic_precond.cpp).
+void ref_solve2(int solver, int restart_freq, int kind, int lx, int ly, int nc, double mass,
+                const double *links, const double *clover, const double *hopping,
+                const double *two_link, const double *shifts6, double *phi, const double *phi0,
+                int max_iter, double eps, int iparam, double param, int pkind, int n_step,
+                double rel_res, int verbosity, const char *prefix, int pverbosity,
+                const char *pprefix, double *info4, char *name, int name_cap, char *log,
+                int log_cap)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> b((const cd *)phi0, (const cd *)phi0 + o->size);
+    inversion_verbose_struct verb = make_verb(verbosity, prefix);
+    verb.precond_verbosity = (inversion_verbose_level)pverbosity;
+    verb.precond_verb_prefix = pprefix ? pprefix : "";
+    minres_precond_struct_complex mps;
+    gcr_precond_struct_complex gps;
+    mps.n_step = gps.n_step = n_step;
+    mps.rel_res = gps.rel_res = rel_res;
+    mps.matrix_vector = gps.matrix_vector = o->fn;
+    mps.matrix_extra_data = gps.matrix_extra_data = o->extra;
+    typedef void (*pc_fn)(cd *, cd *, int, void *, inversion_verbose_struct *);
+    pc_fn pfn_id = identity_preconditioner, pfn_mr = minres_preconditioner, pfn_gcr = gcr_preconditioner;
+    pc_fn pfn = pkind == 1 ? pfn_mr : pkind == 2 ? pfn_gcr : pfn_id;
+    void *pinfo = pkind == 1 ? (void *)&mps : pkind == 2 ? (void *)&gps : nullptr;
+    inversion_info inv;
+    with_log(log, log_cap, [&]() {
+        cd *x = (cd *)phi;
+        int sz = (int)o->size;
+        switch (solver) {
+        case 3:
+            inv = restart_freq > 0
+                      ? minv_vector_cr_restart(x, b.data(), sz, max_iter, eps, restart_freq, o->fn, o->extra, &verb)
+                      : minv_vector_cr(x, b.data(), sz, max_iter, eps, o->fn, o->extra, &verb);
+            break;
+        case 4: inv = minv_vector_minres(x, b.data(), sz, max_iter, eps, param, o->fn, o->extra, &verb); break;
+        case 5:
+            inv = restart_freq > 0
+                      ? minv_vector_bicgstab_l_restart(x, b.data(), sz, max_iter, eps, restart_freq, iparam, o->fn, o->extra, &verb)
+                      : minv_vector_bicgstab_l(x, b.data(), sz, max_iter, eps, iparam, o->fn, o->extra, &verb);
+            break;
+        case 6:
+            inv = restart_freq > 0
+                      ? minv_vector_cg_flex_precond_restart(x, b.data(), sz, max_iter, eps, restart_freq, o->fn, o->extra, pfn, pinfo, &verb)
+                      : minv_vector_cg_flex_precond(x, b.data(), sz, max_iter, eps, o->fn, o->extra, pfn, pinfo, &verb);
+            break;
+        default:
+            inv = restart_freq > 0
+                      ? minv_vector_gcr_var_precond_restart(x, b.data(), sz, max_iter, eps, restart_freq, o->fn, o->extra, pfn, pinfo, &verb)
+                      : minv_vector_gcr_var_precond(x, b.data(), sz, max_iter, eps, o->fn, o->extra, pfn, pinfo, &verb);
+            break;
+        }
+    });
+    fill_info(inv, info4, name, name_cap);
+    delete o;
+}
+
+// Multishift CR (solver 0, generic_cr_m.cpp:312) or BiCGstab-M (solver 1,
+// generic_bicgstab_m.cpp:398).  phi holds n_shift vectors back to back.
+void ref_multishift2(int solver, int kind, int lx, int ly, int nc, double mass, const double *links,
+                     const double *clover, const double *hopping, const double *two_link,
+                     const double *shifts6, double *phi, const double *phi0, int n_shift,
+                     int resid_freq_check, int max_iter, double eps, double *shifts, int worst_first,
+                     int verbosity, const char *prefix, double *info4, double *resSqmrhs, char *log,
+                     int log_cap)
+{
+    RefOp *o = make_op(kind, lx, ly, nc, mass, links, clover, hopping, two_link, shifts6);
+    std::vector<cd> b((const cd *)phi0, (const cd *)phi0 + o->size);
+    std::vector<cd *> ptrs(n_shift);
+    for (int n = 0; n < n_shift; n++) ptrs[n] = (cd *)phi + (long)n * o->size;
+    inversion_verbose_struct verb = make_verb(verbosity, prefix);
+    inversion_info inv;
+    with_log(log, log_cap, [&]() {
+        if (solver == 0)
+            inv = minv_vector_cr_m(ptrs.data(), b.data(), n_shift, (int)o->size, resid_freq_check,
+                                   max_iter, eps, shifts, o->fn, o->extra, worst_first != 0, &verb);
+        else
+            inv = minv_vector_bicgstab_m(ptrs.data(), b.data(), n_shift, (int)o->size, resid_freq_check,
+                                         max_iter, eps, shifts, o->fn, o->extra, worst_first != 0, &verb);
     });
     fill_info(inv, info4, nullptr, 0);
     for (int n = 0; n < n_shift; n++) resSqmrhs[n] = inv.resSqmrhs[n];

@@ -142,6 +142,49 @@ def main():
     vec["l32_eo_solution"] = R.eoprec_reconstruct(eo, xe, b_)
     info["cases"]["l32_eo_cg"] = {**d, "log": log, "max_iter": 10000, "eps": 1e-10, "mass": 0.1}
 
+    # ---- sibling Krylov solvers on the 32x32 system (tol 1e-10): CR and the flexible CG on
+    # D^dagger D, BiCGstab-l and the variably preconditioned GCR on D, MinRes on the gauge
+    # Laplacian at mass 0.5; preconditioners run on the solve's own operator
+    lap5 = Op("laplace", lx, ly, 0.5, U)
+    sib = [
+        ("cr", normal, {}), ("cr", normal, {"restart_freq": 17}),
+        ("minres", lap5, {}), ("minres", lap5, {"omega": 0.8}),
+        ("bicgstab_l", stag, {"l": 1}), ("bicgstab_l", stag, {"l": 2}), ("bicgstab_l", stag, {"l": 4}),
+        ("bicgstab_l", stag, {"l": 4, "restart_freq": 16}),
+        ("fpcg", normal, {"precond": "identity"}), ("fpcg", normal, {"precond": "minres"}),
+        ("fpcg", normal, {"precond": "gcr"}), ("fpcg", normal, {"precond": "minres", "restart_freq": 12}),
+        ("vpgcr", stag, {"precond": "identity"}), ("vpgcr", stag, {"precond": "minres"}),
+        ("vpgcr", stag, {"precond": "gcr"}), ("vpgcr", stag, {"precond": "minres", "restart_freq": 12}),
+    ]
+    opname = {id(normal): "staggered_normal", id(stag): "staggered", id(lap5): "laplace_m0.5"}
+    for solver, op, kw in sib:
+        key = "l32_" + solver + "".join(f"_{k}{v}" for k, v in sorted(kw.items()))
+        rf = kw.get("restart_freq", 0)
+        xs, d, log = R.solve2(solver, op, b, max_iter=10000, eps=1e-10, verbosity=1 if rf == 0 else 2,
+                              prefix="[SIB] ", **kw)
+        vec[key] = xs
+        info["cases"][key] = {**d, "log": log, "solver": solver, "kw": kw, "max_iter": 10000, "eps": 1e-10,
+                              "op": opname[id(op)]}
+    # detail logs with a max_iter cut, and a preconditioner that prints its own summaries
+    for solver, op, kw, mi in (("cr", normal, {}, 6), ("minres", lap5, {}, 5), ("bicgstab_l", stag, {"l": 2}, 6),
+                               ("fpcg", normal, {"precond": "minres"}, 4), ("vpgcr", stag, {"precond": "gcr"}, 4)):
+        key = f"l32_{solver}_maxiter{mi}"
+        _, d, log = R.solve2(solver, op, b, max_iter=mi, eps=1e-10, verbosity=3, prefix="", **kw)
+        info["cases"][key] = {**d, "log": log, "solver": solver, "kw": kw, "max_iter": mi,
+                              "op": opname[id(op)]}
+    _, d, log = R.solve2("fpcg", normal, b, max_iter=3, eps=1e-10, verbosity=3, prefix="[OUT] ",
+                         precond="minres", precond_verbosity=1, precond_prefix="  [MR] ")
+    info["cases"]["l32_fpcg_precond_log"] = {**d, "log": log, "max_iter": 3, "op": "staggered_normal"}
+    # multishift CR on the gauge Laplacian, multishift BiCGstab on D
+    for solver, op in (("cr_m", lap), ("bicgstab_m", stag)):
+        for rfc, wf in ((1, False), (3, False), (1, True)):
+            xs, d, res, log = R.multishift(solver, op, b, msh, resid_freq_check=rfc, max_iter=10000,
+                                           eps=1e-10, worst_first=wf, verbosity=1, prefix="[MS] ")
+            key = f"l32_{solver}_rfc{rfc}_wf{int(wf)}"
+            vec[key] = xs.reshape(-1)
+            info["cases"][key] = {**d, "resSqmrhs": res.tolist(), "log": log, "shifts": msh, "rfc": rfc,
+                                  "worst_first": wf, "op": "laplace_m0.001" if op is lap else "staggered"}
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     with open(os.path.join(HERE, "reference_info.json"), "w") as f:
         json.dump(info, f, indent=1, default=lambda o: o.item() if hasattr(o, "item") else str(o))
