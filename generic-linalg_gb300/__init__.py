@@ -16,8 +16,12 @@ interface for the path:
   forms (operators.cpp:543-620, operators_stencil.cpp:179-236);
 * solvers ``minv_vector_cg``, ``minv_vector_cg_restart``, ``minv_vector_cg_m``,
   ``minv_vector_bicgstab``, ``minv_vector_bicgstab_restart``, ``minv_vector_gcr``,
-  ``minv_vector_gcr_restart`` with the reference's argument order, returning
-  ``InversionInfo`` (inverter_struct.h:14-43);
+  ``minv_vector_gcr_restart`` and the siblings ``minv_vector_cr``, ``minv_vector_cr_restart``,
+  ``minv_vector_minres``, ``minv_vector_cr_m``, ``minv_vector_bicgstab_l``,
+  ``minv_vector_bicgstab_l_restart``, ``minv_vector_bicgstab_m``,
+  ``minv_vector_cg_flex_precond``, ``minv_vector_gcr_var_precond`` (and their restarted forms,
+  with ``identity_preconditioner``, ``minres_preconditioner``, ``gcr_preconditioner``) with the
+  reference's argument order, returning ``InversionInfo`` (inverter_struct.h:14-43);
 * ``InversionVerboseStruct`` and the ``VERB_*`` levels (verbosity.h:9-24).
 
 Fields are numpy complex128 arrays (host) or CUDA torch tensors of dtype complex128
@@ -50,6 +54,12 @@ __all__ = [
     "apply_square_staggered_eoprec_reconstruct_stencil",
     "minv_vector_cg", "minv_vector_cg_restart", "minv_vector_cg_m", "minv_vector_bicgstab",
     "minv_vector_bicgstab_restart", "minv_vector_gcr", "minv_vector_gcr_restart",
+    "minv_vector_cr", "minv_vector_cr_restart", "minv_vector_minres", "minv_vector_cr_m",
+    "minv_vector_bicgstab_l", "minv_vector_bicgstab_l_restart", "minv_vector_bicgstab_m",
+    "minv_vector_cg_flex_precond", "minv_vector_cg_flex_precond_restart",
+    "minv_vector_gcr_var_precond", "minv_vector_gcr_var_precond_restart",
+    "identity_preconditioner", "minres_preconditioner", "gcr_preconditioner",
+    "MinresPrecondStruct", "GcrPrecondStruct",
     "Generator", "dot", "norm2sq", "staggered_force", "staggered_action_grad",
     "cg_batch", "cg_m_multi",
     "PREC_DOUBLE", "PREC_SINGLE", "PREC_HALF", "PREC_BFLOAT",
@@ -350,7 +360,7 @@ def _params(precision=PREC_DOUBLE, delta=0.0, device=False):
 
 
 def _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity, restart=None,
-           precision=PREC_DOUBLE, delta=0.0):
+           precision=PREC_DOUBLE, delta=0.0, extra_args=()):
     op, temp = _resolve(matrix_vector, extra_info)
     try:
         pp, pn, pdev = _field_ptr(phi, writable=True)
@@ -364,6 +374,7 @@ def _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbos
         args = [op.handle, _dptr(pp), _dptr(bp), int(size), int(max_iter), float(eps)]
         if restart is not None:
             args.append(int(restart))
+        args += list(extra_args)
         args += [C.byref(verb) if verb is not None else None,
                  C.byref(_params(precision, delta, pdev)), C.byref(info)]
         _capi.check(fn(*args), fn.__name__)
@@ -417,6 +428,142 @@ def minv_vector_gcr_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix
 def minv_vector_cg_m(phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, shifts,
                      matrix_vector, extra_info, worst_first=False, verbosity=None):
     """minv_vector_cg_m (generic_cg_m.cpp:312).  phi: a list of n_shift output fields."""
+    return _multishift(lib().glinalg_cg_m, phi, phi0, n_shift, size, resid_freq_check, max_iter, eps,
+                       shifts, matrix_vector, extra_info, worst_first, verbosity)
+
+
+def minv_vector_cr_m(phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, shifts,
+                     matrix_vector, extra_info, worst_first=False, verbosity=None):
+    """minv_vector_cr_m (generic_cr_m.cpp:323): multishift conjugate residual."""
+    return _multishift(lib().glinalg_cr_m, phi, phi0, n_shift, size, resid_freq_check, max_iter, eps,
+                       shifts, matrix_vector, extra_info, worst_first, verbosity)
+
+
+def minv_vector_bicgstab_m(phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, shifts,
+                           matrix_vector, extra_info, worst_first=False, verbosity=None):
+    """minv_vector_bicgstab_m (generic_bicgstab_m.cpp:402): multishift BiCGstab."""
+    return _multishift(lib().glinalg_bicgstab_m, phi, phi0, n_shift, size, resid_freq_check, max_iter,
+                       eps, shifts, matrix_vector, extra_info, worst_first, verbosity)
+
+
+def minv_vector_cr(phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity=None):
+    """minv_vector_cr (generic_cr.cpp:198)."""
+    return _solve(lib().glinalg_cr, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity)
+
+
+def minv_vector_cr_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector, extra_info,
+                           verbosity=None):
+    """minv_vector_cr_restart (generic_cr.cpp:326)."""
+    return _solve(lib().glinalg_cr_restart, phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                  verbosity, restart=restart_freq)
+
+
+def minv_vector_minres(phi, phi0, size, max_iter, eps, *args, verbosity=None):
+    """minv_vector_minres (generic_minres.cpp:130 and :234): the two reference overloads,
+    ``(phi, phi0, size, max_iter, eps, omega, matrix_vector, extra_info[, verbosity])`` and
+    ``(phi, phi0, size, max_iter, eps, matrix_vector, extra_info[, verbosity])`` (omega 1)."""
+    if args and isinstance(args[0], (int, float)):
+        omega, rest = float(args[0]), args[1:]
+    else:
+        omega, rest = 1.0, args
+    matrix_vector, extra_info = rest[0], rest[1]
+    if len(rest) > 2:
+        verbosity = rest[2]
+    return _solve(lib().glinalg_minres, phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                  verbosity, extra_args=(C.c_double(omega),))
+
+
+def minv_vector_bicgstab_l(phi, phi0, size, max_iter, eps, l, matrix_vector, extra_info, verbosity=None):
+    """minv_vector_bicgstab_l (generic_bicgstab_l.cpp:317)."""
+    return _solve(lib().glinalg_bicgstab_l, phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                  verbosity, extra_args=(C.c_int(int(l)),))
+
+
+def minv_vector_bicgstab_l_restart(phi, phi0, size, max_iter, eps, restart_freq, l, matrix_vector,
+                                   extra_info, verbosity=None):
+    """minv_vector_bicgstab_l_restart (generic_bicgstab_l.cpp:564)."""
+    return _solve(lib().glinalg_bicgstab_l_restart, phi, phi0, size, max_iter, eps, matrix_vector,
+                  extra_info, verbosity, restart=restart_freq, extra_args=(C.c_int(int(l)),))
+
+
+class MinresPrecondStruct:
+    """Mirror of minres_precond_struct_complex (generic_precond.h:37-43)."""
+
+    def __init__(self, n_step, rel_res, matrix_vector, matrix_extra_data):
+        self.n_step, self.rel_res = n_step, rel_res
+        self.matrix_vector, self.matrix_extra_data = matrix_vector, matrix_extra_data
+
+
+class GcrPrecondStruct(MinresPrecondStruct):
+    """Mirror of gcr_precond_struct_complex (generic_precond.h:64-70)."""
+
+
+def _precond(kind, name, ref):
+    def pc(lhs, rhs, size, extra_data, verb=None):
+        raise UnsupportedOperator(f"{name} runs inside the GPU solvers only; pass it to "
+                                  "minv_vector_cg_flex_precond or minv_vector_gcr_var_precond")
+    pc.__name__ = name
+    pc.__doc__ = f"{name} ({ref}); selects the device preconditioner of the flexible solvers."
+    pc._glinalg_precond = kind
+    return pc
+
+
+identity_preconditioner = _precond(0, "identity_preconditioner", "generic_precond.cpp:34")
+minres_preconditioner = _precond(1, "minres_preconditioner", "generic_precond.cpp:53")
+gcr_preconditioner = _precond(2, "gcr_preconditioner", "generic_precond.cpp:70")
+
+
+def _flex(fn, phi, phi0, size, max_iter, eps, restart, matrix_vector, extra_info, precond_matrix_vector,
+          precond_info, verbosity):
+    kind = getattr(precond_matrix_vector, "_glinalg_precond", None)
+    if kind is None:
+        raise UnsupportedOperator(f"{precond_matrix_vector!r} is not one of the GPU preconditioners")
+    pc = _capi.PrecondStruct()
+    pc.kind = kind
+    pop, ptemp = None, False
+    if kind != 0:
+        pc.n_step, pc.rel_res = int(precond_info.n_step), float(precond_info.rel_res)
+        if precond_info.matrix_vector is not matrix_vector or precond_info.matrix_extra_data is not extra_info:
+            pop, ptemp = _resolve(precond_info.matrix_vector, precond_info.matrix_extra_data)
+            pc.op = pop.handle
+    try:
+        return _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity,
+                      restart=restart, extra_args=(C.byref(pc),))
+    finally:
+        if ptemp:
+            pop.close()
+
+
+def minv_vector_cg_flex_precond(phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                                precond_matrix_vector, precond_info, verbosity=None):
+    """minv_vector_cg_flex_precond (generic_cg_flex_precond.cpp:223)."""
+    return _flex(lib().glinalg_cg_flex_precond, phi, phi0, size, max_iter, eps, None, matrix_vector,
+                 extra_info, precond_matrix_vector, precond_info, verbosity)
+
+
+def minv_vector_cg_flex_precond_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector,
+                                        extra_info, precond_matrix_vector, precond_info, verbosity=None):
+    """minv_vector_cg_flex_precond_restart (generic_cg_flex_precond.cpp:367)."""
+    return _flex(lib().glinalg_cg_flex_precond_restart, phi, phi0, size, max_iter, eps, restart_freq,
+                 matrix_vector, extra_info, precond_matrix_vector, precond_info, verbosity)
+
+
+def minv_vector_gcr_var_precond(phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
+                                precond_matrix_vector, precond_info, verbosity=None):
+    """minv_vector_gcr_var_precond (generic_gcr_var_precond.cpp:220)."""
+    return _flex(lib().glinalg_gcr_var_precond, phi, phi0, size, max_iter, eps, None, matrix_vector,
+                 extra_info, precond_matrix_vector, precond_info, verbosity)
+
+
+def minv_vector_gcr_var_precond_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector,
+                                        extra_info, precond_matrix_vector, precond_info, verbosity=None):
+    """minv_vector_gcr_var_precond_restart (generic_gcr_var_precond.cpp:369)."""
+    return _flex(lib().glinalg_gcr_var_precond_restart, phi, phi0, size, max_iter, eps, restart_freq,
+                 matrix_vector, extra_info, precond_matrix_vector, precond_info, verbosity)
+
+
+def _multishift(fn, phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, shifts,
+                matrix_vector, extra_info, worst_first, verbosity):
     op, temp = _resolve(matrix_vector, extra_info)
     try:
         ptrs = [_field_ptr(p, writable=True) for p in phi[:n_shift]]
@@ -430,11 +577,11 @@ def minv_vector_cg_m(phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, 
         info.resSqmrhs = res.ctypes.data_as(C.POINTER(C.c_double))
         info.n_rhs = n_shift
         verb = verbosity.struct() if verbosity is not None else None
-        _capi.check(lib().glinalg_cg_m(op.handle, arr, _dptr(bp), int(n_shift), int(size),
-                                       int(resid_freq_check), int(max_iter), float(eps),
-                                       sh.ctypes.data_as(C.POINTER(C.c_double)), int(bool(worst_first)),
-                                       C.byref(verb) if verb is not None else None,
-                                       C.byref(_params(device=bdev)), C.byref(info)), "glinalg_cg_m")
+        _capi.check(fn(op.handle, arr, _dptr(bp), int(n_shift), int(size),
+                       int(resid_freq_check), int(max_iter), float(eps),
+                       sh.ctypes.data_as(C.POINTER(C.c_double)), int(bool(worst_first)),
+                       C.byref(verb) if verb is not None else None,
+                       C.byref(_params(device=bdev)), C.byref(info)), fn.__name__)
         return InversionInfo(info, res)
     finally:
         if temp:

@@ -36,7 +36,7 @@ class VerbStruct(C.Structure):
 
 class InfoStruct(C.Structure):
     _fields_ = [("resSq", C.c_double), ("iter", C.c_int), ("success", C.c_int),
-                ("ops_count", C.c_int), ("name", C.c_char * 32), ("resSqmrhs", _dp),
+                ("ops_count", C.c_int), ("name", C.c_char * 64), ("resSqmrhs", _dp),
                 ("n_rhs", C.c_int), ("status", C.c_int), ("reliable_updates", C.c_int),
                 ("device_ms", C.c_double), ("gbytes", C.c_double), ("kernel_ms", C.c_double),
                 ("kernel_gbytes", C.c_double), ("kernel_launches", C.c_int)]
@@ -45,6 +45,10 @@ class InfoStruct(C.Structure):
 class SolverParams(C.Structure):
     _fields_ = [("precision", C.c_int), ("delta", C.c_double), ("flags", C.c_int),
                 ("reserved", C.c_int)]
+
+
+class PrecondStruct(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n_step", C.c_int), ("rel_res", C.c_double), ("op", C.c_void_p)]
 
 
 # Every function the header declares, with its ctypes prototype.
@@ -82,6 +86,24 @@ def _prototypes():
         "glinalg_gcr_restart": (st, restart),
         "glinalg_cg_m": (st, [vp, P(_dp), _dp, i, i, i, i, d, _dp, i, P(VerbStruct),
                               P(SolverParams), P(InfoStruct)]),
+        "glinalg_cr": (st, solver),
+        "glinalg_cr_restart": (st, restart),
+        "glinalg_minres": (st, [vp, _dp, _dp, i, i, d, d, P(VerbStruct), P(SolverParams), P(InfoStruct)]),
+        "glinalg_bicgstab_l": (st, [vp, _dp, _dp, i, i, d, i, P(VerbStruct), P(SolverParams), P(InfoStruct)]),
+        "glinalg_bicgstab_l_restart": (st, [vp, _dp, _dp, i, i, d, i, i, P(VerbStruct), P(SolverParams),
+                                            P(InfoStruct)]),
+        "glinalg_cr_m": (st, [vp, P(_dp), _dp, i, i, i, i, d, _dp, i, P(VerbStruct),
+                              P(SolverParams), P(InfoStruct)]),
+        "glinalg_bicgstab_m": (st, [vp, P(_dp), _dp, i, i, i, i, d, _dp, i, P(VerbStruct),
+                                    P(SolverParams), P(InfoStruct)]),
+        "glinalg_cg_flex_precond": (st, [vp, _dp, _dp, i, i, d, P(PrecondStruct), P(VerbStruct),
+                                         P(SolverParams), P(InfoStruct)]),
+        "glinalg_cg_flex_precond_restart": (st, [vp, _dp, _dp, i, i, d, i, P(PrecondStruct), P(VerbStruct),
+                                                 P(SolverParams), P(InfoStruct)]),
+        "glinalg_gcr_var_precond": (st, [vp, _dp, _dp, i, i, d, P(PrecondStruct), P(VerbStruct),
+                                         P(SolverParams), P(InfoStruct)]),
+        "glinalg_gcr_var_precond_restart": (st, [vp, _dp, _dp, i, i, d, i, P(PrecondStruct), P(VerbStruct),
+                                                 P(SolverParams), P(InfoStruct)]),
         "glinalg_cg_m_multi": (st, [vp, _dp, _dp, i, i, i, i, i, d, _dp, P(SolverParams),
                                     P(InfoStruct)]),
         "glinalg_cg_batch": (st, [P(vp), i, P(_dp), P(_dp), i, d, P(SolverParams), P(InfoStruct)]),

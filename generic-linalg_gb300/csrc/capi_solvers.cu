@@ -184,3 +184,242 @@ extern "C" glinalg_status glinalg_cg_m(glinalg_operator op, double *const *phi, 
     GL_CUDA(cudaStreamSynchronize(st));
     return GLINALG_SUCCESS;
 }
+
+// ---------------------------------------------------------------- sibling solvers
+
+namespace {
+
+glinalg_status fp64_only(const glinalg_solver_params *params, const char *what)
+{
+    if (precision_of(params) != GLINALG_PREC_DOUBLE) {
+        set_last_error(std::string(what) + " runs in FP64 only");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    return GLINALG_SUCCESS;
+}
+
+glinalg_status positive(int v, const char *what)
+{
+    if (v <= 0) {
+        set_last_error(std::string(what) + " must be positive");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    return GLINALG_SUCCESS;
+}
+
+// Runs one single-vector solve: argument checks, staging of phi / phi0, the solver, copy-back.
+template <class F>
+glinalg_status single_solve(glinalg_operator op, double *phi, const double *phi0, int size,
+                            const glinalg_solver_params *params, glinalg_info *info, const char *what, F solve)
+{
+    GL_TRY(ensure_device());
+    GL_TRY(fp64_only(params, what));
+    SolveCall c;
+    GL_TRY(prologue(op, phi, phi0, size, params, info, c));
+    GL_TRY(solve(c));
+    return finish_call(c, phi, op->size);
+}
+
+glinalg_status make_precond(const glinalg_precond *p, glinalg_operator op, Precond *out)
+{
+    *out = Precond{};
+    if (!p) return GLINALG_SUCCESS;
+    if (p->kind < GLINALG_PRECOND_IDENTITY || p->kind > GLINALG_PRECOND_GCR) {
+        set_last_error("unknown preconditioner kind");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    if (p->kind != GLINALG_PRECOND_IDENTITY && p->n_step < 0) {
+        set_last_error("preconditioner n_step must not be negative");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    if (p->op && p->op->size != op->size) {
+        set_last_error("the preconditioner's operator has another field size");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    out->kind = p->kind;
+    out->n_step = p->n_step;
+    out->rel_res = p->rel_res;
+    out->op = p->op;
+    return GLINALG_SUCCESS;
+}
+
+// Multishift entry: staging of the n_shift solution vectors, then solver(X, b).
+template <class F>
+glinalg_status multishift_entry(glinalg_operator op, double *const *phi, const double *phi0, int n_shift,
+                                int size, int resid_freq_check, const double *shifts,
+                                const glinalg_solver_params *params, glinalg_info *info, const char *what,
+                                F solve)
+{
+    GL_TRY(ensure_device());
+    if (!op || !phi || !phi0 || !shifts || !info || n_shift <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    GL_TRY(positive(resid_freq_check, "resid_freq_check"));
+    if ((long)size != op->size) {
+        set_last_error("size does not match the operator's field size");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    for (int j = 0; j < n_shift; j++)
+        if (!phi[j]) return GLINALG_ERROR_INVALID_VALUE;
+    GL_TRY(fp64_only(params, what));
+    const bool dev = params && (params->flags & GLINALG_PTR_DEVICE);
+    cudaStream_t st = lib_stream();
+    Scratch sc(st);
+    const long n = op->size;
+    std::vector<double2 *> X(n_shift);
+    const double2 *b = (const double2 *)phi0;
+    if (dev) {
+        for (int j = 0; j < n_shift; j++) X[j] = (double2 *)phi[j];
+    } else {
+        for (int j = 0; j < n_shift; j++) GL_TRY(sc.alloc(&X[j], n));
+        double2 *bb;
+        GL_TRY(sc.alloc(&bb, n));
+        GL_CUDA(cudaMemcpyAsync(bb, phi0, sizeof(double2) * n, cudaMemcpyHostToDevice, st));
+        b = bb;
+    }
+    double *keep = info->resSqmrhs;
+    *info = glinalg_info{};
+    info->resSqmrhs = keep;
+    GL_TRY(solve(X.data(), b, st));
+    if (!dev)
+        for (int j = 0; j < n_shift; j++)
+            GL_CUDA(cudaMemcpyAsync(phi[j], X[j], sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
+    GL_CUDA(cudaStreamSynchronize(st));
+    return GLINALG_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" glinalg_status glinalg_cr(glinalg_operator op, double *phi, const double *phi0, int size,
+                                     int max_iter, double eps, const glinalg_verbosity *verb,
+                                     const glinalg_solver_params *params, glinalg_info *info)
+{
+    return single_solve(op, phi, phi0, size, params, info, "CR", [&](SolveCall &c) {
+        return cr_fp64(op, c.sg.x, c.sg.b, max_iter, eps, Verb::from(verb), info, c.st);
+    });
+}
+
+extern "C" glinalg_status glinalg_cr_restart(glinalg_operator op, double *phi, const double *phi0, int size,
+                                             int max_iter, double eps, int restart_freq,
+                                             const glinalg_verbosity *verb,
+                                             const glinalg_solver_params *params, glinalg_info *info)
+{
+    GL_TRY(positive(restart_freq, "restart_freq"));
+    return single_solve(op, phi, phi0, size, params, info, "CR", [&](SolveCall &c) {
+        return cr_restart_fp64(op, c.sg.x, c.sg.b, max_iter, eps, restart_freq, Verb::from(verb), info, c.st);
+    });
+}
+
+extern "C" glinalg_status glinalg_minres(glinalg_operator op, double *phi, const double *phi0, int size,
+                                         int max_iter, double eps, double omega,
+                                         const glinalg_verbosity *verb, const glinalg_solver_params *params,
+                                         glinalg_info *info)
+{
+    return single_solve(op, phi, phi0, size, params, info, "MinRes", [&](SolveCall &c) {
+        return minres_fp64(op, c.sg.x, c.sg.b, max_iter, eps, omega, Verb::from(verb), info, c.st);
+    });
+}
+
+extern "C" glinalg_status glinalg_bicgstab_l(glinalg_operator op, double *phi, const double *phi0, int size,
+                                             int max_iter, double eps, int l, const glinalg_verbosity *verb,
+                                             const glinalg_solver_params *params, glinalg_info *info)
+{
+    if (l < 1 || l > kMaxBicgstabL) {
+        set_last_error("BiCGstab-l needs 1 <= l <= 16");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    return single_solve(op, phi, phi0, size, params, info, "BiCGstab-l", [&](SolveCall &c) {
+        return bicgstab_l_fp64(op, c.sg.x, c.sg.b, max_iter, eps, l, Verb::from(verb), info, c.st);
+    });
+}
+
+extern "C" glinalg_status glinalg_bicgstab_l_restart(glinalg_operator op, double *phi, const double *phi0,
+                                                     int size, int max_iter, double eps, int restart_freq, int l,
+                                                     const glinalg_verbosity *verb,
+                                                     const glinalg_solver_params *params, glinalg_info *info)
+{
+    GL_TRY(positive(restart_freq, "restart_freq"));
+    if (l < 1 || l > kMaxBicgstabL) {
+        set_last_error("BiCGstab-l needs 1 <= l <= 16");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
+    return single_solve(op, phi, phi0, size, params, info, "BiCGstab-l", [&](SolveCall &c) {
+        return bicgstab_l_restart_fp64(op, c.sg.x, c.sg.b, max_iter, eps, restart_freq, l, Verb::from(verb), info,
+                                       c.st);
+    });
+}
+
+extern "C" glinalg_status glinalg_cr_m(glinalg_operator op, double *const *phi, const double *phi0, int n_shift,
+                                       int size, int resid_freq_check, int max_iter, double eps,
+                                       const double *shifts, int worst_first, const glinalg_verbosity *verb,
+                                       const glinalg_solver_params *params, glinalg_info *info)
+{
+    return multishift_entry(op, phi, phi0, n_shift, size, resid_freq_check, shifts, params, info, "CR-M",
+                            [&](double2 *const *X, const double2 *b, cudaStream_t st) {
+                                return cr_m_fp64(op, X, b, n_shift, resid_freq_check, max_iter, eps, shifts,
+                                                 worst_first != 0, Verb::from(verb), info, st);
+                            });
+}
+
+extern "C" glinalg_status glinalg_bicgstab_m(glinalg_operator op, double *const *phi, const double *phi0,
+                                             int n_shift, int size, int resid_freq_check, int max_iter,
+                                             double eps, const double *shifts, int worst_first,
+                                             const glinalg_verbosity *verb, const glinalg_solver_params *params,
+                                             glinalg_info *info)
+{
+    return multishift_entry(op, phi, phi0, n_shift, size, resid_freq_check, shifts, params, info, "BiCGstab-M",
+                            [&](double2 *const *X, const double2 *b, cudaStream_t st) {
+                                return bicgstab_m_fp64(op, X, b, n_shift, resid_freq_check, max_iter, eps, shifts,
+                                                       worst_first != 0, Verb::from(verb), info, st);
+                            });
+}
+
+static glinalg_status flex_entry(int mode, int restart_freq, glinalg_operator op, double *phi, const double *phi0,
+                                 int size, int max_iter, double eps, const glinalg_precond *precond,
+                                 const glinalg_verbosity *verb, const glinalg_solver_params *params,
+                                 glinalg_info *info)
+{
+    if (!op) return GLINALG_ERROR_INVALID_VALUE;
+    Precond pc;
+    GL_TRY(make_precond(precond, op, &pc));
+    return single_solve(op, phi, phi0, size, params, info, mode == 0 ? "FPCG" : "VPGCR", [&](SolveCall &c) {
+        const Verb v = Verb::from(verb);
+        return restart_freq > 0
+                   ? flex_restart_fp64(mode, op, c.sg.x, c.sg.b, max_iter, eps, restart_freq, pc, v, info, c.st)
+                   : flex_fp64(mode, op, c.sg.x, c.sg.b, max_iter, eps, pc, v, info, c.st);
+    });
+}
+
+extern "C" glinalg_status glinalg_cg_flex_precond(glinalg_operator op, double *phi, const double *phi0, int size,
+                                                  int max_iter, double eps, const glinalg_precond *precond,
+                                                  const glinalg_verbosity *verb,
+                                                  const glinalg_solver_params *params, glinalg_info *info)
+{
+    return flex_entry(0, 0, op, phi, phi0, size, max_iter, eps, precond, verb, params, info);
+}
+
+extern "C" glinalg_status glinalg_cg_flex_precond_restart(glinalg_operator op, double *phi, const double *phi0,
+                                                          int size, int max_iter, double eps, int restart_freq,
+                                                          const glinalg_precond *precond,
+                                                          const glinalg_verbosity *verb,
+                                                          const glinalg_solver_params *params, glinalg_info *info)
+{
+    GL_TRY(positive(restart_freq, "restart_freq"));
+    return flex_entry(0, restart_freq, op, phi, phi0, size, max_iter, eps, precond, verb, params, info);
+}
+
+extern "C" glinalg_status glinalg_gcr_var_precond(glinalg_operator op, double *phi, const double *phi0, int size,
+                                                  int max_iter, double eps, const glinalg_precond *precond,
+                                                  const glinalg_verbosity *verb,
+                                                  const glinalg_solver_params *params, glinalg_info *info)
+{
+    return flex_entry(1, 0, op, phi, phi0, size, max_iter, eps, precond, verb, params, info);
+}
+
+extern "C" glinalg_status glinalg_gcr_var_precond_restart(glinalg_operator op, double *phi, const double *phi0,
+                                                          int size, int max_iter, double eps, int restart_freq,
+                                                          const glinalg_precond *precond,
+                                                          const glinalg_verbosity *verb,
+                                                          const glinalg_solver_params *params, glinalg_info *info)
+{
+    GL_TRY(positive(restart_freq, "restart_freq"));
+    return flex_entry(1, restart_freq, op, phi, phi0, size, max_iter, eps, precond, verb, params, info);
+}

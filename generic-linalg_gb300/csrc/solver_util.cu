@@ -169,6 +169,17 @@ Verb Verb::restart_inner() const
     return r;
 }
 
+Verb Verb::precond_inner() const
+{
+    Verb r;
+    r.present = true;  // the reference always passes a struct to the preconditioner
+    if (present) {
+        r.level = precond_level == -1 ? level : precond_level;
+        r.prefix = precond_prefix;
+    }
+    return r;
+}
+
 void Verb::resid(const std::string &alg, int iter, int ops, double relres) const
 {
     if (present && level == 3)

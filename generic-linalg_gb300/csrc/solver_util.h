@@ -144,6 +144,7 @@ struct Verb {
     bool present = false;
     static Verb from(const glinalg_verbosity *v);
     Verb restart_inner() const;  // shuffle_verbosity_restart (verbosity.h:27-43)
+    Verb precond_inner() const;  // shuffle_verbosity_precond (verbosity.h:46-67)
     void resid(const std::string &alg, int iter, int ops, double relres) const;
     void summary(const std::string &alg, bool success, int iter, int ops, double relres) const;
     void summary_multi(bool success, int iter, int ops, const double *relres, int n) const;

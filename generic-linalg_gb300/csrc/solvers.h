@@ -33,6 +33,41 @@ glinalg_status restart_driver(int which, const glinalg_operator_s *op, double2 *
                               const double2 *b, int max_iter, double eps, int restart_freq,
                               const Verb &verb, glinalg_info *info, cudaStream_t st);
 
+// ---- sibling solvers (solvers_more.cu) ----
+// A preconditioner of the flexible solvers: kind GLINALG_PRECOND_*, n_step inner iterations
+// to rel_res on op (null: the solve's own operator).
+struct Precond {
+    int kind = GLINALG_PRECOND_IDENTITY;
+    int n_step = 0;
+    double rel_res = 0.0;
+    const glinalg_operator_s *op = nullptr;
+};
+glinalg_status cr_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                       double eps, const Verb &verb, glinalg_info *info, cudaStream_t st);
+glinalg_status cr_restart_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                               double eps, int restart_freq, const Verb &verb, glinalg_info *info,
+                               cudaStream_t st);
+glinalg_status minres_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                           double eps, double omega, const Verb &verb, glinalg_info *info, cudaStream_t st);
+glinalg_status cr_m_fp64(const glinalg_operator_s *op, double2 *const *X, const double2 *b, int n_shift,
+                         int rfc, int max_iter, double eps, const double *shifts, bool worst_first,
+                         const Verb &verb, glinalg_info *info, cudaStream_t st);
+glinalg_status bicgstab_m_fp64(const glinalg_operator_s *op, double2 *const *X, const double2 *b,
+                               int n_shift, int rfc, int max_iter, double eps, const double *shifts,
+                               bool worst_first, const Verb &verb, glinalg_info *info, cudaStream_t st);
+constexpr int kMaxBicgstabL = 16;
+glinalg_status bicgstab_l_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                               double eps, int l, const Verb &verb, glinalg_info *info, cudaStream_t st);
+glinalg_status bicgstab_l_restart_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b,
+                                       int max_iter, double eps, int restart_freq, int l, const Verb &verb,
+                                       glinalg_info *info, cudaStream_t st);
+// mode 0: flexibly preconditioned CG; mode 1: variably preconditioned GCR
+glinalg_status flex_fp64(int mode, const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                         double eps, const Precond &pc, const Verb &verb, glinalg_info *info, cudaStream_t st);
+glinalg_status flex_restart_fp64(int mode, const glinalg_operator_s *op, double2 *x, const double2 *b,
+                                 int max_iter, double eps, int restart_freq, const Precond &pc,
+                                 const Verb &verb, glinalg_info *info, cudaStream_t st);
+
 // Mixed-precision CG with FP64 reliable updates (cg_mixed.cu).  sigma: diagonal shift added to
 // the operator (0 for the plain system).
 glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GLINALG_ABI_VERSION 1
+#define GLINALG_ABI_VERSION 2
 
 typedef enum glinalg_status {
     GLINALG_SUCCESS = 0,
@@ -111,7 +111,7 @@ typedef struct glinalg_info {
     int iter;            /* iterations */
     int success;         /* 1 if converged */
     int ops_count;       /* operator applications, counted as the reference counts them */
-    char name[32];       /* "CG", "CG(n)", "CG-M", "BiCGStab", "GCR", ... */
+    char name[64];       /* "CG", "CG(n)", "CG-M", "BiCGStab", "GCR", ... */
     double *resSqmrhs;   /* caller-provided, n_rhs entries: per-shift |(A+s)x - b|^2 (CG-M) */
     int n_rhs;
     int status;          /* glinalg_solve_status */
@@ -223,6 +223,88 @@ glinalg_status glinalg_cg_m(glinalg_operator op, double *const *phi, const doubl
                             double eps, const double *shifts, int worst_first,
                             const glinalg_verbosity *verb, const glinalg_solver_params *params,
                             glinalg_info *info);
+
+/* ---- sibling solvers: the reference's other Krylov methods on the same operators (FP64) ---- */
+
+/* minv_vector_cr                 generic_cr.cpp:198 (A Hermitian).  As in the reference,
+ * info->success is 1 whenever max_iter > 0 (generic_cr.cpp:288 compares k with max_iter, a
+ * value the loop never reaches); info->status says whether the tolerance was met. */
+glinalg_status glinalg_cr(glinalg_operator op, double *phi, const double *phi0, int size,
+                          int max_iter, double eps, const glinalg_verbosity *verb,
+                          const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_cr_restart         generic_cr.cpp:326 */
+glinalg_status glinalg_cr_restart(glinalg_operator op, double *phi, const double *phi0, int size,
+                                  int max_iter, double eps, int restart_freq,
+                                  const glinalg_verbosity *verb,
+                                  const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_minres (with omega) generic_minres.cpp:130: minimal residual, x += omega alpha r */
+glinalg_status glinalg_minres(glinalg_operator op, double *phi, const double *phi0, int size,
+                              int max_iter, double eps, double omega,
+                              const glinalg_verbosity *verb, const glinalg_solver_params *params,
+                              glinalg_info *info);
+/* minv_vector_bicgstab_l         generic_bicgstab_l.cpp:317 (1 <= l <= 16) */
+glinalg_status glinalg_bicgstab_l(glinalg_operator op, double *phi, const double *phi0, int size,
+                                  int max_iter, double eps, int l, const glinalg_verbosity *verb,
+                                  const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_bicgstab_l_restart generic_bicgstab_l.cpp:564 */
+glinalg_status glinalg_bicgstab_l_restart(glinalg_operator op, double *phi, const double *phi0,
+                                          int size, int max_iter, double eps, int restart_freq, int l,
+                                          const glinalg_verbosity *verb,
+                                          const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_cr_m               generic_cr_m.cpp:323 and
+ * minv_vector_bicgstab_m         generic_bicgstab_m.cpp:402: arguments as glinalg_cg_m.  The
+ * multishift summary line reads "CG-M" for every method, as the reference prints it. */
+glinalg_status glinalg_cr_m(glinalg_operator op, double *const *phi, const double *phi0,
+                            int n_shift, int size, int resid_freq_check, int max_iter,
+                            double eps, const double *shifts, int worst_first,
+                            const glinalg_verbosity *verb, const glinalg_solver_params *params,
+                            glinalg_info *info);
+glinalg_status glinalg_bicgstab_m(glinalg_operator op, double *const *phi, const double *phi0,
+                                  int n_shift, int size, int resid_freq_check, int max_iter,
+                                  double eps, const double *shifts, int worst_first,
+                                  const glinalg_verbosity *verb,
+                                  const glinalg_solver_params *params, glinalg_info *info);
+
+/* Preconditioners of the flexible solvers (generic_precond.h): the reference passes a
+ * callback plus a struct; here the kind selects the callback and the fields are the struct's. */
+typedef enum glinalg_precond_kind {
+    GLINALG_PRECOND_IDENTITY = 0, /* identity_preconditioner  generic_precond.cpp:34 */
+    GLINALG_PRECOND_MINRES = 1,   /* minres_preconditioner    generic_precond.cpp:53 */
+    GLINALG_PRECOND_GCR = 2       /* gcr_preconditioner       generic_precond.cpp:70 */
+} glinalg_precond_kind;
+typedef struct glinalg_precond {
+    int kind;             /* glinalg_precond_kind */
+    int n_step;           /* {minres,gcr}_precond_struct_complex::n_step */
+    double rel_res;       /* ::rel_res */
+    glinalg_operator op;  /* ::matrix_vector / matrix_extra_data; NULL: the solve's operator */
+} glinalg_precond;
+
+/* minv_vector_cg_flex_precond    generic_cg_flex_precond.cpp:223 (NULL precond: identity) */
+glinalg_status glinalg_cg_flex_precond(glinalg_operator op, double *phi, const double *phi0,
+                                       int size, int max_iter, double eps,
+                                       const glinalg_precond *precond,
+                                       const glinalg_verbosity *verb,
+                                       const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_cg_flex_precond_restart generic_cg_flex_precond.cpp:367 */
+glinalg_status glinalg_cg_flex_precond_restart(glinalg_operator op, double *phi, const double *phi0,
+                                               int size, int max_iter, double eps, int restart_freq,
+                                               const glinalg_precond *precond,
+                                               const glinalg_verbosity *verb,
+                                               const glinalg_solver_params *params,
+                                               glinalg_info *info);
+/* minv_vector_gcr_var_precond    generic_gcr_var_precond.cpp:220 */
+glinalg_status glinalg_gcr_var_precond(glinalg_operator op, double *phi, const double *phi0,
+                                       int size, int max_iter, double eps,
+                                       const glinalg_precond *precond,
+                                       const glinalg_verbosity *verb,
+                                       const glinalg_solver_params *params, glinalg_info *info);
+/* minv_vector_gcr_var_precond_restart generic_gcr_var_precond.cpp:369 */
+glinalg_status glinalg_gcr_var_precond_restart(glinalg_operator op, double *phi, const double *phi0,
+                                               int size, int max_iter, double eps, int restart_freq,
+                                               const glinalg_precond *precond,
+                                               const glinalg_verbosity *verb,
+                                               const glinalg_solver_params *params,
+                                               glinalg_info *info);
 
 /* ---- batched solves (no reference counterpart: the reference solves systems one at a
  * time in a loop; these run many independent systems in one device launch sequence) ---- */

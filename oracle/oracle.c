@@ -756,7 +756,7 @@ void orc_cr(const orc_op *op, double *phi_, const double *phi0_, long size, int 
     set_name(info, "CR");
 }
 
-/* generic_cr.cpp:326-366 */
+/* generic_cr.cpp:326-366 (complex minv_vector_cr_restart) */
 void orc_cr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
                     double eps, int restart_freq, orc_info *info)
 {
@@ -765,7 +765,7 @@ void orc_cr_restart(const orc_op *op, double *phi, const double *phi0, long size
 
 /* ---------------------------------------------------------------- MinRes */
 
-/* generic_minres.cpp (complex minv_vector_minres with omega, the "MR_<omega>" solver):
+/* generic_minres.cpp:130-231 (complex minv_vector_minres with omega, printed as "MR_<omega>"):
  * x += omega alpha r, r -= omega alpha A r with alpha = <Ar, r> / |Ar|^2. */
 void orc_minres(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
                 double eps, double omega, orc_info *info, double *hist, int hist_cap)
@@ -808,7 +808,7 @@ void orc_minres(const orc_op *op, double *phi_, const double *phi0_, long size, 
 
 /* ---------------------------------------------------------------- CR-M */
 
-/* generic_cr_m.cpp:312-622 (complex minv_vector_cr_m): multishift conjugate residual.  The
+/* generic_cr_m.cpp:323-622 (complex minv_vector_cr_m): multishift conjugate residual.  The
  * shift bookkeeping (retire, swap, restore) is the one of CG-M. */
 void orc_cr_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shift, long size,
               int resid_freq_check, int max_iter, double eps, const double *shifts_in,
@@ -1062,7 +1062,7 @@ void orc_bicgstab_l_restart(const orc_op *op, double *phi, const double *phi0, l
 
 /* ---------------------------------------------------------------- BiCGstab-M */
 
-/* generic_bicgstab_m.cpp:398-774 (complex minv_vector_bicgstab_m): multishift BiCGstab
+/* generic_bicgstab_m.cpp:402-774 (complex minv_vector_bicgstab_m): multishift BiCGstab
  * (Jegerlehner, hep-lat/9612014).  The shadow vector is conj(b), so <wdag, v> = sum b_i v_i. */
 void orc_bicgstab_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shift, long size,
                     int resid_freq_check, int max_iter, double eps, const double *shifts_in,
@@ -1223,7 +1223,7 @@ void orc_bicgstab_m(const orc_op *op, double *phi_all, const double *phi0_, int 
 
 /* ---------------------------------------------------------------- preconditioned solvers */
 
-/* generic_precond.cpp: identity_preconditioner copies; minres_preconditioner runs n_step
+/* generic_precond.cpp:34-77: identity_preconditioner copies; minres_preconditioner runs n_step
  * iterations of minv_vector_minres (omega 1) and gcr_preconditioner n_step iterations of
  * minv_vector_gcr, both from the guess in lhs (the callers zero it). */
 static void precond_apply(const orc_precond *pc, cplx *lhs, const cplx *rhs, long size)
@@ -1243,7 +1243,7 @@ static void precond_apply(const orc_precond *pc, cplx *lhs, const cplx *rhs, lon
     }
 }
 
-/* generic_cg_flex_precond.cpp:208-365 (complex minv_vector_cg_flex_precond): flexible CG,
+/* generic_cg_flex_precond.cpp:223-364 (complex minv_vector_cg_flex_precond): flexible CG,
  * each new direction A-orthogonalised against every stored one. */
 void orc_fpcg(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
               double eps, const orc_precond *pc, orc_info *info, double *hist, int hist_cap)
@@ -1309,7 +1309,7 @@ void orc_fpcg(const orc_op *op, double *phi_, const double *phi0_, long size, in
     set_name(info, "Flexibly Preconditioned CG");
 }
 
-/* generic_cg_flex_precond.cpp:368-415: the restarted driver adds one application for the
+/* generic_cg_flex_precond.cpp:367-415: the restarted driver adds one application for the
  * final true residual to ops_count after printing the summary. */
 void orc_fpcg_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
                       double eps, int restart_freq, const orc_precond *pc, orc_info *info)
@@ -1336,7 +1336,7 @@ void orc_fpcg_restart(const orc_op *op, double *phi, const double *phi0, long si
     set_name(info, nm);
 }
 
-/* generic_gcr_var_precond.cpp:221-364 (complex minv_vector_gcr_var_precond): GCR with a
+/* generic_gcr_var_precond.cpp:220-366 (complex minv_vector_gcr_var_precond): GCR with a
  * preconditioner that may change between iterations. */
 void orc_vpgcr(const orc_op *op, double *phi_, const double *phi0_, long size, int max_iter,
                double eps, const orc_precond *pc, orc_info *info, double *hist, int hist_cap)
@@ -1403,7 +1403,7 @@ void orc_vpgcr(const orc_op *op, double *phi_, const double *phi0_, long size, i
     set_name(info, "Variably Preconditioned GCR");
 }
 
-/* generic_gcr_var_precond.cpp:367-411 */
+/* generic_gcr_var_precond.cpp:369-411 */
 void orc_vpgcr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
                        double eps, int restart_freq, const orc_precond *pc, orc_info *info)
 {

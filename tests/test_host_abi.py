@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol(gl):
 
 def test_abi_version_and_strings(gl):
     L = gl.lib()
-    assert L.glinalg_abi_version() == 1
+    assert L.glinalg_abi_version() == 2
     assert L.glinalg_status_string(0) == b"success"
     assert L.glinalg_status_string(4) == b"no CUDA device"
 
