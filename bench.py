@@ -338,6 +338,87 @@ def workload_batch(args):
     print(json.dumps(line))
 
 
+def workload_siblings(args):
+    """The reference's sibling Krylov solvers (FP64, the reference's recurrences) on one
+    256x256 system from std::mt19937(1337): CR, CR-M (12 shifts logspace[1e-4, 1]) and the
+    flexibly preconditioned CG (MinRes(4) preconditioner) on D^dagger D with m = 0.05;
+    BiCGstab-2, BiCGstab-4, BiCGstab-M and the variably preconditioned GCR (MinRes(4)) on D;
+    MinRes on the gauge Laplacian with mass 0.5.  Tolerance 1e-10; device-resident fields, L2
+    flushed before every solve.  The CPU baseline is the oracle's same solver on the same
+    system for a few iterations, extrapolated linearly to the GPU's iteration count."""
+    import numpy as np
+    import torch
+    gl = importlib.import_module("generic-linalg_gb300")
+    L = gl.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
+    lx = ly = 256
+    g = gl.Generator(SEED)
+    U = g.rand_gauge_u1(lx, ly)
+    b = g.gaussian(lx * ly)
+    Ud, bd = torch.from_numpy(U).to(dev), torch.from_numpy(b).to(dev)
+    nrm = gl.StaggeredU1Op(Ud, 0.05, lx, ly)
+    lap = gl.StaggeredU1Op(Ud, 0.5, lx, ly)
+    N, D, LAP = gl.square_staggered_normal_u1, gl.square_staggered_u1, gl.square_laplace_u1
+    shifts = np.logspace(-4, 0, 12)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    x = torch.zeros_like(bd)
+    xs = [torch.zeros_like(bd) for _ in shifts]
+    n = lx * ly
+    cases = {
+        "CR": lambda: gl.minv_vector_cr(x, bd, n, 100000, EPS, N, nrm),
+        "MinRes (Laplacian, mass 0.5)": lambda: gl.minv_vector_minres(x, bd, n, 100000, EPS, 1.0, LAP, lap),
+        "BiCGStab-2": lambda: gl.minv_vector_bicgstab_l(x, bd, n, 100000, EPS, 2, D, nrm),
+        "BiCGStab-4": lambda: gl.minv_vector_bicgstab_l(x, bd, n, 100000, EPS, 4, D, nrm),
+        "FPCG, MinRes(4) preconditioner": lambda: gl.minv_vector_cg_flex_precond(
+            x, bd, n, 100000, EPS, N, nrm, gl.minres_preconditioner, gl.MinresPrecondStruct(4, 0.1, N, nrm)),
+        "VPGCR, MinRes(4) preconditioner": lambda: gl.minv_vector_gcr_var_precond(
+            x, bd, n, 100000, EPS, D, nrm, gl.minres_preconditioner, gl.MinresPrecondStruct(4, 0.1, D, nrm)),
+        "CR-M (12 shifts)": lambda: gl.minv_vector_cr_m(xs, bd, 12, n, 1, 100000, EPS, shifts.copy(), N, nrm),
+        "BiCGstab-M (12 shifts)": lambda: gl.minv_vector_bicgstab_m(xs, bd, 12, n, 1, 100000, EPS, shifts.copy(),
+                                                                    D, nrm),
+    }
+    out = {}
+    for name, fn in cases.items():
+        ts, info = [], None
+        for i in range(args.warmup + args.steps):
+            x.zero_()
+            t, info = _flush_and_time(fn, flush, stream)
+            if i >= args.warmup:
+                ts.append(t)
+        ms = statistics.mean(ts)
+        out[name] = {"ms": round(ms, 3), "iters": info.iter, "ops": info.ops_count, "success": info.success,
+                     "algorithmic_GBps": round(info.gbytes / (ms * 1e-3), 1)}
+    line = {"workload": "sibling Krylov solvers, 256x256, m=0.05 (Laplacian mass 0.5), tol 1e-10, FP64",
+            "steps": args.steps, "warmup": args.warmup, "l2": "flushed (512 MiB write) before every solve",
+            "solvers": out}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        O = pyoracle.Oracle()
+        on = pyoracle.Operator("staggered_normal", lx, ly, 0.05, U)
+        od = pyoracle.Operator("staggered", lx, ly, 0.05, U)
+        ol = pyoracle.Operator("laplace", lx, ly, 0.5, U)
+        samples = {"CR": ("cr", on, {}), "MinRes (Laplacian, mass 0.5)": ("minres", ol, {}),
+                   "BiCGStab-2": ("bicgstab_l", od, {"l": 2}), "BiCGStab-4": ("bicgstab_l", od, {"l": 4}),
+                   "FPCG, MinRes(4) preconditioner": ("fpcg", on, {"precond": "minres", "rel_res": 0.1}),
+                   "VPGCR, MinRes(4) preconditioner": ("vpgcr", od, {"precond": "minres", "rel_res": 0.1})}
+        cpu = {}
+        for name, (solver, oop, kw) in samples.items():
+            k = 8 if solver != "bicgstab_l" else 8 * kw["l"]
+            t0 = time.perf_counter()
+            O.solve2(solver, oop, b, max_iter=k, eps=EPS, **kw)
+            dt = time.perf_counter() - t0
+            cpu[name] = round(dt / k * out[name]["iters"] * 1e3, 1)
+        line["cpu_baseline"] = {"unit": "ms per solve", "cores": 1, "kind": "port", "values": cpu,
+                                "sample": "8 iterations (BiCGStab-l: 8 cycles) of the oracle's same solver on "
+                                          "the same system, extrapolated linearly to the GPU's iteration count "
+                                          "(an underestimate for FPCG / VPGCR, whose cost per iteration grows)"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,7 +433,7 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only time the two inner-iteration kernels of the headline variant "
                          "(a small case for ncu captures)")
-    ap.add_argument("--workload", default="headline", choices=["headline", "multishift", "batch"],
+    ap.add_argument("--workload", default="headline", choices=["headline", "multishift", "batch", "siblings"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")
     ap.add_argument("--probe-iters", type=int, default=0,
                     help="run one headline-variant solve stopped after this many inner iterations "
@@ -364,6 +445,8 @@ def main():
         return workload_multishift(args)
     if args.workload == "batch" and args.impl == "ours":
         return workload_batch(args)
+    if args.workload == "siblings" and args.impl == "ours":
+        return workload_siblings(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.kernels_only:

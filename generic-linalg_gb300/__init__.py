@@ -22,7 +22,10 @@ interface for the path:
   ``minv_vector_cg_flex_precond``, ``minv_vector_gcr_var_precond`` (and their restarted forms,
   with ``identity_preconditioner``, ``minres_preconditioner``, ``gcr_preconditioner``) with the
   reference's argument order, returning ``InversionInfo`` (inverter_struct.h:14-43);
-* ``InversionVerboseStruct`` and the ``VERB_*`` levels (verbosity.h:9-24).
+* ``InversionVerboseStruct`` and the ``VERB_*`` levels (verbosity.h:9-24);
+* the U(1) gauge-field utilities of u1_utils.h: ``read_gauge_u1``, ``write_gauge_u1``,
+  ``unit_gauge_u1``, ``get_plaquette_u1``, ``get_topo_u1``, ``apply_gauge_trans_u1``,
+  ``apply_ape_smear_u1`` and ``Generator.rand_trans_u1``.
 
 Fields are numpy complex128 arrays (host) or CUDA torch tensors of dtype complex128
 (device; the call then passes device pointers).  As in the reference, the solver recognises
@@ -62,6 +65,8 @@ __all__ = [
     "MinresPrecondStruct", "GcrPrecondStruct",
     "Generator", "dot", "norm2sq", "staggered_force", "staggered_action_grad",
     "cg_batch", "cg_m_multi",
+    "read_gauge_u1", "write_gauge_u1", "unit_gauge_u1", "get_plaquette_u1", "get_topo_u1",
+    "apply_gauge_trans_u1", "apply_ape_smear_u1",
     "PREC_DOUBLE", "PREC_SINGLE", "PREC_HALF", "PREC_BFLOAT",
 ]
 
@@ -700,8 +705,79 @@ class Generator:
         _capi.check(lib().glinalg_rng_gaussian(self.h, _dptr(C.c_void_p(v.ctypes.data)), C.c_long(n)), "gaussian")
         return v
 
+    def rand_trans_u1(self, lx, ly):
+        """rand_trans_u1 (u1_utils.cpp:116-126): a random U(1) gauge transform."""
+        g = np.zeros(lx * ly, np.complex128)
+        _capi.check(lib().glinalg_rng_trans_u1(self.h, _dptr(C.c_void_p(g.ctypes.data)), lx, ly), "trans")
+        return g
+
     def __del__(self):
         try:
             lib().glinalg_rng_destroy(self.h)
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------- U(1) gauge fields (u1_utils.h)
+
+def _flags(dev):
+    return GLINALG_PTR_DEVICE if dev else GLINALG_PTR_HOST
+
+
+def read_gauge_u1(gauge_field, x_len, y_len, input_file):
+    """read_gauge_u1 (u1_utils.cpp:17-38): fills the host array gauge_field from the
+    reference's text format."""
+    p, n, dev = _field_ptr(gauge_field, writable=True)
+    if dev or n < 2 * x_len * y_len:
+        raise ValueError("gauge_field must be a host array of 2*x_len*y_len entries")
+    _capi.check(lib().glinalg_read_gauge_u1(_dptr(p), x_len, y_len, os.fsencode(input_file)), "read_gauge_u1")
+
+
+def write_gauge_u1(gauge_field, x_len, y_len, output_file):
+    """write_gauge_u1 (u1_utils.cpp:44-65)."""
+    p, n, dev = _field_ptr(gauge_field)
+    if dev or n < 2 * x_len * y_len:
+        raise ValueError("gauge_field must be a host array of 2*x_len*y_len entries")
+    _capi.check(lib().glinalg_write_gauge_u1(_dptr(p), x_len, y_len, os.fsencode(output_file)), "write_gauge_u1")
+
+
+def unit_gauge_u1(gauge_field, x_len, y_len):
+    """unit_gauge_u1 (u1_utils.cpp:69-75)."""
+    p, _, dev = _field_ptr(gauge_field, writable=True)
+    _capi.check(lib().glinalg_unit_gauge_u1(_dptr(p), x_len, y_len, _flags(dev)), "unit_gauge_u1")
+
+
+def get_plaquette_u1(gauge_field, x_len, y_len):
+    """get_plaquette_u1 (u1_utils.cpp:190-207): the average plaquette (complex)."""
+    p, _, dev = _field_ptr(gauge_field)
+    out = np.zeros(2)
+    _capi.check(lib().glinalg_plaquette_u1(_dptr(p), x_len, y_len, out.ctypes.data_as(C.POINTER(C.c_double)),
+                                           _flags(dev)), "plaquette_u1")
+    return complex(out[0], out[1])
+
+
+def get_topo_u1(gauge_field, x_len, y_len):
+    """get_topo_u1 (u1_utils.cpp:210-226): the topological charge."""
+    p, _, dev = _field_ptr(gauge_field)
+    out = C.c_double()
+    _capi.check(lib().glinalg_topo_u1(_dptr(p), x_len, y_len, C.byref(out), _flags(dev)), "topo_u1")
+    return out.value
+
+
+def apply_gauge_trans_u1(gauge_field, gauge_trans, x_len, y_len):
+    """apply_gauge_trans_u1 (u1_utils.cpp:128-142), in place."""
+    p, _, dev = _field_ptr(gauge_field, writable=True)
+    g, _, gdev = _field_ptr(gauge_trans)
+    if dev != gdev:
+        raise ValueError("gauge_field and gauge_trans must both be on the host or both on the device")
+    _capi.check(lib().glinalg_apply_gauge_trans_u1(_dptr(p), _dptr(g), x_len, y_len, _flags(dev)), "gauge_trans")
+
+
+def apply_ape_smear_u1(smeared_field, gauge_field, x_len, y_len, alpha, n_iter):
+    """apply_ape_smear_u1 (u1_utils.cpp:145-187)."""
+    o, _, odev = _field_ptr(smeared_field, writable=True)
+    p, _, dev = _field_ptr(gauge_field)
+    if dev != odev:
+        raise ValueError("both fields must be on the host or both on the device")
+    _capi.check(lib().glinalg_apply_ape_smear_u1(_dptr(o), _dptr(p), x_len, y_len, float(alpha), int(n_iter),
+                                                 _flags(dev)), "ape_smear_u1")

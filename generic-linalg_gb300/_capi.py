@@ -115,6 +115,14 @@ def _prototypes():
         "glinalg_rng_gauge_u1": (st, [vp, _dp, i, i]),
         "glinalg_rng_gauss_gauge_u1": (st, [vp, _dp, i, i, d]),
         "glinalg_rng_gaussian": (st, [vp, _dp, l]),
+        "glinalg_rng_trans_u1": (st, [vp, _dp, i, i]),
+        "glinalg_read_gauge_u1": (st, [_dp, i, i, C.c_char_p]),
+        "glinalg_write_gauge_u1": (st, [_dp, i, i, C.c_char_p]),
+        "glinalg_unit_gauge_u1": (st, [_dp, i, i, i]),
+        "glinalg_plaquette_u1": (st, [_dp, i, i, _dp, i]),
+        "glinalg_topo_u1": (st, [_dp, i, i, _dp, i]),
+        "glinalg_apply_gauge_trans_u1": (st, [_dp, _dp, i, i, i]),
+        "glinalg_apply_ape_smear_u1": (st, [_dp, _dp, i, i, d, i, i]),
     }
 
 

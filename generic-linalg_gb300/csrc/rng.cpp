@@ -70,3 +70,13 @@ extern "C" glinalg_status glinalg_rng_gaussian(glinalg_rng rng, double *v, long 
     }
     return GLINALG_SUCCESS;
 }
+
+// rand_trans_u1 (u1_utils.cpp:116-126): lx*ly phases uniform in (-pi, pi).
+extern "C" glinalg_status glinalg_rng_trans_u1(glinalg_rng rng, double *trans, int lx, int ly)
+{
+    if (!rng || !trans || lx <= 0 || ly <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    std::uniform_real_distribution<> dist(-kPi, kPi);
+    std::complex<double> *g = reinterpret_cast<std::complex<double> *>(trans);
+    for (long i = 0; i < (long)lx * ly; i++) g[i] = std::polar(1.0, dist(rng->gen));
+    return GLINALG_SUCCESS;
+}

@@ -306,6 +306,27 @@ glinalg_status glinalg_gcr_var_precond_restart(glinalg_operator op, double *phi,
                                                const glinalg_solver_params *params,
                                                glinalg_info *info);
 
+/* ---- U(1) gauge fields (u1_utils.h); links are 2*lx*ly complex, U[2*i + mu] ---- */
+
+/* read_gauge_u1 / write_gauge_u1 (u1_utils.cpp:17 / :44): the reference's text format, one
+ * phase per line, x outermost, then y, then mu (fixed notation, 20 decimals on write).  Host
+ * arrays; read fails with GLINALG_ERROR_INVALID_VALUE if the file holds fewer phases. */
+glinalg_status glinalg_read_gauge_u1(double *links, int lx, int ly, const char *path);
+glinalg_status glinalg_write_gauge_u1(const double *links, int lx, int ly, const char *path);
+/* unit_gauge_u1 (u1_utils.cpp:69) */
+glinalg_status glinalg_unit_gauge_u1(double *links, int lx, int ly, int flags);
+/* get_plaquette_u1 (u1_utils.cpp:190): the average plaquette, out = (re, im) */
+glinalg_status glinalg_plaquette_u1(const double *links, int lx, int ly, double out[2], int flags);
+/* get_topo_u1 (u1_utils.cpp:210): sum of plaquette phases over 2 pi */
+glinalg_status glinalg_topo_u1(const double *links, int lx, int ly, double *out, int flags);
+/* apply_gauge_trans_u1 (u1_utils.cpp:128): U_mu(x) = g(x) U_mu(x) g(x+mu)^*, in place;
+ * trans: lx*ly complex */
+glinalg_status glinalg_apply_gauge_trans_u1(double *links, const double *trans, int lx, int ly, int flags);
+/* apply_ape_smear_u1 (u1_utils.cpp:145): n_iter APE sweeps with weight alpha, each projected
+ * back onto U(1); smeared and links may not overlap */
+glinalg_status glinalg_apply_ape_smear_u1(double *smeared, const double *links, int lx, int ly,
+                                          double alpha, int n_iter, int flags);
+
 /* ---- batched solves (no reference counterpart: the reference solves systems one at a
  * time in a loop; these run many independent systems in one device launch sequence) ---- */
 
@@ -396,6 +417,8 @@ glinalg_status glinalg_rng_gauge_u1(glinalg_rng rng, double *links, int lx, int 
 /* gauss_gauge_u1 (u1_utils.cpp:92-112): theta normal with variance 1/beta. */
 glinalg_status glinalg_rng_gauss_gauge_u1(glinalg_rng rng, double *links, int lx, int ly,
                                           double beta);
+/* rand_trans_u1 (u1_utils.cpp:116): a random gauge transform, lx*ly complex */
+glinalg_status glinalg_rng_trans_u1(glinalg_rng rng, double *trans, int lx, int ly);
 /* gaussian<complex> (generic_vector.h:48-60): re and im independent N(0,1). */
 glinalg_status glinalg_rng_gaussian(glinalg_rng rng, double *v, long n_complex);
 

@@ -1424,3 +1424,86 @@ void orc_vpgcr_restart(const orc_op *op, double *phi, const double *phi0, long s
     snprintf(nm, sizeof(nm), "Variably Preconditioned Restarted GCR(%d)", restart_freq);
     set_name(info, nm);
 }
+
+/* ================================================================ gauge-field utilities */
+
+#define ORC_PI 3.14159265358979323846
+
+/* u1_utils.cpp:190-207 (get_plaquette_u1): average of U_x(x) U_y(x+x) U_x(x+y)^* U_y(x)^*,
+ * summed in site order. */
+void orc_plaquette_u1(const double *links, int lx, int ly, double out[2])
+{
+    const cplx *U = CCX(links);
+    cplx plaq = 0.0, tmp;
+    for (int y = 0; y < ly; y++) {
+        for (int x = 0; x < lx; x++) {
+            tmp = U[2 * lx * y + 2 * x] * U[2 * lx * y + 2 * ((x + 1) % lx) + 1] *
+                  conj(U[2 * lx * ((y + 1) % ly) + 2 * x]) * conj(U[2 * lx * y + 2 * x + 1]);
+            plaq += tmp;
+        }
+    }
+    plaq = cdivr(plaq, (double)(lx * ly));
+    out[0] = creal(plaq);
+    out[1] = cimag(plaq);
+}
+
+/* u1_utils.cpp:210-226 (get_topo_u1): sum over plaquettes of arg(w), divided by 2 pi. */
+double orc_topo_u1(const double *links, int lx, int ly)
+{
+    const cplx *U = CCX(links);
+    double top = 0.0;
+    for (int y = 0; y < ly; y++) {
+        for (int x = 0; x < lx; x++) {
+            cplx w = U[y * lx * 2 + x * 2 + 0] * U[y * lx * 2 + ((x + 1) % lx) * 2 + 1] *
+                     conj(U[((y + 1) % ly) * lx * 2 + x * 2 + 0]) * conj(U[y * lx * 2 + x * 2 + 1]);
+            top += carg(w);
+        }
+    }
+    return 0.5 * top / ORC_PI;
+}
+
+/* u1_utils.cpp:128-142 (apply_gauge_trans_u1): U_mu(x) = g(x) U_mu(x) g(x + mu)^*, in place,
+ * in site order. */
+void orc_gauge_trans_u1(double *links, const double *trans, int lx, int ly)
+{
+    cplx *U = CX(links);
+    const cplx *g = CCX(trans);
+    for (int y = 0; y < ly; y++) {
+        for (int x = 0; x < lx; x++) {
+            U[2 * lx * y + 2 * x] = g[lx * y + x] * U[2 * lx * y + 2 * x] * conj(g[lx * y + (x + 1) % lx]);
+            U[2 * lx * y + 2 * x + 1] = g[lx * y + x] * U[2 * lx * y + 2 * x + 1] * conj(g[lx * ((y + 1) % ly) + x]);
+        }
+    }
+}
+
+/* std::polar(1.0, theta) of libstdc++: (cos theta, sin theta). */
+static inline cplx polar1(double th) { return mk(cos(th), sin(th)); }
+
+/* u1_utils.cpp:145-187 (apply_ape_smear_u1): n_iter sweeps of U + alpha (sum of the two
+ * staples), each projected back onto U(1) by its phase. */
+void orc_ape_smear_u1(double *smeared_, const double *links, int lx, int ly, double alpha, int n_iter)
+{
+    const long n2 = 2L * lx * ly;
+    cplx *S = CX(smeared_);
+    cplx *T = (cplx *)malloc(sizeof(cplx) * n2);
+    memcpy(T, links, sizeof(cplx) * n2);
+    for (int it = 0; it < n_iter; it++) {
+        for (int y = 0; y < ly; y++) {
+            const int yp = (y + 1) % ly, ym = (y - 1 + ly) % ly;
+            for (int x = 0; x < lx; x++) {
+                const int xp = (x + 1) % lx, xm = (x - 1 + lx) % lx;
+                cplx v = T[y * lx * 2 + x * 2 + 0];
+                v += alpha * T[y * lx * 2 + x * 2 + 1] * T[yp * lx * 2 + x * 2 + 0] * conj(T[y * lx * 2 + xp * 2 + 1]);
+                v += alpha * conj(T[ym * lx * 2 + x * 2 + 1]) * T[ym * lx * 2 + x * 2 + 0] * T[ym * lx * 2 + xp * 2 + 1];
+                S[y * lx * 2 + x * 2 + 0] = v;
+                v = T[y * lx * 2 + x * 2 + 1];
+                v += alpha * conj(T[y * lx * 2 + xm * 2 + 0]) * T[y * lx * 2 + xm * 2 + 1] * T[yp * lx * 2 + xm * 2 + 0];
+                v += alpha * T[y * lx * 2 + x * 2 + 0] * T[y * lx * 2 + xp * 2 + 1] * conj(T[yp * lx * 2 + x * 2 + 0]);
+                S[y * lx * 2 + x * 2 + 1] = v;
+            }
+        }
+        for (long i = 0; i < n2; i++) T[i] = polar1(carg(S[i]));
+    }
+    memcpy(S, T, sizeof(cplx) * n2);
+    free(T);
+}

@@ -136,6 +136,12 @@ void orc_vpgcr(const orc_op *op, double *phi, const double *phi0, long size, int
 void orc_vpgcr_restart(const orc_op *op, double *phi, const double *phi0, long size, int max_iter,
                        double eps, int restart_freq, const orc_precond *pc, orc_info *info);
 
+/* ---- gauge-field utilities (u1_utils.cpp) ---- */
+void orc_plaquette_u1(const double *links, int lx, int ly, double out[2]);
+double orc_topo_u1(const double *links, int lx, int ly);
+void orc_gauge_trans_u1(double *links, const double *trans, int lx, int ly);
+void orc_ape_smear_u1(double *smeared, const double *links, int lx, int ly, double alpha, int n_iter);
+
 /* Adjoint force for S = phi^dagger (D^dagger D + sigma)^-1 phi with respect to the link
  * angles theta_mu(x) (U = exp(i theta)), given X = (D^dagger D + sigma)^-1 phi and Y = D X:
  * dS/dtheta_mu(x) = -2 Re( Y^dagger (dD/dtheta_mu(x)) X ).  out has 2*lx*ly reals. */

@@ -148,6 +148,11 @@ class Oracle:
             getattr(L, n).argtypes = [P(OrcOp), _dp, _dp, C.c_long, C.c_int, C.c_double, C.c_int,
                                       P(OrcPrecond), P(OrcInfo)]
         L.orc_eoprec_prepare.argtypes = [P(OrcOp), _dp, _dp]
+        L.orc_plaquette_u1.argtypes = [_dp, C.c_int, C.c_int, _dp]
+        L.orc_topo_u1.argtypes = [_dp, C.c_int, C.c_int]
+        L.orc_topo_u1.restype = C.c_double
+        L.orc_gauge_trans_u1.argtypes = [_dp, _dp, C.c_int, C.c_int]
+        L.orc_ape_smear_u1.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int]
         L.orc_eoprec_reconstruct.argtypes = [P(OrcOp), _dp, _dp, _dp]
 
     def apply(self, op: Operator, rhs):
@@ -258,6 +263,24 @@ class Oracle:
                                            hist_cap)
         return phi, info.as_dict(), res
 
+    def plaquette(self, links, lx, ly):
+        out = np.zeros(2)
+        self.lib.orc_plaquette_u1(_ptr(np.ascontiguousarray(links)), lx, ly, _ptr(out))
+        return complex(out[0], out[1])
+
+    def topo(self, links, lx, ly):
+        return self.lib.orc_topo_u1(_ptr(np.ascontiguousarray(links)), lx, ly)
+
+    def gauge_trans(self, links, trans, lx, ly):
+        out = np.array(links, dtype=np.complex128)
+        self.lib.orc_gauge_trans_u1(_ptr(out), _ptr(np.ascontiguousarray(trans)), lx, ly)
+        return out
+
+    def ape_smear(self, links, lx, ly, alpha, n_iter):
+        out = np.zeros(2 * lx * ly, np.complex128)
+        self.lib.orc_ape_smear_u1(_ptr(out), _ptr(np.ascontiguousarray(links)), lx, ly, alpha, n_iter)
+        return out
+
     def staggered_force(self, links, mass, lx, ly, X, Y):
         out = np.zeros(2 * lx * ly)
         self.lib.orc_staggered_force(_ptr(np.ascontiguousarray(links)), mass, lx, ly,
@@ -290,6 +313,13 @@ class RefOracle:
                                                                C.c_int, C.c_char_p, C.c_int]
         L.ref_multishift2.argtypes = [C.c_int] + L.ref_cg_m.argtypes
         L.ref_eoprec_prepare.argtypes = opargs + [_dp, _dp]
+        L.ref_plaquette.argtypes = [_dp, C.c_int, C.c_int, _dp]
+        L.ref_topo.argtypes = [_dp, C.c_int, C.c_int]
+        L.ref_topo.restype = C.c_double
+        L.ref_gauge_trans.argtypes = [C.c_uint, _dp, _dp, C.c_int, C.c_int]
+        L.ref_ape_smear.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int]
+        L.ref_write_gauge.argtypes = [cp, _dp, C.c_int, C.c_int]
+        L.ref_unit_gauge.argtypes = [_dp, C.c_int, C.c_int]
         L.ref_eoprec_reconstruct.argtypes = opargs + [_dp, _dp, _dp]
 
     def make_inputs(self, seed, lx, ly, n_src=1, src_len=None):
@@ -405,3 +435,26 @@ class RefOracle:
         d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]),
              "ops_count": int(info[3]), "name": {"cr_m": "CR-M", "bicgstab_m": "BICGSTAB-M"}[solver]}
         return phi, d, res, log.value.decode()
+
+    def plaquette(self, links, lx, ly):
+        out = np.zeros(2)
+        self.lib.ref_plaquette(_ptr(np.ascontiguousarray(links)), lx, ly, _ptr(out))
+        return complex(out[0], out[1])
+
+    def topo(self, links, lx, ly):
+        return self.lib.ref_topo(_ptr(np.ascontiguousarray(links)), lx, ly)
+
+    def gauge_trans(self, seed, links, lx, ly):
+        """rand_trans_u1 from std::mt19937(seed), then apply_gauge_trans_u1; (links', trans)."""
+        out = np.array(links, dtype=np.complex128)
+        trans = np.zeros(lx * ly, np.complex128)
+        self.lib.ref_gauge_trans(seed, _ptr(out), _ptr(trans), lx, ly)
+        return out, trans
+
+    def ape_smear(self, links, lx, ly, alpha, n_iter):
+        out = np.zeros(2 * lx * ly, np.complex128)
+        self.lib.ref_ape_smear(_ptr(out), _ptr(np.ascontiguousarray(links)), lx, ly, alpha, n_iter)
+        return out
+
+    def write_gauge(self, path, links, lx, ly):
+        self.lib.ref_write_gauge(path.encode(), _ptr(np.ascontiguousarray(links)), lx, ly)

@@ -11,6 +11,8 @@
 
 #include <complex>
 #include <cstring>
+#include <fstream>
+#include <vector>
 #include <random>
 #include <sstream>
 #include <iostream>
@@ -369,5 +371,38 @@ void ref_multishift2(int solver, int kind, int lx, int ly, int nc, double mass, 
     for (int n = 0; n < n_shift; n++) resSqmrhs[n] = inv.resSqmrhs[n];
     delete o;
 }
+
+// Gauge-field utilities (u1_utils.cpp).
+void ref_plaquette(const double *links, int lx, int ly, double *out2)
+{
+    cd p = get_plaquette_u1((cd *)links, lx, ly);
+    out2[0] = p.real();
+    out2[1] = p.imag();
+}
+
+double ref_topo(const double *links, int lx, int ly) { return get_topo_u1((cd *)links, lx, ly); }
+
+// rand_trans_u1 from std::mt19937(seed), then apply_gauge_trans_u1 in place.
+void ref_gauge_trans(unsigned seed, double *links, double *trans, int lx, int ly)
+{
+    std::mt19937 gen(seed);
+    rand_trans_u1((cd *)trans, lx, ly, gen);
+    apply_gauge_trans_u1((cd *)links, (cd *)trans, lx, ly);
+}
+
+void ref_ape_smear(double *smeared, const double *links, int lx, int ly, double alpha, int n_iter)
+{
+    std::vector<cd> in((const cd *)links, (const cd *)links + 2L * lx * ly);
+    apply_ape_smear_u1((cd *)smeared, in.data(), lx, ly, alpha, n_iter);
+}
+
+void ref_write_gauge(const char *path, const double *links, int lx, int ly)
+{
+    // write_gauge_u1 opens with ios::in|ios::out|ios::trunc, which needs the file to exist
+    { std::ofstream touch(path); }
+    write_gauge_u1((cd *)links, lx, ly, std::string(path));
+}
+
+void ref_unit_gauge(double *links, int lx, int ly) { unit_gauge_u1((cd *)links, lx, ly); }
 
 }  // extern "C"

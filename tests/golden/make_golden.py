@@ -185,6 +185,25 @@ def main():
             info["cases"][key] = {**d, "resSqmrhs": res.tolist(), "log": log, "shifts": msh, "rfc": rfc,
                                   "worst_first": wf, "op": "laplace_m0.001" if op is lap else "staggered"}
 
+    # ---- gauge-field utilities (u1_utils.cpp): plaquette, topological charge, a random gauge
+    # transform (rand_trans_u1 from mt19937(99)), APE smearing, and the text format of
+    # write_gauge_u1 / read_gauge_u1
+    for key in ("l32", "l12x6", "g16"):
+        lx, ly = (lat[key][0], lat[key][1]) if key in lat else (16, 16)
+        U = vec[f"{key}_links"]
+        info["cases"][f"{key}_gauge"] = {"plaquette": [R.plaquette(U, lx, ly).real, R.plaquette(U, lx, ly).imag],
+                                         "topo": R.topo(U, lx, ly)}
+        Ut, g = R.gauge_trans(99, U, lx, ly)
+        vec[f"{key}_trans"], vec[f"{key}_links_trans"] = g, Ut
+        vec[f"{key}_ape"] = R.ape_smear(U, lx, ly, 0.5, 3)
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        pth = os.path.join(td, "g16.dat")
+        R.write_gauge(pth, vec["g16_links"], 16, 16)
+        text = open(pth).read()
+        vec["g16_links_read"] = R.read_gauge(pth, 16, 16)
+    info["cases"]["g16_gauge"]["text"] = text
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     with open(os.path.join(HERE, "reference_info.json"), "w") as f:
         json.dump(info, f, indent=1, default=lambda o: o.item() if hasattr(o, "item") else str(o))
