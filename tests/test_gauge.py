@@ -4,8 +4,8 @@ the host, and the device kernels (plaquette, topological charge, gauge transform
 smearing) on the GPU.
 
 Bars: oracle bit-exact; write_gauge_u1 text identical to the reference's; read_gauge_u1
-within 1 ulp of the reference's read (the same text through cos / sin); rand_trans_u1 bit-exact
-(same std::mt19937 stream); device plaquette and topological charge within 1e-13 (absolute:
+within 1 ulp of the reference's read (the same text through cos / sin); rand_trans_u1 the same
+phases (same std::mt19937 stream) within 1 ulp; device plaquette and topological charge within 1e-13 (absolute:
 both are sums of O(V) unit-size terms in another order), gauge transform within 1e-15 per
 link, APE smearing within 1e-13 per link (three sweeps of atan2, sin, cos on the device)."""
 from __future__ import annotations
@@ -58,9 +58,11 @@ def test_read_gauge_short_file_is_an_error(gl, tmp_path):
 
 
 def test_rand_trans_matches_reference(gl, golden):
+    """The same phases from the same std::mt19937 stream; cos / sin of another libm (the
+    fixtures were written on x86-64) may differ in the last bit."""
     vec, _ = golden
     for key, (lx, ly) in LATS.items():
-        assert np.array_equal(gl.Generator(99).rand_trans_u1(lx, ly), vec[f"{key}_trans"])
+        assert np.max(np.abs(gl.Generator(99).rand_trans_u1(lx, ly) - vec[f"{key}_trans"])) <= 2.3e-16
 
 
 def test_unit_gauge_host(gl):
