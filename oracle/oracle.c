@@ -71,8 +71,10 @@ static void laplace_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass
 }
 
 /* stencil_2d/coarse_stencil.cpp:12-172 (apply_stencil_2d, DIR_ALL), :395-460 (_eo) and
- * :560-625 (_oe).  parity: 0 = full stencil, 1 = even output sites only (hopping only),
- * 2 = odd output sites only (hopping only).  Site parity is even when x+y is even
+ * :560-625 (_oe), :725-1117 (_tb) and :1120-1512 (_bt).  parity: 0 = full stencil, 1 = even
+ * output sites only (hopping only), 2 = odd output sites only (hopping only), 3 = top half
+ * of the colours out, bottom half in (clover, hopping and two-link, no shifts), 4 = bottom
+ * out, top in.  Site parity is even when x+y is even
  * (lattice/lattice.h:128-139). */
 static void stencil_apply(const orc_op *op, cplx *lhs, const cplx *rhs, int parity)
 {
@@ -96,19 +98,23 @@ static void stencil_apply(const orc_op *op, cplx *lhs, const cplx *rhs, int pari
         cplx acc = 0.0;
         if (parity == 1 && !even) { lhs[i] = 0.0; continue; }
         if (parity == 2 && even) { lhs[i] = 0.0; continue; }
-        if (parity == 0)
-            for (int c = 0; c < nc; c++) acc += clov[c + (long)nc * i] * rhs[site * nc + c];
+        if (parity == 3 && color >= nc / 2) { lhs[i] = 0.0; continue; }
+        if (parity == 4 && color < nc / 2) { lhs[i] = 0.0; continue; }
+        /* tb (3) reads the bottom half of the input colours, bt (4) the top half */
+        const int c0 = parity == 3 ? nc / 2 : 0, c1 = parity == 4 ? nc / 2 : nc;
+        if (parity == 0 || parity >= 3)
+            for (int c = c0; c < c1; c++) acc += clov[c + (long)nc * i] * rhs[site * nc + c];
         for (int d = 0; d < 4; d++) {
             int xx = (x + hx[d] + lx) % lx, yy = (y + hy[d] + ly) % ly;
             long nb = ((long)yy * lx + xx) * nc;
-            for (int c = 0; c < nc; c++)
+            for (int c = c0; c < c1; c++)
                 acc += hop[c + (long)nc * i + (long)d * nc * lsize] * rhs[nb + c];
         }
-        if (parity == 0 && two != NULL) {
+        if ((parity == 0 || parity >= 3) && two != NULL) {
             for (int d = 0; d < 8; d++) {
                 int xx = (x + tx[d] + 2 * lx) % lx, yy = (y + ty[d] + 2 * ly) % ly;
                 long nb = ((long)yy * lx + xx) * nc;
-                for (int c = 0; c < nc; c++)
+                for (int c = c0; c < c1; c++)
                     acc += two[c + (long)nc * i + (long)d * nc * lsize] * rhs[nb + c];
             }
         }
@@ -211,10 +217,92 @@ void orc_eoprec_reconstruct(const orc_op *op, double *lhs_full_, const double *l
     }
 }
 
+/* The stencil operators of multigrid/aa_mg/mg_complex.cpp:1228-1375, nc = lattice colours:
+ *   m^2 - D_tb D_bt (top rows; bottom zeroed)           :1228-1249
+ *   m^2 - D_eo D_oe - D_oe D_eo                          :1277-1302
+ *   m^2 - D_tb D_bt - D_bt D_tb                          :1305-1330
+ *   epsilon D epsilon (epsilon = +1 on even sites)       :1335-1352
+ *   sigma3 D sigma3 (sigma3 = +1 on the top colours)     :1355-1372
+ * with m = the stencil's shift (complex, squared as shift * shift). */
+static void coarse_pieces_apply(const orc_op *op, cplx *lhs, const cplx *rhs)
+{
+    const int nc = op->nc;
+    const long n = (long)op->lx * op->ly * nc;
+    const cplx shift = mk(op->shift[0], op->shift[1]);
+    cplx *tmp = (cplx *)calloc(n, sizeof(cplx));
+    cplx *tmp2 = (cplx *)calloc(n, sizeof(cplx));
+    long i;
+    switch (op->kind) {
+    case ORC_STENCIL_M2MDTBDBT:
+        stencil_apply(op, tmp, rhs, 4);
+        stencil_apply(op, lhs, tmp, 3);
+        for (i = 0; i < n; i++)
+            if ((int)(i % nc) < nc / 2) lhs[i] = shift * shift * rhs[i] - lhs[i];
+        break;
+    case ORC_STENCIL_NORMAL_EO:
+    case ORC_STENCIL_NORMAL_TB: {
+        const int a = op->kind == ORC_STENCIL_NORMAL_EO ? 1 : 3, b = op->kind == ORC_STENCIL_NORMAL_EO ? 2 : 4;
+        stencil_apply(op, tmp2, rhs, a);
+        stencil_apply(op, lhs, tmp2, b);
+        stencil_apply(op, tmp2, rhs, b);
+        stencil_apply(op, tmp, tmp2, a);
+        for (i = 0; i < n; i++) lhs[i] = shift * shift * rhs[i] - lhs[i] - tmp[i];
+        break;
+    }
+    case ORC_STENCIL_DAGGER_EO:
+    case ORC_STENCIL_DAGGER_TB: {
+        /* lattice_epsilon / lattice_sigma3 (lattice/lattice_functions.h:11-55) */
+        const int eo = op->kind == ORC_STENCIL_DAGGER_EO;
+        for (int pass = 0; pass < 2; pass++) {
+            const cplx *src = pass == 0 ? rhs : tmp;
+            for (i = 0; i < n; i++) {
+                long site = i / nc;
+                int x = (int)(site % op->lx), y = (int)(site / op->lx);
+                int plus = eo ? ((x + y) % 2 == 0) : (nc % 2 != 0 || (int)(i % nc) < nc / 2);
+                lhs[i] = plus ? src[i] : -src[i];
+            }
+            if (pass == 0) stencil_apply(op, tmp, lhs, 0);
+        }
+        break;
+    }
+    default: break;
+    }
+    free(tmp);
+    free(tmp2);
+}
+
+/* apply_square_staggered_tbprec_prepare_stencil / _reconstruct_stencil
+ * (mg_complex.cpp:1211-1225 / :1252-1274): rhs_t = m rhs - D_tb rhs on the top colours
+ * (bottom zeroed); lhs_full = lhs_t on the top colours, (rhs_b - D_bt lhs_t) / Re(m) on the
+ * bottom ones. */
+void orc_tbprec_prepare(const orc_op *op, double *rhs_t_, const double *rhs_)
+{
+    cplx *rhs_t = CX(rhs_t_);
+    const cplx *rhs = CCX(rhs_);
+    const long n = (long)op->lx * op->ly * op->nc;
+    const cplx shift = mk(op->shift[0], op->shift[1]);
+    stencil_apply(op, rhs_t, rhs, 3);
+    for (long i = 0; i < n; i++)
+        if ((int)(i % op->nc) < op->nc / 2) rhs_t[i] = shift * rhs[i] - rhs_t[i];
+}
+
+void orc_tbprec_reconstruct(const orc_op *op, double *lhs_full_, const double *lhs_t_, const double *rhs_b_)
+{
+    cplx *lhs_full = CX(lhs_full_);
+    const cplx *lhs_t = CCX(lhs_t_), *rhs_b = CCX(rhs_b_);
+    const long n = (long)op->lx * op->ly * op->nc;
+    const double inv_mass = 1.0 / op->shift[0];
+    stencil_apply(op, lhs_full, lhs_t, 4);
+    for (long i = 0; i < n; i++) {
+        if ((int)(i % op->nc) >= op->nc / 2) lhs_full[i] = inv_mass * (rhs_b[i] - lhs_full[i]);
+        else lhs_full[i] = lhs_t[i];
+    }
+}
+
 long orc_op_size(const orc_op *op)
 {
     long v = (long)op->lx * op->ly;
-    if (op->kind >= ORC_STENCIL && op->kind <= ORC_STENCIL_OE) v *= op->nc;
+    if ((op->kind >= ORC_STENCIL && op->kind <= ORC_STENCIL_OE) || op->kind >= ORC_STENCIL_TB) v *= op->nc;
     return v;
 }
 
@@ -247,6 +335,13 @@ void orc_apply(const orc_op *op, double *lhs, const double *rhs)
     case ORC_STAGGERED_DOE: staggered_hop_parity(CX(lhs), CCX(rhs), U, op->lx, op->ly, 1); break;
     case ORC_STAGGERED_M2MDEODOE:
     case ORC_STENCIL_M2MDEODOE: m2mdeodoe_apply(op, CX(lhs), CCX(rhs)); break;
+    case ORC_STENCIL_TB: stencil_apply(op, CX(lhs), CCX(rhs), 3); break;
+    case ORC_STENCIL_BT: stencil_apply(op, CX(lhs), CCX(rhs), 4); break;
+    case ORC_STENCIL_M2MDTBDBT:
+    case ORC_STENCIL_NORMAL_EO:
+    case ORC_STENCIL_NORMAL_TB:
+    case ORC_STENCIL_DAGGER_EO:
+    case ORC_STENCIL_DAGGER_TB: coarse_pieces_apply(op, CX(lhs), CCX(rhs)); break;
     default: break;
     }
 }
@@ -1506,4 +1601,221 @@ void orc_ape_smear_u1(double *smeared_, const double *links, int lx, int ly, dou
     }
     memcpy(S, T, sizeof(cplx) * n2);
     free(T);
+}
+
+/* ================================================================ multigrid transfer */
+
+/* Fine index of (coarse site (xc, yc), fine offset (x, y) in the block, dof). */
+static inline long mg_fine_index(const orc_mg_level *lv, int x, int y, int dof)
+{
+    return ((long)y * lv->lx + x) * lv->nc_f + dof;
+}
+
+/* mg_complex.cpp:191-257 (block_normalize): every null vector normalised on every block. */
+void orc_mg_block_normalize(orc_mg_level *lv)
+{
+    const int xc_n = lv->lx / lv->bx, yc_n = lv->ly / lv->by;
+    const long fsize = (long)lv->lx * lv->ly * lv->nc_f;
+    const long csize = (long)xc_n * yc_n * lv->nc_c;
+    for (long i = 0; i < csize; i++) {
+        const int cd = (int)(i % lv->nc_c);
+        const long t = i / lv->nc_c;
+        const int xc = (int)(t % xc_n), yc = (int)(t / xc_n);
+        cplx *v = CX(lv->null_vectors) + (long)cd * fsize;
+        double norm = 0.0;
+        for (int y = yc * lv->by; y < yc * lv->by + lv->by; y++)
+            for (int x = xc * lv->bx; x < xc * lv->bx + lv->bx; x++)
+                for (int d = 0; d < lv->nc_f; d++) {
+                    const cplx z = v[mg_fine_index(lv, x, y, d)];
+                    norm += creal(conj(z) * z);
+                }
+        norm = sqrt(norm);
+        for (int y = yc * lv->by; y < yc * lv->by + lv->by; y++)
+            for (int x = xc * lv->bx; x < xc * lv->bx + lv->bx; x++)
+                for (int d = 0; d < lv->nc_f; d++) v[mg_fine_index(lv, x, y, d)] = cdivr(v[mg_fine_index(lv, x, y, d)], norm);
+    }
+}
+
+/* mg_complex.cpp:259-369 (block_orthonormalize): per block, modified Gram-Schmidt in the
+ * reference's order (normalise vector k-1, then project vector k against 0..k-1), then
+ * block_normalize. */
+void orc_mg_block_orthonormalize(orc_mg_level *lv)
+{
+    const int xc_n = lv->lx / lv->bx, yc_n = lv->ly / lv->by;
+    const long fsize = (long)lv->lx * lv->ly * lv->nc_f;
+    cplx *V = CX(lv->null_vectors);
+    for (long i = 0; i < (long)xc_n * yc_n; i++) {
+        const int xc = (int)(i % xc_n), yc = (int)(i / xc_n);
+        const int x0 = xc * lv->bx, y0 = yc * lv->by;
+        for (int cd = 1; cd < lv->nc_c; cd++) {
+            cplx *prev = V + (long)(cd - 1) * fsize, *cur = V + (long)cd * fsize;
+            double norm = 0.0;
+            for (int y = y0; y < y0 + lv->by; y++)
+                for (int x = x0; x < x0 + lv->bx; x++)
+                    for (int d = 0; d < lv->nc_f; d++) {
+                        const cplx z = prev[mg_fine_index(lv, x, y, d)];
+                        norm += creal(conj(z) * z);
+                    }
+            norm = sqrt(norm);
+            for (int y = y0; y < y0 + lv->by; y++)
+                for (int x = x0; x < x0 + lv->bx; x++)
+                    for (int d = 0; d < lv->nc_f; d++) {
+                        const long f = mg_fine_index(lv, x, y, d);
+                        prev[f] = cdivr(prev[f], norm);
+                    }
+            for (int m = 0; m < cd; m++) {
+                const cplx *vm = V + (long)m * fsize;
+                cplx dot = 0.0;
+                for (int y = y0; y < y0 + lv->by; y++)
+                    for (int x = x0; x < x0 + lv->bx; x++)
+                        for (int d = 0; d < lv->nc_f; d++) {
+                            const long f = mg_fine_index(lv, x, y, d);
+                            dot += conj(vm[f]) * cur[f];
+                        }
+                for (int y = y0; y < y0 + lv->by; y++)
+                    for (int x = x0; x < x0 + lv->bx; x++)
+                        for (int d = 0; d < lv->nc_f; d++) {
+                            const long f = mg_fine_index(lv, x, y, d);
+                            cur[f] -= dot * vm[f];
+                        }
+            }
+        }
+    }
+    orc_mg_block_normalize(lv);
+}
+
+/* mg_complex.cpp:372-418 (prolong): fine = sum over coarse dof of null_vector * coarse. */
+void orc_mg_prolong(const orc_mg_level *lv, double *fine_, const double *coarse_)
+{
+    const int xc_n = lv->lx / lv->bx, yc_n = lv->ly / lv->by;
+    const long fsize = (long)lv->lx * lv->ly * lv->nc_f;
+    const long csize = (long)xc_n * yc_n * lv->nc_c;
+    cplx *fine = CX(fine_);
+    const cplx *coarse = CCX(coarse_);
+    memset(fine, 0, sizeof(cplx) * fsize);
+    for (long i = 0; i < csize; i++) {
+        const int cd = (int)(i % lv->nc_c);
+        const long t = i / lv->nc_c;
+        const int xc = (int)(t % xc_n), yc = (int)(t / xc_n);
+        const cplx *v = CCX(lv->null_vectors) + (long)cd * fsize;
+        for (int y = yc * lv->by; y < yc * lv->by + lv->by; y++)
+            for (int x = xc * lv->bx; x < xc * lv->bx + lv->bx; x++)
+                for (int d = 0; d < lv->nc_f; d++) {
+                    const long f = mg_fine_index(lv, x, y, d);
+                    fine[f] += v[f] * coarse[i];
+                }
+    }
+}
+
+/* mg_complex.cpp:421-467 (restrict): coarse = P^dagger fine. */
+void orc_mg_restrict(const orc_mg_level *lv, double *coarse_, const double *fine_)
+{
+    const int xc_n = lv->lx / lv->bx, yc_n = lv->ly / lv->by;
+    const long fsize = (long)lv->lx * lv->ly * lv->nc_f;
+    const long csize = (long)xc_n * yc_n * lv->nc_c;
+    cplx *coarse = CX(coarse_);
+    const cplx *fine = CCX(fine_);
+    memset(coarse, 0, sizeof(cplx) * csize);
+    for (long i = 0; i < csize; i++) {
+        const int cd = (int)(i % lv->nc_c);
+        const long t = i / lv->nc_c;
+        const int xc = (int)(t % xc_n), yc = (int)(t / xc_n);
+        const cplx *v = CCX(lv->null_vectors) + (long)cd * fsize;
+        for (int y = yc * lv->by; y < yc * lv->by + lv->by; y++)
+            for (int x = xc * lv->bx; x < xc * lv->bx + lv->bx; x++)
+                for (int d = 0; d < lv->nc_f; d++) {
+                    const long f = mg_fine_index(lv, x, y, d);
+                    coarse[i] += conj(v[f]) * fine[f];
+                }
+    }
+}
+
+/* One direction of apply_stencil_2d (stencil_2d::sdir, coarse_stencil.cpp:164-235): dir 0 =
+ * clover and shifts, 1..4 = hopping +x, +y, -x, -y. */
+static void stencil_apply_dir(const orc_op *op, cplx *lhs, const cplx *rhs, int dir)
+{
+    const int lx = op->lx, ly = op->ly, nc = op->nc;
+    const long lsize = (long)lx * ly * nc;
+    const cplx *clov = CCX(op->clover), *hop = CCX(op->hopping);
+    const cplx shift = mk(op->shift[0], op->shift[1]);
+    const cplx eo_shift = mk(op->eo_shift[0], op->eo_shift[1]);
+    const cplx dof_shift = mk(op->dof_shift[0], op->dof_shift[1]);
+    static const int hx[4] = {1, 0, -1, 0}, hy[4] = {0, 1, 0, -1};
+    for (long i = 0; i < lsize; i++) {
+        const int color = (int)(i % nc);
+        const long site = i / nc;
+        const int x = (int)(site % lx), y = (int)(site / lx);
+        cplx acc = 0.0;
+        if (dir == 0) {
+            for (int c = 0; c < nc; c++) acc += clov[c + (long)nc * i] * rhs[site * nc + c];
+            if (cabs(shift) != 0.0) acc += shift * rhs[i];
+            if (cabs(eo_shift) != 0.0) acc += (((x + y) % 2 == 0 ? 1.0 : -1.0) * eo_shift) * rhs[i];
+            if (cabs(dof_shift) != 0.0) acc += ((color < nc / 2 ? 1.0 : -1.0) * dof_shift) * rhs[i];
+        } else {
+            const int d = dir - 1;
+            const int xx = (x + hx[d] + lx) % lx, yy = (y + hy[d] + ly) % ly;
+            const long nb = ((long)yy * lx + xx) * nc;
+            for (int c = 0; c < nc; c++) acc += hop[c + (long)nc * i + (long)d * nc * lsize] * rhs[nb + c];
+        }
+        lhs[i] = acc;
+    }
+}
+
+/* mg_complex.cpp:827-1199 (generate_coarse_from_fine_stencil): P^dagger A_dir P probed with
+ * unit coarse vectors, the clover first, then per coarse colour the +x, -x, +y, -y hopping
+ * terms on even and odd coarse rows / columns, accumulated in that order.  The probing reads
+ * each direction's neighbours on coarse sites of the other parity, so the coarse extents
+ * must be even (the reference's requirement). */
+void orc_mg_coarse_stencil(const orc_mg_level *lv, const orc_op *fine, int ignore_shifts, double *clover_,
+                           double *hopping_)
+{
+    const int xc_n = lv->lx / lv->bx, yc_n = lv->ly / lv->by, nc = lv->nc_c;
+    const long vc = (long)xc_n * yc_n, csize = vc * nc;
+    const long fsize = (long)lv->lx * lv->ly * lv->nc_f;
+    cplx *clover = CX(clover_), *hopping = CX(hopping_);
+    cplx *t_rhs = (cplx *)calloc(csize, sizeof(cplx)), *t_lhs = (cplx *)calloc(csize, sizeof(cplx));
+    cplx *Pr = (cplx *)calloc(fsize, sizeof(cplx)), *APr = (cplx *)calloc(fsize, sizeof(cplx));
+    orc_op f = *fine;
+    if (ignore_shifts) {
+        f.shift[0] = f.shift[1] = f.eo_shift[0] = f.eo_shift[1] = f.dof_shift[0] = f.dof_shift[1] = 0.0;
+    }
+    memset(clover, 0, sizeof(cplx) * vc * nc * nc);
+    memset(hopping, 0, sizeof(cplx) * 4 * vc * nc * nc);
+#define PROBE(dir)                                                  \
+    do {                                                            \
+        orc_mg_prolong(lv, (double *)Pr, (const double *)t_rhs);    \
+        stencil_apply_dir(&f, APr, Pr, dir);                        \
+        orc_mg_restrict(lv, (double *)t_lhs, (const double *)APr);  \
+    } while (0)
+    for (int color = 0; color < nc; color++) {
+        memset(t_rhs, 0, sizeof(cplx) * csize);
+        for (long i = 0; i < vc; i++) t_rhs[i * nc + color] = 1.0;
+        PROBE(0);
+        for (long i = 0; i < csize; i++) clover[color + (long)nc * i] += t_lhs[i];
+    }
+    /* direction (1..4), its hopping slot, whether it runs along y */
+    static const int dirs[4] = {1, 3, 2, 4}, slot[4] = {0, 2, 1, 3}, alongy[4] = {0, 0, 1, 1};
+    for (int color = 0; color < nc; color++) {
+        for (int k = 0; k < 4; k++) {
+            for (int par = 0; par < 2; par++) {
+                memset(t_rhs, 0, sizeof(cplx) * csize);
+                for (long s = 0; s < vc; s++) {
+                    const int xc = (int)(s % xc_n), yc = (int)(s / xc_n);
+                    const int p = alongy[k] ? (yc % 2) : (int)(s % 2);
+                    (void)xc;
+                    if (p == par) t_rhs[s * nc + color] = 1.0;
+                }
+                PROBE(dirs[k]);
+                for (long i = 0; i < csize; i++) {
+                    const long s = i / nc;
+                    const int xc = (int)(s % xc_n), yc = (int)(s / xc_n);
+                    const int p = alongy[k] ? (yc % 2) : (xc % 2);
+                    if (p == par) clover[color + (long)nc * i] += t_lhs[i];
+                    else hopping[color + (long)nc * i + (long)slot[k] * nc * csize] += t_lhs[i];
+                }
+            }
+        }
+    }
+#undef PROBE
+    free(t_rhs); free(t_lhs); free(Pr); free(APr);
 }

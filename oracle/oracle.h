@@ -40,7 +40,14 @@ enum orc_kind {
     ORC_STAGGERED_DEO = 7,    /* square_staggered_deo_u1 */
     ORC_STAGGERED_DOE = 8,    /* square_staggered_doe_u1 */
     ORC_STAGGERED_M2MDEODOE = 9, /* square_staggered_m2mdeodoe_u1 */
-    ORC_STENCIL_M2MDEODOE = 10   /* apply_square_staggered_m2mdeodoe_stencil */
+    ORC_STENCIL_M2MDEODOE = 10,  /* apply_square_staggered_m2mdeodoe_stencil */
+    ORC_STENCIL_TB = 11,         /* apply_stencil_2d_tb */
+    ORC_STENCIL_BT = 12,         /* apply_stencil_2d_bt */
+    ORC_STENCIL_M2MDTBDBT = 13,  /* apply_square_staggered_m2mdtbdbt_stencil (mg_complex.cpp) */
+    ORC_STENCIL_NORMAL_EO = 14,  /* apply_square_staggered_normal_eo_stencil */
+    ORC_STENCIL_NORMAL_TB = 15,  /* apply_square_staggered_normal_tb_stencil */
+    ORC_STENCIL_DAGGER_EO = 16,  /* apply_square_staggered_dagger_eo_stencil */
+    ORC_STENCIL_DAGGER_TB = 17   /* apply_square_staggered_dagger_tb_stencil */
 };
 
 typedef struct {
@@ -72,6 +79,26 @@ long orc_op_size(const orc_op *op); /* number of complex entries of a field */
  * lhs_full = lhs_e on even sites, (rhs_o - D_oe lhs_e) / m on odd sites. */
 void orc_eoprec_prepare(const orc_op *op, double *rhs_e, const double *rhs);
 void orc_eoprec_reconstruct(const orc_op *op, double *lhs_full, const double *lhs_e, const double *rhs_o);
+
+/* Top/bottom preconditioning of a coarse stencil (ORC_STENCIL_M2MDTBDBT). */
+void orc_tbprec_prepare(const orc_op *op, double *rhs_t, const double *rhs);
+void orc_tbprec_reconstruct(const orc_op *op, double *lhs_full, const double *lhs_t, const double *rhs_b);
+
+/* One multigrid level (mg_operator_struct_complex at its current level): a fine lattice
+ * lx x ly with nc_f dof per site blocked bx x by into (lx/bx) x (ly/by) coarse sites with nc_c
+ * dof; null_vectors holds nc_c fields of lx*ly*nc_f complex, index (y*lx + x)*nc_f + dof. */
+typedef struct {
+    int lx, ly, nc_f, bx, by, nc_c;
+    double *null_vectors;
+} orc_mg_level;
+void orc_mg_block_normalize(orc_mg_level *lv);
+void orc_mg_block_orthonormalize(orc_mg_level *lv);
+void orc_mg_prolong(const orc_mg_level *lv, double *fine, const double *coarse);
+void orc_mg_restrict(const orc_mg_level *lv, double *coarse, const double *fine);
+/* generate_coarse_from_fine_stencil: coarse clover (V_c*nc_c*nc_c) and hopping (4*that) of
+ * P^dagger A P for a stencil-kind fine operator (its clover, 4 hops and shifts). */
+void orc_mg_coarse_stencil(const orc_mg_level *lv, const orc_op *fine, int ignore_shifts, double *clover,
+                           double *hopping);
 
 /* Stencil builders (fill hopping[4*V], clover untouched, shift = mass). */
 void orc_staggered_stencil(double *hopping, const double *links, int lx, int ly, int dagger);

@@ -34,6 +34,13 @@ KIND = {
     "staggered_doe": 8,
     "staggered_m2mdeodoe": 9,
     "stencil_m2mdeodoe": 10,
+    "stencil_tb": 11,
+    "stencil_bt": 12,
+    "stencil_m2mdtbdbt": 13,
+    "stencil_normal_eo": 14,
+    "stencil_normal_tb": 15,
+    "stencil_dagger_eo": 16,
+    "stencil_dagger_tb": 17,
 }
 
 _dp = C.POINTER(C.c_double)
@@ -102,11 +109,17 @@ class Operator:
     @property
     def size(self):
         v = self.lx * self.ly
-        return v * self.nc if KIND["stencil"] <= self.kind <= KIND["stencil_oe"] else v
+        return v * self.nc if (KIND["stencil"] <= self.kind <= KIND["stencil_oe"] or
+                               self.kind >= KIND["stencil_tb"]) else v
 
     def shifts6(self):
         return np.array([self.shift.real, self.shift.imag, self.eo_shift.real,
                          self.eo_shift.imag, self.dof_shift.real, self.dof_shift.imag])
+
+
+class OrcMgLevel(C.Structure):
+    _fields_ = [("lx", C.c_int), ("ly", C.c_int), ("nc_f", C.c_int), ("bx", C.c_int), ("by", C.c_int),
+                ("nc_c", C.c_int), ("null_vectors", _dp)]
 
 
 class Oracle:
@@ -149,6 +162,13 @@ class Oracle:
                                       P(OrcPrecond), P(OrcInfo)]
         L.orc_eoprec_prepare.argtypes = [P(OrcOp), _dp, _dp]
         L.orc_plaquette_u1.argtypes = [_dp, C.c_int, C.c_int, _dp]
+        L.orc_tbprec_prepare.argtypes = [P(OrcOp), _dp, _dp]
+        L.orc_tbprec_reconstruct.argtypes = [P(OrcOp), _dp, _dp, _dp]
+        for n in ("orc_mg_block_normalize", "orc_mg_block_orthonormalize"):
+            getattr(L, n).argtypes = [P(OrcMgLevel)]
+        L.orc_mg_prolong.argtypes = [P(OrcMgLevel), _dp, _dp]
+        L.orc_mg_restrict.argtypes = [P(OrcMgLevel), _dp, _dp]
+        L.orc_mg_coarse_stencil.argtypes = [P(OrcMgLevel), P(OrcOp), C.c_int, _dp, _dp]
         L.orc_topo_u1.argtypes = [_dp, C.c_int, C.c_int]
         L.orc_topo_u1.restype = C.c_double
         L.orc_gauge_trans_u1.argtypes = [_dp, _dp, C.c_int, C.c_int]
@@ -263,6 +283,52 @@ class Oracle:
                                            hist_cap)
         return phi, info.as_dict(), res
 
+    def tbprec_prepare(self, op: Operator, rhs):
+        rhs = np.ascontiguousarray(rhs, dtype=np.complex128)
+        out = np.empty_like(rhs)
+        self.lib.orc_tbprec_prepare(C.byref(op.struct), _ptr(out), _ptr(rhs))
+        return out
+
+    def tbprec_reconstruct(self, op: Operator, lhs_t, rhs_b):
+        lhs_t = np.ascontiguousarray(lhs_t, dtype=np.complex128)
+        rhs_b = np.ascontiguousarray(rhs_b, dtype=np.complex128)
+        out = np.empty_like(lhs_t)
+        self.lib.orc_tbprec_reconstruct(C.byref(op.struct), _ptr(out), _ptr(lhs_t), _ptr(rhs_b))
+        return out
+
+    @staticmethod
+    def _mg(lx, ly, nc_f, bx, by, nc_c, nv):
+        return OrcMgLevel(lx, ly, nc_f, bx, by, nc_c, _ptr(nv))
+
+    def mg_block(self, which, lx, ly, nc_f, bx, by, nc_c, null_vectors):
+        """which: "normalize" or "orthonormalize"; returns the new vectors (nc_c, lx*ly*nc_f)."""
+        nv = np.array(null_vectors, dtype=np.complex128).reshape(nc_c, -1).copy()
+        lv = self._mg(lx, ly, nc_f, bx, by, nc_c, nv)
+        getattr(self.lib, f"orc_mg_block_{which}")(C.byref(lv))
+        return nv
+
+    def mg_prolong(self, lx, ly, nc_f, bx, by, nc_c, null_vectors, coarse):
+        nv = np.ascontiguousarray(null_vectors, dtype=np.complex128)
+        out = np.zeros(lx * ly * nc_f, np.complex128)
+        self.lib.orc_mg_prolong(C.byref(self._mg(lx, ly, nc_f, bx, by, nc_c, nv)), _ptr(out),
+                                _ptr(np.ascontiguousarray(coarse, dtype=np.complex128)))
+        return out
+
+    def mg_restrict(self, lx, ly, nc_f, bx, by, nc_c, null_vectors, fine):
+        nv = np.ascontiguousarray(null_vectors, dtype=np.complex128)
+        out = np.zeros((lx // bx) * (ly // by) * nc_c, np.complex128)
+        self.lib.orc_mg_restrict(C.byref(self._mg(lx, ly, nc_f, bx, by, nc_c, nv)), _ptr(out),
+                                 _ptr(np.ascontiguousarray(fine, dtype=np.complex128)))
+        return out
+
+    def mg_coarse_stencil(self, lx, ly, nc_f, bx, by, nc_c, null_vectors, fine: Operator, ignore_shifts=False):
+        nv = np.ascontiguousarray(null_vectors, dtype=np.complex128)
+        vc = (lx // bx) * (ly // by) * nc_c * nc_c
+        clov, hop = np.zeros(vc, np.complex128), np.zeros(4 * vc, np.complex128)
+        self.lib.orc_mg_coarse_stencil(C.byref(self._mg(lx, ly, nc_f, bx, by, nc_c, nv)), C.byref(fine.struct),
+                                       int(ignore_shifts), _ptr(clov), _ptr(hop))
+        return clov, hop
+
     def plaquette(self, links, lx, ly):
         out = np.zeros(2)
         self.lib.orc_plaquette_u1(_ptr(np.ascontiguousarray(links)), lx, ly, _ptr(out))
@@ -314,6 +380,10 @@ class RefOracle:
         L.ref_multishift2.argtypes = [C.c_int] + L.ref_cg_m.argtypes
         L.ref_eoprec_prepare.argtypes = opargs + [_dp, _dp]
         L.ref_plaquette.argtypes = [_dp, C.c_int, C.c_int, _dp]
+        L.ref_tbprec.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_mg_block.argtypes = [C.c_int] + [C.c_int] * 6 + [_dp]
+        L.ref_mg_transfer.argtypes = [C.c_int] + [C.c_int] * 6 + [_dp, _dp, _dp]
+        L.ref_mg_coarse.argtypes = [C.c_int] * 6 + [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp]
         L.ref_topo.argtypes = [_dp, C.c_int, C.c_int]
         L.ref_topo.restype = C.c_double
         L.ref_gauge_trans.argtypes = [C.c_uint, _dp, _dp, C.c_int, C.c_int]
@@ -458,3 +528,38 @@ class RefOracle:
 
     def write_gauge(self, path, links, lx, ly):
         self.lib.ref_write_gauge(path.encode(), _ptr(np.ascontiguousarray(links)), lx, ly)
+
+    def tbprec(self, step, op: Operator, a, b=None):
+        """step 0: tbprec prepare (a = rhs); step 1: reconstruct (a = lhs_t, b = rhs_b)."""
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        out = np.zeros_like(a)
+        self.lib.ref_tbprec(step, op.lx, op.ly, op.nc, _ptr(op.clover), _ptr(op.hopping), _ptr(op.shifts6()),
+                            _ptr(out), _ptr(a), _ptr(None if b is None else np.ascontiguousarray(b)))
+        return out
+
+    def mg_block(self, which, lx, ly, nc_f, bx, by, nc_c, null_vectors):
+        nv = np.array(null_vectors, dtype=np.complex128).reshape(nc_c, -1).copy()
+        self.lib.ref_mg_block({"normalize": 0, "orthonormalize": 1}[which], lx, ly, nc_f, bx, by, nc_c, _ptr(nv))
+        return nv
+
+    def mg_prolong(self, lx, ly, nc_f, bx, by, nc_c, null_vectors, coarse):
+        nv = np.array(null_vectors, dtype=np.complex128)
+        out = np.zeros(lx * ly * nc_f, np.complex128)
+        self.lib.ref_mg_transfer(0, lx, ly, nc_f, bx, by, nc_c, _ptr(nv), _ptr(out),
+                                 _ptr(np.ascontiguousarray(coarse, dtype=np.complex128)))
+        return out
+
+    def mg_restrict(self, lx, ly, nc_f, bx, by, nc_c, null_vectors, fine):
+        nv = np.array(null_vectors, dtype=np.complex128)
+        out = np.zeros((lx // bx) * (ly // by) * nc_c, np.complex128)
+        self.lib.ref_mg_transfer(1, lx, ly, nc_f, bx, by, nc_c, _ptr(nv), _ptr(out),
+                                 _ptr(np.ascontiguousarray(fine, dtype=np.complex128)))
+        return out
+
+    def mg_coarse_stencil(self, lx, ly, nc_f, bx, by, nc_c, null_vectors, fine: Operator, ignore_shifts=False):
+        nv = np.array(null_vectors, dtype=np.complex128)
+        vc = (lx // bx) * (ly // by) * nc_c * nc_c
+        clov, hop = np.zeros(vc, np.complex128), np.zeros(4 * vc, np.complex128)
+        self.lib.ref_mg_coarse(lx, ly, nc_f, bx, by, nc_c, _ptr(nv), _ptr(fine.clover), _ptr(fine.hopping),
+                               _ptr(fine.shifts6()), int(ignore_shifts), _ptr(clov), _ptr(hop))
+        return clov, hop

@@ -38,6 +38,7 @@
 #include "coarse_stencil.h"
 #include "operators_stencil.h"
 #include "u1_utils.h"
+#include "mg_complex.h"
 
 using cd = std::complex<double>;
 typedef void (*mv_fn)(cd *, cd *, void *);
@@ -61,8 +62,9 @@ struct RefOp {
 };
 
 // kind: 0 D, 1 D^dagger, 2 D^dagger D, 3 gauge Laplacian, 4 stencil, 5 stencil_eo,
-// 6 stencil_oe, 7 D_eo, 8 D_oe, 9 m^2 - D_eo D_oe, 10 its stencil form (same numbering as
-// oracle.h).
+// 6 stencil_oe, 7 D_eo, 8 D_oe, 9 m^2 - D_eo D_oe, 10 its stencil form, 11 stencil_tb,
+// 12 stencil_bt, 13 m^2 - D_tb D_bt, 14 normal_eo, 15 normal_tb, 16 dagger_eo, 17 dagger_tb
+// (same numbering as oracle.h).
 RefOp *make_op(int kind, int lx, int ly, int nc, double mass, const double *links,
                const double *clover, const double *hopping, const double *two_link,
                const double *shifts6)
@@ -98,9 +100,19 @@ RefOp *make_op(int kind, int lx, int ly, int nc, double mass, const double *link
             o->st->dof_shift = cd(shifts6[4], shifts6[5]);
         }
         o->st->generated = true;
-        o->fn = kind == 4 ? apply_stencil_2d
-                          : kind == 5 ? apply_stencil_2d_eo
-                          : kind == 6 ? apply_stencil_2d_oe : apply_square_staggered_m2mdeodoe_stencil;
+        switch (kind) {
+        case 4: o->fn = apply_stencil_2d; break;
+        case 5: o->fn = apply_stencil_2d_eo; break;
+        case 6: o->fn = apply_stencil_2d_oe; break;
+        case 10: o->fn = apply_square_staggered_m2mdeodoe_stencil; break;
+        case 11: o->fn = apply_stencil_2d_tb; break;
+        case 12: o->fn = apply_stencil_2d_bt; break;
+        case 13: o->fn = apply_square_staggered_m2mdtbdbt_stencil; break;
+        case 14: o->fn = apply_square_staggered_normal_eo_stencil; break;
+        case 15: o->fn = apply_square_staggered_normal_tb_stencil; break;
+        case 16: o->fn = apply_square_staggered_dagger_eo_stencil; break;
+        default: o->fn = apply_square_staggered_dagger_tb_stencil; break;
+        }
         o->size = (long)lx * ly * nc;
         break;
     }
@@ -404,5 +416,110 @@ void ref_write_gauge(const char *path, const double *links, int lx, int ly)
 }
 
 void ref_unit_gauge(double *links, int lx, int ly) { unit_gauge_u1((cd *)links, lx, ly); }
+
+// Top/bottom preconditioning steps of a coarse stencil (mg_complex.cpp:1211, :1252).
+void ref_tbprec(int step, int lx, int ly, int nc, const double *clover, const double *hopping,
+                const double *shifts6, double *out, const double *a, const double *b)
+{
+    RefOp *o = make_op(13, lx, ly, nc, 0.0, nullptr, clover, hopping, nullptr, shifts6);
+    std::vector<cd> va((const cd *)a, (const cd *)a + o->size);
+    if (step == 0) {
+        apply_square_staggered_tbprec_prepare_stencil((cd *)out, va.data(), o->st);
+    } else {
+        std::vector<cd> vb((const cd *)b, (const cd *)b + o->size);
+        apply_square_staggered_tbprec_reconstruct_stencil((cd *)out, va.data(), vb.data(), o->st);
+    }
+    delete o;
+}
+
+namespace {
+// A one-level mg_operator_struct_complex (mg_complex.h) at level 0 over the given null vectors.
+struct RefMg {
+    mg_operator_struct_complex s;
+    int bx[1], by[1], nv[1];
+    Lattice *lat[2];
+    cd **vecs_level[1];
+    std::vector<cd *> vecs;
+    RefMg(int lx, int ly, int nc_f, int bxs, int bys, int nc_c, double *null_vectors)
+    {
+        int df[2] = {lx, ly}, dc[2] = {lx / bxs, ly / bys};
+        lat[0] = new Lattice(2, df, nc_f);
+        lat[1] = new Lattice(2, dc, nc_c);
+        bx[0] = bxs;
+        by[0] = bys;
+        nv[0] = nc_c;
+        const long fsize = (long)lx * ly * nc_f;
+        for (int c = 0; c < nc_c; c++) vecs.push_back((cd *)null_vectors + c * fsize);
+        vecs_level[0] = vecs.data();
+        s.x_fine = lx;
+        s.y_fine = ly;
+        s.n_refine = 1;
+        s.blocksize_x = bx;
+        s.blocksize_y = by;
+        s.Nc = nc_f;
+        s.latt = lat;
+        s.stencils = nullptr;
+        s.have_dagger_stencil = false;
+        s.dagger_stencils = nullptr;
+        s.n_vectors = nv;
+        s.null_vectors = vecs_level;
+        s.curr_level = 0;
+        s.curr_dof_fine = nc_f;
+        s.curr_x_fine = lx;
+        s.curr_y_fine = ly;
+        s.curr_fine_size = (int)fsize;
+        s.curr_dof_coarse = nc_c;
+        s.curr_x_coarse = dc[0];
+        s.curr_y_coarse = dc[1];
+        s.curr_coarse_size = dc[0] * dc[1] * nc_c;
+        s.dslash_count = nullptr;
+    }
+    ~RefMg()
+    {
+        delete lat[0];
+        delete lat[1];
+    }
+};
+}  // namespace
+
+// op: 0 block_normalize, 1 block_orthonormalize (null_vectors in place)
+void ref_mg_block(int op, int lx, int ly, int nc_f, int bx, int by, int nc_c, double *null_vectors)
+{
+    RefMg m(lx, ly, nc_f, bx, by, nc_c, null_vectors);
+    if (op == 0) block_normalize(&m.s);
+    else block_orthonormalize(&m.s);
+}
+
+// dir: 0 prolong (coarse -> fine), 1 restrict (fine -> coarse)
+void ref_mg_transfer(int dir, int lx, int ly, int nc_f, int bx, int by, int nc_c, double *null_vectors,
+                     double *out, const double *in)
+{
+    RefMg m(lx, ly, nc_f, bx, by, nc_c, null_vectors);
+    const long n_in = dir == 0 ? (long)m.s.curr_coarse_size : (long)m.s.curr_fine_size;
+    std::vector<cd> v((const cd *)in, (const cd *)in + n_in);
+    if (dir == 0) prolong((cd *)out, v.data(), &m.s);
+    else restrict((cd *)out, v.data(), &m.s);
+}
+
+// generate_coarse_from_fine_stencil for a fine stencil (clover, hopping, shifts; no two-link)
+void ref_mg_coarse(int lx, int ly, int nc_f, int bx, int by, int nc_c, double *null_vectors,
+                   const double *fclover, const double *fhopping, const double *shifts6, int ignore_shifts,
+                   double *cclover, double *chopping)
+{
+    RefMg m(lx, ly, nc_f, bx, by, nc_c, null_vectors);
+    stencil_2d fine(m.lat[0], 1);
+    const long vf = (long)lx * ly * nc_f * nc_f;
+    std::memcpy(fine.clover, fclover, sizeof(cd) * vf);
+    std::memcpy(fine.hopping, fhopping, sizeof(cd) * vf * 4);
+    fine.shift = cd(shifts6[0], shifts6[1]);
+    fine.eo_shift = cd(shifts6[2], shifts6[3]);
+    fine.dof_shift = cd(shifts6[4], shifts6[5]);
+    fine.generated = true;
+    stencil_2d coarse(m.lat[1], 1);
+    generate_coarse_from_fine_stencil(&coarse, &fine, &m.s, ignore_shifts != 0);
+    const long vc = (long)(lx / bx) * (ly / by) * nc_c * nc_c;
+    std::memcpy(cclover, coarse.clover, sizeof(cd) * vc);
+    std::memcpy(chopping, coarse.hopping, sizeof(cd) * vc * 4);
+}
 
 }  // extern "C"

@@ -204,6 +204,56 @@ def main():
         vec["g16_links_read"] = R.read_gauge(pth, 16, 16)
     info["cases"]["g16_gauge"]["text"] = text
 
+    # ---- multigrid transfer and coarse operators (multigrid/aa_mg/mg_complex.cpp): a 16x16
+    # staggered stencil (m = 0.1, plus eo_shift and dof_shift so that the shift projection is
+    # exercised) blocked 4x4 with 4 null vectors (Gaussian, numpy seed 5) into a 4x4 lattice
+    # with 4 dof; that coarse stencil blocked 2x2 with 4 vectors into 2x2x4; the stencil
+    # pieces of the coarse level (tb, bt, m^2 - D_tb D_bt, normal_eo / normal_tb,
+    # dagger_eo / dagger_tb) and the top/bottom prepare / reconstruct steps
+    rng = np.random.default_rng(5)
+    lx, ly = 16, 16
+    U16, s16 = R.make_inputs(1337, lx, ly, 1)
+    hop, sh = R.staggered_stencil(U16, lx, ly, 0.1, False)
+    mgcase = {"lx": lx, "ly": ly, "bx": 4, "by": 4, "nc_c": 4, "shift": [sh.real, sh.imag],
+              "eo_shift": [0.03, -0.01], "dof_shift": [0.0, 0.0]}
+    vec.update({"mg16_links": U16, "mg16_src": s16[0], "mg16_hop": hop})
+    fine = Op("stencil", lx, ly, nc=1, clover=np.zeros(lx * ly, np.complex128), hopping=hop, shift=sh,
+              eo_shift=complex(*mgcase["eo_shift"]))
+    nv = rng.normal(size=(4, lx * ly)) + 1j * rng.normal(size=(4, lx * ly))
+    vec["mg16_nv_in"] = nv.reshape(-1)
+    vec["mg16_nv_norm"] = R.mg_block("normalize", lx, ly, 1, 4, 4, 4, nv).reshape(-1)
+    P = R.mg_block("orthonormalize", lx, ly, 1, 4, 4, 4, nv)
+    vec["mg16_nv_orth"] = P.reshape(-1)
+    vc = rng.normal(size=64) + 1j * rng.normal(size=64)
+    vec["mg16_coarse_in"] = vc
+    vec["mg16_prolong"] = R.mg_prolong(lx, ly, 1, 4, 4, 4, P, vc)
+    vec["mg16_restrict"] = R.mg_restrict(lx, ly, 1, 4, 4, 4, P, s16[0])
+    for ig in (0, 1):
+        cl, hp = R.mg_coarse_stencil(lx, ly, 1, 4, 4, 4, P, fine, bool(ig))
+        vec[f"mg16_coarse_clover_ig{ig}"], vec[f"mg16_coarse_hop_ig{ig}"] = cl, hp
+    info["cases"]["mg16"] = mgcase
+    # second level: the coarse stencil (shifts kept) blocked 2x2 with 4 vectors
+    cl, hp = vec["mg16_coarse_clover_ig0"], vec["mg16_coarse_hop_ig0"]
+    lev2 = Op("stencil", 4, 4, nc=4, clover=cl, hopping=hp)
+    nv2 = rng.normal(size=(4, 64)) + 1j * rng.normal(size=(4, 64))
+    vec["mg4_nv_in"] = nv2.reshape(-1)
+    P2 = R.mg_block("orthonormalize", 4, 4, 4, 2, 2, 4, nv2)
+    vec["mg4_nv_orth"] = P2.reshape(-1)
+    vc2 = rng.normal(size=16) + 1j * rng.normal(size=16)
+    vec["mg4_coarse_in"] = vc2
+    vec["mg4_prolong"] = R.mg_prolong(4, 4, 4, 2, 2, 4, P2, vc2)
+    vec["mg4_restrict"] = R.mg_restrict(4, 4, 4, 2, 2, 4, P2, vc)
+    vec["mg4_coarse_clover"], vec["mg4_coarse_hop"] = R.mg_coarse_stencil(4, 4, 4, 2, 2, 4, P2, lev2, False)
+    # coarse-level stencil pieces on the 4x4x4 stencil with shift 0.1 + 0.02i
+    xin = rng.normal(size=64) + 1j * rng.normal(size=64)
+    vec["mg16_piece_in"] = xin
+    for k in ("stencil_tb", "stencil_bt", "stencil_m2mdtbdbt", "stencil_normal_eo", "stencil_normal_tb",
+              "stencil_dagger_eo", "stencil_dagger_tb"):
+        vec[f"mg16_{k}"] = R.apply(Op(k, 4, 4, nc=4, clover=cl, hopping=hp, shift=0.1 + 0.02j), xin)
+    tbop = Op("stencil_m2mdtbdbt", 4, 4, nc=4, clover=cl, hopping=hp, shift=0.1)
+    vec["mg16_tb_prepare"] = R.tbprec(0, tbop, xin)
+    vec["mg16_tb_reconstruct"] = R.tbprec(1, tbop, vc, xin)
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     with open(os.path.join(HERE, "reference_info.json"), "w") as f:
         json.dump(info, f, indent=1, default=lambda o: o.item() if hasattr(o, "item") else str(o))
