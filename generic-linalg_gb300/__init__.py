@@ -55,6 +55,12 @@ __all__ = [
     "apply_square_staggered_m2mdeodoe_stencil", "square_staggered_eoprec_prepare",
     "square_staggered_eoprec_reconstruct", "apply_square_staggered_eoprec_prepare_stencil",
     "apply_square_staggered_eoprec_reconstruct_stencil",
+    "apply_stencil_2d_tb", "apply_stencil_2d_bt", "apply_square_staggered_m2mdtbdbt_stencil",
+    "apply_square_staggered_normal_eo_stencil", "apply_square_staggered_normal_tb_stencil",
+    "apply_square_staggered_dagger_eo_stencil", "apply_square_staggered_dagger_tb_stencil",
+    "apply_square_staggered_tbprec_prepare_stencil", "apply_square_staggered_tbprec_reconstruct_stencil",
+    "MgLevel", "block_normalize", "block_orthonormalize", "prolong", "restrict",
+    "generate_coarse_from_fine_stencil",
     "minv_vector_cg", "minv_vector_cg_restart", "minv_vector_cg_m", "minv_vector_bicgstab",
     "minv_vector_bicgstab_restart", "minv_vector_gcr", "minv_vector_gcr_restart",
     "minv_vector_cr", "minv_vector_cr_restart", "minv_vector_minres", "minv_vector_cr_m",
@@ -75,7 +81,11 @@ VERB_PASS_THROUGH, VERB_NONE, VERB_SUMMARY, VERB_RESTART_DETAIL, VERB_DETAIL = -
 KIND_STAGGERED, KIND_STAGGERED_DAGGER, KIND_STAGGERED_NORMAL, KIND_LAPLACE = 0, 1, 2, 3
 KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE = 4, 5, 6
 KIND_STAGGERED_DEO, KIND_STAGGERED_DOE, KIND_STAGGERED_M2MDEODOE, KIND_STENCIL_M2MDEODOE = 7, 8, 9, 10
-_STENCIL_KINDS = (KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE, KIND_STENCIL_M2MDEODOE)
+KIND_STENCIL_TB, KIND_STENCIL_BT, KIND_STENCIL_M2MDTBDBT = 11, 12, 13
+KIND_STENCIL_NORMAL_EO, KIND_STENCIL_NORMAL_TB, KIND_STENCIL_DAGGER_EO, KIND_STENCIL_DAGGER_TB = 14, 15, 16, 17
+_STENCIL_KINDS = (KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE, KIND_STENCIL_M2MDEODOE, KIND_STENCIL_TB,
+                  KIND_STENCIL_BT, KIND_STENCIL_M2MDTBDBT, KIND_STENCIL_NORMAL_EO, KIND_STENCIL_NORMAL_TB,
+                  KIND_STENCIL_DAGGER_EO, KIND_STENCIL_DAGGER_TB)
 
 
 class UnsupportedOperator(GlinalgError):
@@ -240,12 +250,24 @@ square_staggered_m2mdeodoe_u1 = _callback(KIND_STAGGERED_M2MDEODOE, "square_stag
                                           "operators.cpp:566")
 apply_square_staggered_m2mdeodoe_stencil = _callback(KIND_STENCIL_M2MDEODOE, "apply_square_staggered_m2mdeodoe_stencil",
                                                      "operators_stencil.cpp:197")
+apply_stencil_2d_tb = _callback(KIND_STENCIL_TB, "apply_stencil_2d_tb", "coarse_stencil.cpp:725")
+apply_stencil_2d_bt = _callback(KIND_STENCIL_BT, "apply_stencil_2d_bt", "coarse_stencil.cpp:1120")
+apply_square_staggered_m2mdtbdbt_stencil = _callback(KIND_STENCIL_M2MDTBDBT, "apply_square_staggered_m2mdtbdbt_stencil",
+                                                     "mg_complex.cpp:1228")
+apply_square_staggered_normal_eo_stencil = _callback(KIND_STENCIL_NORMAL_EO, "apply_square_staggered_normal_eo_stencil",
+                                                     "mg_complex.cpp:1277")
+apply_square_staggered_normal_tb_stencil = _callback(KIND_STENCIL_NORMAL_TB, "apply_square_staggered_normal_tb_stencil",
+                                                     "mg_complex.cpp:1305")
+apply_square_staggered_dagger_eo_stencil = _callback(KIND_STENCIL_DAGGER_EO, "apply_square_staggered_dagger_eo_stencil",
+                                                     "mg_complex.cpp:1335")
+apply_square_staggered_dagger_tb_stencil = _callback(KIND_STENCIL_DAGGER_TB, "apply_square_staggered_dagger_tb_stencil",
+                                                     "mg_complex.cpp:1355")
 
 
 def _eo_step(kind, out, a, b, extra):
     op, temp = _op_for(kind, extra)
     try:
-        if op.kind not in (KIND_STAGGERED_M2MDEODOE, KIND_STENCIL_M2MDEODOE):
+        if op.kind not in (KIND_STAGGERED_M2MDEODOE, KIND_STENCIL_M2MDEODOE, KIND_STENCIL_M2MDTBDBT):
             raise UnsupportedOperator("even/odd steps need an m^2 - D_eo D_oe operator")
         op_, on, odev = _field_ptr(out, writable=True)
         ap, an, adev = _field_ptr(a)
@@ -285,6 +307,17 @@ def apply_square_staggered_eoprec_prepare_stencil(rhs_e, rhs_orig, stenc):
 def apply_square_staggered_eoprec_reconstruct_stencil(lhs_full, lhs_e, rhs_o, stenc):
     """The stencil form of square_staggered_eoprec_reconstruct (operators_stencil.cpp:220)."""
     return _eo_step(KIND_STENCIL_M2MDEODOE, lhs_full, lhs_e, rhs_o, stenc)
+
+
+def apply_square_staggered_tbprec_prepare_stencil(rhs_t, rhs_orig, stenc):
+    """rhs_t = m rhs - D_tb rhs on the top colours, 0 on the bottom ones (mg_complex.cpp:1211)."""
+    return _eo_step(KIND_STENCIL_M2MDTBDBT, rhs_t, rhs_orig, None, stenc)
+
+
+def apply_square_staggered_tbprec_reconstruct_stencil(lhs_full, lhs_t, rhs_b, stenc):
+    """lhs_full = lhs_t on the top colours, (rhs_b - D_bt lhs_t) / Re(m) on the bottom ones
+    (mg_complex.cpp:1252)."""
+    return _eo_step(KIND_STENCIL_M2MDTBDBT, lhs_full, lhs_t, rhs_b, stenc)
 
 
 def _stencil_builder(dagger):
@@ -781,3 +814,102 @@ def apply_ape_smear_u1(smeared_field, gauge_field, x_len, y_len, alpha, n_iter):
         raise ValueError("both fields must be on the host or both on the device")
     _capi.check(lib().glinalg_apply_ape_smear_u1(_dptr(o), _dptr(p), x_len, y_len, float(alpha), int(n_iter),
                                                  _flags(dev)), "ape_smear_u1")
+
+
+# ---------------------------------------------------------------- multigrid (mg_complex.cpp)
+
+class MgLevel:
+    """One level of mg_operator_struct_complex (mg_complex.h): a fine lattice x_fine x y_fine
+    with nc_fine dof per site blocked blocksize_x x blocksize_y onto coarse sites with
+    nc_coarse dof, and its null vectors (an (nc_coarse, x_fine*y_fine*nc_fine) complex array
+    or list of fields), held on the device."""
+
+    def __init__(self, x_fine, y_fine, nc_fine, blocksize_x, blocksize_y, nc_coarse, null_vectors):
+        self.x_fine, self.y_fine, self.nc_fine = int(x_fine), int(y_fine), int(nc_fine)
+        self.blocksize_x, self.blocksize_y, self.nc_coarse = int(blocksize_x), int(blocksize_y), int(nc_coarse)
+        self.x_coarse, self.y_coarse = self.x_fine // self.blocksize_x, self.y_fine // self.blocksize_y
+        self.fine_size = self.x_fine * self.y_fine * self.nc_fine
+        self.coarse_size = self.x_coarse * self.y_coarse * self.nc_coarse
+        if _is_torch(null_vectors):
+            nv = null_vectors.contiguous()
+            p, n, dev = _field_ptr(nv)
+        else:
+            nv = np.ascontiguousarray(np.asarray(null_vectors, dtype=np.complex128).reshape(-1))
+            p, n, dev = _field_ptr(nv)
+        if n != self.nc_coarse * self.fine_size:
+            raise ValueError("null_vectors must hold nc_coarse fine fields")
+        self.handle = C.c_void_p()
+        _capi.check(lib().glinalg_mg_level_create(self.x_fine, self.y_fine, self.nc_fine, self.blocksize_x,
+                                                  self.blocksize_y, self.nc_coarse, _dptr(p), _flags(dev),
+                                                  C.byref(self.handle)), "mg_level_create")
+
+    def null_vectors(self):
+        out = np.zeros((self.nc_coarse, self.fine_size), np.complex128)
+        _capi.check(lib().glinalg_mg_get_null_vectors(self.handle, _dptr(C.c_void_p(out.ctypes.data)), 0),
+                    "mg_get_null_vectors")
+        return out
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().glinalg_mg_level_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def block_normalize(mgstruct: MgLevel):
+    """block_normalize (mg_complex.cpp:191)."""
+    _capi.check(lib().glinalg_mg_block_normalize(mgstruct.handle), "mg_block_normalize")
+
+
+def block_orthonormalize(mgstruct: MgLevel):
+    """block_orthonormalize (mg_complex.cpp:259)."""
+    _capi.check(lib().glinalg_mg_block_orthonormalize(mgstruct.handle), "mg_block_orthonormalize")
+
+
+def prolong(vec_fine, vec_coarse, mgstruct: MgLevel):
+    """prolong (mg_complex.cpp:372): vec_fine = P vec_coarse."""
+    o, no, d1 = _field_ptr(vec_fine, writable=True)
+    i, ni, d2 = _field_ptr(vec_coarse)
+    if d1 != d2 or no < mgstruct.fine_size or ni < mgstruct.coarse_size:
+        raise ValueError("field sizes / devices do not match the level")
+    _capi.check(lib().glinalg_mg_prolong(mgstruct.handle, _dptr(o), _dptr(i), _flags(d1)), "mg_prolong")
+
+
+def restrict(vec_coarse, vec_fine, mgstruct: MgLevel):
+    """restrict (mg_complex.cpp:421): vec_coarse = P^dagger vec_fine."""
+    o, no, d1 = _field_ptr(vec_coarse, writable=True)
+    i, ni, d2 = _field_ptr(vec_fine)
+    if d1 != d2 or no < mgstruct.coarse_size or ni < mgstruct.fine_size:
+        raise ValueError("field sizes / devices do not match the level")
+    _capi.check(lib().glinalg_mg_restrict(mgstruct.handle, _dptr(o), _dptr(i), _flags(d1)), "mg_restrict")
+
+
+def _coarse_operator(op_handle, mgstruct):
+    """Wraps a library-created coarse stencil operator."""
+    c = Operator.__new__(Operator)
+    c.handle = op_handle
+    c.kind, c.lx, c.ly, c.nc = KIND_STENCIL, mgstruct.x_coarse, mgstruct.y_coarse, mgstruct.nc_coarse
+    return c
+
+
+def generate_coarse_from_fine_stencil(stenc_coarse, stenc_fine, mgstruct: MgLevel, ignore_shifts=False):
+    """generate_coarse_from_fine_stencil (mg_complex.cpp:827): the Galerkin coarse stencil
+    P^dagger A P.  stenc_fine: a Stencil2D or a stencil Operator; stenc_coarse: a Stencil2D
+    whose clover and hopping arrays receive the coarse coefficients, or None.  Returns the
+    coarse operator on the device (a stencil Operator)."""
+    fine, temp = (stenc_fine, False) if isinstance(stenc_fine, Operator) else _op_for(KIND_STENCIL, stenc_fine)
+    try:
+        h = C.c_void_p()
+        _capi.check(lib().glinalg_mg_coarse_stencil(mgstruct.handle, fine.handle, int(bool(ignore_shifts)),
+                                                    C.byref(h)), "mg_coarse_stencil")
+        coarse = _coarse_operator(h, mgstruct)
+    finally:
+        if temp:
+            fine.close()
+    if stenc_coarse is not None:
+        _capi.check(lib().glinalg_operator_stencil_get(coarse.handle, _dptr(C.c_void_p(stenc_coarse.clover.ctypes.data)),
+                                                       _dptr(C.c_void_p(stenc_coarse.hopping.ctypes.data)), 0),
+                    "operator_stencil_get")
+        stenc_coarse.generated = True
+    return coarse

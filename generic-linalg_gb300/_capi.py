@@ -68,6 +68,17 @@ def _prototypes():
         "glinalg_tuned_persist": (i, [vp, i]),
         "glinalg_eoprec_prepare": (st, [vp, _dp, _dp, i]),
         "glinalg_eoprec_reconstruct": (st, [vp, _dp, _dp, _dp, i]),
+        "glinalg_tbprec_prepare": (st, [vp, _dp, _dp, i]),
+        "glinalg_mg_level_create": (st, [i, i, i, i, i, i, _dp, i, P(vp)]),
+        "glinalg_mg_level_destroy": (st, [vp]),
+        "glinalg_mg_get_null_vectors": (st, [vp, _dp, i]),
+        "glinalg_mg_block_normalize": (st, [vp]),
+        "glinalg_mg_block_orthonormalize": (st, [vp]),
+        "glinalg_mg_prolong": (st, [vp, _dp, _dp, i]),
+        "glinalg_mg_restrict": (st, [vp, _dp, _dp, i]),
+        "glinalg_mg_coarse_stencil": (st, [vp, vp, i, P(vp)]),
+        "glinalg_operator_stencil_get": (st, [vp, _dp, _dp, i]),
+        "glinalg_tbprec_reconstruct": (st, [vp, _dp, _dp, _dp, i]),
         "glinalg_profile_persist_kernel": (st, [vp, i, i, i, _dp, _dp, P(i)]),
         "glinalg_staggered_normal_apply_noalloc": (st, [_dp, d, i, i, _dp, _dp, vp]),
         "glinalg_operator_create": (st, [P(OpDesc), P(vp)]),

@@ -202,7 +202,8 @@ static glinalg_status eo_step(glinalg_operator op, double *out, const double *a,
                               bool reconstruct)
 {
     if (!op || !out || !a || (reconstruct && !b)) return GLINALG_ERROR_INVALID_VALUE;
-    if (op->kind != GLINALG_OP_STAGGERED_M2MDEODOE && op->kind != GLINALG_OP_STENCIL_M2MDEODOE) {
+    const bool tb = op->kind == GLINALG_OP_STENCIL_M2MDTBDBT;
+    if (op->kind != GLINALG_OP_STAGGERED_M2MDEODOE && op->kind != GLINALG_OP_STENCIL_M2MDEODOE && !tb) {
         set_last_error("even/odd preconditioning needs an m^2 - D_eo D_oe operator");
         return GLINALG_ERROR_UNSUPPORTED_OP;
     }
@@ -222,8 +223,13 @@ static glinalg_status eo_step(glinalg_operator op, double *out, const double *a,
             GL_CUDA(cudaMemcpyAsync(d_b, b, bytes, cudaMemcpyHostToDevice, st));
         }
     }
-    if (reconstruct) GL_TRY(launch_eo_reconstruct(op, d_out, d_a, d_b, st));
-    else GL_TRY(launch_eo_prepare(op, d_out, d_a, st));
+    if (tb) {
+        if (reconstruct) GL_TRY(launch_tb_reconstruct(op, d_out, d_a, d_b, st));
+        else GL_TRY(launch_tb_prepare(op, d_out, d_a, st));
+    } else {
+        if (reconstruct) GL_TRY(launch_eo_reconstruct(op, d_out, d_a, d_b, st));
+        else GL_TRY(launch_eo_prepare(op, d_out, d_a, st));
+    }
     if (!dev) GL_CUDA(cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, st));
     GL_CUDA(cudaStreamSynchronize(st));
     return GLINALG_SUCCESS;
@@ -238,4 +244,23 @@ extern "C" glinalg_status glinalg_eoprec_reconstruct(glinalg_operator op, double
                                                      const double *rhs_o, int flags)
 {
     return eo_step(op, lhs_full, lhs_e, rhs_o, flags, true);
+}
+
+extern "C" glinalg_status glinalg_tbprec_prepare(glinalg_operator op, double *rhs_t, const double *rhs, int flags)
+{
+    if (op && op->kind != GLINALG_OP_STENCIL_M2MDTBDBT) {
+        set_last_error("top/bottom preconditioning needs an m^2 - D_tb D_bt stencil operator");
+        return GLINALG_ERROR_UNSUPPORTED_OP;
+    }
+    return eo_step(op, rhs_t, rhs, nullptr, flags, false);
+}
+
+extern "C" glinalg_status glinalg_tbprec_reconstruct(glinalg_operator op, double *lhs_full, const double *lhs_t,
+                                                     const double *rhs_b, int flags)
+{
+    if (op && op->kind != GLINALG_OP_STENCIL_M2MDTBDBT) {
+        set_last_error("top/bottom preconditioning needs an m^2 - D_tb D_bt stencil operator");
+        return GLINALG_ERROR_UNSUPPORTED_OP;
+    }
+    return eo_step(op, lhs_full, lhs_t, rhs_b, flags, true);
 }

@@ -51,9 +51,11 @@ glinalg_status launch_apply_shifted(const glinalg_operator_s *op, double2 *lhs,
                                     const double2 *rhs, double2 *tmp, double sigma,
                                     cudaStream_t stream);
 
-// apply_stencil_2d (parity 0), _eo (1) or _oe (2) of a stencil-described operator.
+// apply_stencil_2d (parity 0), _eo (1), _oe (2), _tb (3) or _bt (4) of a stencil-described
+// operator.  With comb_r, out = (comb_s2 comb_r - out) - (the stencil applied to in).
 glinalg_status launch_stencil_parity(const glinalg_operator_s *op, double2 *out, const double2 *in, int parity,
-                                     const int *done, cudaStream_t stream);
+                                     const int *done, cudaStream_t stream, const double2 *comb_r = nullptr,
+                                     double2 comb_s2 = double2{0.0, 0.0});
 
 // Even/odd preconditioning (eoprec.cu): D_eo, D_oe and m^2 - D_eo D_oe applied; the prepare and
 // reconstruct steps; the even part of a field; x = x_e on even sites.
@@ -67,6 +69,15 @@ glinalg_status launch_even_part(const glinalg_operator_s *op, double2 *out, cons
                                 cudaStream_t stream);
 glinalg_status launch_even_into(const glinalg_operator_s *op, double2 *x, const double2 *xe,
                                 cudaStream_t stream);
+
+// The coarse-level stencil operators of the multigrid code (coarse_ops.cu): m^2 - D_tb D_bt,
+// the normal_eo / normal_tb and dagger_eo / dagger_tb forms; tmp: one scratch field.
+glinalg_status launch_coarse_piece(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs, double2 *tmp,
+                                   const int *done, cudaStream_t stream);
+glinalg_status launch_tb_prepare(const glinalg_operator_s *op, double2 *rhs_t, const double2 *rhs,
+                                 cudaStream_t stream);
+glinalg_status launch_tb_reconstruct(const glinalg_operator_s *op, double2 *full, const double2 *lhs_t,
+                                     const double2 *rhs_b, cudaStream_t stream);
 
 // Staggered-only pieces (used by the force and by the fused solver kernels).
 glinalg_status launch_staggered(const glinalg_operator_s *op, double2 *out, const double2 *in,

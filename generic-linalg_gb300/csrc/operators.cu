@@ -102,7 +102,8 @@ bool is_staggered(int k)
 }
 bool is_stencil(int k)
 {
-    return (k >= GLINALG_OP_STENCIL && k <= GLINALG_OP_STENCIL_OE) || k == GLINALG_OP_STENCIL_M2MDEODOE;
+    return (k >= GLINALG_OP_STENCIL && k <= GLINALG_OP_STENCIL_OE) || k == GLINALG_OP_STENCIL_M2MDEODOE ||
+           (k >= GLINALG_OP_STENCIL_TB && k <= GLINALG_OP_STENCIL_DAGGER_TB);
 }
 bool is_hermitian(int k)
 {
@@ -112,7 +113,7 @@ bool is_hermitian(int k)
 bool needs_tmp(int k)
 {
     return k == GLINALG_OP_STAGGERED_NORMAL || k == GLINALG_OP_STAGGERED_M2MDEODOE ||
-           k == GLINALG_OP_STENCIL_M2MDEODOE;
+           k == GLINALG_OP_STENCIL_M2MDEODOE || (k >= GLINALG_OP_STENCIL_M2MDTBDBT && k <= GLINALG_OP_STENCIL_DAGGER_TB);
 }
 
 double apply_bytes(const glinalg_operator_s *op)
@@ -158,15 +159,18 @@ __global__ void k_laplace(double2 *__restrict__ out, const double2 *__restrict__
         out[i] = lap_site(ld, U, mass, lx, ly, i);
 }
 
-// apply_stencil_2d (parity 0), _eo (parity 1: even output sites, hopping only) and _oe
-// (parity 2).  One (site, colour-row) element per thread.  NC > 0 fixes the colour count
+// apply_stencil_2d (parity 0), _eo (parity 1: even output sites, hopping only), _oe
+// (parity 2), _tb (parity 3: top half of the colours out, bottom half in; clover, hopping and
+// two-link, no shifts; coarse_stencil.cpp:725) and _bt (parity 4, :1120).  One (site,
+// colour-row) element per thread.  NC > 0 fixes the colour count
 // at compile time; NC == 0 reads it from nc_rt.
 template <int NC>
 __global__ void k_stencil(double2 *__restrict__ out, const double2 *__restrict__ in,
                           const double2 *__restrict__ clov, const double2 *__restrict__ hop,
                           const double2 *__restrict__ two, double2 shift, double2 eo_shift,
                           double2 dof_shift, int lx, int ly, int nc_rt, int parity,
-                          const int *__restrict__ done)
+                          const int *__restrict__ done, const double2 *__restrict__ comb_r = nullptr,
+                          double2 comb_s2 = double2{0.0, 0.0})
 {
     if (done && *done) return;
     const int nc = NC > 0 ? NC : nc_rt;
@@ -180,13 +184,17 @@ __global__ void k_stencil(double2 *__restrict__ out, const double2 *__restrict__
         const long site = i / nc;
         const int y = (int)(site / lx), x = (int)(site - (long)y * lx);
         const bool even = ((x + y) & 1) == 0;
-        if ((parity == 1 && !even) || (parity == 2 && even)) {
-            out[i] = cmk(0.0, 0.0);
+        if ((parity == 1 && !even) || (parity == 2 && even) || (parity == 3 && color >= nc / 2) ||
+            (parity == 4 && color < nc / 2)) {
+            out[i] = comb_r ? csub(cmul(comb_s2, comb_r[i]), out[i]) : cmk(0.0, 0.0);
             continue;
         }
+        // tb (3) reads the bottom half of the input colours, bt (4) the top half
+        const int c0 = parity == 3 ? nc / 2 : 0, c1 = parity == 4 ? nc / 2 : nc;
+        const bool full = parity == 0 || parity >= 3;  // clover and two-link terms included
         double2 acc = cmk(0.0, 0.0);
-        if (parity == 0) {
-            for (int c = 0; c < nc; c++)
+        if (full) {
+            for (int c = c0; c < c1; c++)
                 acc = cadd(acc, cmul(clov[c + (long)nc * i], in[site * nc + c]));
         }
         // hopping directions {+x, +y, -x, -y}
@@ -198,9 +206,9 @@ __global__ void k_stencil(double2 *__restrict__ out, const double2 *__restrict__
             yy = yy < 0 ? yy + ly : (yy >= ly ? yy - ly : yy);
             const long nb = ((long)yy * lx + xx) * nc;
             const double2 *h = hop + (long)d * nc * lsize + (long)nc * i;
-            for (int c = 0; c < nc; c++) acc = cadd(acc, cmul(h[c], in[nb + c]));
+            for (int c = c0; c < c1; c++) acc = cadd(acc, cmul(h[c], in[nb + c]));
         }
-        if (parity == 0 && two != nullptr) {
+        if (full && two != nullptr) {
             // two-link directions {+2x, +x+y, +2y, -x+y, -2x, -x-y, -2y, +x-y}
             const int txs[8] = {2, 1, 0, -1, -2, -1, 0, 1}, tys[8] = {0, 1, 2, 1, 0, -1, -2, -1};
 #pragma unroll
@@ -208,7 +216,7 @@ __global__ void k_stencil(double2 *__restrict__ out, const double2 *__restrict__
                 int xx = (x + txs[d] + 2 * lx) % lx, yy = (y + tys[d] + 2 * ly) % ly;
                 const long nb = ((long)yy * lx + xx) * nc;
                 const double2 *h = two + (long)d * nc * lsize + (long)nc * i;
-                for (int c = 0; c < nc; c++) acc = cadd(acc, cmul(h[c], in[nb + c]));
+                for (int c = c0; c < c1; c++) acc = cadd(acc, cmul(h[c], in[nb + c]));
             }
         }
         if (parity == 0) {
@@ -217,7 +225,8 @@ __global__ void k_stencil(double2 *__restrict__ out, const double2 *__restrict__
             if (has_eo) acc = cadd(acc, cmul(cscale(even ? 1.0 : -1.0, eo_shift), r));
             if (has_dof) acc = cadd(acc, cmul(cscale(color < nc / 2 ? 1.0 : -1.0, dof_shift), r));
         }
-        out[i] = acc;
+        // combined form: out = (s2 r - out) - acc, the last step of m^2 - A - B
+        out[i] = comb_r ? csub(csub(cmul(comb_s2, comb_r[i]), out[i]), acc) : acc;
     }
 }
 
@@ -293,30 +302,31 @@ glinalg_status launch_apply(const glinalg_operator_s *op, double2 *lhs, const do
     case GLINALG_OP_STAGGERED_DOE:
     case GLINALG_OP_STAGGERED_M2MDEODOE:
     case GLINALG_OP_STENCIL_M2MDEODOE: return launch_eo_apply(op, lhs, rhs, tmp, done, st);
+    case GLINALG_OP_STENCIL_TB: return launch_stencil_parity(op, lhs, rhs, 3, done, st);
+    case GLINALG_OP_STENCIL_BT: return launch_stencil_parity(op, lhs, rhs, 4, done, st);
+    case GLINALG_OP_STENCIL_M2MDTBDBT:
+    case GLINALG_OP_STENCIL_NORMAL_EO:
+    case GLINALG_OP_STENCIL_NORMAL_TB:
+    case GLINALG_OP_STENCIL_DAGGER_EO:
+    case GLINALG_OP_STENCIL_DAGGER_TB: return launch_coarse_piece(op, lhs, rhs, tmp, done, st);
     default: return GLINALG_ERROR_UNSUPPORTED_OP;
     }
 }
 
 glinalg_status launch_stencil_parity(const glinalg_operator_s *op, double2 *lhs, const double2 *rhs, int parity,
-                                     const int *done, cudaStream_t st)
+                                     const int *done, cudaStream_t st, const double2 *comb_r, double2 comb_s2)
 {
     const int nt = 256;
     const int g = grid_for(op->size, nt);
-    if (op->nc == 1)
-        k_stencil<1><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
-                                       op->dof_shift, op->lx, op->ly, 1, parity, done);
-    else if (op->nc == 2)
-        k_stencil<2><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
-                                       op->dof_shift, op->lx, op->ly, 2, parity, done);
-    else if (op->nc == 4)
-        k_stencil<4><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
-                                       op->dof_shift, op->lx, op->ly, 4, parity, done);
-    else if (op->nc == 8)
-        k_stencil<8><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
-                                       op->dof_shift, op->lx, op->ly, 8, parity, done);
-    else
-        k_stencil<0><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,
-                                       op->dof_shift, op->lx, op->ly, op->nc, parity, done);
+#define GL_STENCIL(NCT, NCR)                                                                                       \
+    k_stencil<NCT><<<g, nt, 0, st>>>(lhs, rhs, op->clover, op->hopping, op->two_link, op->shift, op->eo_shift,     \
+                                     op->dof_shift, op->lx, op->ly, NCR, parity, done, comb_r, comb_s2)
+    if (op->nc == 1) GL_STENCIL(1, 1);
+    else if (op->nc == 2) GL_STENCIL(2, 2);
+    else if (op->nc == 4) GL_STENCIL(4, 4);
+    else if (op->nc == 8) GL_STENCIL(8, 8);
+    else GL_STENCIL(0, op->nc);
+#undef GL_STENCIL
     GL_CUDA(cudaGetLastError());
     return GLINALG_SUCCESS;
 }
@@ -374,7 +384,7 @@ extern "C" glinalg_status glinalg_operator_create(const glinalg_op_desc *d, glin
     if (!d || !out) return GLINALG_ERROR_INVALID_VALUE;
     *out = nullptr;
     if (d->lx <= 0 || d->ly <= 0) return GLINALG_ERROR_INVALID_VALUE;
-    if (d->kind < GLINALG_OP_STAGGERED || d->kind > GLINALG_OP_STENCIL_M2MDEODOE)
+    if (d->kind < GLINALG_OP_STAGGERED || d->kind > GLINALG_OP_STENCIL_DAGGER_TB)
         return GLINALG_ERROR_UNSUPPORTED_OP;
     const bool sten = is_stencil(d->kind);
     if (sten && (d->nc <= 0 || !d->clover || !d->hopping)) return GLINALG_ERROR_INVALID_VALUE;
@@ -511,5 +521,22 @@ extern "C" glinalg_status glinalg_staggered_stencil(const double *links, int lx,
         shift_out[0] = mass;
         shift_out[1] = 0.0;
     }
+    return GLINALG_SUCCESS;
+}
+
+extern "C" glinalg_status glinalg_operator_stencil_get(glinalg_operator op, double *clover, double *hopping,
+                                                       int flags)
+{
+    if (!op) return GLINALG_ERROR_INVALID_VALUE;
+    if (!is_stencil(op->kind) || !op->clover || !op->hopping) {
+        set_last_error("not a stencil operator");
+        return GLINALG_ERROR_UNSUPPORTED_OP;
+    }
+    cudaStream_t st = lib_stream();
+    const size_t cc = sizeof(double2) * (size_t)op->vol * op->nc * op->nc;
+    const cudaMemcpyKind k = (flags & GLINALG_PTR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (clover) GL_CUDA(cudaMemcpyAsync(clover, op->clover, cc, k, st));
+    if (hopping) GL_CUDA(cudaMemcpyAsync(hopping, op->hopping, 4 * cc, k, st));
+    GL_CUDA(cudaStreamSynchronize(st));
     return GLINALG_SUCCESS;
 }

@@ -68,7 +68,16 @@ typedef enum glinalg_op_kind {
     GLINALG_OP_STAGGERED_DOE = 8,     /* square_staggered_doe_u1      operators.cpp:499 */
     GLINALG_OP_STAGGERED_M2MDEODOE = 9, /* square_staggered_m2mdeodoe_u1 operators.cpp:566 */
     /* the stencil form of m^2 - D_eo D_oe (stencil descriptor, nc = 1, shift = mass) */
-    GLINALG_OP_STENCIL_M2MDEODOE = 10 /* apply_square_staggered_m2mdeodoe_stencil operators_stencil.cpp:197 */
+    GLINALG_OP_STENCIL_M2MDEODOE = 10, /* apply_square_staggered_m2mdeodoe_stencil operators_stencil.cpp:197 */
+    /* top/bottom pieces of a coarse stencil (stencil descriptor, even nc) */
+    GLINALG_OP_STENCIL_TB = 11,       /* apply_stencil_2d_tb          coarse_stencil.cpp:725  */
+    GLINALG_OP_STENCIL_BT = 12,       /* apply_stencil_2d_bt          coarse_stencil.cpp:1120 */
+    /* the multigrid code's stencil operators (m = the stencil's shift) */
+    GLINALG_OP_STENCIL_M2MDTBDBT = 13, /* apply_square_staggered_m2mdtbdbt_stencil mg_complex.cpp:1228 */
+    GLINALG_OP_STENCIL_NORMAL_EO = 14, /* apply_square_staggered_normal_eo_stencil mg_complex.cpp:1277 */
+    GLINALG_OP_STENCIL_NORMAL_TB = 15, /* apply_square_staggered_normal_tb_stencil mg_complex.cpp:1305 */
+    GLINALG_OP_STENCIL_DAGGER_EO = 16, /* apply_square_staggered_dagger_eo_stencil mg_complex.cpp:1335 */
+    GLINALG_OP_STENCIL_DAGGER_TB = 17  /* apply_square_staggered_dagger_tb_stencil mg_complex.cpp:1355 */
 } glinalg_op_kind;
 
 /* Pointer-location flags. */
@@ -158,6 +167,9 @@ glinalg_status glinalg_operator_destroy(glinalg_operator op);
 /* The reference's tests shift the operator by editing staggered_u1_op::mass between solves
  * (tests/multishift/multishift.cpp:446); this is the same edit. */
 glinalg_status glinalg_operator_set_mass(glinalg_operator op, double mass);
+/* Copies a stencil-kind operator's clover (lx*ly*nc*nc complex) and hopping (4 times that)
+ * out of the device, in the stencil_2d layout (either pointer may be NULL). */
+glinalg_status glinalg_operator_stencil_get(glinalg_operator op, double *clover, double *hopping, int flags);
 /* Number of complex entries of a field (lx*ly, times nc for stencil kinds). */
 long glinalg_operator_size(glinalg_operator op);
 /* lhs = A rhs, the operator callback of the reference (lhs overwritten, rhs untouched). */
@@ -172,6 +184,14 @@ glinalg_status glinalg_operator_apply(glinalg_operator op, double *lhs, const do
  * odd sites (m: the mass, or Re(shift) for the stencil form).  Fields have op's size;
  * GLINALG_PTR_DEVICE in flags marks device pointers. */
 glinalg_status glinalg_eoprec_prepare(glinalg_operator op, double *rhs_e, const double *rhs, int flags);
+/* The same two steps for the top/bottom colour halves of a coarse stencil, op of kind
+ * GLINALG_OP_STENCIL_M2MDTBDBT (apply_square_staggered_tbprec_prepare_stencil /
+ * _reconstruct_stencil, mg_complex.cpp:1211 / :1252): rhs_t = m rhs - D_tb rhs on the top
+ * colours, 0 on the bottom ones; lhs_full = lhs_t on the top colours, (rhs_b - D_bt lhs_t) /
+ * Re(m) on the bottom ones. */
+glinalg_status glinalg_tbprec_prepare(glinalg_operator op, double *rhs_t, const double *rhs, int flags);
+glinalg_status glinalg_tbprec_reconstruct(glinalg_operator op, double *lhs_full, const double *lhs_t,
+                                          const double *rhs_b, int flags);
 glinalg_status glinalg_eoprec_reconstruct(glinalg_operator op, double *lhs_full, const double *lhs_e,
                                           const double *rhs_o, int flags);
 
@@ -326,6 +346,30 @@ glinalg_status glinalg_apply_gauge_trans_u1(double *links, const double *trans, 
  * back onto U(1); smeared and links may not overlap */
 glinalg_status glinalg_apply_ape_smear_u1(double *smeared, const double *links, int lx, int ly,
                                           double alpha, int n_iter, int flags);
+
+/* ---- multigrid transfer and coarse operators (multigrid/aa_mg/mg_complex.cpp) ---- */
+
+/* One level of mg_operator_struct_complex (mg_complex.h): a fine lattice lx x ly with
+ * nc_fine dof per site, blocked bx x by onto (lx/bx) x (ly/by) coarse sites with nc_coarse
+ * dof.  null_vectors: nc_coarse fields of lx*ly*nc_fine complex (null_vectors[level][c][f],
+ * f = (y*lx + x)*nc_fine + dof), copied to the device. */
+typedef struct glinalg_mg_level_s *glinalg_mg_level;
+glinalg_status glinalg_mg_level_create(int lx, int ly, int nc_fine, int bx, int by, int nc_coarse,
+                                       const double *null_vectors, int flags, glinalg_mg_level *out);
+glinalg_status glinalg_mg_level_destroy(glinalg_mg_level lv);
+glinalg_status glinalg_mg_get_null_vectors(glinalg_mg_level lv, double *out, int flags);
+/* block_normalize / block_orthonormalize (mg_complex.cpp:191 / :259), in place */
+glinalg_status glinalg_mg_block_normalize(glinalg_mg_level lv);
+glinalg_status glinalg_mg_block_orthonormalize(glinalg_mg_level lv);
+/* prolong (mg_complex.cpp:372): fine = P coarse; restrict (:421): coarse = P^dagger fine */
+glinalg_status glinalg_mg_prolong(glinalg_mg_level lv, double *fine, const double *coarse, int flags);
+glinalg_status glinalg_mg_restrict(glinalg_mg_level lv, double *coarse, const double *fine, int flags);
+/* generate_coarse_from_fine_stencil (mg_complex.cpp:827): a new GLINALG_OP_STENCIL operator on
+ * the coarse lattice holding P^dagger A P of the fine stencil operator `fine` (clover, the
+ * four hops and, unless ignore_shifts, its shift / eo_shift / dof_shift; two-link terms do not
+ * enter, as in the reference).  The coarse operator's own shifts are zero. */
+glinalg_status glinalg_mg_coarse_stencil(glinalg_mg_level lv, glinalg_operator fine, int ignore_shifts,
+                                         glinalg_operator *coarse_out);
 
 /* ---- batched solves (no reference counterpart: the reference solves systems one at a
  * time in a loop; these run many independent systems in one device launch sequence) ---- */
