@@ -60,7 +60,9 @@ __all__ = [
     "apply_square_staggered_dagger_eo_stencil", "apply_square_staggered_dagger_tb_stencil",
     "apply_square_staggered_tbprec_prepare_stencil", "apply_square_staggered_tbprec_reconstruct_stencil",
     "MgLevel", "block_normalize", "block_orthonormalize", "prolong", "restrict",
-    "generate_coarse_from_fine_stencil",
+    "generate_coarse_from_fine_stencil", "MgPrecondStruct", "mg_preconditioner",
+    "MINV_INVALID", "MINV_CG", "MINV_CR", "MINV_GCR", "MINV_BICGSTAB", "MINV_BICGSTAB_L", "MINV_MINRES",
+    "NONE", "MINRES", "CG", "GCR", "BICGSTAB", "CR", "BICGSTAB_L", "MLEVEL_SMOOTH", "MLEVEL_RECURSIVE",
     "minv_vector_cg", "minv_vector_cg_restart", "minv_vector_cg_m", "minv_vector_bicgstab",
     "minv_vector_bicgstab_restart", "minv_vector_gcr", "minv_vector_gcr_restart",
     "minv_vector_cr", "minv_vector_cr_restart", "minv_vector_minres", "minv_vector_cr_m",
@@ -546,6 +548,7 @@ def _precond(kind, name, ref):
     return pc
 
 
+mg_preconditioner = _precond(3, "mg_preconditioner", "mg_complex.cpp:514")
 identity_preconditioner = _precond(0, "identity_preconditioner", "generic_precond.cpp:34")
 minres_preconditioner = _precond(1, "minres_preconditioner", "generic_precond.cpp:53")
 gcr_preconditioner = _precond(2, "gcr_preconditioner", "generic_precond.cpp:70")
@@ -559,7 +562,9 @@ def _flex(fn, phi, phi0, size, max_iter, eps, restart, matrix_vector, extra_info
     pc = _capi.PrecondStruct()
     pc.kind = kind
     pop, ptemp = None, False
-    if kind != 0:
+    if kind == 3:
+        pc.mg = precond_info.handle
+    elif kind != 0:
         pc.n_step, pc.rel_res = int(precond_info.n_step), float(precond_info.rel_res)
         if precond_info.matrix_vector is not matrix_vector or precond_info.matrix_extra_data is not extra_info:
             pop, ptemp = _resolve(precond_info.matrix_vector, precond_info.matrix_extra_data)
@@ -913,3 +918,52 @@ def generate_coarse_from_fine_stencil(stenc_coarse, stenc_fine, mgstruct: MgLeve
                     "operator_stencil_get")
         stenc_coarse.generated = True
     return coarse
+
+
+# minv_inverter (generic_inverters.h:70-81), inner_solver (mg.h:5-14), mg_multilevel_type
+MINV_INVALID, MINV_CG, MINV_CR, MINV_GCR, MINV_BICGSTAB, MINV_BICGSTAB_L, MINV_MINRES = -1, 0, 1, 2, 3, 4, 7
+NONE, MINRES, CG, GCR, BICGSTAB, CR, BICGSTAB_L = 0, 1, 2, 3, 4, 5, 6
+MLEVEL_SMOOTH, MLEVEL_RECURSIVE = 0, 1
+
+
+class MgPrecondStruct:
+    """Mirror of mg_precond_struct_complex (mg_complex.h) over a device hierarchy: ops[0] the
+    fine operator, ops[l+1] the coarse operator of levels[l] (MgLevel).  Pass it as the
+    precond_info of mg_preconditioner to minv_vector_cg_flex_precond /
+    minv_vector_gcr_var_precond, or call apply(lhs, rhs)."""
+
+    def __init__(self, ops, levels, in_smooth_type=MINV_MINRES, omega_smooth=1.0, n_pre_smooth=None,
+                 n_post_smooth=None, normal_eqn_mg=False, normal_eqn_smooth=False, mlevel_type=MLEVEL_SMOOTH,
+                 in_solve_type=GCR, n_max=64, n_restart=32, rel_res=None):
+        nr = len(levels)
+        if len(ops) != nr + 1:
+            raise ValueError("need one more operator than levels")
+        p = _capi.MgParams()
+        p.smoother, p.omega_smooth = int(in_smooth_type), float(omega_smooth)
+        for l in range(nr):
+            p.n_pre_smooth[l] = int((n_pre_smooth or [0] * nr)[l])
+            p.n_post_smooth[l] = int((n_post_smooth or [0] * nr)[l])
+            p.rel_res[l] = float((rel_res or [1e-1] * nr)[l])
+        p.normal_eqn_mg, p.normal_eqn_smooth = int(normal_eqn_mg), int(normal_eqn_smooth)
+        p.mlevel_type, p.coarse_solver = int(mlevel_type), int(in_solve_type)
+        p.n_max, p.n_restart = int(n_max), int(n_restart)
+        self.ops, self.levels = list(ops), list(levels)
+        oa = (C.c_void_p * (nr + 1))(*[o.handle.value for o in self.ops])
+        la = (C.c_void_p * nr)(*[lv.handle.value for lv in self.levels])
+        self.handle = C.c_void_p()
+        _capi.check(lib().glinalg_mg_create(nr, oa, la, C.byref(p), C.byref(self.handle)), "mg_create")
+
+    def apply(self, lhs, rhs):
+        """One application of mg_preconditioner on the finest level."""
+        o, _, d1 = _field_ptr(lhs, writable=True)
+        i, _, d2 = _field_ptr(rhs)
+        if d1 != d2:
+            raise ValueError("lhs and rhs must both be on the host or both on the device")
+        _capi.check(lib().glinalg_mg_apply(self.handle, _dptr(o), _dptr(i), _flags(d1)), "mg_apply")
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().glinalg_mg_destroy(self.handle)
+        except Exception:
+            pass

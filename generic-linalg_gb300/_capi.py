@@ -48,7 +48,19 @@ class SolverParams(C.Structure):
 
 
 class PrecondStruct(C.Structure):
-    _fields_ = [("kind", C.c_int), ("n_step", C.c_int), ("rel_res", C.c_double), ("op", C.c_void_p)]
+    _fields_ = [("kind", C.c_int), ("n_step", C.c_int), ("rel_res", C.c_double), ("op", C.c_void_p),
+                ("mg", C.c_void_p)]
+
+
+MG_MAX_LEVELS = 8
+
+
+class MgParams(C.Structure):
+    _fields_ = [("smoother", C.c_int), ("omega_smooth", C.c_double),
+                ("n_pre_smooth", C.c_int * MG_MAX_LEVELS), ("n_post_smooth", C.c_int * MG_MAX_LEVELS),
+                ("normal_eqn_mg", C.c_int), ("normal_eqn_smooth", C.c_int), ("mlevel_type", C.c_int),
+                ("coarse_solver", C.c_int), ("n_max", C.c_int), ("n_restart", C.c_int),
+                ("rel_res", C.c_double * MG_MAX_LEVELS)]
 
 
 # Every function the header declares, with its ctypes prototype.
@@ -78,6 +90,9 @@ def _prototypes():
         "glinalg_mg_restrict": (st, [vp, _dp, _dp, i]),
         "glinalg_mg_coarse_stencil": (st, [vp, vp, i, P(vp)]),
         "glinalg_operator_stencil_get": (st, [vp, _dp, _dp, i]),
+        "glinalg_mg_create": (st, [i, P(vp), P(vp), P(MgParams), P(vp)]),
+        "glinalg_mg_destroy": (st, [vp]),
+        "glinalg_mg_apply": (st, [vp, _dp, _dp, i]),
         "glinalg_tbprec_reconstruct": (st, [vp, _dp, _dp, _dp, i]),
         "glinalg_profile_persist_kernel": (st, [vp, i, i, i, _dp, _dp, P(i)]),
         "glinalg_staggered_normal_apply_noalloc": (st, [_dp, d, i, i, _dp, _dp, vp]),

@@ -224,9 +224,19 @@ glinalg_status make_precond(const glinalg_precond *p, glinalg_operator op, Preco
 {
     *out = Precond{};
     if (!p) return GLINALG_SUCCESS;
-    if (p->kind < GLINALG_PRECOND_IDENTITY || p->kind > GLINALG_PRECOND_GCR) {
+    if (p->kind < GLINALG_PRECOND_IDENTITY || p->kind > GLINALG_PRECOND_MG) {
         set_last_error("unknown preconditioner kind");
         return GLINALG_ERROR_INVALID_VALUE;
+    }
+    if (p->kind == GLINALG_PRECOND_MG) {
+        if (!p->mg) {
+            set_last_error("the multigrid preconditioner needs a hierarchy (glinalg_mg_create)");
+            return GLINALG_ERROR_INVALID_VALUE;
+        }
+        out->kind = GLINALG_PRECOND_MG;
+        out->mg = p->mg;
+        out->level = 0;
+        return GLINALG_SUCCESS;
     }
     if (p->kind != GLINALG_PRECOND_IDENTITY && p->n_step < 0) {
         set_last_error("preconditioner n_step must not be negative");

@@ -309,6 +309,9 @@ glinalg_status mg_prolong(const glinalg_mg_level_s *l, double2 *fine, const doub
     return GLINALG_SUCCESS;
 }
 
+long mg_level_fine_size(const glinalg_mg_level_s *l) { return l->fsize; }
+long mg_level_coarse_size(const glinalg_mg_level_s *l) { return l->csize; }
+
 glinalg_status mg_restrict(const glinalg_mg_level_s *l, double2 *coarse, const double2 *fine, cudaStream_t st)
 {
     k_restrict<<<grid(l->csize), 128, 0, st>>>(coarse, fine, lv_of(l));

@@ -41,7 +41,14 @@ struct Precond {
     int n_step = 0;
     double rel_res = 0.0;
     const glinalg_operator_s *op = nullptr;
+    const glinalg_mg_s *mg = nullptr;  // GLINALG_PRECOND_MG
+    int level = 0;                     // the level the multigrid preconditioner starts on
 };
+// One application of the multigrid preconditioner at `level` (mg_precond.cu).
+glinalg_status mg_apply(const glinalg_mg_s *mg, int level, double2 *lhs, const double2 *rhs, const Verb &verb,
+                        cudaStream_t st);
+long mg_level_fine_size(const glinalg_mg_level_s *l);
+long mg_level_coarse_size(const glinalg_mg_level_s *l);
 glinalg_status cr_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
                        double eps, const Verb &verb, glinalg_info *info, cudaStream_t st);
 glinalg_status cr_restart_fp64(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,

@@ -1295,6 +1295,7 @@ glinalg_status precond_apply(const Precond &pc, const glinalg_operator_s *op, do
     switch (pc.kind) {
     case GLINALG_PRECOND_MINRES: return minres_fp64(pop, z, r, pc.n_step, pc.rel_res, 1.0, vprec, &tmp, st);
     case GLINALG_PRECOND_GCR: return gcr_fp64(pop, z, r, pc.n_step, pc.rel_res, vprec, &tmp, st);
+    case GLINALG_PRECOND_MG: return mg_apply(pc.mg, pc.level, z, r, vprec, st);
     default:
         GL_CUDA(cudaMemcpyAsync(z, r, sizeof(double2) * op->size, cudaMemcpyDeviceToDevice, st));
         return GLINALG_SUCCESS;

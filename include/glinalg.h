@@ -290,13 +290,16 @@ glinalg_status glinalg_bicgstab_m(glinalg_operator op, double *const *phi, const
 typedef enum glinalg_precond_kind {
     GLINALG_PRECOND_IDENTITY = 0, /* identity_preconditioner  generic_precond.cpp:34 */
     GLINALG_PRECOND_MINRES = 1,   /* minres_preconditioner    generic_precond.cpp:53 */
-    GLINALG_PRECOND_GCR = 2       /* gcr_preconditioner       generic_precond.cpp:70 */
+    GLINALG_PRECOND_GCR = 2,      /* gcr_preconditioner       generic_precond.cpp:70 */
+    GLINALG_PRECOND_MG = 3        /* mg_preconditioner        mg_complex.cpp:514 (field mg) */
 } glinalg_precond_kind;
+typedef struct glinalg_mg_s *glinalg_mg;
 typedef struct glinalg_precond {
     int kind;             /* glinalg_precond_kind */
     int n_step;           /* {minres,gcr}_precond_struct_complex::n_step */
     double rel_res;       /* ::rel_res */
     glinalg_operator op;  /* ::matrix_vector / matrix_extra_data; NULL: the solve's operator */
+    glinalg_mg mg;        /* GLINALG_PRECOND_MG: the hierarchy (glinalg_mg_create) */
 } glinalg_precond;
 
 /* minv_vector_cg_flex_precond    generic_cg_flex_precond.cpp:223 (NULL precond: identity) */
@@ -370,6 +373,47 @@ glinalg_status glinalg_mg_restrict(glinalg_mg_level lv, double *coarse, const do
  * enter, as in the reference).  The coarse operator's own shifts are zero. */
 glinalg_status glinalg_mg_coarse_stencil(glinalg_mg_level lv, glinalg_operator fine, int ignore_shifts,
                                          glinalg_operator *coarse_out);
+
+/* The multigrid preconditioner mg_preconditioner (mg_complex.cpp:514) over a hierarchy of
+ * n_refine levels: ops[0] the fine operator, ops[l+1] the operator of the coarse lattice of
+ * levels[l] (for instance from glinalg_mg_coarse_stencil), levels[l] the transfer from
+ * ops[l] to ops[l+1].  params mirrors mg_precond_struct_complex (mg_complex.h). */
+#define GLINALG_MG_MAX_LEVELS 8
+/* minv_inverter (generic_inverters.h:70-81): the smoother */
+#define GLINALG_MINV_INVALID -1
+#define GLINALG_MINV_CG 0
+#define GLINALG_MINV_CR 1
+#define GLINALG_MINV_GCR 2
+#define GLINALG_MINV_BICGSTAB 3
+#define GLINALG_MINV_BICGSTAB_L 4
+#define GLINALG_MINV_MINRES 7
+/* inner_solver (mg.h:5-14): the coarse solver */
+#define GLINALG_MG_NONE 0
+#define GLINALG_MG_MINRES 1
+#define GLINALG_MG_CG 2
+#define GLINALG_MG_GCR 3
+#define GLINALG_MG_BICGSTAB 4
+#define GLINALG_MG_CR 5
+#define GLINALG_MG_BICGSTAB_L 6
+/* mg_multilevel_type (mg_complex.h) */
+#define GLINALG_MLEVEL_SMOOTH 0
+#define GLINALG_MLEVEL_RECURSIVE 1
+typedef struct glinalg_mg_params {
+    int smoother;                              /* in_smooth_type (GLINALG_MINV_*) */
+    double omega_smooth;                       /* kept for the interface; the MinRes smoother uses 1 */
+    int n_pre_smooth[GLINALG_MG_MAX_LEVELS];   /* per level */
+    int n_post_smooth[GLINALG_MG_MAX_LEVELS];
+    int normal_eqn_mg, normal_eqn_smooth;      /* must be 0: normal-equation variants not supported */
+    int mlevel_type;                           /* GLINALG_MLEVEL_* */
+    int coarse_solver;                         /* in_solve_type (GLINALG_MG_*) */
+    int n_max, n_restart;
+    double rel_res[GLINALG_MG_MAX_LEVELS];
+} glinalg_mg_params;
+glinalg_status glinalg_mg_create(int n_refine, const glinalg_operator *ops, const glinalg_mg_level *levels,
+                                 const glinalg_mg_params *params, glinalg_mg *out);
+glinalg_status glinalg_mg_destroy(glinalg_mg mg);
+/* One application lhs = M^-1 rhs on the finest level (fields of ops[0]'s size). */
+glinalg_status glinalg_mg_apply(glinalg_mg mg, double *lhs, const double *rhs, int flags);
 
 /* ---- batched solves (no reference counterpart: the reference solves systems one at a
  * time in a loop; these run many independent systems in one device launch sequence) ---- */

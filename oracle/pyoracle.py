@@ -384,6 +384,10 @@ class RefOracle:
         L.ref_mg_block.argtypes = [C.c_int] + [C.c_int] * 6 + [_dp]
         L.ref_mg_transfer.argtypes = [C.c_int] + [C.c_int] * 6 + [_dp, _dp, _dp]
         L.ref_mg_coarse.argtypes = [C.c_int] * 6 + [_dp, _dp, _dp, _dp, C.c_int, _dp, _dp]
+        ip = C.POINTER(C.c_int)
+        L.ref_mg_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, _dp, C.c_int, ip, ip, _dp, C.c_int, ip,
+                                   ip, C.c_int, C.c_int, C.c_int, _dp, C.c_int, _dp, _dp, C.c_int, C.c_double, _dp,
+                                   C.c_char_p, C.c_int]
         L.ref_topo.argtypes = [_dp, C.c_int, C.c_int]
         L.ref_topo.restype = C.c_double
         L.ref_gauge_trans.argtypes = [C.c_uint, _dp, _dp, C.c_int, C.c_int]
@@ -563,3 +567,22 @@ class RefOracle:
         self.lib.ref_mg_coarse(lx, ly, nc_f, bx, by, nc_c, _ptr(nv), _ptr(fine.clover), _ptr(fine.hopping),
                                _ptr(fine.shifts6()), int(ignore_shifts), _ptr(clov), _ptr(hop))
         return clov, hop
+
+    def mg_solve(self, outer, links, lx, ly, mass, b, blocks, nvecs, null_vectors, smoother, n_pre, n_post,
+                 inner, n_max, n_restart, rel_res, mlevel=0, max_iter=10000, eps=1e-10):
+        """The reference's flexible solve (outer "fpcg" / "vpgcr") preconditioned by its
+        mg_preconditioner; null_vectors: the concatenated Gaussian inputs of every level.
+        Returns (phi, info, log)."""
+        nr = len(blocks)
+        I = lambda a: (C.c_int * len(a))(*a)
+        nv = np.array(null_vectors, dtype=np.complex128).reshape(-1).copy()
+        phi = np.zeros(lx * ly, np.complex128)
+        b = np.ascontiguousarray(b, dtype=np.complex128)
+        info = np.zeros(4)
+        log = C.create_string_buffer(1 << 22)
+        rr = np.ascontiguousarray(rel_res, dtype=np.float64)
+        self.lib.ref_mg_solve({"fpcg": 0, "vpgcr": 1}[outer], lx, ly, mass, _ptr(np.ascontiguousarray(links)), nr,
+                              I(blocks), I(nvecs), _ptr(nv), smoother, I(n_pre), I(n_post), inner, n_max, n_restart,
+                              _ptr(rr), mlevel, _ptr(phi), _ptr(b), max_iter, eps, _ptr(info), log, 1 << 22)
+        d = {"resSq": info[0], "iter": int(info[1]), "success": bool(info[2]), "ops_count": int(info[3])}
+        return phi, d, log.value.decode()

@@ -522,4 +522,122 @@ void ref_mg_coarse(int lx, int ly, int nc_f, int bx, int by, int nc_c, double *n
     std::memcpy(chopping, coarse.hopping, sizeof(cd) * vc * 4);
 }
 
+// An outer flexible solve (outer 0: minv_vector_cg_flex_precond, 1: minv_vector_gcr_var_precond)
+// of the staggered operator on lx x ly (stencil form, shift = mass) preconditioned by the
+// reference's mg_preconditioner (mg_complex.cpp:514) over n_refine levels.  Level l blocks
+// bs[l] x bs[l] with nvec[l] null vectors taken from nv (Gaussian inputs, concatenated per
+// level), block-orthonormalised and turned into Galerkin coarse stencils here, as the
+// reference's driver does after its null-vector generation.  smoother: minv_inverter;
+// inner: inner_solver; mlevel: mg_multilevel_type.
+void ref_mg_solve(int outer, int lx, int ly, double mass, const double *links, int n_refine, const int *bs,
+                  const int *nvec, double *nv, int smoother, const int *n_pre, const int *n_post, int inner,
+                  int n_max, int n_restart, const double *rel_res, int mlevel, double *phi, const double *phi0,
+                  int max_iter, double eps, double *info4, char *log, int log_cap)
+{
+    const int L = n_refine + 1;
+    std::vector<Lattice *> lat(L);
+    std::vector<stencil_2d *> sten(L);
+    std::vector<int> bx(n_refine), by(n_refine), nvs(n_refine);
+    std::vector<cd **> vecs(n_refine);
+    int dims[2] = {lx, ly}, nc = 1;
+    lat[0] = new Lattice(2, dims, 1);
+    for (int l = 0; l < n_refine; l++) {
+        bx[l] = by[l] = bs[l];
+        nvs[l] = nvec[l];
+        dims[0] /= bs[l];
+        dims[1] /= bs[l];
+        lat[l + 1] = new Lattice(2, dims, nvec[l]);
+    }
+    staggered_u1_op stag;
+    stag.lattice = (cd *)links;
+    stag.mass = mass;
+    stag.x_fine = lx;
+    stag.y_fine = ly;
+    stag.Nc = 1;
+    stag.wilson_coeff = 0.0;
+    sten[0] = new stencil_2d(lat[0], 1);
+    get_square_staggered_u1_stencil(sten[0], &stag);
+    for (int l = 1; l < L; l++) sten[l] = new stencil_2d(lat[l], 1);
+    long off = 0;
+    for (int l = 0; l < n_refine; l++) {
+        const long fs = lat[l]->get_lattice_size();
+        vecs[l] = new cd *[nvec[l]];
+        for (int c = 0; c < nvec[l]; c++) vecs[l][c] = (cd *)nv + off + (long)c * fs;
+        off += (long)nvec[l] * fs;
+    }
+    mg_operator_struct_complex mg;
+    mg.x_fine = lx;
+    mg.y_fine = ly;
+    mg.n_refine = n_refine;
+    mg.blocksize_x = bx.data();
+    mg.blocksize_y = by.data();
+    mg.Nc = nc;
+    mg.latt = lat.data();
+    mg.stencils = sten.data();
+    mg.have_dagger_stencil = false;
+    mg.dagger_stencils = nullptr;
+    mg.n_vectors = nvs.data();
+    mg.null_vectors = vecs.data();
+    mg.matrix_vector = square_staggered_u1;
+    mg.matrix_vector_dagger = square_staggered_dagger_u1;
+    mg.matrix_extra_data = &stag;
+    mg.curr_level = 0;
+    mg.curr_dof_fine = 1;
+    mg.curr_x_fine = lx;
+    mg.curr_y_fine = ly;
+    mg.curr_fine_size = lx * ly;
+    mg.curr_dof_coarse = nvec[0];
+    mg.curr_x_coarse = lat[1]->get_lattice_dimension(0);
+    mg.curr_y_coarse = lat[1]->get_lattice_dimension(1);
+    mg.curr_coarse_size = lat[1]->get_lattice_size();
+    mg.dslash_count = new dslash_tracker(n_refine);
+    // null vectors, then the coarse stencils, level by level (going down and back up)
+    for (int l = 0; l < n_refine; l++) {
+        block_orthonormalize(&mg);
+        generate_coarse_from_fine_stencil(sten[l + 1], sten[l], &mg);
+        if (l + 1 < n_refine) level_down(&mg);
+    }
+    for (int l = 0; l + 1 < n_refine; l++) level_up(&mg);
+    std::vector<int> pre(n_pre, n_pre + n_refine), post(n_post, n_post + n_refine);
+    std::vector<double> rr(rel_res, rel_res + n_refine);
+    mg_precond_struct_complex mgp;
+    mgp.in_smooth_type = (minv_inverter)smoother;
+    mgp.omega_smooth = 1.0;
+    mgp.n_pre_smooth = pre.data();
+    mgp.n_post_smooth = post.data();
+    mgp.normal_eqn_mg = false;
+    mgp.normal_eqn_smooth = false;
+    mgp.mlevel_type = (mg_multilevel_type)mlevel;
+    mgp.in_solve_type = (inner_solver)inner;
+    mgp.n_max = n_max;
+    mgp.n_restart = n_restart;
+    mgp.rel_res = rr.data();
+    mgp.mgstruct = &mg;
+    mgp.fine_matrix_vector = fine_square_staggered;
+    mgp.coarse_matrix_vector = coarse_square_staggered;
+    mgp.fine_matrix_vector_dagger = fine_square_staggered_dagger;
+    mgp.coarse_matrix_vector_dagger = coarse_square_staggered_dagger;
+    mgp.fine_matrix_vector_normal = fine_square_staggered_normal;
+    mgp.coarse_matrix_vector_normal = coarse_square_staggered_normal;
+    mgp.matrix_extra_data = &mg;
+    std::vector<cd> b((const cd *)phi0, (const cd *)phi0 + (long)lx * ly);
+    inversion_verbose_struct verb = make_verb(1, "[MGSOLVE] ");
+    inversion_info inv;
+    with_log(log, log_cap, [&]() {
+        if (outer == 0)
+            inv = minv_vector_cg_flex_precond((cd *)phi, b.data(), lx * ly, max_iter, eps, fine_square_staggered, &mg,
+                                              mg_preconditioner, &mgp, &verb);
+        else
+            inv = minv_vector_gcr_var_precond((cd *)phi, b.data(), lx * ly, max_iter, eps, fine_square_staggered, &mg,
+                                              mg_preconditioner, &mgp, &verb);
+    });
+    fill_info(inv, info4, nullptr, 0);
+    delete mg.dslash_count;
+    for (int l = 0; l < n_refine; l++) delete[] vecs[l];
+    for (int l = 0; l < L; l++) {
+        delete sten[l];
+        delete lat[l];
+    }
+}
+
 }  // extern "C"

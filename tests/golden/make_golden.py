@@ -254,6 +254,48 @@ def main():
     vec["mg16_tb_prepare"] = R.tbprec(0, tbop, xin)
     vec["mg16_tb_reconstruct"] = R.tbprec(1, tbop, vc, xin)
 
+    # ---- the multigrid preconditioner (mg_complex.cpp:514) inside the variably preconditioned
+    # GCR on D, 32x32, m = 0.1: null vectors = 4 Gaussian vectors (numpy seed 11) smoothed by
+    # 20 iterations of the reference's CG on D^dagger D, split into even and odd parts (8
+    # vectors); 2 levels (4x4 blocks, MinRes smoother 2 + 2, GCR(32) coarse solves to 1e-2,
+    # n_max 64) and 3 levels (then 2x2 blocks with 8 Gaussian vectors); 30 outer iterations
+    rng = np.random.default_rng(11)
+    y_, x_ = np.divmod(np.arange(1024), 32)
+    ev = (x_ + y_) % 2 == 0
+    sm = []
+    for _ in range(4):
+        v = rng.normal(size=1024) + 1j * rng.normal(size=1024)
+        xs, _, _ = R.solve("cg", normal, v, max_iter=20, eps=1e-30)
+        sm.append(xs)
+    nv1 = np.concatenate([v * ev for v in sm] + [v * (~ev) for v in sm])
+    nv2 = rng.normal(size=8 * 512) + 1j * rng.normal(size=8 * 512)
+    vec["mgs_nv1"], vec["mgs_nv2"] = nv1, nv2
+    U, b = vec["l32_links"], vec["l32_src"]
+    # mgs2: coarse GCR(32) to 1e-2 (n_max 64); mgs2f / mgs3f: fixed coarse work (16 GCR
+    # iterations, rel_res 1e-30), a preconditioner that does not depend on where a tolerance
+    # test falls
+    for key, blocks, nvecs, nv, n_max, rr in (("mgs2", [4], [8], nv1, 64, 1e-2),
+                                              ("mgs2f", [4], [8], nv1, 16, 1e-30),
+                                              ("mgs3f", [4, 2], [8, 8], np.concatenate([nv1, nv2]), 16, 1e-30)):
+        nr = len(blocks)
+        sys.stdout.flush()
+        fd, nul = os.dup(1), os.open(os.devnull, os.O_WRONLY)
+        os.dup2(nul, 1)  # the reference's mg_preconditioner prints its progress with printf
+        try:
+            xs, d, log = R.mg_solve("vpgcr", U, 32, 32, 0.1, b, blocks, nvecs, nv, 7, [2] * nr, [2] * nr, 3, n_max,
+                                    32, [rr] * nr, max_iter=30)
+        finally:
+            import ctypes
+            ctypes.CDLL(None).fflush(None)
+            os.dup2(fd, 1)
+            os.close(fd)
+            os.close(nul)
+        vec[f"{key}_solution"] = xs
+        summary = [l for l in log.splitlines() if l.startswith("[MGSOLVE]")]
+        info["cases"][key] = {**d, "summary": summary[-1], "blocks": blocks, "nvecs": nvecs, "max_iter": 30,
+                              "smoother": 7, "n_pre": 2, "n_post": 2, "coarse": 3, "n_max": n_max, "n_restart": 32,
+                              "rel_res": rr, "mass": 0.1}
+
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     with open(os.path.join(HERE, "reference_info.json"), "w") as f:
         json.dump(info, f, indent=1, default=lambda o: o.item() if hasattr(o, "item") else str(o))
