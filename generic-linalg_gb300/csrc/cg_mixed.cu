@@ -410,15 +410,17 @@ struct PersistKernel {
 // Persistent-kernel shapes (warps per block, rows per thread); one block per SM.  Candidates
 // 4 and 5 are the bulk-copy kernel (stag_bulk.cuh: 16 warps, tiles staged through shared
 // memory); candidates 6-8 are the rectangle-resident kernel (stag_resident.cuh, FP32 only):
-// 16 warps with x_lo in registers, 32 warps, 16 warps with x_lo in global memory.
-constexpr int kNumPersist = 9;
+// 16 warps with x_lo in registers, 32 warps, 16 warps with x_lo in global memory; candidates
+// 9 and 10 its single-reduction form (k_resident1) with 16 and 32 warps.
+constexpr int kNumPersist = 11;
 static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8,
-                                            res::kWX * 4};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0};
-constexpr int kResidentCand = 6;  // 6, 7 and 8
-static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 2; }
-static int resident_wy(int c) { return c == kResidentCand + 1 ? 8 : 4; }
+                                            res::kWX * 4, res::kWX * 4, res::kWX * 8};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0};
+constexpr int kResidentCand = 6;  // 6 .. 10
+static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 4; }
+static int resident_wy(int c) { return c == kResidentCand + 1 || c == kResidentCand + 4 ? 8 : 4; }
 static bool resident_xreg(int c) { return c == kResidentCand; }
+static bool resident_single(int c) { return c >= kResidentCand + 3; }
 
 // The rectangle grid of the resident kernel on this device (its static shared memory, the
 // reduction scratch, comes out of the same per-block budget: 512 bytes are kept for it).
@@ -455,13 +457,27 @@ static bool any_persist_applies(int lx, int ly, int variant)
 }
 
 template <class S, class R, class LK>
-static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy, bool xreg)
+static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy, bool xreg, bool single)
 {
     if constexpr (std::is_same<S, float2>::value && std::is_same<R, float2>::value &&
                   std::is_same<LK, float2>::value) {
         pk.plan = resident_plan(lx, ly, wy);
-        if (!pk.plan.ok || pk.plan.gx * pk.plan.gy > res::kMaxBlocks) return;
-        if (wy == 4 && xreg) {
+        if (!pk.plan.ok || pk.plan.gx * pk.plan.gy > (single ? res::kMaxBlocks1 : res::kMaxBlocks)) return;
+        if (single) {
+            if (wy == 4) {
+                switch (pk.plan.ny) {
+                case 4: pk.fr = k_resident1<4, 4>; break;
+                case 8: pk.fr = k_resident1<8, 4>; break;
+                default: pk.fr = k_resident1<14, 4>; break;
+                }
+            } else {
+                switch (pk.plan.ny) {
+                case 2: pk.fr = k_resident1<2, 8>; break;
+                case 4: pk.fr = k_resident1<4, 8>; break;
+                default: pk.fr = k_resident1<7, 8>; break;
+                }
+            }
+        } else if (wy == 4 && xreg) {
             switch (pk.plan.ny) {
             case 4: pk.fr = k_resident<4, 4, true>; break;
             case 8: pk.fr = k_resident<8, 4, true>; break;
@@ -493,7 +509,7 @@ static PersistKernel<S, R, LK> persist_cand(int c, int lx, int ly)
     pk.by = kPersistBY[c];
     pk.ny = kPersistNY[c];
     if (is_resident(c)) {
-        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xreg(c));
+        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xreg(c), resident_single(c));
         if (!pk.fr) return pk;
         const void *fp = reinterpret_cast<const void *>(pk.fr);
         int per_sm = 0;

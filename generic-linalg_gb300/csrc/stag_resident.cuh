@@ -164,6 +164,8 @@ constexpr long long kSpinCycles = 4000000000LL;  // about 2 s at GB300 clocks
 
 struct PhaseFlags {
     unsigned long long w[2][kMaxBlocks];  // partial-sum words by phase parity
+    // the single-reduction kernel's four partials per block, by iteration parity
+    unsigned long long w4[2][kMaxBlocks][4];
     unsigned epoch;                       // phases completed by all launches so far
     int error;
 };
@@ -351,6 +353,122 @@ __device__ __forceinline__ float sum_partials(const float *sm_part, unsigned nb)
     }
     return hi + lo;
 }
+
+// Publishes the four partial sums of a block (FP32 within warps and across the block's warps;
+// thread 0 writes two tagged 128-bit words), then the border of F as publish() does.
+template <int NW>
+__device__ __forceinline__ void publish4(float4 acc, PhaseFlags *pf, unsigned e, float4 *sm_w4, const float2 *F,
+                                         unsigned long long *M, int nborder, int bpos, int bslot)
+{
+    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_down_sync(0xffffffffu, acc.z, o);
+        acc.w += __shfl_down_sync(0xffffffffu, acc.w, o);
+    }
+    if (lane == 0) sm_w4[warp] = acc;
+    __syncthreads();
+    if (warp == 0) {
+        float4 v = lane < NW ? sm_w4[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+            v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+            v.z += __shfl_down_sync(0xffffffffu, v.z, o);
+            v.w += __shfl_down_sync(0xffffffffu, v.w, o);
+        }
+        if (lane == 0) {
+            unsigned long long *w = pf->w4[(e >> 1) & 1][blockIdx.x];
+            st_relaxed_2u64(w, tag(e, v.x), tag(e, v.y));
+            st_relaxed_2u64(w + 2, tag(e, v.z), tag(e, v.w));
+        }
+    }
+    if (tid < nborder) {
+        const float2 v = F[bpos];
+        st_relaxed_2u64(M + 2 * bslot, tag(e, v.x), tag(e, v.y));
+    }
+}
+
+// Posts the border of F (thread k < nborder posts border slot k), with no partial sum.
+__device__ __forceinline__ void publish_border(unsigned e, const float2 *F, unsigned long long *M, int nborder,
+                                               int bpos, int bslot)
+{
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    if (tid < nborder) {
+        const float2 v = F[bpos];
+        st_relaxed_2u64(M + 2 * bslot, tag(e, v.x), tag(e, v.y));
+    }
+}
+
+// Thread b waits until block b's four partial words carry epoch e and stages them.
+__device__ __forceinline__ void poll_partial4(PhaseFlags *pf, unsigned e, int b, float4 *sm_part4, int *err)
+{
+    const unsigned long long *w = pf->w4[(e >> 1) & 1][b];
+    const long long t0 = clock64();
+    for (unsigned n = 1;; n++) {
+        unsigned long long a0, a1, a2, a3;
+        ld_relaxed_2u64(w, a0, a1);
+        ld_relaxed_2u64(w + 2, a2, a3);
+        if ((unsigned)(a0 >> 32) == e && (unsigned)(a1 >> 32) == e && (unsigned)(a2 >> 32) == e &&
+            (unsigned)(a3 >> 32) == e) {
+            sm_part4[b] = make_float4(__uint_as_float((unsigned)a0), __uint_as_float((unsigned)a1),
+                                      __uint_as_float((unsigned)a2), __uint_as_float((unsigned)a3));
+            return;
+        }
+        if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
+            atomicExch(&pf->error, 1);
+            *err = 1;
+            sm_part4[b] = make_float4(0.f, 0.f, 0.f, 0.f);
+            return;
+        }
+    }
+}
+
+// Compensated sums of the four components of the staged partials, in block order (warp 0),
+// the four chains interleaved; the totals are in lane 0.
+__device__ __forceinline__ float4 sum_partials4(const float4 *sm_part4, unsigned nb)
+{
+    const int lane = threadIdx.x;
+    float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int b = lane; b < (int)nb; b += 32) {
+        const float4 v = sm_part4[b];
+        float c;
+        two_sum(hi.x, v.x, hi.x, c);
+        lo.x += c;
+        two_sum(hi.y, v.y, hi.y, c);
+        lo.y += c;
+        two_sum(hi.z, v.z, hi.z, c);
+        lo.z += c;
+        two_sum(hi.w, v.w, hi.w, c);
+        lo.w += c;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float c;
+        float h2 = __shfl_down_sync(0xffffffffu, hi.x, o), l2 = __shfl_down_sync(0xffffffffu, lo.x, o);
+        two_sum(hi.x, h2, hi.x, c);
+        lo.x += l2 + c;
+        h2 = __shfl_down_sync(0xffffffffu, hi.y, o);
+        l2 = __shfl_down_sync(0xffffffffu, lo.y, o);
+        two_sum(hi.y, h2, hi.y, c);
+        lo.y += l2 + c;
+        h2 = __shfl_down_sync(0xffffffffu, hi.z, o);
+        l2 = __shfl_down_sync(0xffffffffu, lo.z, o);
+        two_sum(hi.z, h2, hi.z, c);
+        lo.z += l2 + c;
+        h2 = __shfl_down_sync(0xffffffffu, hi.w, o);
+        l2 = __shfl_down_sync(0xffffffffu, lo.w, o);
+        two_sum(hi.w, h2, hi.w, c);
+        lo.w += l2 + c;
+    }
+    return make_float4(hi.x + lo.x, hi.y + lo.y, hi.z + lo.z, hi.w + lo.w);
+}
+
+// Blocks of the single-reduction kernel: a GB300 has 152 SMs (the four partials of each block
+// are staged in static shared memory, which shares the per-block budget with the rectangle).
+constexpr int kMaxBlocks1 = 160;
 
 }  // namespace res
 
@@ -600,6 +718,287 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     }
     if (blockIdx.x == 0 && tid == 0) {
         pf->epoch = ep;  // every block ran the same phases
+        s->k = sc.k;
+        s->rmax = sc.rmax;
+        s->rsq = sc.rsq;
+        s->beta = sc.beta;
+        s->rsq_new = sc.rn;
+        s->parity = 0;
+        if (sc.status >= 0) {
+            s->status = sc.status;
+            s->done = 1;
+        }
+        if (sc.reliable) s->reliable = 1;
+        s->inner_ns += gtimer() - t_start;
+        s->inner_iters += sc.iters;
+        s->inner_launches += 1;
+    }
+}
+
+// ---------------------------------------------------------------- single-reduction form
+//
+// k_resident1 runs the same CG on A = D^dagger D + sigma with one grid-wide sum per iteration
+// instead of two.  Iteration k, from r_k, the previous direction p and s = A p:
+//   A: u = D r_k (ring of r); partials gamma = |r_k|^2, delta = <r_k, A r_k> = |u|^2 + sigma
+//      |r_k|^2, rho = Re <r_k, s>, pi = Re <p, s>; export the border of u.
+//   B: w = A r_k = D^dagger u + sigma r_k (ring of u); then the four totals: beta =
+//      gamma / gamma_old, <p', A p'> = delta + 2 beta rho + beta^2 pi for p' = r_k + beta p
+//      (an identity of the Hermitian A, with no orthogonality assumed), alpha = gamma / <p', A p'>;
+//      p' = r_k + beta p, s' = w + beta s, x_lo += alpha p', r -= alpha s'; export the border of r.
+// The stopping tests run on gamma where the two-sum kernel runs them (after the residual's
+// total, before the direction is updated), so the state at exit is the same: r, the previous
+// direction, x_lo, and beta / rsq as that kernel leaves them.  On entry s = A p is formed from
+// the direction p with two stencils (the ring of D p computed from global memory).
+//
+// Measured at 1024^2 (m = 0.01, 2100 inner iterations): 10.9 us per iteration with 16 warps
+// against 8.5 us for k_resident.  The third per-site vector (s) takes the 16-warp kernel to
+// its 128-register limit (with spills, whose reloads go to L2 here, since shared memory leaves
+// 28 KB of L1), and the 32-warp kernel spills more; the saved grid-wide sum does not make up for
+// it.  The autotuner keeps both as candidates.
+//
+// Exchange: u and r borders go through the two mailboxes as in k_resident; a slot is rewritten
+// one iteration later, and a block gets there only after the neighbour that reads the slot has
+// posted its next border, which it does after reading the slot.  The partial words alternate
+// by iteration between two arrays; a block rewrites an array only after the next iteration's
+// sum, which every block joins only after it has read the array.
+
+template <int NY, int WY>
+__global__ void __launch_bounds__(32 * res::kWX * WY, 1)
+k_resident1(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, float mass, float sigma, int lx, int ly,
+            MxDev *s, res::PhaseFlags *pf, unsigned long long *mbox, int ty, int gx)
+{
+    using namespace res;
+    constexpr int NW = kWX * WY, NT = 32 * NW;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ float4 sm_w4[32];
+    __shared__ float sm_alpha, sm_beta;
+    __shared__ int sm_ctl, sm_err;
+    __shared__ ResScalars sc;
+    __shared__ float4 sm_part4[kMaxBlocks1];
+    if (s->done || s->reliable) return;
+    const long long t_start = gtimer();
+    const unsigned nb = gridDim.x;
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    const int tid = warp * 32 + lane;
+    const int xl = (warp % kWX) * 32 + lane, yb = (warp / kWX) * NY;
+    const int bx = blockIdx.x % gx, by = blockIdx.x / gx, gy = (int)nb / gx;
+    const int x0 = bx * kTX, y0 = by * ty;
+    const int tyb = min(ty, ly - y0);
+    const int nrow = min(NY, tyb - yb);
+    const int nring = 2 * kTX + 2 * tyb;
+    const int nslot = mbox_slots(ty);
+    const int nb_l = by * gx + (bx + gx - 1) % gx, nb_r = by * gx + (bx + 1) % gx;
+    const int nb_d = ((by + gy - 1) % gy) * gx + bx, nb_u = ((by + 1) % gy) * gx + bx;
+    unsigned long long *const Mr = mbox, *const Mu = mbox + 2 * (size_t)nb * nslot;
+    Rect R;
+    R.HX = reinterpret_cast<float2 *>(smraw);
+    R.HY = R.HX + (size_t)ty * kTX;
+    R.F = R.HY + (size_t)ty * kTX;
+    R.T = R.F + (ty + 2) * kPW;
+    R.HxL = R.T + (ty + 2) * kPW;
+    R.HyB = R.HxL + ty;
+    float2 *const Rr = R.F, *const Ru = R.T;
+    const bool has_ring = tid < nring;
+    int rslot = 0, rgi = 0, rsrc = 0;
+    if (has_ring) {
+        ring_site(tid, tyb, x0, y0, lx, ly, rslot, rgi);
+        rsrc = ring_source(tid, ty, tyb, nslot, nb_l, nb_r, nb_d, nb_u);
+    }
+    const int nborder = nring;
+    int bpos = 0, bslot = 0;
+    if (tid < nborder) {
+        border_slot(tid, ty, tyb, bpos, bslot);
+        bslot += (int)blockIdx.x * nslot;
+    }
+    const int grow = (y0 + yb) * lx + x0 + xl;
+    if (tid == 0) {
+        sm_err = 0;
+        sc.rsq = (float)s->rsq;
+        sc.rmax = (float)fmin(s->rmax, 1e38);
+        sc.rn = 0.f;
+        sc.beta = (float)s->beta;
+        sc.scale = (float)s->scale;
+        sc.delta = (float)s->delta;
+        sc.stop = (float)(s->eps * sqrt(s->bsq));
+        sc.k = s->k;
+        sc.max_iter = s->max_iter;
+        sc.status = -1;
+        sc.reliable = 0;
+        sc.iters = 0;
+    }
+
+    // ---- entry: r, links and the direction p on chip; s = A p (D p into the u buffer with its
+    // ring, then D^dagger of it)
+    float2 pv[NY], sv[NY], tmp[NY];
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        const int yl = yb + q;
+        pv[q] = make_float2(0.f, 0.f);
+        sv[q] = make_float2(0.f, 0.f);
+        if (q < nrow) {
+            const int gi = grow + q * lx;
+            Rr[(yl + 1) * kPW + xl + 1] = __ldcg(r + gi);
+            pv[q] = __ldcg(p0 + gi);
+            Ru[(yl + 1) * kPW + xl + 1] = pv[q];
+            const float4 h = __ldg(reinterpret_cast<const float4 *>(H) + gi);
+            R.HX[yl * kTX + xl] = make_float2(h.x, h.y);
+            R.HY[yl * kTX + xl] = make_float2(h.z, h.w);
+        }
+    }
+    for (int k = tid; k < tyb + kTX; k += NT) {
+        if (k < tyb) {
+            const int xm = x0 == 0 ? lx - 1 : x0 - 1;
+            R.HxL[k] = __ldg(H + 2 * ((y0 + k) * lx + xm));
+        } else {
+            const int ym = y0 == 0 ? ly - 1 : y0 - 1;
+            R.HyB[k - tyb] = __ldg(H + 2 * (ym * lx + x0 + (k - tyb)) + 1);
+        }
+    }
+    float2 dp_ring = make_float2(0.f, 0.f);
+    if (has_ring) {
+        Rr[rslot] = __ldcg(r + rgi);
+        Ru[rslot] = __ldcg(p0 + rgi);
+        // D p at the ring site, from global memory
+        const int gyy = rgi / lx, gxx = rgi - gyy * lx;
+        const int xp = gxx + 1 == lx ? 0 : gxx + 1, xm = gxx == 0 ? lx - 1 : gxx - 1;
+        const int yp = gyy + 1 == ly ? 0 : gyy + 1, ym = gyy == 0 ? ly - 1 : gyy - 1;
+        const float2 pc = __ldcg(p0 + rgi);
+        float2 hs = fmul(__ldg(H + 2 * rgi), __ldcg(p0 + gyy * lx + xp));
+        hs = fsub(hs, fmulc(__ldg(H + 2 * (gyy * lx + xm)), __ldcg(p0 + gyy * lx + xm)));
+        hs = fadd(hs, fmul(__ldg(H + 2 * rgi + 1), __ldcg(p0 + yp * lx + gxx)));
+        hs = fsub(hs, fmulc(__ldg(H + 2 * (ym * lx + gxx) + 1), __ldcg(p0 + ym * lx + gxx)));
+        dp_ring = fadd(fscale(mass, pc), hs);
+    }
+    __syncthreads();
+    {
+        auto body = [&](int q, int, float2 cur, float2 hs) { tmp[q] = fadd(fscale(mass, cur), hs); };
+        if (nrow == NY) hop_rows<NY, true>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+        else if (nrow > 0) hop_rows<NY, false>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < NY; q++)
+        if (q < nrow) Ru[(yb + q + 1) * kPW + xl + 1] = tmp[q];
+    if (has_ring) Ru[rslot] = dp_ring;
+    __syncthreads();
+    {
+        auto body = [&](int q, int, float2 cur, float2 hs) {
+            sv[q] = fadd(fsub(fscale(mass, cur), hs), fscale(sigma, pv[q]));
+        };
+        if (nrow == NY) hop_rows<NY, true>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+        else if (nrow > 0) hop_rows<NY, false>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+    }
+    __syncthreads();
+
+    unsigned ep = pf->epoch;
+    bool first = true;
+    for (;;) {
+        // ---- A: u = D r and the four partials; export the border of u
+        {
+            auto body = [&](int q, int, float2 cur, float2 hs) { tmp[q] = fadd(fscale(mass, cur), hs); };
+            if (nrow == NY) hop_rows<NY, true>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            else if (nrow > 0) hop_rows<NY, false>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+        }
+        const unsigned eA = ++ep;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int q = 0; q < NY; q++) {
+            if (q < nrow) {
+                const int c = (yb + q + 1) * kPW + xl + 1;
+                const float2 rv = Rr[c];
+                const float r2 = fn2(rv);
+                acc.x += r2;
+                acc.y += fn2(tmp[q]) + sigma * r2;
+                acc.z += rv.x * sv[q].x + rv.y * sv[q].y;
+                acc.w += pv[q].x * sv[q].x + pv[q].y * sv[q].y;
+                Ru[c] = tmp[q];
+            }
+        }
+        publish4<NW>(acc, pf, eA, sm_w4, Ru, Mu, nborder, bpos, bslot);
+        if (has_ring) Ru[rslot] = poll_slot(Mu + rsrc, eA, pf, &sm_err);
+        __syncthreads();
+        // ---- B: w = D^dagger u + sigma r, then the totals, the scalars and the updates
+        {
+            auto body = [&](int q, int yl, float2 cur, float2 hs) {
+                tmp[q] = fadd(fsub(fscale(mass, cur), hs), fscale(sigma, Rr[(yl + 1) * kPW + xl + 1]));
+            };
+            if (nrow == NY) hop_rows<NY, true>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            else if (nrow > 0) hop_rows<NY, false>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+        }
+        if (tid < (int)nb) poll_partial4(pf, eA, tid, sm_part4, &sm_err);
+        __syncthreads();
+        if (warp == 0) {
+            const float4 tot = sum_partials4(sm_part4, nb);
+            const float g = tot.x, d = tot.y, rh = tot.z, pi = tot.w;
+            if (lane == 0) {
+                int ctl = kResGo;
+                if (sm_err) {
+                    sc.status = GLINALG_SOLVE_TIMEOUT;
+                    ctl = kResStop;
+                } else if (!isfinite(g)) {
+                    sc.status = GLINALG_SOLVE_NONFINITE;
+                    ctl = kResStop;
+                } else if (!first) {
+                    sc.rn = g;
+                    sc.k++;
+                    sc.iters++;
+                    const float rho = sqrtf(g) * sc.scale;  // true-scale iterated residual
+                    if (rho > sc.rmax) sc.rmax = rho;
+                    if (rho < sc.delta * sc.rmax || rho < sc.stop || sc.k >= sc.max_iter) {
+                        sc.reliable = 1;
+                        ctl = kResReliable;
+                    }
+                }
+                if (ctl == kResGo) {
+                    const float beta = first ? sc.beta : g / sc.rsq;
+                    const float pap = d + 2.f * beta * rh + beta * beta * pi;  // <p', A p'>
+                    if (!(pap > 0.f) || !isfinite(pap)) {
+                        sc.status = pap == 0.f ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
+                        ctl = kResStop;
+                    } else {
+                        sc.beta = beta;
+                        sc.rsq = g;
+                        sm_beta = beta;
+                        sm_alpha = g / pap;
+                    }
+                }
+                sm_ctl = ctl;
+            }
+        }
+        __syncthreads();
+        if (sm_ctl != kResGo) break;
+        first = false;
+        const float alpha = sm_alpha, beta = sm_beta;
+        const unsigned eB = ++ep;
+#pragma unroll
+        for (int q = 0; q < NY; q++) {
+            if (q < nrow) {
+                const int c = (yb + q + 1) * kPW + xl + 1;
+                const float2 rv = Rr[c];
+                const float2 pn = fadd(rv, fscale(beta, pv[q]));
+                const float2 sn = fadd(tmp[q], fscale(beta, sv[q]));
+                pv[q] = pn;
+                sv[q] = sn;
+                red_add2(xlo + grow + q * lx, fscale(alpha, pn));
+                Rr[c] = fsub(rv, fscale(alpha, sn));
+            }
+        }
+        __syncthreads();
+        publish_border(eB, Rr, Mr, nborder, bpos, bslot);
+        if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err);
+        __syncthreads();
+    }
+    // ---- exit: r, the direction (to p0) back to global memory; x_lo is already there
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (q < nrow) {
+            const int gi = grow + q * lx;
+            r[gi] = Rr[(yb + q + 1) * kPW + xl + 1];
+            p0[gi] = pv[q];
+        }
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+        pf->epoch = ep;
         s->k = sc.k;
         s->rmax = sc.rmax;
         s->rsq = sc.rsq;
