@@ -419,6 +419,149 @@ def workload_siblings(args):
     print(json.dumps(line))
 
 
+def workload_rows(args):
+    """Measurements of the rows beyond the headline at 1024x1024 (links and source from
+    std::mt19937(1337)), L2 flushed before every timed call, device-resident fields:
+    even/odd preconditioning (prepare, the FP64 and FP32 CG on m^2 - D_eo D_oe to 1e-10,
+    reconstruct); the multigrid transfers of a 4x4-blocked level with 8 null vectors (prolong,
+    restrict, block orthonormalisation, the Galerkin coarse stencil and its apply); the gauge
+    utilities (plaquette, gauge transform, one APE sweep).  Algorithmic bytes count every array
+    read or written once; GB/s against the measured HBM copy bandwidth."""
+    import numpy as np
+    import torch
+    gl = importlib.import_module("generic-linalg_gb300")
+    L = gl.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
+    lx = ly = 1024
+    n = lx * ly
+    g = gl.Generator(SEED)
+    U = g.rand_gauge_u1(lx, ly)
+    b = g.gaussian(n)
+    Ud, bd = torch.from_numpy(U).to(dev), torch.from_numpy(b).to(dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    hbm = peaks()[0]
+
+    def timed(fn, reps=None):
+        ts, out = [], None
+        for i in range(args.warmup + (reps or args.steps)):
+            t, out = _flush_and_time(fn, flush, stream)
+            if i >= args.warmup:
+                ts.append(t)
+        return statistics.mean(ts), out
+
+    def rate(nbytes, ms):
+        return {"ms": round(ms, 4), "GBps": round(nbytes / (ms * 1e-3) / 1e9, 1),
+                "frac_of_hbm": round(nbytes / (ms * 1e-3) / 1e9 / hbm, 3)}
+
+    out = {}
+    # even/odd preconditioning (f1)
+    eo = gl.Operator(9, lx, ly, 0.01, Ud)
+    rhs_e = torch.zeros_like(bd)
+    ms, _ = timed(lambda: gl.square_staggered_eoprec_prepare(rhs_e, bd, eo))
+    out["eo_prepare"] = rate(16.0 * n * 4, ms)  # rhs, two links, rhs_e
+    for prec, nm in ((0, "eo_cg_fp64"), (1, "eo_cg_fp32_reliable")):
+        xe = torch.zeros_like(bd)
+
+        def solve():
+            xe.zero_()
+            return gl.minv_vector_cg(xe, rhs_e, n, 100000, EPS, gl.square_staggered_m2mdeodoe_u1, eo, precision=prec)
+        ms, info = timed(solve, reps=max(1, min(args.steps, 3)))
+        out[nm] = {"ms": round(ms, 3), "iters": info.iter, "success": info.success,
+                   "algorithmic_GBps": round(info.gbytes / (ms * 1e-3), 1)}
+    full = torch.zeros_like(bd)
+    ms, _ = timed(lambda: gl.square_staggered_eoprec_reconstruct(full, xe, bd, eo))
+    out["eo_reconstruct"] = rate(16.0 * n * 5, ms)
+    # multigrid transfers (f2): 4x4 blocks, 8 vectors -> 256x256x8
+    nc = 8
+    nv = torch.from_numpy(np.stack([g.gaussian(n) for _ in range(nc)])).to(dev)
+    lv = gl.MgLevel(lx, ly, 1, 4, 4, nc, nv)
+    csize = (lx // 4) * (ly // 4) * nc
+    ms, _ = timed(lambda: gl.block_orthonormalize(lv), reps=3)
+    out["mg_block_orthonormalize"] = rate(16.0 * n * nc * 4, ms)  # (nc-1) passes read+write ~ 2 r/w per vector
+    vc = torch.from_numpy(g.gaussian(csize)).to(dev)
+    fine = torch.zeros_like(bd)
+    ms, _ = timed(lambda: gl.prolong(fine, vc, lv))
+    out["mg_prolong"] = rate(16.0 * (n * nc + n + csize), ms)
+    coarse = torch.zeros_like(vc)
+    ms, _ = timed(lambda: gl.restrict(coarse, bd, lv))
+    out["mg_restrict"] = rate(16.0 * (n * nc + n + csize), ms)
+    st = gl.Stencil2D(lx, ly, 1, shift=0.01)
+    gl.get_square_staggered_u1_stencil(st, gl.StaggeredU1Op(U, 0.01, lx, ly))
+    fop = gl.Operator(4, lx, ly, nc=1, clover=st.clover, hopping=st.hopping, shift=st.shift)
+    ms, cop = timed(lambda: gl.generate_coarse_from_fine_stencil(None, fop, lv), reps=3)
+    out["mg_coarse_stencil"] = rate(16.0 * (n * nc + 5 * n + 5 * (csize // nc) * nc * nc), ms)
+    cin = torch.from_numpy(g.gaussian(csize)).to(dev)
+    cout = torch.zeros_like(cin)
+    ms, _ = timed(lambda: cop.apply(cout, cin))
+    out["mg_coarse_apply_256x256x8"] = rate(16.0 * (2 * csize + 5 * (csize // nc) * nc * nc), ms)
+    # gauge utilities (f4)
+    ms, _ = timed(lambda: gl.get_plaquette_u1(Ud, lx, ly))
+    out["plaquette"] = rate(16.0 * 2 * n, ms)
+    gt = torch.from_numpy(g.rand_trans_u1(lx, ly)).to(dev)
+    Uw = Ud.clone()
+    ms, _ = timed(lambda: gl.apply_gauge_trans_u1(Uw, gt, lx, ly))
+    out["gauge_trans"] = rate(16.0 * (4 * n + n), ms)
+    Us = torch.zeros_like(Ud)
+    ms, _ = timed(lambda: gl.apply_ape_smear_u1(Us, Ud, lx, ly, 0.5, 1))
+    out["ape_smear_1_sweep"] = rate(16.0 * 2 * n * 2 * 2, ms)  # copy in, sweep (read + write), copy out
+    line = {"workload": "rows beyond the headline, 1024x1024, m = 0.01", "steps": args.steps,
+            "warmup": args.warmup, "l2": "flushed (512 MiB write) before every call", "hbm_peak_GBps": hbm,
+            "rows": out}
+    if not args.no_cpu_baseline:
+        # the oracle (the reference's algorithms restated in C, one core) on the same inputs
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        O = pyoracle.Oracle()
+
+        def cpu(fn):
+            t0 = time.perf_counter()
+            r_ = fn()
+            return (time.perf_counter() - t0) * 1e3, r_
+
+        cpu_ms = {}
+        oeo = pyoracle.Operator("staggered_m2mdeodoe", lx, ly, 0.01, U)
+        cpu_ms["eo_prepare"], rhs_h = cpu(lambda: O.eoprec_prepare(oeo, b))
+        t10, _ = cpu(lambda: O.solve("cg", oeo, rhs_h, max_iter=10, eps=EPS))
+        cpu_ms["eo_cg_fp64"] = t10 / 10 * out["eo_cg_fp64"]["iters"]
+        cpu_ms["eo_reconstruct"], _ = cpu(lambda: O.eoprec_reconstruct(oeo, rhs_h, b))
+        nvh = nv.cpu().numpy()
+        cpu_ms["mg_block_orthonormalize"], P = cpu(lambda: O.mg_block("orthonormalize", lx, ly, 1, 4, 4, nc, nvh))
+        vch = vc.cpu().numpy()
+        cpu_ms["mg_prolong"], _ = cpu(lambda: O.mg_prolong(lx, ly, 1, 4, 4, nc, P, vch))
+        cpu_ms["mg_restrict"], _ = cpu(lambda: O.mg_restrict(lx, ly, 1, 4, 4, nc, P, b))
+        ofine = pyoracle.Operator("stencil", lx, ly, nc=1, clover=st.clover, hopping=st.hopping, shift=st.shift)
+        # the probing of generate_coarse_from_fine_stencil on a 256x256 block of the same form,
+        # scaled by the site count
+        lx4 = 256
+        U4 = U.reshape(ly, lx, 2)[:lx4, :lx4].reshape(-1)
+        st4 = gl.Stencil2D(lx4, lx4, 1, shift=0.01)
+        gl.get_square_staggered_u1_stencil(st4, gl.StaggeredU1Op(U4, 0.01, lx4, lx4))
+        o4 = pyoracle.Operator("stencil", lx4, lx4, nc=1, clover=st4.clover, hopping=st4.hopping, shift=st4.shift)
+        P4 = P.reshape(nc, ly, lx)[:, :lx4, :lx4].reshape(nc, -1)
+        t4, _ = cpu(lambda: O.mg_coarse_stencil(lx4, lx4, 1, 4, 4, nc, P4, o4))
+        cpu_ms["mg_coarse_stencil"] = t4 * (n / (lx4 * lx4))
+        del ofine
+        import ctypes
+        cl_h = np.zeros((csize // nc) * nc * nc, np.complex128)
+        hp_h = np.zeros(4 * (csize // nc) * nc * nc, np.complex128)
+        L.glinalg_operator_stencil_get(cop.handle, cl_h.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                       hp_h.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 0)
+        oc = pyoracle.Operator("stencil", lx // 4, ly // 4, nc=nc, clover=cl_h, hopping=hp_h)
+        cpu_ms["mg_coarse_apply_256x256x8"], _ = cpu(lambda: O.apply(oc, cin.cpu().numpy()))
+        cpu_ms["plaquette"], _ = cpu(lambda: O.plaquette(U, lx, ly))
+        cpu_ms["gauge_trans"], _ = cpu(lambda: O.gauge_trans(U, gt.cpu().numpy(), lx, ly))
+        cpu_ms["ape_smear_1_sweep"], _ = cpu(lambda: O.ape_smear(U, lx, ly, 0.5, 1))
+        line["cpu_baseline"] = {"unit": "ms per call", "cores": 1, "kind": "port",
+                                "values": {k: round(v, 3) for k, v in cpu_ms.items()},
+                                "sample": "the oracle on the same inputs, one call each; the FP64 even/odd CG "
+                                          "from 10 iterations scaled to the GPU's count; the coarse-stencil "
+                                          "probing on a 256x256 corner scaled by the site count"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -433,7 +576,8 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only time the two inner-iteration kernels of the headline variant "
                          "(a small case for ncu captures)")
-    ap.add_argument("--workload", default="headline", choices=["headline", "multishift", "batch", "siblings"],
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "multishift", "batch", "siblings", "rows"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")
     ap.add_argument("--probe-iters", type=int, default=0,
                     help="run one headline-variant solve stopped after this many inner iterations "
@@ -447,6 +591,8 @@ def main():
         return workload_batch(args)
     if args.workload == "siblings" and args.impl == "ours":
         return workload_siblings(args)
+    if args.workload == "rows" and args.impl == "ours":
+        return workload_rows(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.kernels_only:
