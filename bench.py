@@ -462,7 +462,7 @@ def workload_rows(args):
     rhs_e = torch.zeros_like(bd)
     ms, _ = timed(lambda: gl.square_staggered_eoprec_prepare(rhs_e, bd, eo))
     out["eo_prepare"] = rate(16.0 * n * 4, ms)  # rhs, two links, rhs_e
-    for prec, nm in ((0, "eo_cg_fp64"), (1, "eo_cg_fp32_reliable")):
+    for prec, nm in (() if args.rows_kernels else ((0, "eo_cg_fp64"), (1, "eo_cg_fp32_reliable"))):
         xe = torch.zeros_like(bd)
 
         def solve():
@@ -472,6 +472,8 @@ def workload_rows(args):
         out[nm] = {"ms": round(ms, 3), "iters": info.iter, "success": info.success,
                    "algorithmic_GBps": round(info.gbytes / (ms * 1e-3), 1)}
     full = torch.zeros_like(bd)
+    if args.rows_kernels:
+        xe = rhs_e
     ms, _ = timed(lambda: gl.square_staggered_eoprec_reconstruct(full, xe, bd, eo))
     out["eo_reconstruct"] = rate(16.0 * n * 5, ms)
     # multigrid transfers (f2): 4x4 blocks, 8 vectors -> 256x256x8
@@ -510,7 +512,7 @@ def workload_rows(args):
     line = {"workload": "rows beyond the headline, 1024x1024, m = 0.01", "steps": args.steps,
             "warmup": args.warmup, "l2": "flushed (512 MiB write) before every call", "hbm_peak_GBps": hbm,
             "rows": out}
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and not args.rows_kernels:
         # the oracle (the reference's algorithms restated in C, one core) on the same inputs
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
@@ -576,6 +578,8 @@ def main():
     ap.add_argument("--kernels-only", action="store_true",
                     help="only time the two inner-iteration kernels of the headline variant "
                          "(a small case for ncu captures)")
+    ap.add_argument("--rows-kernels", action="store_true",
+                    help="rows workload: the kernels only (no solves, no CPU baseline), for a launch list")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "multishift", "batch", "siblings", "rows"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")

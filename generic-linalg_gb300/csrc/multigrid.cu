@@ -62,13 +62,16 @@ __global__ void k_prolong(double2 *__restrict__ fine, const double2 *__restrict_
     }
 }
 
-// restrict (mg_complex.cpp:421-467): coarse(X, c) = sum over the block of conj(P_c(f)) fine(f)
+// restrict (mg_complex.cpp:421-467): coarse(X, c) = sum over the block of conj(P_c(f)) fine(f).
+// Threads run colour-major (consecutive threads take consecutive blocks of one null vector), so
+// a warp reads a contiguous stretch of that vector and of the fine field.
 __global__ void k_restrict(double2 *__restrict__ coarse, const double2 *__restrict__ fine, Lv v)
 {
-    const long csize = (long)v.xc * v.yc * v.nc_c;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < csize; i += (long)gridDim.x * blockDim.x) {
-        const int c = (int)(i % v.nc_c);
-        const long X = i / v.nc_c;
+    const long vc = (long)v.xc * v.yc, csize = vc * v.nc_c;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < csize; t += (long)gridDim.x * blockDim.x) {
+        const int c = (int)(t / vc);
+        const long X = t - (long)c * vc;
+        const long i = X * v.nc_c + c;
         const int yc = (int)(X / v.xc), xc = (int)(X - (long)yc * v.xc);
         const double2 *p = v.P + (long)c * v.fsize;
         double2 acc = cmk(0.0, 0.0);
