@@ -274,16 +274,22 @@ def main():
     # mgs2: coarse GCR(32) to 1e-2 (n_max 64); mgs2f / mgs3f: fixed coarse work (16 GCR
     # iterations, rel_res 1e-30), a preconditioner that does not depend on where a tolerance
     # test falls
-    for key, blocks, nvecs, nv, n_max, rr in (("mgs2", [4], [8], nv1, 64, 1e-2),
-                                              ("mgs2f", [4], [8], nv1, 16, 1e-30),
-                                              ("mgs3f", [4, 2], [8, 8], np.concatenate([nv1, nv2]), 16, 1e-30)):
+    # mgs3r: the recursive form (MLEVEL_RECURSIVE: the middle level solved by a restarted
+    # variably preconditioned GCR, 8 iterations, preconditioned by the level below); mgs3v: a V
+    # cycle with no coarse solver (smoothing on every level)
+    nv12 = np.concatenate([nv1, nv2])
+    for key, blocks, nvecs, nv, n_max, rr, inner, ml in (("mgs2", [4], [8], nv1, 64, 1e-2, 3, 0),
+                                                         ("mgs2f", [4], [8], nv1, 16, 1e-30, 3, 0),
+                                                         ("mgs3f", [4, 2], [8, 8], nv12, 16, 1e-30, 3, 0),
+                                                         ("mgs3r", [4, 2], [8, 8], nv12, 8, 1e-30, 3, 1),
+                                                         ("mgs3v", [4, 2], [8, 8], nv12, 8, 1e-30, 0, 0)):
         nr = len(blocks)
         sys.stdout.flush()
         fd, nul = os.dup(1), os.open(os.devnull, os.O_WRONLY)
         os.dup2(nul, 1)  # the reference's mg_preconditioner prints its progress with printf
         try:
-            xs, d, log = R.mg_solve("vpgcr", U, 32, 32, 0.1, b, blocks, nvecs, nv, 7, [2] * nr, [2] * nr, 3, n_max,
-                                    32, [rr] * nr, max_iter=30)
+            xs, d, log = R.mg_solve("vpgcr", U, 32, 32, 0.1, b, blocks, nvecs, nv, 7, [2] * nr, [2] * nr, inner,
+                                    n_max, 32 if ml == 0 else 8, [rr] * nr, mlevel=ml, max_iter=30)
         finally:
             import ctypes
             ctypes.CDLL(None).fflush(None)
@@ -293,8 +299,8 @@ def main():
         vec[f"{key}_solution"] = xs
         summary = [l for l in log.splitlines() if l.startswith("[MGSOLVE]")]
         info["cases"][key] = {**d, "summary": summary[-1], "blocks": blocks, "nvecs": nvecs, "max_iter": 30,
-                              "smoother": 7, "n_pre": 2, "n_post": 2, "coarse": 3, "n_max": n_max, "n_restart": 32,
-                              "rel_res": rr, "mass": 0.1}
+                              "smoother": 7, "n_pre": 2, "n_post": 2, "coarse": inner, "n_max": n_max,
+                              "n_restart": 32 if ml == 0 else 8, "rel_res": rr, "mass": 0.1, "mlevel": ml}
 
     np.savez_compressed(os.path.join(HERE, "reference_vectors.npz"), **vec)
     with open(os.path.join(HERE, "reference_info.json"), "w") as f:

@@ -158,18 +158,22 @@ def _mg_hierarchy(gl, vec, case):
     nr = len(levels)
     mgp = gl.MgPrecondStruct(ops, levels, in_smooth_type=case["smoother"], n_pre_smooth=[case["n_pre"]] * nr,
                              n_post_smooth=[case["n_post"]] * nr, in_solve_type=case["coarse"], n_max=case["n_max"],
-                             n_restart=case["n_restart"], rel_res=[case["rel_res"]] * nr)
+                             n_restart=case["n_restart"], rel_res=[case["rel_res"]] * nr,
+                             mlevel_type=case.get("mlevel", 0))
     return st, ops, mgp
 
 
-@pytest.mark.parametrize("key", ["mgs2f", "mgs3f", "mgs2"])
+@pytest.mark.parametrize("key", ["mgs2f", "mgs3f", "mgs3r", "mgs3v", "mgs2"])
 def test_mg_preconditioned_vpgcr_matches_reference(gl, gpu, golden, capfd, key):
     """The variably preconditioned GCR with the multigrid preconditioner follows the reference's
     solve: the same iteration and operator counts, the printed relative residual, and the
-    solution.  With fixed coarse work (mgs2f, mgs3f) the preconditioner is a smooth function
-    of its input and the solutions agree to 1e-9; with the coarse GCR stopped at 1e-2 (mgs2)
-    the stopping iteration of each coarse solve can move by one under rounding, and the bar is
-    the residual within 10% and the solution within 1e-2."""
+    solution.  With fixed coarse work the preconditioner is a smooth function of its input and
+    the solutions agree to 1e-9: two levels (mgs2f), three levels with the V cycle and a coarse
+    GCR (mgs3f), the recursive form whose middle level runs a restarted variably preconditioned
+    GCR preconditioned by the level below (mgs3r), and the V cycle with no coarse solver
+    (mgs3v).  With the coarse GCR stopped at 1e-2 (mgs2) the stopping iteration of each coarse
+    solve can move by one under rounding, and the bar is the residual within 10% and the
+    solution within 1e-2."""
     vec, cases = golden
     c = cases[key]
     st, ops, mgp = _mg_hierarchy(gl, vec, c)
