@@ -273,10 +273,12 @@ __device__ __forceinline__ float2 poll_slot(const unsigned long long *p, unsigne
     return make_float2(__uint_as_float((unsigned)a), __uint_as_float((unsigned)b));
 }
 
-// *p += v, performed in L2 (no value comes back).
+// *p += v, performed in L2 (no value comes back).  No memory clobber: the kernels never read
+// x_lo back (the next launch does, after the kernel boundary), so the shared-memory loads and
+// stores around the reduction may move past it.
 __device__ __forceinline__ void red_add2(float2 *p, float2 v)
 {
-    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(v.x), "f"(v.y) : "memory");
+    asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(v.x), "f"(v.y));
 }
 
 // s + c = a + b exactly (Knuth's TwoSum), for the compensated sums below.
@@ -311,39 +313,33 @@ __device__ __forceinline__ void publish(float acc, PhaseFlags *pf, unsigned e, f
     }
 }
 
-// Called by threads 0 .. nb-1: thread b waits until block b's word carries epoch e and stages
-// its partial in sm_part[b]; a wait that runs out sets *err.  One word per thread keeps the
+// Called by threads 0 .. nb-1: thread b waits until block b's word carries epoch e and returns
+// its partial (0 when the wait runs out, which sets *err).  One word per thread keeps the
 // poll's registers few (they count for every thread of the block).
-__device__ __forceinline__ void poll_partial(PhaseFlags *pf, unsigned e, int b, float *sm_part, int *err)
+__device__ __forceinline__ float poll_partial(PhaseFlags *pf, unsigned e, int b, int *err)
 {
     const unsigned long long *w = pf->w[e & 1] + b;
     const long long t0 = clock64();
     for (unsigned n = 1;; n++) {
         const unsigned long long v = ld_relaxed_u64(w);
-        if ((unsigned)(v >> 32) == e) {
-            sm_part[b] = __uint_as_float((unsigned)v);
-            return;
-        }
+        if ((unsigned)(v >> 32) == e) return __uint_as_float((unsigned)v);
         if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
             atomicExch(&pf->error, 1);
             *err = 1;
-            sm_part[b] = 0.f;
-            return;
+            return 0.f;
         }
     }
 }
 
-// Called by warp 0 after the partials are staged: their sum in block order (compensated FP32),
-// identical in every block; the total is in lane 0.
-__device__ __forceinline__ float sum_partials(const float *sm_part, unsigned nb)
+// Called by every thread right after the polls (thread b < nb holds block b's partial v, the
+// others 0): each polling warp sums its 32 partials (compensated FP32, shuffle tree) and lane 0
+// stages the pair (sum, error) in sm_hl[warp].  The reduction runs as each warp's polls end, so
+// after the barrier only total_partials' short chain remains.
+__device__ __forceinline__ void stage_partials(float v, unsigned nb, float2 *sm_hl)
 {
-    const int lane = threadIdx.x;
-    float hi = 0.f, lo = 0.f;
-    for (int b = lane; b < (int)nb; b += 32) {
-        float c;
-        two_sum(hi, sm_part[b], hi, c);
-        lo += c;
-    }
+    const int lane = threadIdx.x, warp = threadIdx.y;
+    if (warp * 32 >= (int)nb) return;
+    float hi = v, lo = 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float h2 = __shfl_down_sync(0xffffffffu, hi, o), l2 = __shfl_down_sync(0xffffffffu, lo, o);
@@ -351,7 +347,45 @@ __device__ __forceinline__ float sum_partials(const float *sm_part, unsigned nb)
         two_sum(hi, h2, hi, c);
         lo += l2 + c;
     }
+    if (lane == 0) sm_hl[warp] = make_float2(hi, lo);
+}
+
+// After the barrier that follows stage_partials: the total over the polling warps in warp order.
+// The order of every addition is fixed by the block numbers alone, so every block forms the same
+// total.
+__device__ __forceinline__ float total_partials(const float2 *sm_hl, unsigned nb)
+{
+    const int npw = ((int)nb + 31) / 32;
+    float hi = 0.f, lo = 0.f;
+    for (int w = 0; w < npw; w++) {
+        const float2 p = sm_hl[w];
+        float c;
+        two_sum(hi, p.x, hi, c);
+        lo += p.y + c;
+    }
     return hi + lo;
+}
+
+// Phase A's pointwise pass over the thread's rows: t = u + beta t_old into T and p' = r + beta p;
+// returns |t|^2 + sigma |p'|^2.  T and F are distinct buffers: restrict-qualified, the loads of
+// later rows need not wait for the stores of earlier ones.
+template <int NY>
+__device__ __forceinline__ float pass_A(float2 *__restrict__ T, const float2 *__restrict__ F, const float2 (&u)[NY],
+                                        float2 (&pv)[NY], float beta, float sigma, int c0, int nrow)
+{
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (q < nrow) {
+            const int c = c0 + q * kPW;
+            const float2 tv = fadd(u[q], fscale(beta, T[c]));
+            const float2 pn = fadd(F[c], fscale(beta, pv[q]));
+            pv[q] = pn;
+            T[c] = tv;
+            acc += fn2(tv) + sigma * fn2(pn);
+        }
+    }
+    return acc;
 }
 
 // Publishes the four partial sums of a block (FP32 within warps and across the block's warps;
@@ -498,7 +532,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     __shared__ float sm_scalar;
     __shared__ int sm_ctl, sm_err;
     __shared__ ResScalars sc;
-    __shared__ float sm_part[kMaxBlocks];
+    __shared__ float2 sm_hl[kMaxBlocks / 32];
     if (s->done || s->reliable) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
@@ -609,35 +643,33 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             else if (nrow > 0) hop_rows<NY, false>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
         if (!first) {
-            if (tid < (int)nb) poll_partial(pf, ep, tid, sm_part, &sm_err);
+            stage_partials(tid < (int)nb ? poll_partial(pf, ep, tid, &sm_err) : 0.f, nb, sm_hl);
             __syncthreads();
-            if (warp == 0) {
-                const float tot = sum_partials(sm_part, nb);
-                if (lane == 0) {
-                    int ctl = kResGo;
-                    sc.rn = tot;
-                    sc.k++;
-                    sc.iters++;
-                    if (sm_err) {
-                        sc.status = GLINALG_SOLVE_TIMEOUT;
-                        ctl = kResStop;
-                    } else if (!isfinite(tot)) {
-                        sc.status = GLINALG_SOLVE_NONFINITE;
-                        ctl = kResStop;
+            if (tid == 0) {
+                const float tot = total_partials(sm_hl, nb);
+                int ctl = kResGo;
+                sc.rn = tot;
+                sc.k++;
+                sc.iters++;
+                if (sm_err) {
+                    sc.status = GLINALG_SOLVE_TIMEOUT;
+                    ctl = kResStop;
+                } else if (!isfinite(tot)) {
+                    sc.status = GLINALG_SOLVE_NONFINITE;
+                    ctl = kResStop;
+                } else {
+                    const float rho = sqrtf(tot) * sc.scale;  // true-scale iterated residual
+                    if (rho > sc.rmax) sc.rmax = rho;
+                    if (rho < sc.delta * sc.rmax || rho < sc.stop || sc.k >= sc.max_iter) {
+                        sc.reliable = 1;
+                        ctl = kResReliable;
                     } else {
-                        const float rho = sqrtf(tot) * sc.scale;  // true-scale iterated residual
-                        if (rho > sc.rmax) sc.rmax = rho;
-                        if (rho < sc.delta * sc.rmax || rho < sc.stop || sc.k >= sc.max_iter) {
-                            sc.reliable = 1;
-                            ctl = kResReliable;
-                        } else {
-                            sc.beta = tot / sc.rsq;
-                            sc.rsq = tot;
-                            sm_scalar = sc.beta;
-                        }
+                        sc.beta = tot / sc.rsq;
+                        sc.rsq = tot;
+                        sm_scalar = sc.beta;
                     }
-                    sm_ctl = ctl;
                 }
+                sm_ctl = ctl;
             }
             __syncthreads();
             if (sm_ctl != kResGo) break;
@@ -645,18 +677,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         }
         first = false;
         const unsigned eA = ++ep;
-        float acc = 0.f;
-#pragma unroll
-        for (int q = 0; q < NY; q++) {
-            if (q < nrow) {
-                const int yl = yb + q, c = (yl + 1) * kPW + xl + 1;
-                const float2 tv = fadd(tmp[q], fscale(fb, R.T[c]));
-                const float2 pn = fadd(Rr[c], fscale(fb, pv[q]));
-                pv[q] = pn;
-                R.T[c] = tv;
-                acc += fn2(tv) + sigma * fn2(pn);
-            }
-        }
+        float acc = pass_A<NY>(R.T, Rr, tmp, pv, fb, sigma, (yb + 1) * kPW + xl + 1, nrow);
         publish<NW>(acc, pf, eA, sm_w, R.T, Mt, nborder, bpos, bslot);
         if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err);
         __syncthreads();
@@ -669,22 +690,20 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
             else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
-        if (tid < (int)nb) poll_partial(pf, eA, tid, sm_part, &sm_err);
+        stage_partials(tid < (int)nb ? poll_partial(pf, eA, tid, &sm_err) : 0.f, nb, sm_hl);
         __syncthreads();
-        if (warp == 0) {
-            const float tot = sum_partials(sm_part, nb);
-            if (lane == 0) {
-                int ctl = kResGo;
-                if (sm_err) {
-                    sc.status = GLINALG_SOLVE_TIMEOUT;
-                    ctl = kResStop;
-                } else if (!(tot > 0.f) || !isfinite(tot)) {
-                    sc.status = tot == 0.f ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
-                    ctl = kResStop;
-                }
-                sm_scalar = sc.rsq / tot;
-                sm_ctl = ctl;
+        if (tid == 0) {
+            const float tot = total_partials(sm_hl, nb);
+            int ctl = kResGo;
+            if (sm_err) {
+                sc.status = GLINALG_SOLVE_TIMEOUT;
+                ctl = kResStop;
+            } else if (!(tot > 0.f) || !isfinite(tot)) {
+                sc.status = tot == 0.f ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
+                ctl = kResStop;
             }
+            sm_scalar = sc.rsq / tot;
+            sm_ctl = ctl;
         }
         __syncthreads();
         if (sm_ctl != kResGo) break;
