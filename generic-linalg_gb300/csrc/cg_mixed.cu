@@ -411,16 +411,24 @@ struct PersistKernel {
 // 4 and 5 are the bulk-copy kernel (stag_bulk.cuh: 16 warps, tiles staged through shared
 // memory); candidates 6-8 are the rectangle-resident kernel (stag_resident.cuh, FP32 only):
 // 16 warps with x_lo in registers, 32 warps, 16 warps with x_lo in global memory; candidates
-// 9 and 10 its single-reduction form (k_resident1) with 16 and 32 warps.
-constexpr int kNumPersist = 11;
+// 9 and 10 its single-reduction form (k_resident1) with 16 and 32 warps; candidates 11 and 12
+// the two-reduction form with x_lo in tensor memory, 16 and 32 warps.
+constexpr int kNumPersist = 13;
 static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8,
-                                            res::kWX * 4, res::kWX * 4, res::kWX * 8};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0};
-constexpr int kResidentCand = 6;  // 6 .. 10
-static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 4; }
-static int resident_wy(int c) { return c == kResidentCand + 1 || c == kResidentCand + 4 ? 8 : 4; }
-static bool resident_xreg(int c) { return c == kResidentCand; }
-static bool resident_single(int c) { return c >= kResidentCand + 3; }
+                                            res::kWX * 4, res::kWX * 4, res::kWX * 8, res::kWX * 4, res::kWX * 8};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+constexpr int kResidentCand = 6;  // 6 .. 12
+static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 6; }
+static int resident_wy(int c)
+{
+    return c == kResidentCand + 1 || c == kResidentCand + 4 || c == kResidentCand + 6 ? 8 : 4;
+}
+// where x_lo lives (kXGlobal, kXReg, kXTmem)
+static int resident_xmode(int c)
+{
+    return c == kResidentCand ? kXReg : (c >= kResidentCand + 5 ? kXTmem : kXGlobal);
+}
+static bool resident_single(int c) { return c == kResidentCand + 3 || c == kResidentCand + 4; }
 
 // The rectangle grid of the resident kernel on this device (its static shared memory, the
 // reduction scratch, comes out of the same per-block budget: 512 bytes are kept for it).
@@ -457,7 +465,7 @@ static bool any_persist_applies(int lx, int ly, int variant)
 }
 
 template <class S, class R, class LK>
-static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy, bool xreg, bool single)
+static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy, int xmode, bool single)
 {
     if constexpr (std::is_same<S, float2>::value && std::is_same<R, float2>::value &&
                   std::is_same<LK, float2>::value) {
@@ -477,23 +485,35 @@ static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy,
                 default: pk.fr = k_resident1<7, 8>; break;
                 }
             }
-        } else if (wy == 4 && xreg) {
+        } else if (wy == 4 && xmode == kXReg) {
             switch (pk.plan.ny) {
-            case 4: pk.fr = k_resident<4, 4, true>; break;
-            case 8: pk.fr = k_resident<8, 4, true>; break;
-            default: pk.fr = k_resident<14, 4, true>; break;
+            case 4: pk.fr = k_resident<4, 4, kXReg>; break;
+            case 8: pk.fr = k_resident<8, 4, kXReg>; break;
+            default: pk.fr = k_resident<14, 4, kXReg>; break;
+            }
+        } else if (wy == 4 && xmode == kXTmem) {
+            switch (pk.plan.ny) {
+            case 4: pk.fr = k_resident<4, 4, kXTmem>; break;
+            case 8: pk.fr = k_resident<8, 4, kXTmem>; break;
+            default: pk.fr = k_resident<14, 4, kXTmem>; break;
             }
         } else if (wy == 4) {
             switch (pk.plan.ny) {
-            case 4: pk.fr = k_resident<4, 4, false>; break;
-            case 8: pk.fr = k_resident<8, 4, false>; break;
-            default: pk.fr = k_resident<14, 4, false>; break;
+            case 4: pk.fr = k_resident<4, 4, kXGlobal>; break;
+            case 8: pk.fr = k_resident<8, 4, kXGlobal>; break;
+            default: pk.fr = k_resident<14, 4, kXGlobal>; break;
+            }
+        } else if (xmode == kXTmem) {
+            switch (pk.plan.ny) {
+            case 2: pk.fr = k_resident<2, 8, kXTmem>; break;
+            case 4: pk.fr = k_resident<4, 8, kXTmem>; break;
+            default: pk.fr = k_resident<7, 8, kXTmem>; break;
             }
         } else {
             switch (pk.plan.ny) {
-            case 2: pk.fr = k_resident<2, 8, false>; break;
-            case 4: pk.fr = k_resident<4, 8, false>; break;
-            default: pk.fr = k_resident<7, 8, false>; break;
+            case 2: pk.fr = k_resident<2, 8, kXGlobal>; break;
+            case 4: pk.fr = k_resident<4, 8, kXGlobal>; break;
+            default: pk.fr = k_resident<7, 8, kXGlobal>; break;
             }
         }
         pk.smem = (int)pk.plan.smem;
@@ -509,7 +529,7 @@ static PersistKernel<S, R, LK> persist_cand(int c, int lx, int ly)
     pk.by = kPersistBY[c];
     pk.ny = kPersistNY[c];
     if (is_resident(c)) {
-        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xreg(c), resident_single(c));
+        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xmode(c), resident_single(c));
         if (!pk.fr) return pk;
         const void *fp = reinterpret_cast<const void *>(pk.fr);
         int per_sm = 0;

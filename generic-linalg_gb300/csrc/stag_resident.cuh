@@ -500,6 +500,53 @@ __device__ __forceinline__ float4 sum_partials4(const float4 *sm_part4, unsigned
     return make_float4(hi.x + lo.x, hi.y + lo.y, hi.z + lo.z, hi.w + lo.w);
 }
 
+// ---------------------------------------------------------------- tensor memory
+//
+// The kernel does not use the tensor cores, but their accumulator memory (TMEM, 512 columns of
+// 128 lanes x 32 bits per SM) is storage outside the register file and the shared-memory pipe.
+// A warp reaches only the 32 lanes of its sub-partition (lanes 32 (warp % 4) ..), through
+// tcgen05.ld / tcgen05.st of 32-bit columns (shape 32x32b: thread i of the warp reads or writes
+// lane 32 (warp % 4) + i).  The block allocates its columns once (one warp, tcgen05.alloc) and
+// frees them on every exit path before it returns.
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
+
+// Called by one whole warp: allocates ncols columns (a power of two >= 32) and writes their base
+// address to *dst (shared memory); gives up the right to allocate again (the block allocates once).
+__device__ __forceinline__ void tmem_alloc(unsigned *dst, unsigned ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+// Called by the warp that allocated, after every access of the block has completed.
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// Two consecutive columns of the thread's lane (issued by the whole warp; the values are valid
+// after tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld2(unsigned taddr, float2 &v)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st2(unsigned taddr, float2 v)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "f"(v.x), "f"(v.y) : "memory");
+}
+// Waits for the thread's outstanding tcgen05.ld; the values pass through the statement so that
+// no use of them is scheduled before the wait.
+template <int N>
+__device__ __forceinline__ void tmem_wait_ld(float2 (&v)[N])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < N; q++) asm volatile("" : "+f"(v[q].x), "+f"(v[q].y));
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
 // Blocks of the single-reduction kernel: a GB300 has 152 SMs (the four partials of each block
 // are staged in static shared memory, which shares the per-block budget with the rectangle).
 constexpr int kMaxBlocks1 = 160;
@@ -517,10 +564,24 @@ struct ResScalars {
     int k, max_iter, status, reliable, iters;
 };
 
-// XREG: x_lo of the thread's sites in registers for the whole launch; else every update goes to
-// global memory as a vector reduction (fire-and-forget, no register and no round trip; each site
-// has one writer, so the additions happen in program order).
-template <int NY, int WY, bool XREG>
+// Where x_lo of the thread's sites lives for the launch (XM):
+//   kXGlobal: every update goes to global memory as a vector reduction (fire-and-forget, no
+//             register and no round trip; each site has one writer, so the additions happen in
+//             program order);
+//   kXReg:    in registers;
+//   kXTmem:   in tensor memory, two columns per row of the thread (loaded, updated and stored
+//             back once per iteration), so that it takes neither registers across the stencils
+//             nor the load/store pipe.
+enum : int { kXGlobal = 0, kXReg = 1, kXTmem = 2 };
+
+// Tensor-memory columns of a block with WY warps along y and NY rows per thread (the WY warps
+// of one sub-partition take 2 NY columns each): a power of two, at least 32.
+__host__ __device__ constexpr unsigned res_tmem_cols(int NY, int WY)
+{
+    return 2 * NY * WY <= 32 ? 32u : (2 * NY * WY <= 64 ? 64u : (2 * NY * WY <= 128 ? 128u : (2 * NY * WY <= 256 ? 256u : 512u)));
+}
+
+template <int NY, int WY, int XM>
 __global__ void __launch_bounds__(32 * res::kWX * WY, 1)
 k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, float mass, float sigma, int lx, int ly,
            MxDev *s, res::PhaseFlags *pf, unsigned long long *mbox, int ty, int gx)
@@ -533,6 +594,9 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     __shared__ int sm_ctl, sm_err;
     __shared__ ResScalars sc;
     __shared__ float2 sm_hl[kMaxBlocks / 32];
+    __shared__ unsigned sm_taddr;
+    constexpr bool XREG = XM == kXReg, XTM = XM == kXTmem;
+    constexpr unsigned kTmemCols = res_tmem_cols(NY, WY);
     if (s->done || s->reliable) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
@@ -590,6 +654,14 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
 
     // ---- entry: r, links and the direction p of the rectangle on chip (p in registers and,
     // for one stencil, in T with its ring); t_old = D p into T
+    if (XTM) {
+        if (warp == 0) tmem_alloc(&sm_taddr, kTmemCols);
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+    }
+    // the thread's first x_lo column: its sub-partition's lanes, its warp's 2 NY columns
+    const unsigned xcol = XTM ? sm_taddr + ((unsigned)(32 * (warp % 4)) << 16) + (unsigned)(2 * NY * (warp / 4)) : 0u;
     float2 pv[NY], tmp[NY], xv[XREG ? NY : 1];
 #pragma unroll
     for (int q = 0; q < NY; q++) {
@@ -601,6 +673,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             Rr[(yl + 1) * kPW + xl + 1] = __ldcg(r + gi);
             pv[q] = __ldcg(p0 + gi);
             if (XREG) xv[q] = __ldcg(xlo + gi);
+            if (XTM) tmp[q] = __ldcg(xlo + gi);
             R.T[(yl + 1) * kPW + xl + 1] = pv[q];
             const float4 h = __ldg(reinterpret_cast<const float4 *>(H) + gi);
             R.HX[yl * kTX + xl] = make_float2(h.x, h.y);
@@ -615,6 +688,10 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             const int ym = y0 == 0 ? ly - 1 : y0 - 1;
             R.HyB[k - tyb] = __ldg(H + 2 * (ym * lx + x0 + (k - tyb)) + 1);
         }
+    }
+    if (XTM) {
+#pragma unroll
+        for (int q = 0; q < NY; q++) tmem_st2(xcol + 2 * q, q < nrow ? tmp[q] : make_float2(0.f, 0.f));
     }
     if (has_ring) {
         Rr[rslot] = __ldcg(r + rgi);
@@ -710,12 +787,21 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         const float alpha = sm_scalar;
         const unsigned eB = ++ep;
         acc = 0.f;
+        if (XTM) {
+            float2 xt[NY];
+            tmem_wait_st();
+#pragma unroll
+            for (int q = 0; q < NY; q++) tmem_ld2(xcol + 2 * q, xt[q]);
+            tmem_wait_ld(xt);
+#pragma unroll
+            for (int q = 0; q < NY; q++) tmem_st2(xcol + 2 * q, fadd(xt[q], fscale(alpha, pv[q])));
+        }
 #pragma unroll
         for (int q = 0; q < NY; q++) {
             if (q < nrow) {
                 const int yl = yb + q, c = (yl + 1) * kPW + xl + 1;
                 if (XREG) xv[q] = fadd(xv[q], fscale(alpha, pv[q]));
-                else red_add2(xlo + grow + q * lx, fscale(alpha, pv[q]));
+                else if (!XTM) red_add2(xlo + grow + q * lx, fscale(alpha, pv[q]));
                 const float2 rnv = fsub(Rr[c], fscale(alpha, tmp[q]));
                 Rr[c] = rnv;
                 acc += fn2(rnv);
@@ -726,6 +812,12 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         __syncthreads();
     }
     // ---- exit: the rectangle's r, x_lo and direction back to global memory (direction in p0)
+    if (XTM) {  // x_lo out of tensor memory (into tmp), then the columns are freed
+        tmem_wait_st();
+#pragma unroll
+        for (int q = 0; q < NY; q++) tmem_ld2(xcol + 2 * q, tmp[q]);
+        tmem_wait_ld(tmp);
+    }
 #pragma unroll
     for (int q = 0; q < NY; q++) {
         if (q < nrow) {
@@ -733,7 +825,14 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             r[gi] = Rr[(yb + q + 1) * kPW + xl + 1];
             p0[gi] = pv[q];
             if (XREG) xlo[gi] = xv[q];
+            if (XTM) xlo[gi] = tmp[q];
         }
+    }
+    if (XTM) {
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+        if (warp == 0) tmem_dealloc(sm_taddr, kTmemCols);
     }
     if (blockIdx.x == 0 && tid == 0) {
         pf->epoch = ep;  // every block ran the same phases
