@@ -412,21 +412,25 @@ struct PersistKernel {
 // memory); candidates 6-8 are the rectangle-resident kernel (stag_resident.cuh, FP32 only):
 // 16 warps with x_lo in registers, 32 warps, 16 warps with x_lo in global memory; candidates
 // 9 and 10 its single-reduction form (k_resident1) with 16 and 32 warps; candidates 11 and 12
-// the two-reduction form with x_lo in tensor memory, 16 and 32 warps.
-constexpr int kNumPersist = 13;
+// the two-reduction form with x_lo in tensor memory, 16 and 32 warps; candidates 13 and 14 the
+// same with the links in tensor memory too.
+constexpr int kNumPersist = 15;
 static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8,
-                                            res::kWX * 4, res::kWX * 4, res::kWX * 8, res::kWX * 4, res::kWX * 8};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-constexpr int kResidentCand = 6;  // 6 .. 12
-static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 6; }
+                                            res::kWX * 4, res::kWX * 4, res::kWX * 8, res::kWX * 4, res::kWX * 8,
+                                            res::kWX * 4, res::kWX * 8};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+constexpr int kResidentCand = 6;  // 6 .. 14
+static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 8; }
 static int resident_wy(int c)
 {
-    return c == kResidentCand + 1 || c == kResidentCand + 4 || c == kResidentCand + 6 ? 8 : 4;
+    return c == kResidentCand + 1 || c == kResidentCand + 4 || c == kResidentCand + 6 || c == kResidentCand + 8 ? 8 : 4;
 }
-// where x_lo lives (kXGlobal, kXReg, kXTmem)
+// where x_lo (and the links) live (kXGlobal, kXReg, kXTmem, kXTmemL)
 static int resident_xmode(int c)
 {
-    return c == kResidentCand ? kXReg : (c >= kResidentCand + 5 ? kXTmem : kXGlobal);
+    if (c == kResidentCand) return kXReg;
+    if (c >= kResidentCand + 7) return kXTmemL;
+    return c >= kResidentCand + 5 ? kXTmem : kXGlobal;
 }
 static bool resident_single(int c) { return c == kResidentCand + 3 || c == kResidentCand + 4; }
 
@@ -496,6 +500,18 @@ static void resident_kernel(PersistKernel<S, R, LK> &pk, int lx, int ly, int wy,
             case 4: pk.fr = k_resident<4, 4, kXTmem>; break;
             case 8: pk.fr = k_resident<8, 4, kXTmem>; break;
             default: pk.fr = k_resident<14, 4, kXTmem>; break;
+            }
+        } else if (wy == 4 && xmode == kXTmemL) {
+            switch (pk.plan.ny) {
+            case 4: pk.fr = k_resident<4, 4, kXTmemL>; break;
+            case 8: pk.fr = k_resident<8, 4, kXTmemL>; break;
+            default: pk.fr = k_resident<14, 4, kXTmemL>; break;
+            }
+        } else if (xmode == kXTmemL) {
+            switch (pk.plan.ny) {
+            case 2: pk.fr = k_resident<2, 8, kXTmemL>; break;
+            case 4: pk.fr = k_resident<4, 8, kXTmemL>; break;
+            default: pk.fr = k_resident<7, 8, kXTmemL>; break;
             }
         } else if (wy == 4) {
             switch (pk.plan.ny) {

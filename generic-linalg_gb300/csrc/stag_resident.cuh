@@ -142,6 +142,115 @@ __device__ __forceinline__ void hop_rows(const float2 *__restrict__ F, const flo
     }
 }
 
+// ---------------------------------------------------------------- tensor memory
+//
+// The kernel does not use the tensor cores, but their accumulator memory (TMEM, 512 columns of
+// 128 lanes x 32 bits per SM) is storage outside the register file and the shared-memory pipe.
+// A warp reaches only the 32 lanes of its sub-partition (lanes 32 (warp % 4) ..), through
+// tcgen05.ld / tcgen05.st of 32-bit columns (shape 32x32b: thread i of the warp reads or writes
+// lane 32 (warp % 4) + i).  The block allocates its columns once (one warp, tcgen05.alloc) and
+// frees them on every exit path before it returns.
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
+
+// Called by one whole warp: allocates ncols columns (a power of two >= 32) and writes their base
+// address to *dst (shared memory); gives up the right to allocate again (the block allocates once).
+__device__ __forceinline__ void tmem_alloc(unsigned *dst, unsigned ncols)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+// Called by the warp that allocated, after every access of the block has completed.
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tmem_fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// Two consecutive columns of the thread's lane (issued by the whole warp; the values are valid
+// after tmem_wait_ld).
+__device__ __forceinline__ void tmem_ld2(unsigned taddr, float2 &v)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st2(unsigned taddr, float2 v)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "f"(v.x), "f"(v.y) : "memory");
+}
+// Waits for the thread's outstanding tcgen05.ld; the values pass through the statement so that
+// no use of them is scheduled before the wait.
+template <int N>
+__device__ __forceinline__ void tmem_wait_ld(float2 (&v)[N])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int q = 0; q < N; q++) asm volatile("" : "+f"(v[q].x), "+f"(v[q].y));
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld4(unsigned taddr, float4 &v)
+{
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_st4(unsigned taddr, float4 v)
+{
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr), "f"(v.x), "f"(v.y),
+                 "f"(v.z), "f"(v.w)
+                 : "memory");
+}
+// tmem_wait_ld for one row of links (h_x, h_y in a, h_x of the left neighbour in b).
+__device__ __forceinline__ void tmem_wait_ld_row(float4 &a, float2 &b)
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    asm volatile("" : "+f"(a.x), "+f"(a.y), "+f"(a.z), "+f"(a.w), "+f"(b.x), "+f"(b.y));
+}
+
+// hop_rows with the links of the thread's sites in tensor memory instead of shared memory: tA
+// addresses its rows' (h_x, h_y) (4 columns a row), tB its rows' h_x of the left neighbour (2
+// columns a row); hyp0 is h_y of the row below the first.  Each row's links are loaded while
+// the row before is computed.  Shared memory serves only the field: 3 loads per site, not 6.
+template <int NY, bool FULL, class Body>
+__device__ __forceinline__ void hop_rows_tm(const float2 *__restrict__ F, unsigned tA, unsigned tB, float2 hyp0,
+                                            int xl, int yb, int nrow, Body body)
+{
+    float2 prev = F[yb * kPW + xl + 1], cur = F[(yb + 1) * kPW + xl + 1];
+    float2 hyp = hyp0;
+    float4 L;
+    float2 Lm;
+    tmem_ld4(tA, L);
+    tmem_ld2(tB, Lm);
+    tmem_wait_ld_row(L, Lm);
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (!FULL && q >= nrow) break;
+        float4 Ln;
+        float2 Lmn;
+        if (q + 1 < NY) {
+            tmem_ld4(tA + 4 * (q + 1), Ln);
+            tmem_ld2(tB + 2 * (q + 1), Lmn);
+        }
+        const int yl = yb + q;
+        const float2 next = F[(yl + 2) * kPW + xl + 1];
+        const float2 xm = F[(yl + 1) * kPW + xl], xp = F[(yl + 1) * kPW + xl + 2];
+        const float2 hx = make_float2(L.x, L.y), hy = make_float2(L.z, L.w);
+        float2 s = fmul(hx, xp);
+        s = fsub(s, fmulc(Lm, xm));
+        s = fadd(s, fmul(hy, next));
+        s = fsub(s, fmulc(hyp, prev));
+        body(q, yl, cur, s);
+        prev = cur;
+        cur = next;
+        hyp = hy;
+        if (q + 1 < NY) {
+            tmem_wait_ld_row(Ln, Lmn);
+            L = Ln;
+            Lm = Lmn;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- exchange between blocks
 //
 // Nothing in the inner loop waits for a memory fence.  Every value one block hands to another
@@ -500,53 +609,6 @@ __device__ __forceinline__ float4 sum_partials4(const float4 *sm_part4, unsigned
     return make_float4(hi.x + lo.x, hi.y + lo.y, hi.z + lo.z, hi.w + lo.w);
 }
 
-// ---------------------------------------------------------------- tensor memory
-//
-// The kernel does not use the tensor cores, but their accumulator memory (TMEM, 512 columns of
-// 128 lanes x 32 bits per SM) is storage outside the register file and the shared-memory pipe.
-// A warp reaches only the 32 lanes of its sub-partition (lanes 32 (warp % 4) ..), through
-// tcgen05.ld / tcgen05.st of 32-bit columns (shape 32x32b: thread i of the warp reads or writes
-// lane 32 (warp % 4) + i).  The block allocates its columns once (one warp, tcgen05.alloc) and
-// frees them on every exit path before it returns.
-
-__device__ __forceinline__ unsigned smem_addr(const void *p) { return static_cast<unsigned>(__cvta_generic_to_shared(p)); }
-
-// Called by one whole warp: allocates ncols columns (a power of two >= 32) and writes their base
-// address to *dst (shared memory); gives up the right to allocate again (the block allocates once).
-__device__ __forceinline__ void tmem_alloc(unsigned *dst, unsigned ncols)
-{
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-// Called by the warp that allocated, after every access of the block has completed.
-__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols)
-{
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tmem_fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tmem_fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-// Two consecutive columns of the thread's lane (issued by the whole warp; the values are valid
-// after tmem_wait_ld).
-__device__ __forceinline__ void tmem_ld2(unsigned taddr, float2 &v)
-{
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x2.b32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(taddr));
-}
-__device__ __forceinline__ void tmem_st2(unsigned taddr, float2 v)
-{
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x2.b32 [%0], {%1, %2};" ::"r"(taddr), "f"(v.x), "f"(v.y) : "memory");
-}
-// Waits for the thread's outstanding tcgen05.ld; the values pass through the statement so that
-// no use of them is scheduled before the wait.
-template <int N>
-__device__ __forceinline__ void tmem_wait_ld(float2 (&v)[N])
-{
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int q = 0; q < N; q++) asm volatile("" : "+f"(v[q].x), "+f"(v[q].y));
-}
-__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
 // Blocks of the single-reduction kernel: a GB300 has 152 SMs (the four partials of each block
 // are staged in static shared memory, which shares the per-block budget with the rectangle).
 constexpr int kMaxBlocks1 = 160;
@@ -571,8 +633,13 @@ struct ResScalars {
 //   kXReg:    in registers;
 //   kXTmem:   in tensor memory, two columns per row of the thread (loaded, updated and stored
 //             back once per iteration), so that it takes neither registers across the stencils
-//             nor the load/store pipe.
-enum : int { kXGlobal = 0, kXReg = 1, kXTmem = 2 };
+//             nor the load/store pipe;
+//   kXTmemL:  as kXTmem, and the links of the thread's sites are in tensor memory as well
+//             (hop_rows_tm), so that the stencils read only the field from shared memory.
+//             Columns (per sub-partition lane): (h_x, h_y) of the rows at 0 .. 255 (4 NY per
+//             warp), h_x of the left neighbours at 256 .. 383 (2 NY per warp), x_lo at 384 ..
+//             511 (2 NY per warp); 512 in all.
+enum : int { kXGlobal = 0, kXReg = 1, kXTmem = 2, kXTmemL = 3 };
 
 // Tensor-memory columns of a block with WY warps along y and NY rows per thread (the WY warps
 // of one sub-partition take 2 NY columns each): a power of two, at least 32.
@@ -595,8 +662,9 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     __shared__ ResScalars sc;
     __shared__ float2 sm_hl[kMaxBlocks / 32];
     __shared__ unsigned sm_taddr;
-    constexpr bool XREG = XM == kXReg, XTM = XM == kXTmem;
-    constexpr unsigned kTmemCols = res_tmem_cols(NY, WY);
+    constexpr bool XREG = XM == kXReg, XTM = XM == kXTmem || XM == kXTmemL, LTM = XM == kXTmemL;
+    constexpr unsigned kTmemCols = LTM ? 512u : res_tmem_cols(NY, WY);
+    static_assert(!LTM || (4 * NY * WY <= 256 && 2 * NY * WY <= 128), "tensor-memory layout");
     if (s->done || s->reliable) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
@@ -661,7 +729,11 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         tmem_fence_after_sync();
     }
     // the thread's first x_lo column: its sub-partition's lanes, its warp's 2 NY columns
-    const unsigned xcol = XTM ? sm_taddr + ((unsigned)(32 * (warp % 4)) << 16) + (unsigned)(2 * NY * (warp / 4)) : 0u;
+    const unsigned tlane = XTM ? sm_taddr + ((unsigned)(32 * (warp % 4)) << 16) : 0u;
+    const unsigned xcol = tlane + (LTM ? 384u : 0u) + (unsigned)(2 * NY * (warp / 4));
+    // the links of the thread's rows: (h_x, h_y), and h_x of the left neighbour
+    const unsigned tA = tlane + (unsigned)(4 * NY * (warp / 4));
+    const unsigned tB = tlane + 256u + (unsigned)(2 * NY * (warp / 4));
     float2 pv[NY], tmp[NY], xv[XREG ? NY : 1];
 #pragma unroll
     for (int q = 0; q < NY; q++) {
@@ -698,6 +770,19 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         R.T[rslot] = __ldcg(p0 + rgi);
     }
     __syncthreads();
+    if (LTM) {  // the links of the thread's rows into tensor memory (zeros past the rectangle)
+#pragma unroll
+        for (int q = 0; q < NY; q++) {
+            const int yl = yb + q;
+            const bool in = q < nrow;
+            const float2 hx = in ? R.HX[yl * kTX + xl] : make_float2(0.f, 0.f);
+            const float2 hy = in ? R.HY[yl * kTX + xl] : make_float2(0.f, 0.f);
+            const float2 hxm = in ? (xl ? R.HX[yl * kTX + xl - 1] : R.HxL[yl]) : make_float2(0.f, 0.f);
+            tmem_st4(tA + 4 * q, make_float4(hx.x, hx.y, hy.x, hy.y));
+            tmem_st2(tB + 2 * q, hxm);
+        }
+        tmem_wait_st();
+    }
     {
         auto body = [&](int q, int, float2 cur, float2 hs) { tmp[q] = fadd(fscale(mass, cur), hs); };
         if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
@@ -716,8 +801,16 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         // t = u + beta t_old (= D p'), p' = r + beta p
         {
             auto body = [&](int q, int, float2 cur, float2 hs) { tmp[q] = fadd(fscale(mass, cur), hs); };
-            if (nrow == NY) hop_rows<NY, true>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
-            else if (nrow > 0) hop_rows<NY, false>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            if (LTM) {
+                if (nrow > 0) {  // (yb < tyb: the row below the first is in range)
+                    const float2 hyp0 = yb == 0 ? R.HyB[xl] : R.HY[(yb - 1) * kTX + xl];
+                    if (nrow == NY) hop_rows_tm<NY, true>(Rr, tA, tB, hyp0, xl, yb, nrow, body);
+                    else hop_rows_tm<NY, false>(Rr, tA, tB, hyp0, xl, yb, nrow, body);
+                }
+            } else {
+                if (nrow == NY) hop_rows<NY, true>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+                else if (nrow > 0) hop_rows<NY, false>(Rr, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            }
         }
         if (!first) {
             stage_partials(tid < (int)nb ? poll_partial(pf, ep, tid, &sm_err) : 0.f, nb, sm_hl);
@@ -764,8 +857,16 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             auto body = [&](int q, int, float2 cur, float2 hs) {
                 tmp[q] = fadd(fsub(fscale(mass, cur), hs), fscale(sigma, pv[q]));
             };
-            if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
-            else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            if (LTM) {
+                if (nrow > 0) {  // (yb < tyb: the row below the first is in range)
+                    const float2 hyp0 = yb == 0 ? R.HyB[xl] : R.HY[(yb - 1) * kTX + xl];
+                    if (nrow == NY) hop_rows_tm<NY, true>(R.T, tA, tB, hyp0, xl, yb, nrow, body);
+                    else hop_rows_tm<NY, false>(R.T, tA, tB, hyp0, xl, yb, nrow, body);
+                }
+            } else {
+                if (nrow == NY) hop_rows<NY, true>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+                else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
+            }
         }
         stage_partials(tid < (int)nb ? poll_partial(pf, eA, tid, &sm_err) : 0.f, nb, sm_hl);
         __syncthreads();

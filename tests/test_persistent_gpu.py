@@ -2,7 +2,7 @@
 reliable-update cycle): the register-tiled kernels, the bulk-copy kernels and the
 rectangle-resident kernel (shared-memory / register state per SM, borders exchanged through
 L2) in its two-reduction and single-reduction forms, with x_lo in registers, global memory or
-tensor memory.  Each candidate is forced with GLINALG_PERSIST_SHAPE in a process of its own (the
+tensor memory, and with x_lo and the links in tensor memory.  Each candidate is forced with GLINALG_PERSIST_SHAPE in a process of its own (the
 autotuner's pick is cached per process).
 
 Bar: the FP64-true relative residual below 1e-10 (re-checked with the FP64 GPU operator), the
@@ -78,7 +78,7 @@ def check(res, kappa):
     assert nbytes > 0, res
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14])
 def test_persistent_candidate_1024(gl, gpu, tmp_path, shape):
     """The 1024x1024, m = 0.01 system (kappa ~ 2e4) with each persistent kernel forced."""
     res = run_case(tmp_path, 1024, 1024, 0.01, 1337, shape)
@@ -90,7 +90,7 @@ def test_persistent_candidate_1024(gl, gpu, tmp_path, shape):
 def test_resident_kernel_small_lattices(gl, gpu, tmp_path, lx, ly):
     """Lattices that only the rectangle-resident kernel serves: one or several 128-column
     rectangles across, full and short last rectangles, one-row rectangles (128 x 90)."""
-    for shape in (6, 7, 8, 9, 10, 11, 12):
+    for shape in (6, 7, 8, 9, 10, 11, 12, 13, 14):
         res = run_case(tmp_path, lx, ly, 0.05, 99, shape)
         assert res["tuned"] == shape
         check(res, 1e3)
