@@ -303,6 +303,13 @@ __device__ __forceinline__ void st_relaxed_2u64(unsigned long long *p, unsigned 
 {
     asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
 }
+// st_relaxed_2u64 without the memory clobber: for words posted from registers, whose order
+// against the thread's plain loads and stores does not matter (volatile statements keep their
+// order among themselves, so a post still precedes the thread's later polls).
+__device__ __forceinline__ void st_relaxed_2u64_nc(unsigned long long *p, unsigned long long a, unsigned long long b)
+{
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b));
+}
 __device__ __forceinline__ int ld_relaxed_s32(const int *p)
 {
     int v;
@@ -338,6 +345,34 @@ __device__ __forceinline__ void border_slot(int k, int ty, int tyb, int &pos, in
         slot = 2 * kTX + ty + yl;
     }
     pos = (yl + 1) * kPW + xl + 1;
+}
+
+// Posts site (xl, yl) of a rectangle of tyb rows, value v of epoch e, to the bottom-row and
+// top-row border slots that carry it (mb: this block's mailbox within the field), straight from
+// the register of the thread that computed it.  yl is the same in the whole warp, so the
+// branches do not split it.
+__device__ __forceinline__ void post_rows(unsigned long long *mb, unsigned e, int xl, int yl, int tyb, float2 v)
+{
+    const unsigned long long a = tag(e, v.x), b = tag(e, v.y);
+    if (yl == 0) st_relaxed_2u64_nc(mb + 2 * xl, a, b);
+    if (yl == tyb - 1) st_relaxed_2u64_nc(mb + 2 * (kTX + xl), a, b);
+}
+
+// Posts the left (wx == 0) or right (wx == kWX - 1) column of the warp's rows (yb .. yb+nrow-1)
+// of F, epoch e, after the warp has written them to shared memory: lane q posts row yb + q, one
+// store instruction for the warp.  Other warps return at once.
+__device__ __forceinline__ void post_columns(unsigned long long *mb, unsigned e, const float2 *F, int wx, int yb,
+                                             int nrow, int ty)
+{
+    if (wx != 0 && wx != kWX - 1) return;
+    __syncwarp();
+    const int lane = threadIdx.x;
+    if (lane < nrow) {
+        const int yl = yb + lane;
+        const int xl = wx == 0 ? 0 : kTX - 1;
+        const float2 v = F[(yl + 1) * kPW + xl + 1];
+        st_relaxed_2u64(mb + 2 * (2 * kTX + (wx == 0 ? 0 : ty) + yl), tag(e, v.x), tag(e, v.y));
+    }
 }
 
 // The mailbox word (within a field) that feeds ring site k: the row below comes from the top
@@ -398,30 +433,6 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &c)
     c = (a - (s - bb)) + (b - bb);
 }
 
-// Publishes phase e (every thread passes its `acc`): the block's partial sum (FP32 within warps
-// and across the block's warps, one tagged word written by thread 0) and the border of the field
-// F just written to shared memory (thread k < nborder posts border slot k to the mailbox M).
-template <int NW>
-__device__ __forceinline__ void publish(float acc, PhaseFlags *pf, unsigned e, float *sm_w, const float2 *F,
-                                        unsigned long long *M, int nborder, int bpos, int bslot)
-{
-    const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if (lane == 0) sm_w[warp] = acc;
-    __syncthreads();
-    if (warp == 0) {
-        float v = lane < NW ? sm_w[lane] : 0.f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) st_relaxed_u64(pf->w[e & 1] + blockIdx.x, tag(e, v));
-    }
-    if (tid < nborder) {
-        const float2 v = F[bpos];
-        st_relaxed_2u64(M + 2 * bslot, tag(e, v.x), tag(e, v.y));
-    }
-}
-
 // Called by threads 0 .. nb-1: thread b waits until block b's word carries epoch e and returns
 // its partial (0 when the wait runs out, which sets *err).  One word per thread keeps the
 // poll's registers few (they count for every thread of the block).
@@ -465,22 +476,27 @@ __device__ __forceinline__ void stage_partials(float v, unsigned nb, float2 *sm_
 __device__ __forceinline__ float total_partials(const float2 *sm_hl, unsigned nb)
 {
     const int npw = ((int)nb + 31) / 32;
+    float2 p[kMaxBlocks / 32];
+#pragma unroll
+    for (int w = 0; w < kMaxBlocks / 32; w++) p[w] = w < npw ? sm_hl[w] : make_float2(0.f, 0.f);
     float hi = 0.f, lo = 0.f;
-    for (int w = 0; w < npw; w++) {
-        const float2 p = sm_hl[w];
+#pragma unroll
+    for (int w = 0; w < kMaxBlocks / 32; w++) {
         float c;
-        two_sum(hi, p.x, hi, c);
-        lo += p.y + c;
+        two_sum(hi, p[w].x, hi, c);
+        lo += p[w].y + c;
     }
     return hi + lo;
 }
 
 // Phase A's pointwise pass over the thread's rows: t = u + beta t_old into T and p' = r + beta p;
-// returns |t|^2 + sigma |p'|^2.  T and F are distinct buffers: restrict-qualified, the loads of
-// later rows need not wait for the stores of earlier ones.
+// returns |t|^2 + sigma |p'|^2.  Sites of the bottom and top row of the rectangle go to the
+// mailbox mbT (epoch e) as they are computed.  T and F are distinct buffers: restrict-qualified, the loads of later rows need not
+// wait for the stores of earlier ones.
 template <int NY>
 __device__ __forceinline__ float pass_A(float2 *__restrict__ T, const float2 *__restrict__ F, const float2 (&u)[NY],
-                                        float2 (&pv)[NY], float beta, float sigma, int c0, int nrow)
+                                        float2 (&pv)[NY], float beta, float sigma, int c0, int nrow,
+                                        unsigned long long *mbT, unsigned e, int xl, int yb, int tyb)
 {
     float acc = 0.f;
 #pragma unroll
@@ -491,14 +507,34 @@ __device__ __forceinline__ float pass_A(float2 *__restrict__ T, const float2 *__
             const float2 pn = fadd(F[c], fscale(beta, pv[q]));
             pv[q] = pn;
             T[c] = tv;
+            post_rows(mbT, e, xl, yb + q, tyb, tv);
             acc += fn2(tv) + sigma * fn2(pn);
         }
     }
     return acc;
 }
 
+// Publishes the block's partial sum of phase e (every thread passes its `acc`): FP32 sums within warps and across the block's warps, one
+// tagged word written by thread 0.
+template <int NW>
+__device__ __forceinline__ void publish_sum(float acc, PhaseFlags *pf, unsigned e, float *sm_w)
+{
+    const int lane = threadIdx.x, warp = threadIdx.y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) sm_w[warp] = acc;
+    __syncthreads();
+    if (warp == 0) {
+        float v = lane < NW ? sm_w[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) st_relaxed_u64(pf->w[e & 1] + blockIdx.x, tag(e, v));
+    }
+}
+
 // Publishes the four partial sums of a block (FP32 within warps and across the block's warps;
-// thread 0 writes two tagged 128-bit words), then the border of F as publish() does.
+// thread 0 writes two tagged 128-bit words), then the border of F (thread k < nborder posts
+// border slot k from shared memory).
 template <int NW>
 __device__ __forceinline__ void publish4(float4 acc, PhaseFlags *pf, unsigned e, float4 *sm_w4, const float2 *F,
                                          unsigned long long *M, int nborder, int bpos, int bslot)
@@ -695,14 +731,9 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         ring_site(tid, tyb, x0, y0, lx, ly, rslot, rgi);
         rsrc = ring_source(tid, ty, tyb, nslot, nb_l, nb_r, nb_d, nb_u);
     }
-    // border slot tid (posted from shared memory after each pointwise pass); the slot index
-    // includes this block's mailbox offset
-    const int nborder = nring;
-    int bpos = 0, bslot = 0;
-    if (tid < nborder) {
-        border_slot(tid, ty, tyb, bpos, bslot);
-        bslot += (int)blockIdx.x * nslot;
-    }
+    // this block's mailboxes (border sites are posted by the threads that compute them)
+    unsigned long long *const mbR = Mr + 2 * (size_t)blockIdx.x * nslot;
+    unsigned long long *const mbT = Mt + 2 * (size_t)blockIdx.x * nslot;
     const int grow = (y0 + yb) * lx + x0 + xl;      // lattice index of the thread's first row
     if (tid == 0) {
         sm_err = 0;
@@ -847,8 +878,9 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         }
         first = false;
         const unsigned eA = ++ep;
-        float acc = pass_A<NY>(R.T, Rr, tmp, pv, fb, sigma, (yb + 1) * kPW + xl + 1, nrow);
-        publish<NW>(acc, pf, eA, sm_w, R.T, Mt, nborder, bpos, bslot);
+        float acc = pass_A<NY>(R.T, Rr, tmp, pv, fb, sigma, (yb + 1) * kPW + xl + 1, nrow, mbT, eA, xl, yb, tyb);
+        post_columns(mbT, eA, R.T, warp % kWX, yb, nrow, ty);
+        publish_sum<NW>(acc, pf, eA, sm_w);
         if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err);
         __syncthreads();
         // ---- B: Ap = D^dagger t + sigma p' (needs only the ring of t), then alpha from the
@@ -905,10 +937,12 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
                 else if (!XTM) red_add2(xlo + grow + q * lx, fscale(alpha, pv[q]));
                 const float2 rnv = fsub(Rr[c], fscale(alpha, tmp[q]));
                 Rr[c] = rnv;
+                post_rows(mbR, eB, xl, yl, tyb, rnv);
                 acc += fn2(rnv);
             }
         }
-        publish<NW>(acc, pf, eB, sm_w, Rr, Mr, nborder, bpos, bslot);
+        post_columns(mbR, eB, Rr, warp % kWX, yb, nrow, ty);
+        publish_sum<NW>(acc, pf, eB, sm_w);
         if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err);
         __syncthreads();
     }
