@@ -60,7 +60,9 @@ PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 r
                    9: "k_resident1<16 warps> (single-reduction form)",
                    10: "k_resident1<32 warps> (single-reduction form)",
                    11: "k_resident<16 warps, x_lo in tensor memory> (rectangle state on chip)",
-                   12: "k_resident<32 warps, x_lo in tensor memory> (rectangle state on chip)"}
+                   12: "k_resident<32 warps, x_lo in tensor memory> (rectangle state on chip)",
+                   13: "k_resident<16 warps, x_lo and links in tensor memory> (rectangle state on chip)",
+                   14: "k_resident<32 warps, x_lo and links in tensor memory> (rectangle state on chip)"}
 
 
 def peaks():
@@ -702,7 +704,7 @@ def main():
     k_launch = max(1, hi_.kernel_launches)
     persist_cand = L.glinalg_tuned_persist(op.handle, head_prec)
     persist_kernel = PERSIST_KERNELS.get(persist_cand, "none")
-    resident = persist_cand in (6, 7, 8, 11, 12)
+    resident = persist_cand in (6, 7, 8, 11, 12, 13, 14)
     # algorithmic bytes: the canonical CG iteration on D^dagger D, 17 complex words per site
     # (D p -> t: p, 2 links, t; D^dagger t -> Ap: t, 2 links, Ap; x, p, r, Ap in, x, r out;
     # p = r + beta p: 3), 136 B per site in FP32

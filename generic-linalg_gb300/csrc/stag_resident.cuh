@@ -12,9 +12,13 @@
 //   B: Ap = D^dagger t + sigma p'; then alpha = |r|^2 / <p', A p'> (the total of A);
 //      x_lo += alpha p', r -= alpha Ap, |r|^2; export the border of r.
 // Shared memory holds r and t, each with a one-site ring, and the hopping coefficients; the
-// direction p' and (16-warp blocks) x_lo stay in registers.  Border sites travel through
-// epoch-tagged mailboxes in global memory (L2), with no memory fence in the loop (see the
-// exchange section below).
+// direction p' stays in registers.  x_lo stays in registers, in global memory (updated by
+// vector reductions in L2) or in tensor memory; in the fastest form the links of each
+// thread's sites are in tensor memory too, so that the stencils read only the field from
+// shared memory (see the tensor-memory section and k_resident's XM).  Border sites travel
+// through epoch-tagged mailboxes in global memory (L2), with no memory fence in the loop (see
+// the exchange section below); each border site is posted by the warp that computes it, as
+// soon as it is computed.
 //
 // On entry the kernel loads r and the direction (p0) of its rectangle and computes t_old = D p;
 // on exit it writes r, x_lo and the direction (to p0, parity 0) back for the FP64 reliable
