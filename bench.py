@@ -40,15 +40,15 @@ METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB3
 HEADLINE = ("fp32", 1)
 # DRAM bytes (read + write) of one launch of the persistent inner-loop kernels on this workload,
 # from ncu --set full captures: k_persist (fields in L2; the first launch of a solve, 254 inner
-# iterations) and k_resident (rectangle state on chip, x_lo in tensor memory; a 20-iteration
-# launch).  In both the traffic is the compulsory load of the launch's state and does not grow
-# with its iterations.
+# iterations) and k_resident (rectangle state on chip, x_lo and links in tensor memory; a
+# 20-iteration launch).  In both the traffic is the compulsory load of the launch's state and
+# does not grow with its iterations.
 K_PERSIST_DRAM_BYTES = 41.987328e6 + 3.212544e6
-K_RESIDENT_DRAM_BYTES = 42.761728e6 + 0.044544e6
+K_RESIDENT_DRAM_BYTES = 42.13248e6 + 0.00896e6
 # Shared-memory wavefronts (128 B) per SM and inner iteration of k_resident at 1024^2, from the
-# same capture (26.61 M over 152 SMs and 20 iterations, entry included); GB300 serves one per
+# same capture (19.95 M over 152 SMs and 20 iterations, entry included); GB300 serves one per
 # clock per SM.
-K_RESIDENT_SMEM_WAVEFRONTS = 8.75e3
+K_RESIDENT_SMEM_WAVEFRONTS = 6.56e3
 VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 # persistent inner-loop kernels by the library's candidate index (glinalg_tuned_persist)
 PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 rows>",
@@ -771,7 +771,7 @@ def main():
         smem_ach = smem_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else 0.0
         onchip = {"resource": "shared memory", "achieved": round(smem_ach, 1), "peak": round(smem_peak, 1),
                   "unit": "GB/s", "frac": round(smem_ach / smem_peak, 3),
-                  "note": "128 B x 8.75k wavefronts per SM and iteration (ncu) over the kernel's device time; peak "
+                  "note": "128 B x 6.56k wavefronts per SM and iteration (ncu) over the kernel's device time; peak "
                           "128 B per clock per SM at the sampled SM clock"}
     line = {
         "metric": METRIC, "value": round(ms_max, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
