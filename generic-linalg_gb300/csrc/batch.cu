@@ -82,7 +82,7 @@ extern "C" glinalg_status glinalg_cg_batch(const glinalg_operator *ops, int n_sy
     GL_TRY(ensure_device());
     const bool dev = params && (params->flags & GLINALG_PTR_DEVICE);
     const int prec = params ? params->precision : GLINALG_PREC_DOUBLE;
-    const double delta = params && params->delta > 0 ? params->delta : 0.1;
+    const double delta = params && params->delta > 0 ? params->delta : 0.0;  // 0: the per-precision default
     cudaStream_t st = lib_stream();
     Scratch sc(st);
     std::vector<double2 *> xs(n_sys);

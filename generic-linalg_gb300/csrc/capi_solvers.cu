@@ -40,7 +40,9 @@ glinalg_status prologue(glinalg_operator op, double *phi, const double *phi0, in
 }
 
 int precision_of(const glinalg_solver_params *p) { return p ? p->precision : GLINALG_PREC_DOUBLE; }
-double delta_of(const glinalg_solver_params *p) { return p && p->delta > 0 ? p->delta : 0.1; }
+// The caller's reliable-update trigger, or 0: the mixed solvers then pick their per-precision
+// default (0.01 for FP32 iterates, 0.1 for 16-bit ones).
+double delta_of(const glinalg_solver_params *p) { return p && p->delta > 0 ? p->delta : 0.0; }
 
 }  // namespace
 

@@ -100,7 +100,7 @@ extern "C" glinalg_status glinalg_staggered_action_grad(glinalg_operator op, con
     const long n = op->vol;
     const bool dev = params && (params->flags & GLINALG_PTR_DEVICE);
     const int prec = params ? params->precision : GLINALG_PREC_DOUBLE;
-    const double delta = params && params->delta > 0 ? params->delta : 0.1;
+    const double delta = params && params->delta > 0 ? params->delta : 0.0;  // 0: the per-precision default
     const double2 *dphi = (const double2 *)phi;
     double2 *X, *Y;
     double *dg = grad;
