@@ -127,3 +127,19 @@ np.savez(sys.argv[1], **out)
         res[mode] = np.load(tmp_path / f"out{mode}.npz")
     for k in res["1"].files:
         assert np.array_equal(res["1"][k], res["0"][k]), k
+
+
+def test_mixed_cg_default_delta(gl, gpu, golden):
+    """An unset reliable-update trigger is the documented 0.01 for FP32 iterates: the same
+    iterations and reliable updates as delta = 0.01, and fewer updates than delta = 0.1."""
+    vec, _ = golden
+    U, b = vec["l32_links"], vec["l32_src"]
+    got = {}
+    for d in (0.0, 0.01, 0.1):
+        x = np.zeros_like(b)
+        info = gl.minv_vector_cg(x, b, b.size, 20000, 1e-10, gl.square_staggered_normal_u1,
+                                 gl.StaggeredU1Op(U, 0.1, 32, 32), precision=PRECS["single"], delta=d)
+        assert info.success
+        got[d] = (info.iter, info.reliable_updates)
+    assert got[0.0] == got[0.01], got
+    assert got[0.1][1] > got[0.01][1], got
