@@ -267,7 +267,8 @@ __device__ __forceinline__ void hop_rows_tm(const float2 *__restrict__ F, unsign
 // Epochs grow by one per phase (two per iteration) across the launches of a solve.  A mailbox
 // slot is rewritten two phases later (the same field, the next iteration), and a block reaches
 // that write only after the grid-wide sum in between, which every block contributes to only
-// after it has read the slot's previous contents; partial-sum words alternate between two
+// after it has read the slot's previous contents (k_resident posts border words from its
+// update passes, which come after the wait for that sum); partial-sum words alternate between two
 // arrays by phase parity for the same reason.  Every wait is bounded (kSpinCycles); a wait
 // that runs out raises the error word, which ends the waits of every other block too.
 
