@@ -204,6 +204,29 @@ def main():
         vec["g16_links_read"] = R.read_gauge(pth, 16, 16)
     info["cases"]["g16_gauge"]["text"] = text
 
+    # ---- the reference's own heat-bath gauge fields (multigrid/aa_mg/cfg/*.dat, read with
+    # read_gauge_u1): beta = 30, and two beta = 60 fields whose file names give their
+    # topological charge (q1: +1, qm3: -3).  Smooth fields, unlike rand_gauge_u1's.  Stored: the
+    # links as read, the gauge utilities as above, and the reference's CG on the staggered
+    # normal equations with the l32 source at m = 0.1 and m = 0.01
+    refdir = os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
+    heatbath = {"hb30": "l32t32b30_heatbath.dat", "hb60q1": "l32t32b60_heatbath_q1.dat",
+                "hb60qm3": "l32t32b60_heatbath_qm3.dat"}
+    for key, fn in heatbath.items():
+        U = R.read_gauge(os.path.join(refdir, "multigrid", "aa_mg", "cfg", fn), 32, 32)
+        vec[f"{key}_links"] = U
+        pl = R.plaquette(U, 32, 32)
+        info["cases"][f"{key}_gauge"] = {"plaquette": [pl.real, pl.imag], "topo": R.topo(U, 32, 32),
+                                         "file": fn}
+        Ut, g = R.gauge_trans(99, U, 32, 32)
+        vec[f"{key}_trans"], vec[f"{key}_links_trans"] = g, Ut
+        vec[f"{key}_ape"] = R.ape_smear(U, 32, 32, 0.5, 3)
+        for tag, m in (("m0.1", 0.1), ("m0.01", 0.01)):
+            x, d, _ = R.solve("cg", Op("staggered_normal", 32, 32, m, U), vec["l32_src"], max_iter=10000,
+                              eps=1e-10)
+            vec[f"{key}_cg_{tag}"] = x
+            info["cases"][f"{key}_cg_{tag}"] = {**d, "mass": m, "max_iter": 10000, "eps": 1e-10}
+
     # ---- multigrid transfer and coarse operators (multigrid/aa_mg/mg_complex.cpp): a 16x16
     # staggered stencil (m = 0.1, plus eo_shift and dof_shift so that the shift projection is
     # exercised) blocked 4x4 with 4 null vectors (Gaussian, numpy seed 5) into a 4x4 lattice

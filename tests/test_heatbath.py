@@ -1,0 +1,126 @@
+"""The reference's own heat-bath gauge fields as parity inputs: multigrid/aa_mg/cfg/
+l32t32b30_heatbath.dat, l32t32b60_heatbath_q1.dat and l32t32b60_heatbath_qm3.dat, read with
+the reference's read_gauge_u1 (u1_utils.cpp:17-38) when the golden fixtures were written.
+They are smooth fields, where rand_gauge_u1's are as rough as a U(1) field can be, and the two
+beta = 60 fields carry the topological charge their file names state (+1 and -3).
+
+CPU: the oracle bit for bit against the reference's plaquette, topological charge, gauge
+transform and APE smearing (u1_utils.cpp) and its CG on the staggered normal equations
+(generic_cg.cpp:278-382) on these fields, and the known charges.
+GPU: the device kernels and solvers against the same reference outputs.
+
+Bars on the GPU.  Gauge utilities as for the random fields: plaquette and charge within 1e-13
+absolute, gauge transform within 1e-15 and APE smearing within 1e-13 per link.  FP64 CG: the
+FP64-true relative residual below 1e-10, the iteration count within one of the reference's,
+and the solution within 1e-11 relative when the count is the reference's.  The count is not
+held exact because the stopping test can be marginal on these fields: on the beta = 30 field at
+m = 0.1 the reference's own recurrence with its dot products summed in another order (numpy's
+pairwise sum) stops at 153 iterations instead of 154.  A solve one iteration apart is held to
+the bound that any two solutions with relative residual below 1e-10 satisfy,
+2 kappa 1e-10 with kappa(M^dagger M) <= (m^2 + 4) / m^2.  Mixed FP32 CG at m = 0.1: the FP64-true
+relative residual below 1e-10 and the solution within that same bound (8.0e-8) of the
+reference's."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import rel
+from pyoracle import Operator
+
+HB = {"hb30": 0, "hb60q1": 1, "hb60qm3": -3}   # field -> topological charge from its file name
+MASSES = {"m0.1": 0.1, "m0.01": 0.01}
+L = 32
+
+
+def kappa_bound(m):
+    """Upper bound of the condition number of M^dagger M = m^2 + D_hop^dagger D_hop on a U(1)
+    field: the hopping part's eigenvalues are i lambda with |lambda| <= 2."""
+    return (m * m + 4.0) / (m * m)
+
+
+def true_relres(oracle, m, U, x, b):
+    Ax = oracle.apply(Operator("staggered_normal", L, L, m, U), x)
+    return np.linalg.norm(b - Ax) / np.linalg.norm(b)
+
+
+# ---- CPU: the oracle against the reference on the heat-bath fields
+
+@pytest.mark.parametrize("key", list(HB))
+def test_oracle_gauge_utilities_bit_exact(oracle, golden, key):
+    vec, cases = golden
+    U, c = vec[f"{key}_links"], cases[f"{key}_gauge"]
+    assert oracle.plaquette(U, L, L) == complex(*c["plaquette"])
+    assert oracle.topo(U, L, L) == c["topo"]
+    assert np.array_equal(oracle.gauge_trans(U, vec[f"{key}_trans"], L, L), vec[f"{key}_links_trans"])
+    assert np.array_equal(oracle.ape_smear(U, L, L, 0.5, 3), vec[f"{key}_ape"])
+
+
+@pytest.mark.parametrize("key", list(HB))
+def test_known_topological_charge(oracle, golden, key):
+    """The charge the reference computes is the integer the fixture's file name gives, and it
+    is gauge invariant."""
+    vec, cases = golden
+    q = cases[f"{key}_gauge"]["topo"]
+    assert round(q) == HB[key] and abs(q - HB[key]) < 1e-12
+    assert abs(oracle.topo(vec[f"{key}_links_trans"], L, L) - HB[key]) < 1e-12
+
+
+@pytest.mark.parametrize("key", list(HB))
+@pytest.mark.parametrize("tag", list(MASSES))
+def test_oracle_cg_bit_exact(oracle, golden, key, tag):
+    vec, cases = golden
+    c = cases[f"{key}_cg_{tag}"]
+    op = Operator("staggered_normal", L, L, c["mass"], vec[f"{key}_links"])
+    x, info, _ = oracle.solve("cg", op, vec["l32_src"], max_iter=c["max_iter"], eps=c["eps"])
+    for f in ("iter", "ops_count", "success", "name", "resSq"):
+        assert info[f] == c[f], f
+    assert np.array_equal(x, vec[f"{key}_cg_{tag}"])
+
+
+# ---- GPU: the device kernels and solvers against the reference on the heat-bath fields
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", list(HB))
+def test_device_gauge_utilities_match_reference(gl, gpu, golden, key):
+    vec, cases = golden
+    U, c = vec[f"{key}_links"], cases[f"{key}_gauge"]
+    assert abs(gl.get_plaquette_u1(U, L, L) - complex(*c["plaquette"])) < 1e-13
+    assert abs(gl.get_topo_u1(U, L, L) - c["topo"]) < 1e-13
+    Ut = U.copy()
+    gl.apply_gauge_trans_u1(Ut, vec[f"{key}_trans"], L, L)
+    assert np.max(np.abs(Ut - vec[f"{key}_links_trans"])) < 1e-15
+    S = np.zeros_like(U)
+    gl.apply_ape_smear_u1(S, U, L, L, 0.5, 3)
+    assert np.max(np.abs(S - vec[f"{key}_ape"])) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", list(HB))
+@pytest.mark.parametrize("tag", list(MASSES))
+def test_device_cg_matches_reference(gl, gpu, oracle, golden, key, tag):
+    vec, cases = golden
+    c = cases[f"{key}_cg_{tag}"]
+    m, U, b = c["mass"], vec[f"{key}_links"], vec["l32_src"]
+    x = np.zeros_like(b)
+    info = gl.minv_vector_cg(x, b, b.size, c["max_iter"], c["eps"], gl.square_staggered_normal_u1,
+                             gl.StaggeredU1Op(U, m, L, L))
+    assert info.success and info.name == "CG"
+    assert true_relres(oracle, m, U, x, b) < 1e-10
+    assert abs(info.iter - c["iter"]) <= 1 and info.ops_count - info.iter == c["ops_count"] - c["iter"]
+    bound = 1e-11 if info.iter == c["iter"] else 2.0 * kappa_bound(m) * 1e-10
+    assert rel(x, vec[f"{key}_cg_{tag}"]) < bound
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", list(HB))
+def test_device_mixed_cg_matches_reference(gl, gpu, oracle, golden, key):
+    vec, cases = golden
+    c = cases[f"{key}_cg_m0.1"]
+    U, b = vec[f"{key}_links"], vec["l32_src"]
+    x = np.zeros_like(b)
+    info = gl.minv_vector_cg(x, b, b.size, 20000, 1e-10, gl.square_staggered_normal_u1,
+                             gl.StaggeredU1Op(U, 0.1, L, L), precision=gl.PREC_SINGLE)
+    assert info.success and info.status == 0
+    assert true_relres(oracle, 0.1, U, x, b) < 1e-10
+    assert rel(x, vec[f"{key}_cg_m0.1"]) < 2.0 * kappa_bound(0.1) * 1e-10
