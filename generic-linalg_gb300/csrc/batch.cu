@@ -24,7 +24,8 @@ extern "C" glinalg_status glinalg_cg_m_multi(glinalg_operator op, double *phi, c
 {
     if (!op || !phi || !phi0 || !shifts || !infos || n_rhs <= 0 || n_shift <= 0)
         return GLINALG_ERROR_INVALID_VALUE;
-    if ((long)size != op->size || resid_freq_check <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if ((long)size != op->size || resid_freq_check <= 0)
+        return invalid_arg("(long)size != op->size || resid_freq_check <= 0");
     GL_TRY(ensure_device());
     const bool dev = params && (params->flags & GLINALG_PTR_DEVICE);
     cudaStream_t st = lib_stream();
@@ -74,7 +75,8 @@ extern "C" glinalg_status glinalg_cg_batch(const glinalg_operator *ops, int n_sy
                                            const double *const *phi0, int max_iter, double eps,
                                            const glinalg_solver_params *params, glinalg_info *infos)
 {
-    if (!ops || !phi || !phi0 || !infos || n_sys <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!ops || !phi || !phi0 || !infos || n_sys <= 0)
+        return invalid_arg("!ops || !phi || !phi0 || !infos || n_sys <= 0");
     for (int q = 0; q < n_sys; q++)
         if (!ops[q] || !phi[q] || !phi0[q] ||
             !(ops[q]->kind == GLINALG_OP_STAGGERED_NORMAL || ops[q]->kind == GLINALG_OP_LAPLACE))

@@ -28,7 +28,10 @@ glinalg_status finish_call(SolveCall &c, double *phi, long n)
 glinalg_status prologue(glinalg_operator op, double *phi, const double *phi0, int size,
                         const glinalg_solver_params *params, glinalg_info *info, SolveCall &c)
 {
-    if (!info) return GLINALG_ERROR_INVALID_VALUE;
+    if (!info) {
+        set_last_error("null info");
+        return GLINALG_ERROR_INVALID_VALUE;
+    }
     GL_TRY(check_solver_args(op, phi, phi0, size, &c.dev, params));
     GL_TRY(c.sg.stage(c.sc, phi, phi0, op->size, c.dev, c.st));
     double *keep = info->resSqmrhs;
@@ -145,7 +148,8 @@ extern "C" glinalg_status glinalg_cg_m(glinalg_operator op, double *const *phi, 
                                        const glinalg_solver_params *params, glinalg_info *info)
 {
     GL_TRY(ensure_device());
-    if (!op || !phi || !phi0 || !shifts || !info || n_shift <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !phi || !phi0 || !shifts || !info || n_shift <= 0)
+        return invalid_arg("!op || !phi || !phi0 || !shifts || !info || n_shift <= 0");
     if (resid_freq_check <= 0) {
         set_last_error("resid_freq_check must be positive");
         return GLINALG_ERROR_INVALID_VALUE;
@@ -155,7 +159,7 @@ extern "C" glinalg_status glinalg_cg_m(glinalg_operator op, double *const *phi, 
         return GLINALG_ERROR_INVALID_VALUE;
     }
     for (int j = 0; j < n_shift; j++)
-        if (!phi[j]) return GLINALG_ERROR_INVALID_VALUE;
+        if (!phi[j]) return invalid_arg("!phi[j]");
     if (precision_of(params) != GLINALG_PREC_DOUBLE) {
         set_last_error("CG-M runs its vectors in FP64 (the shift recurrences need it)");
         return GLINALG_ERROR_INVALID_VALUE;
@@ -263,14 +267,15 @@ glinalg_status multishift_entry(glinalg_operator op, double *const *phi, const d
                                 F solve)
 {
     GL_TRY(ensure_device());
-    if (!op || !phi || !phi0 || !shifts || !info || n_shift <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !phi || !phi0 || !shifts || !info || n_shift <= 0)
+        return invalid_arg("!op || !phi || !phi0 || !shifts || !info || n_shift <= 0");
     GL_TRY(positive(resid_freq_check, "resid_freq_check"));
     if ((long)size != op->size) {
         set_last_error("size does not match the operator's field size");
         return GLINALG_ERROR_INVALID_VALUE;
     }
     for (int j = 0; j < n_shift; j++)
-        if (!phi[j]) return GLINALG_ERROR_INVALID_VALUE;
+        if (!phi[j]) return invalid_arg("!phi[j]");
     GL_TRY(fp64_only(params, what));
     const bool dev = params && (params->flags & GLINALG_PTR_DEVICE);
     cudaStream_t st = lib_stream();
@@ -389,7 +394,7 @@ static glinalg_status flex_entry(int mode, int restart_freq, glinalg_operator op
                                  const glinalg_verbosity *verb, const glinalg_solver_params *params,
                                  glinalg_info *info)
 {
-    if (!op) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op) return invalid_arg("!op");
     Precond pc;
     GL_TRY(make_precond(precond, op, &pc));
     return single_solve(op, phi, phi0, size, params, info, mode == 0 ? "FPCG" : "VPGCR", [&](SolveCall &c) {

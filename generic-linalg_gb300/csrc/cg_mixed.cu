@@ -1331,7 +1331,8 @@ extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int
                                                         double ms[2], double bytes[2])
 {
     using namespace glinalg;
-    if (!op || !ms || !bytes || n_launch <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !ms || !bytes || n_launch <= 0)
+        return invalid_arg("!op || !ms || !bytes || n_launch <= 0");
     if (op->kind != GLINALG_OP_STAGGERED_NORMAL) return GLINALG_ERROR_UNSUPPORTED_OP;
     GL_TRY(ensure_device());
     switch (precision) {
@@ -1346,7 +1347,8 @@ extern "C" glinalg_status glinalg_profile_persist_kernel(glinalg_operator op, in
                                                          int n_iter, double *ms, double *bytes, int *cand)
 {
     using namespace glinalg;
-    if (!op || !ms || !bytes || !cand || n_launch <= 0 || n_iter <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !ms || !bytes || !cand || n_launch <= 0 || n_iter <= 0)
+        return invalid_arg("!op || !ms || !bytes || !cand || n_launch <= 0 || n_iter <= 0");
     if (op->kind != GLINALG_OP_STAGGERED_NORMAL) return GLINALG_ERROR_UNSUPPORTED_OP;
     GL_TRY(ensure_device());
     switch (precision) {

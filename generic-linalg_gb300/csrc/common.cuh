@@ -28,6 +28,14 @@ void set_last_error(const std::string &msg);
         }                                                                                 \
     } while (0)
 
+// Rejects an argument: records the message for glinalg_last_error() and returns
+// GLINALG_ERROR_INVALID_VALUE.
+inline glinalg_status invalid_arg(const char *msg)
+{
+    set_last_error(std::string("invalid argument: ") + msg);
+    return GLINALG_ERROR_INVALID_VALUE;
+}
+
 #define GL_TRY(expr)                              \
     do {                                          \
         glinalg_status _s = (expr);               \

@@ -201,7 +201,8 @@ using namespace glinalg;
 static glinalg_status eo_step(glinalg_operator op, double *out, const double *a, const double *b, int flags,
                               bool reconstruct)
 {
-    if (!op || !out || !a || (reconstruct && !b)) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !out || !a || (reconstruct && !b))
+        return invalid_arg("!op || !out || !a || (reconstruct && !b)");
     const bool tb = op->kind == GLINALG_OP_STENCIL_M2MDTBDBT;
     if (op->kind != GLINALG_OP_STAGGERED_M2MDEODOE && op->kind != GLINALG_OP_STENCIL_M2MDEODOE && !tb) {
         set_last_error("even/odd preconditioning needs an m^2 - D_eo D_oe operator");

@@ -55,7 +55,7 @@ using namespace glinalg;
 extern "C" glinalg_status glinalg_staggered_force(glinalg_operator op, const double *X,
                                                   const double *Y, double *grad, int flags)
 {
-    if (!op || !X || !Y || !grad) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !X || !Y || !grad) return invalid_arg("!op || !X || !Y || !grad");
     if (!is_staggered(op->kind)) {
         set_last_error("the force needs a staggered operator");
         return GLINALG_ERROR_UNSUPPORTED_OP;
@@ -89,7 +89,7 @@ extern "C" glinalg_status glinalg_staggered_action_grad(glinalg_operator op, con
                                                         const glinalg_solver_params *params,
                                                         glinalg_info *info)
 {
-    if (!op || !phi || !grad || !info) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !phi || !grad || !info) return invalid_arg("!op || !phi || !grad || !info");
     if (op->kind != GLINALG_OP_STAGGERED_NORMAL) {
         set_last_error("action_grad needs the staggered normal operator (D^dagger D)");
         return GLINALG_ERROR_UNSUPPORTED_OP;

@@ -151,7 +151,7 @@ using namespace glinalg;
 extern "C" glinalg_status glinalg_read_gauge_u1(double *links, int lx, int ly, const char *path)
 {
     GL_TRY(check_lattice(links, lx, ly));
-    if (!path) return GLINALG_ERROR_INVALID_VALUE;
+    if (!path) return invalid_arg("!path");
     std::ifstream in(path);
     if (!in) {
         set_last_error(std::string("cannot open ") + path);
@@ -174,7 +174,7 @@ extern "C" glinalg_status glinalg_read_gauge_u1(double *links, int lx, int ly, c
 extern "C" glinalg_status glinalg_write_gauge_u1(const double *links, int lx, int ly, const char *path)
 {
     GL_TRY(check_lattice(links, lx, ly));
-    if (!path) return GLINALG_ERROR_INVALID_VALUE;
+    if (!path) return invalid_arg("!path");
     FILE *f = std::fopen(path, "w");
     if (!f) {
         set_last_error(std::string("cannot write ") + path);
@@ -212,7 +212,7 @@ extern "C" glinalg_status glinalg_unit_gauge_u1(double *links, int lx, int ly, i
 
 extern "C" glinalg_status glinalg_plaquette_u1(const double *links, int lx, int ly, double out[2], int flags)
 {
-    if (!out) return GLINALG_ERROR_INVALID_VALUE;
+    if (!out) return invalid_arg("!out");
     double s[3];
     GL_TRY(plaq_sums(links, lx, ly, flags, s));
     const double v = (double)((long)lx * ly);
@@ -223,7 +223,7 @@ extern "C" glinalg_status glinalg_plaquette_u1(const double *links, int lx, int 
 
 extern "C" glinalg_status glinalg_topo_u1(const double *links, int lx, int ly, double *out, int flags)
 {
-    if (!out) return GLINALG_ERROR_INVALID_VALUE;
+    if (!out) return invalid_arg("!out");
     double s[3];
     GL_TRY(plaq_sums(links, lx, ly, flags, s));
     *out = 0.5 * s[2] / kPi;
@@ -233,7 +233,7 @@ extern "C" glinalg_status glinalg_topo_u1(const double *links, int lx, int ly, d
 extern "C" glinalg_status glinalg_apply_gauge_trans_u1(double *links, const double *trans, int lx, int ly, int flags)
 {
     GL_TRY(check_lattice(links, lx, ly));
-    if (!trans) return GLINALG_ERROR_INVALID_VALUE;
+    if (!trans) return invalid_arg("!trans");
     GL_TRY(ensure_device());
     cudaStream_t st = lib_stream();
     Scratch sc(st);
@@ -253,7 +253,7 @@ extern "C" glinalg_status glinalg_apply_ape_smear_u1(double *smeared, const doub
                                                      double alpha, int n_iter, int flags)
 {
     GL_TRY(check_lattice(links, lx, ly));
-    if (!smeared || n_iter < 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!smeared || n_iter < 0) return invalid_arg("!smeared || n_iter < 0");
     GL_TRY(ensure_device());
     cudaStream_t st = lib_stream();
     Scratch sc(st);

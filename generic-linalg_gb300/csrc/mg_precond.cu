@@ -155,16 +155,17 @@ using namespace glinalg;
 extern "C" glinalg_status glinalg_mg_create(int n_refine, const glinalg_operator *ops, const glinalg_mg_level *levels,
                                             const glinalg_mg_params *params, glinalg_mg *out)
 {
-    if (!out || !ops || !levels || !params) return GLINALG_ERROR_INVALID_VALUE;
+    if (!out || !ops || !levels || !params)
+        return invalid_arg("!out || !ops || !levels || !params");
     *out = nullptr;
     if (n_refine < 1 || n_refine > GLINALG_MG_MAX_LEVELS) {
         set_last_error("n_refine must be between 1 and GLINALG_MG_MAX_LEVELS");
         return GLINALG_ERROR_INVALID_VALUE;
     }
     for (int l = 0; l <= n_refine; l++)
-        if (!ops[l]) return GLINALG_ERROR_INVALID_VALUE;
+        if (!ops[l]) return invalid_arg("!ops[l]");
     for (int l = 0; l < n_refine; l++) {
-        if (!levels[l]) return GLINALG_ERROR_INVALID_VALUE;
+        if (!levels[l]) return invalid_arg("!levels[l]");
         if (mg_level_fine_size(levels[l]) != ops[l]->size || mg_level_coarse_size(levels[l]) != ops[l + 1]->size) {
             set_last_error("the transfer levels do not match the operators' field sizes");
             return GLINALG_ERROR_INVALID_VALUE;
@@ -211,7 +212,7 @@ extern "C" glinalg_status glinalg_mg_destroy(glinalg_mg mg)
 
 extern "C" glinalg_status glinalg_mg_apply(glinalg_mg mg, double *lhs, const double *rhs, int flags)
 {
-    if (!mg || !lhs || !rhs) return GLINALG_ERROR_INVALID_VALUE;
+    if (!mg || !lhs || !rhs) return invalid_arg("!mg || !lhs || !rhs");
     GL_TRY(ensure_device());
     cudaStream_t st = lib_stream();
     Scratch sc(st);

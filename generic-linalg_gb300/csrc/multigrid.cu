@@ -233,7 +233,7 @@ using namespace glinalg;
 extern "C" glinalg_status glinalg_mg_level_create(int lx, int ly, int nc_fine, int bx, int by, int nc_coarse,
                                                   const double *null_vectors, int flags, glinalg_mg_level *out)
 {
-    if (!out || !null_vectors) return GLINALG_ERROR_INVALID_VALUE;
+    if (!out || !null_vectors) return invalid_arg("!out || !null_vectors");
     *out = nullptr;
     if (lx <= 0 || ly <= 0 || nc_fine <= 0 || bx <= 0 || by <= 0 || nc_coarse <= 0 || lx % bx || ly % by) {
         set_last_error("the block sizes must divide the lattice extents");
@@ -274,7 +274,7 @@ extern "C" glinalg_status glinalg_mg_level_destroy(glinalg_mg_level l)
 extern "C" glinalg_status glinalg_mg_get_null_vectors(glinalg_mg_level l, double *out, int flags)
 {
     GL_TRY(check_level(l));
-    if (!out) return GLINALG_ERROR_INVALID_VALUE;
+    if (!out) return invalid_arg("!out");
     cudaStream_t st = lib_stream();
     GL_CUDA(cudaMemcpyAsync(out, l->P, sizeof(double2) * (size_t)l->nc_c * l->fsize,
                             (flags & GLINALG_PTR_DEVICE) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
@@ -327,7 +327,7 @@ glinalg_status mg_restrict(const glinalg_mg_level_s *l, double2 *coarse, const d
 static glinalg_status mg_transfer(glinalg_mg_level l, double *out, const double *in, int flags, bool up)
 {
     GL_TRY(check_level(l));
-    if (!out || !in) return GLINALG_ERROR_INVALID_VALUE;
+    if (!out || !in) return invalid_arg("!out || !in");
     cudaStream_t st = lib_stream();
     Scratch sc(st);
     const long n_in = up ? l->csize : l->fsize, n_out = up ? l->fsize : l->csize;
@@ -359,7 +359,7 @@ extern "C" glinalg_status glinalg_mg_coarse_stencil(glinalg_mg_level l, glinalg_
                                                     glinalg_operator *coarse_out)
 {
     GL_TRY(check_level(l));
-    if (!fine || !coarse_out) return GLINALG_ERROR_INVALID_VALUE;
+    if (!fine || !coarse_out) return invalid_arg("!fine || !coarse_out");
     *coarse_out = nullptr;
     if (fine->kind != GLINALG_OP_STENCIL || fine->nc != l->nc_f || fine->lx != l->lx || fine->ly != l->ly) {
         set_last_error("the fine operator must be a stencil (GLINALG_OP_STENCIL) on the level's fine lattice");

@@ -381,18 +381,19 @@ static glinalg_status upload(double2 **dst, const double *src, long n_complex, i
 
 extern "C" glinalg_status glinalg_operator_create(const glinalg_op_desc *d, glinalg_operator *out)
 {
-    if (!d || !out) return GLINALG_ERROR_INVALID_VALUE;
+    if (!d || !out) return invalid_arg("!d || !out");
     *out = nullptr;
-    if (d->lx <= 0 || d->ly <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (d->lx <= 0 || d->ly <= 0) return invalid_arg("d->lx <= 0 || d->ly <= 0");
     if (d->kind < GLINALG_OP_STAGGERED || d->kind > GLINALG_OP_STENCIL_DAGGER_TB)
         return GLINALG_ERROR_UNSUPPORTED_OP;
     const bool sten = is_stencil(d->kind);
-    if (sten && (d->nc <= 0 || !d->clover || !d->hopping)) return GLINALG_ERROR_INVALID_VALUE;
+    if (sten && (d->nc <= 0 || !d->clover || !d->hopping))
+        return invalid_arg("sten && (d->nc <= 0 || !d->clover || !d->hopping)");
     if (d->kind == GLINALG_OP_STENCIL_M2MDEODOE && d->nc != 1) {
         set_last_error("the stencil form of m^2 - D_eo D_oe needs nc = 1 (a staggered stencil)");
         return GLINALG_ERROR_INVALID_VALUE;
     }
-    if (!sten && !d->links) return GLINALG_ERROR_INVALID_VALUE;
+    if (!sten && !d->links) return invalid_arg("!sten && !d->links");
     GL_TRY(ensure_device());
     auto *op = new glinalg_operator_s();
     op->kind = d->kind;
@@ -447,7 +448,7 @@ extern "C" glinalg_status glinalg_operator_destroy(glinalg_operator op)
 
 extern "C" glinalg_status glinalg_operator_set_mass(glinalg_operator op, double mass)
 {
-    if (!op) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op) return invalid_arg("!op");
     op->mass = mass;
     return GLINALG_SUCCESS;
 }
@@ -457,7 +458,7 @@ extern "C" long glinalg_operator_size(glinalg_operator op) { return op ? op->siz
 extern "C" glinalg_status glinalg_operator_apply(glinalg_operator op, double *lhs,
                                                  const double *rhs, int flags)
 {
-    if (!op || !lhs || !rhs) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op || !lhs || !rhs) return invalid_arg("!op || !lhs || !rhs");
     cudaStream_t st = lib_stream();
     const size_t bytes = sizeof(double2) * (size_t)op->size;
     const bool dev = flags & GLINALG_PTR_DEVICE;
@@ -498,7 +499,8 @@ extern "C" glinalg_status glinalg_staggered_stencil(const double *links, int lx,
                                                     double mass, int dagger, double *hopping_out,
                                                     double *shift_out, int flags)
 {
-    if (!links || !hopping_out || lx <= 0 || ly <= 0) return GLINALG_ERROR_INVALID_VALUE;
+    if (!links || !hopping_out || lx <= 0 || ly <= 0)
+        return invalid_arg("!links || !hopping_out || lx <= 0 || ly <= 0");
     GL_TRY(ensure_device());
     cudaStream_t st = lib_stream();
     const long vol = (long)lx * ly;
@@ -527,7 +529,7 @@ extern "C" glinalg_status glinalg_staggered_stencil(const double *links, int lx,
 extern "C" glinalg_status glinalg_operator_stencil_get(glinalg_operator op, double *clover, double *hopping,
                                                        int flags)
 {
-    if (!op) return GLINALG_ERROR_INVALID_VALUE;
+    if (!op) return invalid_arg("!op");
     if (!is_stencil(op->kind) || !op->clover || !op->hopping) {
         set_last_error("not a stencil operator");
         return GLINALG_ERROR_UNSUPPORTED_OP;

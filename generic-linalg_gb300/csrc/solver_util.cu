@@ -265,7 +265,8 @@ extern "C" int glinalg_device_count(void)
 static glinalg_status reduce_entry(int which, const double *a, const double *b, long n,
                                    double *out, int flags)
 {
-    if (!a || !out || n < 0 || (which == 1 && !b)) return GLINALG_ERROR_INVALID_VALUE;
+    if (!a || !out || n < 0 || (which == 1 && !b))
+        return invalid_arg("!a || !out || n < 0 || (which == 1 && !b)");
     GL_TRY(ensure_device());
     cudaStream_t st = lib_stream();
     Scratch sc(st);

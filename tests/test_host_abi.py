@@ -98,3 +98,17 @@ def test_product_never_touches_the_oracle():
                 if re.search(r"pyoracle|liboracle|oracle/|import\s+oracle|orc_", txt):
                     offenders.append(fn)
     assert not offenders, offenders
+
+
+def test_rejected_arguments_name_the_check(gl):
+    """A rejected argument sets the message glinalg_last_error() returns, so a caller never
+    reads an empty or stale message after GLINALG_ERROR_INVALID_VALUE."""
+    L = gl.lib()
+    U = np.ones(2 * 16, np.complex128)
+    ptr = U.ctypes.data_as(C.POINTER(C.c_double))
+    assert L.glinalg_read_gauge_u1(ptr, 4, 4, b"/nonexistent/dir/f.dat") == 1
+    assert b"cannot open" in L.glinalg_last_error()
+    assert L.glinalg_read_gauge_u1(ptr, 4, 4, None) == 1
+    assert L.glinalg_last_error() == b"invalid argument: !path"
+    assert L.glinalg_write_gauge_u1(ptr, 4, 4, None) == 1
+    assert L.glinalg_last_error() == b"invalid argument: !path"
