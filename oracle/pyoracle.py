@@ -70,11 +70,17 @@ class OrcInfo(C.Structure):
                 "ops_count": self.ops_count, "name": self.name.decode()}
 
 
+def reference_dir():
+    """The reference checkout the reference-compiled builds read (GLINALG_REFERENCE_DIR
+    overrides the default location)."""
+    return os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
+
+
 def build(quiet=True):
     """Compile liboracle.so (and libref_oracle.so when the reference checkout exists)."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE], stdout=out)
-    ref = os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
+    ref = reference_dir()
     if os.path.isdir(ref):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], stdout=out)
 

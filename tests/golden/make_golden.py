@@ -209,7 +209,7 @@ def main():
     # topological charge (q1: +1, qm3: -3).  Smooth fields, unlike rand_gauge_u1's.  Stored: the
     # links as read, the gauge utilities as above, and the reference's CG on the staggered
     # normal equations with the l32 source at m = 0.1 and m = 0.01
-    refdir = os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
+    refdir = pyoracle.reference_dir()
     heatbath = {"hb30": "l32t32b30_heatbath.dat", "hb60q1": "l32t32b60_heatbath_q1.dat",
                 "hb60qm3": "l32t32b60_heatbath_qm3.dat"}
     for key, fn in heatbath.items():
