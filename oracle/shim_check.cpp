@@ -2,14 +2,15 @@
 // infrastructure, built by `make -C oracle shim` from the reference's unmodified sources).
 //
 // Links the reference's operators, stencils and solvers with the shim in place of the
-// complex minv_vector_* overloads (generic_cg.cpp, generic_cg_m.cpp, generic_bicgstab.cpp,
-// generic_gcr.cpp compiled under ref_* names), and calls through the reference's own
-// interface.  One line per case on stdout, "case <name> <key>=<value> ...":
+// complex minv_vector_* overloads (the solver files that define them compiled under ref_*
+// names), and calls through the reference's own interface.  One line per case on stdout, "case <name> <key>=<value> ...":
 //   - every reference callback the library drives, through minv_vector_cg (complex);
 //   - a callback the library does not drive, and a single-direction stencil apply;
 //   - minv_vector_cg_m (complex), whose result must carry n_shift per-shift residuals;
-//   - the other complex entry points (restarted CG, BiCGstab, GCR);
-//   - the real-valued minv_vector_cg, which must run the reference's code.
+//   - the other complex entry points (restarted CG, BiCGstab, GCR) and the sibling solvers
+//     (CR, MinRes, BiCGstab-l, CR-M, BiCGstab-M, flexible CG, variably preconditioned GCR);
+//   - preconditioner callbacks recognised by identity, and a foreign one refused;
+//   - the real-valued overloads, which must run the reference's code.
 // With a device the accelerated calls are compared with the reference's CG on the same input;
 // without one they must fail with "glinalg: no CUDA device" (no CPU fallback).
 
@@ -20,9 +21,17 @@
 #include <string>
 
 #include "generic_bicgstab.h"
+#include "generic_bicgstab_l.h"
+#include "generic_bicgstab_m.h"
 #include "generic_cg.h"
+#include "generic_cg_flex_precond.h"
 #include "generic_cg_m.h"
+#include "generic_cr.h"
+#include "generic_cr_m.h"
 #include "generic_gcr.h"
+#include "generic_gcr_var_precond.h"
+#include "generic_minres.h"
+#include "generic_precond.h"
 #include "glinalg.h"
 #include "mg_complex.h"
 #include "operators.h"
@@ -47,6 +56,19 @@ void not_a_library_operator(complex<double> *lhs, complex<double> *rhs, void *)
 void real_diagonal(double *lhs, double *rhs, void *)
 {
     for (int i = 0; i < V; i++) lhs[i] = (1.0 + i % 7) * rhs[i];
+}
+
+void foreign_preconditioner(complex<double> *lhs, complex<double> *rhs, int size, void *, inversion_verbose_struct *)
+{
+    for (int i = 0; i < size; i++) lhs[i] = rhs[i];
+}
+
+// Largest error of x against the exact solution of the real diagonal system.
+double max_err(const double *x, const complex<double> *b)
+{
+    double err = 0.0;
+    for (int i = 0; i < V; i++) err = std::fmax(err, std::fabs(x[i] - b[i].real() / (1.0 + i % 7)));
+    return err;
 }
 
 double rel_diff(const complex<double> *a, const complex<double> *b)
@@ -153,6 +175,62 @@ int main()
     report("gcr", minv_vector_gcr(x, b, V, 1000, 1e-10, square_staggered_u1, &stag));
     for (int i = 0; i < V; i++) x[i] = 0.0;
     report("gcr_restart", minv_vector_gcr_restart(x, b, V, 1000, 1e-10, 16, square_staggered_u1, &stag));
+
+    // The sibling solvers.
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("cr", minv_vector_cr(x, b, V, 1000, 1e-10, square_staggered_normal_u1, &stag));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("cr_restart", minv_vector_cr_restart(x, b, V, 1000, 1e-10, 16, square_staggered_normal_u1, &stag));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("minres", minv_vector_minres(x, b, V, 1000, 1e-10, square_laplace_u1, &stag));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("minres_omega", minv_vector_minres(x, b, V, 1000, 1e-10, 0.8, square_laplace_u1, &stag));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("bicgstab_l", minv_vector_bicgstab_l(x, b, V, 1000, 1e-10, 2, square_staggered_u1, &stag));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("bicgstab_l_restart", minv_vector_bicgstab_l_restart(x, b, V, 1000, 1e-10, 16, 2, square_staggered_u1, &stag));
+    inversion_info rcm = minv_vector_cr_m(phis, b, ns, V, 1, 1000, 1e-10, shifts, square_staggered_normal_u1, &stag);
+    report("cr_m", rcm);
+    std::printf("cr_m_resSqmrhs n_rhs=%d", rcm.n_rhs);
+    for (int n = 0; rcm.resSqmrhs && n < ns; n++) std::printf(" %.6e", rcm.resSqmrhs[n]);
+    std::printf("\n");
+    report("bicgstab_m", minv_vector_bicgstab_m(phis, b, ns, V, 1, 1000, 1e-10, shifts, square_staggered_u1, &stag));
+
+    // Preconditioned solvers: identity, MinRes and GCR preconditioners are recognised by
+    // identity (their inner operator too); a foreign preconditioner is refused.
+    minres_precond_struct_complex mr = {4, 0.1, square_staggered_normal_u1, &stag};
+    gcr_precond_struct_complex gp = {4, 0.1, square_staggered_u1, &stag};
+    minres_precond_struct_complex mr_foreign = {4, 0.1, not_a_library_operator, &stag};
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("cg_flex_identity", minv_vector_cg_flex_precond(x, b, V, 1000, 1e-10, square_staggered_normal_u1, &stag,
+                                                           identity_preconditioner, 0));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("cg_flex_minres", minv_vector_cg_flex_precond(x, b, V, 1000, 1e-10, square_staggered_normal_u1, &stag,
+                                                         minres_preconditioner, &mr));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("cg_flex_restart_minres",
+           minv_vector_cg_flex_precond_restart(x, b, V, 1000, 1e-10, 12, square_staggered_normal_u1, &stag,
+                                               minres_preconditioner, &mr));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("gcr_var_gcr", minv_vector_gcr_var_precond(x, b, V, 1000, 1e-10, square_staggered_u1, &stag,
+                                                      gcr_preconditioner, &gp));
+    for (int i = 0; i < V; i++) x[i] = 0.0;
+    report("gcr_var_restart_gcr",
+           minv_vector_gcr_var_precond_restart(x, b, V, 1000, 1e-10, 12, square_staggered_u1, &stag,
+                                               gcr_preconditioner, &gp));
+    report("precond_foreign_operator", minv_vector_gcr_var_precond(x, b, V, 10, 1e-10, square_staggered_u1, &stag,
+                                                                   minres_preconditioner, &mr_foreign));
+    report("precond_foreign_callback", minv_vector_gcr_var_precond(x, b, V, 10, 1e-10, square_staggered_u1, &stag,
+                                                                   foreign_preconditioner, &mr));
+
+    // Real-valued sibling overloads run the reference's code on the diagonal system.
+    double rx2[V], rb2[V];
+    for (int i = 0; i < V; i++) {
+        rx2[i] = 0.0;
+        rb2[i] = b[i].real();
+    }
+    inversion_info rcr = minv_vector_cr(rx2, rb2, V, 1000, 1e-12, real_diagonal, 0);
+    report("real_cr", rcr, max_err(rx2, b));
 
     // The real-valued overload runs the reference's CG: the diagonal system is solved exactly.
     double rx[V], rb[V];

@@ -29,7 +29,10 @@ RECOGNISED = [
     "apply_square_staggered_normal_eo_stencil", "apply_square_staggered_normal_tb_stencil",
     "apply_square_staggered_dagger_eo_stencil", "apply_square_staggered_dagger_tb_stencil",
 ]
-ENTRY_POINTS = ["cg_m", "cg_restart", "bicgstab", "bicgstab_restart", "gcr", "gcr_restart"]
+ENTRY_POINTS = ["cg_m", "cg_restart", "bicgstab", "bicgstab_restart", "gcr", "gcr_restart", "cr", "cr_restart",
+                "minres", "minres_omega", "bicgstab_l", "bicgstab_l_restart", "cr_m", "bicgstab_m",
+                "cg_flex_identity"]
+PRECONDITIONED = ["cg_flex_minres", "cg_flex_restart_minres", "gcr_var_gcr", "gcr_var_restart_gcr"]
 
 
 def parse(out):
@@ -88,9 +91,10 @@ def test_every_complex_entry_point_reaches_the_library(shim_run):
         assert (c["success"] == 1) if device else (c["name"] == "glinalg: no CUDA device"), (name, c)
 
 
-def test_cg_m_result_owns_per_shift_residuals(shim_run):
+@pytest.mark.parametrize("solver", ["cg_m", "cr_m"])
+def test_multishift_result_owns_per_shift_residuals(shim_run, solver):
     cases, extra = shim_run
-    words = extra["cg_m_resSqmrhs"]
+    words = extra[f"{solver}_resSqmrhs"]
     assert words[0] == "n_rhs=3" and len(words) == 4
     res = [float(w) for w in words[1:]]
     if extra["device"] == ["1"]:
@@ -101,18 +105,33 @@ def test_cg_m_result_owns_per_shift_residuals(shim_run):
         assert all(r == float("inf") for r in res)
 
 
+def test_preconditioners_recognised_by_identity(shim_run):
+    """identity_preconditioner, and minres_ / gcr_preconditioner with a library operator inside,
+    reach the library; a foreign inner operator or preconditioner callback is refused (never
+    replaced by the identity)."""
+    cases, extra = shim_run
+    device = extra["device"] == ["1"]
+    for name in PRECONDITIONED:
+        c = cases[name]
+        assert (c["success"] == 1) if device else c["name"].startswith("glinalg: no CUDA device"), (name, c)
+    for name in ("precond_foreign_operator", "precond_foreign_callback"):
+        assert cases[name]["name"] == "glinalg: unsupported operator (preconditioner)", cases[name]
+
+
 def test_real_overloads_run_the_reference(shim_run):
     cases, _ = shim_run
-    c = cases["real_cg"]
-    assert c["success"] == 1 and c["name"] == "CG" and c["iter"] == 7 and c["diff"] <= 1e-12
+    for name, label in (("real_cg", "CG"), ("real_cr", "CR")):
+        c = cases[name]
+        assert c["success"] == 1 and c["name"] == label and c["iter"] == 7 and c["diff"] <= 1e-12, c
 
 
 def test_reference_multishift_program_runs_through_the_shim(shim_run):
     """The reference's own tests/multishift/multishift.cpp, unmodified, linked with the shim:
-    it runs to the end.  Its real-valued solves and the solvers the shim does not replace
-    (CR, CR-M, BiCGstab-M) keep the reference's code and converge; its complex CG and CG-M
-    calls go to the library (without a device they do no work, "0 matrix ops"), and the
-    per-shift check after CG-M (multishift.cpp:482) reads the residual array the shim returns."""
+    it runs to the end.  Its real-valued solves keep the reference's code and converge; its
+    complex CG, CG-M, CR and CR-M calls on square_laplace_u1 go to the library (without a device
+    they do no work, "0 matrix ops"), and the per-shift checks after the multishift solves
+    (multishift.cpp:482, 543, 601) read the residual arrays the shim returns.  Its complex
+    BiCGstab-M on the real-field callback square_staggered is refused as unsupported."""
     import pyoracle
     _, extra = shim_run
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "shim_multishift",
@@ -122,8 +141,9 @@ def test_reference_multishift_program_runs_through_the_shim(shim_run):
     assert run.returncode == 0, run.stderr[-2000:]
     out = run.stdout
     assert "[BICGSTAB-REAL_mass=1]: BiCGStab Success Y" in out
-    assert "[CR-M-CPLX]: CG-M  Success Y" in out
-    cg_cplx = [l for l in out.splitlines() if l.startswith("[TEST]: CG-CPLX Multirhs took")]
-    assert len(cg_cplx) == 1
-    if extra["device"] == ["0"]:
-        assert cg_cplx[0].startswith("[TEST]: CG-CPLX Multirhs took 0 matrix ops")
+    assert "[CR-REAL_mass=1]: CR Success Y" in out
+    for solver in ("CG", "CR"):
+        line = [l for l in out.splitlines() if l.startswith(f"[TEST]: {solver}-CPLX Multirhs took")]
+        assert len(line) == 1
+        if extra["device"] == ["0"]:
+            assert line[0].startswith(f"[TEST]: {solver}-CPLX Multirhs took 0 matrix ops"), line
