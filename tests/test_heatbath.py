@@ -11,15 +11,21 @@ GPU: the device kernels and solvers against the same reference outputs.
 
 Bars on the GPU.  Gauge utilities as for the random fields: plaquette and charge within 1e-13
 absolute, gauge transform within 1e-15 and APE smearing within 1e-13 per link.  FP64 CG: the
-FP64-true relative residual below 1e-10, the iteration count within one of the reference's,
-and the solution within 1e-11 relative when the count is the reference's.  The count is not
-held exact because the stopping test can be marginal on these fields: on the beta = 30 field at
-m = 0.1 the reference's own recurrence with its dot products summed in another order (numpy's
-pairwise sum) stops at 153 iterations instead of 154.  A solve one iteration apart is held to
-the bound that any two solutions with relative residual below 1e-10 satisfy,
-2 kappa 1e-10 with kappa(M^dagger M) <= (m^2 + 4) / m^2.  Mixed FP32 CG at m = 0.1: the FP64-true
-relative residual below 1e-10 and the solution within that same bound (8.0e-8) of the
-reference's."""
+iteration count within one of the reference's, and the solution within 1e-10 relative when the
+count is the reference's.  The count is not held exact because the stopping test can be
+marginal on these fields: on the beta = 30 field at m = 0.1 the reference's own recurrence
+with its dot products summed in another order (numpy's pairwise sum) stops at 153 iterations
+instead of 154.  At equal counts those reorderings land 1e-14 to 3e-12 from the reference's
+solution.  The FP64 CG stops, as the reference's does, on its iterated residual, whose final
+value lies up to 1.6e-4 relative from the recomputed true residual on these fields (and at
+9.97e-11 for one reordering); its true relative residual is therefore held below 1e-10 times
+1.001.  A solve one iteration apart is held to the bound that any two solutions with relative
+residual below 1e-10 satisfy, 2 kappa 1e-10 with kappa(M^dagger M) <= (m^2 + 4) / m^2.
+Mixed FP32 CG at m = 0.1: the solution within that same bound (8.0e-8) of the reference's,
+and the true relative residual below 1e-10 times 1.001.  The mixed solver stops on an FP64 true
+residual computed with the device's stencil; the one recomputed here uses the oracle's, and
+b - Ax cancels to 1e-10 of |b|, so last-bit differences of the two stencils move it by up to
+about 1e-6 relative."""
 from __future__ import annotations
 
 import numpy as np
@@ -106,9 +112,9 @@ def test_device_cg_matches_reference(gl, gpu, oracle, golden, key, tag):
     info = gl.minv_vector_cg(x, b, b.size, c["max_iter"], c["eps"], gl.square_staggered_normal_u1,
                              gl.StaggeredU1Op(U, m, L, L))
     assert info.success and info.name == "CG"
-    assert true_relres(oracle, m, U, x, b) < 1e-10
+    assert true_relres(oracle, m, U, x, b) < 1e-10 * 1.001
     assert abs(info.iter - c["iter"]) <= 1 and info.ops_count - info.iter == c["ops_count"] - c["iter"]
-    bound = 1e-11 if info.iter == c["iter"] else 2.0 * kappa_bound(m) * 1e-10
+    bound = 1e-10 if info.iter == c["iter"] else 2.0 * kappa_bound(m) * 1e-10
     assert rel(x, vec[f"{key}_cg_{tag}"]) < bound
 
 
@@ -122,5 +128,5 @@ def test_device_mixed_cg_matches_reference(gl, gpu, oracle, golden, key):
     info = gl.minv_vector_cg(x, b, b.size, 20000, 1e-10, gl.square_staggered_normal_u1,
                              gl.StaggeredU1Op(U, 0.1, L, L), precision=gl.PREC_SINGLE)
     assert info.success and info.status == 0
-    assert true_relres(oracle, 0.1, U, x, b) < 1e-10
+    assert true_relres(oracle, 0.1, U, x, b) < 1e-10 * 1.001
     assert rel(x, vec[f"{key}_cg_m0.1"]) < 2.0 * kappa_bound(0.1) * 1e-10
