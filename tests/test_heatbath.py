@@ -6,7 +6,8 @@ beta = 60 fields carry the topological charge their file names state (+1 and -3)
 
 CPU: the oracle bit for bit against the reference's plaquette, topological charge, gauge
 transform and APE smearing (u1_utils.cpp) and its CG on the staggered normal equations
-(generic_cg.cpp:278-382) on these fields, and the known charges.
+(generic_cg.cpp:278-382) on these fields, the known charges, and the library's text reader on
+the reference's files themselves (where the reference checkout is present).
 GPU: the device kernels and solvers against the same reference outputs.
 
 Bars on the GPU.  Gauge utilities as for the random fields: plaquette and charge within 1e-13
@@ -130,3 +131,19 @@ def test_device_mixed_cg_matches_reference(gl, gpu, oracle, golden, key):
     assert info.success and info.status == 0
     assert true_relres(oracle, 0.1, U, x, b) < 1e-10 * 1.001
     assert rel(x, vec[f"{key}_cg_m0.1"]) < 2.0 * kappa_bound(0.1) * 1e-10
+
+
+@pytest.mark.parametrize("key", list(HB))
+def test_library_reads_the_reference_files(gl, golden, key):
+    """The library's host reader (glinalg_read_gauge_u1) on the reference's own heat-bath text
+    files gives the links the reference's read_gauge_u1 gave, within 1 ulp (the same text
+    through cos / sin of another libm).  Needs the reference checkout."""
+    import os
+    import pyoracle
+    vec, cases = golden
+    path = os.path.join(pyoracle.reference_dir(), "multigrid", "aa_mg", "cfg", cases[f"{key}_gauge"]["file"])
+    if not os.path.isfile(path):
+        pytest.skip("the reference checkout is not present")
+    U = np.zeros(2 * L * L, np.complex128)
+    gl.read_gauge_u1(U, L, L, path)
+    assert np.max(np.abs(U - vec[f"{key}_links"])) <= 2.3e-16
