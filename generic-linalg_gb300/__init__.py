@@ -156,11 +156,20 @@ class Operator:
         d.kind, d.lx, d.ly, d.nc, d.mass = int(kind), int(lx), int(ly), int(nc), float(mass)
         keep = []
         dev_flags = []
+        # complex values glinalg_operator_create reads from each array: it gets plain pointers
+        # and cannot check their lengths, so a short array is refused here instead of read past
+        v = max(int(lx), 0) * max(int(ly), 0)
+        nc2 = max(int(nc), 0) ** 2
+        need = {"links": 2 * v, "clover": v * nc2, "hopping": 4 * v * nc2, "two_link": 8 * v * nc2}
 
         def put(name, a):
             if a is None:
                 return
-            p, _, dev = _field_ptr(a if _is_torch(a) else np.ascontiguousarray(a, dtype=np.complex128))
+            a = a if _is_torch(a) else np.ascontiguousarray(a, dtype=np.complex128)
+            p, n, dev = _field_ptr(a)
+            if n < need[name]:
+                raise ValueError(f"{name} holds {n} complex values; a {lx}x{ly} operator with nc = {nc} "
+                                 f"reads {need[name]}")
             keep.append(a)
             dev_flags.append(dev)
             setattr(d, name, _dptr(p))

@@ -112,3 +112,31 @@ def test_rejected_arguments_name_the_check(gl):
     assert L.glinalg_last_error() == b"invalid argument: !path"
     assert L.glinalg_write_gauge_u1(ptr, 4, 4, None) == 1
     assert L.glinalg_last_error() == b"invalid argument: !path"
+
+
+def test_operator_arrays_shorter_than_the_lattice_are_refused(gl):
+    """glinalg_operator_create reads 2*lx*ly links (or lx*ly*nc^2 clover, 4x that hopping, 8x
+    two-link terms) through plain pointers; the Python layer refuses shorter arrays before
+    the call instead of letting the library read past them."""
+    with pytest.raises(ValueError, match="links holds 31 complex values"):
+        gl.Operator(2, 4, 4, 0.1, np.ones(31, np.complex128))
+    v, nc = 16, 2
+    cl, hp = np.zeros(v * nc * nc, np.complex128), np.zeros(4 * v * nc * nc, np.complex128)
+    with pytest.raises(ValueError, match="hopping"):
+        gl.Operator(4, 4, 4, nc=nc, clover=cl, hopping=hp[:-1])
+    with pytest.raises(ValueError, match="two_link"):
+        gl.Operator(4, 4, 4, nc=nc, clover=cl, hopping=hp, two_link=np.zeros(8 * v * nc * nc - 1, np.complex128))
+
+
+def test_operator_descriptor_checks_run_before_the_device(gl):
+    """An empty lattice or missing links are rejected by the library with a message, before it
+    looks for a device; arrays of the right length in another dtype are converted (and kept
+    alive) and reach the device check."""
+    import torch
+    with pytest.raises(gl.GlinalgError, match=r"invalid argument: d->lx <= 0 \|\| d->ly <= 0"):
+        gl.Operator(2, 0, 4, 0.1, np.ones(2, np.complex128))
+    with pytest.raises(gl.GlinalgError, match=r"invalid argument: !sten && !d->links"):
+        gl.Operator(2, 4, 4, 0.1, None)
+    if not torch.cuda.is_available():
+        with pytest.raises(gl.GlinalgError, match="no CUDA device"):
+            gl.Operator(2, 4, 4, 0.1, np.ones(32, np.complex64))
