@@ -118,6 +118,18 @@ def _dptr(p):
     return C.cast(p, C.POINTER(C.c_double))
 
 
+def _need(name, n, want):
+    """The library gets plain pointers and reads (or writes) `want` values through them: refuse
+    a shorter array here rather than let it run past the end."""
+    if n < want:
+        raise ValueError(f"{name} holds {n} values; this call needs {want}")
+
+
+def _same_side(*devs):
+    if len(set(devs)) > 1:
+        raise ValueError("the arrays of one call must all be on the host or all on the device")
+
+
 # ---------------------------------------------------------------- operator descriptors
 
 class StaggeredU1Op:
@@ -618,12 +630,18 @@ def _multishift(fn, phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, s
                 matrix_vector, extra_info, worst_first, verbosity):
     op, temp = _resolve(matrix_vector, extra_info)
     try:
+        if len(phi) < n_shift:
+            raise ValueError(f"phi holds {len(phi)} fields; n_shift is {n_shift}")
         ptrs = [_field_ptr(p, writable=True) for p in phi[:n_shift]]
-        bp, _, bdev = _field_ptr(phi0)
+        bp, bn, bdev = _field_ptr(phi0)
         if any(d != bdev for _, _, d in ptrs):
             raise ValueError("phi and phi0 must all be on the host or all on the device")
+        for j, (_, n, _) in enumerate(ptrs):
+            _need(f"phi[{j}]", n, size)
+        _need("phi0", bn, size)
         arr = (C.POINTER(C.c_double) * n_shift)(*[_dptr(p) for p, _, _ in ptrs])
         sh = np.ascontiguousarray(shifts[:n_shift], dtype=np.float64)
+        _need("shifts", sh.size, n_shift)
         res = np.zeros(n_shift)
         info = InfoStruct()
         info.resSqmrhs = res.ctypes.data_as(C.POINTER(C.c_double))
@@ -646,9 +664,13 @@ def cg_m_multi(op: Operator, phi, phi0, shifts, resid_freq_check=1, max_iter=100
     """Multishift CG for several sources at once.  phi: (n_rhs, n_shift, size), phi0:
     (n_rhs, size); both complex128, host or device."""
     n_rhs, n_shift = phi.shape[0], phi.shape[1]
-    pp, _, dev = _field_ptr(phi, writable=True)
-    bp, _, _ = _field_ptr(phi0)
+    pp, pn, dev = _field_ptr(phi, writable=True)
+    bp, bn, bdev = _field_ptr(phi0)
+    _same_side(dev, bdev)
     sh = np.ascontiguousarray(shifts, dtype=np.float64)
+    _need("phi", pn, n_rhs * n_shift * op.size)
+    _need("phi0", bn, n_rhs * op.size)
+    _need("shifts", sh.size, n_shift)
     infos = (InfoStruct * n_rhs)()
     res = [np.zeros(n_shift) for _ in range(n_rhs)]
     for q in range(n_rhs):
@@ -664,10 +686,16 @@ def cg_m_multi(op: Operator, phi, phi0, shifts, resid_freq_check=1, max_iter=100
 def cg_batch(ops, phis, phi0s, max_iter=10000, eps=1e-10, precision=PREC_DOUBLE, delta=0.0):
     """CG on independent Hermitian systems (one Operator each)."""
     n = len(ops)
+    if len(phis) != n or len(phi0s) != n:
+        raise ValueError("one solution and one source field per operator")
     hs = (C.c_void_p * n)(*[o.handle.value for o in ops])
     pps = [_field_ptr(p, writable=True) for p in phis]
     bps = [_field_ptr(b) for b in phi0s]
     dev = pps[0][2]
+    _same_side(*[d for _, _, d in pps + bps])
+    for q in range(n):
+        _need(f"phis[{q}]", pps[q][1], ops[q].size)
+        _need(f"phi0s[{q}]", bps[q][1], ops[q].size)
     parr = (C.POINTER(C.c_double) * n)(*[_dptr(p) for p, _, _ in pps])
     barr = (C.POINTER(C.c_double) * n)(*[_dptr(p) for p, _, _ in bps])
     infos = (InfoStruct * n)()
@@ -677,12 +705,22 @@ def cg_batch(ops, phis, phi0s, max_iter=10000, eps=1e-10, precision=PREC_DOUBLE,
 
 
 def staggered_force(op: Operator, X, Y, grad):
-    xp, _, dev = _field_ptr(X)
-    yp, _, _ = _field_ptr(Y)
+    """dS/dtheta = -2 Re(Y^dagger dM/dtheta X) for every link angle into grad (float64, 2V)."""
+    xp, xn, dev = _field_ptr(X)
+    yp, yn, ydev = _field_ptr(Y)
     if _is_torch(grad):
-        gp = C.c_void_p(grad.data_ptr())
+        import torch
+        if grad.dtype != torch.float64 or not grad.is_contiguous():
+            raise TypeError("grad must be a contiguous float64 tensor")
+        gp, gn, gdev = C.c_void_p(grad.data_ptr()), grad.numel(), grad.is_cuda
     else:
-        gp = C.c_void_p(grad.ctypes.data)
+        if grad.dtype != np.float64 or not grad.flags["C_CONTIGUOUS"] or not grad.flags["WRITEABLE"]:
+            raise TypeError("grad must be a writable C-contiguous float64 array")
+        gp, gn, gdev = C.c_void_p(grad.ctypes.data), grad.size, False
+    _same_side(dev, ydev, gdev)
+    _need("X", xn, op.size)
+    _need("Y", yn, op.size)
+    _need("grad", gn, 2 * op.size)
     _capi.check(lib().glinalg_staggered_force(op.handle, _dptr(xp), _dptr(yp), _dptr(gp),
                                               GLINALG_PTR_DEVICE if dev else 0), "glinalg_staggered_force")
     return grad
@@ -692,6 +730,10 @@ def staggered_action_grad(op: Operator, phi, sigma=0.0, eps=1e-12, max_iter=1000
                           precision=PREC_DOUBLE, delta=0.0, X_out=None):
     """Returns (S, dS/dtheta, InversionInfo) for S = phi^dagger (D^dagger D + sigma)^-1 phi."""
     pp, n, dev = _field_ptr(phi)
+    _need("phi", n, op.size)
+    if X_out is not None:
+        _need("X_out", _field_ptr(X_out, writable=True)[1], op.size)
+        _same_side(dev, _field_ptr(X_out)[2])
     if dev:
         import torch
         grad = torch.zeros(2 * n, dtype=torch.float64, device=phi.device)
@@ -712,7 +754,9 @@ def staggered_action_grad(op: Operator, phi, sigma=0.0, eps=1e-12, max_iter=1000
 def dot(a, b):
     """<a, b> = sum conj(a_i) b_i (generic_vector.h:102)."""
     ap, n, dev = _field_ptr(a)
-    bp, _, _ = _field_ptr(b)
+    bp, bn, bdev = _field_ptr(b)
+    _same_side(dev, bdev)
+    _need("b", bn, n)
     out = (C.c_double * 2)()
     _capi.check(lib().glinalg_dot(_dptr(ap), _dptr(bp), n, out, GLINALG_PTR_DEVICE if dev else 0), "dot")
     return complex(out[0], out[1])
@@ -790,13 +834,15 @@ def write_gauge_u1(gauge_field, x_len, y_len, output_file):
 
 def unit_gauge_u1(gauge_field, x_len, y_len):
     """unit_gauge_u1 (u1_utils.cpp:69-75)."""
-    p, _, dev = _field_ptr(gauge_field, writable=True)
+    p, n, dev = _field_ptr(gauge_field, writable=True)
+    _need("gauge_field", n, 2 * x_len * y_len)
     _capi.check(lib().glinalg_unit_gauge_u1(_dptr(p), x_len, y_len, _flags(dev)), "unit_gauge_u1")
 
 
 def get_plaquette_u1(gauge_field, x_len, y_len):
     """get_plaquette_u1 (u1_utils.cpp:190-207): the average plaquette (complex)."""
-    p, _, dev = _field_ptr(gauge_field)
+    p, n, dev = _field_ptr(gauge_field)
+    _need("gauge_field", n, 2 * x_len * y_len)
     out = np.zeros(2)
     _capi.check(lib().glinalg_plaquette_u1(_dptr(p), x_len, y_len, out.ctypes.data_as(C.POINTER(C.c_double)),
                                            _flags(dev)), "plaquette_u1")
@@ -805,7 +851,8 @@ def get_plaquette_u1(gauge_field, x_len, y_len):
 
 def get_topo_u1(gauge_field, x_len, y_len):
     """get_topo_u1 (u1_utils.cpp:210-226): the topological charge."""
-    p, _, dev = _field_ptr(gauge_field)
+    p, n, dev = _field_ptr(gauge_field)
+    _need("gauge_field", n, 2 * x_len * y_len)
     out = C.c_double()
     _capi.check(lib().glinalg_topo_u1(_dptr(p), x_len, y_len, C.byref(out), _flags(dev)), "topo_u1")
     return out.value
@@ -813,19 +860,23 @@ def get_topo_u1(gauge_field, x_len, y_len):
 
 def apply_gauge_trans_u1(gauge_field, gauge_trans, x_len, y_len):
     """apply_gauge_trans_u1 (u1_utils.cpp:128-142), in place."""
-    p, _, dev = _field_ptr(gauge_field, writable=True)
-    g, _, gdev = _field_ptr(gauge_trans)
+    p, n, dev = _field_ptr(gauge_field, writable=True)
+    g, gn, gdev = _field_ptr(gauge_trans)
     if dev != gdev:
         raise ValueError("gauge_field and gauge_trans must both be on the host or both on the device")
+    _need("gauge_field", n, 2 * x_len * y_len)
+    _need("gauge_trans", gn, x_len * y_len)
     _capi.check(lib().glinalg_apply_gauge_trans_u1(_dptr(p), _dptr(g), x_len, y_len, _flags(dev)), "gauge_trans")
 
 
 def apply_ape_smear_u1(smeared_field, gauge_field, x_len, y_len, alpha, n_iter):
     """apply_ape_smear_u1 (u1_utils.cpp:145-187)."""
-    o, _, odev = _field_ptr(smeared_field, writable=True)
-    p, _, dev = _field_ptr(gauge_field)
+    o, on, odev = _field_ptr(smeared_field, writable=True)
+    p, n, dev = _field_ptr(gauge_field)
     if dev != odev:
         raise ValueError("both fields must be on the host or both on the device")
+    _need("smeared_field", on, 2 * x_len * y_len)
+    _need("gauge_field", n, 2 * x_len * y_len)
     _capi.check(lib().glinalg_apply_ape_smear_u1(_dptr(o), _dptr(p), x_len, y_len, float(alpha), int(n_iter),
                                                  _flags(dev)), "ape_smear_u1")
 

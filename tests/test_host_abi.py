@@ -140,3 +140,35 @@ def test_operator_descriptor_checks_run_before_the_device(gl):
     if not torch.cuda.is_available():
         with pytest.raises(gl.GlinalgError, match="no CUDA device"):
             gl.Operator(2, 4, 4, 0.1, np.ones(32, np.complex64))
+
+
+def test_wrappers_refuse_short_or_mismatched_arrays(gl):
+    """The Python layer checks what the C ABI cannot (plain pointers): array lengths against
+    what the call reads or writes, dtypes of raw outputs, and arrays of one call on one side.
+    Every refusal happens before the library is called (an operator stand-in with only a
+    size is enough here)."""
+    import types
+    z = lambda n: np.zeros(n, np.complex128)
+    with pytest.raises(ValueError, match="b holds 15 values"):
+        gl.dot(z(16), z(15))
+    with pytest.raises(ValueError, match="gauge_field holds 31"):
+        gl.get_plaquette_u1(z(31), 4, 4)
+    with pytest.raises(ValueError, match="gauge_field holds 31"):
+        gl.unit_gauge_u1(z(31), 4, 4)
+    with pytest.raises(ValueError, match="gauge_trans holds 15"):
+        gl.apply_gauge_trans_u1(z(32), z(15), 4, 4)
+    with pytest.raises(ValueError, match="smeared_field holds 31"):
+        gl.apply_ape_smear_u1(z(31), z(32), 4, 4, 0.5, 1)
+    op = types.SimpleNamespace(size=16, handle=C.c_void_p())
+    with pytest.raises(TypeError, match="float64"):
+        gl.staggered_force(op, z(16), z(16), np.zeros(32, np.float32))
+    with pytest.raises(ValueError, match="grad holds 31 values"):
+        gl.staggered_force(op, z(16), z(16), np.zeros(31))
+    with pytest.raises(ValueError, match="phi0 holds 31 values"):
+        gl.cg_m_multi(op, np.zeros((2, 3, 16), np.complex128), z(31), np.ones(3))
+    with pytest.raises(ValueError, match="shifts holds 2 values"):
+        gl.cg_m_multi(op, np.zeros((2, 3, 16), np.complex128), z(32), np.ones(2))
+    with pytest.raises(ValueError, match="one solution and one source field per operator"):
+        gl.cg_batch([op, op], [z(16)], [z(16), z(16)])
+    with pytest.raises(ValueError, match=r"phis\[1\] holds 15 values"):
+        gl.cg_batch([op, op], [z(16), z(15)], [z(16), z(16)])
