@@ -973,6 +973,10 @@ def generate_coarse_from_fine_stencil(stenc_coarse, stenc_fine, mgstruct: MgLeve
         if temp:
             fine.close()
     if stenc_coarse is not None:
+        # the library writes the coarse clover (V_c nc_c^2) and hopping (4 V_c nc_c^2) terms
+        cc = mgstruct.coarse_size * mgstruct.nc_coarse
+        _need("stenc_coarse.clover", stenc_coarse.clover.size, cc)
+        _need("stenc_coarse.hopping", stenc_coarse.hopping.size, 4 * cc)
         _capi.check(lib().glinalg_operator_stencil_get(coarse.handle, _dptr(C.c_void_p(stenc_coarse.clover.ctypes.data)),
                                                        _dptr(C.c_void_p(stenc_coarse.hopping.ctypes.data)), 0),
                     "operator_stencil_get")
@@ -1015,10 +1019,12 @@ class MgPrecondStruct:
 
     def apply(self, lhs, rhs):
         """One application of mg_preconditioner on the finest level."""
-        o, _, d1 = _field_ptr(lhs, writable=True)
-        i, _, d2 = _field_ptr(rhs)
+        o, no, d1 = _field_ptr(lhs, writable=True)
+        i, ni, d2 = _field_ptr(rhs)
         if d1 != d2:
             raise ValueError("lhs and rhs must both be on the host or both on the device")
+        _need("lhs", no, self.ops[0].size)
+        _need("rhs", ni, self.ops[0].size)
         _capi.check(lib().glinalg_mg_apply(self.handle, _dptr(o), _dptr(i), _flags(d1)), "mg_apply")
 
     def __del__(self):
