@@ -25,6 +25,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -38,17 +40,43 @@ MAX_ITER = 100000
 REF_ITERS = 2093
 METRIC = "time-to-1e-10 resid, 1024^2 staggered CG: mixed/batched vs FP64 on GB300; HBM GB/s"
 HEADLINE = ("fp32", 1)
-# DRAM bytes (read + write) of one launch of the persistent inner-loop kernels on this workload,
-# from ncu --set full captures: k_persist (fields in L2; the first launch of a solve, 254 inner
-# iterations) and k_resident (rectangle state on chip, x_lo and links in tensor memory; a
-# 20-iteration launch).  In both the traffic is the compulsory load of the launch's state and
-# does not grow with its iterations.
-K_PERSIST_DRAM_BYTES = 41.987328e6 + 3.212544e6
-K_RESIDENT_DRAM_BYTES = 42.13248e6 + 0.00896e6
-# Shared-memory wavefronts (128 B) per SM and inner iteration of k_resident at 1024^2, from the
-# same capture (19.95 M over 152 SMs and 20 iterations, entry included); GB300 serves one per
-# clock per SM.
-K_RESIDENT_SMEM_WAVEFRONTS = 6.56e3
+# ncu captures of the persistent inner-loop kernels on this workload (profiles/), each stamped
+# with the SHA-256 of the kernel's source file when it was captured.  A capture whose stamp no
+# longer matches the source is reported as stale (its figures null) rather than applied to a
+# changed kernel; tests/test_host_abi.py fails while any stamp is out of date.
+#   dram_bytes_per_launch: dram__bytes_read.sum + dram__bytes_write.sum of one launch
+#   smem_wavefronts_per_sm_iter: l1tex__data_pipe_lsu_wavefronts_mem_shared.sum over the SMs and
+#     the launch's inner iterations (entry included); GB300 serves one 128 B wavefront per clock
+#     per SM
+CAPTURES = {
+    "resident": {"source": "generic-linalg_gb300/csrc/stag_resident.cuh", "sha256": None,
+                 "kernel": "k_resident<16 warps, x_lo and links in tensor memory>",
+                 "profile": "profiles/k_resident_fp32_1024.md", "iters_per_launch": 20,
+                 "dram_bytes_per_launch": 42.13248e6 + 0.00896e6, "smem_wavefronts_per_sm_iter": 6.56e3},
+    "persist": {"source": "generic-linalg_gb300/csrc/stag_tiles.cuh", "sha256": None,
+                "kernel": "k_persist", "profile": "profiles/k_persist_fp32_1024.md", "iters_per_launch": 254,
+                "dram_bytes_per_launch": 41.987328e6 + 3.212544e6},
+}
+RESIDENT_CANDIDATES = (6, 7, 8, 11, 12, 13, 14)
+
+
+def source_sha256(rel):
+    import hashlib
+    with open(os.path.join(ROOT, rel), "rb") as f:
+        return hashlib.sha256(f.read()).hexdigest()
+
+
+def capture_for(cand):
+    """The ncu capture that describes persistent-kernel candidate `cand`, with "fresh" telling
+    whether the kernel source still matches it; None if no capture covers the candidate."""
+    key = "resident" if cand in RESIDENT_CANDIDATES else ("persist" if 0 <= cand <= 3 else None)
+    if key is None:
+        return None
+    c = dict(CAPTURES[key])
+    c["fresh"] = c["sha256"] is not None and c["sha256"] == source_sha256(c["source"])
+    return c
+
+
 VARIANTS = [("fp32", 1), ("fp16", 2), ("bf16", 3)]
 # persistent inner-loop kernels by the library's candidate index (glinalg_tuned_persist)
 PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 rows>",
@@ -126,49 +154,77 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(iters_needed, n_iter=30):
-    """The reference's CG (CPU oracle restatement, single thread) on the same system, a
-    bounded sample of n_iter iterations, extrapolated to the full iteration count."""
-    import numpy as np
+# The workload both arms are quoted on (printed as `config` by each).
+CONFIG = {"workload": "staggered normal-equation CG to FP64-true relres 1e-10, 1024x1024, m=0.01, x0=0",
+          "lattice": [LX, LY], "mass": MASS, "tol": EPS, "max_iter": MAX_ITER,
+          "inputs": "std::mt19937(1337): rand_gauge_u1 links (theta uniform in (-pi, pi)), then a "
+                    "gaussian complex source"}
+
+
+def oracle_inputs():
+    """Links and source from the oracle's own restatement of the reference tests' generators
+    (std::mt19937(1337), rand_gauge_u1, then gaussian): no library code involved."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    gl = importlib.import_module("generic-linalg_gb300")
-    g = gl.Generator(SEED)
+    g = pyoracle.Generator(SEED)
     U = g.rand_gauge_u1(LX, LY)
     b = g.gaussian(LX * LY)
+    return U, b
+
+
+def oracle_solve(U, b, threads=None):
+    """One complete FP64 CG solve of the workload by the CPU oracle (the reference's
+    minv_vector_cg, generic_cg.cpp:278-382, restated; operator and vector loops spread over
+    `threads` host threads, sums serial in the reference's order, so the iterates are the
+    serial reference's bit for bit).  Returns (x, info, seconds, threads used)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
     O = pyoracle.Oracle()
+    nth = O.set_threads(threads)
     op = pyoracle.Operator("staggered_normal", LX, LY, MASS, U)
     t0 = time.perf_counter()
-    _, info, _ = O.solve("cg", op, b, max_iter=n_iter, eps=EPS)
+    x, info, _ = O.solve("cg", op, b, max_iter=MAX_ITER, eps=EPS)
     dt = time.perf_counter() - t0
-    # the sample ran n_iter iterations plus 3 setup / check operator applications
-    per_iter = dt / (info["iter"] + 3 * 0.67)
-    return {
-        "value": per_iter * iters_needed * 1e3, "unit": "ms", "cores": 1, "kind": "port",
-        "sample": f"{info['iter']} CG iterations of the 1024^2 m=0.01 system ({dt:.1f} s, "
-                  f"{per_iter * 1e3:.1f} ms/iteration) extrapolated to {iters_needed} iterations",
-    }
+    return x, info, dt, nth
+
+
+def cpu_sample_text(info, nth):
+    return (f"one complete solve per step: {info['iter']} CG iterations, {info['ops_count']} operator "
+            f"applications, true relres {np.sqrt(info['resSq']) / BNORM[0]:.3e}; operator and vector "
+            f"loops on {nth} host threads, dot and norm sums serial in the reference's order")
+
+
+BNORM = [1.0]
 
 
 def run_reference(args):
-    """--impl reference: the reference algorithm on the host cores (rank 0 only)."""
+    """--impl reference: the reference's CG (the oracle port: oracle/_ref needs the reference
+    checkout, absent on the GPU box) on the host cores, W + K complete solves of the workload;
+    rank 0 only.  Loads only the oracle's library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    samples = []
+    U, b = oracle_inputs()
+    BNORM[0] = float(np.linalg.norm(b))
+    samples, info, nth = [], None, 1
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(REF_ITERS, n_iter=args.ref_iters)
+        _, info, dt, nth = oracle_solve(U, b)
+        if not info["success"]:
+            raise RuntimeError(f"reference CG did not converge: {info}")
         if i >= args.warmup:
-            samples.append(cb["value"])
+            samples.append(dt * 1e3)
     v = statistics.mean(samples)
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "staggered normal-equation CG, 1024x1024, m=0.01, tol 1e-10, FP64 (reference CPU CG)",
-                   "lattice": [LX, LY], "mass": MASS, "tol": EPS, "seed": SEED},
-        "cpu_baseline": {**cb, "value": v},
-        "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v, 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG,
+        "variant": "fp64 CG (the reference's algorithm on the host cores)",
+        "results": {"iters": info["iter"], "ops_count": info["ops_count"],
+                    "true_relres_fp64": float(np.sqrt(info["resSq"]) / BNORM[0]),
+                    "ms_min_max": [round(min(samples), 3), round(max(samples), 3)]},
+        "cpu_baseline": {"value": round(v, 3), "unit": "ms", "cores": nth, "kind": "port",
+                         "sample": cpu_sample_text(info, nth)},
+        "e2e": {"value": round(v, 3), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
@@ -658,7 +714,7 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
-    results = {}
+    results, sols = {}, {}
     clocks = ClockSampler(local)
     head_name, head_prec = HEADLINE
     wanted = set(args.variants.split(","))
@@ -677,11 +733,13 @@ def main():
         if name == head_name:
             clk = clocks.stop()
         results[name] = (times, infos)
+        sols[name] = x.cpu().numpy().copy()
     # the plain FP64 GPU CG (reference recurrence) on the same system
     if "fp64" in wanted:
         solve(0)
         t64 = [solve(0) for _ in range(max(1, args.fp64_steps))]
         results["fp64"] = ([t for t, _ in t64], [i for _, i in t64])
+        sols["fp64"] = x.cpu().numpy().copy()
 
     head_times, head_infos = results[head_name]
     ms = statistics.mean(head_times)
@@ -691,32 +749,35 @@ def main():
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms_max = tt.item()
 
-    # true residual of the last headline solve, rechecked with the FP64 operator
+    # true residual of the headline solution, rechecked with the FP64 operator
+    xh_head = torch.from_numpy(sols[head_name]).to(dev)
     Ax = torch.zeros_like(bd)
-    op.apply(Ax, x)
+    op.apply(Ax, xh_head)
 
     # dominant kernel: the persistent inner-loop kernel of the headline solve (both stencil
     # phases, the vector updates and the grid-wide sums), timed with CUDA events around launches
     # of its own on the library stream, each running the timed solve's mean inner iterations per
     # launch; cross-checked with the kernel's device clock inside the timed solves
-    peak, peak_src = peaks()
+    hbm_peak, peak_src = peaks()
     hi_ = head_infos[-1]
     k_launch = max(1, hi_.kernel_launches)
     persist_cand = L.glinalg_tuned_persist(op.handle, head_prec)
     persist_kernel = PERSIST_KERNELS.get(persist_cand, "none")
-    resident = persist_cand in (6, 7, 8, 11, 12, 13, 14)
+    resident = persist_cand in RESIDENT_CANDIDATES
     # algorithmic bytes: the canonical CG iteration on D^dagger D, 17 complex words per site
     # (D p -> t: p, 2 links, t; D^dagger t -> Ap: t, 2 links, Ap; x, p, r, Ap in, x, r out;
     # p = r + beta p: 3), 136 B per site in FP32
     cg_bytes = 17 * 8.0 * LX * LY
     k_ms_solve = hi_.kernel_ms / k_launch
-    achieved_solve = (cg_bytes * hi_.iter / k_launch / (k_ms_solve * 1e-3) / 1e9) if k_ms_solve > 0 else 0.0
     it_per_launch = max(1, round(hi_.iter / k_launch))
     ev_ms, ev_bytes, ev_cand = C_double(), C_double(), C_int()
     gl._capi.check(L.glinalg_profile_persist_kernel(op.handle, head_prec, 5, it_per_launch, ev_ms, ev_bytes,
                                                     ev_cand), "profile_persist_kernel")
     k_ms, k_bytes = ev_ms.value, cg_bytes * it_per_launch
-    achieved = k_bytes / (k_ms * 1e-3) / 1e9
+    hbm_equiv = k_bytes / (k_ms * 1e-3) / 1e9
+    hbm_equiv_solve = (cg_bytes * hi_.iter / k_launch / (k_ms_solve * 1e-3) / 1e9) if k_ms_solve > 0 else 0.0
+    smem_gbs, smem_ms = C_double(), C_double()
+    gl._capi.check(L.glinalg_probe_smem_bandwidth(smem_gbs, smem_ms), "probe_smem_bandwidth")
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
     Uh = torch.from_numpy(U).pin_memory().numpy()
@@ -740,10 +801,19 @@ def main():
         if dist:
             dist.destroy_process_group()
         return
-    cb = None if args.no_cpu_baseline else cpu_baseline(results["fp64"][1][0].iter if "fp64" in results else REF_ITERS)
     hi = head_infos[-1]
     t64m = statistics.mean(results["fp64"][0]) if "fp64" in results else float("nan")
     relres = (torch.linalg.vector_norm(bd - Ax) / torch.linalg.vector_norm(bd)).item()
+    # the FP64 CPU oracle's solution of the same system (its own generator, bit-identical inputs):
+    # the CPU baseline and the reference point of every variant's solution error
+    cb, x_or, or_info = None, None, None
+    if not args.no_cpu_baseline:
+        Uo, bo = oracle_inputs()
+        assert np.array_equal(Uo, U) and np.array_equal(bo, b), "oracle and library generators disagree"
+        BNORM[0] = float(np.linalg.norm(bo))
+        x_or, or_info, dt, nth = oracle_solve(Uo, bo)
+        cb = {"value": round(dt * 1e3, 3), "unit": "ms", "cores": nth, "kind": "port",
+              "sample": cpu_sample_text(or_info, nth)}
     variants = {}
     for name in [n for n in ("fp32", "fp16", "bf16", "fp64") if n in results]:
         ts, ins = results[name]
@@ -752,58 +822,71 @@ def main():
                           "reliable_updates": ins[-1].reliable_updates,
                           "true_relres": float(np.sqrt(ins[-1].resSq) / np.linalg.norm(b)),
                           "gbytes": round(ins[-1].gbytes, 3)}
+        if x_or is not None:
+            variants[name]["err_vs_oracle"] = float(np.linalg.norm(sols[name] - x_or) / np.linalg.norm(x_or))
     # kernels of one headline solve: link packing, |b|^2 and the setup reliable update (6),
     # then per cycle of the outer loop the persistent inner-loop kernel, the reliable update
     # (6), the outer-loop tail and the graph's loop guard
     launches = 8 + 9 * hi.kernel_launches
-    roof_note = ("dram__bytes_read.sum + dram__bytes_write.sum of one launch of this kernel (ncu --set full "
-                 "capture): the compulsory load of the launch's state, which does not grow with its iterations")
-    onchip = None
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    roof = {"kernel": f"{persist_kernel} ({head_name}; inner CG iterations: D p, D^dagger t, updates, "
+                      "2 grid-wide sums)",
+            "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 4), "iters_per_launch": it_per_launch,
+            "launches_per_solve": hi_.kernel_launches,
+            "share_of_solve": round(hi_.kernel_ms / hi_.device_ms, 3) if hi_.device_ms else None,
+            "timing": "CUDA events on the library stream around 5 launches of the kernel, each running the "
+                      "timed solve's mean inner iterations per launch",
+            "hbm_equivalent_gbs": round(hbm_equiv, 1),
+            "hbm_equivalent_note": "136 B per site and inner iteration (the CG iteration on D^dagger D as 17 "
+                                   "complex FP32 words per site: D p -> t: 4; D^dagger t -> Ap: 4; x, p, r, Ap "
+                                   "in, x, r out: 6; p = r + beta p: 3) over the kernel's time: the rate any "
+                                   "HBM-streaming iteration would need to match it; its fields stay on chip",
+            "hbm_equivalent_gbs_in_solve": round(hbm_equiv_solve, 1),
+            "hbm_peak_gbs": hbm_peak, "hbm_peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"}
+    cap = capture_for(persist_cand)
     if resident:
-        # the CG iteration's fields never leave the SM: the HBM-roofline fraction (algorithmic bytes
-        # over the HBM peak) above 1 says how much faster than any HBM-streaming iteration it runs;
-        # the binding on-chip resource is shared-memory bandwidth (measured wavefronts per iteration)
-        n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
-        iters_l = it_per_launch
-        smem_bytes = K_RESIDENT_SMEM_WAVEFRONTS * 128.0 * n_sm * iters_l
-        sm_clk = (clk.get("sm_mhz") or 2070.0) if isinstance(clk, dict) else 2070.0
-        smem_peak = 128.0 * sm_clk * 1e6 * n_sm / 1e9
-        smem_ach = smem_bytes / (k_ms * 1e-3) / 1e9 if k_ms > 0 else 0.0
-        onchip = {"resource": "shared memory", "achieved": round(smem_ach, 1), "peak": round(smem_peak, 1),
-                  "unit": "GB/s", "frac": round(smem_ach / smem_peak, 3),
-                  "note": "128 B x 6.56k wavefronts per SM and iteration (ncu) over the kernel's device time; peak "
-                          "128 B per clock per SM at the sampled SM clock"}
+        # the iteration's fields never leave the SM: the binding resource is shared memory.
+        # achieved = shared-memory wavefronts (128 B each, from the ncu capture of this kernel
+        # source) per launch over the launch's CUDA-event time; peak = the probe's measured rate
+        fresh = cap is not None and cap["fresh"]
+        smem_bytes = cap["smem_wavefronts_per_sm_iter"] * 128.0 * n_sm * it_per_launch if fresh else None
+        smem_ach = smem_bytes / (k_ms * 1e-3) / 1e9 if smem_bytes else None
+        roof.update({
+            "bound": "smem", "unit": "GB/s", "peak": round(smem_gbs.value, 1),
+            "achieved": round(smem_ach, 1) if smem_ach else None,
+            "frac": round(smem_ach / smem_gbs.value, 3) if smem_ach else None,
+            "peak_source": "measured in this run: glinalg_probe_smem_bandwidth (conflict-free 128-bit "
+                           "shared-memory loads, 2 x 1024 threads per SM)",
+            "achieved_note": "128 B x shared-memory wavefronts per SM and inner iteration (ncu capture of this "
+                             "kernel source, profiles/k_resident_fp32_1024.md) x SMs x iterations per launch, "
+                             "over the launch's CUDA-event time",
+            "traffic": cap["dram_bytes_per_launch"] if fresh else None,
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum of one launch (ncu capture of this "
+                            "kernel source): the entry load of the launch's state; it does not grow with "
+                            "its iterations",
+            "capture": {k: v for k, v in (cap or {}).items() if k != "fresh"} or None,
+            "capture_matches_source": fresh})
+    else:
+        fresh = cap is not None and cap["fresh"]
+        roof.update({"bound": "hbm", "unit": "GB/s", "achieved": round(hbm_equiv, 1), "peak": hbm_peak,
+                     "frac": round(hbm_equiv / hbm_peak, 3), "peak_source": roof["hbm_peak_source"],
+                     "traffic": cap["dram_bytes_per_launch"] if fresh else None,
+                     "capture_matches_source": fresh})
     line = {
         "metric": METRIC, "value": round(ms_max, 3), "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_max, 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (inner iterations; fp64 reliable updates and solution)",
         "data": "synthetic (seeded U(1) links and Gaussian source, std::mt19937 1337)",
-        "config": {"workload": "staggered normal-equation CG to FP64-true relres 1e-10, 1024x1024, m=0.01, x0=0",
-                   "lattice": [LX, LY], "mass": MASS, "tol": EPS, "variant": f"{head_name} inner + fp64 reliable updates",
-                   "parallelism": f"replicas x{world}", "l2": "flushed (512 MiB write) before every step",
-                   "inner_iters": hi.iter, "reliable_updates": hi.reliable_updates,
-                   "true_relres_fp64": relres, "fp64_gpu_ms": round(t64m, 3),
-                   "speedup_vs_fp64_gpu": round(t64m / ms, 2), "variants": variants},
-        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3),
-                     "traffic": K_RESIDENT_DRAM_BYTES if resident else K_PERSIST_DRAM_BYTES,
-                     "traffic_note": roof_note,
-                     "algorithmic_bytes": "136 B per site and inner iteration: the CG iteration on D^dagger D "
-                                          "as 17 complex FP32 words per site (D p -> t: 4; D^dagger t -> Ap: 4; "
-                                          "x, p, r, Ap in, x, r out: 6; p = r + beta p: 3), its traffic if its "
-                                          "fields streamed from memory",
-                     "onchip": onchip,
-                     "kernel": f"{persist_kernel} ({head_name}; inner CG iterations: D p, D^dagger t, updates, "
-                               "2 grid-wide sums)",
-                     "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 4),
-                     "iters_per_launch": it_per_launch, "launches_per_solve": hi_.kernel_launches,
-                     "share_of_solve": round(hi_.kernel_ms / hi_.device_ms, 3) if hi_.device_ms else None,
-                     "timing": "CUDA events on the library stream around 5 launches of the kernel, each running "
-                               "the timed solve's mean inner iterations per launch",
-                     "achieved_in_solve": round(achieved_solve, 1),
-                     "timing_in_solve": "device clock read by the kernel at entry and exit, summed over its "
-                                        "launches inside the timed solves",
-                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+        "config": CONFIG,
+        "variant": f"{head_name} inner + fp64 reliable updates",
+        "parallelism": f"replicas x{world}", "l2": "flushed (512 MiB write) before every step",
+        "results": {"inner_iters": hi.iter, "reliable_updates": hi.reliable_updates,
+                    "true_relres_fp64": relres,
+                    "err_vs_oracle": variants.get(head_name, {}).get("err_vs_oracle"),
+                    "oracle_iters": or_info["iter"] if or_info else None,
+                    "fp64_gpu_ms": round(t64m, 3), "speedup_vs_fp64_gpu": round(t64m / ms, 2),
+                    "variants": variants},
+        "roofline": roof,
         "e2e": {"value": round(e2e_ms, 3), "unit": "ms", "h2d_bytes_per_step": int(Uh.nbytes + bh.nbytes + xh.nbytes),
                 "d2h_bytes_per_step": int(xh.nbytes)},
         "gpu_launches": launches,

@@ -45,7 +45,9 @@ from ._capi import (GLINALG_PTR_DEVICE, GLINALG_PTR_HOST, PREC_BFLOAT, PREC_DOUB
                     load_library)
 
 __all__ = [
-    "lib", "load_library", "GlinalgError", "UnsupportedOperator",
+    "lib", "load_library", "GlinalgError", "UnsupportedOperator", "SolveTimeout",
+    "GLINALG_SOLVE_CONVERGED", "GLINALG_SOLVE_MAX_ITER", "GLINALG_SOLVE_BREAKDOWN",
+    "GLINALG_SOLVE_NONFINITE", "GLINALG_SOLVE_TIMEOUT",
     "StaggeredU1Op", "Stencil2D", "Operator", "InversionInfo", "InversionVerboseStruct",
     "VERB_PASS_THROUGH", "VERB_NONE", "VERB_SUMMARY", "VERB_RESTART_DETAIL", "VERB_DETAIL",
     "square_staggered_u1", "square_staggered_dagger_u1", "square_staggered_normal_u1",
@@ -79,6 +81,9 @@ __all__ = [
 ]
 
 VERB_PASS_THROUGH, VERB_NONE, VERB_SUMMARY, VERB_RESTART_DETAIL, VERB_DETAIL = -1, 0, 1, 2, 3
+# glinalg_solve_status (glinalg_info.status)
+(GLINALG_SOLVE_CONVERGED, GLINALG_SOLVE_MAX_ITER, GLINALG_SOLVE_BREAKDOWN, GLINALG_SOLVE_NONFINITE,
+ GLINALG_SOLVE_TIMEOUT) = 0, 1, 2, 3, 4
 
 KIND_STAGGERED, KIND_STAGGERED_DAGGER, KIND_STAGGERED_NORMAL, KIND_LAPLACE = 0, 1, 2, 3
 KIND_STENCIL, KIND_STENCIL_EO, KIND_STENCIL_OE = 4, 5, 6
@@ -414,14 +419,24 @@ def _resolve(matrix_vector, extra_info):
     return _op_for(kind, extra_info)
 
 
-def _params(precision=PREC_DOUBLE, delta=0.0, device=False):
+def _params(precision=PREC_DOUBLE, delta=0.0, device=False, wait_limit_us=0):
     p = SolverParams()
     p.precision, p.delta, p.flags = int(precision), float(delta), GLINALG_PTR_DEVICE if device else 0
+    p.wait_limit_us = int(wait_limit_us)
     return p
 
 
+class SolveTimeout(GlinalgError):
+    """A bounded device-side wait of the solve gave up (info.status == GLINALG_SOLVE_TIMEOUT);
+    the device is still usable.  `info` holds the solve's state when it stopped."""
+
+    def __init__(self, msg, info):
+        super().__init__(msg)
+        self.info = info
+
+
 def _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity, restart=None,
-           precision=PREC_DOUBLE, delta=0.0, extra_args=()):
+           precision=PREC_DOUBLE, delta=0.0, extra_args=(), wait_limit_us=0):
     op, temp = _resolve(matrix_vector, extra_info)
     try:
         pp, pn, pdev = _field_ptr(phi, writable=True)
@@ -437,8 +452,11 @@ def _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbos
             args.append(int(restart))
         args += list(extra_args)
         args += [C.byref(verb) if verb is not None else None,
-                 C.byref(_params(precision, delta, pdev)), C.byref(info)]
-        _capi.check(fn(*args), fn.__name__)
+                 C.byref(_params(precision, delta, pdev, wait_limit_us)), C.byref(info)]
+        st = fn(*args)
+        if st != 0 and info.status == GLINALG_SOLVE_TIMEOUT:
+            raise SolveTimeout(f"{fn.__name__}: {lib().glinalg_last_error().decode()}", InversionInfo(info))
+        _capi.check(st, fn.__name__)
         return InversionInfo(info)
     finally:
         if temp:
@@ -446,11 +464,13 @@ def _solve(fn, phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbos
 
 
 def minv_vector_cg(phi, phi0, size, max_iter, eps, matrix_vector, extra_info, verbosity=None,
-                   precision=PREC_DOUBLE, delta=0.0):
+                   precision=PREC_DOUBLE, delta=0.0, wait_limit_us=0):
     """minv_vector_cg (generic_cg.cpp:278).  precision != PREC_DOUBLE selects the mixed-precision
-    CG with FP64 reliable updates (Hermitian operators only)."""
+    CG with FP64 reliable updates (Hermitian operators only); wait_limit_us bounds its persistent
+    kernels' waits for other blocks (glinalg_solver_params.wait_limit_us; a wait that runs out
+    raises SolveTimeout)."""
     return _solve(lib().glinalg_cg, phi, phi0, size, max_iter, eps, matrix_vector, extra_info,
-                  verbosity, precision=precision, delta=delta)
+                  verbosity, precision=precision, delta=delta, wait_limit_us=wait_limit_us)
 
 
 def minv_vector_cg_restart(phi, phi0, size, max_iter, eps, restart_freq, matrix_vector, extra_info,

@@ -44,7 +44,7 @@ class InfoStruct(C.Structure):
 
 class SolverParams(C.Structure):
     _fields_ = [("precision", C.c_int), ("delta", C.c_double), ("flags", C.c_int),
-                ("reserved", C.c_int)]
+                ("wait_limit_us", C.c_int)]
 
 
 class PrecondStruct(C.Structure):
@@ -95,6 +95,7 @@ def _prototypes():
         "glinalg_mg_apply": (st, [vp, _dp, _dp, i]),
         "glinalg_tbprec_reconstruct": (st, [vp, _dp, _dp, _dp, i]),
         "glinalg_profile_persist_kernel": (st, [vp, i, i, i, _dp, _dp, P(i)]),
+        "glinalg_probe_smem_bandwidth": (st, [_dp, _dp]),
         "glinalg_staggered_normal_apply_noalloc": (st, [_dp, d, i, i, _dp, _dp, vp]),
         "glinalg_operator_create": (st, [P(OpDesc), P(vp)]),
         "glinalg_operator_destroy": (st, [vp]),

@@ -46,6 +46,7 @@ int precision_of(const glinalg_solver_params *p) { return p ? p->precision : GLI
 // The caller's reliable-update trigger, or 0: the mixed solvers then pick their per-precision
 // default (0.01 for FP32 iterates, 0.1 for 16-bit ones).
 double delta_of(const glinalg_solver_params *p) { return p && p->delta > 0 ? p->delta : 0.0; }
+int wait_limit_of(const glinalg_solver_params *p) { return p ? p->wait_limit_us : 0; }
 
 }  // namespace
 
@@ -59,7 +60,8 @@ extern "C" glinalg_status glinalg_cg(glinalg_operator op, double *phi, const dou
     const Verb v = Verb::from(verb);
     const int prec = precision_of(params);
     if (prec == GLINALG_PREC_DOUBLE) GL_TRY(cg_fp64(op, c.sg.x, c.sg.b, max_iter, eps, v, info, c.st));
-    else GL_TRY(cg_mixed(op, c.sg.x, c.sg.b, max_iter, eps, prec, delta_of(params), 0.0, v, info, c.st));
+    else GL_TRY(cg_mixed(op, c.sg.x, c.sg.b, max_iter, eps, prec, delta_of(params), 0.0, v, info, c.st,
+                         wait_limit_of(params)));
     return finish_call(c, phi, op->size);
 }
 

@@ -263,6 +263,11 @@ __global__ void __launch_bounds__(kRedThreads) k_bR2(BArgs<S, R, LK> a)
         s->done = 1;
         return;
     }
+    if (rt == 0.0) {  // exactly zero residual: x is exact (as k_mx_R2)
+        s->status = GLINALG_SOLVE_BREAKDOWN;
+        s->done = 1;
+        return;
+    }
     if (s->k >= s->max_iter) {
         s->status = GLINALG_SOLVE_MAX_ITER;
         s->done = 1;

@@ -205,6 +205,13 @@ k_mx_R2(double2 *__restrict__ rhi, const double2 *__restrict__ b, const double2 
             s->done = 1;
             return;
         }
+        if (rt == 0.0) {
+            // an exactly zero residual (a zero source with a zero guess): x is exact, and the
+            // rescale below would divide by zero; the FP64 CG stops the same way (<p, Ap> = 0)
+            s->status = GLINALG_SOLVE_BREAKDOWN;
+            s->done = 1;
+            return;
+        }
         if (s->k >= s->max_iter) {
             s->status = GLINALG_SOLVE_MAX_ITER;
             s->done = 1;
@@ -323,7 +330,12 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
           int lx, int ly, MxDev *s, GridSync *gs, double *partA, double *partB)
 {
     __shared__ double sm[33];
-    if (s->done || s->reliable) return;
+    __shared__ int skip;
+    // one read of the solve state per block, so that a block never splits here: block 0 of a
+    // launch whose waits ran out may set s->done while other blocks are still starting
+    if (threadIdx.x == 0 && threadIdx.y == 0) skip = s->done || s->reliable;
+    __syncthreads();
+    if (skip) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
     const int lane = threadIdx.x, warp = threadIdx.y;
@@ -335,6 +347,7 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
     const int max_iter = s->max_iter;
     int j = 0, status = -1;
     bool reliable = false;
+    const long long lim = peer_wait_ns(s);
     for (;;) {
         const S *pold = (j & 1) ? p1 : p0;
         S *pnew = (j & 1) ? p0 : p1;
@@ -345,7 +358,7 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
             acc += tile_A<S, R, LK, NY, true, true>(r, pold, pnew, t, H, fb, mass, sigma, lx, ly, lane,
                                                     (tile % ntx) * 32 + lane, true, (tile / ntx) * NY);
         block_partial(acc, partA, sm);
-        if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
+        if (!grid_sync(gs, nb, lim)) { status = GLINALG_SOLVE_TIMEOUT; break; }
         const double pAp = grid_total(partA, nb, sm);
         if (!(pAp > 0.0) || !isfinite(pAp)) {
             status = pAp == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
@@ -358,7 +371,7 @@ k_persist(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, float
             acc += tile_B<S, R, LK, NY, true, true>(t, pnew, r, xlo, H, alpha, mass, sigma, lx, ly, lane,
                                                     (tile % ntx) * 32 + lane, true, (tile / ntx) * NY);
         block_partial(acc, partB, sm);
-        if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
+        if (!grid_sync(gs, nb, lim)) { status = GLINALG_SOLVE_TIMEOUT; break; }
         rn = grid_total(partB, nb, sm);
         j++;
         k++;
@@ -841,7 +854,8 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
 template <class S, class R, class LK>
 static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b,
                                 int max_iter, double eps, double delta, double sigma,
-                                glinalg_info *info, cudaStream_t st, const char *name, int variant)
+                                glinalg_info *info, cudaStream_t st, const char *name, int variant,
+                                int wait_limit_us)
 {
     const long n = op->size;
     const int lx = op->lx, ly = op->ly;
@@ -904,6 +918,7 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     h.sigma = sigma;
     h.max_iter = max_iter;
     h.scale = 1.0;
+    h.wait_ns = wait_limit_us > 0 ? 1000LL * wait_limit_us : (wait_limit_us < 0 ? -1LL : 0LL);
     GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
 
     EventTimer tm;
@@ -1061,7 +1076,14 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     if (ex) cudaGraphExecDestroy(ex);
     if (g) cudaGraphDestroy(g);
     if (h.status == GLINALG_SOLVE_TIMEOUT) {
-        set_last_error("a grid-wide barrier of the persistent CG kernel timed out");
+        // the kernel gave up a bounded wait for other blocks and returned; the context is intact
+        info->resSq = 0.0;
+        info->iter = h.k;
+        info->success = 0;
+        info->ops_count = h.k + h.n_reliable;
+        info->status = GLINALG_SOLVE_TIMEOUT;
+        info->reliable_updates = h.n_reliable;
+        set_last_error("a bounded wait of the persistent CG kernel for other blocks ran out");
         return GLINALG_ERROR_INTERNAL;
     }
     info->resSq = h.rsq_true;
@@ -1092,7 +1114,7 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
 // zero, as square_staggered_eoprec_prepare makes them; they are not read).
 static glinalg_status cg_mixed_even(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
                                     double eps, int precision, double delta, double sigma, const Verb &verb,
-                                    glinalg_info *info, cudaStream_t st)
+                                    glinalg_info *info, cudaStream_t st, int wait_limit_us)
 {
     Scratch sc(st);
     double2 *be, *xe;
@@ -1110,7 +1132,8 @@ static glinalg_status cg_mixed_even(const glinalg_operator_s *op, double2 *x, co
     view.size = op->size;
     view.device = op->device;
     view.U = op->U;
-    const glinalg_status s = cg_mixed(&view, xe, be, max_iter, eps, precision, delta, sigma, verb, info, st);
+    const glinalg_status s =
+        cg_mixed(&view, xe, be, max_iter, eps, precision, delta, sigma, verb, info, st, wait_limit_us);
     view.U = nullptr;
     GL_TRY(s);
     return launch_even_into(op, x, xe, st);
@@ -1118,10 +1141,10 @@ static glinalg_status cg_mixed_even(const glinalg_operator_s *op, double2 *x, co
 
 glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
                         double eps, int precision, double delta, double sigma, const Verb &verb,
-                        glinalg_info *info, cudaStream_t st)
+                        glinalg_info *info, cudaStream_t st, int wait_limit_us)
 {
     if (op->kind == GLINALG_OP_STAGGERED_M2MDEODOE)
-        return cg_mixed_even(op, x, b, max_iter, eps, precision, delta, sigma, verb, info, st);
+        return cg_mixed_even(op, x, b, max_iter, eps, precision, delta, sigma, verb, info, st, wait_limit_us);
     if (!(op->kind == GLINALG_OP_STAGGERED_NORMAL || op->kind == GLINALG_OP_LAPLACE)) {
         set_last_error("mixed-precision CG needs the staggered normal operator, m^2 - D_eo D_oe or the gauge "
                        "Laplacian");
@@ -1134,13 +1157,13 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
     glinalg_status s;
     switch (precision) {
     case GLINALG_PREC_SINGLE:
-        s = run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32", 1);
+        s = run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32", 1, wait_limit_us);
         break;
     case GLINALG_PREC_HALF:
-        s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16", 2);
+        s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16", 2, wait_limit_us);
         break;
     case GLINALG_PREC_BFLOAT:
-        s = run_mixed<__nv_bfloat162, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16", 3);
+        s = run_mixed<__nv_bfloat162, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16", 3, wait_limit_us);
         break;
     default: set_last_error("unknown precision"); return GLINALG_ERROR_INVALID_VALUE;
     }

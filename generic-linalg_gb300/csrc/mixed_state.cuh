@@ -26,6 +26,7 @@ struct MxDev {
     long long inner_ns;  // device time spent in the persistent inner-loop kernel
     int inner_iters;     // iterations it ran
     int inner_launches;
+    long long wait_ns;   // bound on each wait for other blocks: 0 = the default, < 0 = none
 };
 
 __device__ __forceinline__ void mx_stop_inner(cudaGraphConditionalHandle cond, int use_cond)
@@ -93,10 +94,19 @@ __device__ __forceinline__ long long gtimer()
 // GLINALG_SOLVE_TIMEOUT) instead of spinning on.
 constexpr long long kBarrierTimeoutNs = 2000000000LL;
 
+// The bound, in ns, on a persistent kernel's waits for other blocks (grid barriers, mailbox
+// polls) during this solve: MxDev::wait_ns if positive, the default if 0, and none at all (give
+// up at the first check that finds the data missing) if negative.  Waits of a block on its own
+// asynchronous copies keep the fixed kBarrierTimeoutNs.
+__device__ __forceinline__ long long peer_wait_ns(const MxDev *s)
+{
+    return s->wait_ns > 0 ? s->wait_ns : (s->wait_ns == 0 ? kBarrierTimeoutNs : 0LL);
+}
+
 // Grid-wide barrier for a co-resident grid (generation counter; acquire/release atomics at
 // device scope).  Returns false in every thread of the block once any block has given up
 // waiting.
-__device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
+__device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks, long long lim_ns = kBarrierTimeoutNs)
 {
     __shared__ int ok;
     __syncthreads();
@@ -113,7 +123,7 @@ __device__ __forceinline__ bool grid_sync(GridSync *g, unsigned nblocks)
             const long long t0 = gtimer();
             while (gen.load(cuda::memory_order_acquire) == my) {
                 if (err.load(cuda::memory_order_relaxed)) { good = 0; break; }
-                if (gtimer() - t0 > kBarrierTimeoutNs) {
+                if (gtimer() - t0 > lim_ns) {
                     err.store(1, cuda::memory_order_relaxed);
                     good = 0;
                     break;

@@ -13,9 +13,11 @@
 // The array (kNoAllocSites complex<double> values, 4 MiB) lives in this library's device
 // image: every GPU that loads the library holds it until the process exits.  Its device
 // address is looked up once per device (cudaGetSymbolAddress), on the first call made with
-// that device current; make that first call before any stream capture.  All calls share the
-// one array: calls whose work overlaps on the GPU (different streams, or different host
-// threads) race on it and must be serialised by the caller.  The array keeps the previous
+// that device current; make that first call before any stream capture.  The call only
+// enqueues its two kernels on the caller's stream and returns; lhs is complete once that
+// stream has reached them.  All calls share the one array: calls whose work overlaps on the
+// GPU (different streams, or different host threads) race on it and must be serialised by
+// the caller.  The array keeps the previous
 // call's contents; this operator overwrites every entry it reads before reading it, so
 // nothing needs clearing.
 
@@ -98,7 +100,8 @@ extern "C" glinalg_status glinalg_staggered_normal_apply_noalloc(const double *l
                                     nullptr);
     k_staggered<<<grid, nt, 0, st>>>((double2 *)lhs, scratch, (const double2 *)links, mass, lx, ly, -1.0,
                                     nullptr);
+    // no synchronisation here: the work is ordered on the caller's stream, and the caller waits
+    // on that stream (or an event recorded after the call) before reading lhs
     GL_CUDA(cudaGetLastError());
-    GL_CUDA(cudaStreamSynchronize(st));
     return GLINALG_SUCCESS;
 }

@@ -76,9 +76,9 @@ glinalg_status flex_restart_fp64(int mode, const glinalg_operator_s *op, double2
                                  const Verb &verb, glinalg_info *info, cudaStream_t st);
 
 // Mixed-precision CG with FP64 reliable updates (cg_mixed.cu).  sigma: diagonal shift added to
-// the operator (0 for the plain system).
+// the operator (0 for the plain system).  wait_limit_us: glinalg_solver_params::wait_limit_us.
 glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
                         double eps, int precision, double delta, double sigma, const Verb &verb,
-                        glinalg_info *info, cudaStream_t st);
+                        glinalg_info *info, cudaStream_t st, int wait_limit_us = 0);
 
 }  // namespace glinalg

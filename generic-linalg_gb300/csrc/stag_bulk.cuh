@@ -305,7 +305,12 @@ k_persist_bulk(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, 
     __shared__ double sm[33];
     __shared__ __align__(8) uint64_t bars[kStages];
     __shared__ int bad;
-    if (s->done || s->reliable) return;
+    // one read of the solve state per block (bad doubles as the flag), so that a block never
+    // splits here: block 0 of a launch whose waits ran out may set s->done while other blocks
+    // are still starting
+    if (threadIdx.x == 0 && threadIdx.y == 0) bad = s->done || s->reliable;
+    __syncthreads();
+    if (bad) return;
     const long long t_start = gtimer();
     const unsigned nb = gridDim.x;
     const int tid = threadIdx.y * 32 + threadIdx.x;
@@ -368,7 +373,7 @@ k_persist_bulk(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, 
         float acc = 0.f;
         if (!phase(0, pold, pnew, (float)beta, 0.f, acc)) { status = GLINALG_SOLVE_TIMEOUT; break; }
         block_partial(acc, partA, sm);
-        if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
+        if (!grid_sync(gs, nb, peer_wait_ns(s))) { status = GLINALG_SOLVE_TIMEOUT; break; }
         const double pAp = grid_total(partA, nb, sm);
         if (!(pAp > 0.0) || !isfinite(pAp)) {
             status = pAp == 0.0 ? GLINALG_SOLVE_BREAKDOWN : GLINALG_SOLVE_NONFINITE;
@@ -378,7 +383,7 @@ k_persist_bulk(const LK *__restrict__ H, R *r, S *p0, S *p1, S *t, float2 *xlo, 
         acc = 0.f;
         if (!phase(1, pold, pnew, 0.f, alpha, acc)) { status = GLINALG_SOLVE_TIMEOUT; break; }
         block_partial(acc, partB, sm);
-        if (!grid_sync(gs, nb)) { status = GLINALG_SOLVE_TIMEOUT; break; }
+        if (!grid_sync(gs, nb, peer_wait_ns(s))) { status = GLINALG_SOLVE_TIMEOUT; break; }
         rn = grid_total(partB, nb, sm);
         j++;
         k++;

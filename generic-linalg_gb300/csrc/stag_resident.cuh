@@ -269,12 +269,21 @@ __device__ __forceinline__ void hop_rows_tm(const float2 *__restrict__ F, unsign
 // that write only after the grid-wide sum in between, which every block contributes to only
 // after it has read the slot's previous contents (k_resident posts border words from its
 // update passes, which come after the wait for that sum); partial-sum words alternate between two
-// arrays by phase parity for the same reason.  Every wait is bounded (kSpinCycles); a wait
-// that runs out raises the error word, which ends the waits of every other block too.
+// arrays by phase parity for the same reason.  Every wait is bounded (kSpinCycles by default,
+// the caller's limit when the solve sets one: peer_wait_cycles); a wait that runs out raises
+// the error word, which ends the waits of every other block too.
 
 constexpr int kMaxBlocks = 256;  // one rectangle per SM: above any GB300 SM count
 constexpr int kPerLane = kMaxBlocks / 32;
 constexpr long long kSpinCycles = 4000000000LL;  // about 2 s at GB300 clocks
+
+// The solve's bound on a wait, in SM clock cycles (2 per ns: GB300's SM clock is at most
+// 2.07 GHz, so the wait lasts at least the requested time): MxDev::wait_ns > 0 converted, the
+// default for 0, and 0 (give up at the first poll that finds the data missing) for < 0.
+__device__ __forceinline__ long long peer_wait_cycles(const MxDev *s)
+{
+    return s->wait_ns > 0 ? 2 * s->wait_ns : (s->wait_ns == 0 ? kSpinCycles : 0LL);
+}
 
 struct PhaseFlags {
     unsigned long long w[2][kMaxBlocks];  // partial-sum words by phase parity
@@ -406,14 +415,15 @@ __device__ __forceinline__ int ring_source(int k, int ty, int tyb, int nslot, in
 
 // Polls a mailbox slot until both words carry epoch e; returns the value, or sets *err (and the
 // error word) when the wait runs out or another block has raised the error word.
-__device__ __forceinline__ float2 poll_slot(const unsigned long long *p, unsigned e, PhaseFlags *pf, int *err)
+__device__ __forceinline__ float2 poll_slot(const unsigned long long *p, unsigned e, PhaseFlags *pf, int *err,
+                                           long long lim)
 {
     unsigned long long a, b;
     const long long t0 = clock64();
     for (unsigned n = 1;; n++) {
         ld_relaxed_2u64(p, a, b);
         if ((unsigned)(a >> 32) == e && (unsigned)(b >> 32) == e) break;
-        if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
+        if (((n & 63) == 0 || lim == 0) && (clock64() - t0 > lim || ld_relaxed_s32(&pf->error) != 0)) {
             atomicExch(&pf->error, 1);
             *err = 1;
             break;
@@ -441,14 +451,14 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &c)
 // Called by threads 0 .. nb-1: thread b waits until block b's word carries epoch e and returns
 // its partial (0 when the wait runs out, which sets *err).  One word per thread keeps the
 // poll's registers few (they count for every thread of the block).
-__device__ __forceinline__ float poll_partial(PhaseFlags *pf, unsigned e, int b, int *err)
+__device__ __forceinline__ float poll_partial(PhaseFlags *pf, unsigned e, int b, int *err, long long lim)
 {
     const unsigned long long *w = pf->w[e & 1] + b;
     const long long t0 = clock64();
     for (unsigned n = 1;; n++) {
         const unsigned long long v = ld_relaxed_u64(w);
         if ((unsigned)(v >> 32) == e) return __uint_as_float((unsigned)v);
-        if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
+        if (((n & 63) == 0 || lim == 0) && (clock64() - t0 > lim || ld_relaxed_s32(&pf->error) != 0)) {
             atomicExch(&pf->error, 1);
             *err = 1;
             return 0.f;
@@ -587,7 +597,8 @@ __device__ __forceinline__ void publish_border(unsigned e, const float2 *F, unsi
 }
 
 // Thread b waits until block b's four partial words carry epoch e and stages them.
-__device__ __forceinline__ void poll_partial4(PhaseFlags *pf, unsigned e, int b, float4 *sm_part4, int *err)
+__device__ __forceinline__ void poll_partial4(PhaseFlags *pf, unsigned e, int b, float4 *sm_part4, int *err,
+                                              long long lim)
 {
     const unsigned long long *w = pf->w4[(e >> 1) & 1][b];
     const long long t0 = clock64();
@@ -601,7 +612,7 @@ __device__ __forceinline__ void poll_partial4(PhaseFlags *pf, unsigned e, int b,
                                       __uint_as_float((unsigned)a2), __uint_as_float((unsigned)a3));
             return;
         }
-        if ((n & 63) == 0 && (clock64() - t0 > kSpinCycles || ld_relaxed_s32(&pf->error) != 0)) {
+        if (((n & 63) == 0 || lim == 0) && (clock64() - t0 > lim || ld_relaxed_s32(&pf->error) != 0)) {
             atomicExch(&pf->error, 1);
             *err = 1;
             sm_part4[b] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -706,8 +717,13 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     constexpr bool XREG = XM == kXReg, XTM = XM == kXTmem || XM == kXTmemL, LTM = XM == kXTmemL;
     constexpr unsigned kTmemCols = LTM ? 512u : res_tmem_cols(NY, WY);
     static_assert(!LTM || (4 * NY * WY <= 256 && 2 * NY * WY <= 128), "tensor-memory layout");
-    if (s->done || s->reliable) return;
+    // one read of the solve state per block, so that a block never splits here: block 0 of a
+    // launch whose waits ran out may set s->done while other blocks are still starting
+    if (threadIdx.x == 0 && threadIdx.y == 0) sm_ctl = (s->done || s->reliable) ? kResStop : kResGo;
+    __syncthreads();
+    if (sm_ctl != kResGo) return;
     const long long t_start = gtimer();
+    const long long lim = peer_wait_cycles(s);
     const unsigned nb = gridDim.x;
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int tid = warp * 32 + lane;
@@ -849,7 +865,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
             }
         }
         if (!first) {
-            stage_partials(tid < (int)nb ? poll_partial(pf, ep, tid, &sm_err) : 0.f, nb, sm_hl);
+            stage_partials(tid < (int)nb ? poll_partial(pf, ep, tid, &sm_err, lim) : 0.f, nb, sm_hl);
             __syncthreads();
             if (tid == 0) {
                 const float tot = total_partials(sm_hl, nb);
@@ -886,7 +902,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         float acc = pass_A<NY>(R.T, Rr, tmp, pv, fb, sigma, (yb + 1) * kPW + xl + 1, nrow, mbT, eA, xl, yb, tyb);
         post_columns(mbT, eA, R.T, warp % kWX, yb, nrow, ty);
         publish_sum<NW>(acc, pf, eA, sm_w);
-        if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err);
+        if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err, lim);
         __syncthreads();
         // ---- B: Ap = D^dagger t + sigma p' (needs only the ring of t), then alpha from the
         // total of A; x_lo += alpha p', r -= alpha Ap
@@ -905,7 +921,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
                 else if (nrow > 0) hop_rows<NY, false>(R.T, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
             }
         }
-        stage_partials(tid < (int)nb ? poll_partial(pf, eA, tid, &sm_err) : 0.f, nb, sm_hl);
+        stage_partials(tid < (int)nb ? poll_partial(pf, eA, tid, &sm_err, lim) : 0.f, nb, sm_hl);
         __syncthreads();
         if (tid == 0) {
             const float tot = total_partials(sm_hl, nb);
@@ -948,7 +964,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         }
         post_columns(mbR, eB, Rr, warp % kWX, yb, nrow, ty);
         publish_sum<NW>(acc, pf, eB, sm_w);
-        if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err);
+        if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err, lim);
         __syncthreads();
     }
     // ---- exit: the rectangle's r, x_lo and direction back to global memory (direction in p0)
@@ -1033,8 +1049,13 @@ k_resident1(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, fl
     __shared__ int sm_ctl, sm_err;
     __shared__ ResScalars sc;
     __shared__ float4 sm_part4[kMaxBlocks1];
-    if (s->done || s->reliable) return;
+    // one read of the solve state per block, so that a block never splits here: block 0 of a
+    // launch whose waits ran out may set s->done while other blocks are still starting
+    if (threadIdx.x == 0 && threadIdx.y == 0) sm_ctl = (s->done || s->reliable) ? kResStop : kResGo;
+    __syncthreads();
+    if (sm_ctl != kResGo) return;
     const long long t_start = gtimer();
+    const long long lim = peer_wait_cycles(s);
     const unsigned nb = gridDim.x;
     const int lane = threadIdx.x, warp = threadIdx.y;
     const int tid = warp * 32 + lane;
@@ -1173,7 +1194,7 @@ k_resident1(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, fl
             }
         }
         publish4<NW>(acc, pf, eA, sm_w4, Ru, Mu, nborder, bpos, bslot);
-        if (has_ring) Ru[rslot] = poll_slot(Mu + rsrc, eA, pf, &sm_err);
+        if (has_ring) Ru[rslot] = poll_slot(Mu + rsrc, eA, pf, &sm_err, lim);
         __syncthreads();
         // ---- B: w = D^dagger u + sigma r, then the totals, the scalars and the updates
         {
@@ -1183,7 +1204,7 @@ k_resident1(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, fl
             if (nrow == NY) hop_rows<NY, true>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
             else if (nrow > 0) hop_rows<NY, false>(Ru, R.HX, R.HY, R.HxL, R.HyB, xl, yb, nrow, body);
         }
-        if (tid < (int)nb) poll_partial4(pf, eA, tid, sm_part4, &sm_err);
+        if (tid < (int)nb) poll_partial4(pf, eA, tid, sm_part4, &sm_err, lim);
         __syncthreads();
         if (warp == 0) {
             const float4 tot = sum_partials4(sm_part4, nb);
@@ -1243,7 +1264,7 @@ k_resident1(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, fl
         }
         __syncthreads();
         publish_border(eB, Rr, Mr, nborder, bpos, bslot);
-        if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err);
+        if (has_ring) Rr[rslot] = poll_slot(Mr + rsrc, eB, pf, &sm_err, lim);
         __syncthreads();
     }
     // ---- exit: r, the direction (to p0) back to global memory; x_lo is already there

@@ -51,7 +51,7 @@ typedef enum glinalg_solve_status {
     GLINALG_SOLVE_BREAKDOWN = 2,  /* a recurrence denominator was exactly zero */
     GLINALG_SOLVE_NONFINITE = 3,  /* NaN or Inf appeared in a residual norm */
     GLINALG_SOLVE_TIMEOUT = 4     /* a bounded device-side wait gave up (the call reports
-                                     GLINALG_ERROR_INTERNAL) */
+                                     GLINALG_ERROR_INTERNAL; info is filled) */
 } glinalg_solve_status;
 
 /* Operator kinds.  Each names the reference callback it replaces. */
@@ -146,7 +146,13 @@ typedef struct glinalg_solver_params {
     double delta;      /* reliable-update trigger: recompute when |r| < delta * max|r| (0 -> 0.01
                           for SINGLE, 0.1 for HALF and BFLOAT) */
     int flags;         /* GLINALG_PTR_DEVICE: phi / phi0 are device pointers */
-    int reserved;
+    int wait_limit_us; /* bound on each wait of the mixed CG's persistent kernels for other
+                          blocks (grid barriers, border and partial-sum polls), in microseconds:
+                          0 = the default (2 s); < 0 = give up at the first check that finds the
+                          data missing (a diagnostic).  A wait that runs out ends the kernel
+                          cleanly: the call returns GLINALG_ERROR_INTERNAL with info->status
+                          GLINALG_SOLVE_TIMEOUT, and the device stays usable.  No counterpart
+                          in the reference (its solvers never wait on a device). */
 } glinalg_solver_params;
 
 /* ---- library ---- */
@@ -456,8 +462,9 @@ glinalg_status glinalg_staggered_action_grad(glinalg_operator op, const double *
  * framework's allocator or memory budget, a latency-critical loop that cannot afford
  * cudaMalloc / cudaFree): lhs = D^dagger D rhs, the staggered normal operator of
  * square_staggered_normal_u1, on caller-provided DEVICE buffers (links: 2*lx*ly complex,
- * lhs / rhs: lx*ly complex), issued on `stream` (a cudaStream_t, NULL for the legacy default
- * stream) and finished before return.  The intermediate D rhs lives in a fixed array inside
+ * lhs / rhs: lx*ly complex), enqueued on `stream` (a cudaStream_t, NULL for the legacy default
+ * stream); the call returns without waiting, and lhs is complete once that stream has reached
+ * the work (synchronise the stream before reading it on the host).  The intermediate D rhs lives in a fixed array inside
  * the library (GLINALG_NOALLOC_MAX_SITES complex values, 4 MiB, held on every GPU that loads
  * the library until exit); lattices with more sites are rejected with
  * GLINALG_ERROR_INVALID_VALUE.  The first call on a device looks up that array's address;
@@ -483,6 +490,11 @@ glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int precision,
  * Staggered normal operator only. */
 glinalg_status glinalg_profile_persist_kernel(glinalg_operator op, int precision, int n_launch, int n_iter,
                                               double *ms, double *bytes, int *cand);
+/* Measured shared-memory bandwidth of the current device: 2 blocks of 1024 threads per SM
+ * stream conflict-free 128-bit loads from shared memory (5 timed launches, CUDA events on the
+ * library stream).  gbs: bytes loaded per second / 1e9; ms (may be NULL): one launch.  No
+ * counterpart in the reference: the denominator of the on-chip roofline of the resident CG. */
+glinalg_status glinalg_probe_smem_bandwidth(double *gbs, double *ms);
 /* Tile shape the autotuner picked for op's lattice and precision (an index into the
  * library's candidate list: 0 = 32x16, 1 = 32x32, 2 = 32x32 (4 rows of 8), 3 = 32x32
  * (16 rows of 2) sites per block), or -1 if no mixed solve has run on this lattice yet. */

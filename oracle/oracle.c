@@ -14,6 +14,8 @@
 #include <stdlib.h>
 #include <stdio.h>
 #include <string.h>
+#include <pthread.h>
+#include <stdatomic.h>
 
 typedef double _Complex cplx;
 
@@ -22,19 +24,232 @@ typedef double _Complex cplx;
 
 static inline cplx mk(double re, double im) { cplx z; __real__ z = re; __imag__ z = im; return z; }
 
+/* ---------------------------------------------------------------- site-loop threads
+ *
+ * The reference is single-threaded.  Its site loops (operator applications, axpy-type
+ * updates) compute every site independently, so spreading them over threads changes no bit
+ * of any result.  Its reductions (dot, norm) are serial left-to-right sums; they stay serial,
+ * in that order, on the calling thread.  par_ordered() overlaps such a sum with the parallel
+ * pass that produces its terms: workers take fixed-size chunks in increasing order, and the
+ * calling thread adds up each chunk, in order, once it is finished.  orc_set_threads(n) sets
+ * the number of threads (default 1: the plain serial oracle).  A child process made by fork()
+ * starts with no workers and recreates them on its first parallel loop. */
+
+typedef void (*range_fn)(void *ctx, long lo, long hi);
+typedef void (*task_fn)(void *ctx, int id, int parts);
+
+#define ORC_MAX_THREADS 256
+static struct {
+    pthread_mutex_t mu;
+    pthread_cond_t go, done;
+    int nthreads;        /* threads used by a loop, the caller included */
+    int nworkers;        /* workers started */
+    unsigned long gen;   /* bumped per task */
+    int pending;         /* workers still running the current task */
+    task_fn fn;
+    void *ctx;
+    int parts;
+} pool = {PTHREAD_MUTEX_INITIALIZER, PTHREAD_COND_INITIALIZER, PTHREAD_COND_INITIALIZER, 1, 0, 0, 0,
+          NULL, NULL, 1};
+
+/* generation current when worker j was started (under the pool lock, before the task that
+ * started it bumped the generation), so a worker never misses that task */
+static unsigned long worker_start_gen[ORC_MAX_THREADS];
+
+static void *pool_worker(void *arg)
+{
+    int id = (int)(long)arg; /* 1 .. nworkers */
+    pthread_mutex_lock(&pool.mu);
+    unsigned long seen = worker_start_gen[id];
+    for (;;) {
+        while (pool.gen == seen) pthread_cond_wait(&pool.go, &pool.mu);
+        seen = pool.gen;
+        task_fn fn = pool.fn;
+        void *ctx = pool.ctx;
+        int parts = pool.parts;
+        pthread_mutex_unlock(&pool.mu);
+        if (id < parts) fn(ctx, id, parts);
+        pthread_mutex_lock(&pool.mu);
+        if (--pool.pending == 0) pthread_cond_signal(&pool.done);
+    }
+    return NULL;
+}
+
+static void pool_after_fork_child(void)
+{
+    pthread_mutex_init(&pool.mu, NULL);
+    pthread_cond_init(&pool.go, NULL);
+    pthread_cond_init(&pool.done, NULL);
+    pool.nworkers = 0;
+    pool.pending = 0;
+}
+
+void orc_set_threads(int n)
+{
+    static int atfork_done = 0;
+    if (n < 1) n = 1;
+    if (n > ORC_MAX_THREADS) n = ORC_MAX_THREADS;
+    pthread_mutex_lock(&pool.mu);
+    if (!atfork_done) {
+        pthread_atfork(NULL, NULL, pool_after_fork_child);
+        atfork_done = 1;
+    }
+    pool.nthreads = n;
+    pthread_mutex_unlock(&pool.mu);
+}
+
+int orc_get_threads(void) { return pool.nthreads; }
+
+/* Starts fn(ctx, id, parts) on workers id = 1 .. parts-1 and returns parts (the caller is
+ * part 0 and runs its own share); pool_wait() then waits for the workers. */
+static int pool_start(task_fn fn, void *ctx)
+{
+    int t = pool.nthreads;
+    pthread_mutex_lock(&pool.mu);
+    while (pool.nworkers < t - 1) {
+        pthread_t th;
+        worker_start_gen[pool.nworkers + 1] = pool.gen;
+        if (pthread_create(&th, NULL, pool_worker, (void *)(long)(pool.nworkers + 1)) != 0) break;
+        pthread_detach(th);
+        pool.nworkers++;
+    }
+    int parts = pool.nworkers + 1 < t ? pool.nworkers + 1 : t;
+    pool.fn = fn;
+    pool.ctx = ctx;
+    pool.parts = parts;
+    pool.pending = pool.nworkers;
+    pool.gen++;
+    pthread_cond_broadcast(&pool.go);
+    pthread_mutex_unlock(&pool.mu);
+    return parts;
+}
+
+static void pool_wait(void)
+{
+    pthread_mutex_lock(&pool.mu);
+    while (pool.pending > 0) pthread_cond_wait(&pool.done, &pool.mu);
+    pthread_mutex_unlock(&pool.mu);
+}
+
+typedef struct {
+    long n;
+    range_fn fn;
+    void *ctx;
+} range_task_args;
+
+static void range_task(void *ctx, int id, int parts)
+{
+    const range_task_args *r = (const range_task_args *)ctx;
+    long lo = r->n * id / parts, hi = r->n * (id + 1) / parts;
+    if (hi > lo) r->fn(r->ctx, lo, hi);
+}
+
+/* fn(ctx, lo, hi) over [0, n) split into contiguous ranges, one per thread. */
+static void par_range(long n, range_fn fn, void *ctx)
+{
+    if (pool.nthreads <= 1 || n < 4096) {
+        fn(ctx, 0, n);
+        return;
+    }
+    range_task_args r = {n, fn, ctx};
+    int parts = pool_start(range_task, &r);
+    range_task(&r, 0, parts);
+    pool_wait();
+}
+
+#define ORC_CHUNK 8192L
+#define ORC_MAX_CHUNKS 65536L
+static _Atomic unsigned long chunk_done[ORC_MAX_CHUNKS];
+static unsigned long ordered_gen = 0;
+
+typedef struct {
+    long n, chunk, nch;
+    range_fn work;
+    void *ctx;
+    _Atomic long next;
+    unsigned long gen;
+} ordered_args;
+
+static void ordered_task(void *ctx, int id, int parts)
+{
+    ordered_args *o = (ordered_args *)ctx;
+    (void)id;
+    (void)parts;
+    for (;;) {
+        long c = atomic_fetch_add_explicit(&o->next, 1, memory_order_relaxed);
+        if (c >= o->nch) break;
+        long lo = c * o->chunk, hi = lo + o->chunk < o->n ? lo + o->chunk : o->n;
+        o->work(o->ctx, lo, hi);
+        atomic_store_explicit(&chunk_done[c], o->gen, memory_order_release);
+    }
+}
+
+/* work(ctx, lo, hi) over [0, n) on the workers, chunk by chunk in increasing order, while the
+ * calling thread runs sum(ctx, lo, hi) over the same chunks strictly in order, each once its
+ * work is finished.  With one thread: work then sum per chunk, in order. */
+static void par_ordered(long n, range_fn work, range_fn sum, void *ctx)
+{
+    long chunk = ORC_CHUNK;
+    while ((n + chunk - 1) / chunk > ORC_MAX_CHUNKS) chunk *= 2;
+    long nch = (n + chunk - 1) / chunk;
+    if (pool.nthreads <= 1 || nch < 2) {
+        for (long c = 0; c < nch; c++) {
+            long lo = c * chunk, hi = lo + chunk < n ? lo + chunk : n;
+            work(ctx, lo, hi);
+            sum(ctx, lo, hi);
+        }
+        return;
+    }
+    ordered_args o;
+    o.n = n;
+    o.chunk = chunk;
+    o.nch = nch;
+    o.work = work;
+    o.ctx = ctx;
+    atomic_init(&o.next, 0);
+    o.gen = ++ordered_gen;
+    pool_start(ordered_task, &o);
+    for (long c = 0; c < nch; c++) {
+        long lo = c * chunk, hi = lo + chunk < n ? lo + chunk : n;
+        while (atomic_load_explicit(&chunk_done[c], memory_order_acquire) != o.gen) {
+            /* a worker holds this chunk; take an unclaimed one meanwhile if any is left */
+            long d = atomic_fetch_add_explicit(&o.next, 1, memory_order_relaxed);
+            if (d < nch) {
+                long dlo = d * chunk, dhi = dlo + chunk < n ? dlo + chunk : n;
+                work(ctx, dlo, dhi);
+                atomic_store_explicit(&chunk_done[d], o.gen, memory_order_release);
+            }
+        }
+        sum(ctx, lo, hi);
+    }
+    pool_wait();
+}
+
 /* ---------------------------------------------------------------- operators */
 
 /* operator_utils/operators.cpp:184-239 (square_staggered_u1): hopping with eta_x = 1,
  * eta_y = (-1)^x, then 0.5 * sum, then + mass*psi.  sign = +1 for D, -1 for D^dagger
  * (operators.cpp:372-441 flips every hopping sign and keeps the mass). */
-static void staggered_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass, int lx,
-                            int ly, double sign)
+typedef struct {
+    cplx *lhs;
+    const cplx *rhs, *U;
+    double mass, sign;
+    int lx, ly;
+} site_args;
+
+static void staggered_range(void *ctx, long lo, long hi)
 {
-    for (long i = 0; i < (long)lx * ly; i++) {
-        int x = (int)(i % lx), y = (int)(i / lx);
+    const site_args *a = (const site_args *)ctx;
+    cplx *lhs = a->lhs;
+    const cplx *rhs = a->rhs, *U = a->U;
+    const double mass = a->mass, sign = a->sign;
+    const int lx = a->lx, ly = a->ly;
+    /* the coordinates advance with i instead of being recomputed with % per site */
+    int x = (int)(lo % lx), y = (int)(lo / lx);
+    for (long i = lo; i < hi; i++) {
         double eta1 = (double)(1 - 2 * (x % 2));
-        int xp = (x + 1) % lx, xm = (x + lx - 1) % lx;
-        int yp = (y + 1) % ly, ym = (y + ly - 1) % ly;
+        int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
+        int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
         cplx acc = 0.0;
         cplx t;
         t = U[(long)y * lx * 2 + x * 2] * rhs[(long)y * lx + xp];
@@ -48,18 +263,34 @@ static void staggered_apply(cplx *lhs, const cplx *rhs, const cplx *U, double ma
         acc = 0.5 * acc;
         acc = acc + mass * rhs[i];
         lhs[i] = acc;
+        if (++x == lx) {
+            x = 0;
+            y++;
+        }
     }
+}
+
+static void staggered_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass, int lx,
+                            int ly, double sign)
+{
+    site_args a = {lhs, rhs, U, mass, sign, lx, ly};
+    par_range((long)lx * ly, staggered_range, &a);
 }
 
 /* operator_utils/operators.cpp:73-120 (square_laplace_u1): lhs = (4+mass) psi
  * - sum_mu [U_mu(x) psi(x+mu) + U_mu(x-mu)^* psi(x-mu)], accumulated in the order
  * +x, -x, +y, -y, then the diagonal. */
-static void laplace_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass, int lx, int ly)
+static void laplace_range(void *ctx, long lo, long hi)
 {
-    for (long i = 0; i < (long)lx * ly; i++) {
-        int x = (int)(i % lx), y = (int)(i / lx);
-        int xp = (x + 1) % lx, xm = (x + lx - 1) % lx;
-        int yp = (y + 1) % ly, ym = (y + ly - 1) % ly;
+    const site_args *a = (const site_args *)ctx;
+    cplx *lhs = a->lhs;
+    const cplx *rhs = a->rhs, *U = a->U;
+    const double mass = a->mass;
+    const int lx = a->lx, ly = a->ly;
+    int x = (int)(lo % lx), y = (int)(lo / lx);
+    for (long i = lo; i < hi; i++) {
+        int xp = x + 1 == lx ? 0 : x + 1, xm = x == 0 ? lx - 1 : x - 1;
+        int yp = y + 1 == ly ? 0 : y + 1, ym = y == 0 ? ly - 1 : y - 1;
         cplx acc = 0.0;
         acc = acc - U[(long)y * lx * 2 + x * 2] * rhs[(long)y * lx + xp];
         acc = acc - conj(U[(long)y * lx * 2 + xm * 2]) * rhs[(long)y * lx + xm];
@@ -67,7 +298,17 @@ static void laplace_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass
         acc = acc - conj(U[(long)ym * lx * 2 + x * 2 + 1]) * rhs[(long)ym * lx + x];
         acc = acc + (4 + mass) * rhs[i];
         lhs[i] = acc;
+        if (++x == lx) {
+            x = 0;
+            y++;
+        }
     }
+}
+
+static void laplace_apply(cplx *lhs, const cplx *rhs, const cplx *U, double mass, int lx, int ly)
+{
+    site_args a = {lhs, rhs, U, mass, 0.0, lx, ly};
+    par_range((long)lx * ly, laplace_range, &a);
 }
 
 /* stencil_2d/coarse_stencil.cpp:12-172 (apply_stencil_2d, DIR_ALL), :395-460 (_eo) and
@@ -418,6 +659,126 @@ static void set_name(orc_info *info, const char *name)
     info->name[sizeof(info->name) - 1] = 0;
 }
 
+/* Site-parallel forms of the solvers' update loops.  Each writes the same expression, in the
+ * same operation order, as the serial loop it replaces. */
+typedef struct {
+    cplx *x, *r, *p;
+    const cplx *Ap;
+    cplx a;
+    cplx **xs, **ps;          /* multishift: per-shift solution and direction vectors */
+    const cplx *as, *bs;      /* multishift: per-shift scalars */
+    int ns;
+} upd_args;
+
+/* x = x + a p; r = r - a Ap (generic_cg.cpp:320-324) */
+static void upd_xr_range(void *ctx, long lo, long hi)
+{
+    const upd_args *u = (const upd_args *)ctx;
+    for (long i = lo; i < hi; i++) {
+        u->x[i] = u->x[i] + u->a * u->p[i];
+        u->r[i] = u->r[i] - u->a * u->Ap[i];
+    }
+}
+
+/* p = r + a p (generic_cg.cpp:343-346; generic_cg_m.cpp:515-518) */
+static void upd_p_range(void *ctx, long lo, long hi)
+{
+    const upd_args *u = (const upd_args *)ctx;
+    for (long i = lo; i < hi; i++) u->p[i] = u->r[i] + u->a * u->p[i];
+}
+
+/* r = r + a Ap (generic_cg_m.cpp:424-427) */
+static void upd_r_range(void *ctx, long lo, long hi)
+{
+    const upd_args *u = (const upd_args *)ctx;
+    for (long i = lo; i < hi; i++) u->r[i] = u->r[i] + u->a * u->Ap[i];
+}
+
+/* every live shift n: x_n = x_n - bs[n] p_n (generic_cg_m.cpp:410-413) */
+static void upd_shift_x_range(void *ctx, long lo, long hi)
+{
+    const upd_args *u = (const upd_args *)ctx;
+    for (int n = 0; n < u->ns; n++) {
+        cplx *x = u->xs[n];
+        const cplx *ps = u->ps[n];
+        const cplx b = u->bs[n];
+        for (long i = lo; i < hi; i++) x[i] = x[i] - b * ps[i];
+    }
+}
+
+/* every live shift n: p_n = as[n] r + bs[n] p_n (generic_cg_m.cpp:505-512; as = zeta_s,
+ * bs = alpha_s) */
+static void upd_shift_p_range(void *ctx, long lo, long hi)
+{
+    const upd_args *u = (const upd_args *)ctx;
+    for (int n = 0; n < u->ns; n++) {
+        cplx *ps = u->ps[n];
+        const cplx z = u->as[n], a = u->bs[n];
+        for (long i = lo; i < hi; i++) ps[i] = z * u->r[i] + a * ps[i];
+    }
+}
+
+/* The CG's reductions fused with the passes that produce their terms (par_ordered): the
+ * terms are formed and added in the serial loops' order, so the sums are those of cdot and
+ * cnorm2 bit for bit. */
+typedef struct {
+    site_args st;          /* the D^dagger pass of D^dagger D */
+    const cplx *a, *b;     /* dot: sum conj(a_i) b_i */
+    cplx dot;
+    upd_args *upd;         /* the x / r update */
+    double nrm;            /* norm: sum |r_i|^2 */
+} fused_args;
+
+static void fused_stag_work(void *ctx, long lo, long hi) { staggered_range(&((fused_args *)ctx)->st, lo, hi); }
+
+static void fused_dot_sum(void *ctx, long lo, long hi)
+{
+    fused_args *f = (fused_args *)ctx;
+    cplx r = f->dot;
+    for (long i = lo; i < hi; i++) r = r + conj(f->a[i]) * f->b[i];
+    f->dot = r;
+}
+
+static void fused_xr_work(void *ctx, long lo, long hi) { upd_xr_range(((fused_args *)ctx)->upd, lo, hi); }
+
+static void fused_norm_sum(void *ctx, long lo, long hi)
+{
+    fused_args *f = (fused_args *)ctx;
+    const cplx *r_ = f->upd->r;
+    double r = f->nrm;
+    for (long i = lo; i < hi; i++) r = r + creal(conj(r_[i]) * r_[i]);
+    f->nrm = r;
+}
+
+/* Ap = op(p) and returns <p, Ap> (cdot order).  The staggered normal operator runs its D^dagger
+ * pass with the dot fused in; other operators apply, then reduce. */
+static cplx apply_dot(const orc_op *op, cplx *Ap, const cplx *p, long size, cplx *tmp)
+{
+    if (op->kind != ORC_STAGGERED_NORMAL || tmp == NULL) {
+        orc_apply(op, (double *)Ap, (const double *)p);
+        return cdot(p, Ap, size);
+    }
+    staggered_apply(tmp, p, CCX(op->links), op->mass, op->lx, op->ly, +1.0);
+    fused_args f;
+    site_args st = {Ap, tmp, CCX(op->links), op->mass, -1.0, op->lx, op->ly};
+    f.st = st;
+    f.a = p;
+    f.b = Ap;
+    f.dot = 0.0;
+    par_ordered(size, fused_stag_work, fused_dot_sum, &f);
+    return f.dot;
+}
+
+/* x += alpha p; r -= alpha Ap, and returns |r|^2 (cnorm2 order). */
+static double update_xr_norm(upd_args *u, long size)
+{
+    fused_args f;
+    f.upd = u;
+    f.nrm = 0.0;
+    par_ordered(size, fused_xr_work, fused_norm_sum, &f);
+    return f.nrm;
+}
+
 /* ---------------------------------------------------------------- CG */
 
 /* generic_cg.cpp:278-382 (complex minv_vector_cg). */
@@ -434,32 +795,36 @@ void orc_cg(const orc_op *op, double *phi_, const double *phi0_, long size, int 
     int k, ops = 0;
     long i;
 
+    cplx *tmp = (op->kind == ORC_STAGGERED_NORMAL) ? (cplx *)malloc(sizeof(cplx) * size) : NULL;
+    cplx pAp;
+
     bsqrt = sqrt(cnorm2(phi0, size));
     orc_apply(op, (double *)p, (const double *)phi); ops++;
     for (i = 0; i < size; i++) r[i] = phi0[i] - p[i];
     memcpy(p, r, sizeof(cplx) * size);
-    orc_apply(op, (double *)Ap, (const double *)p); ops++;
+    /* <p, Ap> is formed with Ap (below and at the end of each iteration) rather than at the
+     * top of the next iteration: p and Ap do not change in between */
+    pAp = apply_dot(op, Ap, p, size, tmp); ops++;
     rsq = cnorm2(r, size);
+    upd_args upd = {phi, r, p, Ap, 0.0, NULL, NULL, NULL, NULL, 0};
 
     for (k = 0; k < max_iter; k++) {
-        alpha = rdivc(rsq, cdot(p, Ap, size));
-        for (i = 0; i < size; i++) {
-            phi[i] = phi[i] + alpha * p[i];
-            r[i] = r[i] - alpha * Ap[i];
-        }
-        rsqNew = cnorm2(r, size);
+        alpha = rdivc(rsq, pAp);
+        upd.a = alpha;
+        rsqNew = update_xr_norm(&upd, size);
         record(hist, hist_cap, k, sqrt(rsqNew) / bsqrt);
         if (sqrt(rsqNew) < eps * bsqrt || k == max_iter - 1) break;
         beta = mk(rsqNew / rsq, 0.0);
         rsq = rsqNew;
-        for (i = 0; i < size; i++) p[i] = r[i] + beta * p[i];
-        orc_apply(op, (double *)Ap, (const double *)p); ops++;
+        upd.a = beta;
+        par_range(size, upd_p_range, &upd);
+        pAp = apply_dot(op, Ap, p, size, tmp); ops++;
     }
     info->success = (k == max_iter - 1) ? 0 : 1;
     k++;
     orc_apply(op, (double *)Ap, (const double *)phi); ops++;
     truersq = cdiffnorm2(Ap, phi0, size);
-    free(r); free(p); free(Ap);
+    free(r); free(p); free(Ap); free(tmp);
     info->resSq = truersq;
     info->iter = k;
     info->ops_count = ops;
@@ -684,6 +1049,7 @@ void orc_cg_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shif
     memcpy(r, phi0, sizeof(cplx) * size);
     orc_apply(op, (double *)Ap, (const double *)p); ops++;
     rsq = cnorm2(r, size);
+    upd_args mupd = {NULL, r, p, Ap, 0.0, phi, p_s, NULL, NULL, 0};
 
     for (k = 0; k < max_iter; k++) {
         beta_prev = beta;
@@ -695,9 +1061,12 @@ void orc_cg_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shif
                          zeta_s_prev[n] * beta_prev * (mk(1.0, 0.0) - shifts[n] * beta));
             zeta_s_prev[n] = tmp;
             beta_s[n] = beta * zeta_s[n] / zeta_s_prev[n];
-            for (i = 0; i < size; i++) phi[n][i] = phi[n][i] - beta_s[n] * p_s[n][i];
         }
-        for (i = 0; i < size; i++) r[i] = r[i] + beta * Ap[i];
+        mupd.ns = n_shift_rem;
+        mupd.bs = beta_s;
+        par_range(size, upd_shift_x_range, &mupd);
+        mupd.a = beta;
+        par_range(size, upd_r_range, &mupd);
         rsqNew = cnorm2(r, size);
         record(hist, hist_cap, k, sqrt(rsqNew) / bsqrt);
 
@@ -726,11 +1095,14 @@ void orc_cg_m(const orc_op *op, double *phi_all, const double *phi0_, int n_shif
 
         alpha = mk(rsqNew / rsq, 0.0);
         rsq = rsqNew;
-        for (n = 0; n < n_shift_rem; n++) {
+        for (n = 0; n < n_shift_rem; n++)
             alpha_s[n] = alpha * zeta_s[n] * beta_s[n] / (zeta_s_prev[n] * beta);
-            for (i = 0; i < size; i++) p_s[n][i] = zeta_s[n] * r[i] + alpha_s[n] * p_s[n][i];
-        }
-        for (i = 0; i < size; i++) p[i] = r[i] + alpha * p[i];
+        mupd.ns = n_shift_rem;
+        mupd.as = zeta_s;
+        mupd.bs = alpha_s;
+        par_range(size, upd_shift_p_range, &mupd);
+        mupd.a = alpha;
+        par_range(size, upd_p_range, &mupd);
         orc_apply(op, (double *)Ap, (const double *)p); ops++;
     }
     info->success = (k == max_iter - 1) ? 0 : 1;

@@ -70,22 +70,81 @@ class OrcInfo(C.Structure):
                 "ops_count": self.ops_count, "name": self.name.decode()}
 
 
+REF_RECORD = os.path.join(HERE, "_ref", "REFERENCE_DIR")
+
+
 def reference_dir():
-    """The reference checkout the reference-compiled builds read (GLINALG_REFERENCE_DIR
-    overrides the default location)."""
-    return os.environ.get("GLINALG_REFERENCE_DIR", "/root/reference")
+    """The reference checkout that the reference-compiled builds and fixture scripts read:
+    GLINALG_REFERENCE_DIR if set, else the checkout the last reference build compiled from
+    (recorded in oracle/_ref/REFERENCE_DIR), else None."""
+    d = os.environ.get("GLINALG_REFERENCE_DIR")
+    if d:
+        return d
+    try:
+        with open(REF_RECORD) as f:
+            d = f.read().strip()
+        return d if os.path.isdir(d) else None
+    except OSError:
+        return None
 
 
-def build(quiet=True):
-    """Compile liboracle.so (and libref_oracle.so when the reference checkout exists)."""
+def build(quiet=True, reference=None):
+    """Compile liboracle.so, and libref_oracle.so when a reference checkout is given (the
+    argument, else GLINALG_REFERENCE_DIR) and present."""
     out = subprocess.DEVNULL if quiet else None
     subprocess.check_call(["make", "-s", "-C", HERE], stdout=out)
-    ref = reference_dir()
-    if os.path.isdir(ref):
+    ref = reference or os.environ.get("GLINALG_REFERENCE_DIR")
+    if ref and os.path.isdir(ref):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], stdout=out)
+        with open(REF_RECORD, "w") as f:
+            f.write(os.path.abspath(ref) + "\n")
 
 
 PRECOND = {"identity": 0, "minres": 1, "gcr": 2}
+
+
+class Generator:
+    """The reference tests' input generators on one std::mt19937 stream (oracle/inputs.cpp):
+    rand_gauge_u1, gauss_gauge_u1, rand_trans_u1 and gaussian, drawn in the reference's order."""
+
+    def __init__(self, seed, path=LIB_PATH):
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.orc_rng_create.argtypes = [C.c_uint]
+        L.orc_rng_create.restype = C.c_void_p
+        L.orc_rng_destroy.argtypes = [C.c_void_p]
+        L.orc_rng_gauge_u1.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int]
+        L.orc_rng_gauss_gauge_u1.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int, C.c_double]
+        L.orc_rng_trans_u1.argtypes = [C.c_void_p, _dp, C.c_int, C.c_int]
+        L.orc_rng_gaussian.argtypes = [C.c_void_p, _dp, C.c_long]
+        self.lib = L
+        self.h = L.orc_rng_create(int(seed))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_rng_destroy(self.h)
+            self.h = None
+
+    def rand_gauge_u1(self, lx, ly):
+        U = np.empty(2 * lx * ly, np.complex128)
+        self.lib.orc_rng_gauge_u1(self.h, _ptr(U), lx, ly)
+        return U
+
+    def gauss_gauge_u1(self, lx, ly, beta):
+        U = np.empty(2 * lx * ly, np.complex128)
+        self.lib.orc_rng_gauss_gauge_u1(self.h, _ptr(U), lx, ly, beta)
+        return U
+
+    def rand_trans_u1(self, lx, ly):
+        t = np.empty(lx * ly, np.complex128)
+        self.lib.orc_rng_trans_u1(self.h, _ptr(t), lx, ly)
+        return t
+
+    def gaussian(self, n):
+        v = np.empty(n, np.complex128)
+        self.lib.orc_rng_gaussian(self.h, _ptr(v), n)
+        return v
 
 
 class OrcPrecond(C.Structure):
@@ -180,6 +239,14 @@ class Oracle:
         L.orc_gauge_trans_u1.argtypes = [_dp, _dp, C.c_int, C.c_int]
         L.orc_ape_smear_u1.argtypes = [_dp, _dp, C.c_int, C.c_int, C.c_double, C.c_int]
         L.orc_eoprec_reconstruct.argtypes = [P(OrcOp), _dp, _dp, _dp]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_get_threads.restype = C.c_int
+
+    def set_threads(self, n=None):
+        """Threads for the oracle's site loops (operators and vector updates); reductions stay
+        serial in the reference's order, so results do not depend on n.  None: every core."""
+        self.lib.orc_set_threads(int(n) if n else (os.cpu_count() or 1))
+        return self.lib.orc_get_threads()
 
     def apply(self, op: Operator, rhs):
         rhs = np.ascontiguousarray(rhs, dtype=np.complex128)

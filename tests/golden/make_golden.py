@@ -8,8 +8,9 @@ stores inputs, outputs, solver infos and verbosity logs:
   reference_vectors.npz   complex128 fields (inputs and outputs)
   reference_info.json     solver infos, verbosity logs, parameters
 
-Run from the repository root:  python tests/golden/make_golden.py
-(requires the reference checkout; GLINALG_REFERENCE_DIR overrides its location).
+Run from the repository root:
+  GLINALG_REFERENCE_DIR=<reference checkout> python tests/golden/make_golden.py
+(or without the variable after a build that compiled the reference and recorded its location).
 """
 from __future__ import annotations
 
@@ -27,7 +28,10 @@ import pyoracle  # noqa: E402
 
 
 def main():
-    pyoracle.build()
+    refdir = pyoracle.reference_dir()
+    if not refdir:
+        raise SystemExit("set GLINALG_REFERENCE_DIR to the reference checkout")
+    pyoracle.build(reference=refdir)
     R = pyoracle.RefOracle()
     Op = pyoracle.Operator
     vec = {}
@@ -209,7 +213,6 @@ def main():
     # topological charge (q1: +1, qm3: -3).  Smooth fields, unlike rand_gauge_u1's.  Stored: the
     # links as read, the gauge utilities as above, and the reference's CG on the staggered
     # normal equations with the l32 source at m = 0.1 and m = 0.01
-    refdir = pyoracle.reference_dir()
     heatbath = {"hb30": "l32t32b30_heatbath.dat", "hb60q1": "l32t32b60_heatbath_q1.dat",
                 "hb60qm3": "l32t32b60_heatbath_qm3.dat"}
     for key, fn in heatbath.items():

@@ -141,7 +141,8 @@ def test_library_reads_the_reference_files(gl, golden, key):
     import os
     import pyoracle
     vec, cases = golden
-    path = os.path.join(pyoracle.reference_dir(), "multigrid", "aa_mg", "cfg", cases[f"{key}_gauge"]["file"])
+    ref = pyoracle.reference_dir()
+    path = os.path.join(ref, "multigrid", "aa_mg", "cfg", cases[f"{key}_gauge"]["file"]) if ref else ""
     if not os.path.isfile(path):
         pytest.skip("the reference checkout is not present")
     U = np.zeros(2 * L * L, np.complex128)

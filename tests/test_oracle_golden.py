@@ -207,3 +207,45 @@ def test_cg_m_equals_sequential_cg(oracle, golden):
         kappa = (m + 8.0) / m
         d = np.linalg.norm(x - xs[j]) / np.linalg.norm(xs[j])
         assert d <= 1.01 * kappa * (r1 + r2) and d <= 1e-12, (j, d)
+
+
+# ---- the oracle's own input generator and its threaded site loops
+
+@pytest.mark.parametrize("key,lx,ly,seed", [("l32", 32, 32, 1337), ("l8", 8, 8, 7), ("l12x6", 12, 6, 3)])
+def test_oracle_generator_bit_exact(golden, key, lx, ly, seed):
+    """oracle/inputs.cpp reproduces the reference's rand_gauge_u1 and gaussian streams
+    (u1_utils.cpp:79-87, generic_vector.h:48-60) bit for bit: links, then two sources."""
+    import pyoracle
+    vec, _ = golden
+    g = pyoracle.Generator(seed)
+    assert np.array_equal(g.rand_gauge_u1(lx, ly), vec[f"{key}_links"])
+    assert np.array_equal(g.gaussian(lx * ly), vec[f"{key}_src"])
+    assert np.array_equal(g.gaussian(lx * ly), vec[f"{key}_src2"])
+
+
+def test_oracle_threads_change_no_bit(oracle):
+    """Site loops on several threads, sums serial in the reference's order: CG (with its sums
+    fused into the passes that form their terms) and CG-M give the single-thread results bit for
+    bit, on a lattice large enough to be split into many chunks."""
+    import pyoracle
+    g = pyoracle.Generator(21)
+    lx, ly = 192, 96
+    U = g.rand_gauge_u1(lx, ly)
+    b = g.gaussian(lx * ly)
+    out = {}
+    try:
+        for nth in (1, 3, 8):
+            oracle.set_threads(nth)
+            op = pyoracle.Operator("staggered_normal", lx, ly, 0.05, U)
+            x, info, hist = oracle.solve("cg", op, b, hist_cap=4000)
+            xm, im, rm = oracle.cg_m(op, b, np.logspace(-4, 0, 5))
+            xl, il, _ = oracle.solve("cg", pyoracle.Operator("laplace", lx, ly, 0.3, U), b)
+            out[nth] = (x, info, hist, xm, im, rm, xl, il)
+    finally:
+        oracle.set_threads(1)
+    for nth in (3, 8):
+        for a, c in zip(out[1], out[nth]):
+            if isinstance(a, np.ndarray):
+                assert np.array_equal(a, c), nth
+            else:
+                assert a == c, nth
