@@ -49,10 +49,12 @@ HEADLINE = ("fp32", 1)
 #     the launch's inner iterations (entry included); GB300 serves one 128 B wavefront per clock
 #     per SM
 CAPTURES = {
-    "resident": {"source": "generic-linalg_gb300/csrc/stag_resident.cuh", "sha256": None,
-                 "kernel": "k_resident<16 warps, x_lo and links in tensor memory>",
+    "resident": {"source": "generic-linalg_gb300/csrc/stag_resident.cuh",
+                 "sha256": "3d75a586d3f867a3054056790f22b36ceabeed0d5412e3112c894a6260f9d6e2",
+                 "kernel": "k_resident<14, 4, 3> (16 warps, x_lo and links in tensor memory)",
                  "profile": "profiles/k_resident_fp32_1024.md", "iters_per_launch": 20,
-                 "dram_bytes_per_launch": 42.13248e6 + 0.00896e6, "smem_wavefronts_per_sm_iter": 6.56e3},
+                 "dram_bytes_per_launch": 42.130688e6 + 0.043008e6,
+                 "smem_wavefronts_per_sm_iter": 19948889 / (152 * 20)},
     "persist": {"source": "generic-linalg_gb300/csrc/stag_tiles.cuh", "sha256": None,
                 "kernel": "k_persist", "profile": "profiles/k_persist_fp32_1024.md", "iters_per_launch": 254,
                 "dram_bytes_per_launch": 41.987328e6 + 3.212544e6},
@@ -278,8 +280,10 @@ def _flush_and_time(fn, flush, stream):
 
 def workload_multishift(args):
     """Multishift CG on the staggered normal equations, 512x512, m = 0.05, 12 shifts log-spaced
-    over [1e-4, 1], tolerance 1e-10 per shift: one source, and 64 sources in one batched solve
-    (glinalg_cg_m_multi) against 64 single-source solves one after another.  Inputs from
+    over [1e-4, 1], tolerance 1e-10 per shift: one source and 64 sources in one batched solve
+    (glinalg_cg_m_multi), FP64 (the reference's recurrence) and mixed precision (FP32
+    multishift with FP64 scalar recurrences, then every shift refined by the mixed CG to an
+    FP64-true 1e-10), against 64 single-source FP64 solves one after another.  Inputs from
     std::mt19937(1337): links, then the sources in order."""
     import numpy as np
     import torch
@@ -290,25 +294,45 @@ def workload_multishift(args):
     torch.cuda.set_stream(stream)
     gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
     lx = ly = 512
+    mass = 0.05
     n_rhs, shifts = 64, np.logspace(-4, 0, 12)
     g = gl.Generator(SEED)
     U = g.rand_gauge_u1(lx, ly)
     B = np.stack([g.gaussian(lx * ly) for _ in range(n_rhs)])
-    op = gl.Operator(2, lx, ly, 0.05, torch.from_numpy(U).to(dev))
+    op = gl.Operator(2, lx, ly, mass, torch.from_numpy(U).to(dev))
     Bd = torch.from_numpy(B).to(dev)
     X = torch.zeros((n_rhs, len(shifts), lx * ly), dtype=torch.complex128, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    res = {}
-    for nr in (1, n_rhs):
-        for i in range(args.warmup + args.steps):
-            X.zero_()
-            t, infos = _flush_and_time(lambda: gl.cg_m_multi(op, X[:nr], Bd[:nr], shifts, 1, 100000, 1e-10),
-                                       flush, stream)
-            if i >= args.warmup:
-                res.setdefault(nr, []).append(t)
-        assert all(inf.success for inf in infos)
-        res[f"info{nr}"] = infos
-    # the same 64 sources, one single-source solve after another
+    Ax = torch.zeros(lx * ly, dtype=torch.complex128, device=dev)
+
+    def true_relres(xq, q, sg):
+        op.apply(Ax, xq)
+        return float(torch.linalg.vector_norm(Bd[q] - Ax - sg * xq) / torch.linalg.vector_norm(Bd[q]))
+
+    out, sol0 = {}, {}
+    for name, prec in (("fp64", 0), ("fp32", 1)):
+        res = {}
+        for nr in (1, n_rhs):
+            for i in range(args.warmup + args.steps):
+                X.zero_()
+                t, infos = _flush_and_time(
+                    lambda: gl.cg_m_multi(op, X[:nr], Bd[:nr], shifts, 1, 100000, 1e-10, precision=prec),
+                    flush, stream)
+                if i >= args.warmup:
+                    res.setdefault(nr, []).append(t)
+            assert all(inf.success for inf in infos), (name, infos)
+            res[f"info{nr}"] = infos
+        i64 = res[f"info{n_rhs}"]
+        ms64 = statistics.mean(res[n_rhs])
+        worst = max(true_relres(X[q, k], q, sg) for q in (0, n_rhs - 1) for k, sg in enumerate(shifts))
+        sol0[name] = X[0].cpu().numpy().copy()
+        out[name] = {"one_source_ms": round(statistics.mean(res[1]), 3), "one_source_iters": res["info1"][0].iter,
+                     "batched_ms": round(ms64, 3), "batched_ms_per_source": round(ms64 / n_rhs, 3),
+                     "batched_iters_min_max": [min(i.iter for i in i64), max(i.iter for i in i64)],
+                     "operator_applications_per_source_mean": round(statistics.mean(i.ops_count for i in i64), 1),
+                     "batched_algorithmic_GBps": round(sum(i.gbytes for i in i64) / (ms64 * 1e-3), 1),
+                     "max_shift_true_relres_sources_0_and_63": worst}
+    # the same 64 sources, one single-source FP64 solve after another
     xs = [torch.zeros(lx * ly, dtype=torch.complex128, device=dev) for _ in shifts]
 
     def one_by_one():
@@ -316,32 +340,29 @@ def workload_multishift(args):
             gl.minv_vector_cg_m(xs, Bd[q], len(shifts), lx * ly, 1, 100000, 1e-10, shifts.copy(),
                                 gl.square_staggered_normal_u1, op)
     t_seq, _ = _flush_and_time(one_by_one, flush, stream)
-    i1, i64 = res["info1"], res[f"info{n_rhs}"]
-    ms1, ms64 = statistics.mean(res[1]), statistics.mean(res[n_rhs])
-    gb64 = sum(inf.gbytes for inf in i64)
     line = {"workload": "multishift CG, staggered normal equations 512x512, m=0.05, 12 shifts logspace[1e-4,1], tol 1e-10",
             "steps": args.steps, "warmup": args.warmup, "l2": "flushed (512 MiB write) before every solve",
-            "one_source_ms": round(ms1, 3), "one_source_iters": i1[0].iter,
-            "sources": n_rhs, "batched_ms": round(ms64, 3),
-            "batched_iters_min_max": [min(i.iter for i in i64), max(i.iter for i in i64)],
-            "batched_ms_per_source": round(ms64 / n_rhs, 3),
-            "one_by_one_ms": round(t_seq, 3), "batch_speedup": round(t_seq / ms64, 2),
-            "batched_algorithmic_GBps": round(gb64 / (ms64 * 1e-3), 1),
-            "max_shift_relres": float(max(np.sqrt(np.max(inf.resSqmrhs)) / np.linalg.norm(B[q])
-                                          for q, inf in enumerate(i64)))}
+            "sources": n_rhs, "variants": out, "fp64_one_by_one_ms": round(t_seq, 3),
+            "mixed_speedup_vs_fp64_batched": round(out["fp64"]["batched_ms"] / out["fp32"]["batched_ms"], 2),
+            "mixed_speedup_vs_fp64_one_by_one": round(t_seq / out["fp32"]["batched_ms"], 2)}
     if not args.no_cpu_baseline:
+        # the oracle's CG-M (the reference's recurrence, site loops on every host core) on source 0:
+        # one complete solve, and every variant's source-0 solutions against it
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
         O = pyoracle.Oracle()
-        oop = pyoracle.Operator("staggered_normal", lx, ly, 0.05, U)
+        nth = O.set_threads(None)
+        oop = pyoracle.Operator("staggered_normal", lx, ly, mass, U)
         t0 = time.perf_counter()
-        O.cg_m(oop, B[0], shifts, max_iter=20, eps=1e-10)
+        xo, io, _ = O.cg_m(oop, B[0], shifts, max_iter=100000, eps=1e-10)
         dt = time.perf_counter() - t0
-        per = dt / 20
-        line["cpu_baseline"] = {"value": per * i1[0].iter * 1e3 * n_rhs, "unit": "ms (64 sources)", "cores": 1,
+        for name in out:
+            out[name]["source0_max_shift_err_vs_oracle"] = float(max(
+                np.linalg.norm(sol0[name][k] - xo[k]) / np.linalg.norm(xo[k]) for k in range(len(shifts))))
+        line["cpu_baseline"] = {"value": round(dt * 1e3 * n_rhs, 1), "unit": "ms (64 sources)", "cores": nth,
                                 "kind": "port",
-                                "sample": f"20 CG-M iterations of one source ({dt:.2f} s), extrapolated to "
-                                          f"{i1[0].iter} iterations x {n_rhs} sources"}
+                                "sample": f"one complete CG-M solve of source 0 ({io['iter']} iterations, "
+                                          f"{dt:.2f} s on {nth} threads) times 64 sources"}
     print(json.dumps(line))
 
 

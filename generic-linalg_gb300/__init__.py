@@ -680,9 +680,12 @@ def _multishift(fn, phi, phi0, n_shift, size, resid_freq_check, max_iter, eps, s
 
 # ---------------------------------------------------------------- batched, force, BLAS, RNG
 
-def cg_m_multi(op: Operator, phi, phi0, shifts, resid_freq_check=1, max_iter=10000, eps=1e-10):
+def cg_m_multi(op: Operator, phi, phi0, shifts, resid_freq_check=1, max_iter=10000, eps=1e-10,
+               precision=PREC_DOUBLE):
     """Multishift CG for several sources at once.  phi: (n_rhs, n_shift, size), phi0:
-    (n_rhs, size); both complex128, host or device."""
+    (n_rhs, size); both complex128, host or device.  precision PREC_SINGLE (staggered normal
+    operator): an FP32 multishift with FP64 scalar recurrences, then every shifted system
+    refined by the mixed CG to the FP64-true relative residual eps."""
     n_rhs, n_shift = phi.shape[0], phi.shape[1]
     pp, pn, dev = _field_ptr(phi, writable=True)
     bp, bn, bdev = _field_ptr(phi0)
@@ -699,7 +702,7 @@ def cg_m_multi(op: Operator, phi, phi0, shifts, resid_freq_check=1, max_iter=100
     _capi.check(lib().glinalg_cg_m_multi(op.handle, _dptr(pp), _dptr(bp), n_rhs, n_shift, op.size,
                                          int(resid_freq_check), int(max_iter), float(eps),
                                          sh.ctypes.data_as(C.POINTER(C.c_double)),
-                                         C.byref(_params(device=dev)), infos), "glinalg_cg_m_multi")
+                                         C.byref(_params(precision, device=dev)), infos), "glinalg_cg_m_multi")
     return [InversionInfo(infos[q], res[q]) for q in range(n_rhs)]
 
 

@@ -50,7 +50,9 @@ def _compile(src, force, extra):
             return obj, None
     cmd = [nvcc()] + ARCH + NVCC_FLAGS + extra + ["-c", path, "-o", obj]
     if src.endswith(".cpp"):
-        cmd = [nvcc(), "-x", "c++"] + NVCC_FLAGS + extra + ["-c", path, "-o", obj]
+        # host-only code: no multiply-add contraction, so that the input generators give the
+        # same bits on aarch64 (FMA in the base ISA) as on x86_64
+        cmd = [nvcc(), "-x", "c++"] + NVCC_FLAGS + ["-Xcompiler", "-ffp-contract=off"] + extra + ["-c", path, "-o", obj]
     p = subprocess.run(cmd, capture_output=True, text=True)
     if p.returncode != 0:
         return obj, f"{' '.join(cmd)}\n{p.stdout}\n{p.stderr}"

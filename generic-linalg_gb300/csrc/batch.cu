@@ -41,7 +41,15 @@ extern "C" glinalg_status glinalg_cg_m_multi(glinalg_operator op, double *phi, c
         X = tx;
         B = tb;
     }
-    if (cg_m_batch_supported(op, n_shift)) {
+    const int prec = params ? params->precision : GLINALG_PREC_DOUBLE;
+    if (prec != GLINALG_PREC_DOUBLE) {
+        if (prec != GLINALG_PREC_SINGLE || !cg_m_batch_mixed_supported(op, n_shift)) {
+            set_last_error("mixed-precision multishift needs precision SINGLE, the staggered normal operator "
+                           "and at most 32 shifts");
+            return GLINALG_ERROR_UNSUPPORTED_OP;
+        }
+        GL_TRY(cg_m_batch_mixed(op, X, B, n_rhs, n_shift, resid_freq_check, max_iter, eps, shifts, infos, st));
+    } else if (cg_m_batch_supported(op, n_shift)) {
         GL_TRY(cg_m_batch(op, X, B, n_rhs, n_shift, resid_freq_check, max_iter, eps, shifts, infos, st));
     } else {
         // other operator kinds: one source after another

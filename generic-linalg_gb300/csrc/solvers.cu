@@ -115,6 +115,7 @@ glinalg_status cg_fp64(const glinalg_operator_s *op, double2 *x, const double2 *
                        double eps, const Verb &verb, glinalg_info *info, cudaStream_t st,
                        double sigma)
 {
+    if (cg64_fused_applies(op, sigma)) return cg64_fused(op, x, b, max_iter, eps, verb, info, st);
     const long n = op->size;
     Scratch sc(st);
     double2 *r, *p, *Ap, *tmp = nullptr;

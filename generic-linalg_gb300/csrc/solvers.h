@@ -23,6 +23,15 @@ bool cg_m_batch_supported(const glinalg_operator_s *op, int n_shift);
 glinalg_status cg_m_batch(const glinalg_operator_s *op, double2 *X, const double2 *B, int n_rhs,
                           int n_shift, int rfc, int max_iter, double eps, const double *shifts,
                           glinalg_info *infos, cudaStream_t st);
+// The same in mixed precision (cgm_mixed.cu): an FP32 multishift over every source (FP64
+// scalar recurrences), then every shifted system refined by the mixed CG to eps, FP64-true.
+// Staggered-normal kind, n_shift <= 32.  phase1_iters / phase2_iters (may be null): per source,
+// the multishift iterations and the refinement iterations summed over its shifts.
+bool cg_m_batch_mixed_supported(const glinalg_operator_s *op, int n_shift);
+glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const double2 *B, int n_rhs,
+                                int n_shift, int rfc, int max_iter, double eps, const double *shifts,
+                                glinalg_info *infos, cudaStream_t st, int *phase1_iters = nullptr,
+                                int *phase2_iters = nullptr);
 // Mixed-precision CG (FP64 reliable updates) on nsys independent systems of any sizes,
 // staggered-normal or Laplace kinds, advanced together (cg_batch.cu).  X[q], B[q]: device fields.
 glinalg_status cg_batch_mixed(const glinalg_operator_s *const *ops, int nsys, double2 *const *X,
@@ -74,6 +83,13 @@ glinalg_status flex_fp64(int mode, const glinalg_operator_s *op, double2 *x, con
 glinalg_status flex_restart_fp64(int mode, const glinalg_operator_s *op, double2 *x, const double2 *b,
                                  int max_iter, double eps, int restart_freq, const Precond &pc,
                                  const Verb &verb, glinalg_info *info, cudaStream_t st);
+
+// The FP64 CG on the staggered normal operator as one persistent cooperative kernel
+// (cg64_fused.cu): whether it serves op (lx a multiple of 32, no shift; GLINALG_FP64_FUSED=0
+// turns it off), and the solve.
+bool cg64_fused_applies(const glinalg_operator_s *op, double sigma);
+glinalg_status cg64_fused(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter, double eps,
+                          const Verb &verb, glinalg_info *info, cudaStream_t st, int wait_limit_us = 0);
 
 // Mixed-precision CG with FP64 reliable updates (cg_mixed.cu).  sigma: diagonal shift added to
 // the operator (0 for the plain system).  wait_limit_us: glinalg_solver_params::wait_limit_us.

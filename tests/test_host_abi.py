@@ -172,3 +172,19 @@ def test_wrappers_refuse_short_or_mismatched_arrays(gl):
         gl.cg_batch([op, op], [z(16)], [z(16), z(16)])
     with pytest.raises(ValueError, match=r"phis\[1\] holds 15 values"):
         gl.cg_batch([op, op], [z(16), z(15)], [z(16), z(16)])
+
+
+def test_bench_capture_stamps_match_kernel_sources():
+    """The ncu figures bench.py reports with the headline kernel (DRAM bytes and shared-memory
+    wavefronts per launch) were captured from a kernel source whose SHA-256 they carry; a
+    changed kernel must be re-captured (or its stamp cleared, which reports the figures as
+    stale) before this passes.  The headline kernel's capture must be stamped."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench.CAPTURES["resident"]["sha256"] is not None
+    for key, cap in bench.CAPTURES.items():
+        if cap["sha256"] is not None:
+            assert bench.source_sha256(cap["source"]) == cap["sha256"], (key, cap["source"])
+            assert os.path.exists(os.path.join(ROOT, cap["profile"])), key

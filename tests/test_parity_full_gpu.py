@@ -12,15 +12,21 @@ Bars (each measured figure is printed by the test):
     relative of the oracle's.  A CG whose sums only run in another order lands 6.6e-13 from
     it (2093 iterations): the difference is rounding, and 1e-11 leaves a margin of 15.
   - Mixed CG (FP32 / FP16 / BF16 inner iterations, FP64 reliable updates): FP64-true relative
-    residual below 1e-10, recomputed here by the oracle's operator; solution within
-    2 kappa 1e-10 of the oracle's, kappa(M^dagger M) <= (4 + m^2) / m^2 = 40001: the bound any
-    two solutions with relative residual below 1e-10 meet.  Their Krylov paths differ from the
-    FP64 one, so nothing tighter holds by construction.
+    residual below 1e-10, recomputed here by the oracle's operator; solution within 1e-9
+    relative of the oracle's.  Measured on GB300: 1.7e-13 (FP32), 6.1e-11 (FP16), 5.8e-11
+    (BF16).  Nothing tighter holds by construction (their Krylov paths differ from the FP64
+    one; any two solutions with relative residual below 1e-10 differ by at most
+    2 kappa 1e-10 = 8e-6, kappa(M^dagger M) <= (4 + m^2) / m^2 = 40001), so the bar is the
+    measured worst case with a margin of 16.
   - Multishift, 512^2, m = 0.05, 12 shifts log-spaced over [1e-4, 1], 2 sources: per source the
     oracle's CG-M iteration count; every shift's solution within 1e-10 relative of the oracle's.
     CG-M retires a shift on its iterated residual |zeta_s| |r| < 1e-10 |b|
     (generic_cg_m.cpp:440); the explicit residual drifts from it by rounding, so it is held
     to 1e-9, as in the batched multishift tests.
+  - Mixed multishift (FP32 multishift with FP64 scalar recurrences, then every shift refined by
+    the mixed CG), same system: every shift's FP64-true relative residual below 1e-10 (what the
+    refinement stops on), and its solution within 1e-9 of the oracle's CG-M solution, the bar of
+    the mixed CG above.
 """
 from __future__ import annotations
 
@@ -80,12 +86,11 @@ def test_mixed_cg_1024_matches_oracle(gl, gpu, system1024, precision, name):
                              gl.StaggeredU1Op(U, M1, L1, L1), precision=precision)
     err = float(np.linalg.norm(x - xo) / np.linalg.norm(xo))
     rr = true_relres(O, op, x, b)
-    kappa = (4 + M1 * M1) / (M1 * M1)
     print(f"{name} mixed CG 1024^2: {info.iter} inner iterations, {info.reliable_updates} reliable updates, "
           f"relres {rr:.3e}, err vs oracle {err:.3e}")
     assert info.success
     assert rr < 1e-10
-    assert err < 2 * kappa * 1e-10
+    assert err < 1e-9
 
 
 @pytest.fixture(scope="module")
@@ -122,3 +127,28 @@ def test_multishift_512_two_sources_match_oracle(gl, gpu, system512):
             assert rr < 1e-9, (q, k, rr)
         print(f"multishift 512^2 source {q}: {infos[q].iter} iterations (oracle {io['iter']}), "
               f"worst shift err vs oracle {worst_err:.3e}, worst relres {worst_rr:.3e}")
+
+
+def test_mixed_multishift_512_two_sources_match_oracle(gl, gpu, system512):
+    import torch
+    U, B, ref, O, op = system512
+    gop = gl.Operator(2, L3, L3, M3, torch.from_numpy(U).to(gpu))
+    Bd = torch.from_numpy(B).to(gpu)
+    X = torch.zeros((2, len(SHIFTS), L3 * L3), dtype=torch.complex128, device=gpu)
+    infos = gl.cg_m_multi(gop, X, Bd, SHIFTS, 1, 100000, 1e-10, precision=gl.PREC_SINGLE)
+    Xh = X.cpu().numpy()
+    for q in range(2):
+        xo, io, _ = ref[q]
+        assert infos[q].success, (q, infos[q])
+        worst_err = worst_rr = 0.0
+        for k, sg in enumerate(SHIFTS):
+            err = float(np.linalg.norm(Xh[q, k] - xo[k]) / np.linalg.norm(xo[k]))
+            r = B[q] - O.apply(op, Xh[q, k]) - sg * Xh[q, k]
+            rr = float(np.linalg.norm(r) / np.linalg.norm(B[q]))
+            worst_err, worst_rr = max(worst_err, err), max(worst_rr, rr)
+            assert rr < 1e-10, (q, k, rr)
+            assert err < 1e-9, (q, k, err)
+            assert np.sqrt(infos[q].resSqmrhs[k]) / np.linalg.norm(B[q]) < 1e-10, (q, k)
+        print(f"mixed multishift 512^2 source {q}: {infos[q].iter} FP32 multishift iterations, "
+              f"{infos[q].ops_count} operator applications in all, worst shift err vs oracle {worst_err:.3e}, "
+              f"worst relres {worst_rr:.3e}")
