@@ -288,17 +288,24 @@ def workload_multishift(args):
     import numpy as np
     import torch
     gl = importlib.import_module("generic-linalg_gb300")
+    replicas = importlib.import_module("generic-linalg_gb300.replicas")
+    rank, world, local = dist_setup()
     L = gl.lib()
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
     lx = ly = 512
     mass = 0.05
-    n_rhs, shifts = 64, np.logspace(-4, 0, 12)
+    n_all, shifts = args.sources, np.logspace(-4, 0, 12)
     g = gl.Generator(SEED)
     U = g.rand_gauge_u1(lx, ly)
-    B = np.stack([g.gaussian(lx * ly) for _ in range(n_rhs)])
+    B_all = np.stack([g.gaussian(lx * ly) for _ in range(n_all)])
+    # under torchrun every rank takes an equal share of the sources (no collective on the data
+    # path); source 0 stays on rank 0, where the oracle checks it
+    mine = replicas.my_share([1.0] * n_all, rank, world)
+    B = B_all[mine]
+    n_rhs = len(mine)
     op = gl.Operator(2, lx, ly, mass, torch.from_numpy(U).to(dev))
     Bd = torch.from_numpy(B).to(dev)
     X = torch.zeros((n_rhs, len(shifts), lx * ly), dtype=torch.complex128, device=dev)
@@ -310,16 +317,18 @@ def workload_multishift(args):
         return float(torch.linalg.vector_norm(Bd[q] - Ax - sg * xq) / torch.linalg.vector_norm(Bd[q]))
 
     out, sol0 = {}, {}
-    for name, prec in (("fp64", 0), ("fp32", 1)):
+    for name, prec in [v for v in (("fp64", 0), ("fp32", 1)) if v[0] in args.ms_variants.split(",")]:
         res = {}
         for nr in (1, n_rhs):
             for i in range(args.warmup + args.steps):
                 X.zero_()
+                if world > 1:
+                    torch.distributed.barrier()
                 t, infos = _flush_and_time(
                     lambda: gl.cg_m_multi(op, X[:nr], Bd[:nr], shifts, 1, 100000, 1e-10, precision=prec),
                     flush, stream)
                 if i >= args.warmup:
-                    res.setdefault(nr, []).append(t)
+                    res.setdefault(nr, []).append(replicas.max_over_ranks(t, world, dev) if nr == n_rhs else t)
             assert all(inf.success for inf in infos), (name, infos)
             res[f"info{nr}"] = infos
         i64 = res[f"info{n_rhs}"]
@@ -327,24 +336,34 @@ def workload_multishift(args):
         worst = max(true_relres(X[q, k], q, sg) for q in (0, n_rhs - 1) for k, sg in enumerate(shifts))
         sol0[name] = X[0].cpu().numpy().copy()
         out[name] = {"one_source_ms": round(statistics.mean(res[1]), 3), "one_source_iters": res["info1"][0].iter,
+                     "batched_multishift_phase_ms": round(i64[0].kernel_ms, 3) if prec else None,
                      "batched_ms": round(ms64, 3), "batched_ms_per_source": round(ms64 / n_rhs, 3),
                      "batched_iters_min_max": [min(i.iter for i in i64), max(i.iter for i in i64)],
                      "operator_applications_per_source_mean": round(statistics.mean(i.ops_count for i in i64), 1),
                      "batched_algorithmic_GBps": round(sum(i.gbytes for i in i64) / (ms64 * 1e-3), 1),
                      "max_shift_true_relres_sources_0_and_63": worst}
-    # the same 64 sources, one single-source FP64 solve after another
-    xs = [torch.zeros(lx * ly, dtype=torch.complex128, device=dev) for _ in shifts]
+    # the same 64 sources, one single-source FP64 solve after another (one GPU)
+    t_seq = None
+    if world == 1 and not args.no_one_by_one:
+        xs = [torch.zeros(lx * ly, dtype=torch.complex128, device=dev) for _ in shifts]
 
-    def one_by_one():
-        for q in range(n_rhs):
-            gl.minv_vector_cg_m(xs, Bd[q], len(shifts), lx * ly, 1, 100000, 1e-10, shifts.copy(),
-                                gl.square_staggered_normal_u1, op)
-    t_seq, _ = _flush_and_time(one_by_one, flush, stream)
+        def one_by_one():
+            for q in range(n_rhs):
+                gl.minv_vector_cg_m(xs, Bd[q], len(shifts), lx * ly, 1, 100000, 1e-10, shifts.copy(),
+                                    gl.square_staggered_normal_u1, op)
+        t_seq, _ = _flush_and_time(one_by_one, flush, stream)
+    if rank != 0:
+        torch.distributed.destroy_process_group()
+        return
     line = {"workload": "multishift CG, staggered normal equations 512x512, m=0.05, 12 shifts logspace[1e-4,1], tol 1e-10",
             "steps": args.steps, "warmup": args.warmup, "l2": "flushed (512 MiB write) before every solve",
-            "sources": n_rhs, "variants": out, "fp64_one_by_one_ms": round(t_seq, 3),
-            "mixed_speedup_vs_fp64_batched": round(out["fp64"]["batched_ms"] / out["fp32"]["batched_ms"], 2),
-            "mixed_speedup_vs_fp64_one_by_one": round(t_seq / out["fp32"]["batched_ms"], 2)}
+            "sources": n_all, "n_gpus": world, "scaling": "strong",
+            "parallelism": f"replicas x{world} (sources shared out, no collective on the data path)",
+            "variants": out, "fp64_one_by_one_ms": round(t_seq, 3) if t_seq else None,
+            "mixed_speedup_vs_fp64_batched": (round(out["fp64"]["batched_ms"] / out["fp32"]["batched_ms"], 2)
+                                              if len(out) == 2 else None),
+            "mixed_speedup_vs_fp64_one_by_one": (round(t_seq / out["fp32"]["batched_ms"], 2)
+                                                 if t_seq and "fp32" in out else None)}
     if not args.no_cpu_baseline:
         # the oracle's CG-M (the reference's recurrence, site loops on every host core) on source 0:
         # one complete solve, and every variant's source-0 solutions against it
@@ -359,68 +378,107 @@ def workload_multishift(args):
         for name in out:
             out[name]["source0_max_shift_err_vs_oracle"] = float(max(
                 np.linalg.norm(sol0[name][k] - xo[k]) / np.linalg.norm(xo[k]) for k in range(len(shifts))))
-        line["cpu_baseline"] = {"value": round(dt * 1e3 * n_rhs, 1), "unit": "ms (64 sources)", "cores": nth,
+        line["cpu_baseline"] = {"value": round(dt * 1e3 * n_all, 1), "unit": "ms (64 sources)", "cores": nth,
                                 "kind": "port",
                                 "sample": f"one complete CG-M solve of source 0 ({io['iter']} iterations, "
                                           f"{dt:.2f} s on {nth} threads) times 64 sources"}
     print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def dist_setup():
+    """(rank, world, local rank) from torchrun's environment; the NCCL process group is made
+    only for more than one rank (the systems are shared out, no collective on the data path)."""
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        if not dist.is_initialized():
+            dist.init_process_group("nccl")
+    return rank, world, local
 
 
 def workload_batch(args):
     """256 independent systems in one batch: sides from {32, 64, 128, 256}, links U(1) random,
     masses log-uniform in [0.01, 0.5]; even systems staggered D^dagger D (mass m), odd systems
     the gauge Laplacian (mass m^2); FP32 inner iterations with FP64 reliable updates, tolerance
-    1e-10.  One batched call (glinalg_cg_batch) against one mixed solve per system."""
+    1e-10.  One batched call (glinalg_cg_batch) against one mixed solve per system.  Under
+    torchrun every rank solves its share (replicas.shard_by_cost, cost = sites / mass, about
+    sites x sqrt(kappa)) in one batched call; the job's time is the slowest rank's."""
     import numpy as np
     import torch
     gl = importlib.import_module("generic-linalg_gb300")
+    replicas = importlib.import_module("generic-linalg_gb300.replicas")
+    rank, world, local = dist_setup()
     L = gl.lib()
-    dev = torch.device("cuda", 0)
+    dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     torch.cuda.set_stream(stream)
     gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
     g = gl.Generator(2024)
     rng = np.random.default_rng(2024)
-    ops, bs, xs, meta = [], [], [], []
-    for q in range(256):
+    meta, host = [], []
+    for q in range(args.systems):
         side = int(rng.choice([32, 64, 128, 256]))
         m = float(np.exp(rng.uniform(np.log(0.01), np.log(0.5))))
         kind = 2 if q % 2 == 0 else 3
         U = g.rand_gauge_u1(side, side)
         b = g.gaussian(side * side)
-        mass = m if kind == 2 else m * m
+        meta.append((kind, side, m if kind == 2 else m * m, m))
+        host.append((U, b))
+    mine = replicas.my_share([side * side / m for _, side, _, m in meta], rank, world)
+    ops, bs, xs = [], [], []
+    for q in mine:
+        kind, side, mass, _ = meta[q]
+        U, b = host[q]
         ops.append(gl.Operator(kind, side, side, mass, torch.from_numpy(U).to(dev)))
         bs.append(torch.from_numpy(b).to(dev))
         xs.append(torch.zeros(side * side, dtype=torch.complex128, device=dev))
-        meta.append((kind, side, mass))
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     times = []
     for i in range(args.warmup + args.steps):
         for x in xs:
             x.zero_()
+        if world > 1:
+            torch.distributed.barrier()
         t, infos = _flush_and_time(lambda: gl.cg_batch(ops, xs, bs, 100000, 1e-10, precision=1), flush, stream)
         if i >= args.warmup:
-            times.append(t)
+            times.append(replicas.max_over_ranks(t, world, dev))
     assert all(inf.success for inf in infos)
+    results = replicas.gather_results({q: (inf.iter, inf.gbytes) for q, inf in zip(mine, infos)}, world)
+    assert sorted(results) == list(range(args.systems))
 
     def one_by_one():
         for q in range(len(ops)):
-            cb = gl.square_staggered_normal_u1 if meta[q][0] == 2 else gl.square_laplace_u1
+            cb = gl.square_staggered_normal_u1 if meta[mine[q]][0] == 2 else gl.square_laplace_u1
             gl.minv_vector_cg(xs[q], bs[q], xs[q].numel(), 100000, 1e-10, cb, ops[q], precision=1)
-    for x in xs:
-        x.zero_()
-    one_by_one()
-    for x in xs:
-        x.zero_()
-    t_seq, _ = _flush_and_time(one_by_one, flush, stream)
+    t_seq = None
+    if world == 1 and not args.no_one_by_one:
+        for x in xs:
+            x.zero_()
+        one_by_one()
+        for x in xs:
+            x.zero_()
+        t_seq, _ = _flush_and_time(one_by_one, flush, stream)
     ms = statistics.mean(times)
-    sites = sum(s * s for _, s, _ in meta)
-    line = {"workload": "256 uneven systems (sides 32..256, half staggered normal, half Laplacian), FP32 inner + FP64 reliable, tol 1e-10",
-            "steps": args.steps, "warmup": args.warmup, "sites": sites, "l2": "flushed (512 MiB write) before every solve",
-            "batched_ms": round(ms, 3), "iters_min_max": [min(i.iter for i in infos), max(i.iter for i in infos)],
-            "one_by_one_ms": round(t_seq, 3), "batch_speedup": round(t_seq / ms, 2),
-            "algorithmic_GBps": round(sum(i.gbytes for i in infos) / (ms * 1e-3), 1)}
-    print(json.dumps(line))
+    sites = sum(s * s for _, s, _, _ in meta)
+    if rank == 0:
+        its = [it for it, _ in results.values()]
+        line = {"workload": f"{args.systems} uneven systems (sides 32..256, half staggered normal, half Laplacian), FP32 inner + FP64 reliable, tol 1e-10",
+                "steps": args.steps, "warmup": args.warmup, "sites": sites, "n_gpus": world,
+                "parallelism": f"replicas x{world} (systems shared out by cost, no collective on the data path)",
+                "scaling": "strong", "l2": "flushed (512 MiB write) before every solve",
+                "batched_ms": round(ms, 3), "iters_min_max": [min(its), max(its)],
+                "one_by_one_ms": round(t_seq, 3) if t_seq else None,
+                "batch_speedup": round(t_seq / ms, 2) if t_seq else None,
+                "algorithmic_GBps": round(sum(gb for _, gb in results.values()) / (ms * 1e-3), 1)}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 def workload_siblings(args):
@@ -658,6 +716,11 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--ref-iters", type=int, default=30)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sources", type=int, default=64, help="multishift workload: sources (64)")
+    ap.add_argument("--ms-variants", default="fp64,fp32", help="multishift workload: fp64 and/or fp32")
+    ap.add_argument("--systems", type=int, default=256, help="batch workload: systems (256)")
+    ap.add_argument("--no-one-by-one", action="store_true",
+                    help="batched workloads: skip the one-call-per-system comparison")
     ap.add_argument("--variants", default="fp32,fp16,bf16,fp64",
                     help="comma list of the variants to time besides the headline (fp32)")
     ap.add_argument("--kernels-only", action="store_true",
@@ -799,6 +862,10 @@ def main():
     hbm_equiv_solve = (cg_bytes * hi_.iter / k_launch / (k_ms_solve * 1e-3) / 1e9) if k_ms_solve > 0 else 0.0
     smem_gbs, smem_ms = C_double(), C_double()
     gl._capi.check(L.glinalg_probe_smem_bandwidth(smem_gbs, smem_ms), "probe_smem_bandwidth")
+    # the probe can not exceed what the SMs' shared-memory ports serve (128 B per clock per SM)
+    n_sm0 = torch.cuda.get_device_properties(dev).multi_processor_count
+    smem_arch = 128.0 * n_sm0 * 2070e6 / 1e9
+    assert smem_gbs.value <= 1.05 * smem_arch, (smem_gbs.value, smem_arch)
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
     Uh = torch.from_numpy(U).pin_memory().numpy()

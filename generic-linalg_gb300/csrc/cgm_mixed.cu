@@ -420,6 +420,8 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     const long total = (long)n_rhs * ns * n;
     k_mx_widen<<<mvec_grid(total), 256, 0, st>>>(X, a.Xs, total);
     GL_CUDA(cudaGetLastError());
+    EventTimer t1;  // the FP32 multishift phase ends here
+    t1.start(st);
     std::vector<MxSrc> hsrc(n_rhs);
     GL_CUDA(cudaMemcpyAsync(hsrc.data(), a.src, sizeof(MxSrc) * n_rhs, cudaMemcpyDeviceToHost, st));
     GL_CUDA(cudaStreamSynchronize(st));
@@ -453,8 +455,9 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     for (auto &v : views) v.U = nullptr;
     GL_TRY(s2);
     tm.stop(st);
+    t1.stop(st);
     GL_CUDA(cudaStreamSynchronize(st));
-    const double ms = tm.ms();
+    const double ms = tm.ms(), ms2 = t1.ms();
     for (int q = 0; q < n_rhs; q++) {
         const MxSrc &h = hsrc[q];
         glinalg_info *info = &infos[q];
@@ -489,7 +492,11 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         // phase 1 per iteration: C r, Ap in, r out (3 words); A r, p in, p', t out, 2 links (6);
         // B t in, Ap out, p' in, 2 links (5); per live shift and iteration x_s, p_s in and out
         // (4); FP32 words
-        info->gbytes = ((double)h.iters * 14.0 + 4.0 * h.shift_updates) * 8.0 * n * 1e-9 + gb;
+        const double gb1 = ((double)h.iters * 14.0 + 4.0 * h.shift_updates) * 8.0 * n * 1e-9;
+        info->gbytes = gb1 + gb;
+        // the FP32 multishift phase of the whole batch (every source), and its bytes for this source
+        info->kernel_ms = ms - ms2;
+        info->kernel_gbytes = gb1;
         fill_name(info, "CG-M-FP32");
     }
     return GLINALG_SUCCESS;

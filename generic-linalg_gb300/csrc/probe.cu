@@ -21,12 +21,14 @@ __global__ void __launch_bounds__(kProbeThreads) k_smem_read(float *sink, int re
         buf[i] = make_float4((float)i, 1.f, 2.f, 3.f);
     __syncthreads();
     float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0;
+    // the kProbeUnroll loads of a pass read kProbeUnroll distinct addresses (offsets k * 256
+    // within the 2048-entry buffer), so none can be merged with another
     unsigned idx = threadIdx.x;
     for (int r = 0; r < reps; r++) {
 #pragma unroll
         for (int k = 0; k < kProbeUnroll; k += 2) {
-            const float4 v = buf[(idx + k * kProbeThreads) & (kProbeElems - 1)];
-            const float4 w = buf[(idx + (k + 1) * kProbeThreads) & (kProbeElems - 1)];
+            const float4 v = buf[(idx + k * (kProbeElems / kProbeUnroll)) & (kProbeElems - 1)];
+            const float4 w = buf[(idx + (k + 1) * (kProbeElems / kProbeUnroll)) & (kProbeElems - 1)];
             a0.x += v.x; a0.y += v.y; a0.z += v.z; a0.w += v.w;
             a1.x += w.x; a1.y += w.y; a1.z += w.z; a1.w += w.w;
         }

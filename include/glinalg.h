@@ -128,8 +128,10 @@ typedef struct glinalg_info {
     double device_ms;    /* device time of the solve, CUDA events */
     double gbytes;       /* algorithmic bytes moved by the solve's kernels, in GB */
     double kernel_ms;    /* mixed CG: device time inside the persistent inner-loop kernel
-                            (device clock, summed over its launches; 0 if it did not run) */
-    double kernel_gbytes;/* algorithmic bytes that kernel moved, in GB */
+                            (device clock, summed over its launches; 0 if it did not run);
+                            mixed multishift: device time of the FP32 multishift phase (all
+                            sources) */
+    double kernel_gbytes;/* algorithmic bytes that kernel (phase, for this source) moved, in GB */
     int kernel_launches; /* its launches */
 } glinalg_info;
 

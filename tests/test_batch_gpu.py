@@ -69,12 +69,15 @@ def test_cg_batch_256_uneven_systems(gl, gpu, oracle):
 
 @pytest.mark.parametrize("kind,rfc,max_iter", [(2, 1, 10000), (3, 3, 10000), (2, 2, 40)])
 def test_cg_m_multi_equals_single_source_solves(gl, gpu, kind, rfc, max_iter):
-    """All sources advanced together give, per source, the single-source CG-M: the same
-    iteration count, op count and status, and solutions within 5e-11 (the batched kernels
-    reduce in the same order as the single-source ones, but the compiler may contract a
-    multiply-add differently; the shifted systems' condition numbers, up to ~1.6e3, amplify
-    those last-bit differences to ~1e-11).  The explicit residuals are
-    dominated by rounding at 1e-10, so they are checked against the tolerance, not bitwise.
+    """All sources advanced together give, per source, the single-source CG-M: the same status,
+    the iteration and op counts within one, and solutions within 5e-11 where the counts agree
+    (the batched kernels reduce in the same order as the single-source ones, but the compiler
+    may contract a multiply-add differently; the shifted systems' condition numbers, up to
+    ~1.6e3, amplify those last-bit differences to ~1e-11, and now and then move the stop by
+    one iteration).  A source that stops one iteration apart is held to 2 kappa 1e-10 per
+    shift, the bound any two solutions with relative residual below 1e-10 meet (kappa of
+    A + sigma from the operator's spectral bounds).  The explicit residuals are dominated by
+    rounding at 1e-10, so they are checked against the tolerance, not bitwise.
     Twelve shifts log-spaced over [1e-4, 1] as in the 512^2 multishift workload, on 64x48;
     max_iter = 40 stops every source early."""
     lx, ly = 64, 48
@@ -92,11 +95,17 @@ def test_cg_m_multi_equals_single_source_solves(gl, gpu, kind, rfc, max_iter):
     for q in range(n_rhs):
         xs = [np.zeros(lx * ly, np.complex128) for _ in shifts]
         inf = gl.minv_vector_cg_m(xs, B[q], len(shifts), lx * ly, rfc, max_iter, 1e-10, shifts.copy(), cb, op)
-        assert (infos[q].iter, infos[q].ops_count, infos[q].success) == (inf.iter, inf.ops_count, inf.success)
+        assert abs(infos[q].iter - inf.iter) <= 1 and abs(infos[q].ops_count - inf.ops_count) <= 1
+        assert infos[q].success == inf.success
         assert infos[q].success == (max_iter == 10000)
         iters.add(inf.iter)
         for j in range(len(shifts)):
-            assert rel(X[q, j], xs[j]) < 5e-11, (q, j)
+            if infos[q].iter == inf.iter:
+                assert rel(X[q, j], xs[j]) < 5e-11, (q, j)
+            else:
+                lo, hi = (mass * mass, mass * mass + 4) if kind == 2 else (mass, mass + 8)
+                kappa = (hi + shifts[j]) / (lo + shifts[j])
+                assert rel(X[q, j], xs[j]) < 2 * kappa * 1e-10, (q, j)
         bn = np.linalg.norm(B[q])
         rb, rs = np.sqrt(infos[q].resSqmrhs) / bn, np.sqrt(inf.resSqmrhs) / bn
         if max_iter == 10000:
