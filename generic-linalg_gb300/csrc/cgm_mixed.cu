@@ -2,24 +2,34 @@
 // precision (glinalg_cg_m_multi with precision GLINALG_PREC_SINGLE).
 //
 // Phase 1: the multishift recurrence of generic_cg_m.cpp:312-600 for every source at once,
-// with the vectors (r, p, A p, every shift's p_s and x_s) and the operator in FP32 and the
-// scalar recurrences (beta, alpha, zeta_s, beta_s, alpha_s: complex, as in the reference) in
-// FP64.  FP32 shifted solutions stop improving once their true residuals reach about 1e-7 of
-// |b|: the base residual is updated with an FP32 operator, and every rounding of that update
-// is missing from the shifted solutions, which the recurrence never recomputes.  So phase 1
-// stops each shift at max(eps, kPhase1Tol).
+// with the base vectors (r, p, A p) and the operator in FP32, the scalar recurrences (beta,
+// alpha, zeta_s, beta_s, alpha_s: complex, as in the reference) in FP64, and the shifted
+// solutions x_s accumulated in FP64.  FP32 shifted solutions stop improving once their true
+// residuals reach 1e-5..1e-6 of |b| (the rounding of the FP32 updates never enters them; the
+// recurrence does not recompute them), so phase 1 stops each shift at max(eps, kPhase1Tol).
 // Phase 2: every (source, shift) system is refined from its phase-1 solution by the mixed CG
 // with FP64 reliable updates (cg_batch_mixed: all systems advanced together) to the FP64-true
 // relative residual eps.  D^dagger D + sigma with mass m is exactly D^dagger D with mass
 // sqrt(m^2 + sigma) (D = m + D_hop with D_hop anti-Hermitian, so D^dagger D = m^2 +
 // D_hop^dagger D_hop), so each shifted system is a staggered normal system of its own mass.
 //
+// Blocked shift updates.  Each shift's direction and solution change by
+//   x_s -= beta_s p_s;  p_s = zeta_s r + alpha_s p_s
+// every iteration, so within a block of kBlk iterations starting at k0 both are linear
+// combinations of p_s(k0) and the base residuals r(k0+1) .. r(k0+kBlk) with scalar
+// coefficients.  Phase 1 keeps the last kBlk + 1 residuals in a ring, updates only the FP64
+// coefficients each iteration (one warp per source, lane = basis vector), and every kBlk
+// iterations (or when the source stops) writes x_s and p_s once, in one pass (k_mx_F).  The
+// per-iteration shift traffic drops from 4 complex words per live shift to about
+// (kBlk + 6 live) / kBlk, and x_s is summed in FP64 at no FP64-pipe cost.
+//
 // Phase-1 kernels, for all sources at once (grid.y = source), mirroring cgm_batch.cu:
-//   C  r += beta Ap and |r|^2; in the source's last block: retire converged shifts, alpha,
-//      alpha_s
-//   A  x_s -= beta_s p_s, p_s = zeta_s r + alpha_s p_s, p' = r + alpha p, then t = D p'
+//   C  r(k+1) = r(k) + beta Ap into the ring and |r|^2; in the source's last block: retire
+//      converged shifts, alpha, alpha_s, then the shifts' coefficients
+//   F  at a block's end: x_s += X_s . basis (FP64), p_s = P_s . basis (FP32)
+//   A  p' = r + alpha p, then t = D p'
 //   B  Ap = D^dagger t and <p', Ap>; in the source's last block: beta, zeta_s, beta_s
-//   tail: sources that stopped in this pass are marked finished; all finished ends the loop.
+//   tail: sources that stopped (and flushed) are marked finished; all finished ends the loop.
 // Sums: FP32 per thread, FP64 across threads and blocks.  The operator uses a FP32 hopping
 // table with the 1/2 and eta(x) folded in (exact: powers of two and signs).
 
@@ -33,8 +43,11 @@ namespace glinalg {
 namespace {
 
 constexpr int kMaxMixShifts = 32;
-// Phase-1 target: the FP32 shifted solutions' true residuals level off near 1e-7 |b|.
+// Phase-1 target: the FP32 shifted solutions' true residuals level off at 1e-5..1e-6 |b|.
 constexpr double kPhase1Tol = 1e-6;
+constexpr int kBlk = 16;         // iterations per block of shift updates
+constexpr int kNB = kBlk + 1;    // basis: p_s at the block's start, then r(k0+1) .. r(k0+kBlk)
+constexpr int kRing = kBlk + 1;  // residuals kept: r(k) is in slot k % kRing
 
 int mvec_grid(long n)
 {
@@ -46,7 +59,11 @@ struct MxSrc {  // scalar state of one source (FP64)
     double2 alpha, beta;
     double rsq, bsq;
     int k, done, status, iters, napply, n_rem, n_rem_before, shift_updates;
-    unsigned cnt[2];
+    int k0;         // first iteration of the current block of shift updates
+    int kr;         // the last residual in the ring is r(kr)
+    int flush;      // 1: k_mx_F writes x_s and p_s in this pass
+    int nflush;     // flushes done (bytes accounting)
+    unsigned cnt[3];
 };
 
 struct MxArgs {
@@ -54,8 +71,12 @@ struct MxArgs {
     double2 *zeta, *zeta_prev, *beta_s, *alpha_s;  // [q * ns + slot]
     double *shifts;                                 // [q * ns + slot], permuted with the slots
     int *map;                                       // [q * ns + slot] -> caller's shift index
-    float2 *Xs, *Ps;                                // [(q * ns + j) * n], j = caller's index
-    float2 *r, *p0, *p1, *t, *Ap;                   // [q * n]
+    int *state;                                     // [q * ns + j]: 0 live, 1 retired, 2 written out
+    double2 *Pc, *Xc;                               // [(q * ns + j) * kNB]: coefficients of p_s, dx_s
+    double2 *X;                                     // [(q * ns + j) * n]: the caller's FP64 solutions
+    float2 *Ps;                                     // [(q * ns + j) * n]: p_s at the block's start
+    float2 *R;                                      // [(q * kRing + slot) * n]: the residual ring
+    float2 *p0, *p1, *t, *Ap;                       // [q * n]
     const double2 *b;                               // [q * n]
     const float2 *H;                                // [2 i]: 1/2 U_x(i), 1/2 eta(x) U_y(i)
     double *partials;                               // [q * 2 * gridDim.x]
@@ -71,6 +92,11 @@ __device__ __forceinline__ float2 f2(double2 v) { return make_float2((float)v.x,
 __device__ __forceinline__ double *mrow_partials(const MxArgs &a, int q)
 {
     return a.partials + (size_t)q * 2 * gridDim.x;
+}
+
+__device__ __forceinline__ float2 *ring(const MxArgs &a, int q, int k)
+{
+    return a.R + ((size_t)q * kRing + (k % kRing)) * a.n;
 }
 
 // hs = H_x f(x+1) - H_x(x-1)^* f(x-1) + H_y f(y+1) - H_y(y-1)^* f(y-1): D f = m f - hs,
@@ -108,6 +134,7 @@ __device__ void mx_beta_scalars(const MxArgs &a, MxSrc *s, int q, double re, dou
         s->n_rem_before = 0;
         s->status = GLINALG_SOLVE_BREAKDOWN;
         s->done = 1;
+        s->flush = 1;  // write out what this block accumulated
         return;
     }
     const double2 beta_prev = s->beta;
@@ -131,107 +158,192 @@ __device__ void mx_beta_scalars(const MxArgs &a, MxSrc *s, int q, double re, dou
     s->shift_updates += s->n_rem;
 }
 
-// C: r += beta Ap, |r|^2, then the source's bookkeeping (generic_cg_m.cpp:424-513).
+// C: r(k+1) = r(k) + beta Ap into the ring, |r|^2, then the source's bookkeeping
+// (generic_cg_m.cpp:424-513) and, on warp 0 of the last block, the shifts' coefficients:
+//   x_s -= beta_s p_s  for the shifts live when beta_s was formed,
+//   p_s = zeta_s r(k+1) + alpha_s p_s  for the shifts still live.
 __global__ void __launch_bounds__(kRedThreads) k_mx_C(MxArgs a)
 {
     const int q = blockIdx.y;
     MxSrc *s = a.src + q;
     if (s->done) return;
+    __shared__ int sh_nb, sh_na, sh_idx;
     const long n = a.n;
-    float2 *r = a.r + q * n;
+    const int k = s->k;
+    const float2 *r = ring(a, q, k);
+    float2 *rn_v = ring(a, q, k + 1);
     const float2 *Ap = a.Ap + q * n;
     const float2 bt = f2(s->beta);
     float vf = 0.f;
     for (long i = blockIdx.x * (long)kRedThreads + threadIdx.x; i < n; i += (long)gridDim.x * kRedThreads) {
         const float2 ri = fadd(r[i], fmul(bt, Ap[i]));
-        r[i] = ri;
+        rn_v[i] = ri;
         vf += fn2(ri);
     }
     double v[1] = {(double)vf};
-    if (!(grid_sum_row<1, kRedThreads>(v, mrow_partials(a, q), &s->cnt[1]) && threadIdx.x == 0)) return;
-    const double rn = v[0];
-    const int k = s->k;
-    const double bsqrt = sqrt(s->bsq), srn = sqrt(rn);
-    const int o = q * a.ns;
-    if (k % a.rfc == 0) {
-        for (int j = 0; j < s->n_rem; j++) {
-            if (cabsd(a.zeta[o + j]) * srn < a.eps * bsqrt) {
-                s->n_rem--;
-                const int e = s->n_rem;
-                if (e != j) {
-                    int ti = a.map[o + e]; a.map[o + e] = a.map[o + j]; a.map[o + j] = ti;
-                    double2 tc;
-                    tc = a.alpha_s[o + e]; a.alpha_s[o + e] = a.alpha_s[o + j]; a.alpha_s[o + j] = tc;
-                    tc = a.beta_s[o + e]; a.beta_s[o + e] = a.beta_s[o + j]; a.beta_s[o + j] = tc;
-                    tc = a.zeta[o + e]; a.zeta[o + e] = a.zeta[o + j]; a.zeta[o + j] = tc;
-                    tc = a.zeta_prev[o + e]; a.zeta_prev[o + e] = a.zeta_prev[o + j]; a.zeta_prev[o + j] = tc;
-                    double td = a.shifts[o + e]; a.shifts[o + e] = a.shifts[o + j]; a.shifts[o + j] = td;
-                    j--;
+    if (!grid_sum_row<1, kRedThreads>(v, mrow_partials(a, q), &s->cnt[1])) return;
+    // the last block of this source: all of its threads are here
+    if (threadIdx.x == 0) {
+        const double rn = v[0];
+        const double bsqrt = sqrt(s->bsq), srn = sqrt(rn);
+        const int o = q * a.ns;
+        const int nb = s->n_rem_before;
+        if (k % a.rfc == 0) {
+            for (int j = 0; j < s->n_rem; j++) {
+                if (cabsd(a.zeta[o + j]) * srn < a.eps * bsqrt) {
+                    s->n_rem--;
+                    const int e = s->n_rem;
+                    a.state[o + a.map[o + j]] = 1;
+                    if (e != j) {
+                        int ti = a.map[o + e]; a.map[o + e] = a.map[o + j]; a.map[o + j] = ti;
+                        double2 tc;
+                        tc = a.alpha_s[o + e]; a.alpha_s[o + e] = a.alpha_s[o + j]; a.alpha_s[o + j] = tc;
+                        tc = a.beta_s[o + e]; a.beta_s[o + e] = a.beta_s[o + j]; a.beta_s[o + j] = tc;
+                        tc = a.zeta[o + e]; a.zeta[o + e] = a.zeta[o + j]; a.zeta[o + j] = tc;
+                        tc = a.zeta_prev[o + e]; a.zeta_prev[o + e] = a.zeta_prev[o + j]; a.zeta_prev[o + j] = tc;
+                        double td = a.shifts[o + e]; a.shifts[o + e] = a.shifts[o + j]; a.shifts[o + j] = td;
+                        j--;
+                    }
                 }
             }
         }
+        const bool last = (k == a.max_iter - 1);
+        int na = 0;
+        if (!isfinite(rn)) {
+            s->iters = k + 1;
+            s->status = GLINALG_SOLVE_NONFINITE;
+            s->done = 1;
+        } else if (s->n_rem == 0 || last) {
+            s->iters = k + 1;
+            s->status = last ? GLINALG_SOLVE_MAX_ITER : GLINALG_SOLVE_CONVERGED;
+            s->done = 1;
+        } else {
+            const double2 alpha = cmk(rn / s->rsq, 0.0);
+            s->alpha = alpha;
+            s->rsq = rn;
+            for (int j = 0; j < s->n_rem; j++)
+                a.alpha_s[o + j] =
+                    cdiv(cmul(cmul(alpha, a.zeta[o + j]), a.beta_s[o + j]), cmul(a.zeta_prev[o + j], s->beta));
+            s->k = k + 1;
+            s->napply++;
+            na = s->n_rem;
+        }
+        const int idx = k + 1 - s->k0;  // basis index of r(k+1)
+        s->kr = k + 1;
+        if (s->done || idx == kBlk) s->flush = 1;
+        sh_nb = nb;
+        sh_na = na;
+        sh_idx = idx;
     }
-    const bool last = (k == a.max_iter - 1);
-    if (!isfinite(rn)) {
-        s->iters = k + 1;
-        s->status = GLINALG_SOLVE_NONFINITE;
-        s->done = 1;
-        return;
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    // warp 0: lane l updates basis coefficient l of every shift
+    const int l = threadIdx.x, o = q * a.ns;
+    const int nb = sh_nb, na = sh_na, idx = sh_idx;
+    if (l >= kNB) return;
+    for (int j = 0; j < nb; j++) {
+        const size_t c = (size_t)(o + a.map[o + j]) * kNB + l;
+        const double2 pc = a.Pc[c];
+        a.Xc[c] = csub(a.Xc[c], cmul(a.beta_s[o + j], pc));
+        if (j < na) a.Pc[c] = cadd(cmul(a.alpha_s[o + j], pc), l == idx ? a.zeta[o + j] : cmk(0.0, 0.0));
     }
-    if (s->n_rem == 0 || last) {
-        s->iters = k + 1;
-        s->status = last ? GLINALG_SOLVE_MAX_ITER : GLINALG_SOLVE_CONVERGED;
-        s->done = 1;
-        return;
-    }
-    const double2 alpha = cmk(rn / s->rsq, 0.0);
-    s->alpha = alpha;
-    s->rsq = rn;
-    for (int j = 0; j < s->n_rem; j++)
-        a.alpha_s[o + j] = cdiv(cmul(cmul(alpha, a.zeta[o + j]), a.beta_s[o + j]), cmul(a.zeta_prev[o + j], s->beta));
-    s->k = k + 1;
-    s->napply++;
 }
 
-// A: shift updates and p' = r + alpha p at every site of the source, then t = D p'.
-// setup = 1: p' = p0 as stored (the source), no shift updates.
+// F: at the end of a block (or of the source), for every shift not yet written out:
+//   x_s += sum_l X_s[l] basis_l (summed in FP32, added in FP64), and for live shifts
+//   p_s = sum_l P_s[l] basis_l, with basis_0 = p_s at the block's start and basis_l = r(k0+l).
+// The source's last block then resets the coefficients for the next block.
+__global__ void __launch_bounds__(kRedThreads) k_mx_F(MxArgs a)
+{
+    const int q = blockIdx.y;
+    MxSrc *s = a.src + q;
+    if (s->done == 2 || !s->flush) return;
+    __shared__ float2 cx[kMaxMixShifts][kNB], cp[kMaxMixShifts][kNB];
+    __shared__ int jl[kMaxMixShifts], live[kMaxMixShifts];
+    __shared__ int nj, ticket;
+    const long n = a.n;
+    const int o = q * a.ns;
+    const int k0 = s->k0;
+    // basis vectors used: r(k0+1) .. r(kend), the residuals of this block in the ring
+    const int kend = s->kr;
+    const int nbv = min(kend - k0, kBlk);
+    if (threadIdx.x == 0) {
+        int m = 0;
+        for (int j = 0; j < a.ns; j++) {
+            const int st = a.state[o + j];
+            if (st == 2) continue;
+            jl[m] = j;
+            live[m] = st == 0 && !s->done;
+            m++;
+        }
+        nj = m;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nj * kNB; e += kRedThreads) {
+        const int m = e / kNB, l = e % kNB;
+        const size_t c = (size_t)(o + jl[m]) * kNB + l;
+        cx[m][l] = f2(a.Xc[c]);
+        cp[m][l] = f2(a.Pc[c]);
+    }
+    __syncthreads();
+    for (long i = blockIdx.x * (long)kRedThreads + threadIdx.x; i < n; i += (long)gridDim.x * kRedThreads) {
+        float2 rv[kBlk];
+#pragma unroll
+        for (int l = 0; l < kBlk; l++) rv[l] = l < nbv ? ring(a, q, k0 + 1 + l)[i] : make_float2(0.f, 0.f);
+        for (int m = 0; m < nj; m++) {
+            const size_t f = (size_t)(o + jl[m]) * n + i;
+            const float2 p0 = a.Ps[f];
+            float2 dx = fmul(cx[m][0], p0), pn = fmul(cp[m][0], p0);
+#pragma unroll
+            for (int l = 0; l < kBlk; l++) {
+                dx = fadd(dx, fmul(cx[m][l + 1], rv[l]));
+                pn = fadd(pn, fmul(cp[m][l + 1], rv[l]));
+            }
+            const double2 xo = a.X[f];
+            a.X[f] = make_double2(xo.x + (double)dx.x, xo.y + (double)dx.y);
+            if (live[m]) a.Ps[f] = pn;
+        }
+    }
+    // the last block to finish resets the coefficients and opens the next block
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        ticket = atomicAdd(&s->cnt[2], 1u);
+    }
+    __syncthreads();
+    if (ticket != gridDim.x - 1) return;
+    __threadfence();
+    for (int e = threadIdx.x; e < nj * kNB; e += kRedThreads) {
+        const int m = e / kNB, l = e % kNB;
+        const size_t c = (size_t)(o + jl[m]) * kNB + l;
+        a.Xc[c] = cmk(0.0, 0.0);
+        a.Pc[c] = cmk(l == 0 ? 1.0 : 0.0, 0.0);
+    }
+    if (threadIdx.x == 0) {
+        for (int m = 0; m < nj; m++)
+            if (!live[m]) a.state[o + jl[m]] = 2;
+        s->k0 = kend;
+        s->flush = 0;
+        s->nflush++;
+        s->cnt[2] = 0;
+    }
+}
+
+// A: p' = r + alpha p at every site of the source, then t = D p'.
+// setup = 1: p' = p0 as stored (the source).
 __global__ void __launch_bounds__(kRedThreads) k_mx_A(MxArgs a, int setup)
 {
     const int q = blockIdx.y;
     MxSrc *s = a.src + q;
-    const int done = s->done;
-    if (done == 2) return;
-    __shared__ float2 sb[kMaxMixShifts], sz[kMaxMixShifts], sa[kMaxMixShifts];
-    __shared__ long soff[kMaxMixShifts];
-    const int nb = setup ? 0 : s->n_rem_before;
-    const int na = done ? 0 : s->n_rem;
+    if (s->done) return;
     const long n = a.n;
-    for (int j = threadIdx.x; j < nb; j += kRedThreads) {
-        const int o = q * a.ns + j;
-        sb[j] = f2(a.beta_s[o]);
-        sz[j] = f2(a.zeta[o]);
-        sa[j] = f2(a.alpha_s[o]);
-        soff[j] = ((long)q * a.ns + a.map[o]) * n;
-    }
-    __syncthreads();
     const int k = s->k;
     const float2 alpha = f2(s->alpha);
-    const float2 *r = a.r + q * n;
+    const float2 *r = ring(a, q, k);
     const float2 *pold = ((k & 1) ? a.p0 : a.p1) + q * n;
     float2 *pnew = ((k & 1) ? a.p1 : a.p0) + q * n;
     const float mass = a.mass;
     for (long i = blockIdx.x * (long)kRedThreads + threadIdx.x; i < n; i += (long)gridDim.x * kRedThreads) {
-        if (nb) {
-            const float2 ri = r[i];
-            for (int j = 0; j < nb; j++) {
-                float2 *xs = a.Xs + soff[j];
-                float2 *ps = a.Ps + soff[j];
-                const float2 pv = ps[i];
-                xs[i] = fsub(xs[i], fmul(sb[j], pv));
-                if (j < na) ps[i] = fadd(fmul(sz[j], ri), fmul(sa[j], pv));
-            }
-        }
-        if (done) continue;  // the source stopped: final solution update only
         float2 pc;
         float2 hs;
         if (setup) {
@@ -272,13 +384,15 @@ __global__ void __launch_bounds__(kRedThreads) k_mx_B(MxArgs a)
         mx_beta_scalars(a, s, q, v[0], v[1]);
 }
 
+// Sources that stopped and have written their shifts out are finished; all finished ends the
+// loop.
 __global__ void k_mx_tail(MxArgs a)
 {
     if (threadIdx.x != 0) return;
     int fin = 0;
     for (int q = 0; q < a.nrhs; q++) {
         MxSrc *s = a.src + q;
-        if (s->done == 1) s->done = 2;
+        if (s->done == 1 && !s->flush) s->done = 2;
         fin += s->done == 2;
     }
     if (fin == a.nrhs) *a.all_done = 1;
@@ -300,28 +414,20 @@ __global__ void __launch_bounds__(kRedThreads) k_mx_norms(MxArgs a)
     }
 }
 
-// x_s = 0, p_s = b, r = p = b (generic_cg_m.cpp:372-391), in FP32
+// x_s = 0 (FP64), p_s = b, r(0) = p = b (FP32) (generic_cg_m.cpp:372-391)
 __global__ void k_mx_init(MxArgs a)
 {
     const int q = blockIdx.y;
     const long n = a.n;
+    float2 *r0 = ring(a, q, 0);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const float2 bi = f2(a.b[q * n + i]);
         for (int j = 0; j < a.ns; j++) {
-            a.Xs[((long)q * a.ns + j) * n + i] = make_float2(0.f, 0.f);
+            a.X[((long)q * a.ns + j) * n + i] = make_double2(0.0, 0.0);
             a.Ps[((long)q * a.ns + j) * n + i] = bi;
         }
-        a.r[q * n + i] = bi;
+        r0[i] = bi;
         a.p0[q * n + i] = bi;
-    }
-}
-
-// X (FP64, the caller's) = Xs (FP32), for every source and shift
-__global__ void k_mx_widen(double2 *__restrict__ X, const float2 *__restrict__ Xs, long total)
-{
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-        const float2 v = Xs[i];
-        X[i] = make_double2((double)v.x, (double)v.y);
     }
 }
 
@@ -348,9 +454,11 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     GL_TRY(sc.alloc(&a.alpha_s, (size_t)n_rhs * ns));
     GL_TRY(sc.alloc(&a.shifts, (size_t)n_rhs * ns));
     GL_TRY(sc.alloc(&a.map, (size_t)n_rhs * ns));
-    GL_TRY(sc.alloc(&a.Xs, (size_t)n_rhs * ns * n));
     GL_TRY(sc.alloc(&a.Ps, (size_t)n_rhs * ns * n));
-    GL_TRY(sc.alloc(&a.r, (size_t)n_rhs * n));
+    GL_TRY(sc.alloc(&a.R, (size_t)n_rhs * kRing * n));
+    GL_TRY(sc.zeros(&a.state, (size_t)n_rhs * ns));
+    GL_TRY(sc.zeros(&a.Xc, (size_t)n_rhs * ns * kNB));
+    GL_TRY(sc.alloc(&a.Pc, (size_t)n_rhs * ns * kNB));
     GL_TRY(sc.alloc(&a.p0, (size_t)n_rhs * n));
     GL_TRY(sc.alloc(&a.p1, (size_t)n_rhs * n));
     GL_TRY(sc.alloc(&a.Ap, (size_t)n_rhs * n));
@@ -375,6 +483,9 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         GL_CUDA(cudaMemcpyAsync(a.alpha_s, zeros.data(), sizeof(double2) * zeros.size(), cudaMemcpyHostToDevice, st));
         GL_CUDA(cudaMemcpyAsync(a.shifts, hs.data(), sizeof(double) * hs.size(), cudaMemcpyHostToDevice, st));
         GL_CUDA(cudaMemcpyAsync(a.map, hm.data(), sizeof(int) * hm.size(), cudaMemcpyHostToDevice, st));
+        std::vector<double2> pc((size_t)n_rhs * ns * kNB, cmk(0.0, 0.0));
+        for (size_t c = 0; c < pc.size(); c += kNB) pc[c] = cmk(1.0, 0.0);
+        GL_CUDA(cudaMemcpyAsync(a.Pc, pc.data(), sizeof(double2) * pc.size(), cudaMemcpyHostToDevice, st));
         std::vector<MxSrc> hsrc(n_rhs);
         for (auto &s : hsrc) {
             s = MxSrc{};
@@ -385,6 +496,7 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         GL_CUDA(cudaMemcpyAsync(a.src, hsrc.data(), sizeof(MxSrc) * n_rhs, cudaMemcpyHostToDevice, st));
     }
     a.b = B;
+    a.X = X;
     a.mass = (float)op->mass;
     a.eps = std::max(eps, kPhase1Tol);
     a.lx = op->lx;
@@ -410,6 +522,7 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         GL_CUDA(cudaGetLastError());
         GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
             k_mx_C<<<rg, kRedThreads, 0, cs>>>(a);
+            k_mx_F<<<rg, kRedThreads, 0, cs>>>(a);
             k_mx_A<<<rg, kRedThreads, 0, cs>>>(a, 0);
             k_mx_B<<<rg, kRedThreads, 0, cs>>>(a);
             k_mx_tail<<<1, 32, 0, cs>>>(a);
@@ -417,9 +530,6 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
             return GLINALG_SUCCESS;
         }));
     }
-    const long total = (long)n_rhs * ns * n;
-    k_mx_widen<<<mvec_grid(total), 256, 0, st>>>(X, a.Xs, total);
-    GL_CUDA(cudaGetLastError());
     EventTimer t1;  // the FP32 multishift phase ends here
     t1.start(st);
     std::vector<MxSrc> hsrc(n_rhs);
@@ -489,10 +599,11 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         info->status = status;
         info->reliable_updates = rel;
         info->device_ms = ms;
-        // phase 1 per iteration: C r, Ap in, r out (3 words); A r, p in, p', t out, 2 links (6);
-        // B t in, Ap out, p' in, 2 links (5); per live shift and iteration x_s, p_s in and out
-        // (4); FP32 words
-        const double gb1 = ((double)h.iters * 14.0 + 4.0 * h.shift_updates) * 8.0 * n * 1e-9;
+        // phase 1 per iteration: C r, Ap in, r out (3 FP32 words); A r, p in, p', t out, 2 links
+        // (6); B t in, Ap out, p' in, 2 links (5); per flush the block's residuals (at most kBlk
+        // FP32 words) once, and per shift not yet written out p_s in and out (2 FP32 words) and
+        // x_s in and out (2 FP64 words)
+        const double gb1 = ((double)h.iters * 14.0 * 8.0 + (double)h.nflush * (kBlk * 8.0 + ns * 48.0)) * n * 1e-9;
         info->gbytes = gb1 + gb;
         // the FP32 multishift phase of the whole batch (every source), and its bytes for this source
         info->kernel_ms = ms - ms2;
