@@ -222,6 +222,24 @@ k_cg64(const double2 *__restrict__ H, double2 *r, double2 *t, double2 *p, double
     }
 }
 
+// One FP64 staggered pass out = D in (sign +1) or D^dagger in (sign -1), register-tiled like
+// the fused CG's passes (16 FMAs per site with the hopping table).  done: optional device flag;
+// when it is set the kernel writes nothing (used inside solver loops).
+__global__ void __launch_bounds__(32 * kC64Warps)
+k_stag64(double2 *__restrict__ out, const double2 *__restrict__ in, const double2 *__restrict__ H, double mass,
+         int lx, int ly, double sign, const int *done)
+{
+    if (done && *done) return;
+    const int ntx = lx / 32, nty = (ly + kC64NY - 1) / kC64NY, ntiles = ntx * nty;
+    const int gw = blockIdx.x * kC64Warps + threadIdx.y, nw = gridDim.x * kC64Warps;
+    for (int tile = gw; tile < ntiles; tile += nw) {
+        const int x0 = (tile % ntx) * 32, y0 = (tile / ntx) * kC64NY;
+        tile_hops(in, H, lx, ly, x0, y0, min(kC64NY, ly - y0), [&](int, long i, double2 c, double2 hs) {
+            out[i] = make_double2(fma(mass, c.x, -sign * hs.x), fma(mass, c.y, -sign * hs.y));
+        });
+    }
+}
+
 int vgrid64(long n)
 {
     long g = (n + 255) / 256, cap = (long)sm_count() * 16;
@@ -242,6 +260,23 @@ int cg64_grid()
 }
 
 }  // namespace
+
+glinalg_status launch_make_hop64(double2 *H, const glinalg_operator_s *op, cudaStream_t st)
+{
+    k_make_hop64<<<vgrid64(op->vol), 256, 0, st>>>(H, op->U, op->lx, op->ly);
+    GL_CUDA(cudaGetLastError());
+    return GLINALG_SUCCESS;
+}
+
+glinalg_status launch_stag64(double2 *out, const double2 *in, const double2 *H, const glinalg_operator_s *op,
+                             double sign, const int *done, cudaStream_t st)
+{
+    const int ntiles = (op->lx / 32) * ((op->ly + kC64NY - 1) / kC64NY);
+    const int grid = (ntiles + kC64Warps - 1) / kC64Warps;
+    k_stag64<<<grid, dim3(32, kC64Warps), 0, st>>>(out, in, H, op->mass, op->lx, op->ly, sign, done);
+    GL_CUDA(cudaGetLastError());
+    return GLINALG_SUCCESS;
+}
 
 bool cg64_fused_applies(const glinalg_operator_s *op, double sigma)
 {

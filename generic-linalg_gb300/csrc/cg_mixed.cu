@@ -880,6 +880,13 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     GL_TRY(sc.alloc(&rhi, n));
     GL_TRY(sc.alloc(&tmp64, n));
     GL_TRY(sc.alloc(&Ax, n));
+    // the reliable updates' FP64 passes run register-tiled on a FP64 hopping table where the
+    // lattice allows (lx a multiple of 32)
+    double2 *H64 = nullptr;
+    if (stag && lx % 32 == 0) {
+        GL_TRY(sc.alloc(&H64, 2 * (size_t)n));
+        GL_TRY(launch_make_hop64(H64, op, st));
+    }
     GL_TRY(sc.alloc(&partials, 2 * (size_t)max_blocks));
     GL_TRY(sc.zeros(&s, 1));
     if (stag) k_make_hop<LK><<<vgrid(n), 256, 0, st>>>(L, op->U, lx, ly);
@@ -930,7 +937,10 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     // beta = 0, so the first direction is the residual itself.
     auto reliable_seq = [&](cudaStream_t cs) -> glinalg_status {
         k_mx_R1<<<vgrid(n), 256, 0, cs>>>(x, xlo, n, s);
-        if (stag) {
+        if (H64) {
+            GL_TRY(launch_stag64(tmp64, x, H64, op, +1.0, &s->done, cs));
+            GL_TRY(launch_stag64(Ax, tmp64, H64, op, -1.0, &s->done, cs));
+        } else if (stag) {
             GL_TRY(launch_staggered(op, tmp64, x, +1.0, &s->done, cs));
             GL_TRY(launch_staggered(op, Ax, tmp64, -1.0, &s->done, cs));
         } else {

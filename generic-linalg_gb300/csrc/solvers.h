@@ -91,6 +91,13 @@ bool cg64_fused_applies(const glinalg_operator_s *op, double sigma);
 glinalg_status cg64_fused(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter, double eps,
                           const Verb &verb, glinalg_info *info, cudaStream_t st, int wait_limit_us = 0);
 
+// FP64 staggered passes with the 1/2 and eta(x) folded into a hopping table H (2 complex per
+// site, built by launch_make_hop64 from op's links): out = D in (sign +1) or D^dagger in
+// (sign -1), nothing written while *done is set.  Staggered kinds with lx a multiple of 32.
+glinalg_status launch_make_hop64(double2 *H, const glinalg_operator_s *op, cudaStream_t st);
+glinalg_status launch_stag64(double2 *out, const double2 *in, const double2 *H, const glinalg_operator_s *op,
+                             double sign, const int *done, cudaStream_t st);
+
 // Mixed-precision CG with FP64 reliable updates (cg_mixed.cu).  sigma: diagonal shift added to
 // the operator (0 for the plain system).  wait_limit_us: glinalg_solver_params::wait_limit_us.
 glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
