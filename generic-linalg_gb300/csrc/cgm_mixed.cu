@@ -33,6 +33,7 @@
 // Sums: FP32 per thread, FP64 across threads and blocks.  The operator uses a FP32 hopping
 // table with the 1/2 and eta(x) folded in (exact: powers of two and signs).
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -158,33 +159,15 @@ __device__ void mx_beta_scalars(const MxArgs &a, MxSrc *s, int q, double re, dou
     s->shift_updates += s->n_rem;
 }
 
-// C: r(k+1) = r(k) + beta Ap into the ring, |r|^2, then the source's bookkeeping
-// (generic_cg_m.cpp:424-513) and, on warp 0 of the last block, the shifts' coefficients:
+// The source's bookkeeping once |r(k+1)|^2 = rn is known (generic_cg_m.cpp:424-513), called by
+// every thread of the source's last block: retire converged shifts, alpha, alpha_s; then, on
+// warp 0, the shifts' coefficients:
 //   x_s -= beta_s p_s  for the shifts live when beta_s was formed,
 //   p_s = zeta_s r(k+1) + alpha_s p_s  for the shifts still live.
-__global__ void __launch_bounds__(kRedThreads) k_mx_C(MxArgs a)
+__device__ void mx_bookkeeping(const MxArgs &a, MxSrc *s, int q, int k, double rn)
 {
-    const int q = blockIdx.y;
-    MxSrc *s = a.src + q;
-    if (s->done) return;
     __shared__ int sh_nb, sh_na, sh_idx;
-    const long n = a.n;
-    const int k = s->k;
-    const float2 *r = ring(a, q, k);
-    float2 *rn_v = ring(a, q, k + 1);
-    const float2 *Ap = a.Ap + q * n;
-    const float2 bt = f2(s->beta);
-    float vf = 0.f;
-    for (long i = blockIdx.x * (long)kRedThreads + threadIdx.x; i < n; i += (long)gridDim.x * kRedThreads) {
-        const float2 ri = fadd(r[i], fmul(bt, Ap[i]));
-        rn_v[i] = ri;
-        vf += fn2(ri);
-    }
-    double v[1] = {(double)vf};
-    if (!grid_sum_row<1, kRedThreads>(v, mrow_partials(a, q), &s->cnt[1])) return;
-    // the last block of this source: all of its threads are here
     if (threadIdx.x == 0) {
-        const double rn = v[0];
         const double bsqrt = sqrt(s->bsq), srn = sqrt(rn);
         const int o = q * a.ns;
         const int nb = s->n_rem_before;
@@ -247,6 +230,158 @@ __global__ void __launch_bounds__(kRedThreads) k_mx_C(MxArgs a)
         a.Xc[c] = csub(a.Xc[c], cmul(a.beta_s[o + j], pc));
         if (j < na) a.Pc[c] = cadd(cmul(a.alpha_s[o + j], pc), l == idx ? a.zeta[o + j] : cmk(0.0, 0.0));
     }
+}
+
+// C: r(k+1) = r(k) + beta Ap into the ring, |r|^2, then the source's bookkeeping.
+__global__ void __launch_bounds__(kRedThreads) k_mx_C(MxArgs a)
+{
+    const int q = blockIdx.y;
+    MxSrc *s = a.src + q;
+    if (s->done) return;
+    const long n = a.n;
+    const int k = s->k;
+    const float2 *r = ring(a, q, k);
+    float2 *rn_v = ring(a, q, k + 1);
+    const float2 *Ap = a.Ap + q * n;
+    const float2 bt = f2(s->beta);
+    float vf = 0.f;
+    for (long i = blockIdx.x * (long)kRedThreads + threadIdx.x; i < n; i += (long)gridDim.x * kRedThreads) {
+        const float2 ri = fadd(r[i], fmul(bt, Ap[i]));
+        rn_v[i] = ri;
+        vf += fn2(ri);
+    }
+    double v[1] = {(double)vf};
+    if (!grid_sum_row<1, kRedThreads>(v, mrow_partials(a, q), &s->cnt[1])) return;
+    mx_bookkeeping(a, s, q, k, v[0]);
+}
+
+// ---- register-tiled forms (lx a multiple of 32), using <p', A p'> = |D p'|^2 = |t|^2 for the
+// Hermitian A = D^dagger D, so that an iteration is two stencil kernels and A p is never stored:
+//   At  p' = r + alpha p (formed at every site it is read), t = D p', |t|^2; then beta, zeta_s,
+//       beta_s in the source's last block
+//   Bt  Ap = D^dagger t, r(k+1) = r(k) + beta Ap into the ring, |r|^2; then the bookkeeping
+// A warp owns a tile of 32 columns by kTNY rows; a lane holds its column for rows -1 .. kTNY in
+// registers (y-neighbours) and takes x-neighbours from the adjacent lanes by shuffle (lanes 0
+// and 31 load across the tile edge).
+
+constexpr int kTNY = 4;                    // rows per warp tile
+constexpr int kTWarps = kRedThreads / 32;  // warps per block
+
+__device__ __forceinline__ float2 shfl_dn2(float2 v)
+{
+    return make_float2(__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1));
+}
+__device__ __forceinline__ float2 shfl_up2f(float2 v)
+{
+    return make_float2(__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1));
+}
+
+// Calls body(i, f(i), hs) for the tile's rows below nrow, hs as in hop32; ld(j) gives f at j.
+template <class Ld, class Body>
+__device__ __forceinline__ void tile32_hops(Ld ld, const float2 *__restrict__ H, int lx, int ly, int x0, int y0,
+                                            int nrow, Body body)
+{
+    const int lane = threadIdx.x & 31;
+    const int x = x0 + lane;
+    const int xl = x == 0 ? lx - 1 : x - 1, xr = x + 1 == lx ? 0 : x + 1;
+    float2 col[kTNY + 2], hyc[kTNY + 1];
+#pragma unroll
+    for (int j = 0; j < kTNY + 2; j++) {
+        int y = y0 - 1 + j;
+        y = y < 0 ? y + ly : (y >= ly ? y - ly : y);
+        col[j] = ld((long)y * lx + x);
+        if (j < kTNY + 1) hyc[j] = H[2 * ((long)y * lx + x) + 1];
+    }
+#pragma unroll
+    for (int q = 0; q < kTNY; q++) {
+        if (q >= nrow) break;
+        const long row = (long)(y0 + q) * lx;
+        const long i = row + x;
+        const float2 c = col[q + 1];
+        float2 fr = shfl_dn2(c), fl = shfl_up2f(c);
+        const float2 hx = H[2 * i];
+        float2 hxm = shfl_up2f(hx);
+        if (lane == 31) fr = ld(row + xr);
+        if (lane == 0) {
+            fl = ld(row + xl);
+            hxm = H[2 * (row + xl)];
+        }
+        float2 hs = fmul(hx, fr);
+        hs = fsub(hs, fmulc(hxm, fl));
+        hs = fadd(hs, fmul(hyc[q + 1], col[q + 2]));
+        hs = fsub(hs, fmulc(hyc[q], col[q]));
+        body(i, c, hs);
+    }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_mx_At(MxArgs a, int setup)
+{
+    const int q = blockIdx.y;
+    MxSrc *s = a.src + q;
+    if (s->done) return;
+    const long n = a.n;
+    const int k = s->k;
+    const float2 alpha = f2(s->alpha);
+    const float2 *r = ring(a, q, k);
+    const float2 *pold = ((k & 1) ? a.p0 : a.p1) + q * n;
+    float2 *pnew = ((k & 1) ? a.p1 : a.p0) + q * n;
+    float2 *t = a.t + q * n;
+    const float mass = a.mass;
+    const int ntx = a.lx / 32, ntiles = ntx * ((a.ly + kTNY - 1) / kTNY);
+    const int warp = threadIdx.x >> 5;
+    float acc = 0.f;
+    for (int tile = blockIdx.x * kTWarps + warp; tile < ntiles; tile += gridDim.x * kTWarps) {
+        const int x0 = (tile % ntx) * 32, y0 = (tile / ntx) * kTNY, nrow = min(kTNY, a.ly - y0);
+        if (setup) {
+            auto ld = [pnew](long j) { return pnew[j]; };
+            tile32_hops(ld, a.H, a.lx, a.ly, x0, y0, nrow, [&](long i, float2 c, float2 hs) {
+                const float2 tv = fsub(fscale(mass, c), hs);
+                t[i] = tv;
+                acc += fn2(tv);
+            });
+        } else {
+            auto ld = [r, pold, alpha](long j) { return fadd(r[j], fmul(alpha, pold[j])); };
+            tile32_hops(ld, a.H, a.lx, a.ly, x0, y0, nrow, [&](long i, float2 c, float2 hs) {
+                pnew[i] = c;
+                const float2 tv = fsub(fscale(mass, c), hs);
+                t[i] = tv;
+                acc += fn2(tv);
+            });
+        }
+    }
+    double v[1] = {(double)acc};
+    if (grid_sum_row<1, kRedThreads>(v, mrow_partials(a, q), &s->cnt[0]) && threadIdx.x == 0)
+        mx_beta_scalars(a, s, q, v[0], 0.0);
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_mx_Bt(MxArgs a)
+{
+    const int q = blockIdx.y;
+    MxSrc *s = a.src + q;
+    if (s->done) return;
+    const long n = a.n;
+    const int k = s->k;
+    const float2 *r = ring(a, q, k);
+    float2 *rn_v = ring(a, q, k + 1);
+    const float2 *t = a.t + q * n;
+    const float2 bt = f2(s->beta);
+    const float mass = a.mass;
+    const int ntx = a.lx / 32, ntiles = ntx * ((a.ly + kTNY - 1) / kTNY);
+    const int warp = threadIdx.x >> 5;
+    float acc = 0.f;
+    auto ld = [t](long j) { return t[j]; };
+    for (int tile = blockIdx.x * kTWarps + warp; tile < ntiles; tile += gridDim.x * kTWarps) {
+        const int x0 = (tile % ntx) * 32, y0 = (tile / ntx) * kTNY, nrow = min(kTNY, a.ly - y0);
+        tile32_hops(ld, a.H, a.lx, a.ly, x0, y0, nrow, [&](long i, float2 c, float2 hs) {
+            const float2 ap = fadd(fscale(mass, c), hs);
+            const float2 rv = fadd(r[i], fmul(bt, ap));
+            rn_v[i] = rv;
+            acc += fn2(rv);
+        });
+    }
+    double v[1] = {(double)acc};
+    if (!grid_sum_row<1, kRedThreads>(v, mrow_partials(a, q), &s->cnt[1])) return;
+    mx_bookkeeping(a, s, q, k, v[0]);
 }
 
 // F: at the end of a block (or of the source), for every shift not yet written out:
@@ -466,7 +601,11 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     float2 *H;
     GL_TRY(sc.alloc(&H, 2 * (size_t)n));
     a.H = H;
-    GL_TRY(sc.alloc(&a.partials, (size_t)n_rhs * 2 * nb));
+    // the register-tiled kernels (lx a multiple of 32): one block of warps per kTWarps tiles
+    const bool tiled = op->lx % 32 == 0;
+    const int ntiles = (op->lx / 32) * ((op->ly + kTNY - 1) / kTNY);
+    const int tg = tiled ? (ntiles + kTWarps - 1) / kTWarps : 0;
+    GL_TRY(sc.alloc(&a.partials, (size_t)n_rhs * 2 * std::max(nb, tg)));
     GL_TRY(sc.zeros(&a.all_done, 1));
     {
         std::vector<double2> ones((size_t)n_rhs * ns, cmk(1.0, 0.0)), zeros((size_t)n_rhs * ns, cmk(0.0, 0.0));
@@ -514,7 +653,21 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     k_mx_init<<<vg, 256, 0, st>>>(a);
     k_mx_norms<<<rg, kRedThreads, 0, st>>>(a);
     GL_CUDA(cudaGetLastError());
-    if (max_iter > 0) {
+    if (max_iter > 0 && tiled) {
+        const dim3 tgr(tg, n_rhs);
+        // setup: t = D b and the first beta
+        k_mx_At<<<tgr, kRedThreads, 0, st>>>(a, 1);
+        k_mx_tail<<<1, 32, 0, st>>>(a);
+        GL_CUDA(cudaGetLastError());
+        GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
+            k_mx_Bt<<<tgr, kRedThreads, 0, cs>>>(a);
+            k_mx_F<<<rg, kRedThreads, 0, cs>>>(a);
+            k_mx_At<<<tgr, kRedThreads, 0, cs>>>(a, 0);
+            k_mx_tail<<<1, 32, 0, cs>>>(a);
+            GL_CUDA(cudaGetLastError());
+            return GLINALG_SUCCESS;
+        }));
+    } else if (max_iter > 0) {
         // setup: Ap = A b and the first beta
         k_mx_A<<<rg, kRedThreads, 0, st>>>(a, 1);
         k_mx_B<<<rg, kRedThreads, 0, st>>>(a);
@@ -603,7 +756,8 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         // (6); B t in, Ap out, p' in, 2 links (5); per flush the block's residuals (at most kBlk
         // FP32 words) once, and per shift not yet written out p_s in and out (2 FP32 words) and
         // x_s in and out (2 FP64 words)
-        const double gb1 = ((double)h.iters * 14.0 * 8.0 + (double)h.nflush * (kBlk * 8.0 + ns * 48.0)) * n * 1e-9;
+        const double words = tiled ? 11.0 : 14.0;  // tiled: A r, p in, p', t out, 2 links; B t in, r in and out, 2 links
+        const double gb1 = ((double)h.iters * words * 8.0 + (double)h.nflush * (kBlk * 8.0 + ns * 48.0)) * n * 1e-9;
         info->gbytes = gb1 + gb;
         // the FP32 multishift phase of the whole batch (every source), and its bytes for this source
         info->kernel_ms = ms - ms2;
