@@ -43,6 +43,8 @@ constexpr int kVecSites = 1024;  // sites per block of the vector kernels (256 t
 
 struct BSys {
     long off;          // first site in the packed work vectors
+    long loff;         // first site of its packed link table (systems with the same links share one)
+    int lown;          // 1: this system packs the table at loff
     const double2 *U;  // FP64 links (the operator's device copy)
     double2 *x;        // FP64 solution (device)
     const double2 *b;  // source (device)
@@ -138,13 +140,13 @@ __global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a)
     const float beta = (float)s->beta;
     float acc[1];
     if (!sy.stag)
-        acc[0] = lap_tile_A<S, R, LK, NY>(a.r + o, pold, pnew, a.t + o, a.L + 2 * o, beta, (float)(4.0 + sy.mass),
+        acc[0] = lap_tile_A<S, R, LK, NY>(a.r + o, pold, pnew, a.t + o, a.L + 2 * sy.loff, beta, (float)(4.0 + sy.mass),
                                           sy.lx, sy.ly, x, ybase);
     else if (sy.xs)
-        acc[0] = tile_A<S, R, LK, NY, true, false>(a.r + o, pold, pnew, a.t + o, a.L + 2 * o, beta, (float)sy.mass,
+        acc[0] = tile_A<S, R, LK, NY, true, false>(a.r + o, pold, pnew, a.t + o, a.L + 2 * sy.loff, beta, (float)sy.mass,
                                                    0.f, sy.lx, sy.ly, threadIdx.x, x, true, ybase);
     else
-        acc[0] = tile_A<S, R, LK, NY, false, false>(a.r + o, pold, pnew, a.t + o, a.L + 2 * o, beta,
+        acc[0] = tile_A<S, R, LK, NY, false, false>(a.r + o, pold, pnew, a.t + o, a.L + 2 * sy.loff, beta,
                                                     (float)sy.mass, 0.f, sy.lx, sy.ly, threadIdx.x, x, x < sy.lx,
                                                     ybase);
     double out[1];
@@ -172,10 +174,10 @@ __global__ void __launch_bounds__(32 * BY) k_bB(BArgs<S, R, LK> a)
     if (!sy.stag)
         acc[0] = lap_tile_B<S, R, NY>(a.t + o, p, a.r + o, a.xlo + o, alpha, sy.lx, sy.ly, x, ybase);
     else if (sy.xs)
-        acc[0] = tile_B<S, R, LK, NY, true, false>(a.t + o, p, a.r + o, a.xlo + o, a.L + 2 * o, alpha,
+        acc[0] = tile_B<S, R, LK, NY, true, false>(a.t + o, p, a.r + o, a.xlo + o, a.L + 2 * sy.loff, alpha,
                                                    (float)sy.mass, 0.f, sy.lx, sy.ly, threadIdx.x, x, true, ybase);
     else
-        acc[0] = tile_B<S, R, LK, NY, false, false>(a.t + o, p, a.r + o, a.xlo + o, a.L + 2 * o, alpha,
+        acc[0] = tile_B<S, R, LK, NY, false, false>(a.t + o, p, a.r + o, a.xlo + o, a.L + 2 * sy.loff, alpha,
                                                     (float)sy.mass, 0.f, sy.lx, sy.ly, threadIdx.x, x, x < sy.lx,
                                                     ybase);
     double out[1];
@@ -355,7 +357,8 @@ __global__ void __launch_bounds__(kRedThreads) k_bLinks(BArgs<S, R, LK> a)
     const int sid = a.vblk[blockIdx.x];
     const BSys sy = a.sys[sid];
     const unsigned lb = blockIdx.x - sy.vb0;
-    const long n = (long)sy.lx * sy.ly, o = sy.off;
+    const long n = (long)sy.lx * sy.ly, o = sy.loff;
+    if (!sy.lown) return;
     for (long i = (long)lb * kRedThreads + threadIdx.x; i < n; i += (long)sy.nvb * kRedThreads) {
         if (sy.stag) {
             const int x = (int)(i % sy.lx);
@@ -450,7 +453,7 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     Scratch sc(st);
     std::vector<BSys> sys(nsys);
     std::vector<int> vblk, tblk;
-    long N = 0;
+    long N = 0, NL = 0;
     std::vector<int> sig;
     for (int q = 0; q < nsys; q++) {
         const glinalg_operator_s *op = ops[q];
@@ -466,6 +469,21 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
         y.stag = op->kind == GLINALG_OP_STAGGERED_NORMAL;
         y.xs = op->lx % 32 == 0;
         const long n = op->size;
+        // one packed link table per distinct (links, kind, lattice): systems that differ only in
+        // mass (the shifted systems of a multishift refinement) read the same table
+        y.loff = -1;
+        for (int e = 0; e < q; e++) {
+            const BSys &z = sys[e];
+            if (z.lown && z.U == y.U && z.stag == y.stag && z.lx == y.lx && z.ly == y.ly) {
+                y.loff = z.loff;
+                break;
+            }
+        }
+        if (y.loff < 0) {
+            y.loff = NL;
+            y.lown = 1;
+            NL += n;
+        }
         y.vb0 = (int)vblk.size();
         y.nvb = (int)((n + kVecSites - 1) / kVecSites);
         vblk.insert(vblk.end(), y.nvb, q);
@@ -481,7 +499,7 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     GL_TRY(sc.zeros(&a.p1, N));
     GL_TRY(sc.alloc(&a.t, N));
     GL_TRY(sc.zeros(&a.xlo, N));
-    GL_TRY(sc.alloc(&a.L, 2 * N));
+    GL_TRY(sc.alloc(&a.L, 2 * NL));
     GL_TRY(sc.alloc(&a.rhi, N));
     GL_TRY(sc.alloc(&a.tmp64, N));
     GL_TRY(sc.alloc(&a.Ax, N));
