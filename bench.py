@@ -612,7 +612,8 @@ def workload_rows(args):
             xe.zero_()
             return gl.minv_vector_cg(xe, rhs_e, n, 100000, EPS, gl.square_staggered_m2mdeodoe_u1, eo, precision=prec)
         ms, info = timed(solve, reps=max(1, min(args.steps, 3)))
-        out[nm] = {"ms": round(ms, 3), "iters": info.iter, "success": info.success,
+        out[nm] = {"ms": round(ms, 3), "iters": info.iter, "success": info.success, "solver": info.name,
+                   "reliable_updates": info.reliable_updates, "inner_kernel_ms": round(info.kernel_ms, 3),
                    "algorithmic_GBps": round(info.gbytes / (ms * 1e-3), 1)}
     full = torch.zeros_like(bd)
     if args.rows_kernels:

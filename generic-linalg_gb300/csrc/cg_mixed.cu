@@ -43,6 +43,7 @@
 #include "mixed_state.cuh"
 #include "stag_bulk.cuh"
 #include "stag_resident.cuh"
+#include "stag_resident_eo.cuh"
 
 namespace glinalg {
 
@@ -175,6 +176,43 @@ __global__ void k_mx_R1(double2 *__restrict__ x, float2 *__restrict__ xlo, long 
     }
 }
 
+// After the FP64 true residual |r_hi|^2 = rt of n sites: stop (converged, non-finite, an exactly
+// zero residual, the iteration cap) or rescale for the next inner cycle.  One thread.
+static __device__ void mx_true_residual(MxDev *s, double rt, long n)
+{
+    s->rsq_old_true = s->rsq * s->scale * s->scale;  // |r|^2 at the start of the last iteration
+    s->rsq_true = rt;
+    s->n_reliable++;
+    const double bsqrt = sqrt(s->bsq);
+    if (!isfinite(rt)) {
+        s->status = GLINALG_SOLVE_NONFINITE;
+        s->done = 1;
+        return;
+    }
+    if (sqrt(rt) < s->eps * bsqrt) {
+        s->status = GLINALG_SOLVE_CONVERGED;
+        s->done = 1;
+        return;
+    }
+    if (rt == 0.0) {
+        // an exactly zero residual (a zero source with a zero guess): x is exact, and the
+        // rescale below would divide by zero; the FP64 CG stops the same way (<p, Ap> = 0)
+        s->status = GLINALG_SOLVE_BREAKDOWN;
+        s->done = 1;
+        return;
+    }
+    if (s->k >= s->max_iter) {
+        s->status = GLINALG_SOLVE_MAX_ITER;
+        s->done = 1;
+        return;
+    }
+    const double new_scale = sqrt(rt / (double)n);
+    // p keeps its meaning under the new scale: p_lo_new = p_lo_old * (old/new)
+    s->pscale = s->scale / new_scale;
+    s->scale = new_scale;
+    s->rmax = sqrt(rt);
+}
+
 // R2: r_hi = b - (Ax + sigma x) ; |r_hi|^2 -> scale, convergence
 __global__ void __launch_bounds__(kRedThreads)
 k_mx_R2(double2 *__restrict__ rhi, const double2 *__restrict__ b, const double2 *__restrict__ Ax,
@@ -189,40 +227,7 @@ k_mx_R2(double2 *__restrict__ rhi, const double2 *__restrict__ b, const double2 
         rhi[i] = ri;
         v[0] += cabs2(ri);
     }
-    if (grid_sum<1, kRedThreads>(v, partials, &s->cnt[2]) && threadIdx.x == 0) {
-        const double rt = v[0];
-        s->rsq_old_true = s->rsq * s->scale * s->scale;  // |r|^2 at the start of the last iteration
-        s->rsq_true = rt;
-        s->n_reliable++;
-        const double bsqrt = sqrt(s->bsq);
-        if (!isfinite(rt)) {
-            s->status = GLINALG_SOLVE_NONFINITE;
-            s->done = 1;
-            return;
-        }
-        if (sqrt(rt) < s->eps * bsqrt) {
-            s->status = GLINALG_SOLVE_CONVERGED;
-            s->done = 1;
-            return;
-        }
-        if (rt == 0.0) {
-            // an exactly zero residual (a zero source with a zero guess): x is exact, and the
-            // rescale below would divide by zero; the FP64 CG stops the same way (<p, Ap> = 0)
-            s->status = GLINALG_SOLVE_BREAKDOWN;
-            s->done = 1;
-            return;
-        }
-        if (s->k >= s->max_iter) {
-            s->status = GLINALG_SOLVE_MAX_ITER;
-            s->done = 1;
-            return;
-        }
-        const double new_scale = sqrt(rt / (double)n);
-        // p keeps its meaning under the new scale: p_lo_new = p_lo_old * (old/new)
-        s->pscale = s->scale / new_scale;
-        s->scale = new_scale;
-        s->rmax = sqrt(rt);
-    }
+    if (grid_sum<1, kRedThreads>(v, partials, &s->cnt[2]) && threadIdx.x == 0) mx_true_residual(s, v[0], n);
 }
 
 // R3: r_lo = r_hi / scale ; p_lo *= f ; reduce <r_lo, p_lo> (real part) and |r_lo|^2.
@@ -1117,6 +1122,245 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
     return GLINALG_SUCCESS;
 }
 
+// ---------------------------------------------------------------- checkerboarded even system
+//
+// The FP32 mixed-precision CG on m^2 - D_eo D_oe (+ sigma) with the even fields stored packed
+// (half-lattice layout: even site (x, y) at j = y * lx/2 + x/2) and the inner iterations in the
+// rectangle-resident kernel k_resident_eo.  The FP64 side keeps x on the full lattice (odd
+// sites zero), so that the reliable update's true residual is m^2 x - D_eo D_oe x formed as
+// D^dagger (D x) by the FP64 stencils (on an even-only field the two agree at the even sites).
+
+// Full-lattice index of packed even site j.
+__device__ __forceinline__ long eo_full_even(long j, int hw, int lx)
+{
+    const long y = j / hw;
+    const long u = j - y * hw;
+    return y * lx + 2 * u + (y & 1);
+}
+
+// Packed FP32 hopping table: H2[2 j] = h_x, H2[2 j + 1] = h_y of the even site at packed index
+// j, the odd sites from 4 nh on (the values of k_make_hop: h_x = -U_x / 2, h_y = -eta(x) U_y / 2).
+__global__ void k_eo_pack_hop(float2 *__restrict__ H2, const double2 *__restrict__ U, int lx, int ly)
+{
+    const long vol = (long)lx * ly, nh = vol / 2;
+    const int hw = lx / 2;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < vol; i += (long)gridDim.x * blockDim.x) {
+        const int y = (int)(i / lx), x = (int)(i - (long)y * lx);
+        const double eta = (x & 1) ? -1.0 : 1.0;
+        const long j = (long)y * hw + (x >> 1) + (((x + y) & 1) ? nh : 0);
+        H2[2 * j] = Fmt<float2>::from(cscale(-0.5, U[2 * i]));
+        H2[2 * j + 1] = Fmt<float2>::from(cscale(-0.5 * eta, U[2 * i + 1]));
+    }
+}
+
+// be = b at the even sites, packed.
+__global__ void k_eo_gather(double2 *__restrict__ be, const double2 *__restrict__ b, int lx, int ly)
+{
+    const long nh = (long)lx * ly / 2;
+    for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < nh; j += (long)gridDim.x * blockDim.x)
+        be[j] = b[eo_full_even(j, lx / 2, lx)];
+}
+
+// R1 on the packed x_lo: x_hi(even site of j) += scale * x_lo[j] ; x_lo = 0
+__global__ void k_eo_R1(double2 *__restrict__ x, float2 *__restrict__ xlo, int lx, int ly, const MxDev *s)
+{
+    if (s->done) return;
+    const long nh = (long)lx * ly / 2;
+    const double sc = s->scale;
+    for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < nh; j += (long)gridDim.x * blockDim.x) {
+        const long i = eo_full_even(j, lx / 2, lx);
+        const float2 d = xlo[j];
+        const double2 xv = x[i];
+        x[i] = cmk(xv.x + sc * (double)d.x, xv.y + sc * (double)d.y);
+        xlo[j] = make_float2(0.f, 0.f);
+    }
+}
+
+// R2 on the even sites: r_hi[j] = b_e[j] - (Ax + sigma x)(even site of j) ; |r_hi|^2
+__global__ void __launch_bounds__(kRedThreads)
+k_eo_R2(double2 *__restrict__ rhi, const double2 *__restrict__ be, const double2 *__restrict__ Ax,
+        const double2 *__restrict__ x, int lx, int ly, MxDev *s, double *partials)
+{
+    if (s->done) return;
+    const long nh = (long)lx * ly / 2;
+    const double sg = s->sigma;
+    double v[1] = {0.0};
+    for (long j = blockIdx.x * (long)kRedThreads + threadIdx.x; j < nh; j += (long)gridDim.x * kRedThreads) {
+        const long i = eo_full_even(j, lx / 2, lx);
+        const double2 ri = csub(be[j], cadd(Ax[i], cscale(sg, x[i])));
+        rhi[j] = ri;
+        v[0] += cabs2(ri);
+    }
+    if (grid_sum<1, kRedThreads>(v, partials, &s->cnt[2]) && threadIdx.x == 0) mx_true_residual(s, v[0], nh);
+}
+
+// The rectangle grid of k_resident_eo on this device (512 bytes of the per-block budget kept for
+// its static shared memory).
+static res::Plan eo_plan(int lx, int ly)
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return res::Plan{};
+    }
+    return reseo::plan(lx, ly, sm_count(), (size_t)std::max(0, optin - 512));
+}
+
+using EoKernel = void (*)(const float2 *, float2 *, float2 *, float2 *, float, float, int, int, MxDev *,
+                          res::PhaseFlags *, unsigned long long *, int, int);
+
+// The kernel instance for a plan, with its shared memory set and its grid checked against the
+// device's co-resident blocks; nullptr when it cannot run.
+static EoKernel eo_kernel(const res::Plan &p)
+{
+    if (!p.ok) return nullptr;
+    EoKernel f = p.ny == 8 ? k_resident_eo<8> : (p.ny == 14 ? k_resident_eo<14> : nullptr);
+    if (!f) return nullptr;
+    int per_sm = 0;
+    const void *fp = reinterpret_cast<const void *>(f);
+    if (cudaFuncSetAttribute(fp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)p.smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fp, 32 * res::kWX * reseo::kWY, p.smem) !=
+            cudaSuccess ||
+        per_sm < 1 || p.gx * p.gy > sm_count() * per_sm) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return f;
+}
+
+// GLINALG_EO_PACKED=0 keeps the even system on the full-lattice solver.
+static bool eo_packed_enabled()
+{
+    static const bool on = [] {
+        const char *e = std::getenv("GLINALG_EO_PACKED");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
+
+static bool eo_packed_applies(const glinalg_operator_s *op)
+{
+    return eo_packed_enabled() && persist_enabled() && op->kind == GLINALG_OP_STAGGERED_M2MDEODOE &&
+           eo_plan(op->lx, op->ly).ok;
+}
+
+static glinalg_status run_mixed_eo(const glinalg_operator_s *op, double2 *x, const double2 *b, int max_iter,
+                                   double eps, double delta, double sigma, glinalg_info *info, cudaStream_t st,
+                                   int wait_limit_us)
+{
+    const long n = op->size, nh = n / 2;
+    const int lx = op->lx, ly = op->ly;
+    const res::Plan pl = eo_plan(lx, ly);
+    const EoKernel kern = eo_kernel(pl);
+    if (!kern) {
+        set_last_error("the checkerboarded resident kernel does not fit this device");
+        return GLINALG_ERROR_UNSUPPORTED_OP;
+    }
+    Scratch sc(st);
+    float2 *r, *p0, *xlo, *H2;
+    double2 *xf, *be, *rhi, *tmp64, *Ax, *H64;
+    double *partials;
+    MxDev *s;
+    res::PhaseFlags *pf;
+    unsigned long long *mbox;
+    const int nb = reduction_blocks(n);
+    GL_TRY(sc.alloc(&r, nh));
+    GL_TRY(sc.zeros(&p0, nh));
+    GL_TRY(sc.zeros(&xlo, nh));
+    GL_TRY(sc.alloc(&H2, 2 * (size_t)n));
+    GL_TRY(sc.alloc(&xf, n));
+    GL_TRY(sc.alloc(&be, nh));
+    GL_TRY(sc.alloc(&rhi, nh));
+    GL_TRY(sc.alloc(&tmp64, n));
+    GL_TRY(sc.alloc(&Ax, n));
+    GL_TRY(sc.alloc(&H64, 2 * (size_t)n));
+    GL_TRY(sc.alloc(&partials, 2 * (size_t)nb));
+    GL_TRY(sc.zeros(&s, 1));
+    GL_TRY(sc.zeros(&pf, 1));
+    GL_TRY(sc.zeros(&mbox, res::mbox_words(pl.gx * pl.gy, pl.ty)));
+    k_eo_pack_hop<<<vgrid(n), 256, 0, st>>>(H2, op->U, lx, ly);
+    k_eo_gather<<<vgrid(nh), 256, 0, st>>>(be, b, lx, ly);
+    GL_CUDA(cudaGetLastError());
+    GL_TRY(launch_make_hop64(H64, op, st));
+    // x on the full lattice with its odd sites zero (only the even sites come back)
+    GL_TRY(launch_even_part(op, xf, x, st));
+
+    MxDev h = {};
+    h.eps = eps;
+    h.delta = delta;
+    h.sigma = sigma;
+    h.max_iter = max_iter;
+    h.scale = 1.0;
+    h.wait_ns = wait_limit_us > 0 ? 1000LL * wait_limit_us : (wait_limit_us < 0 ? -1LL : 0LL);
+    GL_CUDA(cudaMemcpyAsync(s, &h, sizeof(h), cudaMemcpyHostToDevice, st));
+
+    EventTimer tm;
+    tm.start(st);
+    GL_TRY(launch_norm2(be, nh, partials, &s->cnt[4], &s->bsq, st));
+    const int nbh = reduction_blocks(nh);
+    auto reliable_seq = [&](cudaStream_t cs) -> glinalg_status {
+        k_eo_R1<<<vgrid(nh), 256, 0, cs>>>(xf, xlo, lx, ly, s);
+        GL_TRY(launch_stag64(tmp64, xf, H64, op, +1.0, &s->done, cs));
+        GL_TRY(launch_stag64(Ax, tmp64, H64, op, -1.0, &s->done, cs));
+        k_eo_R2<<<nbh, kRedThreads, 0, cs>>>(rhi, be, Ax, xf, lx, ly, s, partials);
+        // the resident kernel leaves the direction in p0 (parity 0)
+        k_mx_R3<float2, float2><<<nbh, kRedThreads, 0, cs>>>(r, p0, p0, rhi, nh, s, partials);
+        k_mx_R4<float2, float2><<<vgrid(nh), 256, 0, cs>>>(p0, p0, r, nh, s);
+        GL_CUDA(cudaGetLastError());
+        return GLINALG_SUCCESS;
+    };
+    GL_TRY(reliable_seq(st));
+    GL_TRY(run_loop(st, &s->done, [&](cudaStream_t cs) -> glinalg_status {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(pl.gx * pl.gy);
+        cfg.blockDim = dim3(32, res::kWX * reseo::kWY);
+        cfg.dynamicSmemBytes = pl.smem;
+        cfg.stream = cs;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        GL_CUDA(cudaLaunchKernelEx(&cfg, kern, (const float2 *)H2, r, p0, xlo, (float)op->mass, (float)sigma, lx, ly,
+                                   s, pf, mbox, pl.ty, pl.gx));
+        GL_TRY(reliable_seq(cs));
+        k_mx_outer_tail<<<1, 32, 0, cs>>>(s, 0, 0);
+        GL_CUDA(cudaGetLastError());
+        return GLINALG_SUCCESS;
+    }));
+    tm.stop(st);
+    GL_TRY(launch_even_into(op, x, xf, st));
+    GL_CUDA(cudaMemcpyAsync(&h, s, sizeof(h), cudaMemcpyDeviceToHost, st));
+    GL_CUDA(cudaStreamSynchronize(st));
+    if (h.status == GLINALG_SOLVE_TIMEOUT) {
+        info->resSq = 0.0;
+        info->iter = h.k;
+        info->success = 0;
+        info->ops_count = h.k + h.n_reliable;
+        info->status = GLINALG_SOLVE_TIMEOUT;
+        info->reliable_updates = h.n_reliable;
+        set_last_error("a bounded wait of the persistent CG kernel for other blocks ran out");
+        return GLINALG_ERROR_INTERNAL;
+    }
+    info->resSq = h.rsq_true;
+    info->iter = h.k;
+    info->success = h.status == GLINALG_SOLVE_CONVERGED ? 1 : 0;
+    info->ops_count = h.k + h.n_reliable;
+    info->status = h.status;
+    info->reliable_updates = h.n_reliable;
+    info->device_ms = tm.ms();
+    // a streaming iteration on the half lattice: the full-lattice iteration's words per even site
+    const double per_iter = 6.0 * 8 + 4.0 * 8 + 3.0 * 8 + 16.0;
+    const double per_rel = 16.0 * 2 + 16.0 + 8.0 * 64.0 / 8.0 + 16.0 * 3 + 2 * 8 + 4 * 8;
+    info->gbytes = ((double)h.k * per_iter * nh + (double)h.n_reliable * per_rel * n) * 1e-9;
+    info->kernel_ms = (double)h.inner_ns * 1e-6;
+    info->kernel_gbytes = (double)h.inner_iters * per_iter * nh * 1e-9;
+    info->kernel_launches = h.inner_launches;
+    fill_name(info, "CG-FP32-EO");
+    return GLINALG_SUCCESS;
+}
+
 // Mixed-precision CG on m^2 - D_eo D_oe (square_staggered_m2mdeodoe_u1, operators.cpp:566).  On
 // even-only fields this operator equals D^dagger D, so the staggered normal solver runs on the
 // even parts of b and of the guess.  Only x's even sites are written: the odd sites keep their
@@ -1153,9 +1397,13 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
                         double eps, int precision, double delta, double sigma, const Verb &verb,
                         glinalg_info *info, cudaStream_t st, int wait_limit_us)
 {
-    if (op->kind == GLINALG_OP_STAGGERED_M2MDEODOE)
+    // the even system runs checkerboarded (k_resident_eo) in FP32 where the lattice allows,
+    // otherwise on the full-lattice solver
+    const bool eo_packed = op->kind == GLINALG_OP_STAGGERED_M2MDEODOE && precision == GLINALG_PREC_SINGLE &&
+                           eo_packed_applies(op);
+    if (op->kind == GLINALG_OP_STAGGERED_M2MDEODOE && !eo_packed)
         return cg_mixed_even(op, x, b, max_iter, eps, precision, delta, sigma, verb, info, st, wait_limit_us);
-    if (!(op->kind == GLINALG_OP_STAGGERED_NORMAL || op->kind == GLINALG_OP_LAPLACE)) {
+    if (!(op->kind == GLINALG_OP_STAGGERED_NORMAL || op->kind == GLINALG_OP_LAPLACE || eo_packed)) {
         set_last_error("mixed-precision CG needs the staggered normal operator, m^2 - D_eo D_oe or the gauge "
                        "Laplacian");
         return GLINALG_ERROR_UNSUPPORTED_OP;
@@ -1167,7 +1415,9 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
     glinalg_status s;
     switch (precision) {
     case GLINALG_PREC_SINGLE:
-        s = run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32", 1, wait_limit_us);
+        s = eo_packed ? run_mixed_eo(op, x, b, max_iter, eps, delta, sigma, info, st, wait_limit_us)
+                      : run_mixed<float2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP32",
+                                                          1, wait_limit_us);
         break;
     case GLINALG_PREC_HALF:
         s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16", 2, wait_limit_us);

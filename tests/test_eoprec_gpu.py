@@ -7,7 +7,18 @@ max(|ref_i|, s_i), s_i the summed magnitude of the terms at site i); the FP64 CG
 m^2 - D_eo D_oe takes the reference's iterations and operator applications, and its solution
 is within 1e-11 of the reference's (the reconstructed full solution within 1e-11 (1 + 1/m):
 the odd half is divided by the mass); the mixed-precision
-even/odd solve reaches the FP64-true residual of its tolerance."""
+even/odd solve reaches the FP64-true residual of its tolerance.
+
+Where lx is a multiple of 256 and ly is even, the FP32 even/odd solve runs checkerboarded (the
+even fields packed to half the lattice, the inner iterations in the rectangle-resident kernel
+k_resident_eo); its bars, against the oracle's FP64 even/odd solve on the same inputs
+(prepare, CG on m^2 - D_eo D_oe, reconstruct; tests/staggered_pieces/staggered_pieces.cpp:331-346):
+the FP64-true relative residual of the even system below 1e-10, recomputed by the oracle's
+operator; the even solution within 1e-9 of the oracle's (two solutions with relative residual
+below 1e-10 differ by at most 2 kappa 1e-10; the measured distance is printed); odd sites of
+the guess untouched; and the reconstructed full solution's residual |b - M x| equal to
+|r_e| / m (the even rows of M x - b are r_e / m after reconstruct, the odd rows vanish), so
+below 1.01e-10 |rhs_e| / m."""
 from __future__ import annotations
 
 import numpy as np
@@ -148,3 +159,49 @@ def test_eo_solve_1024(gl, gpu):
     gl.Operator(0, lx, ly, 0.01, Ud).apply(Mx, x)
     rr = (torch.linalg.vector_norm(Mx - bd) / torch.linalg.vector_norm(bd)).item()
     assert rr < 1e-9, rr
+
+
+def oracle_eo(lx, ly, m, seed=1337):
+    import pyoracle
+    O = pyoracle.Oracle()
+    O.set_threads(None)
+    g = pyoracle.Generator(seed)
+    U = g.rand_gauge_u1(lx, ly)
+    b = g.gaussian(lx * ly)
+    eo = pyoracle.Operator("staggered_m2mdeodoe", lx, ly, m, U)
+    rhs_e = O.eoprec_prepare(eo, b)
+    xe, info, _ = O.solve("cg", eo, rhs_e, max_iter=100000, eps=1e-10)
+    assert info["success"], info
+    return U, b, rhs_e, xe, info, O, eo
+
+
+@pytest.mark.parametrize("lx,ly,m", [(1024, 1024, 0.01), (256, 310, 0.05), (512, 76, 0.1)])
+def test_eo_checkerboarded_solve_matches_oracle(gl, gpu, lx, ly, m):
+    """The checkerboarded FP32 even/odd solve against the oracle's FP64 one.  1024^2 is the
+    benchmark's system (4 x 38 rectangles of 128 packed columns by 27 rows); 256 x 310 has one
+    rectangle across and a last row of rectangles one row high (3 rows elsewhere); 512 x 76 has
+    rectangles one row high."""
+    import pyoracle
+    U, b, rhs_e, xo, io, O, eo = oracle_eo(lx, ly, m)
+    n = lx * ly
+    odd = ~even_mask(lx, ly)
+    xe = np.zeros_like(b)
+    xe[odd] = 7.0  # odd sites of the guess must come back untouched
+    extra = gl.StaggeredU1Op(U, m, lx, ly)
+    info = gl.minv_vector_cg(xe, rhs_e, n, 100000, 1e-10, gl.square_staggered_m2mdeodoe_u1, extra, precision=1)
+    assert info.success, info
+    assert info.name == "CG-FP32-EO" and info.kernel_launches >= 1, info
+    assert np.all(xe[odd] == 7.0)
+    xe[odd] = 0.0
+    rr = float(np.linalg.norm(rhs_e - O.apply(eo, xe)) / np.linalg.norm(rhs_e))
+    err = rel(xe, xo)
+    full = np.zeros_like(b)
+    gl.square_staggered_eoprec_reconstruct(full, xe, b, extra)
+    M = pyoracle.Operator("staggered", lx, ly, m, U)
+    res_full = float(np.linalg.norm(b - O.apply(M, full)))
+    print(f"checkerboarded FP32 even/odd {lx}x{ly} m={m}: {info.iter} inner iterations "
+          f"(oracle FP64 {io['iter']}), {info.reliable_updates} reliable updates, even relres {rr:.3e}, "
+          f"err vs oracle {err:.3e}, full |b - Mx| / |b| {res_full / np.linalg.norm(b):.3e}")
+    assert rr < 1e-10
+    assert err < 1e-9
+    assert res_full < 1.01e-10 * np.linalg.norm(rhs_e) / m

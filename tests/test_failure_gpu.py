@@ -146,3 +146,30 @@ def test_persistent_wait_limit_runs_out_cleanly(gl, gpu, tmp_path, shape):
     assert "bounded wait" in msg, res
     ok, st, relres = res["after"]
     assert ok and st == gl.GLINALG_SOLVE_CONVERGED and relres < 1e-10, res
+
+
+def test_checkerboarded_wait_limit_runs_out_cleanly(gl, gpu):
+    """The same bounded-wait exit in the checkerboarded even/odd kernel (k_resident_eo): a solve
+    told to give up every wait at its first miss reports GLINALG_SOLVE_TIMEOUT, and a normal
+    solve on the same device then converges."""
+    import torch
+    lx = ly = 1024
+    U, b = system(gl, lx=lx, ly=ly)
+    dev = torch.device("cuda:0")
+    Ud, bd = torch.from_numpy(U).to(dev), torch.from_numpy(b).to(dev)
+    eo = gl.Operator(9, lx, ly, 0.01, Ud)
+    rhs_e = torch.zeros_like(bd)
+    gl.square_staggered_eoprec_prepare(rhs_e, bd, eo)
+    x = torch.zeros_like(bd)
+    with pytest.raises(gl.SolveTimeout) as ei:
+        gl.minv_vector_cg(x, rhs_e, b.size, 100000, 1e-10, gl.square_staggered_m2mdeodoe_u1, eo, precision=1,
+                          wait_limit_us=-1)
+    assert ei.value.info.status == gl.GLINALG_SOLVE_TIMEOUT and not ei.value.info.success
+    assert "bounded wait" in str(ei.value)
+    x.zero_()
+    info = gl.minv_vector_cg(x, rhs_e, b.size, 100000, 1e-10, gl.square_staggered_m2mdeodoe_u1, eo, precision=1)
+    assert info.success and info.status == gl.GLINALG_SOLVE_CONVERGED and info.name == "CG-FP32-EO", info
+    Ax = torch.zeros_like(bd)
+    eo.apply(Ax, x)
+    rr = (torch.linalg.vector_norm(rhs_e - Ax) / torch.linalg.vector_norm(rhs_e)).item()
+    assert rr < 1e-10, rr
