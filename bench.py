@@ -708,6 +708,109 @@ def workload_rows(args):
     print(json.dumps(line))
 
 
+def workload_eo(args):
+    """Even/odd solve of M x = b (M = m + D, the staggered operator) on the 1024x1024, m = 0.01
+    system of the headline, by the reference's recipe (tests/staggered_pieces/staggered_pieces.cpp:
+    331-346): prepare rhs_e = m b_e - D_eo b_o, CG on m^2 - D_eo D_oe to 1e-10, reconstruct
+    x_o = (b_o - D_oe x_e) / m.  GPU: the checkerboarded FP32 CG with FP64 reliable updates,
+    device-resident fields (L2 flushed before every step), and end to end through the public API
+    from pinned host buffers (the operator built from host links once per step).  Inputs from
+    the oracle's generator (std::mt19937(1337)); the solution is checked against the oracle's
+    FP64 even/odd solve, whose time on the host threads is the CPU baseline."""
+    import numpy as np
+    import torch
+    gl = importlib.import_module("generic-linalg_gb300")
+    L = gl.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    gl._capi.check(L.glinalg_set_stream(C_void(stream.cuda_stream), 1), "set_stream")
+    U, b = oracle_inputs()
+    n = LX * LY
+    Ud, bd = torch.from_numpy(U).to(dev), torch.from_numpy(b).to(dev)
+    eo = gl.Operator(9, LX, LY, MASS, Ud)
+    rhs_e, xe, x = torch.zeros_like(bd), torch.zeros_like(bd), torch.zeros_like(bd)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def step():
+        gl.square_staggered_eoprec_prepare(rhs_e, bd, eo)
+        xe.zero_()
+        info = gl.minv_vector_cg(xe, rhs_e, n, MAX_ITER, EPS, gl.square_staggered_m2mdeodoe_u1, eo, precision=1)
+        gl.square_staggered_eoprec_reconstruct(x, xe, bd, eo)
+        return info
+
+    clocks = ClockSampler(0)
+    for _ in range(args.warmup):
+        _flush_and_time(step, flush, stream)
+    clocks.start()
+    times, infos = [], []
+    for _ in range(args.steps):
+        t, info = _flush_and_time(step, flush, stream)
+        times.append(t)
+        infos.append(info)
+    clk = clocks.stop()
+    info = infos[-1]
+    if not info.success:
+        raise RuntimeError(f"even/odd solve did not converge: {info}")
+    Mx = torch.zeros_like(bd)
+    gl.Operator(0, LX, LY, MASS, Ud).apply(Mx, x)
+    relres = (torch.linalg.vector_norm(bd - Mx) / torch.linalg.vector_norm(bd)).item()
+    xg = x.cpu().numpy()
+
+    # end to end: host links and fields, copies inside the timed region
+    Uh = torch.from_numpy(U).pin_memory().numpy()
+    bh = torch.from_numpy(b).pin_memory().numpy()
+    rh, xeh, xh = (torch.zeros(n, dtype=torch.complex128).pin_memory().numpy() for _ in range(3))
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op_h = gl.Operator(9, LX, LY, MASS, Uh)
+        gl.square_staggered_eoprec_prepare(rh, bh, op_h)
+        xeh[:] = 0
+        inf_h = gl.minv_vector_cg(xeh, rh, n, MAX_ITER, EPS, gl.square_staggered_m2mdeodoe_u1, op_h, precision=1)
+        gl.square_staggered_eoprec_reconstruct(xh, xeh, bh, op_h)
+        op_h.close()
+        if i >= args.warmup:
+            e2e.append((time.perf_counter() - t0) * 1e3)
+        assert inf_h.success
+    field = 16 * n
+    line = {"workload": "even/odd solve of M x = b (prepare, CG on m^2 - D_eo D_oe to 1e-10, reconstruct), "
+                        "1024x1024, m=0.01, checkerboarded FP32 CG with FP64 reliable updates",
+            "metric": "even/odd solve time", "value": round(statistics.mean(times), 3), "unit": "ms",
+            "higher_is_better": False, "steps": args.steps, "warmup": args.warmup, "dtype": "fp32 (FP64 reliable)",
+            "data": "synthetic: std::mt19937(1337) links and gaussian source (the oracle's generator)",
+            "l2": "flushed (512 MiB write) before every step",
+            "e2e": {"value": round(statistics.mean(e2e), 3), "unit": "ms",
+                    "h2d_bytes_per_step": 2 * field + field + 2 * field + 2 * field,
+                    "d2h_bytes_per_step": 3 * field},
+            "results": {"solver": info.name, "inner_iters": info.iter, "reliable_updates": info.reliable_updates,
+                        "inner_kernel_ms": round(info.kernel_ms, 3),
+                        "inner_us_per_iter": round(1e3 * info.kernel_ms / max(1, info.iter), 3),
+                        "true_relres_full_system_fp64": relres,
+                        "ms_min_max": [round(min(times), 3), round(max(times), 3)]},
+            "clocks": clk}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        O = pyoracle.Oracle()
+        nth = O.set_threads(None)
+        oeo = pyoracle.Operator("staggered_m2mdeodoe", LX, LY, MASS, U)
+        t0 = time.perf_counter()
+        rhs_o = O.eoprec_prepare(oeo, b)
+        xo_e, oinfo, _ = O.solve("cg", oeo, rhs_o, max_iter=MAX_ITER, eps=EPS)
+        x_or = O.eoprec_reconstruct(oeo, xo_e, b)
+        cpu_ms = (time.perf_counter() - t0) * 1e3
+        line["results"]["oracle_iters"] = oinfo["iter"]
+        line["results"]["err_vs_oracle"] = float(np.linalg.norm(xg - x_or) / np.linalg.norm(x_or))
+        line["cpu_baseline"] = {"value": round(cpu_ms, 3), "unit": "ms", "cores": nth, "kind": "port",
+                                "sample": f"one complete FP64 even/odd solve (prepare, {oinfo['iter']} CG iterations, "
+                                          f"reconstruct) by the oracle, operator and vector loops on {nth} host "
+                                          f"threads, sums serial in the reference's order"}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -730,7 +833,7 @@ def main():
     ap.add_argument("--rows-kernels", action="store_true",
                     help="rows workload: the kernels only (no solves, no CPU baseline), for a launch list")
     ap.add_argument("--workload", default="headline",
-                    choices=["headline", "multishift", "batch", "siblings", "rows"],
+                    choices=["headline", "multishift", "batch", "siblings", "rows", "eo"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")
     ap.add_argument("--probe-iters", type=int, default=0,
                     help="run one headline-variant solve stopped after this many inner iterations "
@@ -746,6 +849,8 @@ def main():
         return workload_siblings(args)
     if args.workload == "rows" and args.impl == "ours":
         return workload_rows(args)
+    if args.workload == "eo" and args.impl == "ours":
+        return workload_eo(args)
     if args.impl == "reference":
         return run_reference(args)
     if args.kernels_only:

@@ -372,9 +372,13 @@ static void stencil_apply(const orc_op *op, cplx *lhs, const cplx *rhs, int pari
  * (square_staggered_doe_u1): the hopping part of square_staggered_u1 (no mass) at the even
  * (odd = 0) or odd (odd = 1) output sites, in the reference's order +x, -x, +y, -y, then the
  * factor 1/2; sites of the other parity are zeroed. */
-static void staggered_hop_parity(cplx *lhs, const cplx *rhs, const cplx *U, int lx, int ly, int odd)
+static void hop_parity_range(void *ctx, long lo, long hi)
 {
-    for (long i = 0; i < (long)lx * ly; i++) {
+    const site_args *a = (const site_args *)ctx;
+    cplx *lhs = a->lhs;
+    const cplx *rhs = a->rhs, *U = a->U;
+    const int lx = a->lx, ly = a->ly, odd = (int)a->sign;
+    for (long i = lo; i < hi; i++) {
         int x = (int)(i % lx), y = (int)(i / lx);
         double eta1 = (double)(1 - 2 * (x % 2));
         lhs[i] = 0.0;
@@ -390,21 +394,45 @@ static void staggered_hop_parity(cplx *lhs, const cplx *rhs, const cplx *U, int 
     }
 }
 
+/* (site loop spread over the pool; each site is independent, so the result is the serial
+ * loop's bit for bit) */
+static void staggered_hop_parity(cplx *lhs, const cplx *rhs, const cplx *U, int lx, int ly, int odd)
+{
+    site_args a = {lhs, rhs, U, 0.0, (double)odd, lx, ly};
+    par_range((long)lx * ly, hop_parity_range, &a);
+}
+
 static int site_even(long i, int lx) { return ((i % lx) + (i / lx)) % 2 == 0; }
 
 /* operators.cpp:566-589 (square_staggered_m2mdeodoe_u1): tmp = D_oe rhs; lhs = D_eo tmp;
  * lhs = m*m rhs - lhs on even sites (odd sites stay zero).  The stencil form
  * (operators_stencil.cpp:195-216, apply_square_staggered_m2mdeodoe_stencil) uses
  * apply_stencil_2d_oe / _eo and shift*shift. */
+static void m2m_even_range(void *ctx, long lo, long hi)
+{
+    const site_args *a = (const site_args *)ctx;
+    const double m2 = a->mass * a->mass;
+    for (long i = lo; i < hi; i++)
+        if (site_even(i, a->lx)) a->lhs[i] = m2 * a->rhs[i] - a->lhs[i];
+}
+
 static void m2mdeodoe_apply(const orc_op *op, cplx *lhs, const cplx *rhs)
 {
     const long v = (long)op->lx * op->ly;
-    cplx *tmp = (cplx *)malloc(sizeof(cplx) * v);
+    /* the intermediate D_oe rhs, kept between calls (the oracle is driven from one thread) */
+    static cplx *tmp = NULL;
+    static long tmp_n = 0;
+    if (tmp_n < v) {
+        free(tmp);
+        tmp = (cplx *)malloc(sizeof(cplx) * v);
+        tmp_n = tmp ? v : 0;
+        if (!tmp) return;
+    }
     if (op->kind == ORC_STAGGERED_M2MDEODOE) {
         staggered_hop_parity(tmp, rhs, CCX(op->links), op->lx, op->ly, 1);
         staggered_hop_parity(lhs, tmp, CCX(op->links), op->lx, op->ly, 0);
-        for (long i = 0; i < v; i++)
-            if (site_even(i, op->lx)) lhs[i] = (op->mass * op->mass) * rhs[i] - lhs[i];
+        site_args a = {lhs, rhs, NULL, op->mass, 0.0, op->lx, op->ly};
+        par_range(v, m2m_even_range, &a);
     } else {
         const cplx shift = mk(op->shift[0], op->shift[1]);
         stencil_apply(op, tmp, rhs, 2);
@@ -412,7 +440,6 @@ static void m2mdeodoe_apply(const orc_op *op, cplx *lhs, const cplx *rhs)
         for (long i = 0; i < v; i++)
             if (site_even(i, op->lx)) lhs[i] = (shift * shift) * rhs[i] - lhs[i];
     }
-    free(tmp);
 }
 
 /* operators.cpp:543-563 (square_staggered_eoprec_prepare) and operators_stencil.cpp:179-193
