@@ -50,11 +50,11 @@ HEADLINE = ("fp32", 1)
 #     per SM
 CAPTURES = {
     "resident": {"source": "generic-linalg_gb300/csrc/stag_resident.cuh",
-                 "sha256": "3d75a586d3f867a3054056790f22b36ceabeed0d5412e3112c894a6260f9d6e2",
+                 "sha256": "5cff730dfc24880feeabc9cca4e08fde534ede08f16e7543afee199bca0c321e",
                  "kernel": "k_resident<14, 4, 3> (16 warps, x_lo and links in tensor memory)",
                  "profile": "profiles/k_resident_fp32_1024.md", "iters_per_launch": 20,
-                 "dram_bytes_per_launch": 42.130688e6 + 0.043008e6,
-                 "smem_wavefronts_per_sm_iter": 19948889 / (152 * 20)},
+                 "dram_bytes_per_launch": 42.142208e6 + 0.022272e6,
+                 "smem_wavefronts_per_sm_iter": 18110200 / (152 * 20)},
     "persist": {"source": "generic-linalg_gb300/csrc/stag_tiles.cuh", "sha256": None,
                 "kernel": "k_persist", "profile": "profiles/k_persist_fp32_1024.md", "iters_per_launch": 254,
                 "dram_bytes_per_launch": 41.987328e6 + 3.212544e6},

@@ -505,28 +505,62 @@ __device__ __forceinline__ float total_partials(const float2 *sm_hl, unsigned nb
 }
 
 // Phase A's pointwise pass over the thread's rows: t = u + beta t_old into T and p' = r + beta p;
-// returns |t|^2 + sigma |p'|^2.  Sites of the bottom and top row of the rectangle go to the
-// mailbox mbT (epoch e) as they are computed.  T and F are distinct buffers: restrict-qualified, the loads of later rows need not
-// wait for the stores of earlier ones.
-template <int NY>
+// returns |t|^2 + sigma |p'|^2.  T and F point at the thread's first row; restrict-qualified,
+// so the loads of later rows need not wait for the stores of earlier ones.  FULL (nrow == NY)
+// drops the per-row guard, and the values of the rectangle's bottom row (the thread's row 0)
+// and top row (the thread's row qtop) come out in vbot / vtop for the caller to post: with no
+// branch between the rows, the compiler interleaves their shared-memory loads (the posts inside
+// the loop, each under its own test, cost the pass 40% of its time).
+template <int NY, bool FULL>
 __device__ __forceinline__ float pass_A(float2 *__restrict__ T, const float2 *__restrict__ F, const float2 (&u)[NY],
-                                        float2 (&pv)[NY], float beta, float sigma, int c0, int nrow,
-                                        unsigned long long *mbT, unsigned e, int xl, int yb, int tyb)
+                                        float2 (&pv)[NY], float beta, float sigma, int nrow, int qtop, float2 &vbot,
+                                        float2 &vtop)
 {
     float acc = 0.f;
 #pragma unroll
     for (int q = 0; q < NY; q++) {
-        if (q < nrow) {
-            const int c = c0 + q * kPW;
-            const float2 tv = fadd(u[q], fscale(beta, T[c]));
-            const float2 pn = fadd(F[c], fscale(beta, pv[q]));
-            pv[q] = pn;
-            T[c] = tv;
-            post_rows(mbT, e, xl, yb + q, tyb, tv);
-            acc += fn2(tv) + sigma * fn2(pn);
-        }
+        if (!FULL && q >= nrow) break;
+        const float2 tv = fadd(u[q], fscale(beta, T[q * kPW]));
+        const float2 pn = fadd(F[q * kPW], fscale(beta, pv[q]));
+        pv[q] = pn;
+        T[q * kPW] = tv;
+        if (q == 0) vbot = tv;
+        vtop = q == qtop ? tv : vtop;
+        acc += fn2(tv) + sigma * fn2(pn);
     }
     return acc;
+}
+
+// Phase B's pointwise pass: r -= alpha Ap into R (the thread's first row), x_lo += alpha p' in
+// registers (XREG) or in global memory (XGLOB, xg: the thread's first row of x_lo, rows lx
+// apart); returns |r|^2.  Border rows as in pass_A.
+template <int NY, bool FULL, bool XREG, bool XGLOB, int NX>
+__device__ __forceinline__ float pass_B(float2 *__restrict__ R, const float2 (&ap)[NY], const float2 (&pv)[NY],
+                                        float2 (&xv)[NX], float2 *xg, int lx, float alpha, int nrow, int qtop,
+                                        float2 &vbot, float2 &vtop)
+{
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (!FULL && q >= nrow) break;
+        if (XREG) xv[q < NX ? q : 0] = fadd(xv[q < NX ? q : 0], fscale(alpha, pv[q]));
+        else if (XGLOB) red_add2(xg + (long)q * lx, fscale(alpha, pv[q]));
+        const float2 rnv = fsub(R[q * kPW], fscale(alpha, ap[q]));
+        R[q * kPW] = rnv;
+        if (q == 0) vbot = rnv;
+        vtop = q == qtop ? rnv : vtop;
+        acc += fn2(rnv);
+    }
+    return acc;
+}
+
+// Posts the rectangle's bottom row (vbot, when the thread's first row is row 0) and top row
+// (vtop, the thread's row qtop) after a pointwise pass.
+__device__ __forceinline__ void post_border_rows(unsigned long long *mb, unsigned e, int xl, int yb, int nrow,
+                                                 int qtop, int tyb, float2 vbot, float2 vtop)
+{
+    if (yb == 0 && nrow > 0) post_rows(mb, e, xl, 0, tyb, vbot);
+    if (qtop >= 0 && qtop < nrow) post_rows(mb, e, xl, tyb - 1, tyb, vtop);
 }
 
 // Publishes the block's partial sum of phase e (every thread passes its `acc`): FP32 sums within warps and across the block's warps, one
@@ -756,6 +790,7 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
     unsigned long long *const mbR = Mr + 2 * (size_t)blockIdx.x * nslot;
     unsigned long long *const mbT = Mt + 2 * (size_t)blockIdx.x * nslot;
     const int grow = (y0 + yb) * lx + x0 + xl;      // lattice index of the thread's first row
+    const int qtop = tyb - 1 - yb;                  // the thread's row that is the rectangle's last
     if (tid == 0) {
         sm_err = 0;
         sc.rsq = (float)s->rsq;
@@ -899,7 +934,14 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
         }
         first = false;
         const unsigned eA = ++ep;
-        float acc = pass_A<NY>(R.T, Rr, tmp, pv, fb, sigma, (yb + 1) * kPW + xl + 1, nrow, mbT, eA, xl, yb, tyb);
+        float acc;
+        {
+            const int c0 = (yb + 1) * kPW + xl + 1;
+            float2 vb = make_float2(0.f, 0.f), vt = vb;
+            if (nrow == NY) acc = pass_A<NY, true>(R.T + c0, Rr + c0, tmp, pv, fb, sigma, nrow, qtop, vb, vt);
+            else acc = pass_A<NY, false>(R.T + c0, Rr + c0, tmp, pv, fb, sigma, nrow, qtop, vb, vt);
+            post_border_rows(mbT, eA, xl, yb, nrow, qtop, tyb, vb, vt);
+        }
         post_columns(mbT, eA, R.T, warp % kWX, yb, nrow, ty);
         publish_sum<NW>(acc, pf, eA, sm_w);
         if (has_ring) R.T[rslot] = poll_slot(Mt + rsrc, eA, pf, &sm_err, lim);
@@ -950,17 +992,16 @@ k_resident(const float2 *__restrict__ H, float2 *r, float2 *p0, float2 *xlo, flo
 #pragma unroll
             for (int q = 0; q < NY; q++) tmem_st2(xcol + 2 * q, fadd(xt[q], fscale(alpha, pv[q])));
         }
-#pragma unroll
-        for (int q = 0; q < NY; q++) {
-            if (q < nrow) {
-                const int yl = yb + q, c = (yl + 1) * kPW + xl + 1;
-                if (XREG) xv[q] = fadd(xv[q], fscale(alpha, pv[q]));
-                else if (!XTM) red_add2(xlo + grow + q * lx, fscale(alpha, pv[q]));
-                const float2 rnv = fsub(Rr[c], fscale(alpha, tmp[q]));
-                Rr[c] = rnv;
-                post_rows(mbR, eB, xl, yl, tyb, rnv);
-                acc += fn2(rnv);
-            }
+        {
+            const int c0 = (yb + 1) * kPW + xl + 1;
+            float2 vb = make_float2(0.f, 0.f), vt = vb;
+            if (nrow == NY)
+                acc = pass_B<NY, true, XREG, !XREG && !XTM>(Rr + c0, tmp, pv, xv, xlo + grow, lx, alpha, nrow, qtop,
+                                                           vb, vt);
+            else
+                acc = pass_B<NY, false, XREG, !XREG && !XTM>(Rr + c0, tmp, pv, xv, xlo + grow, lx, alpha, nrow, qtop,
+                                                            vb, vt);
+            post_border_rows(mbR, eB, xl, yb, nrow, qtop, tyb, vb, vt);
         }
         post_columns(mbR, eB, Rr, warp % kWX, yb, nrow, ty);
         publish_sum<NW>(acc, pf, eB, sm_w);

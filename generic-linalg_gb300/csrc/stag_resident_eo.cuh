@@ -112,6 +112,51 @@ __device__ __forceinline__ void hop_rows_eo(const RectEO &S, const float2 *__res
     }
 }
 
+// The pointwise passes after each stencil, over the thread's rows of column xl (T, R: the
+// thread's first row in the t and r buffers).  FULL (nrow == NY) drops the per-row guard, and
+// the border rows' values come out in vbot (the rectangle's first row, when the thread owns it)
+// and vtop (row qtop of the thread), so that the rows carry no branch between them and the
+// compiler can interleave their shared-memory loads; the posts follow the pass.
+// A: t = u + beta t_old, p' = r + beta p; returns |t|^2 + m2s |p'|^2.
+template <int NY, bool FULL>
+__device__ __forceinline__ float update_A(float2 *__restrict__ T, const float2 *__restrict__ R, const float2 (&u)[NY],
+                                          float2 (&pv)[NY], float beta, float m2s, int nrow, int qtop, float2 &vbot,
+                                          float2 &vtop)
+{
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (!FULL && q >= nrow) break;
+        const float2 tv = fadd(u[q], fscale(beta, T[q * kPW]));
+        const float2 pn = fadd(R[q * kPW], fscale(beta, pv[q]));
+        pv[q] = pn;
+        T[q * kPW] = tv;
+        if (q == 0) vbot = tv;
+        vtop = q == qtop ? tv : vtop;
+        acc += fn2(tv) + m2s * fn2(pn);
+    }
+    return acc;
+}
+
+// B: x_lo += alpha p', r -= alpha Ap; returns |r|^2.
+template <int NY, bool FULL>
+__device__ __forceinline__ float update_B(float2 *__restrict__ R, const float2 (&ap)[NY], const float2 (&pv)[NY],
+                                          float2 (&xv)[NY], float alpha, int nrow, int qtop, float2 &vbot, float2 &vtop)
+{
+    float acc = 0.f;
+#pragma unroll
+    for (int q = 0; q < NY; q++) {
+        if (!FULL && q >= nrow) break;
+        xv[q] = fadd(xv[q], fscale(alpha, pv[q]));
+        const float2 rnv = fsub(R[q * kPW], fscale(alpha, ap[q]));
+        R[q * kPW] = rnv;
+        if (q == 0) vbot = rnv;
+        vtop = q == qtop ? rnv : vtop;
+        acc += fn2(rnv);
+    }
+    return acc;
+}
+
 }  // namespace reseo
 
 // The kernel: one cooperative launch per reliable-update cycle, one block of 16 warps (4 across,
@@ -169,6 +214,8 @@ k_resident_eo(const float2 *__restrict__ H2, float2 *r, float2 *p0, float2 *xlo,
     unsigned long long *const mbR = Mr + 2 * (size_t)blockIdx.x * nslot;
     unsigned long long *const mbT = Mt + 2 * (size_t)blockIdx.x * nslot;
     const long grow = (long)(y0 + yb) * hw + x0 + xl;  // packed index of the thread's first row
+    float2 *const Tt = S.T + (yb + 1) * kPW + xl + 1, *const Rt = S.R + (yb + 1) * kPW + xl + 1;
+    const int qtop = tyb - 1 - yb;  // the thread's row that is the rectangle's last (if in range)
     if (tid == 0) {
         sm_err = 0;
         sc.rsq = (float)s->rsq;
@@ -275,18 +322,13 @@ k_resident_eo(const float2 *__restrict__ H2, float2 *r, float2 *p0, float2 *xlo,
         }
         first = false;
         const unsigned eA = ++ep;
-        float acc = 0.f;
-#pragma unroll
-        for (int q = 0; q < NY; q++) {
-            if (q < nrow) {
-                const int c = (yb + q + 1) * kPW + xl + 1;
-                const float2 tv = fadd(tmp[q], fscale(fb, S.T[c]));
-                const float2 pn = fadd(S.R[c], fscale(fb, pv[q]));
-                pv[q] = pn;
-                S.T[c] = tv;
-                post_rows(mbT, eA, xl, yb + q, tyb, tv);
-                acc += fn2(tv) + (m2 + sigma) * fn2(pn);
-            }
+        float acc;
+        {
+            float2 vb = make_float2(0.f, 0.f), vt = vb;
+            if (nrow == NY) acc = update_A<NY, true>(Tt, Rt, tmp, pv, fb, m2 + sigma, nrow, qtop, vb, vt);
+            else acc = update_A<NY, false>(Tt, Rt, tmp, pv, fb, m2 + sigma, nrow, qtop, vb, vt);
+            if (yb == 0 && nrow > 0) post_rows(mbT, eA, xl, 0, tyb, vb);
+            if (qtop >= 0 && qtop < nrow) post_rows(mbT, eA, xl, tyb - 1, tyb, vt);
         }
         post_columns(mbT, eA, S.T, warp % kWX, yb, nrow, ty);
         publish_sum<NW>(acc, pf, eA, sm_w);
@@ -315,17 +357,12 @@ k_resident_eo(const float2 *__restrict__ H2, float2 *r, float2 *p0, float2 *xlo,
         if (sm_ctl != kResGo) break;
         const float alpha = sm_scalar;
         const unsigned eB = ++ep;
-        acc = 0.f;
-#pragma unroll
-        for (int q = 0; q < NY; q++) {
-            if (q < nrow) {
-                const int yl = yb + q, c = (yl + 1) * kPW + xl + 1;
-                xv[q] = fadd(xv[q], fscale(alpha, pv[q]));
-                const float2 rnv = fsub(S.R[c], fscale(alpha, tmp[q]));
-                S.R[c] = rnv;
-                post_rows(mbR, eB, xl, yl, tyb, rnv);
-                acc += fn2(rnv);
-            }
+        {
+            float2 vb = make_float2(0.f, 0.f), vt = vb;
+            if (nrow == NY) acc = update_B<NY, true>(Rt, tmp, pv, xv, alpha, nrow, qtop, vb, vt);
+            else acc = update_B<NY, false>(Rt, tmp, pv, xv, alpha, nrow, qtop, vb, vt);
+            if (yb == 0 && nrow > 0) post_rows(mbR, eB, xl, 0, tyb, vb);
+            if (qtop >= 0 && qtop < nrow) post_rows(mbR, eB, xl, tyb - 1, tyb, vt);
         }
         post_columns(mbR, eB, S.R, warp % kWX, yb, nrow, ty);
         publish_sum<NW>(acc, pf, eB, sm_w);
