@@ -173,3 +173,36 @@ def test_checkerboarded_wait_limit_runs_out_cleanly(gl, gpu):
     eo.apply(Ax, x)
     rr = (torch.linalg.vector_norm(rhs_e - Ax) / torch.linalg.vector_norm(rhs_e)).item()
     assert rr < 1e-10, rr
+
+
+@pytest.mark.parametrize("case", ["source_nan", "link_inf", "zero_source"])
+def test_checkerboarded_failure_statuses(gl, gpu, case):
+    """The checkerboarded even/odd solve (256 x 256, where lx allows the packed layout) stops
+    with GLINALG_SOLVE_NONFINITE on a NaN in the prepared source or an Inf in the links, and
+    with GLINALG_SOLVE_BREAKDOWN and x = 0 on an all-zero source; an ordinary solve converges
+    on the same device afterwards."""
+    lx = ly = 256
+    U, b = system(gl, lx=lx, ly=ly)
+    if case == "link_inf":
+        U[2 * 1000 + 1] = complex(float("inf"), 0.0)
+    extra = gl.StaggeredU1Op(U, 0.05, lx, ly)
+    rhs_e = np.zeros_like(b)
+    if case != "zero_source":
+        gl.square_staggered_eoprec_prepare(rhs_e, b, extra)
+    if case == "source_nan":
+        rhs_e[2 * 777] = complex(float("nan"), 0.0)  # an even site (row 6, x = 18)
+    x = np.zeros_like(b)
+    info = gl.minv_vector_cg(x, rhs_e, b.size, 20000, 1e-10, gl.square_staggered_m2mdeodoe_u1, extra, precision=1)
+    assert not info.success
+    if case == "zero_source":
+        assert info.status == gl.GLINALG_SOLVE_BREAKDOWN, info
+        assert np.all(x == 0)
+    else:
+        assert info.status == gl.GLINALG_SOLVE_NONFINITE, info
+    U2, b2 = system(gl, seed=9, lx=lx, ly=ly)
+    ok = gl.StaggeredU1Op(U2, 0.05, lx, ly)
+    r2 = np.zeros_like(b2)
+    gl.square_staggered_eoprec_prepare(r2, b2, ok)
+    x2 = np.zeros_like(b2)
+    info2 = gl.minv_vector_cg(x2, r2, b2.size, 20000, 1e-10, gl.square_staggered_m2mdeodoe_u1, ok, precision=1)
+    assert info2.success and info2.name == "CG-FP32-EO", info2
