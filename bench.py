@@ -92,7 +92,8 @@ PERSIST_KERNELS = {0: "k_persist<16 warps, 4 rows>", 1: "k_persist<16 warps, 8 r
                    11: "k_resident<16 warps, x_lo in tensor memory> (rectangle state on chip)",
                    12: "k_resident<32 warps, x_lo in tensor memory> (rectangle state on chip)",
                    13: "k_resident<16 warps, x_lo and links in tensor memory> (rectangle state on chip)",
-                   14: "k_resident<32 warps, x_lo and links in tensor memory> (rectangle state on chip)"}
+                   14: "k_resident<32 warps, x_lo and links in tensor memory> (rectangle state on chip)",
+                   15: "k_resident_s<16 warps, 16-bit p' and t> (rectangle state on chip, t = D p' each iteration)"}
 
 
 def peaks():

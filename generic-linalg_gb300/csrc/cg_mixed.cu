@@ -44,6 +44,7 @@
 #include "stag_bulk.cuh"
 #include "stag_resident.cuh"
 #include "stag_resident_eo.cuh"
+#include "stag_resident_s.cuh"
 
 namespace glinalg {
 
@@ -431,12 +432,14 @@ struct PersistKernel {
 // 16 warps with x_lo in registers, 32 warps, 16 warps with x_lo in global memory; candidates
 // 9 and 10 its single-reduction form (k_resident1) with 16 and 32 warps; candidates 11 and 12
 // the two-reduction form with x_lo in tensor memory, 16 and 32 warps; candidates 13 and 14 the
-// same with the links in tensor memory too.
-constexpr int kNumPersist = 15;
+// same with the links in tensor memory too.  Candidate 15 is the rectangle-resident kernel of
+// the 16-bit variants (stag_resident_s.cuh: t = D p' formed from the stored p' each iteration).
+constexpr int kNumPersist = 16;
+constexpr int kResident16Cand = 15;
 static const int kPersistBY[kNumPersist] = {16, 16, 32, 16, bulk::kBY, bulk::kBY, res::kWX * 4, res::kWX * 8,
                                             res::kWX * 4, res::kWX * 4, res::kWX * 8, res::kWX * 4, res::kWX * 8,
-                                            res::kWX * 4, res::kWX * 8};
-static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+                                            res::kWX * 4, res::kWX * 8, res::kWX * ress::kWY};
+static const int kPersistNY[kNumPersist] = {4, 8, 2, 2, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 constexpr int kResidentCand = 6;  // 6 .. 14
 static bool is_resident(int c) { return c >= kResidentCand && c <= kResidentCand + 8; }
 static int resident_wy(int c)
@@ -465,13 +468,32 @@ static res::Plan resident_plan(int lx, int ly, int wy)
     return res::plan(lx, ly, sm_count(), (size_t)std::max(0, optin - 512), wy);
 }
 
+// The rectangle grid of the 16-bit resident kernel (S: the storage of p' and t, LK: the links).
+static res::Plan resident16_plan(int lx, int ly, size_t s_bytes, size_t lk_bytes)
+{
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        cudaGetLastError();
+        return res::Plan{};
+    }
+    return ress::plan(lx, ly, sm_count(), (size_t)std::max(0, optin - 512), s_bytes, lk_bytes);
+}
+
+// storage bytes of the variant's p' / t and links (FP16: 4 and 4; BF16: 4 and 8)
+static size_t variant_s_bytes(int variant) { return variant == 1 ? 8 : 4; }
+static size_t variant_lk_bytes(int variant) { return variant == 2 ? 4 : 8; }
+
 static bool persist_applies(int lx, int ly);
 
-// Whether persistent candidate c serves an lx x ly lattice in variant `variant` (the resident
-// kernel exists for the FP32 variant only).
+// Whether persistent candidate c serves an lx x ly lattice in variant `variant` (the FP32
+// resident kernels serve the FP32 variant, candidate 15 the 16-bit ones).
 static bool persist_cand_applies(int c, int lx, int ly, int variant)
 {
     if (is_resident(c)) return variant == 1 && resident_plan(lx, ly, resident_wy(c)).ok;
+    if (c == kResident16Cand)
+        return (variant == 2 || variant == 3) &&
+               resident16_plan(lx, ly, variant_s_bytes(variant), variant_lk_bytes(variant)).ok;
     if (!persist_applies(lx, ly)) return false;
     if (c == 4) return bulk_applies<bulk::Geom256x4>(lx, ly, sm_count());
     if (c == 5) return bulk_applies<bulk::Geom512x2>(lx, ly, sm_count());
@@ -562,8 +584,22 @@ static PersistKernel<S, R, LK> persist_cand(int c, int lx, int ly)
     if (c < 0 || c >= kNumPersist) return pk;
     pk.by = kPersistBY[c];
     pk.ny = kPersistNY[c];
-    if (is_resident(c)) {
-        resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xmode(c), resident_single(c));
+    if (is_resident(c) || c == kResident16Cand) {
+        if (c == kResident16Cand) {
+            pk.plan = resident16_plan(lx, ly, sizeof(S), sizeof(LK));
+            if (!pk.plan.ok) return pk;
+            pk.smem = (int)pk.plan.smem;
+            pk.grid = pk.plan.gx * pk.plan.gy;
+            if constexpr (std::is_same<R, float2>::value) {
+                switch (pk.plan.ny) {
+                case 4: pk.fr = k_resident_s<4, S, LK>; break;
+                case 8: pk.fr = k_resident_s<8, S, LK>; break;
+                default: pk.fr = k_resident_s<14, S, LK>; break;
+                }
+            }
+        } else {
+            resident_kernel<S, R, LK>(pk, lx, ly, resident_wy(c), resident_xmode(c), resident_single(c));
+        }
         if (!pk.fr) return pk;
         const void *fp = reinterpret_cast<const void *>(pk.fr);
         int per_sm = 0;
@@ -909,7 +945,9 @@ static glinalg_status run_mixed(const glinalg_operator_s *op, double2 *x, const 
         GL_TRY(sc.zeros(&pf, 1));
         // border mailboxes of the rectangle-resident kernel (the same rectangles for 16 and 32 warps)
         const res::Plan rp = resident_plan(lx, ly, 4);
+        const res::Plan rp16 = resident16_plan(lx, ly, sizeof(S), sizeof(LK));
         if (variant == 1 && rp.ok) GL_TRY(sc.zeros(&mbox, res::mbox_words(sm_count(), rp.ty)));
+        else if (variant != 1 && rp16.ok) GL_TRY(sc.zeros(&mbox, res::mbox_words(sm_count(), rp16.ty)));
         GL_TRY(sc.alloc(&partA, sm_count()));
         GL_TRY(sc.alloc(&partB, sm_count()));
     }

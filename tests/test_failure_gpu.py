@@ -94,6 +94,7 @@ import numpy as np, torch
 sys.path.insert(0, sys.argv[1])
 gl = importlib.import_module("generic-linalg_gb300")
 lx = ly = int(sys.argv[2])
+prec = int(sys.argv[3])
 g = gl.Generator(1337)
 U = g.rand_gauge_u1(lx, ly)
 b = g.gaussian(lx * ly)
@@ -102,18 +103,18 @@ op = gl.Operator(2, lx, ly, 0.01, torch.from_numpy(U).to(dev))
 bt = torch.from_numpy(b).to(dev)
 out = {}
 x = torch.zeros_like(bt)
-first = gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=1)
+first = gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=prec)
 out["first"] = [bool(first.success), first.status, first.kernel_launches]
-out["tuned"] = gl.lib().glinalg_tuned_persist(op.handle, 1)
+out["tuned"] = gl.lib().glinalg_tuned_persist(op.handle, prec)
 x.zero_()
 try:
-    gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=1,
+    gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=prec,
                       wait_limit_us=-1)
     out["timeout"] = None
 except gl.SolveTimeout as e:
     out["timeout"] = [e.info.status, bool(e.info.success), str(e)]
 x.zero_()
-after = gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=1)
+after = gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=prec)
 Ax = torch.zeros_like(bt)
 op.apply(Ax, x)
 out["after"] = [bool(after.success), after.status,
@@ -122,20 +123,21 @@ print(json.dumps(out))
 '''
 
 
-@pytest.mark.parametrize("shape", [13, 11, 8, 0])
-def test_persistent_wait_limit_runs_out_cleanly(gl, gpu, tmp_path, shape):
+@pytest.mark.parametrize("shape,prec", [(13, 1), (11, 1), (8, 1), (0, 1), (15, 2), (15, 3)])
+def test_persistent_wait_limit_runs_out_cleanly(gl, gpu, tmp_path, shape, prec):
     """glinalg_solver_params.wait_limit_us < 0 makes every wait of the persistent inner loop on
     other blocks give up at its first miss.  The kernel raises its error word, every block leaves
     its loop (tensor memory written back and freed), and the call reports
     GLINALG_SOLVE_TIMEOUT; a normal solve on the same device then converges.  Shapes: the
     resident kernel with x_lo and links in tensor memory (13), with x_lo in tensor memory (11),
-    with x_lo in L2 (8), and the register-tiled kernel with grid barriers (0)."""
+    with x_lo in L2 (8), the register-tiled kernel with grid barriers (0), and the resident
+    kernel of the FP16 and BF16 variants (15)."""
     script = tmp_path / "timeout_case.py"
     script.write_text(TIMEOUT_SCRIPT)
     env = dict(os.environ)
     env["GLINALG_PERSIST_SHAPE"] = str(shape)
-    p = subprocess.run([sys.executable, str(script), ROOT, "1024"], env=env, capture_output=True, text=True,
-                       timeout=600)
+    p = subprocess.run([sys.executable, str(script), ROOT, "1024", str(prec)], env=env, capture_output=True,
+                       text=True, timeout=600)
     assert p.returncode == 0, p.stderr[-3000:]
     res = json.loads(p.stdout.strip().splitlines()[-1])
     assert res["tuned"] == shape, res

@@ -1,8 +1,9 @@
-"""The persistent inner-loop kernels of the FP32 mixed-precision CG (one cooperative launch per
+"""The persistent inner-loop kernels of the mixed-precision CG (one cooperative launch per
 reliable-update cycle): the register-tiled kernels, the bulk-copy kernels and the
 rectangle-resident kernel (shared-memory / register state per SM, borders exchanged through
 L2) in its two-reduction and single-reduction forms, with x_lo in registers, global memory or
-tensor memory, and with x_lo and the links in tensor memory.  Each candidate is forced with GLINALG_PERSIST_SHAPE in a process of its own (the
+tensor memory, and with x_lo and the links in tensor memory; and the rectangle-resident kernel
+of the FP16 / BF16 variants.  Each candidate is forced with GLINALG_PERSIST_SHAPE in a process of its own (the
 autotuner's pick is cached per process).
 
 Bar: the FP64-true relative residual below 1e-10 (re-checked with the FP64 GPU operator), the
@@ -94,3 +95,63 @@ def test_resident_kernel_small_lattices(gl, gpu, tmp_path, lx, ly):
         res = run_case(tmp_path, lx, ly, 0.05, 99, shape)
         assert res["tuned"] == shape
         check(res, 1e3)
+
+
+SCRIPT16 = r'''
+import importlib, json, sys
+import numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+gl = importlib.import_module("generic-linalg_gb300")
+lx, ly, mass, seed = int(sys.argv[2]), int(sys.argv[3]), float(sys.argv[4]), int(sys.argv[5])
+g = gl.Generator(seed)
+U = g.rand_gauge_u1(lx, ly)
+b = g.gaussian(lx * ly)
+dev = torch.device("cuda:0")
+op = gl.Operator(2, lx, ly, mass, torch.from_numpy(U).to(dev))
+bt = torch.from_numpy(b).to(dev)
+x64 = torch.zeros_like(bt)
+gl.minv_vector_cg(x64, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op)
+out = {}
+for prec in (2, 3):
+    x = torch.zeros_like(bt)
+    info = gl.minv_vector_cg(x, bt, b.size, 100000, 1e-10, gl.square_staggered_normal_u1, op, precision=prec)
+    Ax = torch.zeros_like(bt)
+    op.apply(Ax, x)
+    out[str(prec)] = {"iter": info.iter, "success": bool(info.success), "launches": info.kernel_launches,
+                      "relres": (torch.linalg.vector_norm(bt - Ax) / torch.linalg.vector_norm(bt)).item(),
+                      "err": (torch.linalg.vector_norm(x - x64) / torch.linalg.vector_norm(x64)).item(),
+                      "tuned": gl.lib().glinalg_tuned_persist(op.handle, prec)}
+print(json.dumps(out))
+'''
+
+
+def run16(tmp_path, lx, ly, mass, seed, shape):
+    script = tmp_path / "persist16_case.py"
+    script.write_text(SCRIPT16)
+    env = dict(os.environ)
+    env["GLINALG_PERSIST_SHAPE"] = str(shape)
+    p = subprocess.run([sys.executable, str(script), ROOT, str(lx), str(ly), str(mass), str(seed)], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-3000:]
+    return json.loads(p.stdout.strip().splitlines()[-1])
+
+
+@pytest.mark.parametrize("lx,ly,mass", [(1024, 1024, 0.01), (256, 256, 0.05), (512, 300, 0.05), (128, 90, 0.05)])
+def test_resident_16bit_candidate(gl, gpu, tmp_path, lx, ly, mass):
+    """The rectangle-resident kernel of the FP16 and BF16 variants (candidate 15: t = D p'
+    formed from the stored p' every iteration) against the streaming persistent kernel of the
+    same variant (candidate 1) on the same system.  Bars: FP64-true relative residual below
+    1e-10; solution within 1e-9 of the FP64 GPU CG's (measured at 1024^2: 6.1e-11 FP16,
+    1.4e-11 BF16); at most 10% more inner iterations than the streaming kernel (measured at
+    1024^2: FP16 5456 against 5516, BF16 2342 against 6162: the resident kernel's stored p'
+    and t are the ones its stencils read, so its BF16 rounding stays consistent)."""
+    res = run16(tmp_path, lx, ly, mass, 1337, 15)
+    ref = run16(tmp_path, lx, ly, mass, 1337, 1) if lx % 32 == 0 and lx * ly >= 1024 * 1024 // 2 else None
+    for prec in ("2", "3"):
+        r = res[prec]
+        assert r["tuned"] == 15 and r["launches"] >= 1, r
+        assert r["success"] and r["relres"] < 1e-10, r
+        assert r["err"] < 1e-9, r
+        if ref is not None:
+            assert ref[prec]["tuned"] == 1, ref
+            assert r["iter"] <= 1.1 * ref[prec]["iter"], (r, ref[prec])
