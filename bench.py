@@ -251,8 +251,9 @@ def kernels_only(args):
 
 
 def probe_solve(args):
-    """One headline-variant solve of the 1024x1024 system stopped after --probe-iters inner
-    iterations: one launch of the persistent inner-loop kernel, a small case for ncu captures."""
+    """One solve of the 1024x1024 system in the variant --probe-variant (the headline's by
+    default) stopped after --probe-iters inner iterations: one launch of the persistent
+    inner-loop kernel, a small case for ncu captures."""
     import torch
     gl = importlib.import_module("generic-linalg_gb300")
     g = gl.Generator(SEED)
@@ -261,9 +262,10 @@ def probe_solve(args):
     op = gl.Operator(2, LX, LY, MASS, torch.from_numpy(U).cuda())
     bd = torch.from_numpy(b).cuda()
     x = torch.zeros_like(bd)
+    prec = dict([HEADLINE] + VARIANTS)[args.probe_variant]
     info = gl.minv_vector_cg(x, bd, bd.numel(), args.probe_iters, EPS, gl.square_staggered_normal_u1, op,
-                             precision=HEADLINE[1])
-    print(json.dumps({"probe": "headline variant, 1024x1024", "iters": info.iter,
+                             precision=prec)
+    print(json.dumps({"probe": f"{args.probe_variant} variant, 1024x1024", "iters": info.iter,
                       "kernel_launches": info.kernel_launches, "kernel_ms": info.kernel_ms}))
 
 
@@ -836,6 +838,8 @@ def main():
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "multishift", "batch", "siblings", "rows", "eo"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")
+    ap.add_argument("--probe-variant", default="fp32", choices=["fp32", "fp16", "bf16"],
+                    help="the variant of the --probe-iters solve")
     ap.add_argument("--probe-iters", type=int, default=0,
                     help="run one headline-variant solve stopped after this many inner iterations "
                          "(one persistent-kernel launch; a small case for ncu captures) and exit")
