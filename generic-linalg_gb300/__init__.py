@@ -101,6 +101,12 @@ class UnsupportedOperator(GlinalgError):
 
 # ---------------------------------------------------------------- field plumbing
 
+def release_memory():
+    """glinalg_release_memory: hand the memory the library's pools keep between calls (the work
+    vectors of finished calls) back to the device."""
+    _capi.check(lib().glinalg_release_memory(), "release_memory")
+
+
 def _is_torch(a):
     return type(a).__module__.startswith("torch")
 

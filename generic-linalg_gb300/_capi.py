@@ -75,6 +75,7 @@ def _prototypes():
         "glinalg_last_error": (C.c_char_p, []),
         "glinalg_device_count": (i, []),
         "glinalg_set_stream": (st, [vp, i]),
+        "glinalg_release_memory": (st, []),
         "glinalg_profile_mixed_kernels": (st, [vp, i, i, _dp, _dp]),
         "glinalg_tuned_tile": (i, [vp, i]),
         "glinalg_tuned_persist": (i, [vp, i]),

@@ -766,7 +766,7 @@ static int autotune(const glinalg_operator_s *op, int variant, R *r, S *p0, S *p
     h.max_iter = 0x7fffffff;
     std::vector<double2> ones(op->size, cmk(1.0, 0.0));
     double2 *d1 = nullptr;
-    if (cudaMallocAsync((void **)&d1, sizeof(double2) * op->size, st) != cudaSuccess) return 1;
+    if (lib_malloc_async((void **)&d1, sizeof(double2) * op->size, st) != cudaSuccess) return 1;
     cudaMemcpyAsync(d1, ones.data(), sizeof(double2) * op->size, cudaMemcpyHostToDevice, st);
     k_copy_links<R><<<vgrid(op->size), 256, 0, st>>>(r, d1, op->size);
     cudaFreeAsync(d1, st);
@@ -838,7 +838,7 @@ static void autotune_persist(const glinalg_operator_s *op, int variant, R *r, S 
     const long n = op->size;
     std::vector<double2> ones(n, cmk(1.0, 0.0));
     double2 *d1 = nullptr;
-    if (cudaMallocAsync((void **)&d1, sizeof(double2) * n, st) != cudaSuccess) return;
+    if (lib_malloc_async((void **)&d1, sizeof(double2) * n, st) != cudaSuccess) return;
     cudaMemcpyAsync(d1, ones.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, st);
     MxDev h = {};
     h.rsq = (double)n;  // |r|^2 of r = 1

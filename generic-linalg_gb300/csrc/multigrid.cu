@@ -375,8 +375,9 @@ extern "C" glinalg_status glinalg_mg_coarse_stencil(glinalg_mg_level l, glinalg_
     op->size = l->csize;
     cudaGetDevice(&op->device);
     const long cc = op->vol * op->nc * op->nc;
-    cudaError_t e = cudaMalloc((void **)&op->clover, sizeof(double2) * cc);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&op->hopping, sizeof(double2) * 4 * cc);
+    // (operator arrays come from the library's pool: the operator's destructor returns them there)
+    cudaError_t e = lib_malloc_async((void **)&op->clover, sizeof(double2) * cc, st);
+    if (e == cudaSuccess) e = lib_malloc_async((void **)&op->hopping, sizeof(double2) * 4 * cc, st);
     if (e != cudaSuccess) {
         set_last_error(std::string("coarse stencil: ") + cudaGetErrorString(e));
         delete op;

@@ -19,14 +19,6 @@ struct glinalg_operator_s {
     double2 *two_link = nullptr;
     double2 shift{0, 0}, eo_shift{0, 0}, dof_shift{0, 0};
 
-    // Reduced-precision link copies for the inner iterations of mixed-precision solves,
-    // built on first use: the staggered hopping coefficients with the 1/2 and eta folded
-    // in (exact in every format: powers of two and signs).  Layout per site i:
-    // {h_x(i) = -1/2 U_x(i), h_y(i) = -1/2 eta(i) U_y(i)}.
-    float2 *H32 = nullptr;
-    __half2 *H16 = nullptr;
-    __nv_bfloat162 *Hbf = nullptr;
-
     ~glinalg_operator_s();
 };
 
@@ -85,6 +77,9 @@ glinalg_status launch_staggered(const glinalg_operator_s *op, double2 *out, cons
 
 // The library's stream on the current device and its device-side scratch allocator.
 cudaStream_t lib_stream();
+// Stream-ordered allocation from the library's memory pool of the current device (freed with
+// cudaFreeAsync; the pool keeps freed memory for the next call).
+cudaError_t lib_malloc_async(void **p, size_t bytes, cudaStream_t st);
 void set_user_stream(cudaStream_t s, bool use);
 // A private stream of the current device used only to capture CUDA graphs.
 cudaStream_t capture_stream();

@@ -52,7 +52,7 @@ extern "C" glinalg_status glinalg_probe_smem_bandwidth(double *gbs, double *ms)
     GL_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     cudaStream_t st = lib_stream();
     float *sink = nullptr;
-    GL_CUDA(cudaMallocAsync((void **)&sink, sizeof(float) * 2 * nsm, st));
+    GL_CUDA(lib_malloc_async((void **)&sink, sizeof(float) * 2 * nsm, st));
     const int grid = 2 * nsm, reps = 4096;
     cudaEvent_t e0, e1;
     GL_CUDA(cudaEventCreate(&e0));

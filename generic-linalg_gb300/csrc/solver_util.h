@@ -22,9 +22,9 @@ class Scratch {
     glinalg_status alloc(T **out, size_t count)
     {
         void *p = nullptr;
-        cudaError_t e = cudaMallocAsync(&p, sizeof(T) * (count ? count : 1), st_);
+        cudaError_t e = lib_malloc_async(&p, sizeof(T) * (count ? count : 1), st_);
         if (e != cudaSuccess) {
-            set_last_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+            set_last_error(std::string("stream-ordered allocation: ") + cudaGetErrorString(e));
             return e == cudaErrorMemoryAllocation ? GLINALG_ERROR_OUT_OF_MEMORY : GLINALG_ERROR_CUDA;
         }
         ptrs_.push_back(p);

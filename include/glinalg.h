@@ -169,6 +169,11 @@ int glinalg_device_count(void);
  * return only after their work has finished. */
 glinalg_status glinalg_set_stream(void *stream, int use);
 
+/* The library takes the work vectors of its calls from a stream-ordered memory pool per device
+ * that keeps what calls free, so that repeated calls do not map device memory again.  This
+ * returns the pools' unused memory to the device; later calls allocate it again. */
+glinalg_status glinalg_release_memory(void);
+
 /* ---- operators ---- */
 glinalg_status glinalg_operator_create(const glinalg_op_desc *desc, glinalg_operator *out);
 glinalg_status glinalg_operator_destroy(glinalg_operator op);

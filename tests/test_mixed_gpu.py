@@ -143,3 +143,24 @@ def test_mixed_cg_default_delta(gl, gpu, golden):
         got[d] = (info.iter, info.reliable_updates)
     assert got[0.0] == got[0.01], got
     assert got[0.1][1] > got[0.01][1], got
+
+
+def test_release_memory_between_solves(gl, gpu):
+    """The library keeps the work vectors of finished calls in its memory pool; handing that
+    memory back (glinalg_release_memory) between two identical solves changes nothing in the
+    second solve's result."""
+    import torch
+    lx = ly = 256
+    g = gl.Generator(31)
+    U = g.rand_gauge_u1(lx, ly)
+    b = g.gaussian(lx * ly)
+    op = gl.Operator(2, lx, ly, 0.05, torch.from_numpy(U).to(gpu))
+    bd = torch.from_numpy(b).to(gpu)
+    xs = []
+    for k in range(2):
+        x = torch.zeros_like(bd)
+        info = gl.minv_vector_cg(x, bd, b.size, 10000, 1e-10, gl.square_staggered_normal_u1, op, precision=1)
+        assert info.success, info
+        xs.append(x)
+        gl.release_memory()
+    assert torch.equal(xs[0], xs[1])
