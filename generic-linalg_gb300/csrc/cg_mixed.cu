@@ -1466,6 +1466,7 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
     default: set_last_error("unknown precision"); return GLINALG_ERROR_INVALID_VALUE;
     }
     if (s != GLINALG_SUCCESS) return s;
+    if (!verb.prints_summary()) return GLINALG_SUCCESS;
     double bsqrt = 0.0;
     {
         // |b| for the summary line

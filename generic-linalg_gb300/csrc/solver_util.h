@@ -147,6 +147,8 @@ struct Verb {
     Verb precond_inner() const;  // shuffle_verbosity_precond (verbosity.h:46-67)
     void resid(const std::string &alg, int iter, int ops, double relres) const;
     void summary(const std::string &alg, bool success, int iter, int ops, double relres) const;
+    // whether summary() prints (a caller can skip the work of its arguments otherwise)
+    bool prints_summary() const { return present && (level == 1 || level == 2 || level == 3); }
     void summary_multi(bool success, int iter, int ops, const double *relres, int n) const;
     void restart(const std::string &alg, int iter, int ops, double relres) const;
 };
