@@ -262,7 +262,7 @@ def probe_solve(args):
     op = gl.Operator(2, LX, LY, MASS, torch.from_numpy(U).cuda())
     bd = torch.from_numpy(b).cuda()
     x = torch.zeros_like(bd)
-    prec = dict([HEADLINE] + VARIANTS)[args.probe_variant]
+    prec = dict([HEADLINE] + VARIANTS + [("fp64", 0)])[args.probe_variant]
     info = gl.minv_vector_cg(x, bd, bd.numel(), args.probe_iters, EPS, gl.square_staggered_normal_u1, op,
                              precision=prec)
     print(json.dumps({"probe": f"{args.probe_variant} variant, 1024x1024", "iters": info.iter,
@@ -838,7 +838,7 @@ def main():
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "multishift", "batch", "siblings", "rows", "eo"],
                     help="multishift / batch: time the batched workloads instead (one JSON line each)")
-    ap.add_argument("--probe-variant", default="fp32", choices=["fp32", "fp16", "bf16"],
+    ap.add_argument("--probe-variant", default="fp32", choices=["fp32", "fp16", "bf16", "fp64"],
                     help="the variant of the --probe-iters solve")
     ap.add_argument("--probe-iters", type=int, default=0,
                     help="run one headline-variant solve stopped after this many inner iterations "
