@@ -111,7 +111,10 @@ __device__ __forceinline__ void post_columns_s(unsigned long long *mb, unsigned 
     }
 }
 
-// The word slot of block b for a partial of epoch e (three epochs an iteration).
+// The word slot of block b for a partial of epoch e (three epochs an iteration).  A's partials
+// use PhaseFlags::w, B's the first word of each block's PhaseFlags::w4 entry (the
+// single-reduction FP32 kernel's four-partial words, which this kernel never shares a launch
+// with); each alternates between its two slots by iteration.
 __device__ __forceinline__ unsigned long long *word_A(res::PhaseFlags *pf, unsigned e, int b)
 {
     return pf->w[((e - 1) / 3) & 1] + b;
