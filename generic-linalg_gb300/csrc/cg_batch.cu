@@ -38,7 +38,10 @@ __global__ void k_busy_wait(long long ns);
 
 namespace {
 
-constexpr int kBatchUnroll = 4;
+// Inner iterations per graph pass.  A system that flags a reliable update idles until the pass
+// ends; a longer pass spreads the per-pass kernels (reliable update, tail, loop guard) over more
+// iterations.  The 256-system workload: 108 ms with 4, 98 with 8, 92 with 16, 90 with 32.
+constexpr int kBatchUnroll = 32;
 constexpr int kVecSites = 1024;  // sites per block of the vector kernels (256 threads x 4)
 
 struct BSys {
