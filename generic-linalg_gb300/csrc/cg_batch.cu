@@ -8,19 +8,22 @@
 // the same tile bodies), so each system converges to the same FP64-true tolerance.
 //
 // Layout: the work vectors of all systems are packed one after another (system s starts at
-// site sys[s].off).  Inner kernels run one block per tile of one system (tile blocks are
-// numbered system by system; tblk maps a block to its system); the vector and FP64 kernels run
-// blocks of up to 1024 sites of one system (vblk).  Every reduction is over the blocks of one
-// system (grid_sum_*_ids with the block's index inside its system), so a system's sums do not
-// depend on the other systems.
+// site sys[s].off).  Inner kernels work on tiles of one system (32 columns by BY * NY rows,
+// numbered system by system); the vector and FP64 kernels on blocks of up to 1024 sites of one
+// system.  Every reduction is over the blocks of one system (grid_sum_*_ids with the block's
+// index inside its system), so a system's sums do not depend on the other systems.
 //
-// Control: every kernel starts by reading its system's flags, and a block whose system has
-// nothing to do returns at once.  The graph body is kBatchUnroll inner iterations (A, B) for the
-// systems that are iterating, then the reliable-update steps (R1, FP64 operator, R2, R3, R4)
-// for the systems that flagged one, then a tail that re-arms those systems and ends the loop
-// when every system has stopped.  A system that flags an update during the unrolled iterations
-// waits for the end of the pass; its own arithmetic does not depend on the pass structure.
-// The tile shape of the inner kernels is picked for the batch by timing the candidates.
+// Control: the graph body is kBatchUnroll inner iterations (A, B) for the systems that are
+// iterating, then the reliable-update steps (R1, FP64 operator, R2, R3, R4) for the systems
+// that flagged one, then a tail that re-arms those systems and ends the loop when every system
+// has stopped.  A system that flags an update during the unrolled iterations waits for the end
+// of the pass; its own arithmetic does not depend on the pass structure.  The kernels do not
+// launch a block per tile of every system: a list kernel (k_bList) writes the (system, block)
+// pairs of the systems that still run (after each tail, for the inner kernels; before the
+// reliable-update steps, for the systems that flagged one), and a grid of resident blocks
+// walks that list.  Every kernel still reads its system's flags first and skips a system with
+// nothing to do (one that flagged an update or stopped during the pass).  The tile shape of
+// the inner kernels is picked for the batch by timing the candidates.
 
 #include <algorithm>
 #include <map>
@@ -61,7 +64,7 @@ template <class S, class R, class LK>
 struct BArgs {
     const BSys *sys;
     MxDev *st;
-    const int *tblk, *vblk;
+    const int *vblk;  // system of each vector block (the one-off kernels: norms, links)
     R *r;
     S *p0, *p1, *t;
     float2 *xlo;
@@ -70,6 +73,8 @@ struct BArgs {
     double *tpart, *vpart;
     int *all_done;
     int nsys;
+    const int2 *tlist, *vlist;  // (system, tile block) / (system, vector block) pairs to run
+    const int *ntl, *nvl;       // their lengths
 };
 
 // ---------------------------------------------------------------- Laplace tile bodies
@@ -127,13 +132,11 @@ __device__ __forceinline__ float lap_tile_B(const S *Ap, const S *p, R *r, float
 
 // A: p' = r + beta p ; t = D p' and |t|^2 (staggered) or Ap = L p' and <p', Ap> (Laplace)
 template <class S, class R, class LK, int BY, int NY>
-__global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bA_tile(const BArgs<S, R, LK> &a, int sid, int lb)
 {
-    const int sid = a.tblk[blockIdx.x];
     const BSys sy = a.sys[sid];
     MxDev *s = a.st + sid;
     if (s->done || s->reliable) return;
-    const int lb = blockIdx.x - sy.tb0;
     const int x = (lb % sy.tiles_x) * 32 + threadIdx.x;
     const int ybase = (lb / sy.tiles_x) * (BY * NY) + threadIdx.y * NY;
     const int par = s->parity;
@@ -160,13 +163,11 @@ __global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a)
 
 // B: Ap = D^dagger t (staggered; Laplace reads Ap from t) ; x_lo += alpha p' ; r -= alpha Ap
 template <class S, class R, class LK, int BY, int NY>
-__global__ void __launch_bounds__(32 * BY) k_bB(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bB_tile(const BArgs<S, R, LK> &a, int sid, int lb)
 {
-    const int sid = a.tblk[blockIdx.x];
     const BSys sy = a.sys[sid];
     MxDev *s = a.st + sid;
     if (s->done || s->reliable) return;
-    const int lb = blockIdx.x - sy.tb0;
     const int x = (lb % sy.tiles_x) * 32 + threadIdx.x;
     const int ybase = (lb / sy.tiles_x) * (BY * NY) + threadIdx.y * NY;
     const int par = s->parity;  // A wrote the new direction into the other buffer
@@ -189,22 +190,121 @@ __global__ void __launch_bounds__(32 * BY) k_bB(BArgs<S, R, LK> a)
         mx_after_B(s, out[0], 1 - par, 0, 0);
 }
 
+// The inner kernels: a grid of resident blocks takes the tiles of the list in order.  Block b
+// starts with entry b; while a tile runs, its first thread claims the next entry from the
+// launch's counter (zeroed by k_bList), so the tiles in flight stay a narrow window of the
+// list, as a launch with one block per tile would keep them: neighbouring tiles share their
+// halo rows and the shifted systems of one source their link table in L2.  A tile whose system
+// skips returns before any barrier, so the whole block takes the same path through the
+// reduction.
+template <class S, class R, class LK, int BY, int NY>
+__global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a, int *claim)
+{
+    __shared__ int next;
+    const int nt = *a.ntl;
+    const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+    for (int v = blockIdx.x; v < nt;) {
+        int c = 0;
+        if (lead) c = atomicAdd(claim, 1);
+        const int2 e = a.tlist[v];
+        bA_tile<S, R, LK, BY, NY>(a, e.x, e.y);
+        if (lead) next = c + (int)gridDim.x;
+        __syncthreads();
+        v = next;
+        __syncthreads();
+    }
+}
+
+template <class S, class R, class LK, int BY, int NY>
+__global__ void __launch_bounds__(32 * BY) k_bB(BArgs<S, R, LK> a, int *claim)
+{
+    __shared__ int next;
+    const int nt = *a.ntl;
+    const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+    for (int v = blockIdx.x; v < nt;) {
+        int c = 0;
+        if (lead) c = atomicAdd(claim, 1);
+        const int2 e = a.tlist[v];
+        bB_tile<S, R, LK, BY, NY>(a, e.x, e.y);
+        if (lead) next = c + (int)gridDim.x;
+        __syncthreads();
+        v = next;
+        __syncthreads();
+    }
+}
+
+// Lists the blocks that the next kernels run: mode 0, the tile blocks of every system that has
+// not stopped (for the inner kernels); mode 1, the vector blocks of every system that runs a
+// reliable update in this pass.  Entries are (system, block index inside the system), system by
+// system.  Every block forms the same prefix sum of the systems' block counts (1024 systems at
+// a time) and writes the entries of the systems q with q % gridDim.x == blockIdx.x.  Mode 0
+// also zeroes the nclaim claim counters of the inner kernels.
+__global__ void __launch_bounds__(1024) k_bList(const BSys *sys, const MxDev *st, int nsys, int mode, int2 *list,
+                                                int *total, int *claims, int nclaim)
+{
+    if (mode == 0 && blockIdx.x == 0)
+        for (int j = threadIdx.x; j < nclaim; j += blockDim.x) claims[j] = 0;
+    __shared__ int wsum[32];
+    __shared__ int cstart[1024], ccnt[1024];
+    __shared__ int carry;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int c0 = 0; c0 < nsys; c0 += 1024) {
+        const int q = c0 + threadIdx.x;
+        int cnt = 0;
+        if (q < nsys) {
+            const bool on = mode == 0 ? !st[q].done : (st[q].reliable && !st[q].done);
+            cnt = on ? (mode == 0 ? sys[q].ntb : sys[q].nvb) : 0;
+        }
+        int inc = cnt;  // inclusive scan within the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (lane == 31) wsum[warp] = inc;
+        __syncthreads();
+        if (warp == 0) {
+            int w = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += t;
+            }
+            wsum[lane] = w;
+        }
+        __syncthreads();
+        const int start = carry + (warp ? wsum[warp - 1] : 0) + inc - cnt;
+        cstart[threadIdx.x] = start;
+        ccnt[threadIdx.x] = cnt;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = start + cnt;
+        const int m = min(1024, nsys - c0);
+        const int G = gridDim.x;
+        for (int j = ((int)blockIdx.x - c0 % G + G) % G; j < m; j += G) {
+            const int n = ccnt[j], b = cstart[j];
+            for (int e = threadIdx.x; e < n; e += 1024) list[b + e] = make_int2(c0 + j, e);
+        }
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *total = carry;
+}
+
 // ---------------------------------------------------------------- reliable-update kernels
 // One block covers up to kVecSites sites of one system; `upd` is true for systems that run a
 // reliable update in this pass.
 
 #define BATCH_VEC_PROLOGUE                                                                  \
-    const int sid = a.vblk[blockIdx.x];                                                     \
     const BSys sy = a.sys[sid];                                                             \
     MxDev *s = a.st + sid;                                                                  \
     if (s->done || !s->reliable) return;                                                    \
-    const unsigned lb = blockIdx.x - sy.vb0;                                                \
     const long n = (long)sy.lx * sy.ly, o = sy.off;                                         \
     const long i0 = (long)lb * kRedThreads + threadIdx.x, di = (long)sy.nvb * kRedThreads;
 
 // R1: x_hi += scale x_lo ; x_lo = 0
 template <class S, class R, class LK>
-__global__ void __launch_bounds__(kRedThreads) k_bR1(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bR1_blk(const BArgs<S, R, LK> &a, int sid, unsigned lb)
 {
     BATCH_VEC_PROLOGUE
     const double sc = s->scale;
@@ -218,7 +318,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bR1(BArgs<S, R, LK> a)
 
 // FP64 operator on x: staggered pass 1 (tmp = D x) or the Laplacian (Ax = L x)
 template <class S, class R, class LK>
-__global__ void __launch_bounds__(kRedThreads) k_bOp1(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bOp1_blk(const BArgs<S, R, LK> &a, int sid, unsigned lb)
 {
     BATCH_VEC_PROLOGUE
     const double2 *x = sy.x;
@@ -231,7 +331,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bOp1(BArgs<S, R, LK> a)
 
 // staggered pass 2: Ax = D^dagger tmp
 template <class S, class R, class LK>
-__global__ void __launch_bounds__(kRedThreads) k_bOp2(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bOp2_blk(const BArgs<S, R, LK> &a, int sid, unsigned lb)
 {
     BATCH_VEC_PROLOGUE
     if (!sy.stag) return;
@@ -242,7 +342,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bOp2(BArgs<S, R, LK> a)
 
 // R2: r_hi = b - A x ; |r_hi|^2 -> convergence and the new scale (as k_mx_R2, sigma = 0)
 template <class S, class R, class LK>
-__global__ void __launch_bounds__(kRedThreads) k_bR2(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bR2_blk(const BArgs<S, R, LK> &a, int sid, unsigned lb)
 {
     BATCH_VEC_PROLOGUE
     double v[1] = {0.0};
@@ -286,7 +386,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bR2(BArgs<S, R, LK> a)
 
 // R3: r_lo = r_hi / scale ; p *= pscale ; <r_lo, p>, |r_lo|^2 (as k_mx_R3)
 template <class S, class R, class LK>
-__global__ void __launch_bounds__(kRedThreads) k_bR3(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bR3_blk(const BArgs<S, R, LK> &a, int sid, unsigned lb)
 {
     BATCH_VEC_PROLOGUE
     S *plo = (s->parity ? a.p1 : a.p0) + o;
@@ -314,7 +414,7 @@ __global__ void __launch_bounds__(kRedThreads) k_bR3(BArgs<S, R, LK> a)
 
 // R4: p0 = p - rp r_lo (the direction is in p0 afterwards)
 template <class S, class R, class LK>
-__global__ void __launch_bounds__(kRedThreads) k_bR4(BArgs<S, R, LK> a)
+__device__ __forceinline__ void bR4_blk(const BArgs<S, R, LK> &a, int sid, unsigned lb)
 {
     BATCH_VEC_PROLOGUE
     const S *plo = (s->parity ? a.p1 : a.p0) + o;
@@ -323,6 +423,26 @@ __global__ void __launch_bounds__(kRedThreads) k_bR4(BArgs<S, R, LK> a)
     const float rp = (float)s->rp;
     for (long i = i0; i < n; i += di) Fmt<S>::st(p0, i, fsub(Fmt<S>::ld(plo, i), fscale(rp, Fmt<R>::ld(rlo, i))));
 }
+
+// The reliable-update kernels: a grid of resident blocks walks the vector-block list.
+#define BATCH_VEC_KERNEL(name, body)                                                        \
+    template <class S, class R, class LK>                                                   \
+    __global__ void __launch_bounds__(kRedThreads) name(BArgs<S, R, LK> a)                  \
+    {                                                                                       \
+        const int nv = *a.nvl;                                                              \
+        for (int v = blockIdx.x; v < nv; v += gridDim.x) {                                  \
+            const int2 e = a.vlist[v];                                                      \
+            body<S, R, LK>(a, e.x, (unsigned)e.y);                                          \
+            __syncthreads();                                                                \
+        }                                                                                   \
+    }
+BATCH_VEC_KERNEL(k_bR1, bR1_blk)
+BATCH_VEC_KERNEL(k_bOp1, bOp1_blk)
+BATCH_VEC_KERNEL(k_bOp2, bOp2_blk)
+BATCH_VEC_KERNEL(k_bR2, bR2_blk)
+BATCH_VEC_KERNEL(k_bR3, bR3_blk)
+BATCH_VEC_KERNEL(k_bR4, bR4_blk)
+#undef BATCH_VEC_KERNEL
 
 // |b|^2 of every system
 template <class S, class R, class LK>
@@ -413,8 +533,8 @@ constexpr int kBatchTileRows[kNumBatchTiles] = {16, 32, 32, 32};  // BY * NY
 
 template <class S, class R, class LK>
 struct BKern {
-    void (*A)(BArgs<S, R, LK>);
-    void (*B)(BArgs<S, R, LK>);
+    void (*A)(BArgs<S, R, LK>, int *);
+    void (*B)(BArgs<S, R, LK>, int *);
     dim3 block;
 };
 
@@ -455,7 +575,7 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     const int dev = ops[0]->device;
     Scratch sc(st);
     std::vector<BSys> sys(nsys);
-    std::vector<int> vblk, tblk;
+    std::vector<int> vblk, tblk;  // tblk: host-side count of the tile blocks
     long N = 0, NL = 0;
     std::vector<int> sig;
     for (int q = 0; q < nsys; q++) {
@@ -510,25 +630,46 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     GL_TRY(sc.zeros(&a.st, nsys));
     GL_TRY(sc.zeros(&a.all_done, 1));
     BSys *dsys;
-    int *dvblk, *dtblk;
+    int *dvblk, *dcounts, *dclaims;  // dclaims: one tile counter per inner-kernel launch of a pass
+    int2 *dtlist, *dvlist;
     GL_TRY(sc.alloc(&dsys, nsys));
     GL_TRY(sc.alloc(&dvblk, nvb));
     // the largest tile-block count over the candidates
     int max_tb = 0;
     for (int c = 0; c < kNumBatchTiles; c++) max_tb = std::max(max_tb, layout_tiles(sys, tblk, c));
-    GL_TRY(sc.alloc(&dtblk, max_tb));
+    GL_TRY(sc.alloc(&dtlist, max_tb));
+    GL_TRY(sc.alloc(&dvlist, nvb));
+    GL_TRY(sc.zeros(&dcounts, 2));
+    GL_TRY(sc.zeros(&dclaims, 2 * kBatchUnroll));
     GL_TRY(sc.alloc(&a.tpart, max_tb));
     a.sys = dsys;
     a.vblk = dvblk;
-    a.tblk = dtblk;
     a.nsys = nsys;
+    a.tlist = dtlist;
+    a.vlist = dvlist;
+    a.ntl = dcounts;
+    a.nvl = dcounts + 1;
     GL_CUDA(cudaMemcpyAsync(dvblk, vblk.data(), sizeof(int) * nvb, cudaMemcpyHostToDevice, st));
     auto upload = [&](int c) -> glinalg_status {
-        const int ntb = layout_tiles(sys, tblk, c);
+        layout_tiles(sys, tblk, c);
         GL_CUDA(cudaMemcpyAsync(dsys, sys.data(), sizeof(BSys) * nsys, cudaMemcpyHostToDevice, st));
-        GL_CUDA(cudaMemcpyAsync(dtblk, tblk.data(), sizeof(int) * ntb, cudaMemcpyHostToDevice, st));
         return GLINALG_SUCCESS;
     };
+    // the list kernels and the resident grids that walk the lists
+    const int list_grid = std::max(1, std::min(nsys, 2 * sm_count()));
+    auto list_tiles = [&](cudaStream_t cs) {
+        k_bList<<<list_grid, 1024, 0, cs>>>(dsys, a.st, nsys, 0, dtlist, dcounts, dclaims, 2 * kBatchUnroll);
+    };
+    auto list_vec = [&](cudaStream_t cs) {
+        k_bList<<<list_grid, 1024, 0, cs>>>(dsys, a.st, nsys, 1, dvlist, dcounts + 1, nullptr, 0);
+    };
+    auto resident = [&](const void *fn, int threads, int cap) -> int {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        return std::max(1, std::min(cap, per_sm * sm_count()));
+    };
+    const int vgrid = resident((const void *)k_bOp1<S, R, LK>, kRedThreads, nvb);
     GL_TRY(upload(0));
     k_bLinks<S, R, LK><<<nvb, kRedThreads, 0, st>>>(a);
     GL_CUDA(cudaGetLastError());
@@ -563,17 +704,20 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
             GL_TRY(upload(c));
             const BKern<S, R, LK> k = batch_kernels<S, R, LK>(c);
             const int ntb = sys.back().tb0 + sys.back().ntb;
+            const int nth = (int)(k.block.x * k.block.y);
+            const int gA = resident((const void *)k.A, nth, ntb), gB = resident((const void *)k.B, nth, ntb);
             float m = 1e30f;
             for (int rep = 0; rep < 3; rep++) {
                 // r = 1 everywhere, p = 0, fresh state
                 k_bFillR<S, R, LK><<<nvb, kRedThreads, 0, st>>>(a);
                 GL_CUDA(cudaMemsetAsync(a.p0, 0, sizeof(S) * N, st));
                 GL_CUDA(cudaMemcpyAsync(a.st, hs.data(), sizeof(MxDev) * nsys, cudaMemcpyHostToDevice, st));
+                list_tiles(st);
                 k_busy_wait<<<1, 1, 0, st>>>(30000);  // keep launch latency out of the events
                 GL_CUDA(cudaEventRecord(e0, st));
                 for (int it = 0; it < 2; it++) {
-                    k.A<<<ntb, k.block, 0, st>>>(a);
-                    k.B<<<ntb, k.block, 0, st>>>(a);
+                    k.A<<<gA, k.block, 0, st>>>(a, dclaims + 2 * it);
+                    k.B<<<gB, k.block, 0, st>>>(a, dclaims + 2 * it + 1);
                 }
                 GL_CUDA(cudaEventRecord(e1, st));
                 GL_CUDA(cudaEventSynchronize(e1));
@@ -597,6 +741,8 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     GL_TRY(upload(cand));
     const BKern<S, R, LK> k = batch_kernels<S, R, LK>(cand);
     const int ntb = sys.back().tb0 + sys.back().ntb;
+    const int nth = (int)(k.block.x * k.block.y);
+    const int gA = resident((const void *)k.A, nth, ntb), gB = resident((const void *)k.B, nth, ntb);
 
     // ---- initial state: every system starts with a reliable update (r = b - A x0)
     {
@@ -614,12 +760,13 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     EventTimer tm;
     tm.start(st);
     auto reliable_seq = [&](cudaStream_t cs) -> glinalg_status {
-        k_bR1<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
-        k_bOp1<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
-        k_bOp2<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
-        k_bR2<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
-        k_bR3<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
-        k_bR4<S, R, LK><<<nvb, kRedThreads, 0, cs>>>(a);
+        list_vec(cs);
+        k_bR1<S, R, LK><<<vgrid, kRedThreads, 0, cs>>>(a);
+        k_bOp1<S, R, LK><<<vgrid, kRedThreads, 0, cs>>>(a);
+        k_bOp2<S, R, LK><<<vgrid, kRedThreads, 0, cs>>>(a);
+        k_bR2<S, R, LK><<<vgrid, kRedThreads, 0, cs>>>(a);
+        k_bR3<S, R, LK><<<vgrid, kRedThreads, 0, cs>>>(a);
+        k_bR4<S, R, LK><<<vgrid, kRedThreads, 0, cs>>>(a);
         GL_CUDA(cudaGetLastError());
         return GLINALG_SUCCESS;
     };
@@ -628,9 +775,10 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     k_bTail<<<1, 256, 0, st>>>(a.st, nsys, a.all_done, 1);
     GL_CUDA(cudaGetLastError());
     GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
+        list_tiles(cs);
         for (int u = 0; u < kBatchUnroll; u++) {
-            k.A<<<ntb, k.block, 0, cs>>>(a);
-            k.B<<<ntb, k.block, 0, cs>>>(a);
+            k.A<<<gA, k.block, 0, cs>>>(a, dclaims + 2 * u);
+            k.B<<<gB, k.block, 0, cs>>>(a, dclaims + 2 * u + 1);
         }
         GL_TRY(reliable_seq(cs));
         k_bTail<<<1, 256, 0, cs>>>(a.st, nsys, a.all_done, 0);
