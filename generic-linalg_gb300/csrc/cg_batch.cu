@@ -196,9 +196,10 @@ __device__ __forceinline__ void bB_tile(const BArgs<S, R, LK> &a, int sid, int l
 // list, as a launch with one block per tile would keep them: neighbouring tiles share their
 // halo rows and the shifted systems of one source their link table in L2.  A tile whose system
 // skips returns before any barrier, so the whole block takes the same path through the
-// reduction.
-template <class S, class R, class LK, int BY, int NY>
-__global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a, int *claim)
+// reduction.  MINB: blocks per SM that the register budget must allow (the warps an SM keeps in
+// flight: 32 warps need 64 registers a thread).
+template <class S, class R, class LK, int BY, int NY, int MINB>
+__global__ void __launch_bounds__(32 * BY, MINB) k_bA(BArgs<S, R, LK> a, int *claim)
 {
     __shared__ int next;
     const int nt = *a.ntl;
@@ -215,8 +216,8 @@ __global__ void __launch_bounds__(32 * BY) k_bA(BArgs<S, R, LK> a, int *claim)
     }
 }
 
-template <class S, class R, class LK, int BY, int NY>
-__global__ void __launch_bounds__(32 * BY) k_bB(BArgs<S, R, LK> a, int *claim)
+template <class S, class R, class LK, int BY, int NY, int MINB>
+__global__ void __launch_bounds__(32 * BY, MINB) k_bB(BArgs<S, R, LK> a, int *claim)
 {
     __shared__ int next;
     const int nt = *a.ntl;
@@ -528,6 +529,11 @@ __global__ void k_bTail(MxDev *st, int nsys, int *all_done, int setup)
 
 // ---------------------------------------------------------------- tile candidates
 
+// Candidates (BY warps of NY rows, blocks per SM): shapes of up to four rows a thread fit 64
+// registers without spilling (32 warps an SM); the eight-row shape keeps its own register
+// count.  Uneven batch: 84.7 ms with every shape at its own register count (three blocks of
+// eight warps for the 8 x 4 shape the autotuner picks), 76.0 with the 64-register bound; a
+// 40-register bound on the two-row shapes (48 warps) spills and gives 81.3.
 constexpr int kNumBatchTiles = 4;
 constexpr int kBatchTileRows[kNumBatchTiles] = {16, 32, 32, 32};  // BY * NY
 
@@ -542,10 +548,10 @@ template <class S, class R, class LK>
 BKern<S, R, LK> batch_kernels(int c)
 {
     switch (c) {
-    case 0: return {k_bA<S, R, LK, 8, 2>, k_bB<S, R, LK, 8, 2>, dim3(32, 8)};
-    case 1: return {k_bA<S, R, LK, 8, 4>, k_bB<S, R, LK, 8, 4>, dim3(32, 8)};
-    case 2: return {k_bA<S, R, LK, 4, 8>, k_bB<S, R, LK, 4, 8>, dim3(32, 4)};
-    default: return {k_bA<S, R, LK, 16, 2>, k_bB<S, R, LK, 16, 2>, dim3(32, 16)};
+    case 0: return {k_bA<S, R, LK, 8, 2, 4>, k_bB<S, R, LK, 8, 2, 4>, dim3(32, 8)};
+    case 1: return {k_bA<S, R, LK, 8, 4, 4>, k_bB<S, R, LK, 8, 4, 4>, dim3(32, 8)};
+    case 2: return {k_bA<S, R, LK, 4, 8, 1>, k_bB<S, R, LK, 4, 8, 1>, dim3(32, 4)};
+    default: return {k_bA<S, R, LK, 16, 2, 2>, k_bB<S, R, LK, 16, 2, 2>, dim3(32, 16)};
     }
 }
 
