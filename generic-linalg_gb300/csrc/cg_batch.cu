@@ -45,6 +45,11 @@ namespace {
 // ends; a longer pass spreads the per-pass kernels (reliable update, tail, loop guard) over more
 // iterations.  The 256-system workload: 108 ms with 4, 98 with 8, 92 with 16, 90 with 32.
 constexpr int kBatchUnroll = 32;
+// Inner iterations between rebuilds of the tile list: a system that flags a reliable update
+// leaves the list at the next rebuild instead of the pass's end.  64-source multishift:
+// 646 ms rebuilding once a pass, 619 every 4 iterations, 617 every iteration (where the
+// uneven batch loses 4 ms to the extra list launches).
+constexpr int kListEvery = 4;
 constexpr int kVecSites = 1024;  // sites per block of the vector kernels (256 threads x 4)
 
 struct BSys {
@@ -234,9 +239,9 @@ __global__ void __launch_bounds__(32 * BY, MINB) k_bB(BArgs<S, R, LK> a, int *cl
     }
 }
 
-// Lists the blocks that the next kernels run: mode 0, the tile blocks of every system that has
-// not stopped (for the inner kernels); mode 1, the vector blocks of every system that runs a
-// reliable update in this pass.  Entries are (system, block index inside the system), system by
+// Lists the blocks that the next kernels run: mode 0, the tile blocks of every system that is
+// iterating (not stopped, no reliable update pending; for the inner kernels); mode 1, the
+// vector blocks of every system that runs a reliable update in this pass.  Entries are (system, block index inside the system), system by
 // system.  Every block forms the same prefix sum of the systems' block counts (1024 systems at
 // a time) and writes the entries of the systems q with q % gridDim.x == blockIdx.x.  Mode 0
 // also zeroes the nclaim claim counters of the inner kernels.
@@ -255,7 +260,7 @@ __global__ void __launch_bounds__(1024) k_bList(const BSys *sys, const MxDev *st
         const int q = c0 + threadIdx.x;
         int cnt = 0;
         if (q < nsys) {
-            const bool on = mode == 0 ? !st[q].done : (st[q].reliable && !st[q].done);
+            const bool on = mode == 0 ? !(st[q].done || st[q].reliable) : (st[q].reliable && !st[q].done);
             cnt = on ? (mode == 0 ? sys[q].ntb : sys[q].nvb) : 0;
         }
         int inc = cnt;  // inclusive scan within the warp
@@ -781,8 +786,8 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     k_bTail<<<1, 256, 0, st>>>(a.st, nsys, a.all_done, 1);
     GL_CUDA(cudaGetLastError());
     GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
-        list_tiles(cs);
         for (int u = 0; u < kBatchUnroll; u++) {
+            if (u % kListEvery == 0) list_tiles(cs);
             k.A<<<gA, k.block, 0, cs>>>(a, dclaims + 2 * u);
             k.B<<<gB, k.block, 0, cs>>>(a, dclaims + 2 * u + 1);
         }
