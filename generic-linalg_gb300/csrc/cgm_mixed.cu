@@ -266,6 +266,21 @@ __global__ void __launch_bounds__(kRedThreads) k_mx_C(MxArgs a)
 
 constexpr int kTNY = 4;                    // rows per warp tile
 constexpr int kTWarps = kRedThreads / 32;  // warps per block
+// Tiles per warp: a block covers kTWarps * kTileRuns tiles of its source, so its reduction
+// and its launch serve four times the sites.  512^2, 64 sources: the multishift phase takes
+// 158.5 ms with one tile a warp, 140.3 with two, 133.4 with four, 137.3 with eight (8-row
+// tiles, two a warp: 142.6).
+constexpr int kTileRuns = 4;
+// Blocks of k_mx_F per source: nb / kFlushRuns.  The kernel runs every iteration but flushes
+// every kBlk-th; a smaller grid makes the other launches cheap (multishift phase: 133.8 ms
+// with nb blocks, 124.2 with nb / 4, 122.5 with nb / 8).
+constexpr int kFlushRuns = 8;
+// Reliable-update threshold of the refinement: an FP64 true residual whenever the iterated one
+// has fallen by this factor.  The refinement starts 1e-5..1e-6 from its tolerance, so three
+// orders of magnitude between FP64 updates leave one or two updates per system, each a FP64
+// operator pass bound by GB300's FP64 rate.  512^2, 64 sources: 656 ms with 0.1, 584 with the
+// single-system default 0.01, 557 with 0.001.
+constexpr double kRefineDelta = 1e-3;
 
 __device__ __forceinline__ float2 shfl_dn2(float2 v)
 {
@@ -601,10 +616,11 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     float2 *H;
     GL_TRY(sc.alloc(&H, 2 * (size_t)n));
     a.H = H;
-    // the register-tiled kernels (lx a multiple of 32): one block of warps per kTWarps tiles
+    // the register-tiled kernels (lx a multiple of 32): one block of warps per kTWarps *
+    // kTileRuns tiles
     const bool tiled = op->lx % 32 == 0;
     const int ntiles = (op->lx / 32) * ((op->ly + kTNY - 1) / kTNY);
-    const int tg = tiled ? (ntiles + kTWarps - 1) / kTWarps : 0;
+    const int tg = tiled ? (ntiles + kTWarps * kTileRuns - 1) / (kTWarps * kTileRuns) : 0;
     GL_TRY(sc.alloc(&a.partials, (size_t)n_rhs * 2 * std::max(nb, tg)));
     GL_TRY(sc.zeros(&a.all_done, 1));
     {
@@ -649,6 +665,7 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     EventTimer tm;
     tm.start(st);
     const dim3 rg(nb, n_rhs), vg(mvec_grid(n), n_rhs);
+    const dim3 fg(std::max(1, nb / kFlushRuns), n_rhs);
     k_mx_hop<<<mvec_grid(n), 256, 0, st>>>(H, op->U, op->lx, n);
     k_mx_init<<<vg, 256, 0, st>>>(a);
     k_mx_norms<<<rg, kRedThreads, 0, st>>>(a);
@@ -661,7 +678,7 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         GL_CUDA(cudaGetLastError());
         GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
             k_mx_Bt<<<tgr, kRedThreads, 0, cs>>>(a);
-            k_mx_F<<<rg, kRedThreads, 0, cs>>>(a);
+            k_mx_F<<<fg, kRedThreads, 0, cs>>>(a);
             k_mx_At<<<tgr, kRedThreads, 0, cs>>>(a, 0);
             k_mx_tail<<<1, 32, 0, cs>>>(a);
             GL_CUDA(cudaGetLastError());
@@ -675,7 +692,7 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
         GL_CUDA(cudaGetLastError());
         GL_TRY(run_loop(st, a.all_done, [&](cudaStream_t cs) -> glinalg_status {
             k_mx_C<<<rg, kRedThreads, 0, cs>>>(a);
-            k_mx_F<<<rg, kRedThreads, 0, cs>>>(a);
+            k_mx_F<<<fg, kRedThreads, 0, cs>>>(a);
             k_mx_A<<<rg, kRedThreads, 0, cs>>>(a, 0);
             k_mx_B<<<rg, kRedThreads, 0, cs>>>(a);
             k_mx_tail<<<1, 32, 0, cs>>>(a);
@@ -714,7 +731,7 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
             inf2[y] = glinalg_info{};
         }
     glinalg_status s2 = cg_batch_mixed(ops.data(), nsys, xs.data(), bs.data(), max_iter, eps, GLINALG_PREC_SINGLE,
-                                       0.0, inf2.data(), st);
+                                       kRefineDelta, inf2.data(), st);
     for (auto &v : views) v.U = nullptr;
     GL_TRY(s2);
     tm.stop(st);
