@@ -266,14 +266,17 @@ __global__ void __launch_bounds__(kRedThreads) k_mx_C(MxArgs a)
 
 constexpr int kTNY = 4;                    // rows per warp tile
 constexpr int kTWarps = kRedThreads / 32;  // warps per block
-// Tiles per warp: a block covers kTWarps * kTileRuns tiles of its source, so its reduction
-// and its launch serve four times the sites.  512^2, 64 sources: the multishift phase takes
-// 158.5 ms with one tile a warp, 140.3 with two, 133.4 with four, 137.3 with eight (8-row
-// tiles, two a warp: 142.6).
+// Tiles per warp, at most: a block covers kTWarps * runs tiles of its source, so its reduction
+// and its launch serve that many more sites, as long as all sources together still give every
+// SM kMinBlocksPerSM blocks.  512^2, 64 sources: the multishift phase takes 158.5 ms with one
+// tile a warp, 140.3 with two, 133.4 with four, 137.3 with eight (8-row tiles, two a warp:
+// 142.6).
 constexpr int kTileRuns = 4;
-// Blocks of k_mx_F per source: nb / kFlushRuns.  The kernel runs every iteration but flushes
-// every kBlk-th; a smaller grid makes the other launches cheap (multishift phase: 133.8 ms
-// with nb blocks, 124.2 with nb / 4, 122.5 with nb / 8).
+constexpr int kMinBlocksPerSM = 4;
+// Blocks of k_mx_F per source: nb / runs, runs at most kFlushRuns (and again at least
+// kMinBlocksPerSM blocks an SM over all sources).  The kernel runs every iteration but
+// flushes every kBlk-th; a smaller grid makes the other launches cheap (multishift phase,
+// 64 sources: 133.8 ms with nb blocks, 124.2 with nb / 4, 122.5 with nb / 8).
 constexpr int kFlushRuns = 8;
 // Reliable-update threshold of the refinement: an FP64 true residual whenever the iterated one
 // has fallen by this factor.  The refinement starts 1e-5..1e-6 from its tolerance, so three
@@ -616,11 +619,13 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     float2 *H;
     GL_TRY(sc.alloc(&H, 2 * (size_t)n));
     a.H = H;
-    // the register-tiled kernels (lx a multiple of 32): one block of warps per kTWarps *
-    // kTileRuns tiles
+    // the register-tiled kernels (lx a multiple of 32): one block of warps per kTWarps * runs
+    // tiles
     const bool tiled = op->lx % 32 == 0;
     const int ntiles = (op->lx / 32) * ((op->ly + kTNY - 1) / kTNY);
-    const int tg = tiled ? (ntiles + kTWarps * kTileRuns - 1) / (kTWarps * kTileRuns) : 0;
+    const long min_blocks = (long)kMinBlocksPerSM * sm_count();
+    const int runs = (int)std::max(1L, std::min((long)kTileRuns, (long)ntiles * n_rhs / (kTWarps * min_blocks)));
+    const int tg = tiled ? (ntiles + kTWarps * runs - 1) / (kTWarps * runs) : 0;
     GL_TRY(sc.alloc(&a.partials, (size_t)n_rhs * 2 * std::max(nb, tg)));
     GL_TRY(sc.zeros(&a.all_done, 1));
     {
@@ -665,7 +670,8 @@ glinalg_status cg_m_batch_mixed(const glinalg_operator_s *op, double2 *X, const 
     EventTimer tm;
     tm.start(st);
     const dim3 rg(nb, n_rhs), vg(mvec_grid(n), n_rhs);
-    const dim3 fg(std::max(1, nb / kFlushRuns), n_rhs);
+    const int fruns = (int)std::max(1L, std::min((long)kFlushRuns, (long)nb * n_rhs / min_blocks));
+    const dim3 fg(std::max(1, nb / fruns), n_rhs);
     k_mx_hop<<<mvec_grid(n), 256, 0, st>>>(H, op->U, op->lx, n);
     k_mx_init<<<vg, 256, 0, st>>>(a);
     k_mx_norms<<<rg, kRedThreads, 0, st>>>(a);
