@@ -52,6 +52,36 @@ def test_cg_batch_uneven(gl, gpu, oracle, precision):
         assert rel(xs[q], x1) < 1e-7
 
 
+@pytest.mark.parametrize("precision", [1, 2])
+def test_cg_batch_systems_that_stop_at_setup(gl, gpu, oracle, precision):
+    """Systems that stop at the first reliable update never enter the list of iterating tiles,
+    and the others iterate as if alone: a zero source stops with GLINALG_SOLVE_BREAKDOWN and
+    x = 0, a NaN in a source with GLINALG_SOLVE_NONFINITE; the rest (sides 16..48, both
+    kinds) reach the FP64-true relative residual 1e-10 and agree with their single-system
+    solves."""
+    systems = _uneven_batch(gl, 7, [16, 32, 48], 91)
+    zero, bad = 1, 4
+    systems[zero] = systems[zero][:4] + (np.zeros_like(systems[zero][4]),)
+    b_bad = systems[bad][4].copy()
+    b_bad[5] = complex(float("nan"), 0.0)
+    systems[bad] = systems[bad][:4] + (b_bad,)
+    ops = [gl.Operator(k, L, L, mass, U) for k, L, mass, U, b in systems]
+    xs = [np.zeros_like(b) for *_, b in systems]
+    infos = gl.cg_batch(ops, xs, [b for *_, b in systems], 100000, 1e-10, precision=precision)
+    assert infos[zero].status == gl.GLINALG_SOLVE_BREAKDOWN and not infos[zero].success, infos[zero]
+    assert np.all(xs[zero] == 0)
+    assert infos[bad].status == gl.GLINALG_SOLVE_NONFINITE and not infos[bad].success, infos[bad]
+    for q, (kind, L, mass, U, b) in enumerate(systems):
+        if q in (zero, bad):
+            continue
+        assert infos[q].success and infos[q].status == gl.GLINALG_SOLVE_CONVERGED, (q, infos[q])
+        assert _true_relres(oracle, kind, L, mass, U, xs[q], b) < 1e-10, q
+        x1 = np.zeros_like(b)
+        cb = gl.square_staggered_normal_u1 if kind == 2 else gl.square_laplace_u1
+        gl.minv_vector_cg(x1, b, b.size, 100000, 1e-10, cb, ops[q], precision=precision)
+        assert rel(xs[q], x1) < 1e-7, q
+
+
 def test_cg_batch_256_uneven_systems(gl, gpu, oracle):
     """The uneven-batch workload: 256 systems with sides from {32, 64, 128, 256}, half staggered
     normal equations and half gauge Laplacians, FP32 inner iterations with FP64 reliable
