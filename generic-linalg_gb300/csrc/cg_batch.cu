@@ -836,7 +836,8 @@ glinalg_status cg_batch_mixed(const glinalg_operator_s *const *ops, int nsys, do
     case GLINALG_PREC_SINGLE:
         return run_batch<float2, float2, float2>(ops, nsys, X, B, max_iter, eps, delta, 1, infos, st, "CG-FP32");
     case GLINALG_PREC_HALF:
-        return run_batch<__half2, float2, __half2>(ops, nsys, X, B, max_iter, eps, delta, 2, infos, st, "CG-FP16");
+        // FP16 fields, FP32 links, as the single-system FP16 solver
+        return run_batch<__half2, float2, float2>(ops, nsys, X, B, max_iter, eps, delta, 2, infos, st, "CG-FP16");
     case GLINALG_PREC_BFLOAT:
         return run_batch<__nv_bfloat162, float2, float2>(ops, nsys, X, B, max_iter, eps, delta, 3, infos, st,
                                                          "CG-BF16");

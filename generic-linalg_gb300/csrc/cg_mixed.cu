@@ -480,9 +480,10 @@ static res::Plan resident16_plan(int lx, int ly, size_t s_bytes, size_t lk_bytes
     return ress::plan(lx, ly, sm_count(), (size_t)std::max(0, optin - 512), s_bytes, lk_bytes);
 }
 
-// storage bytes of the variant's p' / t and links (FP16: 4 and 4; BF16: 4 and 8)
+// storage bytes of the variant's p' / t (FP32: 8; FP16, BF16: 4) and links (FP32 in every
+// variant: 8)
 static size_t variant_s_bytes(int variant) { return variant == 1 ? 8 : 4; }
-static size_t variant_lk_bytes(int variant) { return variant == 2 ? 4 : 8; }
+static size_t variant_lk_bytes(int) { return 8; }
 
 static bool persist_applies(int lx, int ly);
 
@@ -1458,7 +1459,11 @@ glinalg_status cg_mixed(const glinalg_operator_s *op, double2 *x, const double2 
                                                           1, wait_limit_us);
         break;
     case GLINALG_PREC_HALF:
-        s = run_mixed<__half2, float2, __half2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16", 2, wait_limit_us);
+        // FP16 fields, FP32 links (as BF16): with FP16 links the inner operator differs from
+        // the FP64 one by the links' rounding, every reliable-update cycle gains only as many
+        // orders as that allows, and the 1024^2 solve took 5456 iterations (63 ms) against
+        // 2103 (24.7 ms) with FP32 links.
+        s = run_mixed<__half2, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-FP16", 2, wait_limit_us);
         break;
     case GLINALG_PREC_BFLOAT:
         s = run_mixed<__nv_bfloat162, float2, float2>(op, x, b, max_iter, eps, delta, sigma, info, st, "CG-BF16", 3, wait_limit_us);
@@ -1659,7 +1664,7 @@ extern "C" glinalg_status glinalg_profile_mixed_kernels(glinalg_operator op, int
     GL_TRY(ensure_device());
     switch (precision) {
     case GLINALG_PREC_SINGLE: return profile_inner<float2, float2, float2>(op, 1, n_launch, ms, bytes);
-    case GLINALG_PREC_HALF: return profile_inner<__half2, float2, __half2>(op, 2, n_launch, ms, bytes);
+    case GLINALG_PREC_HALF: return profile_inner<__half2, float2, float2>(op, 2, n_launch, ms, bytes);
     case GLINALG_PREC_BFLOAT: return profile_inner<__nv_bfloat162, float2, float2>(op, 3, n_launch, ms, bytes);
     default: return GLINALG_ERROR_INVALID_VALUE;
     }
@@ -1675,7 +1680,7 @@ extern "C" glinalg_status glinalg_profile_persist_kernel(glinalg_operator op, in
     GL_TRY(ensure_device());
     switch (precision) {
     case GLINALG_PREC_SINGLE: return profile_persist<float2, float2, float2>(op, 1, n_launch, n_iter, ms, bytes, cand);
-    case GLINALG_PREC_HALF: return profile_persist<__half2, float2, __half2>(op, 2, n_launch, n_iter, ms, bytes, cand);
+    case GLINALG_PREC_HALF: return profile_persist<__half2, float2, float2>(op, 2, n_launch, n_iter, ms, bytes, cand);
     case GLINALG_PREC_BFLOAT:
         return profile_persist<__nv_bfloat162, float2, float2>(op, 3, n_launch, n_iter, ms, bytes, cand);
     default: return GLINALG_ERROR_INVALID_VALUE;

@@ -139,8 +139,8 @@ typedef struct glinalg_info {
 typedef enum glinalg_precision {
     GLINALG_PREC_DOUBLE = 0,  /* FP64 throughout, the reference's recurrence */
     GLINALG_PREC_SINGLE = 1,  /* FP32 inner iterations, FP64 reliable updates */
-    GLINALG_PREC_HALF = 2,    /* FP16 storage / FP32 arithmetic inner, FP64 reliable updates */
-    GLINALG_PREC_BFLOAT = 3   /* BF16 storage / FP32 arithmetic inner, FP64 reliable updates */
+    GLINALG_PREC_HALF = 2,    /* FP16 field storage, FP32 links and arithmetic inner, FP64 reliable updates */
+    GLINALG_PREC_BFLOAT = 3   /* BF16 field storage, FP32 links and arithmetic inner, FP64 reliable updates */
 } glinalg_precision;
 
 typedef struct glinalg_solver_params {

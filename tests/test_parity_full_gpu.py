@@ -13,11 +13,12 @@ Bars (each measured figure is printed by the test):
     it (2093 iterations): the difference is rounding, and 1e-11 leaves a margin of 15.
   - Mixed CG (FP32 / FP16 / BF16 inner iterations, FP64 reliable updates): FP64-true relative
     residual below 1e-10, recomputed here by the oracle's operator; solution within 1e-9
-    relative of the oracle's.  Measured on GB300: 1.4e-13 (FP32), 6.1e-11 (FP16), 1.4e-11
-    (BF16).  Nothing tighter holds by construction (their Krylov paths differ from the FP64
-    one; any two solutions with relative residual below 1e-10 differ by at most
-    2 kappa 1e-10 = 8e-6, kappa(M^dagger M) <= (4 + m^2) / m^2 = 40001), so the bar is the
-    measured worst case with a margin of 16.
+    relative of the oracle's.  Measured on GB300: 1.4e-13 (FP32), 5.7e-13 (FP16, FP32 links),
+    1.4e-11 (BF16); 6.1e-11 for FP16 when it kept FP16 links.  Nothing tighter holds by
+    construction (their Krylov paths differ from the FP64 one; any two solutions with relative
+    residual below 1e-10 differ by at most 2 kappa 1e-10 = 8e-6, kappa(M^dagger M) <=
+    (4 + m^2) / m^2 = 40001), so the bar is the worst case measured over both link formats
+    with a margin of 16.
   - Multishift, 512^2, m = 0.05, 12 shifts log-spaced over [1e-4, 1], 2 sources: per source the
     oracle's CG-M iteration count; every shift's solution within 1e-10 relative of the oracle's.
     CG-M retires a shift on its iterated residual |zeta_s| |r| < 1e-10 |b|
