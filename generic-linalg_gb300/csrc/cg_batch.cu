@@ -241,10 +241,11 @@ __global__ void __launch_bounds__(32 * BY, MINB) k_bB(BArgs<S, R, LK> a, int *cl
 
 // Lists the blocks that the next kernels run: mode 0, the tile blocks of every system that is
 // iterating (not stopped, no reliable update pending; for the inner kernels); mode 1, the
-// vector blocks of every system that runs a reliable update in this pass.  Entries are (system, block index inside the system), system by
-// system.  Every block forms the same prefix sum of the systems' block counts (1024 systems at
-// a time) and writes the entries of the systems q with q % gridDim.x == blockIdx.x.  Mode 0
-// also zeroes the nclaim claim counters of the inner kernels.
+// vector blocks of every system that runs a reliable update in this pass.  Entries are
+// (system, block index inside the system), system by system.  Every block forms the same
+// prefix sum of the systems' block counts (1024 systems at a time, blockDim.x = 1024) and
+// writes the entries of the systems q with q % gridDim.x == blockIdx.x.  Mode 0 also zeroes
+// the nclaim claim counters of the inner kernels.
 __global__ void __launch_bounds__(1024) k_bList(const BSys *sys, const MxDev *st, int nsys, int mode, int2 *list,
                                                 int *total, int *claims, int nclaim)
 {
