@@ -43,13 +43,14 @@ int main()
         for (int ly = 2; ly <= 4096; ly += (ly < 64 ? 2 : 62)) {
             for (int wy : {4, 8}) check("fp32", lx, ly, res::plan(lx, ly, nsm, budget, wy), nsm, budget, 32 * res::kWX * wy, lx);
             check("eo", lx, ly, reseo::plan(lx, ly, nsm, budget), nsm, budget, 32 * res::kWX * reseo::kWY, lx / 2);
-            check("fp16", lx, ly, ress::plan(lx, ly, nsm, budget, 4, 4), nsm, budget, 32 * res::kWX * ress::kWY, lx);
+            // both 16-bit variants: 4-byte fields, 8-byte (FP32) links
+            check("fp16", lx, ly, ress::plan(lx, ly, nsm, budget, 4, 8), nsm, budget, 32 * res::kWX * ress::kWY, lx);
             check("bf16", lx, ly, ress::plan(lx, ly, nsm, budget, 4, 8), nsm, budget, 32 * res::kWX * ress::kWY, lx);
         }
     }
     show("fp32", 1024, 1024, res::plan(1024, 1024, nsm, budget, 4));
     show("eo", 1024, 1024, reseo::plan(1024, 1024, nsm, budget));
-    show("fp16", 1024, 1024, ress::plan(1024, 1024, nsm, budget, 4, 4));
+    show("fp16", 1024, 1024, ress::plan(1024, 1024, nsm, budget, 4, 8));
     show("bf16", 1024, 1024, ress::plan(1024, 1024, nsm, budget, 4, 8));
     show("fp32", 512, 512, res::plan(512, 512, nsm, budget, 4));
     show("fp32", 2048, 2048, res::plan(2048, 2048, nsm, budget, 4));

@@ -46,6 +46,7 @@ def test_benchmark_plans(plans):
     for v in ("fp16", "bf16"):
         s = got[(v, 1024, 1024)]
         assert s["ok"] and (s["gx"], s["gy"], s["ty"], s["ny"]) == (8, 19, 54, 14)
-    assert got[("fp16", 1024, 1024)]["smem"] < got[("bf16", 1024, 1024)]["smem"] < fp32["smem"]
+    # FP16 and BF16 both store 16-bit fields and FP32 links
+    assert got[("fp16", 1024, 1024)]["smem"] == got[("bf16", 1024, 1024)]["smem"] < fp32["smem"]
     # a lattice too large for one rectangle per SM
     assert not got[("fp32", 2048, 2048)]["ok"]
