@@ -19,9 +19,9 @@
 // has stopped.  A system that flags an update during the unrolled iterations waits for the end
 // of the pass; its own arithmetic does not depend on the pass structure.  The kernels do not
 // launch a block per tile of every system: a list kernel (k_bList) writes the (system, block)
-// pairs of the systems that still run (after each tail, for the inner kernels; before the
-// reliable-update steps, for the systems that flagged one), and a grid of resident blocks
-// walks that list.  Every kernel still reads its system's flags first and skips a system with
+// pairs of the systems that still run (every kListEvery inner iterations, the tiles of the
+// systems that are iterating; before the reliable-update steps, the vector blocks of the
+// systems that flagged one), and a grid of resident blocks walks that list.  Every kernel still reads its system's flags first and skips a system with
 // nothing to do (one that flagged an update or stopped during the pass).  The tile shape of
 // the inner kernels is picked for the batch by timing the candidates.
 
@@ -565,18 +565,17 @@ std::mutex g_btune_mu;
 std::map<std::tuple<int, int, std::vector<int>>, int> g_btuned;
 
 // Tile-block layout of the batch for candidate c; returns the number of tile blocks.
-int layout_tiles(std::vector<BSys> &sys, std::vector<int> &tblk, int c)
+int layout_tiles(std::vector<BSys> &sys, int c)
 {
     const int rows = kBatchTileRows[c];
-    tblk.clear();
-    for (int q = 0; q < (int)sys.size(); q++) {
-        BSys &y = sys[q];
+    int ntb = 0;
+    for (BSys &y : sys) {
         y.tiles_x = (y.lx + 31) / 32;
-        y.tb0 = (int)tblk.size();
+        y.tb0 = ntb;
         y.ntb = y.tiles_x * ((y.ly + rows - 1) / rows);
-        tblk.insert(tblk.end(), y.ntb, q);
+        ntb += y.ntb;
     }
-    return (int)tblk.size();
+    return ntb;
 }
 
 template <class S, class R, class LK>
@@ -587,7 +586,7 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     const int dev = ops[0]->device;
     Scratch sc(st);
     std::vector<BSys> sys(nsys);
-    std::vector<int> vblk, tblk;  // tblk: host-side count of the tile blocks
+    std::vector<int> vblk;
     long N = 0, NL = 0;
     std::vector<int> sig;
     for (int q = 0; q < nsys; q++) {
@@ -648,7 +647,7 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     GL_TRY(sc.alloc(&dvblk, nvb));
     // the largest tile-block count over the candidates
     int max_tb = 0;
-    for (int c = 0; c < kNumBatchTiles; c++) max_tb = std::max(max_tb, layout_tiles(sys, tblk, c));
+    for (int c = 0; c < kNumBatchTiles; c++) max_tb = std::max(max_tb, layout_tiles(sys, c));
     GL_TRY(sc.alloc(&dtlist, max_tb));
     GL_TRY(sc.alloc(&dvlist, nvb));
     GL_TRY(sc.zeros(&dcounts, 2));
@@ -663,7 +662,7 @@ glinalg_status run_batch(const glinalg_operator_s *const *ops, int nsys, double2
     a.nvl = dcounts + 1;
     GL_CUDA(cudaMemcpyAsync(dvblk, vblk.data(), sizeof(int) * nvb, cudaMemcpyHostToDevice, st));
     auto upload = [&](int c) -> glinalg_status {
-        layout_tiles(sys, tblk, c);
+        layout_tiles(sys, c);
         GL_CUDA(cudaMemcpyAsync(dsys, sys.data(), sizeof(BSys) * nsys, cudaMemcpyHostToDevice, st));
         return GLINALG_SUCCESS;
     };
