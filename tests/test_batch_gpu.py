@@ -82,6 +82,19 @@ def test_cg_batch_systems_that_stop_at_setup(gl, gpu, oracle, precision):
         assert rel(xs[q], x1) < 1e-7, q
 
 
+def test_cg_batch_more_systems_than_one_list_chunk(gl, gpu, oracle):
+    """1100 small systems (sides 8 and 16, both kinds): the list kernel forms its prefix sum
+    1024 systems at a time, so the tiles and vector blocks of systems 1024.. follow a carried
+    offset.  Every system reaches the FP64-true relative residual 1e-10."""
+    systems = _uneven_batch(gl, 1100, [8, 16], 4242)
+    ops = [gl.Operator(k, L, L, mass, U) for k, L, mass, U, b in systems]
+    xs = [np.zeros_like(b) for *_, b in systems]
+    infos = gl.cg_batch(ops, xs, [b for *_, b in systems], 100000, 1e-10, precision=1)
+    for q, (kind, L, mass, U, b) in enumerate(systems):
+        assert infos[q].success, (q, infos[q])
+        assert _true_relres(oracle, kind, L, mass, U, xs[q], b) < 1e-10, q
+
+
 def test_cg_batch_256_uneven_systems(gl, gpu, oracle):
     """The uneven-batch workload: 256 systems with sides from {32, 64, 128, 256}, half staggered
     normal equations and half gauge Laplacians, FP32 inner iterations with FP64 reliable
